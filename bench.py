@@ -1,0 +1,381 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 hot path: MOM5 tracer advection + split-explicit barotropic step.
+
+One "step" = one baroclinic step of the full hot path on the workload below:
+MDFL Sweby advection of every tracer with the explicit update, then
+update_ocean_barotropic (predictor-corrector subcycles + time averages).
+
+Workload (N=1): 1440x1080x50, 0.25 degree, lat -80..80, cyclic in x, 10 tracers,
+MDFL Sweby + 60 barotropic subcycles, dtts = dtuv = 600 s, dtbt = 20 s; seeded
+synthetic inputs.  Metric: cell-updates/s (cells x steps / s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp64|mixed] [--config c2|c0|c1]
+
+--impl reference times the reference's CPU algorithm (the C restatement in
+oracle/, the reference Fortran cannot be compiled on these hosts) on all host
+cores: the domain is split into one block per process, as MPI ranks would hold
+it, each block stepped independently (no halo exchange is charged).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s (1 GB300): FP64 drop-in vs batched mixed-precision; p99 latency"
+DTTS = 600.0
+DTBT = 20.0
+NTS = 60
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+HBM_FALLBACK = 6800.0  # GB/s
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+def config_spec(name: str, ntr_override=None):
+    from mom5_gb300 import grid
+    if name == "c2":
+        return grid.config_c2(ntracers=ntr_override or 10)
+    if name == "c0":
+        return grid.config_c0()
+    if name == "c1":
+        return grid.config_c1()
+    raise SystemExit(f"unknown config {name}")
+
+
+def adv_bytes(ni, nj, nk, ntr):
+    """Algorithmic bytes of one fused advection step incl. the state update:
+    read T and write T(taup1) per tracer, read u, v, w, rho_dzt, rho_dztr per cell,
+    seven 2-D metric columns."""
+    return 8 * ni * nj * nk * (2 * ntr + 5) + 8 * ni * nj * 7
+
+
+def bt_bytes(ni, nj, nts):
+    """Streaming bytes of the barotropic subcycles: 28 FP64 arrays per column per subcycle."""
+    return 224 * ni * nj * nts
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = []
+        smax = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for name, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(name)
+            except Exception:
+                pass
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- CPU side (reference algorithm)
+def _ref_worker(args):
+    """One host process: one block of the workload stepped with the C restatement."""
+    (ni, nj, nk, ntr, lat0, lat1, lon0, lon1, seed, warmup, steps, nts) = args
+    import numpy as np
+    import torch
+    torch.set_num_threads(1)
+    from mom5_gb300 import grid
+    from oracle import oracle as O
+    sp = grid.DomainSpec(ni=ni, nj=nj, nk=nk, lon0=lon0, lon1=lon1, lat0=lat0, lat1=lat1, cyclic_x=False,
+                         continent=None, hmin=2000.0, ntracers=ntr, seed=seed)
+    dom = grid.make_domain(sp)
+    g = O.domain_arrays(dom)
+    d = O.dims(sp)
+    T = [g["T"][n].copy() for n in range(ntr)]
+    st = {k: g[k].copy() for k in ("eta_t", "eta_t_bar", "udrho_u", "udrho_v")}
+
+    def step():
+        nonlocal st
+        for n in range(ntr):
+            th = O.advect_mdfl_sweby(d, g, T[n], DTTS)
+            T[n] = O.update_tracer(d, g, T[n], th, DTTS)
+        out = O.update_ocean_barotropic(d, g, st, nts, DTBT)
+        st = {"eta_t": st["eta_t"], "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"],
+              "udrho_v": out["udrho_v"]}
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    return time.perf_counter() - t0, ni * nj * nk * steps
+
+
+def cpu_reference(spec, warmup, steps, procs, block_frac=1.0):
+    """Time the reference algorithm on `procs` host processes, one block each."""
+    import multiprocessing as mp
+    px = int(round(math.sqrt(procs)))
+    while procs % px:
+        px -= 1
+    py = procs // px
+    bi = max(8, int(spec.ni / px * math.sqrt(block_frac)))
+    bj = max(8, int(spec.nj / py * math.sqrt(block_frac)))
+    dlon = (spec.lon1 - spec.lon0) / spec.ni
+    dlat = (spec.lat1 - spec.lat0) / spec.nj
+    jobs = []
+    for b in range(procs):
+        ix, iy = b % px, b // px
+        lon0 = spec.lon0 + ix * (spec.ni // px) * dlon
+        lat0 = spec.lat0 + iy * (spec.nj // py) * dlat
+        jobs.append((bi, bj, spec.nk, spec.ntracers, lat0, lat0 + bj * dlat, lon0, lon0 + bi * dlon,
+                     1000 + b, warmup, steps, NTS))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_ref_worker, jobs)
+    tmax = max(r[0] for r in res)
+    cells = sum(r[1] for r in res)
+    return cells / tmax, {"block": [bi, bj, spec.nk], "procs": procs, "seconds": tmax,
+                          "cells_per_step": bi * bj * spec.nk * procs}
+
+
+# --------------------------------------------------------------------------- GPU side
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    from mom5_gb300 import build, capi, grid, harness
+    from mom5_gb300.capi import F
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    build.build()
+    spec = config_spec(args.config)
+    prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_FP64
+    dom = grid.make_domain(spec, device="cuda")
+    opts = capi.default_options(barotropic_time_stepping_B=1, precision=prec)
+    d = harness.load(dom, options=opts)
+    nts = d.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
+    ni, nj, nk, ntr = spec.ni, spec.nj, spec.nk, spec.ntracers
+    cells = ni * nj * nk
+    del dom
+    torch.cuda.empty_cache()
+    stream = torch.cuda.current_stream()
+    d.set_stream(stream.cuda_stream)
+
+    state = {"tau": 1}
+
+    def step():
+        tau = state["tau"]
+        taup1 = 3 - tau
+        if ntr > 0:
+            d.tracer_advection_step(tau, tau, taup1, DTTS)
+        d.update_ocean_barotropic(tau, taup1)
+        state["tau"] = taup1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    d.enable_timing(True)
+    launches0 = d.launches
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    launches = d.launches - launches0
+    sec = {s: d.timing(s) for s in ("mdfl", "mdfl_mixed", "tracer_update", "barotropic")}
+    d.enable_timing(False)
+    ms_step = ms / args.steps
+    value = cells * world * args.steps / (ms / 1e3)
+
+    # dominant kernel group: the advection step (MDFL passes + explicit update)
+    adv_ms = sec["mdfl"][0] + sec["mdfl_mixed"][0] + sec["tracer_update"][0]
+    adv_calls = max(1, max(sec["mdfl"][1], sec["mdfl_mixed"][1]))
+    peak, peak_kind = hbm_peak()
+    if ntr > 0:
+        bytes_adv = adv_bytes(ni, nj, nk, ntr)
+        per = adv_ms / adv_calls
+        achieved = bytes_adv / (per / 1e3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "tracer advection step (mdfl passes + explicit update)",
+                    "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                    "algorithmic_bytes_per_launch": bytes_adv, "ms_per_launch": round(per, 3), "traffic": None}
+    else:
+        roofline = None
+    bt_ms = sec["barotropic"][0] / max(1, sec["barotropic"][1])
+    bt_achieved = bt_bytes(ni, nj, nts) / (bt_ms / 1e3) / 1e9
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e and ntr > 0:
+        pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True)
+        n3 = d.count(F.TRACER)
+        n2 = d.count(F.ETA_T_BAR)
+        nw = d.count(F.WRHO_BT)
+        hT = [pin(n3) for _ in range(ntr)]
+        hU, hV, hW = pin(n3), pin(n3), pin(nw)
+        for n in range(ntr):
+            hT[n].copy_(torch.from_numpy(d.get(F.TRACER, n=n + 1, level=state["tau"])))
+        hU.copy_(torch.from_numpy(d.get(F.UHRHO_ET)))
+        hV.copy_(torch.from_numpy(d.get(F.VHRHO_NT)))
+        hW.copy_(torch.from_numpy(d.get(F.WRHO_BT)))
+        oT = [pin(n3) for _ in range(ntr)]
+        oE, oU, oV = pin(n2), pin(n2), pin(n2)
+        ke = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            tau = state["tau"]
+            taup1 = 3 - tau
+            for n in range(ntr):
+                d.set(F.TRACER, hT[n], n=n + 1, level=tau)
+            d.set(F.UHRHO_ET, hU)
+            d.set(F.VHRHO_NT, hV)
+            d.set(F.WRHO_BT, hW)
+            step()
+            for n in range(ntr):
+                capi.lib().mom5gpu_get_field(d.h, F.TRACER, n + 1, taup1, capi.C.c_void_p(oT[n].data_ptr()), 0)
+            for fid, buf in ((F.ETA_T_BAR, oE), (F.UDRHO_U, oU), (F.UDRHO_V, oV)):
+                capi.lib().mom5gpu_get_field(d.h, fid, 0, taup1, capi.C.c_void_p(buf.data_ptr()), 0)
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / ke
+        e2e = {"value": round(cells / te, 1), "unit": "cell-updates/s",
+               "h2d_bytes_per_step": 8 * (ntr * n3 + 2 * n3 + nw), "d2h_bytes_per_step": 8 * (ntr * n3 + 3 * n2),
+               "steps": ke, "api": "mom5gpu_set_field / mom5gpu_tracer_advection_step / "
+                                   "mom5gpu_update_ocean_barotropic / mom5gpu_get_field (pinned host buffers)"}
+
+    out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-updates/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == capi.PRECISION_FP64 else "f32+f64",
+           "data": "synthetic (seeded streamfunction flow, partial-cell bathymetry)",
+           "config": {"workload": f"{args.config.upper()}: {ni}x{nj}x{nk}, {ntr} tracers, MDFL Sweby + {nts}-subcycle "
+                                  f"B-grid barotropic, dtts={DTTS:g}s dtbt={DTBT:g}s, "
+                                  f"{'FP64 drop-in' if prec == capi.PRECISION_FP64 else 'precision form'}",
+                      "cells": cells, "tracers": ntr, "subcycles": nts, "parallelism": f"replicas x{world}",
+                      "l2": "inputs larger than L2 (tracer state alone %.1f GB)" % (2 * ntr * cells * 8 / 1e9)},
+           "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+           "sections_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sec.items()},
+           "barotropic_roofline": {"achieved": round(bt_achieved, 1), "unit": "GB/s", "peak": peak,
+                                   "frac": round(bt_achieved / peak, 4), "note": "streaming model, 224 B/column/subcycle"},
+           "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline and ntr > 0:
+        # bounded sample of the same workload on one host core: one block of 1/16 of the domain
+        v, info = _cpu_sample(spec)
+        out["cpu_baseline"] = {"value": round(v, 1), "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                               "sample": info}
+    return out
+
+
+def _cpu_sample(spec):
+    """One host core, one 180x135 block of the workload's grid, two steps."""
+    res = _ref_worker((180, 135, spec.nk, spec.ntracers, -40.0, -6.25, 0.0, 45.0, 77, 0, 2, NTS))
+    return res[1] / res[0], f"C restatement, 1 core, 180x135x{spec.nk} block, {spec.ntracers} tracers, 2 steps"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--config", choices=["c2", "c0", "c1"], default="c2")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        spec = config_spec(args.config)
+        procs = os.cpu_count() or 1
+        # bound the run to a few minutes: shrink each block when many steps are asked for
+        est_step = 3.5
+        frac = min(1.0, 150.0 / max(1.0, est_step * (args.steps + args.warmup)))
+        v, info = cpu_reference(spec, args.warmup, args.steps, procs, block_frac=frac)
+        out = {"metric": METRIC, "value": round(v, 1), "unit": "cell-updates/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+               "config": {"workload": f"{args.config.upper()} ({spec.ni}x{spec.nj}x{spec.nk}, {spec.ntracers} tracers, "
+                                      f"MDFL Sweby + {NTS}-subcycle barotropic), one block per host process",
+                          "sample": info},
+               "cpu_baseline": {"value": round(v, 1), "unit": "cell-updates/s", "cores": procs, "kind": "port",
+                                "sample": f"{procs} processes x block {info['block']}, {args.steps} steps"},
+               "e2e": {"value": round(v, 1), "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

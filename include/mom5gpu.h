@@ -1,0 +1,236 @@
+/*
+ * mom5gpu.h -- C ABI of the GB300 library for MOM5's tracer-advection and
+ * split-explicit barotropic path.
+ *
+ * One mom5gpu_domain holds one ocean domain's grid, state and scratch in GPU
+ * memory.  A Fortran host binds these entry points through ISO_C_BINDING
+ * (mom5_gb300/fortran/mom5gpu_mod.F90); any C or Python host can do the same.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: MOM5GPU_OK (0) or a negative
+ *    MOM5GPU_E* code.  Nothing aborts the caller.  mom5gpu_last_error() gives
+ *    the message of the last failure on a domain.
+ *  - Arrays crossing the boundary use the reference's memory layout: Fortran
+ *    column-major over the data domain (isd:ied, jsd:jed) = (ni+2) x (nj+2)
+ *    with a one-cell halo, then k = 1..nk (or 0..nk for wrho_bt).  A C caller
+ *    sees a C array [nk][nj+2][ni+2].
+ *  - Tracer numbers n and time levels (taum1, tau, taup1) are 1-based, exactly
+ *    the values of ntracer and Time%taum1/tau/taup1 in the Fortran interfaces.
+ *  - All work is queued on the domain's CUDA stream (mom5gpu_set_stream) and
+ *    is asynchronous unless an entry point returns host data.
+ *  - Domains are not thread-safe; distinct domains may be driven from
+ *    different host threads concurrently.
+ */
+#ifndef MOM5GPU_H
+#define MOM5GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MOM5GPU_OK 0
+#define MOM5GPU_EINVAL -1      /* bad argument (the reference aborts with mpp_error(FATAL)) */
+#define MOM5GPU_ENOMEM -2      /* device allocation failed */
+#define MOM5GPU_ECUDA -3       /* a CUDA runtime call failed */
+#define MOM5GPU_ESTATE -4      /* called out of order (e.g. before the init routine) */
+#define MOM5GPU_ECFL -5        /* barotropic gravity-wave CFL check failed */
+#define MOM5GPU_ENUMERIC -6    /* non-finite value found in a checked field */
+#define MOM5GPU_ETIMEDOUT -7   /* a bounded device wait gave up */
+#define MOM5GPU_EUNSUPPORTED -8 /* option outside the implemented path */
+#define MOM5GPU_EFULL -9       /* no free slot / HBM budget (serving admission) */
+
+/* ---- enumerations shared with the reference ---------------------------- */
+/* ocean_parameters.F90:141-142 */
+#define MOM5GPU_BGRID 1
+#define MOM5GPU_CGRID 2
+/* tracer advection schemes, ocean_parameters.F90:148-162 (implemented subset) */
+#define MOM5GPU_ADVECT_UPWIND 1
+#define MOM5GPU_ADVECT_QUICKER 5
+#define MOM5GPU_ADVECT_MDFL_SWEBY 9
+#define MOM5GPU_ADVECT_DST_LINEAR 10
+
+/* arithmetic of the advection kernels */
+#define MOM5GPU_PRECISION_FP64 0  /* drop-in: IEEE FP64 in the reference's operation order */
+#define MOM5GPU_PRECISION_MIXED 1 /* FP32 fluxes and limiters, FP64 tracer state */
+
+/* ---- fields -------------------------------------------------------------- */
+/* Shape classes: 2D = (ni+2)(nj+2); 3D = 2D*nk; 3DW = 2D*(nk+1);
+ * "(n)" = per tracer, "(t)" = per time level 1..3. */
+enum mom5gpu_field {
+  /* grid metrics, 2D (ocean_types.F90:206-378) */
+  MOM5GPU_DXT = 1, MOM5GPU_DYT, MOM5GPU_DXU, MOM5GPU_DYU, MOM5GPU_DXTE, MOM5GPU_DYTE, MOM5GPU_DXTN,
+  MOM5GPU_DYTN, MOM5GPU_DAT, MOM5GPU_DATR, MOM5GPU_DXUR, MOM5GPU_DYUR, MOM5GPU_DXTER, MOM5GPU_DYTNR,
+  MOM5GPU_DTE, MOM5GPU_DTW, MOM5GPU_DUS, MOM5GPU_DUN, MOM5GPU_DAUR, MOM5GPU_CORIOLIS_F,
+  MOM5GPU_UMASK1,        /* Grd%umask(:,:,1) */
+  MOM5GPU_TMASKEN_E1,    /* Grd%tmasken(:,:,1,1) */
+  MOM5GPU_TMASKEN_N1,    /* Grd%tmasken(:,:,1,2) */
+  /* 3D grid */
+  MOM5GPU_TMASK = 40,    /* Grd%tmask, 3D */
+  /* advection velocity (ocean_adv_vel_type, ocean_types.F90:408-417) */
+  MOM5GPU_UHRHO_ET = 50, /* 3D */
+  MOM5GPU_VHRHO_NT,      /* 3D */
+  MOM5GPU_WRHO_BT,       /* 3DW, levels 0..nk */
+  /* thickness (ocean_thickness_type, ocean_types.F90:134-203) */
+  MOM5GPU_RHO_DZT = 60,  /* 3D (t) */
+  MOM5GPU_RHO_DZTR,      /* 3D */
+  MOM5GPU_THICKU,        /* 2D (t) */
+  MOM5GPU_THICKEN_E,     /* 2D, Thickness%thicken(:,:,1) */
+  MOM5GPU_THICKEN_N,     /* 2D, Thickness%thicken(:,:,2) */
+  /* prognostic tracers (ocean_prog_tracer_type, ocean_types.F90:468-541) */
+  MOM5GPU_TRACER = 70,   /* 3D (n)(t) */
+  MOM5GPU_TH_TENDENCY,   /* 3D (n) */
+  MOM5GPU_TMASK_LIMIT,   /* 3D (n) */
+  /* external mode (ocean_external_mode_type, ocean_types.F90:591-637) */
+  MOM5GPU_ETA_T = 80,    /* 2D (t) */
+  MOM5GPU_ETA_T_BAR,     /* 2D (t) */
+  MOM5GPU_ETA_U,         /* 2D (t) */
+  MOM5GPU_UDRHO_U,       /* 2D (t), Ext_mode%udrho(:,:,1,t) */
+  MOM5GPU_UDRHO_V,       /* 2D (t), Ext_mode%udrho(:,:,2,t) */
+  MOM5GPU_CONV_RHO_UD_T, /* 2D (t) */
+  MOM5GPU_DETA_DT,       /* 2D */
+  MOM5GPU_FORCING_BT_U,  /* 2D, Ext_mode%forcing_bt(:,:,1) */
+  MOM5GPU_FORCING_BT_V,  /* 2D */
+  MOM5GPU_SOURCE,        /* 2D, Ext_mode%source */
+  MOM5GPU_ETA_SMOOTH,    /* 2D */
+  MOM5GPU_PS,            /* 2D */
+  MOM5GPU_GRAD_PS_X,     /* 2D */
+  MOM5GPU_GRAD_PS_Y,     /* 2D */
+  MOM5GPU_PATM = 100,    /* 2D, patm argument */
+  MOM5GPU_PME,           /* 2D, pme argument */
+  MOM5GPU_RIVER,         /* 2D, river argument */
+  MOM5GPU_RHO_G,         /* 2D, module rho_g (grav*rho at k=1) */
+  MOM5GPU_FIELD_END
+};
+
+/* ---- configuration ------------------------------------------------------- */
+typedef struct mom5gpu_dims {
+  int ni, nj, nk;          /* compute domain isc:iec = 1:ni, jsc:jec = 1:nj, 1:nk */
+  int cyclic_x, cyclic_y;  /* periodic directions (mpp_domains cyclic flags) */
+  int num_prog_tracers;
+  int horz_grid;           /* MOM5GPU_BGRID or MOM5GPU_CGRID */
+} mom5gpu_dims;
+
+typedef struct mom5gpu_options {
+  /* ocean_tracer_advect_nml, ocean_tracer_advect.F90:483-495 */
+  int advect_sweby_all;          /* default 0 */
+  int limit_with_upwind;         /* default 0 */
+  int zero_tracer_advect_horz;   /* default 0 */
+  int zero_tracer_advect_vert;   /* default 0 */
+  /* ocean_barotropic_nml, ocean_barotropic.F90:607-614 */
+  int barotropic_time_stepping_A; /* exactly one of A and B must be 1 */
+  int barotropic_time_stepping_B;
+  int initsum_with_bar;           /* default 1 */
+  double pred_corr_gamma;         /* default 0.2 */
+  /* ocean_parameters.F90:176, :194 */
+  double rho0;                    /* 1035.0 */
+  double grav;                    /* 9.80 */
+  /* this library */
+  int precision;                  /* MOM5GPU_PRECISION_FP64 (default) or _MIXED */
+} mom5gpu_options;
+
+typedef struct mom5gpu_domain mom5gpu_domain;
+
+/* Fill *opt with the reference's namelist defaults.  Neither barotropic time
+ * stepping flag is set, as in the reference, whose init stops until one is. */
+void mom5gpu_default_options(mom5gpu_options* opt);
+
+/* Allocate one domain on the current CUDA device.  Replaces the allocations of
+ * ocean_tracer_advect_init (ocean_tracer_advect.F90:507-756) and
+ * ocean_barotropic_init (ocean_barotropic.F90:946-1780). */
+int mom5gpu_create(const mom5gpu_dims* dims, const mom5gpu_options* opt, mom5gpu_domain** out);
+void mom5gpu_destroy(mom5gpu_domain* d);
+/* Message of the last failure on d; with d == NULL, of the last failed create. */
+const char* mom5gpu_last_error(const mom5gpu_domain* d);
+const char* mom5gpu_strerror(int status);
+/* Queue subsequent work on `stream` (a cudaStream_t); NULL restores the domain's own stream. */
+int mom5gpu_set_stream(mom5gpu_domain* d, void* stream);
+int mom5gpu_synchronize(mom5gpu_domain* d);
+/* Bytes of device memory held by d. */
+size_t mom5gpu_device_bytes(const mom5gpu_domain* d);
+
+/* ---- data movement ------------------------------------------------------ */
+/* Number of doubles in field f (the size of one tracer / time level). */
+size_t mom5gpu_field_count(const mom5gpu_domain* d, int field);
+/* Copy a field in (out) from a host (on_device=0) or device (1) pointer.
+ * n: tracer 1..num_prog_tracers or 0; level: time level 1..3 or 0. */
+int mom5gpu_set_field(mom5gpu_domain* d, int field, int n, int level, const double* src, int on_device);
+int mom5gpu_get_field(mom5gpu_domain* d, int field, int n, int level, double* dst, int on_device);
+/* Device address of a field (for aliasing by a caller that owns device code). */
+int mom5gpu_field_device_ptr(mom5gpu_domain* d, int field, int n, int level, double** dptr);
+/* Vertical grid for quicker_init and the barotropic CFL check: nominal dzt(nk),
+ * zw(nk) and kmt (2D, int). */
+int mom5gpu_set_vertical_grid(mom5gpu_domain* d, const double* dzt, const double* zw, const int* kmt);
+/* Per-tracer field_table choices (ocean_tracer.F90:982-1066). */
+int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz_scheme, int vert_scheme,
+                              double min_tracer_limit, double max_tracer_limit);
+
+/* ---- initialisation (after the grid fields are set) ---------------------- */
+/* ocean_tracer_advect_init's scheme set-up: quicker_init (:1442-1586) and
+ * mdfl_init (:1644-1691). */
+int mom5gpu_tracer_advect_init(mom5gpu_domain* d);
+/* ocean_barotropic_init's time-step set-up (:1109-1115, :1195-1197,
+ * :1283-1288, :1546-1662): nts = nint(2*dtuv/dtbt), cori1/cori2 and the
+ * gravity-wave CFL check (MOM5GPU_ECFL when violated). */
+int mom5gpu_barotropic_init(mom5gpu_domain* d, double dtuv, double dtbt);
+int mom5gpu_barotropic_nts(const mom5gpu_domain* d);
+
+/* ---- the hot path -------------------------------------------------------- */
+/* horz_advect_tracer (ocean_tracer_advect.F90:1898-2083): add the horizontal
+ * (or, for MDFL/DST, 3-D) advection tendency of tracer n to its th_tendency.
+ * With advect_sweby_all and n == 1 it runs advect_tracer_sweby_all for every
+ * tracer, as the reference does. */
+int mom5gpu_horz_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
+/* vert_advect_tracer (ocean_tracer_advect.F90:2095-2226). */
+int mom5gpu_vert_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
+/* advect_tracer_sweby_all (ocean_tracer_advect.F90:4104-4511). */
+int mom5gpu_advect_tracer_sweby_all(mom5gpu_domain* d, int taum1, int tau, double dtime);
+/* compute_tmask_limit (ocean_tracer.F90:2788-2892), tmask_limit_ts_same on
+ * when index_temp/index_salt (1-based) are both > 0. */
+int mom5gpu_compute_tmask_limit(mom5gpu_domain* d, int tau, int index_temp, int index_salt);
+/* Set th_tendency of tracer n (0 = all) to zero. */
+int mom5gpu_zero_th_tendency(mom5gpu_domain* d, int n);
+/* Explicit update of tracer n (0 = all) (ocean_tracer.F90:2341-2350), then
+ * the halo update of field(taup1) (ocean_model.F90:1903-1911). */
+int mom5gpu_update_tracer(mom5gpu_domain* d, int n, int taum1, int taup1, double dtime);
+/* update_advection_only (ocean_tracer.F90:2618-2649) for every tracer in one
+ * call: zero th_tendency, horizontal + vertical advection, explicit update,
+ * halo update. */
+int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime);
+/* eta_and_pbot_tendency (ocean_barotropic.F90:2668-2734), depth-based. */
+int mom5gpu_eta_and_pbot_tendency(mom5gpu_domain* d, int tau);
+/* eta_and_pbot_update (ocean_barotropic.F90:2290-2385), depth-based, no OBC. */
+int mom5gpu_eta_and_pbot_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
+/* update_ocean_barotropic (ocean_barotropic.F90:2763-3033), splitting branch,
+ * depth-based, legacy halos, barotropic_halo = 1: pred_corr_tropic_depth_bgrid
+ * (:3225-3579) or _cgrid (:3601-3965), then the time averages, conv_rho_ud_t,
+ * eta_u, ps and grad_ps. */
+int mom5gpu_update_ocean_barotropic(mom5gpu_domain* d, int tau, int taup1);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+/* Global content of tracer n at a time level, sum of tmask*dat*rho_dzt(level)*T
+ * (total_tracer, ocean_tracer_diag.F90:2380-2415) with a compensated,
+ * fixed-order reduction (double-double), written to *out (host). */
+int mom5gpu_global_tracer_content(mom5gpu_domain* d, int n, int level, double* out);
+/* Sum of tmask1*dat*eta_t_bar(level), compensated, to *out (host). */
+int mom5gpu_global_eta_integral(mom5gpu_domain* d, int field, int level, double* out);
+/* 1 if any non-finite value is in tracer n (0 = all) at `level`, else 0, to *out. */
+int mom5gpu_check_finite(mom5gpu_domain* d, int n, int level, int* out);
+
+/* ---- profiling (the role of mpp_clock_begin/end, mpp_util.inc:797-904) ---- */
+/* Record CUDA events around each section (advection passes, tracer update,
+ * barotropic subcycle loop, ...) on the domain's stream. */
+int mom5gpu_enable_timing(mom5gpu_domain* d, int on);
+/* Total device milliseconds and number of calls of a named section since
+ * timing was enabled; synchronises the stream.  Sections: "mdfl", "mdfl_mixed",
+ * "tracer_update", "barotropic", "upwind", "quicker". */
+int mom5gpu_timing_query(mom5gpu_domain* d, const char* section, double* total_ms, long* calls);
+/* Number of kernels this domain has launched since creation. */
+long mom5gpu_launch_count(const mom5gpu_domain* d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOM5GPU_H */

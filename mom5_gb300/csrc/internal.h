@@ -1,0 +1,145 @@
+// Internal declarations shared by the C-ABI layer and the kernel files.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mom5gpu.h"
+
+namespace mom5 {
+
+// Geometry passed by value to every kernel.
+struct Geo {
+  int ni, nj, nk;   // compute domain
+  int nxd, nyd;     // data domain (halo 1)
+  int cx, cy;       // cyclic flags
+  long n2;          // nxd*nyd
+  long n3;          // n2*nk
+};
+
+// Field shape classes.
+enum Shape { S2D = 0, S3D = 1, S3DW = 2 };
+
+struct FieldInfo {
+  int id;
+  Shape shape;
+  bool per_tracer;
+  bool per_level;
+};
+
+const FieldInfo* field_info(int id);
+
+// Per-tracer scheme selection (field_table).
+struct TracerScheme {
+  int horz = MOM5GPU_ADVECT_MDFL_SWEBY;
+  int vert = MOM5GPU_ADVECT_MDFL_SWEBY;
+  double min_limit = -1.0e10;
+  double max_limit = 1.0e10;
+};
+
+// Quicker weights on the device (quicker_init, ocean_tracer_advect.F90:1442-1586).
+struct QuickerWeights {
+  double* quick_x = nullptr;  // 2 * n2
+  double* quick_y = nullptr;  // 2 * n2
+  double* curv_xp = nullptr;  // 3 * n2
+  double* curv_xn = nullptr;
+  double* curv_yp = nullptr;
+  double* curv_yn = nullptr;
+  double* quick_z = nullptr;  // 2 * nk
+  double* curv_zp = nullptr;  // 3 * nk
+  double* curv_zn = nullptr;
+};
+
+}  // namespace mom5
+
+struct mom5gpu_domain {
+  mom5gpu_dims dims;
+  mom5gpu_options opt;
+  mom5::Geo geo;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  size_t bytes = 0;
+  // one allocation per field id; nullptr until first set/used
+  std::vector<double*> field;  // indexed by field id
+  std::vector<mom5::TracerScheme> scheme;
+  // host copies needed at init time
+  std::vector<double> dzt_h, zw_h;
+  std::vector<int> kmt_h;
+  // derived device data
+  uint8_t* mask2 = nullptr;  // tmask with a 2-cell halo (tmask_mdfl / tmask_quick), (ni+4)(nj+4)nk
+  mom5::QuickerWeights qw;
+  double* cori1 = nullptr;
+  double* cori2 = nullptr;
+  bool advect_ready = false;
+  bool baro_ready = false;
+  int nts = 0;
+  double dtuv = 0.0, dtbt = 0.0;
+  // scratch
+  double* mdfl_a = nullptr;  // tracer_mdfl after the z pass, ntr * n3
+  double* mdfl_b = nullptr;  // after the x pass, ntr * n3
+  size_t mdfl_cap = 0;       // tracers that fit
+  float* mixed_scr = nullptr;  // precision-form scratch
+  size_t mixed_cap = 0;
+  double* bt = nullptr;        // barotropic scratch
+  double* red = nullptr;       // reduction scratch (device)
+  double* red_h = nullptr;     // pinned host result
+  int* flag = nullptr;         // device flag word
+  // profiling
+  bool timing = false;
+  struct Clock {
+    int section;
+    cudaEvent_t a, b;
+  };
+  std::vector<Clock> clocks;           // recorded, not yet resolved
+  std::vector<cudaEvent_t> event_pool;
+  double clock_ms[8] = {0};
+  long clock_calls[8] = {0};
+  long launches = 0;
+};
+
+namespace mom5 {
+
+// error helpers (capi.cu)
+int fail(mom5gpu_domain* d, int code, const char* fmt, ...);
+int cuda_fail(mom5gpu_domain* d, cudaError_t e, const char* where);
+double* fptr(mom5gpu_domain* d, int id, int n, int level);  // nullptr if absent
+size_t field_count(const Geo& g, Shape s);
+
+// profiling sections
+enum Section { SEC_MDFL = 0, SEC_MDFL_MIXED, SEC_UPDATE, SEC_BAROTROPIC, SEC_UPWIND, SEC_QUICKER, SEC_BATCH, SEC_N };
+// RAII: events around a section when timing is on
+struct ClockScope {
+  mom5gpu_domain* d;
+  int sec;
+  cudaEvent_t a = nullptr;
+  ClockScope(mom5gpu_domain* d_, int s);
+  ~ClockScope();
+};
+inline void count_launches(mom5gpu_domain* d, long n) { d->launches += n; }
+
+// ---- FP64 kernels (k_fp64.cu) ----
+void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t s);
+int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,
+                double sweby_limiter);
+int launch_upwind_horz(mom5gpu_domain* d, int n, int taum1);
+int launch_upwind_vert(mom5gpu_domain* d, int n, int taum1);
+int launch_quicker_horz(mom5gpu_domain* d, int n, int taum1, int tau);
+int launch_quicker_vert(mom5gpu_domain* d, int n, int taum1, int tau);
+int launch_update_tracer(mom5gpu_domain* d, int n_first, int ntr, int taum1, int taup1, double dtime);
+int launch_tmask_limit(mom5gpu_domain* d, int n, int tau);
+int launch_tmask_limit_ts_same(mom5gpu_domain* d, int nt, int ns);
+int launch_eta_tendency(mom5gpu_domain* d, int tau);
+int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
+int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);
+int launch_content(mom5gpu_domain* d, int n, int level, double* out_host);
+int launch_eta_integral(mom5gpu_domain* d, const double* eta, double* out_host);
+int launch_check_finite(mom5gpu_domain* d, const double* a, size_t count, int* out_host);
+
+// ---- precision form (k_mixed.cu) ----
+int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, int taup1, double dtime,
+                      bool fused_update);
+
+}  // namespace mom5

@@ -1,0 +1,1197 @@
+/*
+ * mom5_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, FP64, line-by-line restatement of the MOM5 routines on the
+ * tracer-advection and split-explicit barotropic path.  It exists to check the
+ * CUDA implementation; nothing in the shipped library links, loads or calls
+ * it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * use it.
+ *
+ * Parity status: the reference is Fortran and no Fortran compiler exists in
+ * the build container, so this restatement cannot be diffed against a compiled
+ * reference there; the reference tree holds no golden vectors for these
+ * routines (its only regression data are whole-model checksums that need
+ * missing experiment inputs).  Parity of this file is therefore pinned by the
+ * analytic and property tests in tests/test_oracle_*.py and, where a Fortran
+ * compiler exists on the GPU host, by the stubbed-reference comparison recipe
+ * in oracle/ref_fortran/.
+ *
+ * Conventions (mirroring the Fortran arrays of the reference):
+ *   - compute domain i = 1..ni, j = 1..nj (isc=1, iec=ni); the data domain has
+ *     a halo of one cell, so C indices run 0..ni+1 and 0..nj+1 (isd=0).
+ *   - arrays are column-major: i fastest, then j, then k (k = 0..nk-1 for
+ *     Fortran k = 1..nk), then any further index (component, tracer).
+ *   - wrho_bt has levels 0..nk (Fortran dimension 0:nk).
+ *   - one processor element owns the whole domain, so mpp_update_domains
+ *     reduces to a periodic copy in cyclic directions and to "leave the halo
+ *     alone" at non-cyclic walls (halo_update_* below).
+ * Build with -O2 -ffp-contract=off so that no multiply-add is fused: the
+ * reference's gfortran build evaluates every product and sum separately.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct {
+  int ni, nj, nk;
+  int cyclic_x, cyclic_y;
+} orc_dims;
+
+#define NXD(d) ((d)->ni + 2)
+#define NYD(d) ((d)->nj + 2)
+#define I2(d, i, j) ((size_t)(j) * NXD(d) + (size_t)(i))
+#define I3(d, i, j, k) (((size_t)(k) * NYD(d) + (size_t)(j)) * NXD(d) + (size_t)(i))
+
+static inline double fmaxd(double a, double b) { return a > b ? a : b; }
+static inline double fmind(double a, double b) { return a < b ? a : b; }
+
+/* ocean_parameters.F90:92 onesixth = 1.0/6.0; :194-195 rho0, rho0r */
+static const double onesixth = 1.0 / 6.0;
+
+/* ------------------------------------------------------------------------- */
+/* Halo update of a data-domain (halo 1) field on a single-PE domain.        */
+/* flags: 1 = east/west halo (XUPDATE), 2 = north/south (YUPDATE), 3 = both. */
+/* mpp_update_domains semantics: src/shared/mpp/include/mpp_do_update.h;     */
+/* corners are filled only when both directions are cyclic.                  */
+/* ------------------------------------------------------------------------- */
+void orc_halo_update_3d(const orc_dims* d, double* a, int nlev, int flags) {
+  int ni = d->ni, nj = d->nj;
+  for (int k = 0; k < nlev; ++k) {
+    if ((flags & 1) && d->cyclic_x) {
+      for (int j = 1; j <= nj; ++j) {
+        a[I3(d, 0, j, k)] = a[I3(d, ni, j, k)];
+        a[I3(d, ni + 1, j, k)] = a[I3(d, 1, j, k)];
+      }
+    }
+    if ((flags & 2) && d->cyclic_y) {
+      for (int i = 1; i <= ni; ++i) {
+        a[I3(d, i, 0, k)] = a[I3(d, i, nj, k)];
+        a[I3(d, i, nj + 1, k)] = a[I3(d, i, 1, k)];
+      }
+    }
+    if (flags == 3 && d->cyclic_x && d->cyclic_y) {
+      a[I3(d, 0, 0, k)] = a[I3(d, ni, nj, k)];
+      a[I3(d, ni + 1, 0, k)] = a[I3(d, 1, nj, k)];
+      a[I3(d, 0, nj + 1, k)] = a[I3(d, ni, 1, k)];
+      a[I3(d, ni + 1, nj + 1, k)] = a[I3(d, 1, 1, k)];
+    }
+  }
+}
+
+void orc_halo_update_2d(const orc_dims* d, double* a, int flags) { orc_halo_update_3d(d, a, 1, flags); }
+
+/* Halo-2 arrays (isc-2:iec+2, jsc-2:jec+2, nk) used by mdfl and quicker.    */
+#define NX2(d) ((d)->ni + 4)
+#define NY2(d) ((d)->nj + 4)
+/* i, j in data-domain coordinates (isc = 1), so i = -1 is isc-2. */
+#define H3(d, i, j, k) (((size_t)(k) * NY2(d) + (size_t)((j) + 1)) * NX2(d) + (size_t)((i) + 1))
+
+static void halo2_update(const orc_dims* d, double* a, int flags) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  for (int k = 0; k < nk; ++k) {
+    if ((flags & 1) && d->cyclic_x) {
+      for (int j = 1; j <= nj; ++j)
+        for (int h = 1; h <= 2; ++h) {
+          a[H3(d, 1 - h, j, k)] = a[H3(d, ni + 1 - h, j, k)];
+          a[H3(d, ni + h, j, k)] = a[H3(d, h, j, k)];
+        }
+    }
+    if ((flags & 2) && d->cyclic_y) {
+      for (int i = 1; i <= ni; ++i)
+        for (int h = 1; h <= 2; ++h) {
+          a[H3(d, i, 1 - h, k)] = a[H3(d, i, nj + 1 - h, k)];
+          a[H3(d, i, nj + h, k)] = a[H3(d, i, h, k)];
+        }
+    }
+    if (flags == 3 && d->cyclic_x && d->cyclic_y) {
+      for (int hj = 1; hj <= 2; ++hj)
+        for (int hi = 1; hi <= 2; ++hi) {
+          a[H3(d, 1 - hi, 1 - hj, k)] = a[H3(d, ni + 1 - hi, nj + 1 - hj, k)];
+          a[H3(d, ni + hi, 1 - hj, k)] = a[H3(d, hi, nj + 1 - hj, k)];
+          a[H3(d, 1 - hi, nj + hj, k)] = a[H3(d, ni + 1 - hi, hj, k)];
+          a[H3(d, ni + hi, nj + hj, k)] = a[H3(d, hi, hj, k)];
+        }
+    }
+  }
+}
+
+/* tmask copied into a halo-2 array and halo-updated: mdfl_init
+ * (ocean_tracer_advect.F90:1644-1691) and quicker_init (:1478-1487). */
+void orc_mask_halo2(const orc_dims* d, const double* tmask, double* mask2) {
+  memset(mask2, 0, sizeof(double) * NX2(d) * NY2(d) * d->nk);
+  for (int k = 0; k < d->nk; ++k)
+    for (int j = 1; j <= d->nj; ++j)
+      for (int i = 1; i <= d->ni; ++i) mask2[H3(d, i, j, k)] = tmask[I3(d, i, j, k)];
+  halo2_update(d, mask2, 3);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Upwind: ocean_tracer_advect.F90:2238-2294 (horizontal), :2792-2824 (vert). */
+/* Outputs wrk1 = -scheme(...) on the compute domain (horz_advect_tracer     */
+/* :1935-1936 negates the function result), zero elsewhere.                  */
+/* ------------------------------------------------------------------------- */
+void orc_horz_advect_upwind(const orc_dims* d, const double* tmask, const double* dyte, const double* dxtn,
+                            const double* datr, const double* uhrho_et, const double* vhrho_nt, const double* T,
+                            double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* fe = (double*)calloc(n2, sizeof(double));
+  double* fn = (double*)calloc(n2, sizeof(double));
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  for (int k = 0; k < nk; ++k) {
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        double velocity = 0.5 * uhrho_et[I3(d, i, j, k)];
+        double upos = velocity + fabs(velocity);
+        double uneg = velocity - fabs(velocity);
+        fe[I2(d, i, j)] = dyte[I2(d, i, j)] * (upos * T[I3(d, i, j, k)] + uneg * T[I3(d, i + 1, j, k)]) *
+                          tmask[I3(d, i, j, k)] * tmask[I3(d, i + 1, j, k)];
+      }
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double velocity = 0.5 * vhrho_nt[I3(d, i, j, k)];
+        double upos = velocity + fabs(velocity);
+        double uneg = velocity - fabs(velocity);
+        fn[I2(d, i, j)] = dxtn[I2(d, i, j)] * (upos * T[I3(d, i, j, k)] + uneg * T[I3(d, i, j + 1, k)]) *
+                          tmask[I3(d, i, j, k)] * tmask[I3(d, i, j + 1, k)];
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double r = tmask[I3(d, i, j, k)] *
+                   (fe[I2(d, i, j)] - fe[I2(d, i - 1, j)] + fn[I2(d, i, j)] - fn[I2(d, i, j - 1)]) *
+                   datr[I2(d, i, j)];
+        wrk1[I3(d, i, j, k)] = -r;
+      }
+  }
+  free(fe);
+  free(fn);
+}
+
+void orc_vert_advect_upwind(const orc_dims* d, const double* tmask, const double* wrho_bt, const double* T,
+                            double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* ft1 = (double*)calloc(n2, sizeof(double));
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  for (int k = 0; k < nk; ++k) {
+    int kp1 = k + 1 < nk ? k + 1 : nk - 1;
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        /* wrho_bt(i,j,k) for Fortran level k = C level k+1 of the 0:nk array */
+        double velocity = 0.5 * wrho_bt[I3(d, i, j, k + 1)];
+        double wpos = velocity + fabs(velocity);
+        double wneg = velocity - fabs(velocity);
+        double ft2 = (wneg * T[I3(d, i, j, k)] + wpos * T[I3(d, i, j, kp1)]) * tmask[I3(d, i, j, k)] *
+                     tmask[I3(d, i, j, kp1)];
+        double r = tmask[I3(d, i, j, k)] * (ft1[I2(d, i, j)] - ft2);
+        wrk1[I3(d, i, j, k)] = -r;
+        ft1[I2(d, i, j)] = ft2;
+      }
+  }
+  free(ft1);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Quicker: quicker_init :1442-1586, horz :2538-2653, vert :2981-3031.       */
+/* Weight arrays are data-domain 2-D arrays with a trailing component index: */
+/* quick_x(·,·,2), curv_xp(·,·,3) ...; quick_z(nk,2), curv_zp(nk,3).         */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  double *quick_x, *quick_y, *curv_xp, *curv_xn, *curv_yp, *curv_yn; /* data domain × 2 or × 3 */
+  double *quick_z, *curv_zp, *curv_zn;                                /* nk × 2 or nk × 3 (k fastest) */
+  double *tmask_quick;                                                /* halo-2 array */
+} orc_quicker;
+
+/* 2-D halo-2 index */
+#define H2(d, i, j) ((size_t)((j) + 1) * NX2(d) + (size_t)((i) + 1))
+
+void orc_quicker_init(const orc_dims* d, const double* dxt, const double* dyt, const double* dzt,
+                      const double* tmask, orc_quicker* q) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  memset(q->quick_x, 0, sizeof(double) * n2 * 2);
+  memset(q->quick_y, 0, sizeof(double) * n2 * 2);
+  memset(q->curv_xp, 0, sizeof(double) * n2 * 3);
+  memset(q->curv_xn, 0, sizeof(double) * n2 * 3);
+  memset(q->curv_yp, 0, sizeof(double) * n2 * 3);
+  memset(q->curv_yn, 0, sizeof(double) * n2 * 3);
+  orc_mask_halo2(d, tmask, q->tmask_quick);
+
+  size_t nh = (size_t)NX2(d) * NY2(d);
+  double* dxq = (double*)calloc(nh, sizeof(double));
+  double* dyq = (double*)calloc(nh, sizeof(double));
+  for (int i = 1; i <= ni; ++i)
+    for (int j = 1; j <= nj; ++j) {
+      dxq[H2(d, i, j)] = dxt[I2(d, i, j)];
+      dyq[H2(d, i, j)] = dyt[I2(d, i, j)];
+    }
+  /* boundary fill (:1489-1507): x-halo columns replicate isc / iec; dxt only
+   * for the compute rows, dyt for all rows; then the y-halo rows replicate
+   * jsc / jec over the whole (halo-2) row. */
+  for (int i = -1; i <= 0; ++i) {
+    for (int j = 1; j <= nj; ++j) dxq[H2(d, i, j)] = dxq[H2(d, 1, j)];
+    for (int j = -1; j <= nj + 2; ++j) dyq[H2(d, i, j)] = dyq[H2(d, 1, j)];
+  }
+  for (int i = ni + 1; i <= ni + 2; ++i) {
+    for (int j = 1; j <= nj; ++j) dxq[H2(d, i, j)] = dxq[H2(d, ni, j)];
+    for (int j = -1; j <= nj + 2; ++j) dyq[H2(d, i, j)] = dyq[H2(d, ni, j)];
+  }
+  for (int j = -1; j <= 0; ++j)
+    for (int i = -1; i <= ni + 2; ++i) {
+      dxq[H2(d, i, j)] = dxq[H2(d, i, 1)];
+      dyq[H2(d, i, j)] = dyq[H2(d, i, 1)];
+    }
+  for (int j = nj + 1; j <= nj + 2; ++j)
+    for (int i = -1; i <= ni + 2; ++i) {
+      dxq[H2(d, i, j)] = dxq[H2(d, i, nj)];
+      dyq[H2(d, i, j)] = dyq[H2(d, i, nj)];
+    }
+  /* mpp_update_domains(dxt_quick / dyt_quick) with halo 2 (:1508-1509) */
+  {
+    orc_dims d1 = *d;
+    d1.nk = 1;
+    halo2_update(&d1, dxq, 3);
+    halo2_update(&d1, dyq, 3);
+  }
+#define DX(i, j) dxq[H2(d, (i), (j))]
+#define DY(i, j) dyq[H2(d, (i), (j))]
+#define W2(a, i, j, m) (a)[(size_t)(m) * n2 + I2(d, (i), (j))]
+  for (int i = 0; i <= ni; ++i)
+    for (int j = 0; j <= nj; ++j) {
+      W2(q->quick_x, i, j, 0) = DX(i + 1, j) / (DX(i + 1, j) + DX(i, j));
+      W2(q->quick_x, i, j, 1) = DX(i, j) / (DX(i + 1, j) + DX(i, j));
+      W2(q->quick_y, i, j, 0) = DY(i, j + 1) / (DY(i, j + 1) + DY(i, j));
+      W2(q->quick_y, i, j, 1) = DY(i, j) / (DY(i, j + 1) + DY(i, j));
+
+      W2(q->curv_xp, i, j, 0) =
+          DX(i, j) * DX(i + 1, j) / ((DX(i - 1, j) + 2.0 * DX(i, j) + DX(i + 1, j)) * (DX(i, j) + DX(i + 1, j)));
+      W2(q->curv_xp, i, j, 1) =
+          -DX(i, j) * DX(i + 1, j) / ((DX(i, j) + DX(i + 1, j)) * (DX(i - 1, j) + DX(i, j)));
+      W2(q->curv_xp, i, j, 2) =
+          DX(i, j) * DX(i + 1, j) / ((DX(i - 1, j) + 2.0 * DX(i, j) + DX(i + 1, j)) * (DX(i - 1, j) + DX(i, j)));
+
+      W2(q->curv_xn, i, j, 0) = DX(i, j) * DX(i + 1, j) /
+                                ((DX(i, j) + 2.0 * DX(i + 1, j) + DX(i + 2, j)) * (DX(i + 1, j) + DX(i + 2, j)));
+      W2(q->curv_xn, i, j, 1) =
+          -DX(i, j) * DX(i + 1, j) / ((DX(i + 1, j) + DX(i + 2, j)) * (DX(i, j) + DX(i + 1, j)));
+      W2(q->curv_xn, i, j, 2) =
+          DX(i, j) * DX(i + 1, j) / ((DX(i, j) + 2.0 * DX(i + 1, j) + DX(i + 2, j)) * (DX(i, j) + DX(i + 1, j)));
+
+      W2(q->curv_yp, i, j, 0) =
+          DY(i, j) * DY(i, j + 1) / ((DY(i, j - 1) + 2.0 * DY(i, j) + DY(i, j + 1)) * (DY(i, j) + DY(i, j + 1)));
+      W2(q->curv_yp, i, j, 1) =
+          -DY(i, j) * DY(i, j + 1) / ((DY(i, j) + DY(i, j + 1)) * (DY(i, j - 1) + DY(i, j)));
+      W2(q->curv_yp, i, j, 2) =
+          DY(i, j) * DY(i, j + 1) / ((DY(i, j - 1) + 2.0 * DY(i, j) + DY(i, j + 1)) * (DY(i, j - 1) + DY(i, j)));
+
+      W2(q->curv_yn, i, j, 0) = DY(i, j) * DY(i, j + 1) /
+                                ((DY(i, j) + 2.0 * DY(i, j + 1) + DY(i, j + 2)) * (DY(i, j + 1) + DY(i, j + 2)));
+      W2(q->curv_yn, i, j, 1) =
+          -DY(i, j) * DY(i, j + 1) / ((DY(i, j + 1) + DY(i, j + 2)) * (DY(i, j) + DY(i, j + 1)));
+      W2(q->curv_yn, i, j, 2) =
+          DY(i, j) * DY(i, j + 1) / ((DY(i, j) + 2.0 * DY(i, j + 1) + DY(i, j + 2)) * (DY(i, j) + DY(i, j + 1)));
+    }
+#undef DX
+#undef DY
+  for (int k = 0; k < nk; ++k) {
+    int kp2 = k + 2 < nk ? k + 2 : nk - 1;
+    int kp1 = k + 1 < nk ? k + 1 : nk - 1;
+    int km1 = k - 1 > 0 ? k - 1 : 0;
+    q->quick_z[k] = dzt[kp1] / (dzt[kp1] + dzt[k]);
+    q->quick_z[nk + k] = dzt[k] / (dzt[kp1] + dzt[k]);
+    q->curv_zp[k] = dzt[k] * dzt[kp1] / ((dzt[km1] + 2.0 * dzt[k] + dzt[kp1]) * (dzt[k] + dzt[kp1]));
+    q->curv_zp[nk + k] = -dzt[k] * dzt[kp1] / ((dzt[k] + dzt[kp1]) * (dzt[km1] + dzt[k]));
+    q->curv_zp[2 * nk + k] = dzt[k] * dzt[kp1] / ((dzt[km1] + 2.0 * dzt[k] + dzt[kp1]) * (dzt[km1] + dzt[k]));
+    q->curv_zn[k] = dzt[k] * dzt[kp1] / ((dzt[k] + 2.0 * dzt[kp1] + dzt[kp2]) * (dzt[kp1] + dzt[kp2]));
+    q->curv_zn[nk + k] = -dzt[k] * dzt[kp1] / ((dzt[kp1] + dzt[kp2]) * (dzt[k] + dzt[kp1]));
+    q->curv_zn[2 * nk + k] = dzt[k] * dzt[kp1] / ((dzt[k] + 2.0 * dzt[kp1] + dzt[kp2]) * (dzt[k] + dzt[kp1]));
+  }
+  free(dxq);
+  free(dyq);
+}
+
+void orc_horz_advect_quicker(const orc_dims* d, int limit_with_upwind, const orc_quicker* q, const double* tmask,
+                             const double* tmask_limit, const double* dyte, const double* dxtn, const double* datr,
+                             const double* uhrho_et, const double* vhrho_nt, const double* T_taum1,
+                             const double* T_tau, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  size_t nh = (size_t)NX2(d) * NY2(d) * nk;
+  double* tq = (double*)calloc(nh, sizeof(double));
+  double* fx = (double*)calloc(n2 * nk, sizeof(double));
+  double* fy = (double*)calloc(n2 * nk, sizeof(double));
+  const double* tmq = q->tmask_quick;
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  for (int k = 0; k < nk; ++k)
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) tq[H3(d, i, j, k)] = T_taum1[I3(d, i, j, k)];
+  halo2_update(d, tq, 3);
+#define TQ(i, j, k) tq[H3(d, (i), (j), (k))]
+#define MQ(i, j, k) tmq[H3(d, (i), (j), (k))]
+  for (int k = 0; k < nk; ++k) {
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double vel = dxtn[I2(d, i, j)] * vhrho_nt[I3(d, i, j, k)];
+        double upos = 0.5 * (vel + fabs(vel));
+        double uneg = 0.5 * (vel - fabs(vel));
+        double rnormsk = MQ(i, j, k) * (1 - MQ(i, j - 1, k));
+        double soutmsk = MQ(i, j + 1, k) * (1 - MQ(i, j + 2, k));
+        fy[I3(d, i, j, k)] =
+            vel * (W2(q->quick_y, i, j, 0) * T_tau[I3(d, i, j, k)] + W2(q->quick_y, i, j, 1) * T_tau[I3(d, i, j + 1, k)]) -
+            upos * (W2(q->curv_yp, i, j, 0) * TQ(i, j + 1, k) + W2(q->curv_yp, i, j, 1) * TQ(i, j, k) +
+                    W2(q->curv_yp, i, j, 2) * (TQ(i, j - 1, k) * (1 - rnormsk) + TQ(i, j, k) * rnormsk)) -
+            uneg * (W2(q->curv_yn, i, j, 0) * (TQ(i, j + 2, k) * (1 - soutmsk) + TQ(i, j + 1, k) * soutmsk) +
+                    W2(q->curv_yn, i, j, 1) * TQ(i, j + 1, k) + W2(q->curv_yn, i, j, 2) * TQ(i, j, k));
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        double vel = dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)];
+        double upos = 0.5 * (vel + fabs(vel));
+        double uneg = 0.5 * (vel - fabs(vel));
+        double eastmsk = MQ(i, j, k) * (1 - MQ(i - 1, j, k));
+        double westmsk = MQ(i + 1, j, k) * (1 - MQ(i + 2, j, k));
+        fx[I3(d, i, j, k)] =
+            vel * (W2(q->quick_x, i, j, 0) * T_tau[I3(d, i, j, k)] + W2(q->quick_x, i, j, 1) * T_tau[I3(d, i + 1, j, k)]) -
+            upos * (W2(q->curv_xp, i, j, 0) * TQ(i + 1, j, k) + W2(q->curv_xp, i, j, 1) * TQ(i, j, k) +
+                    W2(q->curv_xp, i, j, 2) * (TQ(i - 1, j, k) * (1 - eastmsk) + TQ(i, j, k) * eastmsk)) -
+            uneg * (W2(q->curv_xn, i, j, 0) * (TQ(i + 2, j, k) * (1 - westmsk) + TQ(i + 1, j, k) * westmsk) +
+                    W2(q->curv_xn, i, j, 1) * TQ(i + 1, j, k) + W2(q->curv_xn, i, j, 2) * TQ(i, j, k));
+      }
+    if (limit_with_upwind) {
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 0; i <= ni; ++i)
+          if (tmask_limit[I3(d, i, j, k)] == 1.0) {
+            double vel = uhrho_et[I3(d, i, j, k)];
+            double upos = 0.5 * (vel + fabs(vel));
+            double uneg = 0.5 * (vel - fabs(vel));
+            fx[I3(d, i, j, k)] = dyte[I2(d, i, j)] *
+                                 (upos * T_taum1[I3(d, i, j, k)] + uneg * T_taum1[I3(d, i + 1, j, k)]) *
+                                 tmask[I3(d, i, j, k)] * tmask[I3(d, i + 1, j, k)];
+          }
+      for (int j = 0; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i)
+          if (tmask_limit[I3(d, i, j, k)] == 1.0) {
+            double vel = vhrho_nt[I3(d, i, j, k)];
+            double upos = 0.5 * (vel + fabs(vel));
+            double uneg = 0.5 * (vel - fabs(vel));
+            fy[I3(d, i, j, k)] = dxtn[I2(d, i, j)] *
+                                 (upos * T_taum1[I3(d, i, j, k)] + uneg * T_taum1[I3(d, i, j + 1, k)]) *
+                                 tmask[I3(d, i, j, k)] * tmask[I3(d, i, j + 1, k)];
+          }
+    }
+  }
+  for (int k = 0; k < nk; ++k)
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double r = tmask[I3(d, i, j, k)] *
+                   (fx[I3(d, i, j, k)] - fx[I3(d, i - 1, j, k)] + fy[I3(d, i, j, k)] - fy[I3(d, i, j - 1, k)]) *
+                   datr[I2(d, i, j)];
+        wrk1[I3(d, i, j, k)] = -r;
+      }
+#undef TQ
+#undef MQ
+  free(tq);
+  free(fx);
+  free(fy);
+}
+
+void orc_vert_advect_quicker(const orc_dims* d, const orc_quicker* q, const double* tmask,
+                             const double* tmask_limit, const double* wrho_bt, const double* T_taum1,
+                             const double* T_tau, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* ft1 = (double*)calloc(n2, sizeof(double));
+  double* ft2 = (double*)calloc(n2, sizeof(double));
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  for (int k = 0; k < nk; ++k) {
+    int km1 = k - 1 > 0 ? k - 1 : 0;
+    int kp1 = k + 1 < nk ? k + 1 : nk - 1;
+    int p2 = k + 2 < nk ? k + 2 : nk - 1;
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double vel = wrho_bt[I3(d, i, j, k + 1)];
+        double upos = 0.5 * (vel + fabs(vel));
+        double uneg = 0.5 * (vel - fabs(vel));
+        double f;
+        if (tmask_limit[I3(d, i, j, k)] == 1.0) {
+          f = (uneg * T_taum1[I3(d, i, j, k)] + upos * T_taum1[I3(d, i, j, kp1)]) * tmask[I3(d, i, j, k)] *
+              tmask[I3(d, i, j, kp1)];
+        } else {
+          /* kp2 = nint(tmask(p2)*p2 + (1-tmask(p2))*kp1), Fortran 1-based levels */
+          double mp2 = tmask[I3(d, i, j, p2)];
+          int kp2 = (int)lround(mp2 * (double)(p2 + 1) + (1.0 - mp2) * (double)(kp1 + 1)) - 1;
+          double upmsk = tmask[I3(d, i, j, k)] * (1 - tmask[I3(d, i, j, km1)]);
+          f = vel * (q->quick_z[k] * T_tau[I3(d, i, j, k)] + q->quick_z[nk + k] * T_tau[I3(d, i, j, kp1)]) -
+              uneg * (q->curv_zp[k] * T_taum1[I3(d, i, j, kp1)] + q->curv_zp[nk + k] * T_taum1[I3(d, i, j, k)] +
+                      q->curv_zp[2 * nk + k] * T_taum1[I3(d, i, j, km1)]) -
+              upos * (q->curv_zn[k] * T_taum1[I3(d, i, j, kp2)] + q->curv_zn[nk + k] * T_taum1[I3(d, i, j, kp1)] +
+                      q->curv_zn[2 * nk + k] *
+                          (T_taum1[I3(d, i, j, k)] * (1 - upmsk) + T_taum1[I3(d, i, j, kp1)] * upmsk));
+        }
+        ft2[I2(d, i, j)] = f;
+        double r = tmask[I3(d, i, j, k)] * (ft1[I2(d, i, j)] - f);
+        wrk1[I3(d, i, j, k)] = -r;
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) ft1[I2(d, i, j)] = ft2[I2(d, i, j)];
+  }
+  free(ft1);
+  free(ft2);
+}
+#undef W2
+
+/* ------------------------------------------------------------------------- */
+/* MDFL Sweby, one tracer: advect_tracer_mdfl_sweby :3806-4066.              */
+/* wrk1 receives -advect_tracer_mdfl_sweby (horz_advect_tracer :1953-1959).  */
+/* sweby_limiter = 1 for ADVECT_MDFL_SWEBY, 0 for ADVECT_DST_LINEAR.         */
+/* ------------------------------------------------------------------------- */
+void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime, const double* tmask,
+                           const double* dat, const double* datr, const double* dxte, const double* dyte,
+                           const double* dxtn, const double* dytn, const double* uhrho_et,
+                           const double* vhrho_nt, const double* wrho_bt, const double* rho_dzt,
+                           const double* T, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  size_t nh = (size_t)NX2(d) * NY2(d) * nk;
+  double* tm = (double*)calloc(nh, sizeof(double)); /* tracer_mdfl */
+  double* mk = (double*)calloc(nh, sizeof(double)); /* tmask_mdfl  */
+  double* ftp = (double*)calloc(n2, sizeof(double));
+  double* fbt = (double*)calloc(n2, sizeof(double));
+  double* wkm1 = (double*)calloc(n2, sizeof(double));
+  double* fx = (double*)calloc(n2 * nk, sizeof(double));
+  double* fy = (double*)calloc(n2 * nk, sizeof(double));
+  orc_mask_halo2(d, tmask, mk);
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+#define TM(i, j, k) tm[H3(d, (i), (j), (k))]
+#define MK(i, j, k) mk[H3(d, (i), (j), (k))]
+#define TF(i, j, k) T[I3(d, (i), (j), (k))]
+#define RDZ(i, j, k) rho_dzt[I3(d, (i), (j), (k))]
+#define WB(i, j, k) wrho_bt[I3(d, (i), (j), (k) + 1)]
+  for (int k = 0; k < nk; ++k) {
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) TM(i, j, k) = TF(i, j, k);
+    int kp1 = k + 1 < nk ? k + 1 : nk - 1;
+    int kp2 = k + 2 < nk ? k + 2 : nk - 1;
+    int km1 = k - 1 > 0 ? k - 1 : 0;
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double Rjp = (TF(i, j, km1) - TF(i, j, k)) * MK(i, j, km1) * MK(i, j, k);
+        double Rj = (TF(i, j, k) - TF(i, j, kp1)) * MK(i, j, k) * MK(i, j, kp1);
+        double Rjm = (TF(i, j, kp1) - TF(i, j, kp2)) * MK(i, j, kp1) * MK(i, j, kp2);
+        double massflux = dat[I2(d, i, j)] * WB(i, j, k);
+        double cfl = fabs(WB(i, j, k) * dtime / RDZ(i, j, k));
+        double d0 = (2.0 - cfl) * (1.0 - cfl) * onesixth;
+        double d1 = (1.0 - cfl * cfl) * onesixth;
+        double thetaP = Rjm / (1.0e-30 + Rj);
+        double thetaM = Rjp / (1.0e-30 + Rj);
+        double psiP = d0 + d1 * thetaP;
+        psiP = psiP * (1.0 - sweby_limiter) +
+               fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaP), (1.0 - cfl) / (1.0e-30 + cfl) * thetaP)) * sweby_limiter;
+        double psiM = d0 + d1 * thetaM;
+        psiM = psiM * (1.0 - sweby_limiter) +
+               fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaM), (1.0 - cfl) / (1.0e-30 + cfl) * thetaM)) * sweby_limiter;
+        fbt[I2(d, i, j)] = 0.5 * ((massflux + fabs(massflux)) * (TF(i, j, kp1) + psiP * Rj) +
+                                  (massflux - fabs(massflux)) * (TF(i, j, k) - psiM * Rj)) *
+                           MK(i, j, kp1) * MK(i, j, k);
+        TM(i, j, k) = TM(i, j, k) + dtime / RDZ(i, j, k) *
+                                        (datr[I2(d, i, j)] * (fbt[I2(d, i, j)] - ftp[I2(d, i, j)]) +
+                                         TF(i, j, k) * (wkm1[I2(d, i, j)] - WB(i, j, k)));
+        ftp[I2(d, i, j)] = fbt[I2(d, i, j)];
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) wkm1[I2(d, i, j)] = WB(i, j, k);
+  }
+  halo2_update(d, tm, 1); /* XUPDATE :3912 */
+
+  for (int k = 0; k < nk; ++k) {
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        double Rjp = (TM(i + 2, j, k) - TM(i + 1, j, k)) * MK(i + 2, j, k) * MK(i + 1, j, k);
+        double Rj = (TM(i + 1, j, k) - TM(i, j, k)) * MK(i + 1, j, k) * MK(i, j, k);
+        double Rjm = (TM(i, j, k) - TM(i - 1, j, k)) * MK(i, j, k) * MK(i - 1, j, k);
+        double massflux = dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)];
+        double cfl = fabs(uhrho_et[I3(d, i, j, k)] * dtime * 2.0 /
+                          ((RDZ(i, j, k) + RDZ(i + 1, j, k)) * dxte[I2(d, i, j)]));
+        double d0 = (2.0 - cfl) * (1.0 - cfl) * onesixth;
+        double d1 = (1.0 - cfl * cfl) * onesixth;
+        double thetaP = Rjm / (1.0e-30 + Rj);
+        double thetaM = Rjp / (1.0e-30 + Rj);
+        double psiP = d0 + d1 * thetaP;
+        psiP = psiP * (1.0 - sweby_limiter) +
+               fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaP), (1.0 - cfl) / (1.0e-30 + cfl) * thetaP)) * sweby_limiter;
+        double psiM = d0 + d1 * thetaM;
+        psiM = psiM * (1.0 - sweby_limiter) +
+               fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaM), (1.0 - cfl) / (1.0e-30 + cfl) * thetaM)) * sweby_limiter;
+        fx[I3(d, i, j, k)] = 0.5 * ((massflux + fabs(massflux)) * (TM(i, j, k) + psiP * Rj) +
+                                    (massflux - fabs(massflux)) * (TM(i + 1, j, k) - psiM * Rj)) *
+                             MK(i, j, k) * MK(i + 1, j, k);
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        TM(i, j, k) = TM(i, j, k) + dtime * MK(i, j, k) * datr[I2(d, i, j)] / RDZ(i, j, k) *
+                                        (fx[I3(d, i - 1, j, k)] - fx[I3(d, i, j, k)] +
+                                         TF(i, j, k) * (dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)] -
+                                                        dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)]));
+      }
+  }
+  halo2_update(d, tm, 2); /* YUPDATE :3970 */
+
+  memset(wkm1, 0, sizeof(double) * n2);
+  for (int k = 0; k < nk; ++k) {
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double Rjp = (TM(i, j + 2, k) - TM(i, j + 1, k)) * MK(i, j + 2, k) * MK(i, j + 1, k);
+        double Rj = (TM(i, j + 1, k) - TM(i, j, k)) * MK(i, j + 1, k) * MK(i, j, k);
+        double Rjm = (TM(i, j, k) - TM(i, j - 1, k)) * MK(i, j, k) * MK(i, j - 1, k);
+        double massflux = dxtn[I2(d, i, j)] * vhrho_nt[I3(d, i, j, k)];
+        double cfl = fabs(vhrho_nt[I3(d, i, j, k)] * dtime * 2.0 /
+                          ((RDZ(i, j, k) + RDZ(i, j + 1, k)) * dytn[I2(d, i, j)]));
+        double d0 = (2.0 - cfl) * (1.0 - cfl) * onesixth;
+        double d1 = (1.0 - cfl * cfl) * onesixth;
+        double thetaP = Rjm / (1.0e-30 + Rj);
+        double thetaM = Rjp / (1.0e-30 + Rj);
+        double psiP = d0 + d1 * thetaP;
+        psiP = psiP * (1.0 - sweby_limiter) +
+               fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaP), (1.0 - cfl) / (1.0e-30 + cfl) * thetaP)) * sweby_limiter;
+        double psiM = d0 + d1 * thetaM;
+        psiM = psiM * (1.0 - sweby_limiter) +
+               fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaM), (1.0 - cfl) / (1.0e-30 + cfl) * thetaM)) * sweby_limiter;
+        fy[I3(d, i, j, k)] = 0.5 * ((massflux + fabs(massflux)) * (TM(i, j, k) + psiP * Rj) +
+                                    (massflux - fabs(massflux)) * (TM(i, j + 1, k) - psiM * Rj)) *
+                             MK(i, j, k) * MK(i, j + 1, k);
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i)
+        TM(i, j, k) = TM(i, j, k) + dtime * MK(i, j, k) * datr[I2(d, i, j)] / RDZ(i, j, k) *
+                                        (fy[I3(d, i, j - 1, k)] - fy[I3(d, i, j, k)]);
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        TM(i, j, k) = TM(i, j, k) + dtime * TF(i, j, k) / RDZ(i, j, k) *
+                                        (WB(i, j, k) - wkm1[I2(d, i, j)] +
+                                         datr[I2(d, i, j)] * ((dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)] -
+                                                               dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)])));
+        double adv = -RDZ(i, j, k) * (TM(i, j, k) - TF(i, j, k)) / dtime * MK(i, j, k);
+        wrk1[I3(d, i, j, k)] = -adv;
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) wkm1[I2(d, i, j)] = WB(i, j, k);
+  }
+#undef TM
+#undef MK
+#undef TF
+#undef RDZ
+#undef WB
+  free(tm);
+  free(mk);
+  free(ftp);
+  free(fbt);
+  free(wkm1);
+  free(fx);
+  free(fy);
+}
+
+/* ------------------------------------------------------------------------- */
+/* MDFL Sweby for all tracers at once: advect_tracer_sweby_all :4104-4511.   */
+/* T and wrk1 hold ntr consecutive data-domain 3-D blocks.  Differs from the */
+/* one-tracer routine in the grouping of the update products (:4194-4195,    */
+/* :4277-4284, :4386-4399) and in merging the y-pass with the closing        */
+/* divergence correction.                                                    */
+/* ------------------------------------------------------------------------- */
+void orc_advect_sweby_all(const orc_dims* d, int ntr, double dtime, const double* tmask, const double* dat,
+                          const double* datr, const double* dxte, const double* dyte, const double* dxtn,
+                          const double* dytn, const double* uhrho_et, const double* vhrho_nt,
+                          const double* wrho_bt, const double* rho_dzt, const double* Tall, double* wrk1_all) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  size_t n3 = n2 * nk;
+  size_t nh = (size_t)NX2(d) * NY2(d) * nk;
+  double* tma = (double*)calloc(nh * ntr, sizeof(double));
+  double* mk = (double*)calloc(nh, sizeof(double));
+  double* ftp = (double*)calloc(n2, sizeof(double));
+  double* fbt = (double*)calloc(n2, sizeof(double));
+  double* wkm1 = (double*)calloc(n2, sizeof(double));
+  double* fx = (double*)calloc(n3, sizeof(double));
+  double* fy = (double*)calloc(n3, sizeof(double));
+  double* wrk1 = (double*)calloc(n3, sizeof(double));
+  orc_mask_halo2(d, tmask, mk);
+  memset(wrk1_all, 0, sizeof(double) * n3 * ntr);
+#define MK(i, j, k) mk[H3(d, (i), (j), (k))]
+#define RDZ(i, j, k) rho_dzt[I3(d, (i), (j), (k))]
+#define WB(i, j, k) wrho_bt[I3(d, (i), (j), (k) + 1)]
+  for (int n = 0; n < ntr; ++n) {
+    const double* T = Tall + n3 * n;
+    double* tm = tma + nh * n;
+#define TM(i, j, k) tm[H3(d, (i), (j), (k))]
+#define TF(i, j, k) T[I3(d, (i), (j), (k))]
+    memset(ftp, 0, sizeof(double) * n2);
+    memset(wkm1, 0, sizeof(double) * n2);
+    for (int k = 0; k < nk; ++k) {
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) TM(i, j, k) = TF(i, j, k);
+      int kp1 = k + 1 < nk ? k + 1 : nk - 1;
+      int kp2 = k + 2 < nk ? k + 2 : nk - 1;
+      int km1 = k - 1 > 0 ? k - 1 : 0;
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+          double Rjp = (TF(i, j, km1) - TF(i, j, k)) * MK(i, j, km1) * MK(i, j, k);
+          double Rj = (TF(i, j, k) - TF(i, j, kp1)) * MK(i, j, k) * MK(i, j, kp1);
+          double Rjm = (TF(i, j, kp1) - TF(i, j, kp2)) * MK(i, j, kp1) * MK(i, j, kp2);
+          double massflux = dat[I2(d, i, j)] * WB(i, j, k);
+          double cfl = fabs(WB(i, j, k) * dtime / RDZ(i, j, k));
+          double d0 = (2.0 - cfl) * (1.0 - cfl) * onesixth;
+          double d1 = (1.0 - cfl * cfl) * onesixth;
+          double thetaP = Rjm / (1.0e-30 + Rj);
+          double thetaM = Rjp / (1.0e-30 + Rj);
+          double psiP = fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaP), (1.0 - cfl) / (1.0e-30 + cfl) * thetaP));
+          double psiM = fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaM), (1.0 - cfl) / (1.0e-30 + cfl) * thetaM));
+          fbt[I2(d, i, j)] = 0.5 * ((massflux + fabs(massflux)) * (TF(i, j, kp1) + psiP * Rj) +
+                                    (massflux - fabs(massflux)) * (TF(i, j, k) - psiM * Rj)) *
+                             MK(i, j, kp1) * MK(i, j, k);
+          double w1 = datr[I2(d, i, j)] * (fbt[I2(d, i, j)] - ftp[I2(d, i, j)]) +
+                      TF(i, j, k) * (wkm1[I2(d, i, j)] - WB(i, j, k));
+          TM(i, j, k) = TM(i, j, k) + w1 * dtime / RDZ(i, j, k);
+          ftp[I2(d, i, j)] = fbt[I2(d, i, j)];
+        }
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) wkm1[I2(d, i, j)] = WB(i, j, k);
+    }
+    halo2_update(d, tm, 1);
+#undef TM
+#undef TF
+  }
+  for (int n = 0; n < ntr; ++n) {
+    const double* T = Tall + n3 * n;
+    double* tm = tma + nh * n;
+#define TM(i, j, k) tm[H3(d, (i), (j), (k))]
+#define TF(i, j, k) T[I3(d, (i), (j), (k))]
+    for (int k = 0; k < nk; ++k) {
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 0; i <= ni; ++i) {
+          double Rjp = (TM(i + 2, j, k) - TM(i + 1, j, k)) * MK(i + 2, j, k) * MK(i + 1, j, k);
+          double Rj = (TM(i + 1, j, k) - TM(i, j, k)) * MK(i + 1, j, k) * MK(i, j, k);
+          double Rjm = (TM(i, j, k) - TM(i - 1, j, k)) * MK(i, j, k) * MK(i - 1, j, k);
+          double massflux = dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)];
+          double cfl = fabs(uhrho_et[I3(d, i, j, k)] * dtime * 2.0 /
+                            ((RDZ(i, j, k) + RDZ(i + 1, j, k)) * dxte[I2(d, i, j)]));
+          double d0 = (2.0 - cfl) * (1.0 - cfl) * onesixth;
+          double d1 = (1.0 - cfl * cfl) * onesixth;
+          double thetaP = Rjm / (1.0e-30 + Rj);
+          double thetaM = Rjp / (1.0e-30 + Rj);
+          double psiP = fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaP), (1.0 - cfl) / (1.0e-30 + cfl) * thetaP));
+          double psiM = fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaM), (1.0 - cfl) / (1.0e-30 + cfl) * thetaM));
+          fx[I3(d, i, j, k)] = 0.5 * ((massflux + fabs(massflux)) * (TM(i, j, k) + psiP * Rj) +
+                                      (massflux - fabs(massflux)) * (TM(i + 1, j, k) - psiM * Rj)) *
+                               MK(i, j, k) * MK(i + 1, j, k);
+        }
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+          double w1 = MK(i, j, k) * datr[I2(d, i, j)] *
+                      (fx[I3(d, i - 1, j, k)] - fx[I3(d, i, j, k)] +
+                       TF(i, j, k) * (dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)] -
+                                      dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)]));
+          TM(i, j, k) = TM(i, j, k) + w1 * dtime / RDZ(i, j, k);
+        }
+    }
+    halo2_update(d, tm, 2);
+#undef TM
+#undef TF
+  }
+  for (int n = 0; n < ntr; ++n) {
+    const double* T = Tall + n3 * n;
+    double* tm = tma + nh * n;
+    double* out = wrk1_all + n3 * n;
+#define TM(i, j, k) tm[H3(d, (i), (j), (k))]
+#define TF(i, j, k) T[I3(d, (i), (j), (k))]
+    memset(wkm1, 0, sizeof(double) * n2);
+    for (int k = 0; k < nk; ++k) {
+      for (int j = 0; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+          double Rjp = (TM(i, j + 2, k) - TM(i, j + 1, k)) * MK(i, j + 2, k) * MK(i, j + 1, k);
+          double Rj = (TM(i, j + 1, k) - TM(i, j, k)) * MK(i, j + 1, k) * MK(i, j, k);
+          double Rjm = (TM(i, j, k) - TM(i, j - 1, k)) * MK(i, j, k) * MK(i, j - 1, k);
+          double massflux = dxtn[I2(d, i, j)] * vhrho_nt[I3(d, i, j, k)];
+          double cfl = fabs(vhrho_nt[I3(d, i, j, k)] * dtime * 2.0 /
+                            ((RDZ(i, j, k) + RDZ(i, j + 1, k)) * dytn[I2(d, i, j)]));
+          double d0 = (2.0 - cfl) * (1.0 - cfl) * onesixth;
+          double d1 = (1.0 - cfl * cfl) * onesixth;
+          double thetaP = Rjm / (1.0e-30 + Rj);
+          double thetaM = Rjp / (1.0e-30 + Rj);
+          double psiP = fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaP), (1.0 - cfl) / (1.0e-30 + cfl) * thetaP));
+          double psiM = fmaxd(0.0, fmind(fmind(1.0, d0 + d1 * thetaM), (1.0 - cfl) / (1.0e-30 + cfl) * thetaM));
+          fy[I3(d, i, j, k)] = 0.5 * ((massflux + fabs(massflux)) * (TM(i, j, k) + psiP * Rj) +
+                                      (massflux - fabs(massflux)) * (TM(i, j + 1, k) - psiM * Rj)) *
+                               MK(i, j, k) * MK(i, j + 1, k);
+        }
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+          double w1 = MK(i, j, k) * datr[I2(d, i, j)] * (fy[I3(d, i, j - 1, k)] - fy[I3(d, i, j, k)]) +
+                      TF(i, j, k) * (WB(i, j, k) - wkm1[I2(d, i, j)] +
+                                     datr[I2(d, i, j)] * (dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)] -
+                                                          dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)]));
+          TM(i, j, k) = TM(i, j, k) + w1 * dtime / RDZ(i, j, k);
+          out[I3(d, i, j, k)] = RDZ(i, j, k) * (TM(i, j, k) - TF(i, j, k)) / dtime * MK(i, j, k);
+        }
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) wkm1[I2(d, i, j)] = WB(i, j, k);
+    }
+#undef TM
+#undef TF
+  }
+#undef MK
+#undef RDZ
+#undef WB
+  free(tma);
+  free(mk);
+  free(ftp);
+  free(fbt);
+  free(wkm1);
+  free(fx);
+  free(fy);
+  free(wrk1);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Explicit tracer update: ocean_tracer.F90:2341-2350 / :2640-2647.          */
+/* Compute domain only; the caller halo-updates T(taup1) afterwards          */
+/* (ocean_model.F90:1903-1911).                                              */
+/* ------------------------------------------------------------------------- */
+void orc_update_tracer(const orc_dims* d, double dtime, const double* rho_dzt_taum1, const double* rho_dztr,
+                       const double* T_taum1, const double* th_tendency, double* T_taup1) {
+  for (int k = 0; k < d->nk; ++k)
+    for (int j = 1; j <= d->nj; ++j)
+      for (int i = 1; i <= d->ni; ++i) {
+        size_t p = I3(d, i, j, k);
+        T_taup1[p] = (rho_dzt_taum1[p] * T_taum1[p] + dtime * th_tendency[p]) * rho_dztr[p];
+      }
+}
+
+/* compute_tmask_limit, one tracer: ocean_tracer.F90:2804-2851. */
+void orc_compute_tmask_limit(const orc_dims* d, const double* tmask, const double* T_tau, double tmin,
+                             double tmax, double* tmask_limit) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  for (int k = 0; k < nk; ++k)
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        size_t p = I3(d, i, j, k);
+        tmask_limit[p] = 0.0;
+        if (tmask[p] == 1.0 && (T_tau[p] < tmin || T_tau[p] > tmax)) tmask_limit[p] = tmask[p];
+        size_t pe = I3(d, i + 1, j, k);
+        if (tmask[pe] == 1.0 && (T_tau[pe] < tmin || T_tau[pe] > tmax)) tmask_limit[p] = tmask[p];
+        size_t pn = I3(d, i, j + 1, k);
+        if (tmask[pn] == 1.0 && (T_tau[pn] < tmin || T_tau[pn] > tmax)) tmask_limit[p] = tmask[p];
+      }
+  for (int k = 0; k < nk - 1; ++k)
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        size_t p = I3(d, i, j, k);
+        size_t pd = I3(d, i, j, k + 1);
+        if (tmask[pd] == 1.0 && (T_tau[pd] < tmin || T_tau[pd] > tmax)) tmask_limit[p] = tmask[p];
+      }
+}
+
+/* tmask_limit_ts_same (:2855-2867) */
+void orc_tmask_limit_ts_same(const orc_dims* d, double* tl_temp, double* tl_salt) {
+  for (int k = 0; k < d->nk; ++k)
+    for (int j = 0; j <= d->nj; ++j)
+      for (int i = 0; i <= d->ni; ++i) {
+        size_t p = I3(d, i, j, k);
+        if (tl_temp[p] == 1.0 || tl_salt[p] == 1.0) {
+          tl_temp[p] = 1.0;
+          tl_salt[p] = 1.0;
+        }
+      }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Operators on the barotropic domain (halo 1, halo_in = halo_out = 1).      */
+/* ------------------------------------------------------------------------- */
+
+/* DIV_UD, B-grid non-legacy branch: ocean_operators.F90:559-598, 605-606.   */
+void orc_div_ud_bgrid(const orc_dims* d, const double* udu, const double* udv, const double* dyu,
+                      const double* dxu, const double* datr, double* out) {
+  int ni = d->ni, nj = d->nj;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  memset(out, 0, sizeof(double) * n2);
+  for (int j = 1; j <= nj + 1; ++j) {
+    int i = 1;
+    double uhim = udu[I2(d, i - 1, j)] * dyu[I2(d, i - 1, j)];
+    double vhim = udv[I2(d, i - 1, j)] * dxu[I2(d, i - 1, j)];
+    double uhimjm = udu[I2(d, i - 1, j - 1)] * dyu[I2(d, i - 1, j - 1)];
+    double vhimjm = udv[I2(d, i - 1, j - 1)] * dxu[I2(d, i - 1, j - 1)];
+    double uhim_bay = 0.5 * (uhim + uhimjm);
+    for (i = 1; i <= ni + 1; ++i) {
+      double uh = udu[I2(d, i, j)] * dyu[I2(d, i, j)];
+      double vh = udv[I2(d, i, j)] * dxu[I2(d, i, j)];
+      double uhjm = udu[I2(d, i, j - 1)] * dyu[I2(d, i, j - 1)];
+      double vhjm = udv[I2(d, i, j - 1)] * dxu[I2(d, i, j - 1)];
+      double uh_bay = 0.5 * (uh + uhjm);
+      double vh_bax = 0.5 * (vh + vhim);
+      double vhjm_bax = 0.5 * (vhjm + vhimjm);
+      out[I2(d, i, j)] = ((uh_bay - uhim_bay) + (vh_bax - vhjm_bax)) * datr[I2(d, i, j)];
+      uhim = uh;
+      vhim = vh;
+      uhimjm = uhjm;
+      vhimjm = vhjm;
+      uhim_bay = uh_bay;
+    }
+  }
+}
+
+/* DIV_UD, C-grid branch: ocean_operators.F90:526-535. */
+void orc_div_ud_cgrid(const orc_dims* d, const double* udu, const double* udv, const double* dat,
+                      const double* dxter, const double* dytnr, const double* datr, double* out) {
+  int ni = d->ni, nj = d->nj;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  memset(out, 0, sizeof(double) * n2);
+  for (int j = 1; j <= nj + 1; ++j)
+    for (int i = 1; i <= ni + 1; ++i) {
+      double uhim = udu[I2(d, i - 1, j)] * dat[I2(d, i - 1, j)] * dxter[I2(d, i - 1, j)];
+      double vhjm = udv[I2(d, i, j - 1)] * dat[I2(d, i, j - 1)] * dytnr[I2(d, i, j - 1)];
+      double uh = udu[I2(d, i, j)] * dat[I2(d, i, j)] * dxter[I2(d, i, j)];
+      double vh = udv[I2(d, i, j)] * dat[I2(d, i, j)] * dytnr[I2(d, i, j)];
+      out[I2(d, i, j)] = ((uh - uhim) + (vh - vhjm)) * datr[I2(d, i, j)];
+    }
+}
+
+/* GRAD_BAROTROPIC_P: ocean_operators.F90:643-674. */
+void orc_grad_baro_p(const orc_dims* d, int cgrid, const double* press, const double* rx, const double* ry,
+                     const double* mx, const double* my, double* gx, double* gy) {
+  int ni = d->ni, nj = d->nj;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  memset(gx, 0, sizeof(double) * n2);
+  memset(gy, 0, sizeof(double) * n2);
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i <= ni; ++i) {
+      if (!cgrid) {
+        double p_fay = 0.5 * (press[I2(d, i, j)] + press[I2(d, i, j + 1)]);
+        double p_fax = 0.5 * (press[I2(d, i, j)] + press[I2(d, i + 1, j)]);
+        double pip_fay = 0.5 * (press[I2(d, i + 1, j)] + press[I2(d, i + 1, j + 1)]);
+        double pjp_fax = 0.5 * (press[I2(d, i, j + 1)] + press[I2(d, i + 1, j + 1)]);
+        gx[I2(d, i, j)] = (pip_fay - p_fay) * rx[I2(d, i, j)] * mx[I2(d, i, j)];
+        gy[I2(d, i, j)] = (pjp_fax - p_fax) * ry[I2(d, i, j)] * mx[I2(d, i, j)];
+      } else {
+        gx[I2(d, i, j)] = (press[I2(d, i + 1, j)] - press[I2(d, i, j)]) * rx[I2(d, i, j)] * mx[I2(d, i, j)];
+        gy[I2(d, i, j)] = (press[I2(d, i, j + 1)] - press[I2(d, i, j)]) * ry[I2(d, i, j)] * my[I2(d, i, j)];
+      }
+    }
+}
+
+/* REMAP_BT_TO_BU: ocean_operators.F90:462-477 (halo 1). */
+void orc_remap_bt_to_bu(const orc_dims* d, const double* a, const double* dte, const double* dtw,
+                        const double* dus, const double* dun, const double* daur, double* out) {
+  int ni = d->ni, nj = d->nj;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  memset(out, 0, sizeof(double) * n2);
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i <= ni; ++i)
+      out[I2(d, i, j)] = (a[I2(d, i, j)] * dte[I2(d, i, j)] * dus[I2(d, i, j)] +
+                          a[I2(d, i + 1, j)] * dtw[I2(d, i + 1, j)] * dus[I2(d, i, j)] +
+                          a[I2(d, i, j + 1)] * dte[I2(d, i, j + 1)] * dun[I2(d, i, j)] +
+                          a[I2(d, i + 1, j + 1)] * dtw[I2(d, i + 1, j + 1)] * dun[I2(d, i, j)]) *
+                         daur[I2(d, i, j)];
+}
+
+/* ------------------------------------------------------------------------- */
+/* Barotropic step: pred_corr_tropic_depth_bgrid :3225-3579 (legacy halos,   */
+/* barotropic_halo = 1, no OBC, tides, geoid, smoothing or friction),         */
+/* pred_corr_tropic_depth_cgrid :3601-3965 and the splitting branch of       */
+/* update_ocean_barotropic :2793-2985.                                        */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int nts;
+  double dtbt;
+  double pred_corr_gamma;
+  double rho0;
+  int time_stepping_B; /* 0: barotropic_time_stepping_A, 1: _B */
+  int initsum_with_bar;
+  int cgrid;
+} orc_baro_params;
+
+typedef struct {
+  /* grid, data domain */
+  const double *tmask1, *umask1, *f, *dxu, *dyu, *dxur, *dyur, *dat, *datr, *dxter, *dytnr;
+  const double *tmasken_e, *tmasken_n, *dte, *dtw, *dus, *dun, *daur;
+  /* inputs constant over the step */
+  const double *patm, *pme, *river, *source, *eta_smooth, *thicku, *thicken_e, *thicken_n;
+  const double *forcing_u, *forcing_v, *rho_g;
+  /* state at tau */
+  const double *eta_t_tau, *eta_t_bar_tau, *udrho_u_tau, *udrho_v_tau;
+  /* outputs at taup1 */
+  double *eta_t_bar, *udrho_u, *udrho_v, *conv_rho_ud_t, *eta_u, *ps, *grad_ps_x, *grad_ps_y;
+} orc_baro_io;
+
+static void div_ud_any(const orc_dims* d, const orc_baro_params* p, const orc_baro_io* io, const double* u,
+                       const double* v, double* out) {
+  if (p->cgrid)
+    orc_div_ud_cgrid(d, u, v, io->dat, io->dxter, io->dytnr, io->datr, out);
+  else
+    orc_div_ud_bgrid(d, u, v, io->dyu, io->dxu, io->datr, out);
+}
+
+void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, const orc_baro_io* io) {
+  int ni = d->ni, nj = d->nj, nts = p->nts;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double rho0r = 1.0 / p->rho0;
+  double dtbt = p->dtbt;
+  /* ocean_barotropic_init :1195-1197 */
+  double dtbt_gamma_rho0r = dtbt * p->pred_corr_gamma * rho0r;
+  double dtbt_rho0r = dtbt * rho0r;
+  /* AB3 weights :617-619, onefourth */
+  const double abtau_m0 = 23.0 / 12.0, abtau_m1 = -16.0 / 12.0, abtau_m2 = 5.0 / 12.0, onefourth = 0.25;
+
+  double* eta_bt = (double*)calloc(n2 * 2, sizeof(double));
+  double* ubt = (double*)calloc(n2 * 2, sizeof(double));
+  double* vbt = (double*)calloc(n2 * 2, sizeof(double));
+  double* steady = (double*)calloc(n2, sizeof(double));
+  double* tmp = (double*)calloc(n2, sizeof(double));
+  double* ps = (double*)calloc(n2, sizeof(double));
+  double* gx = (double*)calloc(n2, sizeof(double));
+  double* gy = (double*)calloc(n2, sizeof(double));
+  double* cori1 = (double*)calloc(n2, sizeof(double));
+  double* cori2 = (double*)calloc(n2, sizeof(double));
+  double* cf = (double*)calloc(n2 * 2 * 3, sizeof(double)); /* coriolis_force_bt(·,·,2,3) */
+  double* ca = (double*)calloc(n2 * 2, sizeof(double));     /* coriolis_accel_bt(·,·,2) */
+#define CF(i, j, c, l) cf[((size_t)(l) * 2 + (c)) * n2 + I2(d, (i), (j))]
+#define CA(i, j, c) ca[(size_t)(c) * n2 + I2(d, (i), (j))]
+  /* :1283-1288 */
+  for (size_t q = 0; q < n2; ++q) {
+    cori1[q] = 0.5 * dtbt * io->f[q];
+    cori2[q] = 1.0 / (1.0 + cori1[q] * cori1[q]);
+  }
+  int itime = 1;
+  int fstau = (itime + 0) % 2, fstaup1 = (itime + 1) % 2; /* 0-based versions of mod(itime,2)+1 */
+  for (size_t q = 0; q < n2; ++q) {
+    io->eta_t_bar[q] = p->initsum_with_bar ? io->eta_t_bar_tau[q] : io->eta_t_tau[q];
+    io->udrho_u[q] = 0.0;
+    io->udrho_v[q] = 0.0;
+  }
+  for (size_t q = 0; q < n2; ++q) {
+    eta_bt[fstau * n2 + q] = io->eta_t_bar_tau[q];
+    ubt[fstau * n2 + q] = io->udrho_u_tau[q];
+    vbt[fstau * n2 + q] = io->udrho_v_tau[q];
+    steady[q] = io->tmask1[q] * (io->pme[q] + io->river[q] + io->source[q] - io->eta_smooth[q]);
+  }
+  if (p->cgrid) {
+    int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
+    const double* u = ubt + fstau * n2;
+    const double* v = vbt + fstau * n2;
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        CF(i, j, 0, m0) = onefourth * (io->f[I2(d, i, j)] * (v[I2(d, i, j)] + v[I2(d, i + 1, j)]) +
+                                       io->f[I2(d, i, j - 1)] * (v[I2(d, i, j - 1)] + v[I2(d, i + 1, j - 1)]));
+        CF(i, j, 0, m1) = CF(i, j, 0, m0);
+        CF(i, j, 0, m2) = CF(i, j, 0, m0);
+        CA(i, j, 0) = abtau_m0 * CF(i, j, 0, m0) + abtau_m1 * CF(i, j, 0, m1) + abtau_m2 * CF(i, j, 0, m2);
+        CF(i, j, 1, m0) = -onefourth * (io->f[I2(d, i, j)] * (u[I2(d, i, j)] + u[I2(d, i, j + 1)]) +
+                                        io->f[I2(d, i - 1, j)] * (u[I2(d, i - 1, j)] + u[I2(d, i - 1, j + 1)]));
+        CF(i, j, 1, m1) = CF(i, j, 1, m0);
+        CF(i, j, 1, m2) = CF(i, j, 1, m0);
+        CA(i, j, 1) = abtau_m0 * CF(i, j, 1, m0) + abtau_m1 * CF(i, j, 1, m1) + abtau_m2 * CF(i, j, 1, m2);
+      }
+    orc_halo_update_2d(d, ca, 3);
+    orc_halo_update_2d(d, ca + n2, 3);
+  }
+
+  for (itime = 1; itime <= nts; ++itime) {
+    fstau = (itime + 0) % 2;
+    fstaup1 = (itime + 1) % 2;
+    double* eo = eta_bt + fstau * n2;
+    double* en = eta_bt + fstaup1 * n2;
+    double* uo = ubt + fstau * n2;
+    double* un = ubt + fstaup1 * n2;
+    double* vo = vbt + fstau * n2;
+    double* vn = vbt + fstaup1 * n2;
+    /* predictor */
+    if (p->pred_corr_gamma > 0.0) {
+      div_ud_any(d, p, io, uo, vo, tmp);
+      for (size_t q = 0; q < n2; ++q) tmp[q] = -tmp[q] * io->tmask1[q];
+      for (size_t q = 0; q < n2; ++q) en[q] = eo[q] + dtbt_gamma_rho0r * (tmp[q] + steady[q]);
+    } else {
+      for (size_t q = 0; q < n2; ++q) en[q] = eo[q];
+    }
+    if (!p->cgrid) orc_halo_update_2d(d, en, 3); /* use_legacy_barotropic_halos (B-grid only) */
+    for (size_t q = 0; q < n2; ++q) ps[q] = io->rho_g[q] * en[q] + io->patm[q];
+    if (!p->cgrid) {
+      orc_grad_baro_p(d, 0, ps, io->dxur, io->dyur, io->umask1, io->umask1, gx, gy);
+      for (int j = 0; j <= nj + 1; ++j)
+        for (int i = 0; i <= ni + 1; ++i) {
+          size_t q = I2(d, i, j);
+          double pf1 = -io->thicku[q] * gx[q];
+          double pf2 = -io->thicku[q] * gy[q];
+          double t1 = uo[q] + dtbt * (0.5 * io->f[q] * vo[q] + pf1 + io->forcing_u[q] + 0.0);
+          double t2 = vo[q] + dtbt * (-0.5 * io->f[q] * uo[q] + pf2 + io->forcing_v[q] + 0.0);
+          un[q] = cori2[q] * (t1 + cori1[q] * t2);
+          vn[q] = cori2[q] * (t2 - cori1[q] * t1);
+        }
+    } else {
+      int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
+      memset(ca, 0, sizeof(double) * n2 * 2);
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+          CF(i, j, 0, m0) = onefourth * (io->f[I2(d, i, j)] * (vo[I2(d, i, j)] + vo[I2(d, i + 1, j)]) +
+                                         io->f[I2(d, i, j - 1)] * (vo[I2(d, i, j - 1)] + vo[I2(d, i + 1, j - 1)]));
+          CA(i, j, 0) = abtau_m0 * CF(i, j, 0, m0) + abtau_m1 * CF(i, j, 0, m1) + abtau_m2 * CF(i, j, 0, m2);
+          CF(i, j, 1, m0) = -onefourth * (io->f[I2(d, i, j)] * (uo[I2(d, i, j)] + uo[I2(d, i, j + 1)]) +
+                                          io->f[I2(d, i - 1, j)] * (uo[I2(d, i - 1, j)] + uo[I2(d, i - 1, j + 1)]));
+          CA(i, j, 1) = abtau_m0 * CF(i, j, 1, m0) + abtau_m1 * CF(i, j, 1, m1) + abtau_m2 * CF(i, j, 1, m2);
+        }
+      orc_grad_baro_p(d, 1, ps, io->dxter, io->dytnr, io->tmasken_e, io->tmasken_n, gx, gy);
+      for (int j = 0; j <= nj + 1; ++j)
+        for (int i = 0; i <= ni + 1; ++i) {
+          size_t q = I2(d, i, j);
+          double pf1 = -io->thicken_e[q] * gx[q];
+          double pf2 = -io->thicken_n[q] * gy[q];
+          un[q] = uo[q] + dtbt * io->tmasken_e[q] * (CA(i, j, 0) + pf1 + io->forcing_u[q] + 0.0);
+          vn[q] = vo[q] + dtbt * io->tmasken_n[q] * (CA(i, j, 1) + pf2 + io->forcing_v[q] + 0.0);
+        }
+      orc_halo_update_2d(d, un, 3);
+      orc_halo_update_2d(d, vn, 3);
+    }
+    /* corrector */
+    div_ud_any(d, p, io, un, vn, tmp);
+    for (size_t q = 0; q < n2; ++q) tmp[q] = -tmp[q] * io->tmask1[q];
+    for (size_t q = 0; q < n2; ++q) en[q] = eo[q] + dtbt_rho0r * (tmp[q] + steady[q]);
+    /* accumulate */
+    double wgt = p->time_stepping_B ? (double)(nts - itime + 1) : 1.0;
+    for (size_t q = 0; q < n2; ++q) {
+      io->eta_t_bar[q] = io->eta_t_bar[q] + en[q];
+      if (p->time_stepping_B) {
+        io->udrho_u[q] = io->udrho_u[q] + wgt * un[q];
+        io->udrho_v[q] = io->udrho_v[q] + wgt * vn[q];
+      } else {
+        io->udrho_u[q] = io->udrho_u[q] + un[q];
+        io->udrho_v[q] = io->udrho_v[q] + vn[q];
+      }
+    }
+  }
+#undef CF
+#undef CA
+  /* update_ocean_barotropic, splitting branch :2803-2811, :2846-2901, :2969-2985 */
+  double rntsp1 = 1.0 / ((double)nts + 1.0);
+  double rnts = p->time_stepping_B ? 2.0 / ((double)nts * (double)(nts + 1)) : 1.0 / (double)nts;
+  for (size_t q = 0; q < n2; ++q) io->eta_t_bar[q] = rntsp1 * io->eta_t_bar[q];
+  orc_halo_update_2d(d, io->eta_t_bar, 3);
+  for (size_t q = 0; q < n2; ++q) io->udrho_u[q] = rnts * io->udrho_u[q];
+  for (size_t q = 0; q < n2; ++q) io->udrho_v[q] = rnts * io->udrho_v[q];
+  orc_halo_update_2d(d, io->udrho_u, 3);
+  orc_halo_update_2d(d, io->udrho_v, 3);
+  div_ud_any(d, p, io, io->udrho_u, io->udrho_v, tmp);
+  for (size_t q = 0; q < n2; ++q) io->conv_rho_ud_t[q] = -tmp[q];
+  orc_halo_update_2d(d, io->conv_rho_ud_t, 3);
+  orc_remap_bt_to_bu(d, io->eta_t_bar, io->dte, io->dtw, io->dus, io->dun, io->daur, tmp);
+  for (size_t q = 0; q < n2; ++q) io->eta_u[q] = io->umask1[q] * tmp[q];
+  orc_halo_update_2d(d, io->eta_u, 3);
+  /* twolevel: itime = taup1 (:2797-2801) */
+  for (size_t q = 0; q < n2; ++q) io->ps[q] = io->rho_g[q] * io->eta_t_bar[q] + io->patm[q];
+  if (!p->cgrid)
+    orc_grad_baro_p(d, 0, io->ps, io->dxur, io->dyur, io->umask1, io->umask1, io->grad_ps_x, io->grad_ps_y);
+  else
+    orc_grad_baro_p(d, 1, io->ps, io->dxter, io->dytnr, io->tmasken_e, io->tmasken_n, io->grad_ps_x,
+                    io->grad_ps_y);
+  free(eta_bt);
+  free(ubt);
+  free(vbt);
+  free(steady);
+  free(tmp);
+  free(ps);
+  free(gx);
+  free(gy);
+  free(cori1);
+  free(cori2);
+  free(cf);
+  free(ca);
+}
+
+/* eta_and_pbot_tendency, depth-based: ocean_barotropic.F90:2683-2690. */
+void orc_eta_and_pbot_tendency(const orc_dims* d, double rho0, const double* tmask1, const double* conv_tau,
+                               const double* pme, const double* river, const double* source, double* deta_dt) {
+  double rho0r = 1.0 / rho0;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  for (size_t q = 0; q < n2; ++q)
+    deta_dt[q] = tmask1[q] * rho0r * (conv_tau[q] + pme[q] + river[q] + source[q]);
+}
+
+/* eta_and_pbot_update, depth-based, no OBC: :2314-2330. */
+void orc_eta_and_pbot_update(const orc_dims* d, double dtime, const double* eta_taum1, const double* deta_dt,
+                             double* eta_taup1) {
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) eta_taup1[I2(d, i, j)] = eta_taum1[I2(d, i, j)] + dtime * deta_dt[I2(d, i, j)];
+  orc_halo_update_2d(d, eta_taup1, 3);
+}
+
+/* Continuity for the B-grid tracer vertical mass flux with rho_dzt_tendency =
+ * mass_source = 0: ocean_advection_velocity.F90:600-606 (diverge_t from
+ * BDX_ET/BDY_NT, ocean_operators.F90:951-956, :1236-1241) and :609-627.     */
+void orc_continuity_w(const orc_dims* d, const double* tmask, const double* dyte, const double* dxtn,
+                      const double* datr, const double* uhrho_et, const double* vhrho_nt, const double* pme,
+                      const double* river, double* wrho_bt) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* bdx = (double*)calloc(n2, sizeof(double));
+  double* bdy = (double*)calloc(n2, sizeof(double));
+  for (size_t q = 0; q < n2; ++q) wrho_bt[q] = -(pme[q] + river[q]);
+  for (int k = 0; k < nk; ++k) {
+    memset(bdx, 0, sizeof(double) * n2);
+    memset(bdy, 0, sizeof(double) * n2);
+    for (int j = 0; j <= nj + 1; ++j)
+      for (int i = 1; i <= ni + 1; ++i)
+        bdx[I2(d, i, j)] = (dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)] -
+                            dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)]) *
+                           datr[I2(d, i, j)];
+    for (int j = 1; j <= nj + 1; ++j)
+      for (int i = 0; i <= ni + 1; ++i)
+        bdy[I2(d, i, j)] = (dxtn[I2(d, i, j)] * vhrho_nt[I3(d, i, j, k)] -
+                            dxtn[I2(d, i, j - 1)] * vhrho_nt[I3(d, i, j - 1, k)]) *
+                           datr[I2(d, i, j)];
+    for (size_t q = 0; q < n2; ++q) {
+      double div = tmask[(size_t)k * n2 + q] * (bdx[q] + bdy[q]);
+      wrho_bt[(size_t)(k + 1) * n2 + q] = (0.0 + div + wrho_bt[(size_t)k * n2 + q]) * tmask[(size_t)k * n2 + q];
+    }
+  }
+  free(bdx);
+  free(bdy);
+}
+
+/* total_tracer (ocean_tracer_diag.F90:2395-2412) with conversion = 1: the
+ * per-column sum over k in the reference order, then a global sum.  The
+ * global sum here is Neumaier-compensated; result[0] = sum, result[1] = the
+ * plain left-to-right sum in Fortran array order. */
+void orc_total_tracer(const orc_dims* d, const double* tmask, const double* dat, const double* rho_dzt,
+                      const double* T, double* result) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  double s = 0.0, c = 0.0, plain = 0.0;
+  for (int j = 1; j <= nj; ++j)
+    for (int i = 1; i <= ni; ++i) {
+      double col = 0.0;
+      for (int k = 0; k < nk; ++k) {
+        size_t p = I3(d, i, j, k);
+        col = col + 1.0 * tmask[p] * dat[I2(d, i, j)] * rho_dzt[p] * T[p];
+      }
+      plain += col;
+      double t = s + col;
+      if (fabs(s) >= fabs(col))
+        c += (s - t) + col;
+      else
+        c += (col - t) + s;
+      s = t;
+    }
+  result[0] = s + c;
+  result[1] = plain;
+}
+
+/* mass integral used by the barotropic conservation test: sum of
+ * tmask1 * dat * eta over the compute domain, Neumaier-compensated. */
+double orc_area_integral(const orc_dims* d, const double* tmask1, const double* dat, const double* eta) {
+  double s = 0.0, c = 0.0;
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) {
+      double x = tmask1[I2(d, i, j)] * dat[I2(d, i, j)] * eta[I2(d, i, j)];
+      double t = s + x;
+      if (fabs(s) >= fabs(x))
+        c += (s - t) + x;
+      else
+        c += (x - t) + s;
+      s = t;
+    }
+  return s + c;
+}

@@ -1,0 +1,243 @@
+"""ctypes front end of the C restatement in mom5_oracle.c.
+
+TEST INFRASTRUCTURE ONLY: used by tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of bench.py to check the CUDA library.  The shipped library
+never imports this module.
+
+All arrays are numpy float64 in the reference's data-domain layout (halo 1,
+Fortran column-major == C-ordered ``(nk, nj+2, ni+2)``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Dict
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libmom5oracle.so")
+_lib = None
+
+DP = C.POINTER(C.c_double)
+
+
+class Dims(C.Structure):
+    _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("cyclic_x", C.c_int), ("cyclic_y", C.c_int)]
+
+
+class Quicker(C.Structure):
+    _fields_ = [(n, DP) for n in ("quick_x", "quick_y", "curv_xp", "curv_xn", "curv_yp", "curv_yn",
+                                  "quick_z", "curv_zp", "curv_zn", "tmask_quick")]
+
+
+class BaroParams(C.Structure):
+    _fields_ = [("nts", C.c_int), ("dtbt", C.c_double), ("pred_corr_gamma", C.c_double), ("rho0", C.c_double),
+                ("time_stepping_B", C.c_int), ("initsum_with_bar", C.c_int), ("cgrid", C.c_int)]
+
+
+BARO_IO_FIELDS = ["tmask1", "umask1", "f", "dxu", "dyu", "dxur", "dyur", "dat", "datr", "dxter", "dytnr",
+                  "tmasken_e1", "tmasken_n1", "dte", "dtw", "dus", "dun", "daur",
+                  "patm", "pme", "river", "source", "eta_smooth", "thicku", "thicken_e", "thicken_n",
+                  "forcing_u", "forcing_v", "rho_g",
+                  "eta_t_tau", "eta_t_bar_tau", "udrho_u_tau", "udrho_v_tau",
+                  "out_eta_t_bar", "out_udrho_u", "out_udrho_v", "out_conv_rho_ud_t", "out_eta_u", "out_ps",
+                  "out_grad_ps_x", "out_grad_ps_y"]
+
+
+class BaroIO(C.Structure):
+    _fields_ = [(n, DP) for n in BARO_IO_FIELDS]
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        _lib = C.CDLL(_LIB_PATH)
+        _lib.orc_area_integral.restype = C.c_double
+    return _lib
+
+
+def p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(DP)
+
+
+def dims(spec) -> Dims:
+    return Dims(spec.ni, spec.nj, spec.nk, int(spec.cyclic_x), int(spec.cyclic_y))
+
+
+def np64(t) -> np.ndarray:
+    """torch tensor or array -> contiguous float64 numpy copy."""
+    if hasattr(t, "detach"):
+        t = t.detach().cpu().numpy()
+    return np.ascontiguousarray(t, dtype=np.float64)
+
+
+# ----------------------------------------------------------------------------- wrappers
+def horz_advect_upwind(d: Dims, g: Dict[str, np.ndarray], T: np.ndarray) -> np.ndarray:
+    out = np.zeros_like(T)
+    lib().orc_horz_advect_upwind(C.byref(d), p(g["tmask"]), p(g["dyte"]), p(g["dxtn"]), p(g["datr"]),
+                                 p(g["uhrho_et"]), p(g["vhrho_nt"]), p(T), p(out))
+    return out
+
+
+def vert_advect_upwind(d: Dims, g, T):
+    out = np.zeros_like(T)
+    lib().orc_vert_advect_upwind(C.byref(d), p(g["tmask"]), p(g["wrho_bt"]), p(T), p(out))
+    return out
+
+
+def quicker_init(d: Dims, g, dzt: np.ndarray):
+    nxd, nyd, nk = d.ni + 2, d.nj + 2, d.nk
+    q = {"quick_x": np.zeros((2, nyd, nxd)), "quick_y": np.zeros((2, nyd, nxd)),
+         "curv_xp": np.zeros((3, nyd, nxd)), "curv_xn": np.zeros((3, nyd, nxd)),
+         "curv_yp": np.zeros((3, nyd, nxd)), "curv_yn": np.zeros((3, nyd, nxd)),
+         "quick_z": np.zeros((2, nk)), "curv_zp": np.zeros((3, nk)), "curv_zn": np.zeros((3, nk)),
+         "tmask_quick": np.zeros((nk, d.nj + 4, d.ni + 4))}
+    qs = Quicker(*[p(q[n]) for n, _ in Quicker._fields_])
+    lib().orc_quicker_init(C.byref(d), p(g["dxt"]), p(g["dyt"]), p(np64(dzt)), p(g["tmask"]), C.byref(qs))
+    q["_struct"] = qs
+    return q
+
+
+def horz_advect_quicker(d, g, q, Tm1, T0, tmask_limit=None, limit_with_upwind=False):
+    out = np.zeros_like(Tm1)
+    tl = tmask_limit if tmask_limit is not None else np.zeros_like(Tm1)
+    lib().orc_horz_advect_quicker(C.byref(d), int(limit_with_upwind), C.byref(q["_struct"]), p(g["tmask"]), p(tl),
+                                  p(g["dyte"]), p(g["dxtn"]), p(g["datr"]), p(g["uhrho_et"]), p(g["vhrho_nt"]),
+                                  p(Tm1), p(T0), p(out))
+    return out
+
+
+def vert_advect_quicker(d, g, q, Tm1, T0, tmask_limit=None):
+    out = np.zeros_like(Tm1)
+    tl = tmask_limit if tmask_limit is not None else np.zeros_like(Tm1)
+    lib().orc_vert_advect_quicker(C.byref(d), C.byref(q["_struct"]), p(g["tmask"]), p(tl), p(g["wrho_bt"]),
+                                  p(Tm1), p(T0), p(out))
+    return out
+
+
+def advect_mdfl_sweby(d, g, T, dtime, sweby_limiter=1.0):
+    out = np.zeros_like(T)
+    lib().orc_advect_mdfl_sweby(C.byref(d), C.c_double(sweby_limiter), C.c_double(dtime), p(g["tmask"]),
+                                p(g["dat"]), p(g["datr"]), p(g["dxte"]), p(g["dyte"]), p(g["dxtn"]), p(g["dytn"]),
+                                p(g["uhrho_et"]), p(g["vhrho_nt"]), p(g["wrho_bt"]), p(g["rho_dzt"]), p(T), p(out))
+    return out
+
+
+def advect_sweby_all(d, g, Tall, dtime):
+    out = np.zeros_like(Tall)
+    lib().orc_advect_sweby_all(C.byref(d), int(Tall.shape[0]), C.c_double(dtime), p(g["tmask"]), p(g["dat"]),
+                               p(g["datr"]), p(g["dxte"]), p(g["dyte"]), p(g["dxtn"]), p(g["dytn"]),
+                               p(g["uhrho_et"]), p(g["vhrho_nt"]), p(g["wrho_bt"]), p(g["rho_dzt"]), p(Tall), p(out))
+    return out
+
+
+def update_tracer(d, g, Tm1, th, dtime):
+    out = Tm1.copy()
+    lib().orc_update_tracer(C.byref(d), C.c_double(dtime), p(g["rho_dzt"]), p(g["rho_dztr"]), p(Tm1), p(th), p(out))
+    lib().orc_halo_update_3d(C.byref(d), p(out), d.nk, 3)
+    return out
+
+
+def compute_tmask_limit(d, g, T, tmin, tmax):
+    out = np.zeros_like(T)
+    lib().orc_compute_tmask_limit(C.byref(d), p(g["tmask"]), p(T), C.c_double(tmin), C.c_double(tmax), p(out))
+    return out
+
+
+def tmask_limit_ts_same(d, tl_t, tl_s):
+    lib().orc_tmask_limit_ts_same(C.byref(d), p(tl_t), p(tl_s))
+
+
+def halo_update(d, a, flags=3):
+    nlev = a.shape[0] if a.ndim == 3 else 1
+    lib().orc_halo_update_3d(C.byref(d), p(a), nlev, flags)
+
+
+def continuity_w(d, g):
+    nk = d.nk
+    w = np.zeros((nk + 1, d.nj + 2, d.ni + 2))
+    z = np.zeros((d.nj + 2, d.ni + 2))
+    lib().orc_continuity_w(C.byref(d), p(g["tmask"]), p(g["dyte"]), p(g["dxtn"]), p(g["datr"]), p(g["uhrho_et"]),
+                           p(g["vhrho_nt"]), p(z), p(z), p(w))
+    return w
+
+
+def total_tracer(d, g, T):
+    r = np.zeros(2)
+    lib().orc_total_tracer(C.byref(d), p(g["tmask"]), p(g["dat"]), p(g["rho_dzt"]), p(T), p(r))
+    return r
+
+
+def area_integral(d, g, eta):
+    return lib().orc_area_integral(C.byref(d), p(g["tmask1"]), p(g["dat"]), p(eta))
+
+
+def div_ud_bgrid(d, g, u, v):
+    out = np.zeros_like(u)
+    lib().orc_div_ud_bgrid(C.byref(d), p(u), p(v), p(g["dyu"]), p(g["dxu"]), p(g["datr"]), p(out))
+    return out
+
+
+def grad_baro_p(d, g, press, cgrid=False):
+    gx = np.zeros_like(press)
+    gy = np.zeros_like(press)
+    if cgrid:
+        lib().orc_grad_baro_p(C.byref(d), 1, p(press), p(g["dxter"]), p(g["dytnr"]), p(g["tmasken_e1"]),
+                              p(g["tmasken_n1"]), p(gx), p(gy))
+    else:
+        lib().orc_grad_baro_p(C.byref(d), 0, p(press), p(g["dxur"]), p(g["dyur"]), p(g["umask1"]), p(g["umask1"]),
+                              p(gx), p(gy))
+    return gx, gy
+
+
+def eta_and_pbot_tendency(d, g, conv_tau, rho0=1035.0):
+    out = np.zeros_like(conv_tau)
+    lib().orc_eta_and_pbot_tendency(C.byref(d), C.c_double(rho0), p(g["tmask1"]), p(conv_tau), p(g["pme"]),
+                                    p(g["river"]), p(g["source"]), p(out))
+    return out
+
+
+def eta_and_pbot_update(d, eta_taum1, deta_dt, dtime):
+    out = eta_taum1.copy()
+    lib().orc_eta_and_pbot_update(C.byref(d), C.c_double(dtime), p(eta_taum1), p(deta_dt), p(out))
+    return out
+
+
+def update_ocean_barotropic(d, g, state, nts, dtbt, gamma=0.2, rho0=1035.0, time_stepping_B=True,
+                            initsum_with_bar=True, cgrid=False):
+    """One barotropic step; ``state`` holds eta_t, eta_t_bar, udrho_u, udrho_v at tau.
+    Returns the taup1 fields."""
+    shp = g["tmask1"].shape
+    out = {k: np.zeros(shp) for k in ("eta_t_bar", "udrho_u", "udrho_v", "conv_rho_ud_t", "eta_u", "ps",
+                                      "grad_ps_x", "grad_ps_y")}
+    src = dict(g)
+    src["eta_t_tau"] = state["eta_t"]
+    src["eta_t_bar_tau"] = state["eta_t_bar"]
+    src["udrho_u_tau"] = state["udrho_u"]
+    src["udrho_v_tau"] = state["udrho_v"]
+    ptrs = []
+    for n in BARO_IO_FIELDS:
+        if n.startswith("out_"):
+            ptrs.append(p(out[n[4:]]))
+        else:
+            ptrs.append(p(src[n]))
+    io = BaroIO(*ptrs)
+    prm = BaroParams(int(nts), float(dtbt), float(gamma), float(rho0), int(time_stepping_B), int(initsum_with_bar),
+                     int(cgrid))
+    lib().orc_update_ocean_barotropic(C.byref(d), C.byref(prm), C.byref(io))
+    return out
+
+
+def domain_arrays(dom) -> Dict[str, np.ndarray]:
+    """numpy copies of a grid.Domain's arrays (the oracle's inputs)."""
+    return {k: np64(v) for k, v in dom.f.items() if k != "kmt"}

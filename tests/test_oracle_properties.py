@@ -1,0 +1,286 @@
+"""CPU tests of the C restatement (the oracle) itself.
+
+The reference ships no golden vectors for these routines, so the restatement is
+pinned by properties the reference algorithms must satisfy: conservation,
+preservation of a uniform tracer, the documented reductions between schemes,
+closed-form weights, exact one-cell shifts, symmetric gravity waves and the
+restart identity.  Each test names the reference lines it checks.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from mom5_gb300 import grid
+
+
+def small(ni=24, nj=18, nk=8, ntr=2, seed=1, cyclic_x=False, continent=(8, 6, 5, 4), **kw):
+    return grid.DomainSpec(ni=ni, nj=nj, nk=nk, lon0=0.0, lon1=float(ni), lat0=-20.0, lat1=20.0,
+                           cyclic_x=cyclic_x, continent=continent, wavelength_cells=6.0, ntracers=ntr, seed=seed, **kw)
+
+
+@pytest.fixture(scope="module")
+def O(oracle_lib):
+    return oracle_lib
+
+
+def load(O, sp):
+    dom = grid.make_domain(sp)
+    return dom, O.domain_arrays(dom), O.dims(sp)
+
+
+@pytest.mark.parametrize("cyclic_x", [False, True])
+def test_flow_is_divergence_free(O, cyclic_x):
+    """Continuity (ocean_advection_velocity.F90:600-627) reproduces the generator's
+    vertical mass flux, and it vanishes at the sea floor."""
+    dom, g, d = load(O, small(cyclic_x=cyclic_x))
+    w = O.continuity_w(d, g)
+    assert np.allclose(w, g["wrho_bt"], rtol=0, atol=1e-9 * np.abs(g["uhrho_et"]).max())
+    kmt = dom["kmt"].numpy()
+    scale = np.abs(g["wrho_bt"]).max()
+    assert scale > 0
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            if kmt[j, i] > 0:
+                assert abs(g["wrho_bt"][kmt[j, i], j, i]) <= 1e-10 * scale
+
+
+@pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker"])
+@pytest.mark.parametrize("cyclic_x", [False, True])
+def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
+    """A uniform tracer in a non-divergent flow has zero advective tendency
+    (to roundoff) under every scheme."""
+    dom, g, d = load(O, small(cyclic_x=cyclic_x))
+    U = np.ascontiguousarray(g["tmask"] * 7.25)
+    if scheme == "mdfl":
+        th = O.advect_mdfl_sweby(d, g, U, 3600.0)
+    elif scheme == "dst":
+        th = O.advect_mdfl_sweby(d, g, U, 3600.0, 0.0)
+    elif scheme == "all":
+        th = O.advect_sweby_all(d, g, np.ascontiguousarray(U[None]), 3600.0)[0]
+    elif scheme == "upwind":
+        th = O.horz_advect_upwind(d, g, U) + O.vert_advect_upwind(d, g, U)
+    else:
+        q = O.quicker_init(d, g, dom.dzt.numpy())
+        th = O.horz_advect_quicker(d, g, q, U, U) + O.vert_advect_quicker(d, g, q, U, U)
+    scale = 7.25 * np.abs(g["wrho_bt"]).max() + 7.25 * np.abs(g["uhrho_et"]).max() * g["datr"].max() * 1e5
+    assert np.abs(th).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("scheme", ["mdfl", "upwind", "quicker"])
+def test_global_content_conserved(O, scheme):
+    """sum(dat*rho_dzt*T*tmask) (ocean_tracer_diag.F90:2395-2412) is unchanged by
+    advection plus the explicit update, to FP64 roundoff."""
+    dom, g, d = load(O, small(seed=7))
+    q = O.quicker_init(d, g, dom.dzt.numpy())
+    T = g["T"][0].copy()
+    c0 = O.total_tracer(d, g, T)[0]
+    for _ in range(10):
+        if scheme == "mdfl":
+            th = O.advect_mdfl_sweby(d, g, T, 3600.0 * 6)
+        elif scheme == "upwind":
+            th = O.horz_advect_upwind(d, g, T) + O.vert_advect_upwind(d, g, T)
+        else:
+            th = O.horz_advect_quicker(d, g, q, T, T) + O.vert_advect_quicker(d, g, q, T, T)
+        T = O.update_tracer(d, g, T, th, 3600.0 * 6)
+    c1 = O.total_tracer(d, g, T)[0]
+    assert abs(c1 - c0) <= 1e-13 * abs(c0)
+
+
+def test_sweby_is_monotone_and_quicker_is_not(O):
+    """Torus pulse test (testcase_ocean_solo.pdf section 2), qualitative: Quicker
+    over/undershoots a square pulse, MDFL Sweby's extrema are far smaller.  The
+    reference documents that this legacy MDFL routine is not strictly monotone
+    (ocean_tracer_advect.F90:3755-3760), so small extrema are expected."""
+    sp = small(ni=32, nj=24, nk=4, continent=None, ntr=1, seed=3, cyclic_x=True, hmin=None, depth=400.0,
+               dz_top=80.0, dz_bot=120.0)
+    dom, g, d = load(O, sp)
+    q = O.quicker_init(d, g, dom.dzt.numpy())
+    T = np.zeros_like(g["T"][0])
+    T[:, 8:16, 10:20] = 1.0
+    T *= g["tmask"]
+    O.halo_update(d, T)
+    Ts, Tq = T.copy(), T.copy()
+    dt = 3600.0 * 6
+    for _ in range(20):
+        Ts = O.update_tracer(d, g, Ts, O.advect_mdfl_sweby(d, g, Ts, dt), dt)
+        th = O.horz_advect_quicker(d, g, q, Tq, Tq) + O.vert_advect_quicker(d, g, q, Tq, Tq)
+        Tq = O.update_tracer(d, g, Tq, th, dt)
+    wet = g["tmask"] > 0
+    ext_s = max(-Ts[wet].min(), Ts[wet].max() - 1.0, 0.0)
+    ext_q = max(-Tq[wet].min(), Tq[wet].max() - 1.0, 0.0)
+    assert ext_q > 1e-3
+    assert ext_s < 1e-3 and ext_s < 0.05 * ext_q
+
+
+def test_sweby_all_equals_one_tracer_to_roundoff(O):
+    """advect_tracer_sweby_all (:4104-4511) regroups the products of
+    advect_tracer_mdfl_sweby (:3806-4066): same values to a few ulps."""
+    dom, g, d = load(O, small(ntr=3, seed=9))
+    dt = 3600.0 * 6
+    allv = O.advect_sweby_all(d, g, np.ascontiguousarray(g["T"]), dt)
+    for n in range(3):
+        one = O.advect_mdfl_sweby(d, g, g["T"][n].copy(), dt)
+        # the tendency is rho_dzt*(T_mdfl - T)/dt: roundoff of T_mdfl is amplified by rho_dzt/dt
+        tol = 64 * np.finfo(float).eps * np.abs(g["T"][n]).max() * g["rho_dzt"].max() / dt
+        assert np.abs(allv[n] - one).max() <= tol
+        assert np.abs(allv[n] - one).max() > 0 or n > 0
+
+
+def test_dst_linear_is_sweby_without_limiter(O):
+    """sweby_limiter = 0 gives the linear DST scheme (:1960-1962): it differs from
+    the limited scheme where the limiter is active, and is not monotone."""
+    dom, g, d = load(O, small(ntr=1, seed=12))
+    T = g["T"][0].copy()
+    a = O.advect_mdfl_sweby(d, g, T, 3600.0 * 6, 1.0)
+    b = O.advect_mdfl_sweby(d, g, T, 3600.0 * 6, 0.0)
+    assert np.abs(a - b).max() > 0
+
+
+def test_upwind_cfl_one_shifts_one_cell(O):
+    """1-D upwind at Courant number 1 moves a profile exactly one cell (:2238-2294)."""
+    sp = grid.DomainSpec(ni=16, nj=3, nk=1, lon0=0.0, lon1=16.0, lat0=-1.0, lat1=1.0, cyclic_x=True,
+                         continent=None, hmin=None, ntracers=1, seed=0)
+    dom, g, d = load(O, sp)
+    u = 0.75  # m/s
+    rdz = g["rho_dzt"][0, 1, 1]
+    g["uhrho_et"][:] = u * rdz
+    g["vhrho_nt"][:] = 0.0
+    g["wrho_bt"][:] = 0.0
+    g["tmask"][:] = 0.0
+    g["tmask"][:, 1:-1, :] = 1.0
+    dx = g["dxte"][2, 3]
+    dt = dx / u
+    T = np.zeros_like(g["T"][0])
+    T[0, 2, 1:17] = np.arange(16, dtype=float) ** 2
+    O.halo_update(d, T)
+    th = O.horz_advect_upwind(d, g, T)
+    Tn = O.update_tracer(d, g, T, th, dt)
+    expect = np.roll(T[0, 2, 1:17], 1)
+    assert np.allclose(Tn[0, 2, 1:17], expect, rtol=1e-12, atol=1e-9)
+
+
+def test_quicker_weights_uniform_grid(O):
+    """On a uniform grid quicker_init (:1510-1578) gives quick = 1/2 and the
+    curvature weights 1/8, -1/4 (relative form of the classic 3/8, 6/8, -1/8)."""
+    sp = grid.DomainSpec(ni=10, nj=8, nk=5, lon0=0.0, lon1=10.0, lat0=-0.5, lat1=0.5, continent=None, hmin=None,
+                         ntracers=1, seed=0, dz_top=50.0, dz_bot=50.0, depth=250.0)
+    dom, g, d = load(O, sp)
+    g["dxt"][:] = 1000.0
+    g["dyt"][:] = 1000.0
+    q = O.quicker_init(d, g, np.full(5, 50.0))
+    inner = (slice(None), slice(2, -2), slice(2, -2))
+    assert np.allclose(q["quick_x"][inner], 0.5) and np.allclose(q["quick_y"][inner], 0.5)
+    assert np.allclose(q["curv_xp"][0][2:-2, 2:-2], 1.0 / 8.0)
+    assert np.allclose(q["curv_xp"][1][2:-2, 2:-2], -1.0 / 4.0)
+    assert np.allclose(q["curv_xp"][2][2:-2, 2:-2], 1.0 / 8.0)
+    assert np.allclose(q["quick_z"], 0.5)
+    assert np.allclose(q["curv_zp"][:, 1:-2], np.array([[1 / 8.0], [-1 / 4.0], [1 / 8.0]]))
+
+
+def _flat_basin(O, n=40, f0=0.0, cyclic=False):
+    sp = grid.DomainSpec(ni=n, nj=n, nk=1, lon0=0.0, lon1=float(n) * 0.1, lat0=-0.1 * n / 2, lat1=0.1 * n / 2,
+                         cyclic_x=cyclic, continent=None, hmin=None, ntracers=0, seed=0)
+    dom, g, d = load(O, sp)
+    g["f"][:] = f0
+    g["forcing_u"][:] = 0.0
+    g["forcing_v"][:] = 0.0
+    g["dxu"][:] = g["dxu"][2, 2]
+    g["dxt"][:] = g["dxt"][2, 2]
+    g["dxur"][:] = 1.0 / (g["dxu"] + 1e-40)
+    g["dat"][:] = g["dxt"] * g["dyt"]
+    g["datr"][:] = 1.0 / (g["dat"] + 1e-40)
+    return dom, g, d
+
+
+def test_barotropic_mass_conserved_and_symmetric(O):
+    """Flat bottom, f = 0, a centred eta bump: the subcycle (:3225-3579) keeps
+    sum(dat*eta_t_bar) (no sources) and the solution stays symmetric under i ->
+    mirror and j -> mirror."""
+    n = 40
+    dom, g, d = _flat_basin(O, n)
+    x = np.arange(n + 2) - (n + 1) / 2.0
+    bump = np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 18.0) * 0.1
+    eta = np.ascontiguousarray(bump * g["tmask1"])
+    st = {"eta_t": eta, "eta_t_bar": eta.copy(), "udrho_u": np.zeros_like(eta), "udrho_v": np.zeros_like(eta)}
+    m0 = O.area_integral(d, g, eta)
+    for _ in range(4):
+        out = O.update_ocean_barotropic(d, g, st, 40, 20.0)
+        st = {"eta_t": eta, "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"], "udrho_v": out["udrho_v"]}
+    e = out["eta_t_bar"][1:-1, 1:-1]
+    assert abs(O.area_integral(d, g, out["eta_t_bar"]) - m0) <= 1e-12 * abs(m0)
+    assert np.abs(e - e[:, ::-1]).max() <= 1e-6 * np.abs(e).max() * 10 + 1e-12
+    assert np.abs(e - e[::-1, :]).max() <= 1e-6 * np.abs(e).max() * 10 + 1e-12
+    assert np.abs(e - bump[1:-1, 1:-1]).max() > 1e-4  # the waves moved
+
+
+def test_barotropic_gamma0_nts1_is_forward_backward(O):
+    """With pred_corr_gamma = 0 and nts = 1 the subcycle is one forward-backward
+    step: eta from the old transport divergence is not used for the pressure."""
+    n = 20
+    dom, g, d = _flat_basin(O, n, f0=1e-4)
+    rng = np.random.default_rng(1)
+    eta = np.ascontiguousarray(rng.normal(size=g["tmask1"].shape) * 0.01 * g["tmask1"])
+    st = {"eta_t": eta, "eta_t_bar": eta.copy(), "udrho_u": np.zeros_like(eta), "udrho_v": np.zeros_like(eta)}
+    out = O.update_ocean_barotropic(d, g, st, 1, 10.0, gamma=0.0, time_stepping_B=False)
+    # by hand: ps from eta, momentum from the pressure gradient, eta from the new transport
+    ps = g["rho_g"] * eta + g["patm"]
+    gx, gy = O.grad_baro_p(d, g, ps)
+    c1 = 0.5 * 10.0 * g["f"]
+    c2 = 1.0 / (1.0 + c1 * c1)
+    t1 = 10.0 * (-g["thicku"] * gx)
+    t2 = 10.0 * (-g["thicku"] * gy)
+    u = c2 * (t1 + c1 * t2)
+    v = c2 * (t2 - c1 * t1)
+    dv = O.div_ud_bgrid(d, g, np.ascontiguousarray(u), np.ascontiguousarray(v))
+    eta1 = eta + 10.0 / 1035.0 * (-dv * g["tmask1"])
+    expect_bar = (eta + eta1) / 2.0
+    inner = (slice(1, -1), slice(1, -1))
+    assert np.allclose(out["eta_t_bar"][inner], expect_bar[inner], rtol=1e-12, atol=1e-15)
+    assert np.allclose(out["udrho_u"][inner], u[inner], rtol=1e-12, atol=1e-12)
+
+
+def test_barotropic_restart_identity(O):
+    """N steps == N/2 steps, restart from the saved fields, N/2 steps (the
+    reference's restart identity, testcase_ocean_solo.pdf section 1.1)."""
+    sp = grid.DomainSpec(ni=30, nj=24, nk=1, cyclic_x=True, hmin=None, ridge_amp=800.0, ntracers=0, seed=4)
+    dom, g, d = load(O, sp)
+    st0 = {k: g[k].copy() for k in ("eta_t", "eta_t_bar", "udrho_u", "udrho_v")}
+
+    def run(st, nsteps):
+        for _ in range(nsteps):
+            out = O.update_ocean_barotropic(d, g, st, 10, 30.0)
+            st = {"eta_t": st["eta_t"], "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"],
+                  "udrho_v": out["udrho_v"]}
+        return st
+
+    a = run(st0, 4)
+    half = run(st0, 2)
+    saved = {k: np.frombuffer(v.tobytes()).reshape(v.shape).copy() for k, v in half.items()}
+    b = run(saved, 2)
+    for k in a:
+        assert np.array_equal(a[k], b[k])
+
+
+def test_tmask_limit_flags_out_of_range(O):
+    """compute_tmask_limit (ocean_tracer.F90:2804-2851) flags a wet cell whose own,
+    east, north or lower neighbour is outside the tracer's range."""
+    dom, g, d = load(O, small(ntr=1, seed=2, continent=None, hmin=None))
+    T = np.full_like(g["T"][0], 10.0) * g["tmask"]
+    T[3, 5, 7] = 50.0
+    tl = O.compute_tmask_limit(d, g, T, 0.0, 20.0)
+    assert tl[3, 5, 7] == 1 and tl[3, 5, 6] == 1 and tl[3, 4, 7] == 1 and tl[2, 5, 7] == 1
+    assert tl[3, 5, 8] == 0 and tl[3, 6, 7] == 0 and tl[4, 5, 7] == 0
+    assert tl.sum() == 4
+
+
+def test_halo_update_semantics(O):
+    """Single-PE mpp_update_domains: periodic copy in cyclic directions, halo
+    untouched at walls, corners only when both directions are cyclic."""
+    from oracle.oracle import Dims
+    d = Dims(4, 3, 1, 1, 0)
+    a = np.arange(6 * 5, dtype=float).reshape(1, 5, 6)
+    b = a.copy()
+    O.halo_update(d, b)
+    assert np.array_equal(b[0, 1:4, 0], a[0, 1:4, 4]) and np.array_equal(b[0, 1:4, 5], a[0, 1:4, 1])
+    assert np.array_equal(b[0, 0, :], a[0, 0, :]) and np.array_equal(b[0, 4, :], a[0, 4, :])
