@@ -56,6 +56,8 @@ def config_spec(name: str, ntr_override=None):
         return grid.config_c0()
     if name == "c1":
         return grid.config_c1()
+    if name == "c2s":
+        return grid.config_c2_block()
     raise SystemExit(f"unknown config {name}")
 
 
@@ -203,7 +205,10 @@ def run_ours(args, rank, world):
     cells = ni * nj * nk
     del dom
     torch.cuda.empty_cache()
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the legacy default stream's handle is 0, which the C ABI
+    # reads as "the domain's own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     d.set_stream(stream.cuda_stream)
 
     state = {"tau": 1}
@@ -337,7 +342,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--config", choices=["c2", "c0", "c1"], default="c2")
+    ap.add_argument("--config", choices=["c2", "c0", "c1", "c2s"], default="c2")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

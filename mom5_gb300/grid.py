@@ -93,6 +93,13 @@ def config_c2(seed: int = 2, ntracers: int = 10) -> DomainSpec:
                       ntracers=ntracers, seed=seed)
 
 
+def config_c2_block(seed: int = 3, ntracers: int = 10) -> DomainSpec:
+    """A 360x270x50 block of the 0.25 degree grid (lon 0-90, lat -40..27.5) with
+    10 tracers: 1/16 of the global config, used for profiling captures."""
+    return DomainSpec(ni=360, nj=270, nk=50, lon0=0.0, lon1=90.0, lat0=-40.0, lat1=27.5,
+                      cyclic_x=False, continent=(150, 100, 40, 30), hmin=2000.0, ntracers=ntracers, seed=seed)
+
+
 def stretched_dz(nk: int, top: float, bot: float, total: float) -> torch.Tensor:
     """Level thicknesses growing from ``top`` to ``bot`` as a power law whose
     exponent is solved so that the levels sum to ``total``."""
