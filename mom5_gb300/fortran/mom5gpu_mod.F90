@@ -1,0 +1,332 @@
+!-----------------------------------------------------------------------
+! mom5gpu_mod: ISO_C_BINDING interface to libmom5gpu.so (include/mom5gpu.h)
+! and drop-in wrappers with the procedure names and dummy argument lists of
+!   ocean_tracer_advect_mod : horz_advect_tracer, vert_advect_tracer
+!                             (ocean_tracer_advect.F90:1898-1908, :2095-2104)
+!   ocean_barotropic_mod    : update_ocean_barotropic, eta_and_pbot_tendency,
+!                             eta_and_pbot_update
+!                             (ocean_barotropic.F90:2763-2774, :2668, :2290)
+!
+! The device domain keeps the grid, the advection velocity and the tracer
+! state resident.  The wrappers copy in only what the host changed since the
+! last call (flags set by mom5gpu_mark_*), call the C entry point and copy the
+! outputs the caller reads (th_tendency, Ext_mode fields) back.  Arrays are
+! passed with their Fortran data-domain bounds (isd:ied, jsd:jed, ...), which
+! is the layout the C ABI expects.
+!
+! Build (where a Fortran compiler exists):
+!   gfortran -fdefault-real-8 -c mom5gpu_mod.F90   (after ocean_types_mod)
+!   link with -L<repo>/mom5_gb300 -lmom5gpu -lcudart
+!-----------------------------------------------------------------------
+module mom5gpu_c
+  use, intrinsic :: iso_c_binding
+  implicit none
+  public
+
+  integer(c_int), parameter :: MOM5GPU_OK = 0
+  integer(c_int), parameter :: MOM5GPU_BGRID = 1, MOM5GPU_CGRID = 2
+  integer(c_int), parameter :: MOM5GPU_PRECISION_FP64 = 0, MOM5GPU_PRECISION_MIXED = 1
+  ! field ids (enum mom5gpu_field)
+  integer(c_int), parameter :: F_DXT = 1, F_DYT = 2, F_DXU = 3, F_DYU = 4, F_DXTE = 5, F_DYTE = 6, &
+       F_DXTN = 7, F_DYTN = 8, F_DAT = 9, F_DATR = 10, F_DXUR = 11, F_DYUR = 12, F_DXTER = 13, &
+       F_DYTNR = 14, F_DTE = 15, F_DTW = 16, F_DUS = 17, F_DUN = 18, F_DAUR = 19, F_CORIOLIS_F = 20, &
+       F_UMASK1 = 21, F_TMASKEN_E1 = 22, F_TMASKEN_N1 = 23, F_TMASK = 40, F_UHRHO_ET = 50, &
+       F_VHRHO_NT = 51, F_WRHO_BT = 52, F_RHO_DZT = 60, F_RHO_DZTR = 61, F_THICKU = 62, &
+       F_THICKEN_E = 63, F_THICKEN_N = 64, F_TRACER = 70, F_TH_TENDENCY = 71, F_TMASK_LIMIT = 72, &
+       F_ETA_T = 80, F_ETA_T_BAR = 81, F_ETA_U = 82, F_UDRHO_U = 83, F_UDRHO_V = 84, &
+       F_CONV_RHO_UD_T = 85, F_DETA_DT = 86, F_FORCING_BT_U = 87, F_FORCING_BT_V = 88, &
+       F_SOURCE = 89, F_ETA_SMOOTH = 90, F_PS = 91, F_GRAD_PS_X = 92, F_GRAD_PS_Y = 93, &
+       F_PATM = 100, F_PME = 101, F_RIVER = 102, F_RHO_G = 103
+
+  type, bind(C) :: mom5gpu_dims
+     integer(c_int) :: ni, nj, nk, cyclic_x, cyclic_y, num_prog_tracers, horz_grid
+  end type mom5gpu_dims
+
+  type, bind(C) :: mom5gpu_options
+     integer(c_int) :: advect_sweby_all, limit_with_upwind, zero_tracer_advect_horz, zero_tracer_advect_vert
+     integer(c_int) :: barotropic_time_stepping_A, barotropic_time_stepping_B, initsum_with_bar
+     real(c_double) :: pred_corr_gamma, rho0, grav
+     integer(c_int) :: precision
+  end type mom5gpu_options
+
+  interface
+     subroutine mom5gpu_default_options(opt) bind(C, name="mom5gpu_default_options")
+       import :: mom5gpu_options
+       type(mom5gpu_options), intent(out) :: opt
+     end subroutine
+     integer(c_int) function mom5gpu_create(dims, opt, dom) bind(C, name="mom5gpu_create")
+       import :: c_int, c_ptr, mom5gpu_dims, mom5gpu_options
+       type(mom5gpu_dims), intent(in) :: dims
+       type(mom5gpu_options), intent(in) :: opt
+       type(c_ptr), intent(out) :: dom
+     end function
+     subroutine mom5gpu_destroy(dom) bind(C, name="mom5gpu_destroy")
+       import :: c_ptr
+       type(c_ptr), value :: dom
+     end subroutine
+     type(c_ptr) function mom5gpu_last_error(dom) bind(C, name="mom5gpu_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: dom
+     end function
+     integer(c_int) function mom5gpu_set_field(dom, field, n, level, src, on_device) &
+          bind(C, name="mom5gpu_set_field")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: field, n, level, on_device
+       real(c_double), intent(in) :: src(*)
+     end function
+     integer(c_int) function mom5gpu_get_field(dom, field, n, level, dst, on_device) &
+          bind(C, name="mom5gpu_get_field")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: field, n, level, on_device
+       real(c_double), intent(out) :: dst(*)
+     end function
+     integer(c_int) function mom5gpu_set_vertical_grid(dom, dzt, zw, kmt) bind(C, name="mom5gpu_set_vertical_grid")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       real(c_double), intent(in) :: dzt(*), zw(*)
+       integer(c_int), intent(in) :: kmt(*)
+     end function
+     integer(c_int) function mom5gpu_set_tracer_scheme(dom, n, horz, vert, tmin, tmax) &
+          bind(C, name="mom5gpu_set_tracer_scheme")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, horz, vert
+       real(c_double), value :: tmin, tmax
+     end function
+     integer(c_int) function mom5gpu_tracer_advect_init(dom) bind(C, name="mom5gpu_tracer_advect_init")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+     end function
+     integer(c_int) function mom5gpu_barotropic_init(dom, dtuv, dtbt) bind(C, name="mom5gpu_barotropic_init")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       real(c_double), value :: dtuv, dtbt
+     end function
+     integer(c_int) function mom5gpu_horz_advect_tracer(dom, n, taum1, tau, dtime) &
+          bind(C, name="mom5gpu_horz_advect_tracer")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, taum1, tau
+       real(c_double), value :: dtime
+     end function
+     integer(c_int) function mom5gpu_vert_advect_tracer(dom, n, taum1, tau, dtime) &
+          bind(C, name="mom5gpu_vert_advect_tracer")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, taum1, tau
+       real(c_double), value :: dtime
+     end function
+     integer(c_int) function mom5gpu_compute_tmask_limit(dom, tau, index_temp, index_salt) &
+          bind(C, name="mom5gpu_compute_tmask_limit")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: tau, index_temp, index_salt
+     end function
+     integer(c_int) function mom5gpu_zero_th_tendency(dom, n) bind(C, name="mom5gpu_zero_th_tendency")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n
+     end function
+     integer(c_int) function mom5gpu_update_tracer(dom, n, taum1, taup1, dtime) bind(C, name="mom5gpu_update_tracer")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, taum1, taup1
+       real(c_double), value :: dtime
+     end function
+     integer(c_int) function mom5gpu_eta_and_pbot_tendency(dom, tau) bind(C, name="mom5gpu_eta_and_pbot_tendency")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: tau
+     end function
+     integer(c_int) function mom5gpu_eta_and_pbot_update(dom, taum1, taup1, dtime) &
+          bind(C, name="mom5gpu_eta_and_pbot_update")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: taum1, taup1
+       real(c_double), value :: dtime
+     end function
+     integer(c_int) function mom5gpu_update_ocean_barotropic(dom, tau, taup1) &
+          bind(C, name="mom5gpu_update_ocean_barotropic")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: tau, taup1
+     end function
+     integer(c_int) function mom5gpu_global_tracer_content(dom, n, level, total) &
+          bind(C, name="mom5gpu_global_tracer_content")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, level
+       real(c_double), intent(out) :: total
+     end function
+  end interface
+end module mom5gpu_c
+
+
+module mom5gpu_mod
+  ! Drop-in wrappers.  ocean_tracer.F90:2300-2303 and ocean_model.F90:1752,
+  ! :1819, :1941 call these exactly as they call the reference procedures once
+  ! the use statements point here (see INTEGRATION.md).
+  use, intrinsic :: iso_c_binding
+  use mom5gpu_c
+  use mpp_mod,          only: mpp_error, FATAL
+  use ocean_types_mod,  only: ocean_time_type, ocean_adv_vel_type, ocean_thickness_type, ocean_density_type, &
+                              ocean_prog_tracer_type, ocean_external_mode_type
+  implicit none
+  private
+
+  public :: mom5gpu_attach, mom5gpu_mark_velocity_changed, mom5gpu_mark_state_changed
+  public :: horz_advect_tracer, vert_advect_tracer
+  public :: update_ocean_barotropic, eta_and_pbot_tendency, eta_and_pbot_update
+
+  type(c_ptr), save :: dom = c_null_ptr
+  logical, save :: velocity_dirty = .true.
+  logical, save :: state_dirty = .true.
+
+contains
+
+  subroutine check(st, where)
+    integer(c_int), intent(in) :: st
+    character(len=*), intent(in) :: where
+    character(len=256), pointer :: msg
+    type(c_ptr) :: p
+    if (st /= MOM5GPU_OK) then
+       p = mom5gpu_last_error(dom)
+       call c_f_pointer(p, msg)
+       call mpp_error(FATAL, 'mom5gpu ('//where//'): '//trim(msg(1:index(msg, c_null_char)-1)))
+    endif
+  end subroutine check
+
+  ! Called once from ocean_model_init after the grid and the first state exist:
+  ! takes ownership of the device domain created by the host driver.
+  subroutine mom5gpu_attach(handle)
+    type(c_ptr), intent(in) :: handle
+    dom = handle
+  end subroutine mom5gpu_attach
+
+  subroutine mom5gpu_mark_velocity_changed()
+    velocity_dirty = .true.
+  end subroutine mom5gpu_mark_velocity_changed
+
+  subroutine mom5gpu_mark_state_changed()
+    state_dirty = .true.
+  end subroutine mom5gpu_mark_state_changed
+
+  subroutine push_inputs(Time, Adv_vel, Thickness, T_prog)
+    type(ocean_time_type),        intent(in) :: Time
+    type(ocean_adv_vel_type),     intent(in) :: Adv_vel
+    type(ocean_thickness_type),   intent(in) :: Thickness
+    type(ocean_prog_tracer_type), intent(in) :: T_prog(:)
+    integer :: n
+    if (velocity_dirty) then
+       call check(mom5gpu_set_field(dom, F_UHRHO_ET, 0, 0, Adv_vel%uhrho_et, 0), 'uhrho_et')
+       call check(mom5gpu_set_field(dom, F_VHRHO_NT, 0, 0, Adv_vel%vhrho_nt, 0), 'vhrho_nt')
+       call check(mom5gpu_set_field(dom, F_WRHO_BT, 0, 0, Adv_vel%wrho_bt, 0), 'wrho_bt')
+       call check(mom5gpu_set_field(dom, F_RHO_DZT, 0, Time%tau, Thickness%rho_dzt(:,:,:,Time%tau), 0), 'rho_dzt')
+       call check(mom5gpu_set_field(dom, F_RHO_DZT, 0, Time%taum1, Thickness%rho_dzt(:,:,:,Time%taum1), 0), 'rho_dzt')
+       call check(mom5gpu_set_field(dom, F_RHO_DZTR, 0, 0, Thickness%rho_dztr, 0), 'rho_dztr')
+       velocity_dirty = .false.
+    endif
+    if (state_dirty) then
+       do n = 1, size(T_prog)
+          call check(mom5gpu_set_field(dom, F_TRACER, n, Time%taum1, T_prog(n)%field(:,:,:,Time%taum1), 0), 'T')
+          if (Time%tau /= Time%taum1) &
+             call check(mom5gpu_set_field(dom, F_TRACER, n, Time%tau, T_prog(n)%field(:,:,:,Time%tau), 0), 'T')
+          call check(mom5gpu_set_field(dom, F_TH_TENDENCY, n, 0, T_prog(n)%th_tendency, 0), 'th_tendency')
+       enddo
+       state_dirty = .false.
+    endif
+  end subroutine push_inputs
+
+  ! ocean_tracer_advect.F90:1898-1908
+  subroutine horz_advect_tracer(Time, Adv_vel, Thickness, Dens, T_prog, Tracer, ntracer, dtime, store_flux)
+    type(ocean_time_type),        intent(in)    :: Time
+    type(ocean_adv_vel_type),     intent(in)    :: Adv_vel
+    type(ocean_thickness_type),   intent(in)    :: Thickness
+    type(ocean_density_type),     intent(in)    :: Dens
+    type(ocean_prog_tracer_type), intent(inout) :: T_prog(:)
+    type(ocean_prog_tracer_type), intent(inout) :: Tracer
+    integer,                      intent(in)    :: ntracer
+    real,                         intent(in)    :: dtime
+    logical, optional,            intent(in)    :: store_flux
+    call push_inputs(Time, Adv_vel, Thickness, T_prog)
+    call check(mom5gpu_horz_advect_tracer(dom, int(ntracer, c_int), int(Time%taum1, c_int), int(Time%tau, c_int), &
+         real(dtime, c_double)), 'horz_advect_tracer')
+    call check(mom5gpu_get_field(dom, F_TH_TENDENCY, int(ntracer, c_int), 0, Tracer%th_tendency, 0), 'th_tendency')
+  end subroutine horz_advect_tracer
+
+  ! ocean_tracer_advect.F90:2095-2104
+  subroutine vert_advect_tracer(Time, Adv_vel, Dens, Thickness, T_prog, Tracer, ntracer, dtime)
+    type(ocean_time_type),        intent(in)    :: Time
+    type(ocean_adv_vel_type),     intent(in)    :: Adv_vel
+    type(ocean_density_type),     intent(in)    :: Dens
+    type(ocean_thickness_type),   intent(in)    :: Thickness
+    type(ocean_prog_tracer_type), intent(inout) :: T_prog(:)
+    type(ocean_prog_tracer_type), intent(inout) :: Tracer
+    integer,                      intent(in)    :: ntracer
+    real,                         intent(in)    :: dtime
+    call push_inputs(Time, Adv_vel, Thickness, T_prog)
+    call check(mom5gpu_vert_advect_tracer(dom, int(ntracer, c_int), int(Time%taum1, c_int), int(Time%tau, c_int), &
+         real(dtime, c_double)), 'vert_advect_tracer')
+    call check(mom5gpu_get_field(dom, F_TH_TENDENCY, int(ntracer, c_int), 0, Tracer%th_tendency, 0), 'th_tendency')
+    ! th_tendency is modified by other terms on the host before the next tracer call
+    state_dirty = .true.
+  end subroutine vert_advect_tracer
+
+  ! ocean_barotropic.F90:2668
+  subroutine eta_and_pbot_tendency(Time, pme, river, Ext_mode, use_blobs)
+    type(ocean_time_type),          intent(in)    :: Time
+    real, dimension(:,:),           intent(in)    :: pme, river
+    type(ocean_external_mode_type), intent(inout) :: Ext_mode
+    logical,                        intent(in)    :: use_blobs
+    if (use_blobs) call mpp_error(FATAL, 'mom5gpu: use_blobs is outside the implemented path')
+    call check(mom5gpu_set_field(dom, F_PME, 0, 0, pme, 0), 'pme')
+    call check(mom5gpu_set_field(dom, F_RIVER, 0, 0, river, 0), 'river')
+    call check(mom5gpu_set_field(dom, F_SOURCE, 0, 0, Ext_mode%source, 0), 'source')
+    call check(mom5gpu_eta_and_pbot_tendency(dom, int(Time%tau, c_int)), 'eta_and_pbot_tendency')
+    call check(mom5gpu_get_field(dom, F_DETA_DT, 0, 0, Ext_mode%deta_dt, 0), 'deta_dt')
+  end subroutine eta_and_pbot_tendency
+
+  ! ocean_barotropic.F90:2290
+  subroutine eta_and_pbot_update(Time, Ext_mode)
+    type(ocean_time_type),          intent(in)    :: Time
+    type(ocean_external_mode_type), intent(inout) :: Ext_mode
+    call check(mom5gpu_eta_and_pbot_update(dom, int(Time%taum1, c_int), int(Time%taup1, c_int), &
+         real(Time%dtime_e, c_double)), 'eta_and_pbot_update')
+    call check(mom5gpu_get_field(dom, F_ETA_T, 0, int(Time%taup1, c_int), Ext_mode%eta_t(:,:,Time%taup1), 0), 'eta_t')
+  end subroutine eta_and_pbot_update
+
+  ! ocean_barotropic.F90:2763-2774
+  subroutine update_ocean_barotropic(Time, Dens, Thickness, Adv_vel, Ext_mode, patm, pme, river, use_blobs)
+    type(ocean_time_type),          intent(in)    :: Time
+    type(ocean_density_type),       intent(in)    :: Dens
+    type(ocean_thickness_type),     intent(in)    :: Thickness
+    type(ocean_adv_vel_type),       intent(in)    :: Adv_vel
+    type(ocean_external_mode_type), intent(inout) :: Ext_mode
+    real, dimension(:,:),           intent(in)    :: patm, pme, river
+    logical,                        intent(in)    :: use_blobs
+    integer(c_int) :: tau, taup1
+    if (use_blobs) call mpp_error(FATAL, 'mom5gpu: use_blobs is outside the implemented path')
+    tau = int(Time%tau, c_int)
+    taup1 = int(Time%taup1, c_int)
+    call check(mom5gpu_set_field(dom, F_PATM, 0, 0, patm, 0), 'patm')
+    call check(mom5gpu_set_field(dom, F_PME, 0, 0, pme, 0), 'pme')
+    call check(mom5gpu_set_field(dom, F_RIVER, 0, 0, river, 0), 'river')
+    call check(mom5gpu_set_field(dom, F_FORCING_BT_U, 0, 0, Ext_mode%forcing_bt(:,:,1), 0), 'forcing_bt')
+    call check(mom5gpu_set_field(dom, F_FORCING_BT_V, 0, 0, Ext_mode%forcing_bt(:,:,2), 0), 'forcing_bt')
+    call check(mom5gpu_set_field(dom, F_THICKU, 0, tau, Thickness%thicku(:,:,Time%tau), 0), 'thicku')
+    call check(mom5gpu_set_field(dom, F_SOURCE, 0, 0, Ext_mode%source, 0), 'source')
+    call check(mom5gpu_set_field(dom, F_ETA_SMOOTH, 0, 0, Ext_mode%eta_smooth, 0), 'eta_smooth')
+    call check(mom5gpu_update_ocean_barotropic(dom, tau, taup1), 'update_ocean_barotropic')
+    call check(mom5gpu_get_field(dom, F_ETA_T_BAR, 0, taup1, Ext_mode%eta_t_bar(:,:,Time%taup1), 0), 'eta_t_bar')
+    call check(mom5gpu_get_field(dom, F_UDRHO_U, 0, taup1, Ext_mode%udrho(:,:,1,Time%taup1), 0), 'udrho')
+    call check(mom5gpu_get_field(dom, F_UDRHO_V, 0, taup1, Ext_mode%udrho(:,:,2,Time%taup1), 0), 'udrho')
+    call check(mom5gpu_get_field(dom, F_CONV_RHO_UD_T, 0, taup1, Ext_mode%conv_rho_ud_t(:,:,Time%taup1), 0), 'conv')
+    call check(mom5gpu_get_field(dom, F_ETA_U, 0, taup1, Ext_mode%eta_u(:,:,Time%taup1), 0), 'eta_u')
+    call check(mom5gpu_get_field(dom, F_PS, 0, 0, Ext_mode%ps, 0), 'ps')
+    call check(mom5gpu_get_field(dom, F_GRAD_PS_X, 0, 0, Ext_mode%grad_ps(:,:,1), 0), 'grad_ps')
+    call check(mom5gpu_get_field(dom, F_GRAD_PS_Y, 0, 0, Ext_mode%grad_ps(:,:,2), 0), 'grad_ps')
+  end subroutine update_ocean_barotropic
+
+end module mom5gpu_mod
