@@ -230,6 +230,30 @@ int mom5gpu_timing_query(mom5gpu_domain* d, const char* section, double* total_m
 /* Number of kernels this domain has launched since creation. */
 long mom5gpu_launch_count(const mom5gpu_domain* d);
 
+/* ---- allocation-free variant ---------------------------------------------
+ * No counterpart in the reference.  For callers that cannot let the library
+ * allocate device memory (a model whose GPU memory is reserved by its own pool,
+ * a process under a hard device-memory cap, or code that must not call
+ * cudaMalloc/cudaFree because they synchronise the device): adds the MDFL Sweby
+ * (scheme 9) or DST-linear (scheme 10) advection tendency of ONE tracer to
+ * th_tendency, exactly as mom5gpu_horz_advect_tracer does, without any device
+ * allocation.  Every pointer is a caller-owned DEVICE array in the domain
+ * layout above: 2-D metrics (dat, datr, dxte, dyte, dxtn, dytn), 3-D tmask,
+ * uhrho_et, vhrho_nt, rho_dzt(tau), T(taum1), th_tendency (read and written),
+ * and wrho_bt with nk+1 levels.  Work is queued on `stream` (NULL = default).
+ * Limit: (ni+2)*(nj+2)*nk <= 2097152 data-domain cells (and
+ * (ni+4)*(nj+4)*nk <= 4194304); larger domains get MOM5GPU_EINVAL with a
+ * message in mom5gpu_last_error(NULL).  The scratch is a 36 MB file-scope
+ * device array held by every GPU that loads the library until exit; the first
+ * call on each device looks up its address, so make that first call before any
+ * stream capture.  Calls share the one array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int mom5gpu_mdfl_sweby_noalloc(const mom5gpu_dims* dims, int scheme, double dtime, const double* tmask,
+                               const double* dat, const double* datr, const double* dxte, const double* dyte,
+                               const double* dxtn, const double* dytn, const double* uhrho_et,
+                               const double* vhrho_nt, const double* wrho_bt, const double* rho_dzt,
+                               const double* T, double* th_tendency, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -113,6 +113,7 @@ def lib() -> C.CDLL:
             "mom5gpu_enable_timing": (C.c_int, [vp, C.c_int]),
             "mom5gpu_timing_query": (C.c_int, [vp, C.c_char_p, dp, C.POINTER(C.c_long)]),
             "mom5gpu_launch_count": (C.c_long, [vp]),
+            "mom5gpu_mdfl_sweby_noalloc": (C.c_int, [C.POINTER(Dims), C.c_int, C.c_double] + [vp] * 14),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

@@ -120,7 +120,26 @@ struct ClockScope {
 };
 inline void count_launches(mom5gpu_domain* d, long n) { d->launches += n; }
 
+// Arguments of the FP64 MDFL passes (k_fp64.cu).
+struct MdflArgs {
+  Geo g;
+  int ntr;
+  double dtime;
+  const uint8_t* mask2;  // tmask_mdfl
+  const double *dat, *datr, *dxte, *dyte, *dxtn, *dytn;
+  const double *uh, *vh, *w;  // uhrho_et, vhrho_nt, wrho_bt (0:nk)
+  const double* rdz;          // rho_dzt(tau)
+  const double* T;            // tracer 0 at taum1; tracer n at T + n*tstride
+  long tstride;
+  double* tz;                 // after z, tracer n at tz + n*g.n3
+  double* tx;                 // after x
+  double* th;                 // th_tendency of tracer 0, tracer n at th + n*g.n3
+};
+
 // ---- FP64 kernels (k_fp64.cu) ----
+// the three MDFL passes on the stream, for the tracers described by a
+// (at most 8 per call); scratch a.tz/a.tx and a.mask2 are the caller's.
+void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s);
 void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t s);
 int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,
                 double sweby_limiter);

@@ -100,20 +100,6 @@ void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t
 // intermediate tracer_mdfl in global scratch; the tracer-independent terms of
 // each face are computed once and reused for every tracer of the launch.
 // ---------------------------------------------------------------------------
-struct MdflArgs {
-  Geo g;
-  int ntr;
-  double dtime;
-  const uint8_t* mask2;  // tmask_mdfl
-  const double *dat, *datr, *dxte, *dyte, *dxtn, *dytn;
-  const double *uh, *vh, *w;  // uhrho_et, vhrho_nt, wrho_bt (0:nk)
-  const double* rdz;          // rho_dzt(tau)
-  const double* T;            // tracer 0 at taum1; tracer n at T + n*tstride
-  long tstride;
-  double* tz;                 // after z, tracer n at tz + n*g.n3
-  double* tx;                 // after x
-  double* th;                 // th_tendency of tracer 0, tracer n at th + n*g.n3
-};
 
 // z pass: one thread per column, march down k.
 template <bool ALL, bool SWEBY, int MAXN>
@@ -352,6 +338,16 @@ static void run_mdfl_n(const MdflArgs& a, cudaStream_t s) {
   else if (a.ntr <= 2) run_mdfl<ALL, SWEBY, 2>(a, s);
   else if (a.ntr <= 4) run_mdfl<ALL, SWEBY, 4>(a, s);
   else run_mdfl<ALL, SWEBY, 8>(a, s);
+}
+
+void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s) {
+  if (all) {
+    if (sweby) run_mdfl_n<true, true>(a, s);
+    else run_mdfl_n<true, false>(a, s);
+  } else {
+    if (sweby) run_mdfl_n<false, true>(a, s);
+    else run_mdfl_n<false, false>(a, s);
+  }
 }
 
 static int ensure_mdfl_scratch(mom5gpu_domain* d, int ntr) {

@@ -1,0 +1,69 @@
+"""The allocation-free entry point (mom5gpu_mdfl_sweby_noalloc) against the
+domain API's mom5gpu_horz_advect_tracer.
+
+The allocation-free call exists for hosts that cannot let the library call
+cudaMalloc (memory reserved by their own pool, a hard device-memory cap, or no
+device-synchronising calls allowed).  It keeps its scratch in a fixed
+file-scope device array that every call shares, so the test makes two calls in
+a row on different tracers and checks both against the existing entry point,
+with the same tolerance as the other FP64 parity tests: IEEE equality.  This
+file is collected last, after every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mom5_gb300 import grid
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, a):
+    t = a if hasattr(a, "detach") else torch.from_numpy(np.ascontiguousarray(a))
+    return t.to(device="cuda", dtype=torch.float64).contiguous()
+
+
+@pytest.mark.parametrize("cyclic_x,scheme", [(True, 9), (False, 9), (True, 10)])
+def test_noalloc_matches_domain_entry_point(gpu_lib, cyclic_x, scheme):
+    import torch
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    sp = grid.DomainSpec(ni=44, nj=31, nk=11, lon0=0.0, lon1=44.0, lat0=-30.0, lat1=30.0, cyclic_x=cyclic_x,
+                         continent=(12, 9, 7, 5), wavelength_cells=6.0, ntracers=2, seed=17)
+    dom = grid.make_domain(sp)
+    dt = 6 * 3600.0
+    # existing entry point
+    d = harness.load(dom, scheme=scheme)
+    ref = []
+    for n in (1, 2):
+        th0 = np.linspace(-1.0, 1.0, d.count(capi.F.TH_TENDENCY))  # accumulation onto a non-zero tendency
+        d.set(capi.F.TH_TENDENCY, th0, n=n)
+        d.horz_advect_tracer(n, 1, 1, dt)
+        ref.append(d.get(capi.F.TH_TENDENCY, n=n))
+    d.close()
+    # allocation-free entry point: device arrays owned by the caller
+    f = {k: _dev(torch, dom[k]) for k in ("tmask", "dat", "datr", "dxte", "dyte", "dxtn", "dytn", "uhrho_et",
+                                          "vhrho_nt", "wrho_bt", "rho_dzt")}
+    dims = capi.Dims(sp.ni, sp.nj, sp.nk, int(sp.cyclic_x), int(sp.cyclic_y), 2, capi.BGRID)
+    for n in (1, 2):  # two calls in a row share the scratch array
+        T = _dev(torch, dom["T"][n - 1])
+        th = _dev(torch, np.linspace(-1.0, 1.0, T.numel()))
+        st = capi.lib().mom5gpu_mdfl_sweby_noalloc(
+            C.byref(dims), scheme, dt, *[C.c_void_p(f[k].data_ptr()) for k in (
+                "tmask", "dat", "datr", "dxte", "dyte", "dxtn", "dytn", "uhrho_et", "vhrho_nt", "wrho_bt", "rho_dzt")],
+            C.c_void_p(T.data_ptr()), C.c_void_p(th.data_ptr()), None)
+        assert st == capi.OK, capi.lib().mom5gpu_last_error(None)
+        torch.cuda.synchronize()
+        got = th.cpu().numpy()
+        assert np.all(got == ref[n - 1]), f"tracer {n}: {np.abs(got - ref[n - 1]).max()}"
+
+
+def test_noalloc_rejects_oversized_domain(gpu_lib):
+    capi = gpu_lib
+    dims = capi.Dims(1440, 1080, 50, 1, 0, 1, capi.BGRID)
+    dummy = C.c_void_p(16)  # never dereferenced: the size check comes first
+    st = capi.lib().mom5gpu_mdfl_sweby_noalloc(C.byref(dims), 9, 600.0, *([dummy] * 13), None)
+    assert st == capi.EINVAL
+    msg = capi.lib().mom5gpu_last_error(None).decode()
+    assert "at most 2097152" in msg
