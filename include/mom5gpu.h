@@ -230,6 +230,43 @@ int mom5gpu_timing_query(mom5gpu_domain* d, const char* section, double* total_m
 /* Number of kernels this domain has launched since creation. */
 long mom5gpu_launch_count(const mom5gpu_domain* d);
 
+/* ---- batching: many resident domains per launch ---------------------------
+ * A batch groups resident domains so that one step of many domains costs a
+ * handful of launches instead of a handful per domain: the FP64 advection
+ * passes and each barotropic subcycle phase run as one launch over a work list
+ * of (domain, block) items, and the precision form runs as one persistent
+ * launch that drains a (domain, tile) queue.  Domains of a batch share the
+ * precision, the tracer count (<= 8 in FP64, <= 10 in the precision form),
+ * MDFL Sweby for every tracer, the B grid, and nts (mom5gpu_barotropic_init);
+ * sizes may differ.  A batch borrows the domains: destroy it before them. */
+typedef struct mom5gpu_batch mom5gpu_batch;
+int mom5gpu_batch_create(mom5gpu_domain* const* domains, int ndomains, mom5gpu_batch** out);
+void mom5gpu_batch_destroy(mom5gpu_batch* b);
+const char* mom5gpu_batch_last_error(const mom5gpu_batch* b);
+int mom5gpu_batch_set_stream(mom5gpu_batch* b, void* stream);
+/* One baroclinic step -- MDFL advection of every tracer with the explicit
+ * update, then update_ocean_barotropic -- of the domains index[0..count-1]
+ * (positions in the batch), each at its own two-level time state: parity[i] = 0
+ * steps tau = 1 -> taup1 = 2, 1 steps 2 -> 1 (taum1 = tau).  With count = -1
+ * every domain is stepped with parity[0], from a CUDA graph captured on the
+ * first such call for that parity and replayed afterwards. */
+int mom5gpu_batch_step(mom5gpu_batch* b, const int* index, const int* parity, int count, double dtime);
+/* Time the candidate launch shapes (precision-form tile height and resident
+ * blocks per SM; FP64 y-pass rows per thread) on the whole batch and keep the
+ * fastest.  Each trial is a parity-0 step: time level 1 is read, level 2 is
+ * overwritten.  A summary is written to report (may be NULL). */
+int mom5gpu_batch_autotune(mom5gpu_batch* b, double dtime, char* report, size_t report_len);
+/* Read or set the launch shape directly (e.g. to reuse one autotune result on
+ * several batches): rows = precision-form tile height (16 or 32), tj = FP64
+ * y-pass rows per thread (0 = automatic, else 2, 4, 8 or 16), blocks_per_sm =
+ * resident blocks per SM of the persistent launch (1..4). */
+int mom5gpu_batch_get_tuning(const mom5gpu_batch* b, int* rows, int* tj, int* blocks_per_sm);
+int mom5gpu_batch_set_tuning(mom5gpu_batch* b, int rows, int tj, int blocks_per_sm);
+/* Device milliseconds of the last batch step (CUDA events on the batch stream). */
+double mom5gpu_batch_last_ms(mom5gpu_batch* b);
+/* Kernels launched by the batch since creation (graph replays count their kernels). */
+long mom5gpu_batch_launch_count(const mom5gpu_batch* b);
+
 /* ---- allocation-free variant ---------------------------------------------
  * No counterpart in the reference.  For callers that cannot let the library
  * allocate device memory (a model whose GPU memory is reserved by its own pool,

@@ -114,6 +114,16 @@ def lib() -> C.CDLL:
             "mom5gpu_timing_query": (C.c_int, [vp, C.c_char_p, dp, C.POINTER(C.c_long)]),
             "mom5gpu_launch_count": (C.c_long, [vp]),
             "mom5gpu_mdfl_sweby_noalloc": (C.c_int, [C.POINTER(Dims), C.c_int, C.c_double] + [vp] * 14),
+            "mom5gpu_batch_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+            "mom5gpu_batch_destroy": (None, [vp]),
+            "mom5gpu_batch_last_error": (C.c_char_p, [vp]),
+            "mom5gpu_batch_set_stream": (C.c_int, [vp, vp]),
+            "mom5gpu_batch_step": (C.c_int, [vp, ip, ip, C.c_int, C.c_double]),
+            "mom5gpu_batch_autotune": (C.c_int, [vp, C.c_double, C.c_char_p, C.c_size_t]),
+            "mom5gpu_batch_get_tuning": (C.c_int, [vp, ip, ip, ip]),
+            "mom5gpu_batch_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+            "mom5gpu_batch_last_ms": (C.c_double, [vp]),
+            "mom5gpu_batch_launch_count": (C.c_long, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -278,6 +288,71 @@ class Domain:
         out = C.c_int()
         self.check(lib().mom5gpu_check_finite(self.h, n, level, C.byref(out)))
         return out.value == 0
+
+
+class Batch:
+    """A mom5gpu_batch over resident domains (they must outlive the batch)."""
+
+    def __init__(self, domains):
+        self.domains = list(domains)
+        arr = (C.c_void_p * len(self.domains))(*[d.h.value for d in self.domains])
+        h = C.c_void_p()
+        st = lib().mom5gpu_batch_create(arr, len(self.domains), C.byref(h))
+        if st != OK:
+            raise Mom5GpuError(st, lib().mom5gpu_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mom5gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st):
+        if st != OK:
+            raise Mom5GpuError(st, lib().mom5gpu_batch_last_error(self.h).decode())
+
+    def step(self, dtime, index=None, parity=None):
+        """Step the listed domains (all with parity[0] through the CUDA graph when index is None)."""
+        if index is None:
+            p = (C.c_int * 1)(int(parity if parity is not None else 0))
+            self.check(lib().mom5gpu_batch_step(self.h, None, p, -1, float(dtime)))
+            return
+        n = len(index)
+        ia = (C.c_int * n)(*index)
+        pa = (C.c_int * n)(*parity)
+        self.check(lib().mom5gpu_batch_step(self.h, ia, pa, n, float(dtime)))
+
+    def autotune(self, dtime) -> str:
+        buf = C.create_string_buffer(1024)
+        self.check(lib().mom5gpu_batch_autotune(self.h, float(dtime), buf, 1024))
+        return buf.value.decode()
+
+    def set_stream(self, stream_ptr: int):
+        self.check(lib().mom5gpu_batch_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    @property
+    def tuning(self):
+        r, t, b = C.c_int(), C.c_int(), C.c_int()
+        self.check(lib().mom5gpu_batch_get_tuning(self.h, C.byref(r), C.byref(t), C.byref(b)))
+        return (r.value, t.value, b.value)
+
+    @tuning.setter
+    def tuning(self, v):
+        self.check(lib().mom5gpu_batch_set_tuning(self.h, int(v[0]), int(v[1]), int(v[2])))
+
+    @property
+    def last_ms(self) -> float:
+        return lib().mom5gpu_batch_last_ms(self.h)
+
+    @property
+    def launches(self) -> int:
+        return lib().mom5gpu_batch_launch_count(self.h)
 
 
 def header_symbols():

@@ -1,0 +1,525 @@
+// FP64 MDFL Sweby and barotropic kernel bodies, shared by the one-domain
+// kernels (k_fp64.cu) and the batched kernels (k_batch64.cu).  Included only by
+// translation units built with --fmad=false: every product and sum is rounded
+// on its own, in the reference's order (see k_fp64.cu).
+#pragma once
+#include <math.h>
+
+#include "internal.h"
+
+namespace mom5 {
+namespace fp64 {
+
+#define DEVI __device__ __forceinline__
+
+DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
+DEVI long I3(const Geo& g, int i, int j, int k) { return (long)k * g.n2 + (long)j * g.nxd + i; }
+// index into a (ni+4)(nj+4)nk halo-2 array; i, j in data-domain coordinates (isc = 1)
+DEVI long IM(const Geo& g, int i, int j, int k) { return ((long)k * (g.nj + 4) + (j + 1)) * (g.ni + 4) + (i + 1); }
+
+constexpr double kOneSixth = 1.0 / 6.0;  // ocean_parameters.F90:92
+
+// max(0, x) and min(a, b) on the integer pipe (ordered-integer comparison of
+// the bit patterns; equal to the FP comparison for all non-NaN operands).
+DEVI long long ordbits(double x) {
+  long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+DEVI double dmin(double a, double b) { return ordbits(a) <= ordbits(b) ? a : b; }
+DEVI double dmax0(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
+DEVI bool dpos(double x) { return __double_as_longlong(x) > 0; }   // x > 0
+
+// Sweby limiter psi (ocean_tracer_advect.F90:3868-3878).  With the limiter on
+// the reference forms psi*(1-1) + max(...)*1, with it off psi*1 + max(...)*0;
+// for finite psi both reduce to the selected term exactly.
+template <bool SWEBY>
+DEVI double limiter(double theta, double d0, double d1, double c) {
+  double lin = d0 + d1 * theta;
+  if (!SWEBY) return lin;
+  double a = dmin(1.0, lin);
+  return dmax0(dmin(a, c * theta));
+}
+
+// Flux of one face given the upwind-side data.  Reference form
+// 0.5*((mf+|mf|)*(Tup + psiP*Rj) + (mf-|mf|)*(Tdn - psiM*Rj)): for mf > 0 the
+// second product is an exact zero and 0.5*(2mf*X) == mf*X exactly.
+template <bool SWEBY>
+DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, double Tm, double d0, double d1,
+                      double c) {
+  long long b = __double_as_longlong(mf);
+  if (b > 0) {  // mf > 0: upwind value Tp on the minus side, ratio Rjm / Rj
+    double theta = Rjm / (1.0e-30 + Rj);
+    double psi = limiter<SWEBY>(theta, d0, d1, c);
+    return mf * (Tp + psi * Rj);
+  } else if (b < 0 && b != (long long)0x8000000000000000ULL) {  // mf < 0
+    double theta = Rjp / (1.0e-30 + Rj);
+    double psi = limiter<SWEBY>(theta, d0, d1, c);
+    return mf * (Tm - psi * Rj);
+  }
+  return 0.0;
+}
+
+// z pass: one thread per column, march down k.
+template <bool ALL, bool SWEBY, int MAXN>
+DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x + 1;
+  int j = by + 1;
+  if (i > g.ni) return;
+  double ftp[MAXN];
+#pragma unroll
+  for (int n = 0; n < MAXN; ++n) ftp[n] = 0.0;
+  double wkm1 = 0.0;
+  const double dat = a.dat[I2(g, i, j)];
+  const double datr = a.datr[I2(g, i, j)];
+  for (int k = 0; k < g.nk; ++k) {
+    int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
+    int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
+    int km1 = k > 0 ? k - 1 : 0;
+    bool mkm1 = a.mask2[IM(g, i, j, km1)], mk = a.mask2[IM(g, i, j, k)];
+    bool mkp1 = a.mask2[IM(g, i, j, kp1)], mkp2 = a.mask2[IM(g, i, j, kp2)];
+    double wk = a.w[I3(g, i, j, k + 1)];
+    double rdz = a.rdz[I3(g, i, j, k)];
+    double massflux = dat * wk;
+    double cfl = fabs(wk * a.dtime / rdz);
+    double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
+    double d1 = (1.0 - cfl * cfl) * kOneSixth;
+    double c = (1.0 - cfl) / (1.0e-30 + cfl);
+    double dtr = ALL ? 0.0 : a.dtime / rdz;
+    double wdiff = wkm1 - wk;
+    bool fm = mkp1 && mk;
+    long p = I3(g, i, j, k);
+#pragma unroll
+    for (int n = 0; n < MAXN; ++n) {
+      if (n < a.ntr) {
+        const double* T = a.T + n * a.tstride;
+        double Tk = T[p];
+        double Tkm1 = T[I3(g, i, j, km1)], Tkp1 = T[I3(g, i, j, kp1)], Tkp2 = T[I3(g, i, j, kp2)];
+        double Rjp = (mkm1 && mk) ? Tkm1 - Tk : 0.0;
+        double Rj = (mk && mkp1) ? Tk - Tkp1 : 0.0;
+        double Rjm = (mkp1 && mkp2) ? Tkp1 - Tkp2 : 0.0;
+        double fbt = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, Tkp1, Tk, d0, d1, c) : 0.0;
+        double tm;
+        if (!ALL) {
+          tm = Tk + dtr * (datr * (fbt - ftp[n]) + Tk * wdiff);
+        } else {
+          double w1 = datr * (fbt - ftp[n]) + Tk * wdiff;
+          tm = Tk + w1 * a.dtime / rdz;
+        }
+        a.tz[n * g.n3 + p] = tm;
+        ftp[n] = fbt;
+      }
+    }
+    wkm1 = wk;
+  }
+}
+
+// tracer_mdfl after the x halo update (XUPDATE): compute rows only.
+DEVI double tm_xhalo(const Geo& g, const double* a, int i, int j, int k) {
+  if (i < 1) {
+    if (!g.cx) return 0.0;
+    i += g.ni;
+  } else if (i > g.ni) {
+    if (!g.cx) return 0.0;
+    i -= g.ni;
+  }
+  return a[I3(g, i, j, k)];
+}
+DEVI double tm_yhalo(const Geo& g, const double* a, int i, int j, int k) {
+  if (j < 1) {
+    if (!g.cy) return 0.0;
+    j += g.nj;
+  } else if (j > g.nj) {
+    if (!g.cy) return 0.0;
+    j -= g.nj;
+  }
+  return a[I3(g, i, j, k)];
+}
+
+constexpr int kTX = 128;
+
+// x-face i of row (j,k): fluxes of every tracer into sm[n][slot].
+template <bool SWEBY, int MAXN>
+DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], int slot) {
+  const Geo& g = a.g;
+  bool m0 = a.mask2[IM(g, i - 1, j, k)], m1 = a.mask2[IM(g, i, j, k)];
+  bool m2 = a.mask2[IM(g, i + 1, j, k)], m3 = a.mask2[IM(g, i + 2, j, k)];
+  double u = a.uh[I3(g, i, j, k)];
+  double massflux = a.dyte[I2(g, i, j)] * u;
+  double cfl = fabs(u * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
+  double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
+  double d1 = (1.0 - cfl * cfl) * kOneSixth;
+  double c = (1.0 - cfl) / (1.0e-30 + cfl);
+  bool fm = m1 && m2;
+#pragma unroll
+  for (int n = 0; n < MAXN; ++n) {
+    if (n < a.ntr) {
+      const double* tz = a.tz + n * g.n3;
+      double tA = tm_xhalo(g, tz, i - 1, j, k), tB = tm_xhalo(g, tz, i, j, k);
+      double tC = tm_xhalo(g, tz, i + 1, j, k), tD = tm_xhalo(g, tz, i + 2, j, k);
+      double Rjp = (m3 && m2) ? tD - tC : 0.0;
+      double Rj = (m2 && m1) ? tC - tB : 0.0;
+      double Rjm = (m1 && m0) ? tB - tA : 0.0;
+      sm[n][slot] = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
+    }
+  }
+}
+
+template <bool ALL, bool SWEBY, int MAXN>
+DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
+  __shared__ double sm[MAXN][kTX + 1];
+  const Geo& g = a.g;
+  int i0 = bx * kTX + 1;
+  int j = by + 1;
+  int k = bz;
+  int t = threadIdx.x;
+  int i = i0 + t;
+  if (i <= g.ni) x_face<SWEBY, MAXN>(a, i, j, k, sm, t + 1);
+  if (t == 0) x_face<SWEBY, MAXN>(a, i0 - 1, j, k, sm, 0);
+  __syncthreads();
+  if (i > g.ni) return;
+  bool mk = a.mask2[IM(g, i, j, k)];
+  double datr = a.datr[I2(g, i, j)];
+  double rdz = a.rdz[I3(g, i, j, k)];
+  double divx = a.dyte[I2(g, i, j)] * a.uh[I3(g, i, j, k)] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
+  // dtime*tmask*datr/rho_dzt (:3960-3961); tmask_mdfl*datr (:4277)
+  double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
+  long p = I3(g, i, j, k);
+#pragma unroll
+  for (int n = 0; n < MAXN; ++n) {
+    if (n < a.ntr) {
+      double Tk = a.T[n * a.tstride + p];
+      double tm = a.tz[n * g.n3 + p];
+      double s = (sm[n][t] - sm[n][t + 1]) + Tk * divx;
+      if (!ALL) {
+        tm = tm + coef * s;
+      } else {
+        double w1 = mk ? datr * s : 0.0;
+        tm = tm + w1 * a.dtime / rdz;
+      }
+      a.tx[n * g.n3 + p] = tm;
+    }
+  }
+}
+
+// y pass + closing divergence correction + tendency: one thread per (i,k) and a
+// strip of TJ rows, marching north; th_tendency += result.
+template <bool SWEBY, int MAXN>
+DEVI void y_face(const MdflArgs& a, int i, int j, int k, double* f) {
+  const Geo& g = a.g;
+  bool m0 = a.mask2[IM(g, i, j - 1, k)], m1 = a.mask2[IM(g, i, j, k)];
+  bool m2 = a.mask2[IM(g, i, j + 1, k)], m3 = a.mask2[IM(g, i, j + 2, k)];
+  double v = a.vh[I3(g, i, j, k)];
+  double massflux = a.dxtn[I2(g, i, j)] * v;
+  double cfl = fabs(v * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
+  double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
+  double d1 = (1.0 - cfl * cfl) * kOneSixth;
+  double c = (1.0 - cfl) / (1.0e-30 + cfl);
+  bool fm = m1 && m2;
+#pragma unroll
+  for (int n = 0; n < MAXN; ++n) {
+    if (n < a.ntr) {
+      const double* tx = a.tx + n * g.n3;
+      double tA = tm_yhalo(g, tx, i, j - 1, k), tB = tm_yhalo(g, tx, i, j, k);
+      double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
+      double Rjp = (m3 && m2) ? tD - tC : 0.0;
+      double Rj = (m2 && m1) ? tC - tB : 0.0;
+      double Rjm = (m1 && m0) ? tB - tA : 0.0;
+      f[n] = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
+    }
+  }
+}
+
+template <bool ALL, bool SWEBY, int MAXN>
+DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x + 1;
+  int j0 = by * TJ + 1;
+  int k = bz;
+  if (i > g.ni) return;
+  int j1 = j0 + TJ - 1;
+  if (j1 > g.nj) j1 = g.nj;
+  double fprev[MAXN], fcur[MAXN];
+  y_face<SWEBY, MAXN>(a, i, j0 - 1, k, fprev);
+  for (int j = j0; j <= j1; ++j) {
+    y_face<SWEBY, MAXN>(a, i, j, k, fcur);
+    long p = I3(g, i, j, k);
+    bool mk = a.mask2[IM(g, i, j, k)];
+    double datr = a.datr[I2(g, i, j)];
+    double rdz = a.rdz[p];
+    double wk = a.w[I3(g, i, j, k + 1)];
+    double wkm1j = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;  // bottom face of level k-1; 0 at the surface
+    double corr = (wk - wkm1j) + datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] -
+                                         a.dyte[I2(g, i, j)] * a.uh[p]);
+    double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
+#pragma unroll
+    for (int n = 0; n < MAXN; ++n) {
+      if (n < a.ntr) {
+        double Tk = a.T[n * a.tstride + p];
+        double tm = a.tx[n * g.n3 + p];
+        double out;
+        if (!ALL) {
+          tm = tm + coef * (fprev[n] - fcur[n]);
+          tm = tm + a.dtime * Tk / rdz * corr;
+          out = mk ? rdz * (tm - Tk) / a.dtime : 0.0;
+        } else {
+          double w1 = (mk ? datr * (fprev[n] - fcur[n]) : 0.0) + Tk * corr;
+          tm = tm + w1 * a.dtime / rdz;
+          out = mk ? rdz * (tm - Tk) / a.dtime : 0.0;
+        }
+        double* th = a.th + n * g.n3;
+        th[p] = th[p] + out;
+        fprev[n] = fcur[n];
+      }
+    }
+  }
+}
+
+
+
+// DIV_UD at (i,j) (ocean_operators.F90:507-608), halo_in = halo_out = 1.
+DEVI double div_ud(const BtArgs& a, const double* u, const double* v, int i, int j) {
+  const Geo& g = a.g;
+  if (i < 1 || j < 1) return 0.0;
+  if (a.cgrid) {
+    double uhim = u[I2(g, i - 1, j)] * a.dat[I2(g, i - 1, j)] * a.dxter[I2(g, i - 1, j)];
+    double vhjm = v[I2(g, i, j - 1)] * a.dat[I2(g, i, j - 1)] * a.dytnr[I2(g, i, j - 1)];
+    double uh = u[I2(g, i, j)] * a.dat[I2(g, i, j)] * a.dxter[I2(g, i, j)];
+    double vh = v[I2(g, i, j)] * a.dat[I2(g, i, j)] * a.dytnr[I2(g, i, j)];
+    return ((uh - uhim) + (vh - vhjm)) * a.datr[I2(g, i, j)];
+  }
+  double uh = u[I2(g, i, j)] * a.dyu[I2(g, i, j)];
+  double vh = v[I2(g, i, j)] * a.dxu[I2(g, i, j)];
+  double uhjm = u[I2(g, i, j - 1)] * a.dyu[I2(g, i, j - 1)];
+  double vhjm = v[I2(g, i, j - 1)] * a.dxu[I2(g, i, j - 1)];
+  double uhim = u[I2(g, i - 1, j)] * a.dyu[I2(g, i - 1, j)];
+  double vhim = v[I2(g, i - 1, j)] * a.dxu[I2(g, i - 1, j)];
+  double uhimjm = u[I2(g, i - 1, j - 1)] * a.dyu[I2(g, i - 1, j - 1)];
+  double vhimjm = v[I2(g, i - 1, j - 1)] * a.dxu[I2(g, i - 1, j - 1)];
+  double uh_bay = 0.5 * (uh + uhjm);
+  double vh_bax = 0.5 * (vh + vhim);
+  double uhim_bay = 0.5 * (uhim + uhimjm);
+  double vhjm_bax = 0.5 * (vhjm + vhimjm);
+  return ((uh_bay - uhim_bay) + (vh_bax - vhjm_bax)) * a.datr[I2(g, i, j)];
+}
+
+// image of a halo point under the single-PE full halo update; returns false
+// when the point is left untouched (non-cyclic wall, or a corner of a domain
+// cyclic in one direction only).
+DEVI bool halo_image(const Geo& g, int& i, int& j) {
+  bool hx = (i == 0 || i == g.ni + 1), hy = (j == 0 || j == g.nj + 1);
+  if (!hx && !hy) return true;
+  if (hx && hy) {
+    if (!(g.cx && g.cy)) return false;
+  } else if (hx && !g.cx) {
+    return false;
+  } else if (hy && !g.cy) {
+    return false;
+  }
+  if (i == 0) i = g.ni;
+  else if (i == g.ni + 1) i = 1;
+  if (j == 0) j = g.nj;
+  else if (j == g.nj + 1) j = 1;
+  return true;
+}
+
+DEVI void bt_init_body(BtArgs a, const double* eta_bar_tau, const double* eta_tau, const double* ud_tau,
+                          const double* vd_tau, const double* pme, const double* river, const double* source,
+                          const double* eta_smooth, int initsum_with_bar, int bx, int by) {
+  long q = bx * (long)blockDim.x + threadIdx.x;
+  if (q >= a.g.n2) return;
+  a.eta_bar[q] = initsum_with_bar ? eta_bar_tau[q] : eta_tau[q];
+  a.udrho_u[q] = 0.0;
+  a.udrho_v[q] = 0.0;
+  // fstau = mod(1,2)+1 = 2 -> plane 1
+  a.eta_bt[a.g.n2 + q] = eta_bar_tau[q];
+  a.ubt[a.g.n2 + q] = ud_tau[q];
+  a.vbt[a.g.n2 + q] = vd_tau[q];
+  a.steady[q] = a.tmask1[q] * (pme[q] + river[q] + source[q] - eta_smooth[q]);
+}
+
+// C-grid: initial Adams-Bashforth Coriolis history (:3707-3730)
+DEVI void bt_cgrid_init_body(BtArgs a, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x + 1;
+  int j = by + 1;
+  if (i > g.ni) return;
+  const double abm0 = 23.0 / 12.0, abm1 = -16.0 / 12.0, abm2 = 5.0 / 12.0;
+  const int itime = 1;
+  int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
+  const double* u = a.ubt + g.n2;
+  const double* v = a.vbt + g.n2;
+  long n2 = g.n2;
+  long q = I2(g, i, j);
+  double c0 = 0.25 * (a.f[q] * (v[q] + v[I2(g, i + 1, j)]) + a.f[I2(g, i, j - 1)] * (v[I2(g, i, j - 1)] + v[I2(g, i + 1, j - 1)]));
+  a.cf[(m0 * 2 + 0) * n2 + q] = c0;
+  a.cf[(m1 * 2 + 0) * n2 + q] = c0;
+  a.cf[(m2 * 2 + 0) * n2 + q] = c0;
+  a.ca[q] = abm0 * c0 + abm1 * c0 + abm2 * c0;
+  double c1 = -0.25 * (a.f[q] * (u[q] + u[I2(g, i, j + 1)]) + a.f[I2(g, i - 1, j)] * (u[I2(g, i - 1, j)] + u[I2(g, i - 1, j + 1)]));
+  a.cf[(m0 * 2 + 1) * n2 + q] = c1;
+  a.cf[(m1 * 2 + 1) * n2 + q] = c1;
+  a.cf[(m2 * 2 + 1) * n2 + q] = c1;
+  a.ca[n2 + q] = abm0 * c1 + abm1 * c1 + abm2 * c1;
+}
+
+// predictor + ps (both grids)
+DEVI void bt_pred_body(BtArgs a, int so, int sn, int bx, int by) {
+  const Geo& g = a.g;
+  int i0 = bx * blockDim.x + threadIdx.x;
+  int j0 = by;
+  if (i0 > g.ni + 1) return;
+  int i = i0, j = j0;
+  // B-grid legacy halos: eta(fstaup1) is halo-updated right after the predictor,
+  // so a halo point takes the value computed at its periodic image.
+  if (!a.cgrid) {
+    if (!halo_image(g, i, j)) {
+      i = i0;
+      j = j0;
+    }
+  }
+  const double* eo = a.eta_bt + so * g.n2;
+  long q = I2(g, i, j);
+  double en;
+  if (a.gamma > 0.0) {
+    double dv = div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j);
+    double tmp = a.tmask1[q] != 0.0 ? (-dv) * a.tmask1[q] : 0.0;
+    en = eo[q] + a.dtbt_gamma_rho0r * (tmp + a.steady[q]);
+  } else {
+    en = eo[q];
+  }
+  long q0 = I2(g, i0, j0);
+  a.eta_bt[sn * g.n2 + q0] = en;
+  a.ps[q0] = a.rho_g[q0] * en + a.patm[q0];
+}
+
+// momentum update, B grid (:3466-3485)
+DEVI void bt_mom_b_body(BtArgs a, int so, int sn, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x;
+  int j = by;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double gx = 0.0, gy = 0.0;
+  if (i <= g.ni && j <= g.nj) {
+    const double* ps = a.ps;
+    double p_fay = 0.5 * (ps[q] + ps[I2(g, i, j + 1)]);
+    double p_fax = 0.5 * (ps[q] + ps[I2(g, i + 1, j)]);
+    double pip_fay = 0.5 * (ps[I2(g, i + 1, j)] + ps[I2(g, i + 1, j + 1)]);
+    double pjp_fax = 0.5 * (ps[I2(g, i, j + 1)] + ps[I2(g, i + 1, j + 1)]);
+    bool um = a.umask1[q] != 0.0;
+    gx = um ? (pip_fay - p_fay) * a.dxur[q] * a.umask1[q] : 0.0;
+    gy = um ? (pjp_fax - p_fax) * a.dyur[q] * a.umask1[q] : 0.0;
+  }
+  double pf1 = -a.thicku[q] * gx;
+  double pf2 = -a.thicku[q] * gy;
+  double uo = a.ubt[so * g.n2 + q], vo = a.vbt[so * g.n2 + q];
+  double f = a.f[q];
+  double t1 = uo + a.dtbt * (0.5 * f * vo + pf1 + a.forcing_u[q] + 0.0);
+  double t2 = vo + a.dtbt * (-0.5 * f * uo + pf2 + a.forcing_v[q] + 0.0);
+  a.ubt[sn * g.n2 + q] = a.cori2[q] * (t1 + a.cori1[q] * t2);
+  a.vbt[sn * g.n2 + q] = a.cori2[q] * (t2 - a.cori1[q] * t1);
+}
+
+// C grid: Coriolis (compute domain) + gradient + momentum (:3780-3830)
+DEVI void bt_mom_c_body(BtArgs a, int so, int sn, int itime, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x;
+  int j = by;
+  if (i > g.ni + 1) return;
+  long n2 = g.n2;
+  long q = I2(g, i, j);
+  const double abm0 = 23.0 / 12.0, abm1 = -16.0 / 12.0, abm2 = 5.0 / 12.0;
+  int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
+  double ca0 = 0.0, ca1 = 0.0;
+  if (i >= 1 && i <= g.ni && j >= 1 && j <= g.nj) {
+    const double* u = a.ubt + so * n2;
+    const double* v = a.vbt + so * n2;
+    double c0 = 0.25 * (a.f[q] * (v[q] + v[I2(g, i + 1, j)]) + a.f[I2(g, i, j - 1)] * (v[I2(g, i, j - 1)] + v[I2(g, i + 1, j - 1)]));
+    a.cf[(m0 * 2 + 0) * n2 + q] = c0;
+    ca0 = abm0 * c0 + abm1 * a.cf[(m1 * 2 + 0) * n2 + q] + abm2 * a.cf[(m2 * 2 + 0) * n2 + q];
+    double c1 = -0.25 * (a.f[q] * (u[q] + u[I2(g, i, j + 1)]) + a.f[I2(g, i - 1, j)] * (u[I2(g, i - 1, j)] + u[I2(g, i - 1, j + 1)]));
+    a.cf[(m0 * 2 + 1) * n2 + q] = c1;
+    ca1 = abm0 * c1 + abm1 * a.cf[(m1 * 2 + 1) * n2 + q] + abm2 * a.cf[(m2 * 2 + 1) * n2 + q];
+  }
+  double gx = 0.0, gy = 0.0;
+  if (i <= g.ni && j <= g.nj) {
+    gx = (a.ps[I2(g, i + 1, j)] - a.ps[q]) * a.dxter[q] * a.tmen_e[q];
+    gy = (a.ps[I2(g, i, j + 1)] - a.ps[q]) * a.dytnr[q] * a.tmen_n[q];
+  }
+  double pf1 = -a.thicken_e[q] * gx;
+  double pf2 = -a.thicken_n[q] * gy;
+  double uo = a.ubt[so * n2 + q], vo = a.vbt[so * n2 + q];
+  a.ubt[sn * n2 + q] = uo + a.dtbt * a.tmen_e[q] * (ca0 + pf1 + a.forcing_u[q] + 0.0);
+  a.vbt[sn * n2 + q] = vo + a.dtbt * a.tmen_n[q] * (ca1 + pf2 + a.forcing_v[q] + 0.0);
+}
+
+// corrector + accumulation
+DEVI void bt_corr_body(BtArgs a, int so, int sn, double wgt, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x;
+  int j = by;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double dv = div_ud(a, a.ubt + sn * g.n2, a.vbt + sn * g.n2, i, j);
+  double tmp = a.tmask1[q] != 0.0 ? (-dv) * a.tmask1[q] : 0.0;
+  double en = a.eta_bt[so * g.n2 + q] + a.dtbt_rho0r * (tmp + a.steady[q]);
+  a.eta_bt[sn * g.n2 + q] = en;
+  a.eta_bar[q] = a.eta_bar[q] + en;
+  double un = a.ubt[sn * g.n2 + q], vn = a.vbt[sn * g.n2 + q];
+  if (a.stepB) {
+    a.udrho_u[q] = a.udrho_u[q] + wgt * un;
+    a.udrho_v[q] = a.udrho_v[q] + wgt * vn;
+  } else {
+    a.udrho_u[q] = a.udrho_u[q] + un;
+    a.udrho_v[q] = a.udrho_v[q] + vn;
+  }
+}
+
+DEVI void bt_post2_body(BtArgs a, double* conv, double* eta_u, double* ps_out, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x;
+  int j = by;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  conv[q] = -div_ud(a, a.udrho_u, a.udrho_v, i, j);
+  double r = 0.0;
+  if (i <= g.ni && j <= g.nj) {
+    const double* e = a.eta_bar;
+    r = (e[q] * a.dte[q] * a.dus[q] + e[I2(g, i + 1, j)] * a.dtw[I2(g, i + 1, j)] * a.dus[q] +
+         e[I2(g, i, j + 1)] * a.dte[I2(g, i, j + 1)] * a.dun[q] +
+         e[I2(g, i + 1, j + 1)] * a.dtw[I2(g, i + 1, j + 1)] * a.dun[q]) *
+        a.daur[q];
+  }
+  eta_u[q] = a.umask1[q] != 0.0 ? a.umask1[q] * r : 0.0;
+  ps_out[q] = a.rho_g[q] * a.eta_bar[q] + a.patm[q];
+}
+
+DEVI void bt_post3_body(BtArgs a, const double* ps, double* gxo, double* gyo, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x;
+  int j = by;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double gx = 0.0, gy = 0.0;
+  if (i <= g.ni && j <= g.nj) {
+    if (!a.cgrid) {
+      double p_fay = 0.5 * (ps[q] + ps[I2(g, i, j + 1)]);
+      double p_fax = 0.5 * (ps[q] + ps[I2(g, i + 1, j)]);
+      double pip_fay = 0.5 * (ps[I2(g, i + 1, j)] + ps[I2(g, i + 1, j + 1)]);
+      double pjp_fax = 0.5 * (ps[I2(g, i, j + 1)] + ps[I2(g, i + 1, j + 1)]);
+      bool um = a.umask1[q] != 0.0;
+      gx = um ? (pip_fay - p_fay) * a.dxur[q] * a.umask1[q] : 0.0;
+      gy = um ? (pjp_fax - p_fax) * a.dyur[q] * a.umask1[q] : 0.0;
+    } else {
+      gx = (ps[I2(g, i + 1, j)] - ps[q]) * a.dxter[q] * a.tmen_e[q];
+      gy = (ps[I2(g, i, j + 1)] - ps[q]) * a.dytnr[q] * a.tmen_n[q];
+    }
+  }
+  gxo[q] = gx;
+  gyo[q] = gy;
+}
+
+
+}  // namespace fp64
+}  // namespace mom5

@@ -98,6 +98,9 @@ struct mom5gpu_domain {
   double clock_ms[8] = {0};
   long clock_calls[8] = {0};
   long launches = 0;
+  // autotuned launch shapes (0 = built-in heuristic)
+  int tune_mixed_rows = 32;  // precision-form tile height incl. halo: 32 or 16
+  int tune_y_tj = 0;         // FP64 y-pass rows per thread
 };
 
 namespace mom5 {
@@ -134,7 +137,62 @@ struct MdflArgs {
   double* tz;                 // after z, tracer n at tz + n*g.n3
   double* tx;                 // after x
   double* th;                 // th_tendency of tracer 0, tracer n at th + n*g.n3
+  int tj = 0;                 // y-pass rows per thread (0 = choose from the domain size)
 };
+
+
+// Arguments of the barotropic kernels (fp64_bodies.cuh) for one domain and one
+// (tau, taup1) pair, and the step's other inputs and outputs.
+struct BtArgs {
+  Geo g;
+  int cgrid, nts, stepB;
+  double dtbt, dtbt_gamma_rho0r, dtbt_rho0r, gamma;
+  const double *tmask1, *umask1, *f, *dxu, *dyu, *dxur, *dyur, *dat, *datr, *dxter, *dytnr, *tmen_e, *tmen_n;
+  const double *dte, *dtw, *dus, *dun, *daur;
+  const double *patm, *thicku, *thicken_e, *thicken_n, *forcing_u, *forcing_v, *rho_g, *cori1, *cori2;
+  double* eta_bt;  // 2 levels
+  double* ubt;     // 2 levels
+  double* vbt;     // 2 levels
+  double* steady;
+  double* ps;
+  double* cf;  // coriolis_force_bt, 6 planes (component-major within AB level)
+  double* ca;  // coriolis_accel_bt, 2 planes
+  double *eta_bar, *udrho_u, *udrho_v;  // taup1 accumulators
+};
+struct BtExtra {
+  const double *eta_bar_tau, *eta_tau, *ud_tau, *vd_tau, *pme, *river, *source, *eta_smooth;
+  double *conv, *eta_u, *ps_out, *gxo, *gyo;
+  int initsum_with_bar;
+};
+
+// Arguments of the precision-form kernel (mixed_body.cuh).
+struct MixArgs {
+  Geo g;
+  int ntr;
+  float dtime;
+  const uint8_t* mask2;
+  const double *dat, *datr, *dxte, *dyte, *dxtn, *dytn, *uh, *vh, *w;
+  const double *rdz, *rdz_m1, *rdzr;  // rho_dzt(tau), rho_dzt(taum1), rho_dztr
+  const double* T;                    // tracer 0 at taum1 (tracer n at + n*g.n3)
+  double* out;                        // fused: T(taup1); else th_tendency (tracer n at + n*g.n3)
+  int fused;
+};
+
+// Arguments of the FP64 explicit update.
+struct UpdArgs {
+  Geo g;
+  int ntr;
+  long tstride;
+  const double *rdz_m1, *rdzr, *Tm1, *th;
+  double* Tp1;
+  double dtime;
+};
+
+// argument builders (k_fp64.cu, k_mixed.cu); status codes as the C ABI
+int make_mdfl_args(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, double dtime, MdflArgs* a);
+int make_upd_args(mom5gpu_domain* d, int taum1, int taup1, double dtime, UpdArgs* u);
+int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* a, BtExtra* x);
+int make_mix_args(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime, MixArgs* a);
 
 // ---- FP64 kernels (k_fp64.cu) ----
 // the three MDFL passes on the stream, for the tracers described by a
@@ -156,6 +214,38 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);
 int launch_content(mom5gpu_domain* d, int n, int level, double* out_host);
 int launch_eta_integral(mom5gpu_domain* d, const double* eta, double* out_host);
 int launch_check_finite(mom5gpu_domain* d, const double* a, size_t count, int* out_host);
+
+// FP64 MDFL scratch of a domain, for ntr tracers at a time (k_fp64.cu)
+int ensure_mdfl_scratch(mom5gpu_domain* d, int ntr);
+
+// ---- batched launches (k_batch64.cu, k_batch.cu) ----
+// One work list in device memory: entries[e] is the descriptor index of entry
+// e; p*[e] is the first block of entry e in each pass (p*[count] = total).
+struct BatchWork {
+  const int* entries;
+  const int *pz, *px, *py, *pu, *pb2, *pb1, *pm;
+  int count;
+  int tz, tx, ty, tu, tb2, tb1, tm;  // total blocks of each pass
+};
+// blocks of one domain in each pass, for the work-list prefix sums
+struct BatchBlocks {
+  int z, x, y, u, b2, b1, m;
+};
+BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows);
+// FP64: z/x/y MDFL passes and the explicit update for every entry
+void launch_batch_fp64_advection(const MdflArgs* mdfl, const UpdArgs* upd, const BatchWork& w, int ntr, bool sweby,
+                                 int TJ, cudaStream_t s);
+// the barotropic step (init, nts x (pred, mom, corr), post) for every entry; halo fills of
+// cyclic domains are issued by the caller between the post phases
+void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB,
+                                  cudaStream_t s);
+void launch_batch_barotropic_post(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, int phase,
+                                  cudaStream_t s);
+// precision form: persistent kernel over (entry, tile) items
+int launch_batch_mixed(const MixArgs* mix, const BatchWork& w, int ntr, int rows, int blocks, int* counter,
+                       cudaStream_t s);
+// sets the shared-memory attribute of every instantiation (before any graph capture)
+int prepare_batch_mixed();
 
 // ---- precision form (k_mixed.cu) ----
 int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, int taup1, double dtime,

@@ -1,0 +1,82 @@
+// Persistent batched kernel of the precision form: a fixed grid of resident
+// blocks drains a queue of (domain, tile) items (largest domains first),
+// running the same tile body as the one-domain kernel (mixed_body.cuh).
+#include "internal.h"
+#include "mixed_body.cuh"
+
+namespace mom5 {
+
+using namespace mixed;
+
+namespace {
+
+DEVI int find_entry_m(const int* prefix, int count, int b) {
+  int lo = 0, hi = count;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int NC, int ZR>
+__global__ void __launch_bounds__(NT, ZR == 16 ? 3 : 2) kb_mixed(const MixArgs* d, BatchWork w, int* counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
+  __shared__ int item;
+  const int total = w.tm;
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = item;
+    __syncthreads();
+    if (it >= total) break;
+    int e = find_entry_m(w.pm, w.count, it);
+    const MixArgs& a = d[w.entries[e]];
+    int local = it - w.pm[e];
+    int ntx = (a.g.ni + TI - 1) / TI;
+    mixed_tile<NC, ZR>(a, 0, local % ntx, local / ntx, s);
+  }
+}
+
+template <int NC, int ZR>
+int configure() {
+  return cudaFuncSetAttribute(kb_mixed<NC, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemT<ZR>)) ==
+                 cudaSuccess
+             ? MOM5GPU_OK
+             : MOM5GPU_ECUDA;
+}
+
+template <int NC, int ZR>
+int run(const MixArgs* m, const BatchWork& w, int blocks, int* counter, cudaStream_t s) {
+  size_t smem = sizeof(SmemT<ZR>);
+  cudaMemsetAsync(counter, 0, sizeof(int), s);
+  kb_mixed<NC, ZR><<<blocks, NT, smem, s>>>(m, w, counter);
+  return MOM5GPU_OK;
+}
+
+template <int ZR>
+int run_nc(const MixArgs* m, const BatchWork& w, int ntr, int blocks, int* counter, cudaStream_t s) {
+  if (ntr <= 1) return run<1, ZR>(m, w, blocks, counter, s);
+  if (ntr <= 2) return run<2, ZR>(m, w, blocks, counter, s);
+  if (ntr <= 4) return run<4, ZR>(m, w, blocks, counter, s);
+  return run<10, ZR>(m, w, blocks, counter, s);
+}
+
+}  // namespace
+
+int prepare_batch_mixed() {
+  int rc = 0;
+  rc |= configure<1, 32>() | configure<2, 32>() | configure<4, 32>() | configure<10, 32>();
+  rc |= configure<1, 16>() | configure<2, 16>() | configure<4, 16>() | configure<10, 16>();
+  return rc ? MOM5GPU_ECUDA : MOM5GPU_OK;
+}
+
+int launch_batch_mixed(const MixArgs* mix, const BatchWork& w, int ntr, int rows, int blocks, int* counter,
+                       cudaStream_t s) {
+  if (w.tm <= 0) return MOM5GPU_OK;
+  return rows == 16 ? run_nc<16>(mix, w, ntr, blocks, counter, s) : run_nc<32>(mix, w, ntr, blocks, counter, s);
+}
+
+}  // namespace mom5

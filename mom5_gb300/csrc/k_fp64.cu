@@ -12,57 +12,13 @@
 #include <stdio.h>
 
 #include "internal.h"
+#include "fp64_bodies.cuh"
 
 namespace mom5 {
 
 #define DEVI __device__ __forceinline__
 
-DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
-DEVI long I3(const Geo& g, int i, int j, int k) { return (long)k * g.n2 + (long)j * g.nxd + i; }
-// index into a (ni+4)(nj+4)nk halo-2 array; i, j in data-domain coordinates (isc = 1)
-DEVI long IM(const Geo& g, int i, int j, int k) { return ((long)k * (g.nj + 4) + (j + 1)) * (g.ni + 4) + (i + 1); }
-
-static const double kOneSixth = 1.0 / 6.0;  // ocean_parameters.F90:92
-
-// max(0, x) and min(a, b) on the integer pipe (ordered-integer comparison of
-// the bit patterns; equal to the FP comparison for all non-NaN operands).
-DEVI long long ordbits(double x) {
-  long long b = __double_as_longlong(x);
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
-DEVI double dmin(double a, double b) { return ordbits(a) <= ordbits(b) ? a : b; }
-DEVI double dmax0(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
-DEVI bool dpos(double x) { return __double_as_longlong(x) > 0; }   // x > 0
-
-// Sweby limiter psi (ocean_tracer_advect.F90:3868-3878).  With the limiter on
-// the reference forms psi*(1-1) + max(...)*1, with it off psi*1 + max(...)*0;
-// for finite psi both reduce to the selected term exactly.
-template <bool SWEBY>
-DEVI double limiter(double theta, double d0, double d1, double c) {
-  double lin = d0 + d1 * theta;
-  if (!SWEBY) return lin;
-  double a = dmin(1.0, lin);
-  return dmax0(dmin(a, c * theta));
-}
-
-// Flux of one face given the upwind-side data.  Reference form
-// 0.5*((mf+|mf|)*(Tup + psiP*Rj) + (mf-|mf|)*(Tdn - psiM*Rj)): for mf > 0 the
-// second product is an exact zero and 0.5*(2mf*X) == mf*X exactly.
-template <bool SWEBY>
-DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, double Tm, double d0, double d1,
-                      double c) {
-  long long b = __double_as_longlong(mf);
-  if (b > 0) {  // mf > 0: upwind value Tp on the minus side, ratio Rjm / Rj
-    double theta = Rjm / (1.0e-30 + Rj);
-    double psi = limiter<SWEBY>(theta, d0, d1, c);
-    return mf * (Tp + psi * Rj);
-  } else if (b < 0 && b != (long long)0x8000000000000000ULL) {  // mf < 0
-    double theta = Rjp / (1.0e-30 + Rj);
-    double psi = limiter<SWEBY>(theta, d0, d1, c);
-    return mf * (Tm - psi * Rj);
-  }
-  return 0.0;
-}
+using namespace fp64;
 
 // ---------------------------------------------------------------------------
 // halo update of a data-domain array (single-PE mpp_update_domains)
@@ -101,220 +57,19 @@ void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t
 // each face are computed once and reused for every tracer of the launch.
 // ---------------------------------------------------------------------------
 
-// z pass: one thread per column, march down k.
 template <bool ALL, bool SWEBY, int MAXN>
 __global__ void __launch_bounds__(128) k_mdfl_z(MdflArgs a) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j = blockIdx.y + 1;
-  if (i > g.ni) return;
-  double ftp[MAXN];
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) ftp[n] = 0.0;
-  double wkm1 = 0.0;
-  const double dat = a.dat[I2(g, i, j)];
-  const double datr = a.datr[I2(g, i, j)];
-  for (int k = 0; k < g.nk; ++k) {
-    int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
-    int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
-    int km1 = k > 0 ? k - 1 : 0;
-    bool mkm1 = a.mask2[IM(g, i, j, km1)], mk = a.mask2[IM(g, i, j, k)];
-    bool mkp1 = a.mask2[IM(g, i, j, kp1)], mkp2 = a.mask2[IM(g, i, j, kp2)];
-    double wk = a.w[I3(g, i, j, k + 1)];
-    double rdz = a.rdz[I3(g, i, j, k)];
-    double massflux = dat * wk;
-    double cfl = fabs(wk * a.dtime / rdz);
-    double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
-    double d1 = (1.0 - cfl * cfl) * kOneSixth;
-    double c = (1.0 - cfl) / (1.0e-30 + cfl);
-    double dtr = ALL ? 0.0 : a.dtime / rdz;
-    double wdiff = wkm1 - wk;
-    bool fm = mkp1 && mk;
-    long p = I3(g, i, j, k);
-#pragma unroll
-    for (int n = 0; n < MAXN; ++n) {
-      if (n < a.ntr) {
-        const double* T = a.T + n * a.tstride;
-        double Tk = T[p];
-        double Tkm1 = T[I3(g, i, j, km1)], Tkp1 = T[I3(g, i, j, kp1)], Tkp2 = T[I3(g, i, j, kp2)];
-        double Rjp = (mkm1 && mk) ? Tkm1 - Tk : 0.0;
-        double Rj = (mk && mkp1) ? Tk - Tkp1 : 0.0;
-        double Rjm = (mkp1 && mkp2) ? Tkp1 - Tkp2 : 0.0;
-        double fbt = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, Tkp1, Tk, d0, d1, c) : 0.0;
-        double tm;
-        if (!ALL) {
-          tm = Tk + dtr * (datr * (fbt - ftp[n]) + Tk * wdiff);
-        } else {
-          double w1 = datr * (fbt - ftp[n]) + Tk * wdiff;
-          tm = Tk + w1 * a.dtime / rdz;
-        }
-        a.tz[n * g.n3 + p] = tm;
-        ftp[n] = fbt;
-      }
-    }
-    wkm1 = wk;
-  }
-}
-
-// tracer_mdfl after the x halo update (XUPDATE): compute rows only.
-DEVI double tm_xhalo(const Geo& g, const double* a, int i, int j, int k) {
-  if (i < 1) {
-    if (!g.cx) return 0.0;
-    i += g.ni;
-  } else if (i > g.ni) {
-    if (!g.cx) return 0.0;
-    i -= g.ni;
-  }
-  return a[I3(g, i, j, k)];
-}
-DEVI double tm_yhalo(const Geo& g, const double* a, int i, int j, int k) {
-  if (j < 1) {
-    if (!g.cy) return 0.0;
-    j += g.nj;
-  } else if (j > g.nj) {
-    if (!g.cy) return 0.0;
-    j -= g.nj;
-  }
-  return a[I3(g, i, j, k)];
-}
-
-constexpr int kTX = 128;
-
-// x-face i of row (j,k): fluxes of every tracer into sm[n][slot].
-template <bool SWEBY, int MAXN>
-DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], int slot) {
-  const Geo& g = a.g;
-  bool m0 = a.mask2[IM(g, i - 1, j, k)], m1 = a.mask2[IM(g, i, j, k)];
-  bool m2 = a.mask2[IM(g, i + 1, j, k)], m3 = a.mask2[IM(g, i + 2, j, k)];
-  double u = a.uh[I3(g, i, j, k)];
-  double massflux = a.dyte[I2(g, i, j)] * u;
-  double cfl = fabs(u * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
-  double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
-  double d1 = (1.0 - cfl * cfl) * kOneSixth;
-  double c = (1.0 - cfl) / (1.0e-30 + cfl);
-  bool fm = m1 && m2;
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) {
-    if (n < a.ntr) {
-      const double* tz = a.tz + n * g.n3;
-      double tA = tm_xhalo(g, tz, i - 1, j, k), tB = tm_xhalo(g, tz, i, j, k);
-      double tC = tm_xhalo(g, tz, i + 1, j, k), tD = tm_xhalo(g, tz, i + 2, j, k);
-      double Rjp = (m3 && m2) ? tD - tC : 0.0;
-      double Rj = (m2 && m1) ? tC - tB : 0.0;
-      double Rjm = (m1 && m0) ? tB - tA : 0.0;
-      sm[n][slot] = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
-    }
-  }
+  mdfl_z_body<ALL, SWEBY, MAXN>(a, blockIdx.x, blockIdx.y);
 }
 
 template <bool ALL, bool SWEBY, int MAXN>
 __global__ void __launch_bounds__(kTX) k_mdfl_x(MdflArgs a) {
-  __shared__ double sm[MAXN][kTX + 1];
-  const Geo& g = a.g;
-  int i0 = blockIdx.x * kTX + 1;
-  int j = blockIdx.y + 1;
-  int k = blockIdx.z;
-  int t = threadIdx.x;
-  int i = i0 + t;
-  if (i <= g.ni) x_face<SWEBY, MAXN>(a, i, j, k, sm, t + 1);
-  if (t == 0) x_face<SWEBY, MAXN>(a, i0 - 1, j, k, sm, 0);
-  __syncthreads();
-  if (i > g.ni) return;
-  bool mk = a.mask2[IM(g, i, j, k)];
-  double datr = a.datr[I2(g, i, j)];
-  double rdz = a.rdz[I3(g, i, j, k)];
-  double divx = a.dyte[I2(g, i, j)] * a.uh[I3(g, i, j, k)] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
-  // dtime*tmask*datr/rho_dzt (:3960-3961); tmask_mdfl*datr (:4277)
-  double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
-  long p = I3(g, i, j, k);
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) {
-    if (n < a.ntr) {
-      double Tk = a.T[n * a.tstride + p];
-      double tm = a.tz[n * g.n3 + p];
-      double s = (sm[n][t] - sm[n][t + 1]) + Tk * divx;
-      if (!ALL) {
-        tm = tm + coef * s;
-      } else {
-        double w1 = mk ? datr * s : 0.0;
-        tm = tm + w1 * a.dtime / rdz;
-      }
-      a.tx[n * g.n3 + p] = tm;
-    }
-  }
-}
-
-// y pass + closing divergence correction + tendency: one thread per (i,k) and a
-// strip of TJ rows, marching north; th_tendency += result.
-template <bool SWEBY, int MAXN>
-DEVI void y_face(const MdflArgs& a, int i, int j, int k, double* f) {
-  const Geo& g = a.g;
-  bool m0 = a.mask2[IM(g, i, j - 1, k)], m1 = a.mask2[IM(g, i, j, k)];
-  bool m2 = a.mask2[IM(g, i, j + 1, k)], m3 = a.mask2[IM(g, i, j + 2, k)];
-  double v = a.vh[I3(g, i, j, k)];
-  double massflux = a.dxtn[I2(g, i, j)] * v;
-  double cfl = fabs(v * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
-  double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
-  double d1 = (1.0 - cfl * cfl) * kOneSixth;
-  double c = (1.0 - cfl) / (1.0e-30 + cfl);
-  bool fm = m1 && m2;
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) {
-    if (n < a.ntr) {
-      const double* tx = a.tx + n * g.n3;
-      double tA = tm_yhalo(g, tx, i, j - 1, k), tB = tm_yhalo(g, tx, i, j, k);
-      double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
-      double Rjp = (m3 && m2) ? tD - tC : 0.0;
-      double Rj = (m2 && m1) ? tC - tB : 0.0;
-      double Rjm = (m1 && m0) ? tB - tA : 0.0;
-      f[n] = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
-    }
-  }
+  mdfl_x_body<ALL, SWEBY, MAXN>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 template <bool ALL, bool SWEBY, int MAXN>
 __global__ void __launch_bounds__(128) k_mdfl_y(MdflArgs a, int TJ) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j0 = blockIdx.y * TJ + 1;
-  int k = blockIdx.z;
-  if (i > g.ni) return;
-  int j1 = j0 + TJ - 1;
-  if (j1 > g.nj) j1 = g.nj;
-  double fprev[MAXN], fcur[MAXN];
-  y_face<SWEBY, MAXN>(a, i, j0 - 1, k, fprev);
-  for (int j = j0; j <= j1; ++j) {
-    y_face<SWEBY, MAXN>(a, i, j, k, fcur);
-    long p = I3(g, i, j, k);
-    bool mk = a.mask2[IM(g, i, j, k)];
-    double datr = a.datr[I2(g, i, j)];
-    double rdz = a.rdz[p];
-    double wk = a.w[I3(g, i, j, k + 1)];
-    double wkm1j = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;  // bottom face of level k-1; 0 at the surface
-    double corr = (wk - wkm1j) + datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] -
-                                         a.dyte[I2(g, i, j)] * a.uh[p]);
-    double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
-#pragma unroll
-    for (int n = 0; n < MAXN; ++n) {
-      if (n < a.ntr) {
-        double Tk = a.T[n * a.tstride + p];
-        double tm = a.tx[n * g.n3 + p];
-        double out;
-        if (!ALL) {
-          tm = tm + coef * (fprev[n] - fcur[n]);
-          tm = tm + a.dtime * Tk / rdz * corr;
-          out = mk ? rdz * (tm - Tk) / a.dtime : 0.0;
-        } else {
-          double w1 = (mk ? datr * (fprev[n] - fcur[n]) : 0.0) + Tk * corr;
-          tm = tm + w1 * a.dtime / rdz;
-          out = mk ? rdz * (tm - Tk) / a.dtime : 0.0;
-        }
-        double* th = a.th + n * g.n3;
-        th[p] = th[p] + out;
-        fprev[n] = fcur[n];
-      }
-    }
-  }
+  mdfl_y_body<ALL, SWEBY, MAXN>(a, TJ, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 template <bool ALL, bool SWEBY, int MAXN>
@@ -328,6 +83,7 @@ static void run_mdfl(const MdflArgs& a, cudaStream_t s) {
   long cols = (long)g.ni * g.nk;
   int TJ = 16;
   while (TJ > 2 && cols * ((g.nj + TJ - 1) / TJ) < 152L * 32 * 16) TJ /= 2;
+  if (a.tj > 0) TJ = a.tj;
   dim3 by((g.ni + 127) / 128, (g.nj + TJ - 1) / TJ, g.nk);
   k_mdfl_y<ALL, SWEBY, MAXN><<<by, 128, 0, s>>>(a, TJ);
 }
@@ -350,7 +106,7 @@ void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s) {
   }
 }
 
-static int ensure_mdfl_scratch(mom5gpu_domain* d, int ntr) {
+int ensure_mdfl_scratch(mom5gpu_domain* d, int ntr) {
   if ((int)d->mdfl_cap >= ntr) return MOM5GPU_OK;
   if (d->mdfl_a) cudaFree(d->mdfl_a);
   if (d->mdfl_b) cudaFree(d->mdfl_b);
@@ -367,50 +123,50 @@ static int ensure_mdfl_scratch(mom5gpu_domain* d, int ntr) {
   return MOM5GPU_OK;
 }
 
+int make_mdfl_args(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, double dtime, MdflArgs* ap) {
+  MdflArgs& a = *ap;
+  const Geo& g = d->geo;
+  int NT = d->dims.num_prog_tracers;
+  a.g = g;
+  a.ntr = ntr;
+  a.dtime = dtime;
+  a.mask2 = d->mask2;
+  a.dat = fptr(d, MOM5GPU_DAT, 0, 0);
+  a.datr = fptr(d, MOM5GPU_DATR, 0, 0);
+  a.dxte = fptr(d, MOM5GPU_DXTE, 0, 0);
+  a.dyte = fptr(d, MOM5GPU_DYTE, 0, 0);
+  a.dxtn = fptr(d, MOM5GPU_DXTN, 0, 0);
+  a.dytn = fptr(d, MOM5GPU_DYTN, 0, 0);
+  a.uh = fptr(d, MOM5GPU_UHRHO_ET, 0, 0);
+  a.vh = fptr(d, MOM5GPU_VHRHO_NT, 0, 0);
+  a.w = fptr(d, MOM5GPU_WRHO_BT, 0, 0);
+  a.rdz = fptr(d, MOM5GPU_RHO_DZT, 0, tau);
+  a.T = fptr(d, MOM5GPU_TRACER, n_first, taum1);
+  a.tstride = NT > 1 ? (long)(fptr(d, MOM5GPU_TRACER, 2, 1) - fptr(d, MOM5GPU_TRACER, 1, 1)) : g.n3;
+  a.tz = d->mdfl_a;
+  a.tx = d->mdfl_b;
+  a.th = fptr(d, MOM5GPU_TH_TENDENCY, n_first, 0);
+  a.tj = d->tune_y_tj;
+  long thstride = NT > 1 ? (long)(fptr(d, MOM5GPU_TH_TENDENCY, 2, 0) - fptr(d, MOM5GPU_TH_TENDENCY, 1, 0)) : g.n3;
+  if (thstride != g.n3 || a.tstride != g.n3) return fail(d, MOM5GPU_ESTATE, "unexpected tracer layout");
+  if (!a.dat || !a.datr || !a.dxte || !a.dyte || !a.dxtn || !a.dytn || !a.uh || !a.vh || !a.w || !a.rdz || !a.T ||
+      !a.th || !a.mask2)
+    return fail(d, MOM5GPU_ESTATE, "mdfl: a required field was never set");
+  return MOM5GPU_OK;
+}
+
 int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,
                 double sweby_limiter) {
   int rc = ensure_mdfl_scratch(d, ntr < 8 ? ntr : 8);
   if (rc) return rc;
   ClockScope clk(d, SEC_MDFL);
-  const Geo& g = d->geo;
-  int NT = d->dims.num_prog_tracers;
   for (int c0 = 0; c0 < ntr; c0 += 8) {
     int cn = ntr - c0 < 8 ? ntr - c0 : 8;
     MdflArgs a;
-    a.g = g;
-    a.ntr = cn;
-    a.dtime = dtime;
-    a.mask2 = d->mask2;
-    a.dat = fptr(d, MOM5GPU_DAT, 0, 0);
-    a.datr = fptr(d, MOM5GPU_DATR, 0, 0);
-    a.dxte = fptr(d, MOM5GPU_DXTE, 0, 0);
-    a.dyte = fptr(d, MOM5GPU_DYTE, 0, 0);
-    a.dxtn = fptr(d, MOM5GPU_DXTN, 0, 0);
-    a.dytn = fptr(d, MOM5GPU_DYTN, 0, 0);
-    a.uh = fptr(d, MOM5GPU_UHRHO_ET, 0, 0);
-    a.vh = fptr(d, MOM5GPU_VHRHO_NT, 0, 0);
-    a.w = fptr(d, MOM5GPU_WRHO_BT, 0, 0);
-    a.rdz = fptr(d, MOM5GPU_RHO_DZT, 0, tau);
-    a.T = fptr(d, MOM5GPU_TRACER, n_first + c0, taum1);
-    a.tstride = NT > 1 ? (long)(fptr(d, MOM5GPU_TRACER, 2, 1) - fptr(d, MOM5GPU_TRACER, 1, 1)) : g.n3;
-    a.tz = d->mdfl_a;
-    a.tx = d->mdfl_b;
-    a.th = fptr(d, MOM5GPU_TH_TENDENCY, n_first + c0, 0);
-    long thstride = NT > 1 ? (long)(fptr(d, MOM5GPU_TH_TENDENCY, 2, 0) - fptr(d, MOM5GPU_TH_TENDENCY, 1, 0)) : g.n3;
-    if (thstride != g.n3 || a.tstride <= 0)
-      return fail(d, MOM5GPU_ESTATE, "unexpected tracer layout");
-    if (!a.dat || !a.datr || !a.dxte || !a.dyte || !a.dxtn || !a.dytn || !a.uh || !a.vh || !a.w || !a.rdz || !a.T ||
-        !a.th)
-      return fail(d, MOM5GPU_ESTATE, "mdfl: a required field was never set");
-    bool sweby = sweby_limiter != 0.0;
+    rc = make_mdfl_args(d, n_first + c0, cn, taum1, tau, dtime, &a);
+    if (rc) return rc;
     count_launches(d, 3);
-    if (all) {
-      if (sweby) run_mdfl_n<true, true>(a, d->stream);
-      else run_mdfl_n<true, false>(a, d->stream);
-    } else {
-      if (sweby) run_mdfl_n<false, true>(a, d->stream);
-      else run_mdfl_n<false, false>(a, d->stream);
-    }
+    run_mdfl_kernels(a, all, sweby_limiter != 0.0, d->stream);
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "mdfl launch");
@@ -696,33 +452,49 @@ int launch_quicker_vert(mom5gpu_domain* d, int n, int taum1, int tau) {
 // ---------------------------------------------------------------------------
 // explicit tracer update (ocean_tracer.F90:2341-2350)
 // ---------------------------------------------------------------------------
-__global__ void k_update_tracer(Geo g, int ntr, long tstride, const double* rdz_m1, const double* rdzr,
-                                const double* Tm1, const double* th, double* Tp1, double dtime) {
+__global__ void k_update_tracer(UpdArgs u) {
+  const Geo& g = u.g;
   int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   int j = blockIdx.y + 1, k = blockIdx.z;
   if (i > g.ni) return;
   long p = I3(g, i, j, k);
-  double a = rdz_m1[p], r = rdzr[p];
-  for (int n = 0; n < ntr; ++n) {
-    Tp1[n * tstride + p] = (a * Tm1[n * tstride + p] + dtime * th[n * g.n3 + p]) * r;
+  double a = u.rdz_m1[p], r = u.rdzr[p];
+  for (int n = 0; n < u.ntr; ++n) {
+    u.Tp1[n * u.tstride + p] = (a * u.Tm1[n * u.tstride + p] + u.dtime * u.th[n * g.n3 + p]) * r;
   }
+}
+
+int make_upd_args(mom5gpu_domain* d, int taum1, int taup1, double dtime, UpdArgs* u) {
+  const Geo& g = d->geo;
+  int NT = d->dims.num_prog_tracers;
+  u->g = g;
+  u->ntr = NT;
+  u->dtime = dtime;
+  u->rdz_m1 = fptr(d, MOM5GPU_RHO_DZT, 0, taum1);
+  u->rdzr = fptr(d, MOM5GPU_RHO_DZTR, 0, 0);
+  u->Tm1 = fptr(d, MOM5GPU_TRACER, 1, taum1);
+  u->Tp1 = fptr(d, MOM5GPU_TRACER, 1, taup1);
+  u->th = fptr(d, MOM5GPU_TH_TENDENCY, 1, 0);
+  u->tstride = g.n3;
+  if (!u->rdz_m1 || !u->rdzr || !u->Tm1 || !u->Tp1 || !u->th)
+    return fail(d, MOM5GPU_ESTATE, "update_tracer: a required field was never set");
+  return MOM5GPU_OK;
 }
 
 int launch_update_tracer(mom5gpu_domain* d, int n_first, int ntr, int taum1, int taup1, double dtime) {
   const Geo& g = d->geo;
-  int NT = d->dims.num_prog_tracers;
-  const double* rdz = fptr(d, MOM5GPU_RHO_DZT, 0, taum1);
-  const double* rdzr = fptr(d, MOM5GPU_RHO_DZTR, 0, 0);
-  const double* Tm1 = fptr(d, MOM5GPU_TRACER, n_first, taum1);
-  double* Tp1 = fptr(d, MOM5GPU_TRACER, n_first, taup1);
-  const double* th = fptr(d, MOM5GPU_TH_TENDENCY, n_first, 0);
-  if (!rdz || !rdzr || !Tm1 || !Tp1 || !th) return fail(d, MOM5GPU_ESTATE, "update_tracer: a required field was never set");
-  long tstride = NT > 1 ? (long)(fptr(d, MOM5GPU_TRACER, 2, 1) - fptr(d, MOM5GPU_TRACER, 1, 1)) : g.n3;
+  UpdArgs u;
+  int rc = make_upd_args(d, taum1, taup1, dtime, &u);
+  if (rc) return rc;
+  u.ntr = ntr;
+  u.Tm1 += (long)(n_first - 1) * g.n3;
+  u.Tp1 += (long)(n_first - 1) * g.n3;
+  u.th += (long)(n_first - 1) * g.n3;
   ClockScope clk(d, SEC_UPDATE);
   count_launches(d, 1 + ((g.cx || g.cy) ? ntr : 0));
   dim3 grid((g.ni + 127) / 128, g.nj, g.nk);
-  k_update_tracer<<<grid, 128, 0, d->stream>>>(g, ntr, tstride, rdz, rdzr, Tm1, th, Tp1, dtime);
-  for (int n = 0; n < ntr; ++n) launch_halo_fill(g, Tp1 + n * tstride, g.nk, 3, d->stream);
+  k_update_tracer<<<grid, 128, 0, d->stream>>>(u);
+  for (int n = 0; n < ntr; ++n) launch_halo_fill(g, u.Tp1 + n * u.tstride, g.nk, 3, d->stream);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "update_tracer");
 }
@@ -825,222 +597,6 @@ int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime) {
 // ---------------------------------------------------------------------------
 // Barotropic predictor-corrector subcycle.
 // ---------------------------------------------------------------------------
-struct BtArgs {
-  Geo g;
-  int cgrid, nts, stepB;
-  double dtbt, dtbt_gamma_rho0r, dtbt_rho0r, gamma;
-  const double *tmask1, *umask1, *f, *dxu, *dyu, *dxur, *dyur, *dat, *datr, *dxter, *dytnr, *tmen_e, *tmen_n;
-  const double *dte, *dtw, *dus, *dun, *daur;
-  const double *patm, *thicku, *thicken_e, *thicken_n, *forcing_u, *forcing_v, *rho_g, *cori1, *cori2;
-  double* eta_bt;  // 2 levels
-  double* ubt;     // 2 levels
-  double* vbt;     // 2 levels
-  double* steady;
-  double* ps;
-  double* cf;  // coriolis_force_bt, 6 planes (component-major within AB level)
-  double* ca;  // coriolis_accel_bt, 2 planes
-  double *eta_bar, *udrho_u, *udrho_v;  // taup1 accumulators
-};
-
-// DIV_UD at (i,j) (ocean_operators.F90:507-608), halo_in = halo_out = 1.
-DEVI double div_ud(const BtArgs& a, const double* u, const double* v, int i, int j) {
-  const Geo& g = a.g;
-  if (i < 1 || j < 1) return 0.0;
-  if (a.cgrid) {
-    double uhim = u[I2(g, i - 1, j)] * a.dat[I2(g, i - 1, j)] * a.dxter[I2(g, i - 1, j)];
-    double vhjm = v[I2(g, i, j - 1)] * a.dat[I2(g, i, j - 1)] * a.dytnr[I2(g, i, j - 1)];
-    double uh = u[I2(g, i, j)] * a.dat[I2(g, i, j)] * a.dxter[I2(g, i, j)];
-    double vh = v[I2(g, i, j)] * a.dat[I2(g, i, j)] * a.dytnr[I2(g, i, j)];
-    return ((uh - uhim) + (vh - vhjm)) * a.datr[I2(g, i, j)];
-  }
-  double uh = u[I2(g, i, j)] * a.dyu[I2(g, i, j)];
-  double vh = v[I2(g, i, j)] * a.dxu[I2(g, i, j)];
-  double uhjm = u[I2(g, i, j - 1)] * a.dyu[I2(g, i, j - 1)];
-  double vhjm = v[I2(g, i, j - 1)] * a.dxu[I2(g, i, j - 1)];
-  double uhim = u[I2(g, i - 1, j)] * a.dyu[I2(g, i - 1, j)];
-  double vhim = v[I2(g, i - 1, j)] * a.dxu[I2(g, i - 1, j)];
-  double uhimjm = u[I2(g, i - 1, j - 1)] * a.dyu[I2(g, i - 1, j - 1)];
-  double vhimjm = v[I2(g, i - 1, j - 1)] * a.dxu[I2(g, i - 1, j - 1)];
-  double uh_bay = 0.5 * (uh + uhjm);
-  double vh_bax = 0.5 * (vh + vhim);
-  double uhim_bay = 0.5 * (uhim + uhimjm);
-  double vhjm_bax = 0.5 * (vhjm + vhimjm);
-  return ((uh_bay - uhim_bay) + (vh_bax - vhjm_bax)) * a.datr[I2(g, i, j)];
-}
-
-// image of a halo point under the single-PE full halo update; returns false
-// when the point is left untouched (non-cyclic wall, or a corner of a domain
-// cyclic in one direction only).
-DEVI bool halo_image(const Geo& g, int& i, int& j) {
-  bool hx = (i == 0 || i == g.ni + 1), hy = (j == 0 || j == g.nj + 1);
-  if (!hx && !hy) return true;
-  if (hx && hy) {
-    if (!(g.cx && g.cy)) return false;
-  } else if (hx && !g.cx) {
-    return false;
-  } else if (hy && !g.cy) {
-    return false;
-  }
-  if (i == 0) i = g.ni;
-  else if (i == g.ni + 1) i = 1;
-  if (j == 0) j = g.nj;
-  else if (j == g.nj + 1) j = 1;
-  return true;
-}
-
-__global__ void k_bt_init(BtArgs a, const double* eta_bar_tau, const double* eta_tau, const double* ud_tau,
-                          const double* vd_tau, const double* pme, const double* river, const double* source,
-                          const double* eta_smooth, int initsum_with_bar) {
-  long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (q >= a.g.n2) return;
-  a.eta_bar[q] = initsum_with_bar ? eta_bar_tau[q] : eta_tau[q];
-  a.udrho_u[q] = 0.0;
-  a.udrho_v[q] = 0.0;
-  // fstau = mod(1,2)+1 = 2 -> plane 1
-  a.eta_bt[a.g.n2 + q] = eta_bar_tau[q];
-  a.ubt[a.g.n2 + q] = ud_tau[q];
-  a.vbt[a.g.n2 + q] = vd_tau[q];
-  a.steady[q] = a.tmask1[q] * (pme[q] + river[q] + source[q] - eta_smooth[q]);
-}
-
-// C-grid: initial Adams-Bashforth Coriolis history (:3707-3730)
-__global__ void k_bt_cgrid_init(BtArgs a) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j = blockIdx.y + 1;
-  if (i > g.ni) return;
-  const double abm0 = 23.0 / 12.0, abm1 = -16.0 / 12.0, abm2 = 5.0 / 12.0;
-  const int itime = 1;
-  int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
-  const double* u = a.ubt + g.n2;
-  const double* v = a.vbt + g.n2;
-  long n2 = g.n2;
-  long q = I2(g, i, j);
-  double c0 = 0.25 * (a.f[q] * (v[q] + v[I2(g, i + 1, j)]) + a.f[I2(g, i, j - 1)] * (v[I2(g, i, j - 1)] + v[I2(g, i + 1, j - 1)]));
-  a.cf[(m0 * 2 + 0) * n2 + q] = c0;
-  a.cf[(m1 * 2 + 0) * n2 + q] = c0;
-  a.cf[(m2 * 2 + 0) * n2 + q] = c0;
-  a.ca[q] = abm0 * c0 + abm1 * c0 + abm2 * c0;
-  double c1 = -0.25 * (a.f[q] * (u[q] + u[I2(g, i, j + 1)]) + a.f[I2(g, i - 1, j)] * (u[I2(g, i - 1, j)] + u[I2(g, i - 1, j + 1)]));
-  a.cf[(m0 * 2 + 1) * n2 + q] = c1;
-  a.cf[(m1 * 2 + 1) * n2 + q] = c1;
-  a.cf[(m2 * 2 + 1) * n2 + q] = c1;
-  a.ca[n2 + q] = abm0 * c1 + abm1 * c1 + abm2 * c1;
-}
-
-// predictor + ps (both grids)
-__global__ void k_bt_pred(BtArgs a, int so, int sn) {
-  const Geo& g = a.g;
-  int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-  int j0 = blockIdx.y;
-  if (i0 > g.ni + 1) return;
-  int i = i0, j = j0;
-  // B-grid legacy halos: eta(fstaup1) is halo-updated right after the predictor,
-  // so a halo point takes the value computed at its periodic image.
-  if (!a.cgrid) {
-    if (!halo_image(g, i, j)) {
-      i = i0;
-      j = j0;
-    }
-  }
-  const double* eo = a.eta_bt + so * g.n2;
-  long q = I2(g, i, j);
-  double en;
-  if (a.gamma > 0.0) {
-    double dv = div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j);
-    double tmp = a.tmask1[q] != 0.0 ? (-dv) * a.tmask1[q] : 0.0;
-    en = eo[q] + a.dtbt_gamma_rho0r * (tmp + a.steady[q]);
-  } else {
-    en = eo[q];
-  }
-  long q0 = I2(g, i0, j0);
-  a.eta_bt[sn * g.n2 + q0] = en;
-  a.ps[q0] = a.rho_g[q0] * en + a.patm[q0];
-}
-
-// momentum update, B grid (:3466-3485)
-__global__ void k_bt_mom_b(BtArgs a, int so, int sn) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y;
-  if (i > g.ni + 1) return;
-  long q = I2(g, i, j);
-  double gx = 0.0, gy = 0.0;
-  if (i <= g.ni && j <= g.nj) {
-    const double* ps = a.ps;
-    double p_fay = 0.5 * (ps[q] + ps[I2(g, i, j + 1)]);
-    double p_fax = 0.5 * (ps[q] + ps[I2(g, i + 1, j)]);
-    double pip_fay = 0.5 * (ps[I2(g, i + 1, j)] + ps[I2(g, i + 1, j + 1)]);
-    double pjp_fax = 0.5 * (ps[I2(g, i, j + 1)] + ps[I2(g, i + 1, j + 1)]);
-    bool um = a.umask1[q] != 0.0;
-    gx = um ? (pip_fay - p_fay) * a.dxur[q] * a.umask1[q] : 0.0;
-    gy = um ? (pjp_fax - p_fax) * a.dyur[q] * a.umask1[q] : 0.0;
-  }
-  double pf1 = -a.thicku[q] * gx;
-  double pf2 = -a.thicku[q] * gy;
-  double uo = a.ubt[so * g.n2 + q], vo = a.vbt[so * g.n2 + q];
-  double f = a.f[q];
-  double t1 = uo + a.dtbt * (0.5 * f * vo + pf1 + a.forcing_u[q] + 0.0);
-  double t2 = vo + a.dtbt * (-0.5 * f * uo + pf2 + a.forcing_v[q] + 0.0);
-  a.ubt[sn * g.n2 + q] = a.cori2[q] * (t1 + a.cori1[q] * t2);
-  a.vbt[sn * g.n2 + q] = a.cori2[q] * (t2 - a.cori1[q] * t1);
-}
-
-// C grid: Coriolis (compute domain) + gradient + momentum (:3780-3830)
-__global__ void k_bt_mom_c(BtArgs a, int so, int sn, int itime) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y;
-  if (i > g.ni + 1) return;
-  long n2 = g.n2;
-  long q = I2(g, i, j);
-  const double abm0 = 23.0 / 12.0, abm1 = -16.0 / 12.0, abm2 = 5.0 / 12.0;
-  int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
-  double ca0 = 0.0, ca1 = 0.0;
-  if (i >= 1 && i <= g.ni && j >= 1 && j <= g.nj) {
-    const double* u = a.ubt + so * n2;
-    const double* v = a.vbt + so * n2;
-    double c0 = 0.25 * (a.f[q] * (v[q] + v[I2(g, i + 1, j)]) + a.f[I2(g, i, j - 1)] * (v[I2(g, i, j - 1)] + v[I2(g, i + 1, j - 1)]));
-    a.cf[(m0 * 2 + 0) * n2 + q] = c0;
-    ca0 = abm0 * c0 + abm1 * a.cf[(m1 * 2 + 0) * n2 + q] + abm2 * a.cf[(m2 * 2 + 0) * n2 + q];
-    double c1 = -0.25 * (a.f[q] * (u[q] + u[I2(g, i, j + 1)]) + a.f[I2(g, i - 1, j)] * (u[I2(g, i - 1, j)] + u[I2(g, i - 1, j + 1)]));
-    a.cf[(m0 * 2 + 1) * n2 + q] = c1;
-    ca1 = abm0 * c1 + abm1 * a.cf[(m1 * 2 + 1) * n2 + q] + abm2 * a.cf[(m2 * 2 + 1) * n2 + q];
-  }
-  double gx = 0.0, gy = 0.0;
-  if (i <= g.ni && j <= g.nj) {
-    gx = (a.ps[I2(g, i + 1, j)] - a.ps[q]) * a.dxter[q] * a.tmen_e[q];
-    gy = (a.ps[I2(g, i, j + 1)] - a.ps[q]) * a.dytnr[q] * a.tmen_n[q];
-  }
-  double pf1 = -a.thicken_e[q] * gx;
-  double pf2 = -a.thicken_n[q] * gy;
-  double uo = a.ubt[so * n2 + q], vo = a.vbt[so * n2 + q];
-  a.ubt[sn * n2 + q] = uo + a.dtbt * a.tmen_e[q] * (ca0 + pf1 + a.forcing_u[q] + 0.0);
-  a.vbt[sn * n2 + q] = vo + a.dtbt * a.tmen_n[q] * (ca1 + pf2 + a.forcing_v[q] + 0.0);
-}
-
-// corrector + accumulation
-__global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y;
-  if (i > g.ni + 1) return;
-  long q = I2(g, i, j);
-  double dv = div_ud(a, a.ubt + sn * g.n2, a.vbt + sn * g.n2, i, j);
-  double tmp = a.tmask1[q] != 0.0 ? (-dv) * a.tmask1[q] : 0.0;
-  double en = a.eta_bt[so * g.n2 + q] + a.dtbt_rho0r * (tmp + a.steady[q]);
-  a.eta_bt[sn * g.n2 + q] = en;
-  a.eta_bar[q] = a.eta_bar[q] + en;
-  double un = a.ubt[sn * g.n2 + q], vn = a.vbt[sn * g.n2 + q];
-  if (a.stepB) {
-    a.udrho_u[q] = a.udrho_u[q] + wgt * un;
-    a.udrho_v[q] = a.udrho_v[q] + wgt * vn;
-  } else {
-    a.udrho_u[q] = a.udrho_u[q] + un;
-    a.udrho_v[q] = a.udrho_v[q] + vn;
-  }
-}
-
 __global__ void k_bt_post1(long n2, double rntsp1, double rnts, double* eb, double* uu, double* vv) {
   long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (q >= n2) return;
@@ -1049,54 +605,22 @@ __global__ void k_bt_post1(long n2, double rntsp1, double rnts, double* eb, doub
   vv[q] = rnts * vv[q];
 }
 
-__global__ void k_bt_post2(BtArgs a, double* conv, double* eta_u, double* ps_out) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y;
-  if (i > g.ni + 1) return;
-  long q = I2(g, i, j);
-  conv[q] = -div_ud(a, a.udrho_u, a.udrho_v, i, j);
-  double r = 0.0;
-  if (i <= g.ni && j <= g.nj) {
-    const double* e = a.eta_bar;
-    r = (e[q] * a.dte[q] * a.dus[q] + e[I2(g, i + 1, j)] * a.dtw[I2(g, i + 1, j)] * a.dus[q] +
-         e[I2(g, i, j + 1)] * a.dte[I2(g, i, j + 1)] * a.dun[q] +
-         e[I2(g, i + 1, j + 1)] * a.dtw[I2(g, i + 1, j + 1)] * a.dun[q]) *
-        a.daur[q];
-  }
-  eta_u[q] = a.umask1[q] != 0.0 ? a.umask1[q] * r : 0.0;
-  ps_out[q] = a.rho_g[q] * a.eta_bar[q] + a.patm[q];
-}
+__global__ void k_bt_init(BtArgs a, const double* eta_bar_tau, const double* eta_tau, const double* ud_tau,
+                          const double* vd_tau, const double* pme, const double* river, const double* source,
+                          const double* eta_smooth, int initsum_with_bar) { bt_init_body(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, source, eta_smooth, initsum_with_bar, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_cgrid_init(BtArgs a) { bt_cgrid_init_body(a, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_pred(BtArgs a, int so, int sn) { bt_pred_body(a, so, sn, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_mom_b(BtArgs a, int so, int sn) { bt_mom_b_body(a, so, sn, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_mom_c(BtArgs a, int so, int sn, int itime) { bt_mom_c_body(a, so, sn, itime, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) { bt_corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_post2(BtArgs a, double* conv, double* eta_u, double* ps_out) { bt_post2_body(a, conv, eta_u, ps_out, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_post3(BtArgs a, const double* ps, double* gxo, double* gyo) { bt_post3_body(a, ps, gxo, gyo, blockIdx.x, blockIdx.y); }
 
-__global__ void k_bt_post3(BtArgs a, const double* ps, double* gxo, double* gyo) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y;
-  if (i > g.ni + 1) return;
-  long q = I2(g, i, j);
-  double gx = 0.0, gy = 0.0;
-  if (i <= g.ni && j <= g.nj) {
-    if (!a.cgrid) {
-      double p_fay = 0.5 * (ps[q] + ps[I2(g, i, j + 1)]);
-      double p_fax = 0.5 * (ps[q] + ps[I2(g, i + 1, j)]);
-      double pip_fay = 0.5 * (ps[I2(g, i + 1, j)] + ps[I2(g, i + 1, j + 1)]);
-      double pjp_fax = 0.5 * (ps[I2(g, i, j + 1)] + ps[I2(g, i + 1, j + 1)]);
-      bool um = a.umask1[q] != 0.0;
-      gx = um ? (pip_fay - p_fay) * a.dxur[q] * a.umask1[q] : 0.0;
-      gy = um ? (pjp_fax - p_fax) * a.dyur[q] * a.umask1[q] : 0.0;
-    } else {
-      gx = (ps[I2(g, i + 1, j)] - ps[q]) * a.dxter[q] * a.tmen_e[q];
-      gy = (ps[I2(g, i, j + 1)] - ps[q]) * a.dytnr[q] * a.tmen_n[q];
-    }
-  }
-  gxo[q] = gx;
-  gyo[q] = gy;
-}
-
-int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
+int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp) {
   const Geo& g = d->geo;
   if (!d->baro_ready) return fail(d, MOM5GPU_ESTATE, "update_ocean_barotropic before mom5gpu_barotropic_init");
-  BtArgs a;
+  BtArgs& a = *ap;
+  BtExtra& x = *xp;
   a.g = g;
   a.cgrid = d->dims.horz_grid == MOM5GPU_CGRID;
   a.nts = d->nts;
@@ -1144,25 +668,41 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   a.eta_bar = fptr(d, MOM5GPU_ETA_T_BAR, 0, taup1);
   a.udrho_u = fptr(d, MOM5GPU_UDRHO_U, 0, taup1);
   a.udrho_v = fptr(d, MOM5GPU_UDRHO_V, 0, taup1);
-  const double* eta_bar_tau = fptr(d, MOM5GPU_ETA_T_BAR, 0, tau);
-  const double* eta_tau = fptr(d, MOM5GPU_ETA_T, 0, tau);
-  const double* ud_tau = fptr(d, MOM5GPU_UDRHO_U, 0, tau);
-  const double* vd_tau = fptr(d, MOM5GPU_UDRHO_V, 0, tau);
-  const double *pme = fptr(d, MOM5GPU_PME, 0, 0), *river = fptr(d, MOM5GPU_RIVER, 0, 0);
-  const double *src = fptr(d, MOM5GPU_SOURCE, 0, 0), *esm = fptr(d, MOM5GPU_ETA_SMOOTH, 0, 0);
-  double* conv = fptr(d, MOM5GPU_CONV_RHO_UD_T, 0, taup1);
-  double* eta_u = fptr(d, MOM5GPU_ETA_U, 0, taup1);
-  double* ps_out = fptr(d, MOM5GPU_PS, 0, 0);
-  double* gxo = fptr(d, MOM5GPU_GRAD_PS_X, 0, 0);
-  double* gyo = fptr(d, MOM5GPU_GRAD_PS_Y, 0, 0);
+  x.eta_bar_tau = fptr(d, MOM5GPU_ETA_T_BAR, 0, tau);
+  x.eta_tau = fptr(d, MOM5GPU_ETA_T, 0, tau);
+  x.ud_tau = fptr(d, MOM5GPU_UDRHO_U, 0, tau);
+  x.vd_tau = fptr(d, MOM5GPU_UDRHO_V, 0, tau);
+  x.pme = fptr(d, MOM5GPU_PME, 0, 0);
+  x.river = fptr(d, MOM5GPU_RIVER, 0, 0);
+  x.source = fptr(d, MOM5GPU_SOURCE, 0, 0);
+  x.eta_smooth = fptr(d, MOM5GPU_ETA_SMOOTH, 0, 0);
+  x.conv = fptr(d, MOM5GPU_CONV_RHO_UD_T, 0, taup1);
+  x.eta_u = fptr(d, MOM5GPU_ETA_U, 0, taup1);
+  x.ps_out = fptr(d, MOM5GPU_PS, 0, 0);
+  x.gxo = fptr(d, MOM5GPU_GRAD_PS_X, 0, 0);
+  x.gyo = fptr(d, MOM5GPU_GRAD_PS_Y, 0, 0);
+  x.initsum_with_bar = d->opt.initsum_with_bar;
   const void* need[] = {a.tmask1, a.umask1, a.f, a.dxu, a.dyu, a.dxur, a.dyur, a.dat, a.datr, a.patm, a.thicku,
-                        a.forcing_u, a.forcing_v, a.rho_g, a.eta_bar, a.udrho_u, a.udrho_v, eta_bar_tau, eta_tau,
-                        ud_tau, vd_tau, pme, river, src, esm, conv, eta_u, ps_out, gxo, gyo, a.dte, a.dtw, a.dus,
-                        a.dun, a.daur};
+                        a.forcing_u, a.forcing_v, a.rho_g, a.eta_bar, a.udrho_u, a.udrho_v, x.eta_bar_tau, x.eta_tau,
+                        x.ud_tau, x.vd_tau, x.pme, x.river, x.source, x.eta_smooth, x.conv, x.eta_u, x.ps_out, x.gxo,
+                        x.gyo, a.dte, a.dtw, a.dus, a.dun, a.daur};
   for (const void* p : need)
     if (!p) return fail(d, MOM5GPU_ESTATE, "update_ocean_barotropic: a required field was never set");
   if (a.cgrid && (!a.dxter || !a.dytnr || !a.tmen_e || !a.tmen_n || !a.thicken_e || !a.thicken_n))
     return fail(d, MOM5GPU_ESTATE, "C-grid barotropic: a required field was never set");
+  return MOM5GPU_OK;
+}
+
+int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
+  const Geo& g = d->geo;
+  BtArgs a;
+  BtExtra x;
+  int rc = make_bt_args(d, tau, taup1, &a, &x);
+  if (rc) return rc;
+  long n2 = g.n2;
+  const double *eta_bar_tau = x.eta_bar_tau, *eta_tau = x.eta_tau, *ud_tau = x.ud_tau, *vd_tau = x.vd_tau;
+  const double *pme = x.pme, *river = x.river, *src = x.source, *esm = x.eta_smooth;
+  double *conv = x.conv, *eta_u = x.eta_u, *ps_out = x.ps_out, *gxo = x.gxo, *gyo = x.gyo;
   cudaStream_t s = d->stream;
   ClockScope clk(d, SEC_BAROTROPIC);
   int halo = (g.cx || g.cy) ? 1 : 0;

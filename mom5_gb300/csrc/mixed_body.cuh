@@ -1,0 +1,332 @@
+// Body of the precision-form MDFL kernel (FP32 fluxes and limiters, FP64
+// state), shared by the one-domain kernel (k_mixed.cu) and the persistent
+// batched kernel (k_batch.cu).  See k_mixed.cu for the method.
+#pragma once
+#include <math.h>
+
+#include "internal.h"
+
+namespace mom5 {
+namespace mixed {
+
+#define DEVI __device__ __forceinline__
+
+
+constexpr int ZW = 32;       // tile width incl. the 2-cell halo on each side (one warp)
+constexpr int TI = ZW - 4;   // interior width
+constexpr int NT = 256;      // threads
+constexpr int NW = NT / 32;  // warps
+// ZR (template): tile height incl. halo; interior height ZR - 4
+
+DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
+DEVI long I3(const Geo& g, int i, int j, int k) { return (long)k * g.n2 + (long)j * g.nxd + i; }
+DEVI long IM(const Geo& g, int i, int j, int k) { return ((long)k * (g.nj + 4) + (j + 1)) * (g.ni + 4) + (i + 1); }
+
+// FP64 -> FP32 by truncation of the significand, with integer operations.
+DEVI float d2f(double x) {
+  unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  unsigned sign = hi & 0x80000000u, mag = hi & 0x7fffffffu;
+  if (mag < (897u << 20)) return __uint_as_float(sign);
+  if (mag >= (1151u << 20)) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
+}
+// FP32 -> FP64, exact, with integer operations (subnormal floats read as zero).
+DEVI double f2d(float f) {
+  unsigned b = __float_as_uint(f);
+  unsigned sign = b & 0x80000000u, mag = b & 0x7fffffffu;
+  if (mag < 0x00800000u) return __hiloint2double((int)sign, 0);
+  return __hiloint2double((int)(sign | ((mag >> 3) + (896u << 20))), (int)(mag << 29));
+}
+
+DEVI float limiter(float theta, float d0, float d1, float c) {
+  float lin = d0 + d1 * theta;
+  return fmaxf(0.0f, fminf(fminf(1.0f, lin), c * theta));
+}
+
+DEVI float face_flux(float mf, float Rjm, float Rj, float Rjp, float Tp, float Tm, float d0, float d1, float c) {
+  if (mf > 0.0f) {
+    float theta = __fdividef(Rjm, 1.0e-30f + Rj);
+    return mf * (Tp + limiter(theta, d0, d1, c) * Rj);
+  } else if (mf < 0.0f) {
+    float theta = __fdividef(Rjp, 1.0e-30f + Rj);
+    return mf * (Tm - limiter(theta, d0, d1, c) * Rj);
+  }
+  return 0.0f;
+}
+
+
+
+// image of a tile position under the single-domain halo rules; false when it lies
+// outside a non-cyclic boundary (the reference's halo holds zero there)
+DEVI bool image(const Geo& g, int& i, int& j) {
+  if (i < 1 || i > g.ni) {
+    if (!g.cx) return false;
+    i = ((i - 1) % g.ni + g.ni) % g.ni + 1;
+  }
+  if (j < 1 || j > g.nj) {
+    if (!g.cy) return false;
+    j = ((j - 1) % g.nj + g.nj) % g.nj + 1;
+  }
+  return true;
+}
+
+DEVI bool mask_at(const Geo& g, const uint8_t* m2, int i, int j, int k) {
+  if (i < -1 || i > g.ni + 2 || j < -1 || j > g.nj + 2) return false;
+  return m2[IM(g, i, j, k)] != 0;
+}
+
+template <int ZR>
+struct SmemT {
+  // z pass, per z-column (32x32)
+  float zmf[ZR * ZW], zd0[ZR * ZW], zd1[ZR * ZW], zc[ZR * ZW], zdtr[ZR * ZW], zwd[ZR * ZW], zdatr[ZR * ZW];
+  uint8_t zmask[ZR * ZW];  // bit0..3 = wet at k-1, k, k+1, k+2
+  float tz[ZR * ZW];       // tracer after z
+  float tf[ZR * ZW];       // tracer at taum1 (FP32)
+  float fz[ZR * ZW];       // z flux-divergence increment
+  // x pass: faces between columns zi and zi+1 (index zj*ZW+zi), cells
+  float xmf[ZR * ZW], xd0[ZR * ZW], xd1[ZR * ZW], xc[ZR * ZW];
+  float xcoef[ZR * ZW], xdiv[ZR * ZW];
+  float fx[ZR * ZW], tx[ZR * ZW], fxi[ZR * ZW];
+  // y pass: faces between rows zj and zj+1
+  float ymf[ZR * ZW], yd0[ZR * ZW], yd1[ZR * ZW], yc[ZR * ZW];
+  float fy[ZR * ZW];
+  // state-update factors: rho_dzt(taum1)*rho_dztr - 1 and rho_dzt(tau)*rho_dztr*tmask (or rho_dzt/dtime*tmask)
+  float uq[ZR * ZW], ur[ZR * ZW];
+  uint8_t xin[ZR * ZW];  // x-cell position inside the domain (or a cyclic image)
+  int off[ZR * ZW];      // 2-D offset j*nxd+i of the position's image; -1 outside a wall
+};
+
+template <int NC, int ZR>
+DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>& s) {
+  constexpr int TJ = ZR - 4;
+  constexpr int ROWS_PER_WARP = ZR / NW;
+  const Geo& g = a.g;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i0 = 1 + tile_x * TI, j0 = 1 + tile_y * TJ;
+  const float dt = a.dtime;
+  const float sixth = 1.0f / 6.0f;
+
+  // per-thread z columns: zi = lane, zj = warp + NW*m
+  float ftp[NC][ROWS_PER_WARP];
+#pragma unroll
+  for (int n = 0; n < NC; ++n)
+#pragma unroll
+    for (int m = 0; m < ROWS_PER_WARP; ++m) ftp[n][m] = 0.0f;
+
+  for (int k = 0; k < g.nk; ++k) {
+    const int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
+    const int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
+    const int km1 = k > 0 ? k - 1 : 0;
+    __syncthreads();  // previous level done with every tile array
+    // ---- level terms: z columns, x faces/cells, y faces ----
+#pragma unroll
+    for (int m = 0; m < ROWS_PER_WARP; ++m) {
+      const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+      int i = i0 - 2 + zi, j = j0 - 2 + zj;
+      const int pi = i, pj = j;
+      bool in = image(g, i, j);
+      uint8_t mbits = 0;
+      float mf = 0.f, d0 = 0.f, d1 = 0.f, cc = 0.f, dtr = 0.f, wd = 0.f, datr = 0.f;
+      if (in) {
+        mbits = (mask_at(g, a.mask2, pi, pj, km1) ? 1 : 0) | (mask_at(g, a.mask2, pi, pj, k) ? 2 : 0) |
+                (mask_at(g, a.mask2, pi, pj, kp1) ? 4 : 0) | (mask_at(g, a.mask2, pi, pj, kp2) ? 8 : 0);
+        float wk = d2f(a.w[I3(g, i, j, k + 1)]);
+        float wkm1 = k > 0 ? d2f(a.w[I3(g, i, j, k)]) : 0.0f;
+        float rr = 1.0f / d2f(a.rdz[I3(g, i, j, k)]);
+        datr = d2f(a.datr[I2(g, i, j)]);
+        mf = d2f(a.dat[I2(g, i, j)]) * wk;
+        float cfl = fabsf(wk * dt * rr);
+        d0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
+        d1 = (1.0f - cfl * cfl) * sixth;
+        cc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
+        dtr = dt * rr;
+        wd = wkm1 - wk;
+      }
+      s.zmask[c] = mbits;
+      s.off[c] = in ? (int)I2(g, i, j) : -1;
+      s.zmf[c] = mf;
+      s.zd0[c] = d0;
+      s.zd1[c] = d1;
+      s.zc[c] = cc;
+      s.zdtr[c] = dtr;
+      s.zwd[c] = wd;
+      s.zdatr[c] = datr;
+      // x face between zi and zi+1 of row zj (needed for zi = 1..29)
+      float xmf = 0.f, xd0 = 0.f, xd1 = 0.f, xc = 0.f;
+      if (in && zi >= 1 && zi <= ZW - 3) {
+        float u = d2f(a.uh[I3(g, i, j, k)]);
+        xmf = d2f(a.dyte[I2(g, i, j)]) * u;
+        float den = (d2f(a.rdz[I3(g, i, j, k)]) + d2f(a.rdz[I3(g, i + 1, j, k)])) * d2f(a.dxte[I2(g, i, j)]);
+        float cfl = fabsf(__fdividef(u * dt * 2.0f, den));
+        xd0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
+        xd1 = (1.0f - cfl * cfl) * sixth;
+        xc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
+      }
+      s.xmf[c] = xmf;
+      s.xd0[c] = xd0;
+      s.xd1[c] = xd1;
+      s.xc[c] = xc;
+      // x cell terms (cells zi = 2..29): dtime*tmask*datr/rho_dzt and the x divergence
+      float coef = 0.f, div = 0.f;
+      bool xin = in && zi >= 2 && zi <= ZW - 3;
+      if (xin) {
+        bool wet = (mbits & 2) != 0;
+        coef = wet ? dt * datr / d2f(a.rdz[I3(g, i, j, k)]) : 0.0f;
+        div = d2f(a.dyte[I2(g, i, j)]) * d2f(a.uh[I3(g, i, j, k)]) -
+              d2f(a.dyte[I2(g, i - 1, j)]) * d2f(a.uh[I3(g, i - 1, j, k)]);
+      }
+      s.xcoef[c] = coef;
+      s.xdiv[c] = div;
+      s.xin[c] = xin;
+      // y face between rows zj and zj+1 (needed for zj = 1..29, zi = 2..29)
+      float ymf = 0.f, yd0 = 0.f, yd1 = 0.f, yc = 0.f;
+      if (in && zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3) {
+        float v = d2f(a.vh[I3(g, i, j, k)]);
+        ymf = d2f(a.dxtn[I2(g, i, j)]) * v;
+        float den = (d2f(a.rdz[I3(g, i, j, k)]) + d2f(a.rdz[I3(g, i, j + 1, k)])) * d2f(a.dytn[I2(g, i, j)]);
+        float cfl = fabsf(__fdividef(v * dt * 2.0f, den));
+        yd0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
+        yd1 = (1.0f - cfl * cfl) * sixth;
+        yc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
+      }
+      s.ymf[c] = ymf;
+      s.yd0[c] = yd0;
+      s.yd1[c] = yd1;
+      s.yc[c] = yc;
+      // state-update factors of interior cells
+      float uq = 0.f, ur = 0.f;
+      if (in && zj >= 2 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3) {
+        long p = I3(g, i, j, k);
+        bool wet = (mbits & 2) != 0;
+        if (a.fused) {
+          double r = a.rdzr[p];
+          uq = d2f(fma(a.rdz_m1[p], r, -1.0));
+          ur = wet ? d2f(a.rdz[p] * r) : 0.0f;
+        } else {
+          ur = wet ? d2f(a.rdz[p]) / dt : 0.0f;
+        }
+      }
+      s.uq[c] = uq;
+      s.ur[c] = ur;
+    }
+    __syncthreads();
+
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+      if (n >= a.ntr) break;
+      const double* T = a.T + (long)n * g.n3;
+      // ---- z pass ----
+#pragma unroll
+      for (int m = 0; m < ROWS_PER_WARP; ++m) {
+        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        const int o = s.off[c];
+        uint8_t mb = s.zmask[c];
+        float tzv = 0.f, tk = 0.f, fzv = 0.f;
+        if (o >= 0) {
+          tk = d2f(T[(long)k * g.n2 + o]);
+          float tkm1 = d2f(T[(long)km1 * g.n2 + o]);
+          float tkp1 = d2f(T[(long)kp1 * g.n2 + o]);
+          float tkp2 = d2f(T[(long)kp2 * g.n2 + o]);
+          bool mkm1 = mb & 1, mk = mb & 2, mkp1 = mb & 4, mkp2 = mb & 8;
+          float Rjp = (mkm1 && mk) ? tkm1 - tk : 0.f;
+          float Rj = (mk && mkp1) ? tk - tkp1 : 0.f;
+          float Rjm = (mkp1 && mkp2) ? tkp1 - tkp2 : 0.f;
+          float fbt = (mkp1 && mk) ? face_flux(s.zmf[c], Rjm, Rj, Rjp, tkp1, tk, s.zd0[c], s.zd1[c], s.zc[c]) : 0.f;
+          float dtr = s.zdtr[c];
+          float adiv = s.zdatr[c] * (fbt - ftp[n][m]);
+          fzv = dtr * adiv;
+          tzv = tk + dtr * (adiv + tk * s.zwd[c]);
+          ftp[n][m] = fbt;
+        }
+        s.tz[c] = tzv;
+        s.tf[c] = tk;
+        s.fz[c] = fzv;
+      }
+      __syncthreads();
+      // ---- x fluxes: face zi (between zi and zi+1), zi = 1..29 ----
+#pragma unroll
+      for (int m = 0; m < ROWS_PER_WARP; ++m) {
+        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        float f = 0.f;
+        if (zi >= 1 && zi <= ZW - 3) {
+          bool m0 = s.zmask[c - 1] & 2, m1 = s.zmask[c] & 2, m2 = s.zmask[c + 1] & 2, m3 = s.zmask[c + 2] & 2;
+          if (m1 && m2) {
+            float tA = s.tz[c - 1], tB = s.tz[c], tC = s.tz[c + 1], tD = s.tz[c + 2];
+            float Rjp = (m3 && m2) ? tD - tC : 0.f;
+            float Rj = tC - tB;
+            float Rjm = (m1 && m0) ? tB - tA : 0.f;
+            f = face_flux(s.xmf[c], Rjm, Rj, Rjp, tB, tC, s.xd0[c], s.xd1[c], s.xc[c]);
+          }
+        }
+        s.fx[c] = f;
+      }
+      __syncthreads();
+      // ---- x update: cells zi = 2..29 of every row ----
+#pragma unroll
+      for (int m = 0; m < ROWS_PER_WARP; ++m) {
+        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        float t = 0.f, fi = 0.f;
+        if (s.xin[c]) {
+          float coef = s.xcoef[c];
+          fi = coef * (s.fx[c - 1] - s.fx[c]);
+          t = s.tz[c] + (fi + coef * (s.tf[c] * s.xdiv[c]));
+        }
+        s.tx[c] = t;
+        s.fxi[c] = fi;
+      }
+      __syncthreads();
+      // ---- y fluxes: face zj (between rows zj and zj+1), zj = 1..29, zi = 2..29 ----
+#pragma unroll
+      for (int m = 0; m < ROWS_PER_WARP; ++m) {
+        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        float f = 0.f;
+        if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3) {
+          bool m0 = s.zmask[c - ZW] & 2, m1 = s.zmask[c] & 2, m2 = s.zmask[c + ZW] & 2, m3 = s.zmask[c + 2 * ZW] & 2;
+          if (m1 && m2) {
+            float tA = s.tx[c - ZW], tB = s.tx[c], tC = s.tx[c + ZW], tD = s.tx[c + 2 * ZW];
+            float Rjp = (m3 && m2) ? tD - tC : 0.f;
+            float Rj = tC - tB;
+            float Rjm = (m1 && m0) ? tB - tA : 0.f;
+            f = face_flux(s.ymf[c], Rjm, Rj, Rjp, tB, tC, s.yd0[c], s.yd1[c], s.yc[c]);
+          }
+        }
+        s.fy[c] = f;
+      }
+      __syncthreads();
+      // ---- interior: total increment and output ----
+#pragma unroll
+      for (int m = 0; m < ROWS_PER_WARP; ++m) {
+        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        if (zj < 2 || zj > ZR - 3 || zi < 2 || zi > ZW - 3) continue;
+        const int i = i0 - 2 + zi, j = j0 - 2 + zj;
+        if (i > g.ni || j > g.nj) continue;
+        bool wet = s.zmask[c] & 2;
+        if (!wet && !a.fused) continue;
+        float fy = s.xcoef[c] * (s.fy[c - ZW] - s.fy[c]);
+        float dT = s.fz[c] + s.fxi[c] + fy;
+        long p = I3(g, i, j, k);
+        if (a.fused) {
+          // T(taup1) = T + (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT
+          float inc = s.uq[c] * s.tf[c] + s.ur[c] * dT;
+          double tn = T[p] + f2d(inc);
+          double* o = a.out + (long)(n0 + n) * g.n3;
+          o[p] = tn;
+          // halo update of T(taup1) in cyclic directions (ocean_model.F90:1903-1911)
+          int hi = (g.cx && i == g.ni) ? 0 : (g.cx && i == 1) ? g.ni + 1 : -1;
+          int hj = (g.cy && j == g.nj) ? 0 : (g.cy && j == 1) ? g.nj + 1 : -1;
+          if (hi >= 0) o[I3(g, hi, j, k)] = tn;
+          if (hj >= 0) o[I3(g, i, hj, k)] = tn;
+          if (hi >= 0 && hj >= 0) o[I3(g, hi, hj, k)] = tn;
+        } else if (wet) {
+          double* o = a.out + (long)n * g.n3;
+          o[p] = o[p] + f2d(s.ur[c] * dT);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+
+}  // namespace mixed
+}  // namespace mom5
