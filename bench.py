@@ -185,8 +185,56 @@ def cpu_reference(spec, warmup, steps, procs, block_frac=1.0):
 
 
 # --------------------------------------------------------------------------- GPU side
+def _time_domain(d, stream, ntr, steps, warmup, state, clock_index=0):
+    """Warm up, then time `steps` whole steps of one domain on `stream` (CUDA events)."""
+    import torch
+
+    def step():
+        tau = state["tau"]
+        taup1 = 3 - tau
+        if ntr > 0:
+            d.tracer_advection_step(tau, tau, taup1, DTTS)
+        d.update_ocean_barotropic(tau, taup1)
+        state["tau"] = taup1
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    d.enable_timing(True)
+    launches0 = d.launches
+    clocks = ClockSampler(clock_index)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    sec = {s: d.timing(s) for s in ("mdfl", "mdfl_mixed", "tracer_update", "barotropic")}
+    d.enable_timing(False)
+    return {"ms": ms, "sec": sec, "launches": d.launches - launches0, "clocks": clk, "step": step}
+
+
+def _device_copy(d, fid, n, level):
+    """A field of a library domain copied into a new CUDA tensor (device to device)."""
+    import torch
+    from mom5_gb300 import capi
+    t = torch.empty(d.count(fid), dtype=torch.float64, device="cuda")
+    d.check(capi.lib().mom5gpu_get_field(d.h, fid, n, level, capi.C.c_void_p(t.data_ptr()), 1))
+    d.synchronize()
+    return t
+
+
+def _rel_err(a, b):
+    """max|a - b| / max|b| (b the FP64 result)."""
+    return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+
+
 def run_ours(args, rank, world):
-    import numpy as np
     import torch
 
     from mom5_gb300 import build, capi, grid, harness
@@ -197,13 +245,15 @@ def run_ours(args, rank, world):
     build.build()
     spec = config_spec(args.config)
     prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_FP64
+    forms = (not args.no_forms) and world == 1 and prec == capi.PRECISION_FP64 and args.config == "c2"
     dom = grid.make_domain(spec, device="cuda")
     opts = capi.default_options(barotropic_time_stepping_B=1, precision=prec)
     d = harness.load(dom, options=opts)
     nts = d.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
     ni, nj, nk, ntr = spec.ni, spec.nj, spec.nk, spec.ntracers
     cells = ni * nj * nk
-    del dom
+    if not forms:
+        del dom
     torch.cuda.empty_cache()
     # a dedicated stream: the legacy default stream's handle is 0, which the C ABI
     # reads as "the domain's own stream"
@@ -212,42 +262,15 @@ def run_ours(args, rank, world):
     d.set_stream(stream.cuda_stream)
 
     state = {"tau": 1}
-
-    def step():
-        tau = state["tau"]
-        taup1 = 3 - tau
-        if ntr > 0:
-            d.tracer_advection_step(tau, tau, taup1, DTTS)
-        d.update_ocean_barotropic(tau, taup1)
-        state["tau"] = taup1
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    d.enable_timing(True)
-    launches0 = d.launches
-    clocks = ClockSampler(local)
-    clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
+    r = _time_domain(d, stream, ntr, args.steps, args.warmup, state, local)
+    ms, sec, launches, clk, step = r["ms"], r["sec"], r["launches"], r["clocks"], r["step"]
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
         torch.distributed.barrier()
-    launches = d.launches - launches0
-    sec = {s: d.timing(s) for s in ("mdfl", "mdfl_mixed", "tracer_update", "barotropic")}
-    d.enable_timing(False)
     ms_step = ms / args.steps
     value = cells * world * args.steps / (ms / 1e3)
 
@@ -306,6 +329,7 @@ def run_ours(args, rank, world):
                "h2d_bytes_per_step": 8 * (ntr * n3 + 2 * n3 + nw), "d2h_bytes_per_step": 8 * (ntr * n3 + 3 * n2),
                "steps": ke, "api": "mom5gpu_set_field / mom5gpu_tracer_advection_step / "
                                    "mom5gpu_update_ocean_barotropic / mom5gpu_get_field (pinned host buffers)"}
+        del hT, oT, hU, hV, hW
 
     out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-updates/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
@@ -326,13 +350,215 @@ def run_ours(args, rank, world):
         v, info = _cpu_sample(spec)
         out["cpu_baseline"] = {"value": round(v, 1), "unit": "cell-updates/s", "cores": 1, "kind": "port",
                                "sample": info}
+    if forms:
+        out["forms"] = run_forms(args, dom, d, value, stream)
     return out
 
 
+# --------------------------------------------------------------------------- the three forms
+FORM_DT = 400.0     # baroclinic step of the ensemble and serving domains (s)
+FORM_DTBT = 20.0    # barotropic step: nts = 2 * 400 / 20 = 40 subcycles
+
+
+def run_forms(args, dom, d64, plain_value, stream):
+    """Precision form on the same 1440x1080x50 domain, then the batched ensemble
+    (64 domains) and the serving loop (256 resident domains)."""
+    import torch
+
+    from mom5_gb300 import capi, harness
+    from mom5_gb300.capi import F
+    spec = dom.spec
+    ntr = spec.ntracers
+    cells = spec.ni * spec.nj * spec.nk
+    forms = {}
+    # ---- precision form, same workload
+    dm = harness.load(dom, options=capi.default_options(barotropic_time_stepping_B=1, precision=capi.PRECISION_MIXED))
+    dm.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
+    dm.set_stream(stream.cuda_stream)
+    r = _time_domain(dm, stream, ntr, args.steps, args.warmup, {"tau": 1})
+    v = cells * args.steps / (r["ms"] / 1e3)
+    # error against the FP64 drop-in (equal to the oracle bit for bit), one step from the same state
+    errs, drift64, driftm = [], 0.0, 0.0
+    for n in range(1, ntr + 1):
+        d64.set(F.TRACER, dom["T"][n - 1].contiguous(), n=n, level=1)
+        dm.set(F.TRACER, dom["T"][n - 1].contiguous(), n=n, level=1)
+    c0 = [d64.global_tracer_content(n, 1) for n in range(1, ntr + 1)]
+    d64.tracer_advection_step(1, 1, 2, DTTS)
+    dm.tracer_advection_step(1, 1, 2, DTTS)
+    for n in range(1, ntr + 1):
+        errs.append(_rel_err(_device_copy(dm, F.TRACER, n, 2), _device_copy(d64, F.TRACER, n, 2)))
+        drift64 = max(drift64, abs(d64.global_tracer_content(n, 2) - c0[n - 1]) / abs(c0[n - 1]))
+        driftm = max(driftm, abs(dm.global_tracer_content(n, 2) - c0[n - 1]) / abs(c0[n - 1]))
+    forms["precision"] = {
+        "workload": "same as the headline, precision form (FP32 fluxes and limiters, FP64 state, subcycle, sums)",
+        "value": round(v, 1), "unit": "cell-updates/s", "ms_per_step": round(r["ms"] / args.steps, 3),
+        "vs_plain": round(v / plain_value, 3),
+        "sections_ms_per_step": {k: round(x[0] / args.steps, 3) for k, x in r["sec"].items()},
+        "max_rel_err_vs_fp64_1step": max(errs), "content_rel_change_1step": {"fp64": drift64, "precision": driftm},
+        "gpu_launches": r["launches"], "clocks": r["clocks"]}
+    dm.close()
+    d64.close()
+    del dom
+    torch.cuda.empty_cache()
+    # ---- batched ensemble and serving
+    forms["batched"] = form_batched(args, stream)
+    forms["serving"] = form_serving(args, stream, forms["batched"])
+    return forms
+
+
+def _load_set(specs, precisions):
+    """Generate each domain once and load it once per precision."""
+    from mom5_gb300 import capi, grid, harness
+    sets = {p: [] for p in precisions}
+    for s in specs:
+        dom = grid.make_domain(s, device="cuda")
+        for p in precisions:
+            d = harness.load(dom, options=capi.default_options(barotropic_time_stepping_B=1, precision=p))
+            d.barotropic_init(dtuv=FORM_DT, dtbt=FORM_DTBT)
+            sets[p].append(d)
+        del dom
+    return sets
+
+
+def form_batched(args, stream):
+    import torch
+
+    from mom5_gb300 import capi, serving
+    from mom5_gb300.capi import F
+    specs = serving.ensemble_specs(64)
+    cells = sum(s.ni * s.nj * s.nk for s in specs)
+    ntr = specs[0].ntracers
+    P64, PM = capi.PRECISION_FP64, capi.PRECISION_MIXED
+    sets = _load_set(specs, (P64, PM))
+    for p in sets:
+        for d in sets[p]:
+            d.set_stream(stream.cuda_stream)
+    out = {"workload": f"64 regional domains, nx,ny log-uniform in [64,512], nz in [20,50], {ntr} tracers, "
+                       f"MDFL Sweby + {int(2 * FORM_DT / FORM_DTBT)}-subcycle barotropic, dt={FORM_DT:g}s",
+           "cells": cells}
+    batches = {p: capi.Batch(sets[p]) for p in sets}
+    for b in batches.values():
+        b.set_stream(stream.cuda_stream)
+    # one step of both from the same state: error of the precision form
+    for b in batches.values():
+        b.step(FORM_DT, index=list(range(len(specs))), parity=[0] * len(specs))
+    err = 0.0
+    for i in range(len(specs)):
+        for n in range(1, ntr + 1):
+            err = max(err, _rel_err(_device_copy(sets[PM][i], F.TRACER, n, 2), _device_copy(sets[P64][i], F.TRACER, n, 2)))
+    out["precision_max_rel_err_vs_fp64_1step"] = err
+    for p, name in ((P64, "fp64"), (PM, "precision")):
+        b = batches[p]
+        report = b.autotune(FORM_DT)  # parity-0 trials: level 2 rewritten from level 1
+        par = 1
+        for _ in range(args.warmup):
+            b.step(FORM_DT, parity=par)
+            par ^= 1
+        torch.cuda.synchronize()
+        l0 = b.launches
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            b.step(FORM_DT, parity=par)
+            par ^= 1
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        # the same step as plain per-domain launches, one domain after another
+        tau = 1 + par
+        per = []
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(specs) + 1)]
+        ev[0].record(stream)
+        for i, d in enumerate(sets[p]):
+            d.tracer_advection_step(tau, tau, 3 - tau, FORM_DT)
+            d.update_ocean_barotropic(tau, 3 - tau)
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        per = [ev[i].elapsed_time(ev[i + 1]) for i in range(len(specs))]
+        loop_ms = ev[0].elapsed_time(ev[-1])
+        out[name] = {"value": round(cells / (ms / 1e3), 1), "unit": "cell-updates/s", "ms_per_step": round(ms, 3),
+                     "launches_per_step": (b.launches - l0) // args.steps, "autotune": report,
+                     "per_domain_launches": {"value": round(cells / (loop_ms / 1e3), 1), "ms_per_step": round(loop_ms, 3),
+                                             "p50_ms": round(float(sorted(per)[len(per) // 2]), 3),
+                                             "p99_ms": round(float(sorted(per)[min(len(per) - 1, int(0.99 * len(per)))]), 3)}}
+        out[name]["tuning"] = list(b.tuning)
+    out["precision_vs_fp64"] = round(out["precision"]["value"] / out["fp64"]["value"], 3)
+    for b in batches.values():
+        b.close()
+    for p in sets:
+        for d in sets[p]:
+            d.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def form_serving(args, stream, batched):
+    import numpy as np
+    import torch
+
+    from mom5_gb300 import capi, grid, harness, serving
+    ndom = 256
+    specs = serving.ensemble_specs(ndom, seed=1)
+    srv = serving.Server(FORM_DT, precision=capi.PRECISION_MIXED, slots=3, max_batch=64)
+
+    def load(dom):
+        d = harness.load(dom, options=capi.default_options(barotropic_time_stepping_B=1,
+                                                           precision=capi.PRECISION_MIXED))
+        d.barotropic_init(dtuv=FORM_DT, dtbt=FORM_DTBT)
+        return d
+
+    refused = 0
+    for s in specs:
+        try:
+            srv.add_domain(grid.make_domain(s, device="cuda"), load)
+        except serving.AdmissionError:
+            refused += 1
+    torch.cuda.empty_cache()
+    srv.start()
+    srv.slots[0].batch.autotune(FORM_DT)
+    for s in srv.slots[1:]:
+        s.batch.tuning = srv.slots[0].batch.tuning
+    torch.cuda.synchronize()
+    mean_cells = float(np.mean(srv.cells))
+    cap = batched["precision"]["value"] / mean_cells  # requests/s the batched kernels sustain
+    rng = np.random.default_rng(5)
+    runs = []
+    srv.run([0.0] * 64, list(rng.integers(0, len(srv.domains), 64)))  # warm-up
+    for frac in (0.3, 0.6, 0.9):
+        rate = frac * cap
+        n = int(min(3000, max(200, rate * 2.5)))
+        arr = serving.poisson_arrivals(rate, n, seed=int(frac * 100))
+        res = srv.run(arr, list(rng.integers(0, len(srv.domains), n)))
+        res["offered_rps"] = round(rate, 1)
+        runs.append(res)
+    n = 1024
+    sat = srv.run([0.0] * n, list(rng.integers(0, len(srv.domains), n)))
+    sat["offered_rps"] = "all at t=0"
+    runs.append(sat)
+    srv.close()
+    for d in srv.domains:
+        d.close()
+    torch.cuda.empty_cache()
+    plain = batched["fp64"]["per_domain_launches"]
+    rnd = lambda r: {k: (round(v, 3) if isinstance(v, float) else v) for k, v in r.items()}
+    return {"workload": f"{ndom} resident domains (sizes as the ensemble), step = advection + "
+                        f"{int(2 * FORM_DT / FORM_DTBT)} subcycles, Poisson arrivals, precision form, "
+                        f"3 overlapping batch slots, size buckets", "resident": len(srv.domains),
+            "refused_by_admission": refused, "resident_cells": int(sum(srv.cells)),
+            "runs": [rnd(r) for r in runs],
+            "saturation_cell_updates_per_s": round(sat["cell_updates_per_s"], 1),
+            "plain_fp64_per_domain": {"cell_updates_per_s": plain["value"], "p50_ms": plain["p50_ms"],
+                                      "p99_ms": plain["p99_ms"],
+                                      "note": "ensemble domains stepped one at a time through the one-domain "
+                                              "FP64 entry points (service time, no queueing)"},
+            "vs_plain_fp64": round(sat["cell_updates_per_s"] / plain["value"], 3)}
+
+
 def _cpu_sample(spec):
-    """One host core, one 180x135 block of the workload's grid, two steps."""
-    res = _ref_worker((180, 135, spec.nk, spec.ntracers, -40.0, -6.25, 0.0, 45.0, 77, 0, 2, NTS))
-    return res[1] / res[0], f"C restatement, 1 core, 180x135x{spec.nk} block, {spec.ntracers} tracers, 2 steps"
+    """One host core, one 360x270 block (1/16) of the workload's grid, four steps (about 10 s)."""
+    res = _ref_worker((360, 270, spec.nk, spec.ntracers, -40.0, 27.5, 0.0, 90.0, 77, 0, 4, NTS))
+    return res[1] / res[0], f"C restatement, 1 core, 360x270x{spec.nk} block, {spec.ntracers} tracers, 4 steps"
 
 
 def main():
@@ -345,6 +571,8 @@ def main():
     ap.add_argument("--config", choices=["c2", "c0", "c1", "c2s"], default="c2")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the precision, batched and serving forms reported beside the FP64 headline")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
