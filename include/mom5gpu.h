@@ -67,18 +67,28 @@ enum mom5gpu_field {
   MOM5GPU_UMASK1,        /* Grd%umask(:,:,1) */
   MOM5GPU_TMASKEN_E1,    /* Grd%tmasken(:,:,1,1) */
   MOM5GPU_TMASKEN_N1,    /* Grd%tmasken(:,:,1,2) */
+  MOM5GPU_DXT_DXTER,     /* C-grid face-area ratios (ocean_grids.F90), 2D */
+  MOM5GPU_DYT_DYTER,
+  MOM5GPU_DXT_DXTNR,
+  MOM5GPU_DYT_DYTNR,
   /* 3D grid */
   MOM5GPU_TMASK = 40,    /* Grd%tmask, 3D */
   /* advection velocity (ocean_adv_vel_type, ocean_types.F90:408-417) */
   MOM5GPU_UHRHO_ET = 50, /* 3D */
   MOM5GPU_VHRHO_NT,      /* 3D */
   MOM5GPU_WRHO_BT,       /* 3DW, levels 0..nk */
+  MOM5GPU_DIVERGE_T,     /* 3D, Adv_vel%diverge_t */
   /* thickness (ocean_thickness_type, ocean_types.F90:134-203) */
   MOM5GPU_RHO_DZT = 60,  /* 3D (t) */
   MOM5GPU_RHO_DZTR,      /* 3D */
   MOM5GPU_THICKU,        /* 2D (t) */
   MOM5GPU_THICKEN_E,     /* 2D, Thickness%thicken(:,:,1) */
   MOM5GPU_THICKEN_N,     /* 2D, Thickness%thicken(:,:,2) */
+  MOM5GPU_RHO_DZU,       /* 3D (t), Thickness%rho_dzu (B grid) */
+  MOM5GPU_RHO_DZTEN_E,   /* 3D, Thickness%rho_dzten(:,:,:,1) (C grid) */
+  MOM5GPU_RHO_DZTEN_N,   /* 3D, Thickness%rho_dzten(:,:,:,2) */
+  MOM5GPU_RHO_DZT_TENDENCY, /* 3D, Thickness%rho_dzt_tendency */
+  MOM5GPU_MASS_SOURCE,   /* 3D, Thickness%mass_source */
   /* prognostic tracers (ocean_prog_tracer_type, ocean_types.F90:468-541) */
   MOM5GPU_TRACER = 70,   /* 3D (n)(t) */
   MOM5GPU_TH_TENDENCY,   /* 3D (n) */
@@ -102,6 +112,9 @@ enum mom5gpu_field {
   MOM5GPU_PME,           /* 2D, pme argument */
   MOM5GPU_RIVER,         /* 2D, river argument */
   MOM5GPU_RHO_G,         /* 2D, module rho_g (grav*rho at k=1) */
+  /* velocity (ocean_velocity_type, ocean_types.F90) */
+  MOM5GPU_U_VEL = 110,   /* 3D (t), Velocity%u(:,:,:,1,t) */
+  MOM5GPU_V_VEL,         /* 3D (t), Velocity%u(:,:,:,2,t) */
   MOM5GPU_FIELD_END
 };
 
@@ -208,6 +221,12 @@ int mom5gpu_eta_and_pbot_update(mom5gpu_domain* d, int taum1, int taup1, double 
  * (:3225-3579) or _cgrid (:3601-3965), then the time averages, conv_rho_ud_t,
  * eta_u, ps and grad_ps. */
 int mom5gpu_update_ocean_barotropic(mom5gpu_domain* d, int tau, int taup1);
+/* ocean_advection_velocity (ocean_advection_velocity.F90:568-672), T-cell
+ * part: UHRHO_ET, VHRHO_NT (B grid: BAY/BAX of u*dyu*rho_dzu(tau) over dyte /
+ * dxtn; C grid: u*rho_dzten*face-area ratios), DIVERGE_T and the continuity
+ * WRHO_BT from PME, RIVER, RHO_DZT_TENDENCY and MASS_SOURCE (fields never set
+ * read as zero).  The U-cell fluxes for momentum advection are not computed. */
+int mom5gpu_ocean_advection_velocity(mom5gpu_domain* d, int tau);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Global content of tracer n at a time level, sum of tmask*dat*rho_dzt(level)*T
@@ -236,7 +255,7 @@ long mom5gpu_launch_count(const mom5gpu_domain* d);
  * passes and each barotropic subcycle phase run as one launch over a work list
  * of (domain, block) items, and the precision form runs as one persistent
  * launch that drains a (domain, tile) queue.  Domains of a batch share the
- * precision, the tracer count (<= 8 in FP64, <= 10 in the precision form),
+ * precision, the tracer count (<= 10),
  * MDFL Sweby for every tracer, the B grid, and nts (mom5gpu_barotropic_init);
  * sizes may differ.  A batch borrows the domains: destroy it before them. */
 typedef struct mom5gpu_batch mom5gpu_batch;

@@ -107,6 +107,7 @@ def lib() -> C.CDLL:
             "mom5gpu_eta_and_pbot_tendency": (C.c_int, [vp, C.c_int]),
             "mom5gpu_eta_and_pbot_update": (C.c_int, [vp, C.c_int, C.c_int, C.c_double]),
             "mom5gpu_update_ocean_barotropic": (C.c_int, [vp, C.c_int, C.c_int]),
+            "mom5gpu_ocean_advection_velocity": (C.c_int, [vp, C.c_int]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_check_finite": (C.c_int, [vp, C.c_int, C.c_int, ip]),
@@ -262,6 +263,9 @@ class Domain:
         self.check(lib().mom5gpu_update_ocean_barotropic(self.h, tau, taup1))
 
     # ---- diagnostics ----
+    def ocean_advection_velocity(self, tau):
+        self.check(lib().mom5gpu_ocean_advection_velocity(self.h, tau))
+
     def global_tracer_content(self, n, level) -> float:
         out = C.c_double()
         self.check(lib().mom5gpu_global_tracer_content(self.h, n, level, C.byref(out)))

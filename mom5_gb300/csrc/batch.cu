@@ -312,8 +312,8 @@ int mom5gpu_batch_create(mom5gpu_domain* const* domains, int n, mom5gpu_batch** 
       if (domains[j] == d) return fail(nullptr, MOM5GPU_EINVAL, "batch_create: domain %d listed twice", i);
   }
   int ntr = d0->dims.num_prog_tracers;
-  if (d0->opt.precision == MOM5GPU_PRECISION_FP64 && ntr > 8)
-    return fail(nullptr, MOM5GPU_EUNSUPPORTED, "batch_create: FP64 batches take at most 8 tracers");
+  if (d0->opt.precision == MOM5GPU_PRECISION_FP64 && ntr > kMdflChunk)
+    return fail(nullptr, MOM5GPU_EUNSUPPORTED, "batch_create: FP64 batches take at most %d tracers", kMdflChunk);
   if (d0->opt.precision == MOM5GPU_PRECISION_MIXED && ntr > 10)
     return fail(nullptr, MOM5GPU_EUNSUPPORTED, "batch_create: precision-form batches take at most 10 tracers");
   mom5gpu_batch* b = new (std::nothrow) mom5gpu_batch();

@@ -45,6 +45,12 @@ const FieldInfo kFields[] = {
     {MOM5GPU_GRAD_PS_Y, S2D, false, false},   {MOM5GPU_PATM, S2D, false, false},
     {MOM5GPU_PME, S2D, false, false},         {MOM5GPU_RIVER, S2D, false, false},
     {MOM5GPU_RHO_G, S2D, false, false},
+    {MOM5GPU_DXT_DXTER, S2D, false, false},   {MOM5GPU_DYT_DYTER, S2D, false, false},
+    {MOM5GPU_DXT_DXTNR, S2D, false, false},   {MOM5GPU_DYT_DYTNR, S2D, false, false},
+    {MOM5GPU_DIVERGE_T, S3D, false, false},   {MOM5GPU_RHO_DZU, S3D, false, true},
+    {MOM5GPU_RHO_DZTEN_E, S3D, false, false}, {MOM5GPU_RHO_DZTEN_N, S3D, false, false},
+    {MOM5GPU_RHO_DZT_TENDENCY, S3D, false, false}, {MOM5GPU_MASS_SOURCE, S3D, false, false},
+    {MOM5GPU_U_VEL, S3D, false, true},        {MOM5GPU_V_VEL, S3D, false, true},
 };
 
 // field storage: one block per (field, level) holding every tracer of that level
@@ -730,6 +736,12 @@ int mom5gpu_eta_and_pbot_update(mom5gpu_domain* d, int taum1, int taup1, double 
   int rc = check_levels(d, taum1, taup1);
   if (rc) return rc;
   return launch_eta_update(d, taum1, taup1, dtime);
+}
+
+int mom5gpu_ocean_advection_velocity(mom5gpu_domain* d, int tau) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (tau < 1 || tau > 3) return fail(d, MOM5GPU_EINVAL, "ocean_advection_velocity: tau %d", tau);
+  return launch_advection_velocity(d, tau);
 }
 
 int mom5gpu_update_ocean_barotropic(mom5gpu_domain* d, int tau, int taup1) {

@@ -29,6 +29,34 @@ DEVI double dmin(double a, double b) { return ordbits(a) <= ordbits(b) ? a : b; 
 DEVI double dmax0(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
 DEVI bool dpos(double x) { return __double_as_longlong(x) > 0; }   // x > 0
 
+// Exact shortcuts that keep work off the FP64 pipe (GB300 issues FP64 at
+// 1/64 of the FP32 rate; integer operations are cheap).  Each returns the
+// bit pattern the FP64 operation would produce.
+DEVI bool is_one(double m) { return __double_as_longlong(m) == 0x3ff0000000000000LL; }
+DEVI bool is_zero(double m) { return (__double_as_longlong(m) << 1) == 0; }
+// x*m for a mask value m: 1 -> x (x*1 == x), +-0 -> 0.0 as the callers' selects do
+DEVI double mask_mul(double x, double m) {
+  if (is_one(m)) return x;
+  return x * m;
+}
+// x + 0.0: the same value except that -0 becomes +0
+DEVI double plus_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+// 0.5*x: for a normal x whose exponent field is at least 2 the product is the
+// exponent lowered by one; +-0 is unchanged.  Subnormals, the smallest normals,
+// Inf and NaN take the multiply (decided per warp, so the common case issues no
+// FP64 instruction).
+DEVI double half_exact(double x) {
+  long long b = __double_as_longlong(x);
+  unsigned e = (unsigned)((unsigned long long)b >> 52) & 0x7ffu;
+  bool normal = e - 2u < 0x7fdu;  // 2 <= e <= 0x7fe
+  bool fast = normal || (b << 1) == 0;
+  long long r = normal ? b - (1LL << 52) : b;
+  if (__all_sync(__activemask(), fast)) return __longlong_as_double(r);
+  return fast ? __longlong_as_double(r) : 0.5 * x;
+}
+
 // Sweby limiter psi (ocean_tracer_advect.F90:3868-3878).  With the limiter on
 // the reference forms psi*(1-1) + max(...)*1, with it off psi*1 + max(...)*0;
 // for finite psi both reduce to the selected term exactly.
@@ -42,21 +70,22 @@ DEVI double limiter(double theta, double d0, double d1, double c) {
 
 // Flux of one face given the upwind-side data.  Reference form
 // 0.5*((mf+|mf|)*(Tup + psiP*Rj) + (mf-|mf|)*(Tdn - psiM*Rj)): for mf > 0 the
-// second product is an exact zero and 0.5*(2mf*X) == mf*X exactly.
+// second product is an exact zero and 0.5*(2mf*X) == mf*X exactly; for mf < 0
+// the first is.  Both signs share one division and one limiter evaluation (the
+// operands are selected first), so a warp whose faces carry both signs runs
+// the division once, not once per branch; Tdn - p is computed as Tdn + (-p),
+// which IEEE defines to be the same operation.
 template <bool SWEBY>
 DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, double Tm, double d0, double d1,
                       double c) {
   long long b = __double_as_longlong(mf);
-  if (b > 0) {  // mf > 0: upwind value Tp on the minus side, ratio Rjm / Rj
-    double theta = Rjm / (1.0e-30 + Rj);
-    double psi = limiter<SWEBY>(theta, d0, d1, c);
-    return mf * (Tp + psi * Rj);
-  } else if (b < 0 && b != (long long)0x8000000000000000ULL) {  // mf < 0
-    double theta = Rjp / (1.0e-30 + Rj);
-    double psi = limiter<SWEBY>(theta, d0, d1, c);
-    return mf * (Tm - psi * Rj);
-  }
-  return 0.0;
+  bool pos = b > 0;                                                 // mf > 0
+  bool neg = b < 0 && b != (long long)0x8000000000000000ULL;        // mf < 0
+  double theta = (pos ? Rjm : Rjp) / (1.0e-30 + Rj);
+  double psi = limiter<SWEBY>(theta, d0, d1, c);
+  double p = psi * Rj;
+  double r = mf * ((pos ? Tp : Tm) + (pos ? p : -p));
+  return (pos || neg) ? r : 0.0;
 }
 
 // z pass: one thread per column, march down k.
@@ -303,6 +332,19 @@ DEVI double div_ud(const BtArgs& a, const double* u, const double* v, int i, int
   return ((uh_bay - uhim_bay) + (vh_bax - vhjm_bax)) * a.datr[I2(g, i, j)];
 }
 
+// B-grid DIV_UD from the stored products uh = u*dyu, vh = v*dxu: the same
+// operations as div_ud on the same values, without recomputing the products.
+DEVI double div_ud_bh(const BtArgs& a, const double* uh, const double* vh, int i, int j) {
+  const Geo& g = a.g;
+  if (i < 1 || j < 1) return 0.0;
+  long q = I2(g, i, j), qw = q - 1, qs = q - g.nxd, qsw = qs - 1;
+  double uh_bay = half_exact(uh[q] + uh[qs]);
+  double vh_bax = half_exact(vh[q] + vh[qw]);
+  double uhim_bay = half_exact(uh[qw] + uh[qsw]);
+  double vhjm_bax = half_exact(vh[qs] + vh[qsw]);
+  return ((uh_bay - uhim_bay) + (vh_bax - vhjm_bax)) * a.datr[q];
+}
+
 // image of a halo point under the single-PE full halo update; returns false
 // when the point is left untouched (non-cyclic wall, or a corner of a domain
 // cyclic in one direction only).
@@ -335,6 +377,10 @@ DEVI void bt_init_body(BtArgs a, const double* eta_bar_tau, const double* eta_ta
   a.eta_bt[a.g.n2 + q] = eta_bar_tau[q];
   a.ubt[a.g.n2 + q] = ud_tau[q];
   a.vbt[a.g.n2 + q] = vd_tau[q];
+  if (!a.cgrid) {
+    a.uhb[a.g.n2 + q] = ud_tau[q] * a.dyu[q];
+    a.vhb[a.g.n2 + q] = vd_tau[q] * a.dxu[q];
+  }
   a.steady[q] = a.tmask1[q] * (pme[q] + river[q] + source[q] - eta_smooth[q]);
 }
 
@@ -382,8 +428,10 @@ DEVI void bt_pred_body(BtArgs a, int so, int sn, int bx, int by) {
   long q = I2(g, i, j);
   double en;
   if (a.gamma > 0.0) {
-    double dv = div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j);
-    double tmp = a.tmask1[q] != 0.0 ? (-dv) * a.tmask1[q] : 0.0;
+    double dv = a.cgrid ? div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j)
+                        : div_ud_bh(a, a.uhb + so * g.n2, a.vhb + so * g.n2, i, j);
+    double tm = a.tmask1[q];
+    double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
     en = eo[q] + a.dtbt_gamma_rho0r * (tmp + a.steady[q]);
   } else {
     en = eo[q];
@@ -403,22 +451,29 @@ DEVI void bt_mom_b_body(BtArgs a, int so, int sn, int bx, int by) {
   double gx = 0.0, gy = 0.0;
   if (i <= g.ni && j <= g.nj) {
     const double* ps = a.ps;
-    double p_fay = 0.5 * (ps[q] + ps[I2(g, i, j + 1)]);
-    double p_fax = 0.5 * (ps[q] + ps[I2(g, i + 1, j)]);
-    double pip_fay = 0.5 * (ps[I2(g, i + 1, j)] + ps[I2(g, i + 1, j + 1)]);
-    double pjp_fax = 0.5 * (ps[I2(g, i, j + 1)] + ps[I2(g, i + 1, j + 1)]);
-    bool um = a.umask1[q] != 0.0;
-    gx = um ? (pip_fay - p_fay) * a.dxur[q] * a.umask1[q] : 0.0;
-    gy = um ? (pjp_fax - p_fax) * a.dyur[q] * a.umask1[q] : 0.0;
+    double um = a.umask1[q];
+    if (!is_zero(um)) {
+      double p00 = ps[q], p10 = ps[I2(g, i + 1, j)], p01 = ps[I2(g, i, j + 1)], p11 = ps[I2(g, i + 1, j + 1)];
+      double p_fay = half_exact(p00 + p01);
+      double p_fax = half_exact(p00 + p10);
+      double pip_fay = half_exact(p10 + p11);
+      double pjp_fax = half_exact(p01 + p11);
+      gx = mask_mul((pip_fay - p_fay) * a.dxur[q], um);
+      gy = mask_mul((pjp_fax - p_fax) * a.dyur[q], um);
+    }
   }
   double pf1 = -a.thicku[q] * gx;
   double pf2 = -a.thicku[q] * gy;
   double uo = a.ubt[so * g.n2 + q], vo = a.vbt[so * g.n2 + q];
-  double f = a.f[q];
-  double t1 = uo + a.dtbt * (0.5 * f * vo + pf1 + a.forcing_u[q] + 0.0);
-  double t2 = vo + a.dtbt * (-0.5 * f * uo + pf2 + a.forcing_v[q] + 0.0);
-  a.ubt[sn * g.n2 + q] = a.cori2[q] * (t1 + a.cori1[q] * t2);
-  a.vbt[sn * g.n2 + q] = a.cori2[q] * (t2 - a.cori1[q] * t1);
+  double hf = half_exact(a.f[q]);  // 0.5*f; -0.5*f is its negation
+  double t1 = uo + a.dtbt * plus_zero(hf * vo + pf1 + a.forcing_u[q]);
+  double t2 = vo + a.dtbt * plus_zero((-hf) * uo + pf2 + a.forcing_v[q]);
+  double un = a.cori2[q] * (t1 + a.cori1[q] * t2);
+  double vn = a.cori2[q] * (t2 - a.cori1[q] * t1);
+  a.ubt[sn * g.n2 + q] = un;
+  a.vbt[sn * g.n2 + q] = vn;
+  a.uhb[sn * g.n2 + q] = un * a.dyu[q];
+  a.vhb[sn * g.n2 + q] = vn * a.dxu[q];
 }
 
 // C grid: Coriolis (compute domain) + gradient + momentum (:3780-3830)
@@ -461,8 +516,10 @@ DEVI void bt_corr_body(BtArgs a, int so, int sn, double wgt, int bx, int by) {
   int j = by;
   if (i > g.ni + 1) return;
   long q = I2(g, i, j);
-  double dv = div_ud(a, a.ubt + sn * g.n2, a.vbt + sn * g.n2, i, j);
-  double tmp = a.tmask1[q] != 0.0 ? (-dv) * a.tmask1[q] : 0.0;
+  double dv = a.cgrid ? div_ud(a, a.ubt + sn * g.n2, a.vbt + sn * g.n2, i, j)
+                      : div_ud_bh(a, a.uhb + sn * g.n2, a.vhb + sn * g.n2, i, j);
+  double tm = a.tmask1[q];
+  double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
   double en = a.eta_bt[so * g.n2 + q] + a.dtbt_rho0r * (tmp + a.steady[q]);
   a.eta_bt[sn * g.n2 + q] = en;
   a.eta_bar[q] = a.eta_bar[q] + en;

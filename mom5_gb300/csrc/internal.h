@@ -143,6 +143,9 @@ struct MdflArgs {
 
 // Arguments of the barotropic kernels (fp64_bodies.cuh) for one domain and one
 // (tau, taup1) pair, and the step's other inputs and outputs.
+// Largest number of tracers the FP64 MDFL kernels advect per launch set.
+constexpr int kMdflChunk = 10;
+
 struct BtArgs {
   Geo g;
   int cgrid, nts, stepB;
@@ -158,6 +161,7 @@ struct BtArgs {
   double* cf;  // coriolis_force_bt, 6 planes (component-major within AB level)
   double* ca;  // coriolis_accel_bt, 2 planes
   double *eta_bar, *udrho_u, *udrho_v;  // taup1 accumulators
+  double *uhb, *vhb;  // B grid: ubt*dyu and vbt*dxu, 2 levels like ubt (reuse the C-grid Coriolis planes)
 };
 struct BtExtra {
   const double *eta_bar_tau, *eta_tau, *ud_tau, *vd_tau, *pme, *river, *source, *eta_smooth;
@@ -210,6 +214,7 @@ int launch_tmask_limit(mom5gpu_domain* d, int n, int tau);
 int launch_tmask_limit_ts_same(mom5gpu_domain* d, int nt, int ns);
 int launch_eta_tendency(mom5gpu_domain* d, int tau);
 int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
+int launch_advection_velocity(mom5gpu_domain* d, int tau);
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);
 int launch_content(mom5gpu_domain* d, int n, int level, double* out_host);
 int launch_eta_integral(mom5gpu_domain* d, const double* eta, double* out_host);

@@ -142,12 +142,12 @@ void launch_batch_fp64_advection(const MdflArgs* m, const UpdArgs* u, const Batc
     if (ntr <= 1) adv<true, 1>(m, u, w, TJ, s);
     else if (ntr <= 2) adv<true, 2>(m, u, w, TJ, s);
     else if (ntr <= 4) adv<true, 4>(m, u, w, TJ, s);
-    else adv<true, 8>(m, u, w, TJ, s);
+    else adv<true, kMdflChunk>(m, u, w, TJ, s);
   } else {
     if (ntr <= 1) adv<false, 1>(m, u, w, TJ, s);
     else if (ntr <= 2) adv<false, 2>(m, u, w, TJ, s);
     else if (ntr <= 4) adv<false, 4>(m, u, w, TJ, s);
-    else adv<false, 8>(m, u, w, TJ, s);
+    else adv<false, kMdflChunk>(m, u, w, TJ, s);
   }
 }
 

@@ -93,7 +93,7 @@ static void run_mdfl_n(const MdflArgs& a, cudaStream_t s) {
   if (a.ntr <= 1) run_mdfl<ALL, SWEBY, 1>(a, s);
   else if (a.ntr <= 2) run_mdfl<ALL, SWEBY, 2>(a, s);
   else if (a.ntr <= 4) run_mdfl<ALL, SWEBY, 4>(a, s);
-  else run_mdfl<ALL, SWEBY, 8>(a, s);
+  else run_mdfl<ALL, SWEBY, kMdflChunk>(a, s);
 }
 
 void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s) {
@@ -157,11 +157,15 @@ int make_mdfl_args(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, 
 
 int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,
                 double sweby_limiter) {
-  int rc = ensure_mdfl_scratch(d, ntr < 8 ? ntr : 8);
+  // tracers per launch set: at most kMdflChunk, in chunks of equal size (the
+  // tracer-independent face terms are computed once per chunk)
+  int nchunks = (ntr + kMdflChunk - 1) / kMdflChunk;
+  int csize = (ntr + nchunks - 1) / nchunks;
+  int rc = ensure_mdfl_scratch(d, csize);
   if (rc) return rc;
   ClockScope clk(d, SEC_MDFL);
-  for (int c0 = 0; c0 < ntr; c0 += 8) {
-    int cn = ntr - c0 < 8 ? ntr - c0 : 8;
+  for (int c0 = 0; c0 < ntr; c0 += csize) {
+    int cn = ntr - c0 < csize ? ntr - c0 : csize;
     MdflArgs a;
     rc = make_mdfl_args(d, n_first + c0, cn, taum1, tau, dtime, &a);
     if (rc) return rc;
@@ -665,6 +669,8 @@ int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp)
   a.ps = d->bt + 7 * n2;
   a.cf = d->bt + 8 * n2;
   a.ca = d->bt + 14 * n2;
+  a.uhb = a.cgrid ? nullptr : d->bt + 8 * n2;
+  a.vhb = a.cgrid ? nullptr : d->bt + 10 * n2;
   a.eta_bar = fptr(d, MOM5GPU_ETA_T_BAR, 0, taup1);
   a.udrho_u = fptr(d, MOM5GPU_UDRHO_U, 0, taup1);
   a.udrho_v = fptr(d, MOM5GPU_UDRHO_V, 0, taup1);
@@ -739,6 +745,105 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   k_bt_post3<<<g2, 128, 0, s>>>(a, ps_out, gxo, gyo);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "barotropic");
+}
+
+// ---------------------------------------------------------------------------
+// ocean_advection_velocity, T-cell part (ocean_advection_velocity.F90:568-672)
+// ---------------------------------------------------------------------------
+struct AdvVelArgs {
+  Geo g;
+  int cgrid;
+  const double *u, *v, *rdzu, *rdzten_e, *rdzten_n, *dxu, *dyu, *dyte, *dxtn, *dxt_dxter, *dyt_dyter, *dxt_dxtnr,
+      *dyt_dytnr, *datr, *tmask, *tend, *msrc, *pme, *river;
+  double *ue, *vn, *div, *w;
+};
+
+// face fluxes at every data-domain point: B grid BAY/BAX (ocean_operators.F90:834-902,
+// zero on the first row / column) divided by the face length; C grid products (:645-654)
+__global__ void k_adv_vel_faces(AdvVelArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j), p = I3(g, i, j, k);
+  if (!a.cgrid) {
+    double bay = 0.0, bax = 0.0;
+    if (j >= 1) {
+      long qs = q - g.nxd, ps = p - g.nxd;
+      bay = half_exact(a.u[p] * a.dyu[q] * a.rdzu[p] + a.u[ps] * a.dyu[qs] * a.rdzu[ps]);
+    }
+    if (i >= 1) bax = half_exact(a.v[p] * a.dxu[q] * a.rdzu[p] + a.v[p - 1] * a.dxu[q - 1] * a.rdzu[p - 1]);
+    a.ue[p] = bay / a.dyte[q];
+    a.vn[p] = bax / a.dxtn[q];
+  } else {
+    a.ue[p] = a.u[p] * a.rdzten_e[p] * a.dxt_dxter[q] * a.dyt_dyter[q];
+    a.vn[p] = a.v[p] * a.rdzten_n[p] * a.dxt_dxtnr[q] * a.dyt_dytnr[q];
+  }
+}
+
+// diverge_t = tmask*(BDX_ET + BDY_NT) (ocean_operators.F90:945-958, :1230-1243) and the
+// continuity sum down each column (ocean_advection_velocity.F90:609-625)
+__global__ void k_adv_vel_w(AdvVelArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double w = -(a.pme[q] + a.river[q]);
+  a.w[q] = w;
+  double datr = a.datr[q], dyte = a.dyte[q], dxtn = a.dxtn[q];
+  for (int k = 0; k < g.nk; ++k) {
+    long p = I3(g, i, j, k);
+    double bdx = i >= 1 ? (dyte * a.ue[p] - a.dyte[q - 1] * a.ue[p - 1]) * datr : 0.0;
+    double bdy = j >= 1 ? (dxtn * a.vn[p] - a.dxtn[q - g.nxd] * a.vn[p - g.nxd]) * datr : 0.0;
+    double tm = a.tmask[p];
+    double div = tm * (bdx + bdy);
+    a.div[p] = div;
+    double tmp = a.tend[p] - a.msrc[p];
+    w = (tmp + div + w) * tm;
+    a.w[(long)(k + 1) * g.n2 + q] = w;
+  }
+}
+
+int launch_advection_velocity(mom5gpu_domain* d, int tau) {
+  const Geo& g = d->geo;
+  AdvVelArgs a;
+  a.g = g;
+  a.cgrid = d->dims.horz_grid == MOM5GPU_CGRID;
+  a.u = fptr(d, MOM5GPU_U_VEL, 0, tau);
+  a.v = fptr(d, MOM5GPU_V_VEL, 0, tau);
+  a.rdzu = a.cgrid ? nullptr : fptr(d, MOM5GPU_RHO_DZU, 0, tau);
+  a.rdzten_e = a.cgrid ? fptr(d, MOM5GPU_RHO_DZTEN_E, 0, 0) : nullptr;
+  a.rdzten_n = a.cgrid ? fptr(d, MOM5GPU_RHO_DZTEN_N, 0, 0) : nullptr;
+  a.dxu = fptr(d, MOM5GPU_DXU, 0, 0);
+  a.dyu = fptr(d, MOM5GPU_DYU, 0, 0);
+  a.dyte = fptr(d, MOM5GPU_DYTE, 0, 0);
+  a.dxtn = fptr(d, MOM5GPU_DXTN, 0, 0);
+  a.dxt_dxter = a.cgrid ? fptr(d, MOM5GPU_DXT_DXTER, 0, 0) : nullptr;
+  a.dyt_dyter = a.cgrid ? fptr(d, MOM5GPU_DYT_DYTER, 0, 0) : nullptr;
+  a.dxt_dxtnr = a.cgrid ? fptr(d, MOM5GPU_DXT_DXTNR, 0, 0) : nullptr;
+  a.dyt_dytnr = a.cgrid ? fptr(d, MOM5GPU_DYT_DYTNR, 0, 0) : nullptr;
+  a.datr = fptr(d, MOM5GPU_DATR, 0, 0);
+  a.tmask = fptr(d, MOM5GPU_TMASK, 0, 0);
+  a.tend = fptr(d, MOM5GPU_RHO_DZT_TENDENCY, 0, 0);
+  a.msrc = fptr(d, MOM5GPU_MASS_SOURCE, 0, 0);
+  a.pme = fptr(d, MOM5GPU_PME, 0, 0);
+  a.river = fptr(d, MOM5GPU_RIVER, 0, 0);
+  a.ue = fptr(d, MOM5GPU_UHRHO_ET, 0, 0);
+  a.vn = fptr(d, MOM5GPU_VHRHO_NT, 0, 0);
+  a.div = fptr(d, MOM5GPU_DIVERGE_T, 0, 0);
+  a.w = fptr(d, MOM5GPU_WRHO_BT, 0, 0);
+  const void* need[] = {a.u, a.v, a.dxu, a.dyu, a.dyte, a.dxtn, a.datr, a.tmask, a.tend, a.msrc, a.pme, a.river,
+                        a.ue, a.vn, a.div, a.w};
+  for (const void* p : need)
+    if (!p) return fail(d, MOM5GPU_ESTATE, "ocean_advection_velocity: a field could not be allocated");
+  if (a.cgrid ? !(a.rdzten_e && a.rdzten_n && a.dxt_dxter && a.dyt_dyter && a.dxt_dxtnr && a.dyt_dytnr) : !a.rdzu)
+    return fail(d, MOM5GPU_ESTATE, "ocean_advection_velocity: a thickness or metric field could not be allocated");
+  count_launches(d, 2);
+  dim3 g3((g.ni + 2 + 127) / 128, g.nj + 2, g.nk);
+  k_adv_vel_faces<<<g3, 128, 0, d->stream>>>(a);
+  dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
+  k_adv_vel_w<<<g2, 128, 0, d->stream>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "ocean_advection_velocity");
 }
 
 // ---------------------------------------------------------------------------

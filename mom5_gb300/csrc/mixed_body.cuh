@@ -43,15 +43,14 @@ DEVI float limiter(float theta, float d0, float d1, float c) {
   return fmaxf(0.0f, fminf(fminf(1.0f, lin), c * theta));
 }
 
+// One division and one limiter for either sign of mf (operands selected first);
+// Tm - p is evaluated as Tm + (-p), the same IEEE operation.
 DEVI float face_flux(float mf, float Rjm, float Rj, float Rjp, float Tp, float Tm, float d0, float d1, float c) {
-  if (mf > 0.0f) {
-    float theta = __fdividef(Rjm, 1.0e-30f + Rj);
-    return mf * (Tp + limiter(theta, d0, d1, c) * Rj);
-  } else if (mf < 0.0f) {
-    float theta = __fdividef(Rjp, 1.0e-30f + Rj);
-    return mf * (Tm - limiter(theta, d0, d1, c) * Rj);
-  }
-  return 0.0f;
+  bool pos = mf > 0.0f;
+  float theta = __fdividef(pos ? Rjm : Rjp, 1.0e-30f + Rj);
+  float p = limiter(theta, d0, d1, c) * Rj;
+  float r = mf * ((pos ? Tp : Tm) + (pos ? p : -p));
+  return (pos || mf < 0.0f) ? r : 0.0f;
 }
 
 

@@ -1152,6 +1152,79 @@ void orc_continuity_w(const orc_dims* d, const double* tmask, const double* dyte
   free(bdy);
 }
 
+/* ocean_advection_velocity (ocean_advection_velocity.F90:568-672), T-cell part,
+ * no blobs, OBC or inflow.  B grid (:600-606): uhrho_et = BAY(u*dyu*rho_dzu)/dyte,
+ * vhrho_nt = BAX(v*dxu*rho_dzu)/dxtn, with BAY/BAX (ocean_operators.F90:834-902)
+ * zero on the first row/column of the data domain.  C grid (:645-654):
+ * uhrho_et = u*rho_dzten_e*dxt_dxter*dyt_dyter, vhrho_nt = v*rho_dzten_n*dxt_dxtnr*dyt_dytnr.
+ * Both: diverge_t = tmask*(BDX_ET(uhrho_et) + BDY_NT(vhrho_nt)) and
+ * wrho_bt(0) = -(pme+river), wrho_bt(k) = ((rho_dzt_tendency-mass_source) + diverge_t
+ * + wrho_bt(k-1))*tmask (:614-625, :657-662).  Unused pointers may be NULL. */
+void orc_ocean_advection_velocity(const orc_dims* d, int cgrid, const double* u, const double* v,
+                                  const double* rho_dzu, const double* rho_dzten_e, const double* rho_dzten_n,
+                                  const double* dxu, const double* dyu, const double* dyte, const double* dxtn,
+                                  const double* dxt_dxter, const double* dyt_dyter, const double* dxt_dxtnr,
+                                  const double* dyt_dytnr, const double* datr, const double* tmask,
+                                  const double* rho_dzt_tendency, const double* mass_source, const double* pme,
+                                  const double* river, double* uhrho_et, double* vhrho_nt, double* diverge_t,
+                                  double* wrho_bt) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* a = (double*)calloc(n2, sizeof(double));
+  double* bdx = (double*)calloc(n2, sizeof(double));
+  double* bdy = (double*)calloc(n2, sizeof(double));
+  for (int k = 0; k < nk; ++k) {
+    double* ue = uhrho_et + (size_t)k * n2;
+    double* vn = vhrho_nt + (size_t)k * n2;
+    const double* uk = u + (size_t)k * n2;
+    const double* vk = v + (size_t)k * n2;
+    if (!cgrid) {
+      const double* rz = rho_dzu + (size_t)k * n2;
+      for (size_t q = 0; q < n2; ++q) a[q] = uk[q] * dyu[q] * rz[q];
+      for (int j = 0; j <= nj + 1; ++j)
+        for (int i = 0; i <= ni + 1; ++i) {
+          double bay = j >= 1 ? 0.5 * (a[I2(d, i, j)] + a[I2(d, i, j - 1)]) : 0.0;
+          ue[I2(d, i, j)] = bay / dyte[I2(d, i, j)];
+        }
+      for (size_t q = 0; q < n2; ++q) a[q] = vk[q] * dxu[q] * rz[q];
+      for (int j = 0; j <= nj + 1; ++j)
+        for (int i = 0; i <= ni + 1; ++i) {
+          double bax = i >= 1 ? 0.5 * (a[I2(d, i, j)] + a[I2(d, i - 1, j)]) : 0.0;
+          vn[I2(d, i, j)] = bax / dxtn[I2(d, i, j)];
+        }
+    } else {
+      const double* re = rho_dzten_e + (size_t)k * n2;
+      const double* rn = rho_dzten_n + (size_t)k * n2;
+      for (size_t q = 0; q < n2; ++q) {
+        ue[q] = uk[q] * re[q] * dxt_dxter[q] * dyt_dyter[q];
+        vn[q] = vk[q] * rn[q] * dxt_dxtnr[q] * dyt_dytnr[q];
+      }
+    }
+    memset(bdx, 0, sizeof(double) * n2);
+    memset(bdy, 0, sizeof(double) * n2);
+    for (int j = 0; j <= nj + 1; ++j)
+      for (int i = 1; i <= ni + 1; ++i)
+        bdx[I2(d, i, j)] = (dyte[I2(d, i, j)] * ue[I2(d, i, j)] - dyte[I2(d, i - 1, j)] * ue[I2(d, i - 1, j)]) *
+                           datr[I2(d, i, j)];
+    for (int j = 1; j <= nj + 1; ++j)
+      for (int i = 0; i <= ni + 1; ++i)
+        bdy[I2(d, i, j)] = (dxtn[I2(d, i, j)] * vn[I2(d, i, j)] - dxtn[I2(d, i, j - 1)] * vn[I2(d, i, j - 1)]) *
+                           datr[I2(d, i, j)];
+    const double* tm = tmask + (size_t)k * n2;
+    for (size_t q = 0; q < n2; ++q) diverge_t[(size_t)k * n2 + q] = tm[q] * (bdx[q] + bdy[q]);
+  }
+  for (size_t q = 0; q < n2; ++q) wrho_bt[q] = -(pme[q] + river[q]);
+  for (int k = 0; k < nk; ++k)
+    for (size_t q = 0; q < n2; ++q) {
+      size_t p = (size_t)k * n2 + q;
+      double tmp = rho_dzt_tendency[p] - mass_source[p];
+      wrho_bt[(size_t)(k + 1) * n2 + q] = (tmp + diverge_t[p] + wrho_bt[(size_t)k * n2 + q]) * tmask[p];
+    }
+  free(a);
+  free(bdx);
+  free(bdy);
+}
+
 /* total_tracer (ocean_tracer_diag.F90:2395-2412) with conversion = 1: the
  * per-column sum over k in the reference order, then a global sum.  The
  * global sum here is Neumaier-compensated; result[0] = sum, result[1] = the

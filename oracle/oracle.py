@@ -172,6 +172,25 @@ def continuity_w(d, g):
     return w
 
 
+def ocean_advection_velocity(d, g, u, v, rho_dzu=None, rho_dzten_e=None, rho_dzten_n=None, cgrid=False,
+                             rho_dzt_tendency=None, mass_source=None, pme=None, river=None):
+    """ocean_advection_velocity (T-cell part): returns uhrho_et, vhrho_nt, diverge_t, wrho_bt."""
+    nk = d.nk
+    shp3 = (nk, d.nj + 2, d.ni + 2)
+    z3 = np.zeros(shp3)
+    z2 = np.zeros(shp3[1:])
+    ue, vn, dv = np.zeros(shp3), np.zeros(shp3), np.zeros(shp3)
+    w = np.zeros((nk + 1,) + shp3[1:])
+    # the arrays stay referenced by `keep` until the call returns
+    keep = [np.ascontiguousarray(a if a is not None else z, dtype=np.float64) for a, z in (
+        (u, z3), (v, z3), (rho_dzu, z3), (rho_dzten_e, z3), (rho_dzten_n, z3), (g["dxu"], z2), (g["dyu"], z2),
+        (g["dyte"], z2), (g["dxtn"], z2), (g.get("dxt_dxter"), z2), (g.get("dyt_dyter"), z2),
+        (g.get("dxt_dxtnr"), z2), (g.get("dyt_dytnr"), z2), (g["datr"], z2), (g["tmask"], z3),
+        (rho_dzt_tendency, z3), (mass_source, z3), (pme, z2), (river, z2))]
+    lib().orc_ocean_advection_velocity(C.byref(d), int(cgrid), *[p(a) for a in keep], p(ue), p(vn), p(dv), p(w))
+    return ue, vn, dv, w
+
+
 def total_tracer(d, g, T):
     r = np.zeros(2)
     lib().orc_total_tracer(C.byref(d), p(g["tmask"]), p(g["dat"]), p(g["rho_dzt"]), p(T), p(r))

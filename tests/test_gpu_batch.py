@@ -41,11 +41,10 @@ def snapshot(capi, d, ntr, level):
     return out
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_batch_equals_single_domain_steps(gpu_lib, precision):
+@pytest.mark.parametrize("precision,ntr", [(0, 3), (1, 3), (0, 10), (1, 10)])
+def test_batch_equals_single_domain_steps(gpu_lib, precision, ntr):
     capi = gpu_lib
     from mom5_gb300 import harness
-    ntr = 3
     single, _ = make_domains(capi, harness, precision, SIZES, ntr)
     batched, _ = make_domains(capi, harness, precision, SIZES, ntr)
     b = capi.Batch(batched)

@@ -171,6 +171,25 @@ def test_multistep_advection_matches(env, cyclic_x):
         assert equal(got, ref[n - 1]), f"tracer {n}: {diff_report(got, ref[n - 1])}"
 
 
+@pytest.mark.parametrize("ntr", [7, 10, 13])
+def test_tracer_chunks_match(env, ntr):
+    """Whole-step advection of many tracers: one launch set covers up to 10
+    tracers, more are split into equal chunks (13 -> 7 + 6); 3 steps, every
+    value equal to the oracle."""
+    capi, O = env
+    sp = spec(ni=33, nj=21, nk=7, cyclic_x=True, ntr=ntr, seed=31)
+    dom, d, g, dims = setup(env, sp)
+    dt = 6 * 3600.0
+    tau = 1
+    for s in range(3):
+        d.tracer_advection_step(tau, tau, 3 - tau, dt)
+        tau = 3 - tau
+    ref = _oracle_steps(O, dims, g, 3, dt)
+    for n in range(1, ntr + 1):
+        got = d.get(capi.F.TRACER, n=n, level=tau)
+        assert equal(got, ref[n - 1]), f"tracer {n}: {diff_report(got, ref[n - 1])}"
+
+
 def test_c0_hundred_steps_matches_and_conserves(env):
     """Config C0 (120x80x30, 2 tracers, MDFL Sweby, dt = 3600 s, 100 steps):
     identical to the restatement, global content conserved to roundoff."""
