@@ -57,15 +57,62 @@ DEVI double half_exact(double x) {
   return fast ? __longlong_as_double(r) : 0.5 * x;
 }
 
+// Arithmetic policy of the MDFL bodies: the FP64 instructions.  (Integer-pipe
+// emulation of the FP64 additions and products was measured on C2 and was
+// 13-90% slower than the FP64 pipe at this occupancy, so none is used.)
+struct HwArith {
+  static DEVI double add(double a, double b) { return a + b; }
+  static DEVI double sub(double a, double b) { return a - b; }
+  static DEVI double mul(double a, double b) { return a * b; }
+};
+using MdflFaceArith = HwArith;
+using MdflUpdArith = HwArith;
+
+// a / b from y = RN(1/b), for a divisor shared by many quotients (Markstein's
+// correction: P. Markstein, IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al.,
+// Handbook of Floating-Point Arithmetic, ch. 5): q = RN(a*y), r = a - b*q
+// (one FMA), q1 = RN(q + r*y).  The result is then proven correctly rounded
+// at run time: with r1 = a - b*q1 from one more FMA (exact when q1 is within
+// an ulp), q1 = RN(a/b) when |r1| < |b|*ulp(q1)/2 and q1 is normal and not a
+// power of two.  A lane that cannot prove it (a tie, a binade edge, extreme
+// exponents) takes the division instruction, so the result always equals a / b.
+DEVI double div_recip(double a, double b, double y) {
+  const long long kAbsMask = 0x7fffffffffffffffLL;
+  long long ab = __double_as_longlong(a) & kAbsMask, bb = __double_as_longlong(b) & kAbsMask;
+  int ea = (int)(ab >> 52), eb = (int)(bb >> 52);
+  double q1;
+  bool ok;
+  if (ab == 0) {  // 0 / b = +-0 for finite non-zero b
+    q1 = __longlong_as_double((__double_as_longlong(a) ^ __double_as_longlong(b)) & (long long)0x8000000000000000ULL);
+    ok = eb >= 1 && eb <= 2046;
+  } else {
+    double q = a * y;
+    double r = fma(-q, b, a);
+    q1 = fma(r, y, q);
+    double r1 = fma(-q1, b, a);
+    long long qb = __double_as_longlong(q1) & kAbsMask;
+    int eq = (int)(qb >> 52);
+    int et = eb + eq - 1076;  // exponent of |b| * ulp(q1) / 2
+    ok = ea >= 64 && ea <= 1980 && eb >= 64 && eb <= 1980 && eq >= 64 && eq <= 1980 &&
+         (qb & 0x000fffffffffffffLL) != 0 && et >= 1 && et <= 2046;
+    long long thr = (bb & 0x000fffffffffffffLL) | ((long long)et << 52);
+    ok = ok && (__double_as_longlong(r1) & kAbsMask) < thr;
+  }
+  if (!__all_sync(__activemask(), ok)) {
+    if (!ok) q1 = a / b;
+  }
+  return q1;
+}
+
 // Sweby limiter psi (ocean_tracer_advect.F90:3868-3878).  With the limiter on
 // the reference forms psi*(1-1) + max(...)*1, with it off psi*1 + max(...)*0;
 // for finite psi both reduce to the selected term exactly.
-template <bool SWEBY>
+template <bool SWEBY, class Ar>
 DEVI double limiter(double theta, double d0, double d1, double c) {
-  double lin = d0 + d1 * theta;
+  double lin = Ar::add(d0, Ar::mul(d1, theta));
   if (!SWEBY) return lin;
   double a = dmin(1.0, lin);
-  return dmax0(dmin(a, c * theta));
+  return dmax0(dmin(a, Ar::mul(c, theta)));
 }
 
 // Flux of one face given the upwind-side data.  Reference form
@@ -75,29 +122,34 @@ DEVI double limiter(double theta, double d0, double d1, double c) {
 // operands are selected first), so a warp whose faces carry both signs runs
 // the division once, not once per branch; Tdn - p is computed as Tdn + (-p),
 // which IEEE defines to be the same operation.
-template <bool SWEBY>
+template <bool SWEBY, class Ar>
 DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, double Tm, double d0, double d1,
                       double c) {
   long long b = __double_as_longlong(mf);
   bool pos = b > 0;                                                 // mf > 0
   bool neg = b < 0 && b != (long long)0x8000000000000000ULL;        // mf < 0
-  double theta = (pos ? Rjm : Rjp) / (1.0e-30 + Rj);
-  double psi = limiter<SWEBY>(theta, d0, d1, c);
-  double p = psi * Rj;
-  double r = mf * ((pos ? Tp : Tm) + (pos ? p : -p));
+  double theta = (pos ? Rjm : Rjp) / Ar::add(1.0e-30, Rj);
+  double psi = limiter<SWEBY, Ar>(theta, d0, d1, c);
+  double p = Ar::mul(psi, Rj);
+  double r = Ar::mul(mf, Ar::add(pos ? Tp : Tm, pos ? p : -p));
   return (pos || neg) ? r : 0.0;
 }
 
+// Per-tracer running values live in shared memory, [tracer][thread], so the
+// tracer loops stay rolled (one copy of the loop body in the instruction cache).
+constexpr int kMdflThreads = 128;
+
 // z pass: one thread per column, march down k.
-template <bool ALL, bool SWEBY, int MAXN>
+template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
+  __shared__ double ftp[MAXN][kMdflThreads];
   const Geo& g = a.g;
-  int i = bx * blockDim.x + threadIdx.x + 1;
+  const int t = threadIdx.x;
+  int i = bx * blockDim.x + t + 1;
   int j = by + 1;
   if (i > g.ni) return;
-  double ftp[MAXN];
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) ftp[n] = 0.0;
+#pragma unroll 1
+  for (int n = 0; n < a.ntr; ++n) ftp[n][t] = 0.0;
   double wkm1 = 0.0;
   const double dat = a.dat[I2(g, i, j)];
   const double datr = a.datr[I2(g, i, j)];
@@ -118,26 +170,24 @@ DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
     double wdiff = wkm1 - wk;
     bool fm = mkp1 && mk;
     long p = I3(g, i, j, k);
-#pragma unroll
-    for (int n = 0; n < MAXN; ++n) {
-      if (n < a.ntr) {
-        const double* T = a.T + n * a.tstride;
-        double Tk = T[p];
-        double Tkm1 = T[I3(g, i, j, km1)], Tkp1 = T[I3(g, i, j, kp1)], Tkp2 = T[I3(g, i, j, kp2)];
-        double Rjp = (mkm1 && mk) ? Tkm1 - Tk : 0.0;
-        double Rj = (mk && mkp1) ? Tk - Tkp1 : 0.0;
-        double Rjm = (mkp1 && mkp2) ? Tkp1 - Tkp2 : 0.0;
-        double fbt = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, Tkp1, Tk, d0, d1, c) : 0.0;
-        double tm;
-        if (!ALL) {
-          tm = Tk + dtr * (datr * (fbt - ftp[n]) + Tk * wdiff);
-        } else {
-          double w1 = datr * (fbt - ftp[n]) + Tk * wdiff;
-          tm = Tk + w1 * a.dtime / rdz;
-        }
-        a.tz[n * g.n3 + p] = tm;
-        ftp[n] = fbt;
+#pragma unroll 1
+    for (int n = 0; n < a.ntr; ++n) {
+      const double* T = a.T + n * a.tstride;
+      double Tk = T[p];
+      double Tkm1 = T[I3(g, i, j, km1)], Tkp1 = T[I3(g, i, j, kp1)], Tkp2 = T[I3(g, i, j, kp2)];
+      double Rjp = (mkm1 && mk) ? Ar::sub(Tkm1, Tk) : 0.0;
+      double Rj = (mk && mkp1) ? Ar::sub(Tk, Tkp1) : 0.0;
+      double Rjm = (mkp1 && mkp2) ? Ar::sub(Tkp1, Tkp2) : 0.0;
+      double fbt = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, Tkp1, Tk, d0, d1, c) : 0.0;
+      double div = Au::add(Au::mul(datr, Au::sub(fbt, ftp[n][t])), Au::mul(Tk, wdiff));
+      double tm;
+      if (!ALL) {
+        tm = Au::add(Tk, Au::mul(dtr, div));
+      } else {
+        tm = Au::add(Tk, Au::mul(div, a.dtime) / rdz);
       }
+      a.tz[n * g.n3 + p] = tm;
+      ftp[n][t] = fbt;
     }
     wkm1 = wk;
   }
@@ -168,7 +218,7 @@ DEVI double tm_yhalo(const Geo& g, const double* a, int i, int j, int k) {
 constexpr int kTX = 128;
 
 // x-face i of row (j,k): fluxes of every tracer into sm[n][slot].
-template <bool SWEBY, int MAXN>
+template <bool SWEBY, int MAXN, class Ar>
 DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], int slot) {
   const Geo& g = a.g;
   bool m0 = a.mask2[IM(g, i - 1, j, k)], m1 = a.mask2[IM(g, i, j, k)];
@@ -180,21 +230,19 @@ DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], 
   double d1 = (1.0 - cfl * cfl) * kOneSixth;
   double c = (1.0 - cfl) / (1.0e-30 + cfl);
   bool fm = m1 && m2;
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) {
-    if (n < a.ntr) {
-      const double* tz = a.tz + n * g.n3;
-      double tA = tm_xhalo(g, tz, i - 1, j, k), tB = tm_xhalo(g, tz, i, j, k);
-      double tC = tm_xhalo(g, tz, i + 1, j, k), tD = tm_xhalo(g, tz, i + 2, j, k);
-      double Rjp = (m3 && m2) ? tD - tC : 0.0;
-      double Rj = (m2 && m1) ? tC - tB : 0.0;
-      double Rjm = (m1 && m0) ? tB - tA : 0.0;
-      sm[n][slot] = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
-    }
+#pragma unroll 1
+  for (int n = 0; n < a.ntr; ++n) {
+    const double* tz = a.tz + n * g.n3;
+    double tA = tm_xhalo(g, tz, i - 1, j, k), tB = tm_xhalo(g, tz, i, j, k);
+    double tC = tm_xhalo(g, tz, i + 1, j, k), tD = tm_xhalo(g, tz, i + 2, j, k);
+    double Rjp = (m3 && m2) ? Ar::sub(tD, tC) : 0.0;
+    double Rj = (m2 && m1) ? Ar::sub(tC, tB) : 0.0;
+    double Rjm = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
+    sm[n][slot] = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
   }
 }
 
-template <bool ALL, bool SWEBY, int MAXN>
+template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
   __shared__ double sm[MAXN][kTX + 1];
   const Geo& g = a.g;
@@ -203,8 +251,8 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
   int k = bz;
   int t = threadIdx.x;
   int i = i0 + t;
-  if (i <= g.ni) x_face<SWEBY, MAXN>(a, i, j, k, sm, t + 1);
-  if (t == 0) x_face<SWEBY, MAXN>(a, i0 - 1, j, k, sm, 0);
+  if (i <= g.ni) x_face<SWEBY, MAXN, Ar>(a, i, j, k, sm, t + 1);
+  if (t == 0) x_face<SWEBY, MAXN, Ar>(a, i0 - 1, j, k, sm, 0);
   __syncthreads();
   if (i > g.ni) return;
   bool mk = a.mask2[IM(g, i, j, k)];
@@ -214,27 +262,25 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
   // dtime*tmask*datr/rho_dzt (:3960-3961); tmask_mdfl*datr (:4277)
   double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
   long p = I3(g, i, j, k);
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) {
-    if (n < a.ntr) {
-      double Tk = a.T[n * a.tstride + p];
-      double tm = a.tz[n * g.n3 + p];
-      double s = (sm[n][t] - sm[n][t + 1]) + Tk * divx;
-      if (!ALL) {
-        tm = tm + coef * s;
-      } else {
-        double w1 = mk ? datr * s : 0.0;
-        tm = tm + w1 * a.dtime / rdz;
-      }
-      a.tx[n * g.n3 + p] = tm;
+#pragma unroll 1
+  for (int n = 0; n < a.ntr; ++n) {
+    double Tk = a.T[n * a.tstride + p];
+    double tm = a.tz[n * g.n3 + p];
+    double s = Au::add(Au::sub(sm[n][t], sm[n][t + 1]), Au::mul(Tk, divx));
+    if (!ALL) {
+      tm = Au::add(tm, Au::mul(coef, s));
+    } else {
+      double w1 = mk ? Au::mul(datr, s) : 0.0;
+      tm = Au::add(tm, Au::mul(w1, a.dtime) / rdz);
     }
+    a.tx[n * g.n3 + p] = tm;
   }
 }
 
 // y pass + closing divergence correction + tendency: one thread per (i,k) and a
 // strip of TJ rows, marching north; th_tendency += result.
-template <bool SWEBY, int MAXN>
-DEVI void y_face(const MdflArgs& a, int i, int j, int k, double* f) {
+template <bool SWEBY, int MAXN, class Ar>
+DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThreads], int t) {
   const Geo& g = a.g;
   bool m0 = a.mask2[IM(g, i, j - 1, k)], m1 = a.mask2[IM(g, i, j, k)];
   bool m2 = a.mask2[IM(g, i, j + 1, k)], m3 = a.mask2[IM(g, i, j + 2, k)];
@@ -245,33 +291,33 @@ DEVI void y_face(const MdflArgs& a, int i, int j, int k, double* f) {
   double d1 = (1.0 - cfl * cfl) * kOneSixth;
   double c = (1.0 - cfl) / (1.0e-30 + cfl);
   bool fm = m1 && m2;
-#pragma unroll
-  for (int n = 0; n < MAXN; ++n) {
-    if (n < a.ntr) {
-      const double* tx = a.tx + n * g.n3;
-      double tA = tm_yhalo(g, tx, i, j - 1, k), tB = tm_yhalo(g, tx, i, j, k);
-      double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
-      double Rjp = (m3 && m2) ? tD - tC : 0.0;
-      double Rj = (m2 && m1) ? tC - tB : 0.0;
-      double Rjm = (m1 && m0) ? tB - tA : 0.0;
-      f[n] = fm ? face_flux<SWEBY>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
-    }
+#pragma unroll 1
+  for (int n = 0; n < a.ntr; ++n) {
+    const double* tx = a.tx + n * g.n3;
+    double tA = tm_yhalo(g, tx, i, j - 1, k), tB = tm_yhalo(g, tx, i, j, k);
+    double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
+    double Rjp = (m3 && m2) ? Ar::sub(tD, tC) : 0.0;
+    double Rj = (m2 && m1) ? Ar::sub(tC, tB) : 0.0;
+    double Rjm = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
+    f[n][t] = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
   }
 }
 
-template <bool ALL, bool SWEBY, int MAXN>
+template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
+  __shared__ double fprev[MAXN][kMdflThreads], fcur[MAXN][kMdflThreads];
   const Geo& g = a.g;
-  int i = bx * blockDim.x + threadIdx.x + 1;
+  const int t = threadIdx.x;
+  int i = bx * blockDim.x + t + 1;
   int j0 = by * TJ + 1;
   int k = bz;
   if (i > g.ni) return;
   int j1 = j0 + TJ - 1;
   if (j1 > g.nj) j1 = g.nj;
-  double fprev[MAXN], fcur[MAXN];
-  y_face<SWEBY, MAXN>(a, i, j0 - 1, k, fprev);
+  const double rdtime = 1.0 / a.dtime;
+  y_face<SWEBY, MAXN, Ar>(a, i, j0 - 1, k, fprev, t);
   for (int j = j0; j <= j1; ++j) {
-    y_face<SWEBY, MAXN>(a, i, j, k, fcur);
+    y_face<SWEBY, MAXN, Ar>(a, i, j, k, fcur, t);
     long p = I3(g, i, j, k);
     bool mk = a.mask2[IM(g, i, j, k)];
     double datr = a.datr[I2(g, i, j)];
@@ -281,25 +327,24 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
     double corr = (wk - wkm1j) + datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] -
                                          a.dyte[I2(g, i, j)] * a.uh[p]);
     double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
-#pragma unroll
-    for (int n = 0; n < MAXN; ++n) {
-      if (n < a.ntr) {
-        double Tk = a.T[n * a.tstride + p];
-        double tm = a.tx[n * g.n3 + p];
-        double out;
-        if (!ALL) {
-          tm = tm + coef * (fprev[n] - fcur[n]);
-          tm = tm + a.dtime * Tk / rdz * corr;
-          out = mk ? rdz * (tm - Tk) / a.dtime : 0.0;
-        } else {
-          double w1 = (mk ? datr * (fprev[n] - fcur[n]) : 0.0) + Tk * corr;
-          tm = tm + w1 * a.dtime / rdz;
-          out = mk ? rdz * (tm - Tk) / a.dtime : 0.0;
-        }
-        double* th = a.th + n * g.n3;
-        th[p] = th[p] + out;
-        fprev[n] = fcur[n];
+    const double rrdz = 1.0 / rdz;  // shared by every tracer's division by rho_dzt
+#pragma unroll 1
+    for (int n = 0; n < a.ntr; ++n) {
+      double Tk = a.T[n * a.tstride + p];
+      double tm = a.tx[n * g.n3 + p];
+      double fp = fprev[n][t], fc = fcur[n][t];
+      double out;
+      if (!ALL) {
+        tm = Au::add(tm, Au::mul(coef, Au::sub(fp, fc)));
+        tm = Au::add(tm, Au::mul(div_recip(Au::mul(a.dtime, Tk), rdz, rrdz), corr));
+      } else {
+        double w1 = Au::add(mk ? Au::mul(datr, Au::sub(fp, fc)) : 0.0, Au::mul(Tk, corr));
+        tm = Au::add(tm, div_recip(Au::mul(w1, a.dtime), rdz, rrdz));
       }
+      out = mk ? div_recip(Au::mul(rdz, Au::sub(tm, Tk)), a.dtime, rdtime) : 0.0;
+      double* th = a.th + n * g.n3;
+      th[p] = Au::add(th[p], out);
+      fprev[n][t] = fc;
     }
   }
 }

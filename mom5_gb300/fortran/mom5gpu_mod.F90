@@ -36,7 +36,10 @@ module mom5gpu_c
        F_ETA_T = 80, F_ETA_T_BAR = 81, F_ETA_U = 82, F_UDRHO_U = 83, F_UDRHO_V = 84, &
        F_CONV_RHO_UD_T = 85, F_DETA_DT = 86, F_FORCING_BT_U = 87, F_FORCING_BT_V = 88, &
        F_SOURCE = 89, F_ETA_SMOOTH = 90, F_PS = 91, F_GRAD_PS_X = 92, F_GRAD_PS_Y = 93, &
-       F_PATM = 100, F_PME = 101, F_RIVER = 102, F_RHO_G = 103
+       F_PATM = 100, F_PME = 101, F_RIVER = 102, F_RHO_G = 103, &
+       F_DXT_DXTER = 24, F_DYT_DYTER = 25, F_DXT_DXTNR = 26, F_DYT_DYTNR = 27, F_DIVERGE_T = 53, &
+       F_RHO_DZU = 65, F_RHO_DZTEN_E = 66, F_RHO_DZTEN_N = 67, F_RHO_DZT_TENDENCY = 68, &
+       F_MASS_SOURCE = 69, F_U_VEL = 110, F_V_VEL = 111
 
   type, bind(C) :: mom5gpu_dims
      integer(c_int) :: ni, nj, nk, cyclic_x, cyclic_y, num_prog_tracers, horz_grid
@@ -153,6 +156,12 @@ module mom5gpu_c
        type(c_ptr), value :: dom
        integer(c_int), value :: tau, taup1
      end function
+     integer(c_int) function mom5gpu_ocean_advection_velocity(dom, tau) &
+          bind(C, name="mom5gpu_ocean_advection_velocity")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: tau
+     end function
      integer(c_int) function mom5gpu_global_tracer_content(dom, n, level, total) &
           bind(C, name="mom5gpu_global_tracer_content")
        import :: c_int, c_ptr, c_double
@@ -172,17 +181,20 @@ module mom5gpu_mod
   use mom5gpu_c
   use mpp_mod,          only: mpp_error, FATAL
   use ocean_types_mod,  only: ocean_time_type, ocean_adv_vel_type, ocean_thickness_type, ocean_density_type, &
-                              ocean_prog_tracer_type, ocean_external_mode_type
+                              ocean_prog_tracer_type, ocean_external_mode_type, ocean_velocity_type, &
+                              ocean_lagrangian_type
   implicit none
   private
 
   public :: mom5gpu_attach, mom5gpu_mark_velocity_changed, mom5gpu_mark_state_changed
   public :: horz_advect_tracer, vert_advect_tracer
   public :: update_ocean_barotropic, eta_and_pbot_tendency, eta_and_pbot_update
+  public :: ocean_advection_velocity
 
   type(c_ptr), save :: dom = c_null_ptr
   logical, save :: velocity_dirty = .true.
   logical, save :: state_dirty = .true.
+  logical, save :: velocity_on_device = .false.
 
 contains
 
@@ -220,9 +232,12 @@ contains
     type(ocean_prog_tracer_type), intent(in) :: T_prog(:)
     integer :: n
     if (velocity_dirty) then
-       call check(mom5gpu_set_field(dom, F_UHRHO_ET, 0, 0, Adv_vel%uhrho_et, 0), 'uhrho_et')
-       call check(mom5gpu_set_field(dom, F_VHRHO_NT, 0, 0, Adv_vel%vhrho_nt, 0), 'vhrho_nt')
-       call check(mom5gpu_set_field(dom, F_WRHO_BT, 0, 0, Adv_vel%wrho_bt, 0), 'wrho_bt')
+       if (.not. velocity_on_device) then
+          call check(mom5gpu_set_field(dom, F_UHRHO_ET, 0, 0, Adv_vel%uhrho_et, 0), 'uhrho_et')
+          call check(mom5gpu_set_field(dom, F_VHRHO_NT, 0, 0, Adv_vel%vhrho_nt, 0), 'vhrho_nt')
+          call check(mom5gpu_set_field(dom, F_WRHO_BT, 0, 0, Adv_vel%wrho_bt, 0), 'wrho_bt')
+       endif
+       velocity_on_device = .false.
        call check(mom5gpu_set_field(dom, F_RHO_DZT, 0, Time%tau, Thickness%rho_dzt(:,:,:,Time%tau), 0), 'rho_dzt')
        call check(mom5gpu_set_field(dom, F_RHO_DZT, 0, Time%taum1, Thickness%rho_dzt(:,:,:,Time%taum1), 0), 'rho_dzt')
        call check(mom5gpu_set_field(dom, F_RHO_DZTR, 0, 0, Thickness%rho_dztr, 0), 'rho_dztr')
@@ -328,5 +343,37 @@ contains
     call check(mom5gpu_get_field(dom, F_GRAD_PS_X, 0, 0, Ext_mode%grad_ps(:,:,1), 0), 'grad_ps')
     call check(mom5gpu_get_field(dom, F_GRAD_PS_Y, 0, 0, Ext_mode%grad_ps(:,:,2), 0), 'grad_ps')
   end subroutine update_ocean_barotropic
+
+  ! ocean_advection_velocity.F90:568-579.  Computes the T-cell fluxes on the
+  ! device (they stay there for the advection calls); the U-cell fluxes for
+  ! momentum advection are left to the host's own routine.
+  subroutine ocean_advection_velocity(Velocity, Time, Thickness, Dens, pme, river, Adv_vel, L_system, use_blobs)
+    type(ocean_velocity_type),   intent(in)    :: Velocity
+    type(ocean_time_type),       intent(in)    :: Time
+    type(ocean_thickness_type),  intent(in)    :: Thickness
+    type(ocean_density_type),    intent(in)    :: Dens
+    real, dimension(:,:),        intent(in)    :: pme, river
+    type(ocean_adv_vel_type),    intent(inout) :: Adv_vel
+    type(ocean_lagrangian_type), intent(in)    :: L_system
+    logical,                     intent(in)    :: use_blobs
+    integer(c_int) :: tau
+    if (use_blobs) call mpp_error(FATAL, 'mom5gpu: use_blobs is outside the implemented path')
+    tau = int(Time%tau, c_int)
+    call check(mom5gpu_set_field(dom, F_U_VEL, 0, tau, Velocity%u(:,:,:,1,Time%tau), 0), 'u')
+    call check(mom5gpu_set_field(dom, F_V_VEL, 0, tau, Velocity%u(:,:,:,2,Time%tau), 0), 'v')
+    call check(mom5gpu_set_field(dom, F_RHO_DZU, 0, tau, Thickness%rho_dzu(:,:,:,Time%tau), 0), 'rho_dzu')
+    call check(mom5gpu_set_field(dom, F_RHO_DZT_TENDENCY, 0, 0, Thickness%rho_dzt_tendency, 0), 'rho_dzt_tendency')
+    call check(mom5gpu_set_field(dom, F_MASS_SOURCE, 0, 0, Thickness%mass_source, 0), 'mass_source')
+    call check(mom5gpu_set_field(dom, F_PME, 0, 0, pme, 0), 'pme')
+    call check(mom5gpu_set_field(dom, F_RIVER, 0, 0, river, 0), 'river')
+    call check(mom5gpu_ocean_advection_velocity(dom, tau), 'ocean_advection_velocity')
+    call check(mom5gpu_get_field(dom, F_UHRHO_ET, 0, 0, Adv_vel%uhrho_et, 0), 'uhrho_et')
+    call check(mom5gpu_get_field(dom, F_VHRHO_NT, 0, 0, Adv_vel%vhrho_nt, 0), 'vhrho_nt')
+    call check(mom5gpu_get_field(dom, F_WRHO_BT, 0, 0, Adv_vel%wrho_bt, 0), 'wrho_bt')
+    call check(mom5gpu_get_field(dom, F_DIVERGE_T, 0, 0, Adv_vel%diverge_t, 0), 'diverge_t')
+    ! the device copy of the fluxes is current: the next advection call need
+    ! not push them again (thickness is still pushed)
+    velocity_on_device = .true.
+  end subroutine ocean_advection_velocity
 
 end module mom5gpu_mod

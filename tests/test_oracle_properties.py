@@ -45,6 +45,27 @@ def test_flow_is_divergence_free(O, cyclic_x):
                 assert abs(g["wrho_bt"][kmt[j, i], j, i]) <= 1e-10 * scale
 
 
+def test_advection_velocity_restatements_agree(O):
+    """The full ocean_advection_velocity restatement (ocean_advection_velocity.F90:
+    600-627) and the continuity-only one give the same wrho_bt for the same face
+    fluxes when the thickness tendency and mass source vanish; on the C grid with
+    unit face-area ratios uhrho_et = u*rho_dzten exactly (:645-654)."""
+    dom, g, d = load(O, small(seed=4))
+    rng = np.random.default_rng(3)
+    shp = g["uhrho_et"].shape
+    u, v = rng.standard_normal(shp), rng.standard_normal(shp)
+    rz = 1035.0 * (5.0 + rng.random(shp))
+    ue, vn, dv, w = O.ocean_advection_velocity(d, g, u, v, rho_dzu=rz)
+    g2 = dict(g, uhrho_et=ue, vhrho_nt=vn)
+    assert np.array_equal(w, O.continuity_w(d, g2))
+    # BAY / BAX vanish on the first row / column of the data domain
+    assert np.all(ue[:, 0, :] == 0.0) and np.all(vn[:, :, 0] == 0.0)
+    one = np.ones(shp[1:])
+    g3 = dict(g, dxt_dxter=one, dyt_dyter=one, dxt_dxtnr=one, dyt_dytnr=one)
+    ue, vn, dv, w = O.ocean_advection_velocity(d, g3, u, v, rho_dzten_e=rz, rho_dzten_n=2 * rz, cgrid=True)
+    assert np.array_equal(ue, u * rz) and np.array_equal(vn, v * (2 * rz))
+
+
 @pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker"])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
