@@ -262,6 +262,7 @@ def run_ours(args, rank, world):
     d.set_stream(stream.cuda_stream)
 
     state = {"tau": 1}
+    tune = d.autotune(DTTS) if ntr > 0 else None  # trial steps 1 -> 2; the timed steps start at level 1
     if world > 1:
         torch.distributed.barrier()
     r = _time_domain(d, stream, ntr, args.steps, args.warmup, state, local)
@@ -340,7 +341,7 @@ def run_ours(args, rank, world):
                                   f"{'FP64 drop-in' if prec == capi.PRECISION_FP64 else 'precision form'}",
                       "cells": cells, "tracers": ntr, "subcycles": nts, "parallelism": f"replicas x{world}",
                       "l2": "inputs larger than L2 (tracer state alone %.1f GB)" % (2 * ntr * cells * 8 / 1e9)},
-           "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+           "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "autotune": tune,
            "sections_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sec.items()},
            "barotropic_roofline": {"achieved": round(bt_achieved, 1), "unit": "GB/s", "peak": peak,
                                    "frac": round(bt_achieved / peak, 4), "note": "streaming model, 224 B/column/subcycle"},
@@ -375,6 +376,7 @@ def run_forms(args, dom, d64, plain_value, stream):
     dm = harness.load(dom, options=capi.default_options(barotropic_time_stepping_B=1, precision=capi.PRECISION_MIXED))
     dm.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
     dm.set_stream(stream.cuda_stream)
+    tune = dm.autotune(DTTS)
     r = _time_domain(dm, stream, ntr, args.steps, args.warmup, {"tau": 1})
     v = cells * args.steps / (r["ms"] / 1e3)
     # error against the FP64 drop-in (equal to the oracle bit for bit), one step from the same state
@@ -395,7 +397,7 @@ def run_forms(args, dom, d64, plain_value, stream):
         "vs_plain": round(v / plain_value, 3),
         "sections_ms_per_step": {k: round(x[0] / args.steps, 3) for k, x in r["sec"].items()},
         "max_rel_err_vs_fp64_1step": max(errs), "content_rel_change_1step": {"fp64": drift64, "precision": driftm},
-        "gpu_launches": r["launches"], "clocks": r["clocks"]}
+        "gpu_launches": r["launches"], "clocks": r["clocks"], "autotune": tune}
     dm.close()
     d64.close()
     del dom

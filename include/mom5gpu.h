@@ -48,6 +48,9 @@ extern "C" {
 #define MOM5GPU_CGRID 2
 /* tracer advection schemes, ocean_parameters.F90:148-162 (implemented subset) */
 #define MOM5GPU_ADVECT_UPWIND 1
+#define MOM5GPU_ADVECT_2ND_ORDER 2
+#define MOM5GPU_ADVECT_4TH_ORDER 3
+#define MOM5GPU_ADVECT_6TH_ORDER 4
 #define MOM5GPU_ADVECT_QUICKER 5
 #define MOM5GPU_ADVECT_MDFL_SWEBY 9
 #define MOM5GPU_ADVECT_DST_LINEAR 10
@@ -73,6 +76,8 @@ enum mom5gpu_field {
   MOM5GPU_DYT_DYTNR,
   /* 3D grid */
   MOM5GPU_TMASK = 40,    /* Grd%tmask, 3D */
+  MOM5GPU_TMASKEN_E,     /* Grd%tmasken(:,:,:,1), 3D */
+  MOM5GPU_TMASKEN_N,     /* Grd%tmasken(:,:,:,2), 3D */
   /* advection velocity (ocean_adv_vel_type, ocean_types.F90:408-417) */
   MOM5GPU_UHRHO_ET = 50, /* 3D */
   MOM5GPU_VHRHO_NT,      /* 3D */
@@ -93,6 +98,9 @@ enum mom5gpu_field {
   MOM5GPU_TRACER = 70,   /* 3D (n)(t) */
   MOM5GPU_TH_TENDENCY,   /* 3D (n) */
   MOM5GPU_TMASK_LIMIT,   /* 3D (n) */
+  MOM5GPU_TPME,          /* 2D (n), T_prog(n)%tpme */
+  MOM5GPU_TRACER_ETA_SMOOTH, /* 2D (n), T_prog(n)%eta_smooth */
+  MOM5GPU_PBOT_SMOOTH,   /* 2D (n), T_prog(n)%pbot_smooth */
   /* external mode (ocean_external_mode_type, ocean_types.F90:591-637) */
   MOM5GPU_ETA_T = 80,    /* 2D (t) */
   MOM5GPU_ETA_T_BAR,     /* 2D (t) */
@@ -115,6 +123,12 @@ enum mom5gpu_field {
   /* velocity (ocean_velocity_type, ocean_types.F90) */
   MOM5GPU_U_VEL = 110,   /* 3D (t), Velocity%u(:,:,:,1,t) */
   MOM5GPU_V_VEL,         /* 3D (t), Velocity%u(:,:,:,2,t) */
+  MOM5GPU_ACCEL_U,       /* 3D, Velocity%accel(:,:,:,1) */
+  MOM5GPU_ACCEL_V,       /* 3D, Velocity%accel(:,:,:,2) */
+  MOM5GPU_SMF_U,         /* 2D, Velocity%smf(:,:,1) */
+  MOM5GPU_SMF_V,
+  MOM5GPU_BMF_U,         /* 2D, Velocity%bmf(:,:,1) */
+  MOM5GPU_BMF_V,
   MOM5GPU_FIELD_END
 };
 
@@ -142,6 +156,9 @@ typedef struct mom5gpu_options {
   double grav;                    /* 9.80 */
   /* this library */
   int precision;                  /* MOM5GPU_PRECISION_FP64 (default) or _MIXED */
+  /* ocean_barotropic_nml, ocean_barotropic.F90:528-529 */
+  int zero_forcing_bt;            /* default 0 */
+  int zero_nonlinear_forcing_bt;  /* default 0 */
 } mom5gpu_options;
 
 typedef struct mom5gpu_domain mom5gpu_domain;
@@ -212,6 +229,12 @@ int mom5gpu_update_tracer(mom5gpu_domain* d, int n, int taum1, int taup1, double
  * call: zero th_tendency, horizontal + vertical advection, explicit update,
  * halo update. */
 int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime);
+/* Time the candidate launch shapes of mom5gpu_tracer_advection_step on this
+ * domain (precision form: tile height 32 or 16 rows; FP64: y-pass rows per
+ * thread 2..16) and keep the fastest.  The trials step taum1 = tau = 1 to
+ * taup1 = 2: time level 2 of the tracers and th_tendency are overwritten.
+ * A summary is written to report (may be NULL). */
+int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len);
 /* eta_and_pbot_tendency (ocean_barotropic.F90:2668-2734), depth-based. */
 int mom5gpu_eta_and_pbot_tendency(mom5gpu_domain* d, int tau);
 /* eta_and_pbot_update (ocean_barotropic.F90:2290-2385), depth-based, no OBC. */
@@ -227,6 +250,17 @@ int mom5gpu_update_ocean_barotropic(mom5gpu_domain* d, int tau, int taup1);
  * WRHO_BT from PME, RIVER, RHO_DZT_TENDENCY and MASS_SOURCE (fields never set
  * read as zero).  The U-cell fluxes for momentum advection are not computed. */
 int mom5gpu_ocean_advection_velocity(mom5gpu_domain* d, int tau);
+/* Surface and bottom source terms of the explicit tracer step
+ * (ocean_tracer.F90:2318-2336): th_tendency(k=1) += tmask*(pme*tpme + eta_smooth)
+ * and th_tendency(kmt) += tmask*pbot_smooth on the compute domain, for tracer
+ * n (0 = every tracer).  Reads PME and the per-tracer TPME, TRACER_ETA_SMOOTH
+ * and PBOT_SMOOTH (zero until set); needs mom5gpu_set_vertical_grid (kmt). */
+int mom5gpu_tracer_boundary_terms(mom5gpu_domain* d, int n);
+/* ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141) without the
+ * optional barotropic friction: FORCING_BT_U/V = sum_k tmasken*accel +
+ * tmasken(k=1)*(smf - bmf) on the compute domain, zero halo then the single-PE
+ * halo update; honours zero_forcing_bt and zero_nonlinear_forcing_bt. */
+int mom5gpu_ocean_barotropic_forcing(mom5gpu_domain* d);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Global content of tracer n at a time level, sum of tmask*dat*rho_dzt(level)*T

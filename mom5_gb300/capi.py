@@ -24,6 +24,7 @@ OK = 0
 EINVAL, ENOMEM, ECUDA, ESTATE, ECFL, ENUMERIC, ETIMEDOUT, EUNSUPPORTED, EFULL = range(-1, -10, -1)
 BGRID, CGRID = 1, 2
 ADVECT_UPWIND, ADVECT_QUICKER, ADVECT_MDFL_SWEBY, ADVECT_DST_LINEAR = 1, 5, 9, 10
+ADVECT_2ND_ORDER, ADVECT_4TH_ORDER, ADVECT_6TH_ORDER = 2, 3, 4
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 
@@ -62,7 +63,8 @@ class Options(C.Structure):
                 ("zero_tracer_advect_horz", C.c_int), ("zero_tracer_advect_vert", C.c_int),
                 ("barotropic_time_stepping_A", C.c_int), ("barotropic_time_stepping_B", C.c_int),
                 ("initsum_with_bar", C.c_int), ("pred_corr_gamma", C.c_double), ("rho0", C.c_double),
-                ("grav", C.c_double), ("precision", C.c_int)]
+                ("grav", C.c_double), ("precision", C.c_int), ("zero_forcing_bt", C.c_int),
+                ("zero_nonlinear_forcing_bt", C.c_int)]
 
 
 class Mom5GpuError(RuntimeError):
@@ -108,6 +110,9 @@ def lib() -> C.CDLL:
             "mom5gpu_eta_and_pbot_update": (C.c_int, [vp, C.c_int, C.c_int, C.c_double]),
             "mom5gpu_update_ocean_barotropic": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_ocean_advection_velocity": (C.c_int, [vp, C.c_int]),
+            "mom5gpu_autotune": (C.c_int, [vp, C.c_double, C.c_char_p, C.c_size_t]),
+            "mom5gpu_tracer_boundary_terms": (C.c_int, [vp, C.c_int]),
+            "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_check_finite": (C.c_int, [vp, C.c_int, C.c_int, ip]),
@@ -263,6 +268,17 @@ class Domain:
         self.check(lib().mom5gpu_update_ocean_barotropic(self.h, tau, taup1))
 
     # ---- diagnostics ----
+    def autotune(self, dtime) -> str:
+        buf = C.create_string_buffer(1024)
+        self.check(lib().mom5gpu_autotune(self.h, float(dtime), buf, 1024))
+        return buf.value.decode()
+
+    def tracer_boundary_terms(self, n=0):
+        self.check(lib().mom5gpu_tracer_boundary_terms(self.h, n))
+
+    def ocean_barotropic_forcing(self):
+        self.check(lib().mom5gpu_ocean_barotropic_forcing(self.h))
+
     def ocean_advection_velocity(self, tau):
         self.check(lib().mom5gpu_ocean_advection_velocity(self.h, tau))
 

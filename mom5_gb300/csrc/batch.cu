@@ -180,9 +180,9 @@ int enqueue_step(mom5gpu_batch* b, const BatchWork& w, const std::vector<std::pa
       launches += 1;
     }
   }
-  launch_batch_barotropic_loop(b->d_bt, b->d_btx, w, b->nts, b->stepB, s);
+  launch_batch_barotropic_loop(b->d_bt, b->d_btx, w, b->nts, b->stepB, b->prec == MOM5GPU_PRECISION_MIXED, s);
   launch_batch_barotropic_post(b->d_bt, b->d_btx, w, b->nts, b->stepB, 1, s);
-  launches += 2 + 3L * b->nts;
+  launches += 2 + 3L * b->nts + (b->prec == MOM5GPU_PRECISION_MIXED ? 1 : 0);
   auto fill = [&](int field) {
     for (auto& it : list) {
       mom5gpu_domain* d = b->doms[it.first];

@@ -51,6 +51,12 @@ const FieldInfo kFields[] = {
     {MOM5GPU_RHO_DZTEN_E, S3D, false, false}, {MOM5GPU_RHO_DZTEN_N, S3D, false, false},
     {MOM5GPU_RHO_DZT_TENDENCY, S3D, false, false}, {MOM5GPU_MASS_SOURCE, S3D, false, false},
     {MOM5GPU_U_VEL, S3D, false, true},        {MOM5GPU_V_VEL, S3D, false, true},
+    {MOM5GPU_TMASKEN_E, S3D, false, false},   {MOM5GPU_TMASKEN_N, S3D, false, false},
+    {MOM5GPU_TPME, S2D, true, false},         {MOM5GPU_TRACER_ETA_SMOOTH, S2D, true, false},
+    {MOM5GPU_PBOT_SMOOTH, S2D, true, false},  {MOM5GPU_ACCEL_U, S3D, false, false},
+    {MOM5GPU_ACCEL_V, S3D, false, false},     {MOM5GPU_SMF_U, S2D, false, false},
+    {MOM5GPU_SMF_V, S2D, false, false},       {MOM5GPU_BMF_U, S2D, false, false},
+    {MOM5GPU_BMF_V, S2D, false, false},
 };
 
 // field storage: one block per (field, level) holding every tracer of that level
@@ -175,6 +181,8 @@ void mom5gpu_default_options(mom5gpu_options* o) {
   o->rho0 = 1035.0;
   o->grav = 9.80;
   o->precision = MOM5GPU_PRECISION_FP64;
+  o->zero_forcing_bt = 0;
+  o->zero_nonlinear_forcing_bt = 0;
 }
 
 const char* mom5gpu_strerror(int s) {
@@ -244,6 +252,7 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
     if (p) cudaFree(p);
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
+  if (d->kmt_d) cudaFree(d->kmt_d);
   if (d->red_h) cudaFreeHost(d->red_h);
   for (auto& c : d->clocks) {
     cudaEventDestroy(c.a);
@@ -332,12 +341,17 @@ int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz, int vert, doub
   if (!d) return MOM5GPU_EINVAL;
   if (n < 1 || n > d->dims.num_prog_tracers) return fail(d, MOM5GPU_EINVAL, "set_tracer_scheme: tracer %d", n);
   auto ok = [](int s) {
-    return s == MOM5GPU_ADVECT_UPWIND || s == MOM5GPU_ADVECT_QUICKER || s == MOM5GPU_ADVECT_MDFL_SWEBY ||
+    return s == MOM5GPU_ADVECT_UPWIND || s == MOM5GPU_ADVECT_2ND_ORDER || s == MOM5GPU_ADVECT_4TH_ORDER ||
+           s == MOM5GPU_ADVECT_6TH_ORDER || s == MOM5GPU_ADVECT_QUICKER || s == MOM5GPU_ADVECT_MDFL_SWEBY ||
            s == MOM5GPU_ADVECT_DST_LINEAR;
   };
   if (!ok(horz) || !ok(vert))
-    return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: scheme %d/%d is outside upwind, quicker, mdfl_sweby, "
-                                          "dst_linear", horz, vert);
+    return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: scheme %d/%d is outside upwind, 2nd/4th/6th order, "
+                                          "quicker, mdfl_sweby, dst_linear", horz, vert);
+  // a halo of 3 (6th order) needs at least 3 compute points across a cyclic direction
+  if ((horz == MOM5GPU_ADVECT_6TH_ORDER || horz == MOM5GPU_ADVECT_4TH_ORDER) &&
+      ((d->geo.cx && d->geo.ni < 3) || (d->geo.cy && d->geo.nj < 3)))
+    return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: 4th/6th order needs ni, nj >= 3 across cyclic edges");
   // ocean_tracer.F90:1076-1087: a 3-D scheme must be chosen for both directions
   bool h3 = horz == MOM5GPU_ADVECT_MDFL_SWEBY || horz == MOM5GPU_ADVECT_DST_LINEAR;
   bool v3 = vert == MOM5GPU_ADVECT_MDFL_SWEBY || vert == MOM5GPU_ADVECT_DST_LINEAR;
@@ -590,7 +604,8 @@ int mom5gpu_barotropic_init(mom5gpu_domain* d, double dtuv, double dtbt) {
   }
   if ((rc = upload_new(d, &d->cori1, c1)) || (rc = upload_new(d, &d->cori2, c2))) return rc;
   if (!d->bt) {
-    size_t bytes = sizeof(double) * 16 * (size_t)g.n2;
+    int planes = kBtPlanes + (d->opt.precision == MOM5GPU_PRECISION_MIXED ? kBtFastPlanes : 0);
+    size_t bytes = sizeof(double) * planes * (size_t)g.n2;
     cudaError_t e = cudaMalloc(&d->bt, bytes);
     if (e != cudaSuccess) return cuda_fail(d, e, "barotropic scratch");
     cudaMemsetAsync(d->bt, 0, bytes, d->stream);
@@ -634,6 +649,9 @@ int mom5gpu_horz_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
   }
   switch (d->scheme[n - 1].horz) {
     case MOM5GPU_ADVECT_UPWIND: return launch_upwind_horz(d, n, taum1);
+    case MOM5GPU_ADVECT_2ND_ORDER: return launch_centred(d, n, tau, 2, true);
+    case MOM5GPU_ADVECT_4TH_ORDER: return launch_centred(d, n, tau, 4, true);
+    case MOM5GPU_ADVECT_6TH_ORDER: return launch_centred(d, n, tau, 6, true);
     case MOM5GPU_ADVECT_QUICKER:
       if (!d->qw.quick_x) return fail(d, MOM5GPU_ESTATE, "quicker needs mom5gpu_set_vertical_grid before init");
       return launch_quicker_horz(d, n, taum1, tau);
@@ -655,6 +673,9 @@ int mom5gpu_vert_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
   if (d->opt.advect_sweby_all) return MOM5GPU_OK;
   switch (d->scheme[n - 1].vert) {
     case MOM5GPU_ADVECT_UPWIND: return launch_upwind_vert(d, n, taum1);
+    case MOM5GPU_ADVECT_2ND_ORDER: return launch_centred(d, n, tau, 2, false);
+    case MOM5GPU_ADVECT_4TH_ORDER: return launch_centred(d, n, tau, 4, false);
+    case MOM5GPU_ADVECT_6TH_ORDER: return launch_centred(d, n, tau, 6, false);
     case MOM5GPU_ADVECT_QUICKER:
       if (!d->qw.quick_z) return fail(d, MOM5GPU_ESTATE, "quicker needs mom5gpu_set_vertical_grid before init");
       return launch_quicker_vert(d, n, taum1, tau);
@@ -725,6 +746,62 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
   return launch_update_tracer(d, 1, ntr, taum1, taup1, dtime);
 }
 
+int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (!d->advect_ready) return fail(d, MOM5GPU_ESTATE, "autotune before mom5gpu_tracer_advect_init");
+  bool mixed = d->opt.precision == MOM5GPU_PRECISION_MIXED;
+  // candidate launch shapes: precision-form tile height; FP64 y-pass rows per thread
+  const int kRows[] = {32, 16};
+  const int kTj[] = {2, 4, 8, 16};
+  int ncand = mixed ? 2 : 4;
+  cudaEvent_t t0, t1;
+  if (cudaEventCreate(&t0) != cudaSuccess) return fail(d, MOM5GPU_ECUDA, "autotune events");
+  if (cudaEventCreate(&t1) != cudaSuccess) {
+    cudaEventDestroy(t0);
+    return fail(d, MOM5GPU_ECUDA, "autotune events");
+  }
+  std::string rep;
+  double best = 1e30;
+  int bestc = 0, rc = MOM5GPU_OK;
+  for (int c = 0; c < ncand && rc == MOM5GPU_OK; ++c) {
+    if (mixed) d->tune_mixed_rows = kRows[c];
+    else d->tune_y_tj = kTj[c];
+    rc = mom5gpu_tracer_advection_step(d, 1, 1, 2, dtime);  // warm-up
+    cudaEventRecord(t0, d->stream);
+    for (int r = 0; r < 3 && rc == MOM5GPU_OK; ++r) rc = mom5gpu_tracer_advection_step(d, 1, 1, 2, dtime);
+    cudaEventRecord(t1, d->stream);
+    if (rc) break;
+    cudaError_t e = cudaEventSynchronize(t1);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(d, e, "autotune");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    ms /= 3.f;
+    char line[96];
+    snprintf(line, sizeof(line), mixed ? "rows=%d: %.3f ms; " : "tj=%d: %.3f ms; ", mixed ? kRows[c] : kTj[c], ms);
+    rep += line;
+    if (ms < best) {
+      best = ms;
+      bestc = c;
+    }
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (mixed) d->tune_mixed_rows = kRows[bestc];
+  else d->tune_y_tj = kTj[bestc];
+  if (rc) return rc;
+  char line[64];
+  snprintf(line, sizeof(line), mixed ? "chosen rows=%d" : "chosen tj=%d", mixed ? kRows[bestc] : kTj[bestc]);
+  rep += line;
+  if (report && report_len) {
+    strncpy(report, rep.c_str(), report_len - 1);
+    report[report_len - 1] = 0;
+  }
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_eta_and_pbot_tendency(mom5gpu_domain* d, int tau) {
   if (!d) return MOM5GPU_EINVAL;
   if (tau < 1 || tau > 3) return fail(d, MOM5GPU_EINVAL, "eta_and_pbot_tendency: tau %d", tau);
@@ -742,6 +819,22 @@ int mom5gpu_ocean_advection_velocity(mom5gpu_domain* d, int tau) {
   if (!d) return MOM5GPU_EINVAL;
   if (tau < 1 || tau > 3) return fail(d, MOM5GPU_EINVAL, "ocean_advection_velocity: tau %d", tau);
   return launch_advection_velocity(d, tau);
+}
+
+int mom5gpu_tracer_boundary_terms(mom5gpu_domain* d, int n) {
+  if (!d) return MOM5GPU_EINVAL;
+  int ntr = d->dims.num_prog_tracers;
+  if (n < 0 || n > ntr) return fail(d, MOM5GPU_EINVAL, "tracer_boundary_terms: tracer %d", n);
+  if ((int)d->kmt_h.size() != (int)d->geo.n2)
+    return fail(d, MOM5GPU_ESTATE, "tracer_boundary_terms before mom5gpu_set_vertical_grid");
+  int rc = MOM5GPU_OK;
+  for (int m = (n == 0 ? 1 : n); m <= (n == 0 ? ntr : n) && rc == MOM5GPU_OK; ++m) rc = launch_tracer_boundary(d, m);
+  return rc;
+}
+
+int mom5gpu_ocean_barotropic_forcing(mom5gpu_domain* d) {
+  if (!d) return MOM5GPU_EINVAL;
+  return launch_barotropic_forcing(d);
 }
 
 int mom5gpu_update_ocean_barotropic(mom5gpu_domain* d, int tau, int taup1) {

@@ -84,6 +84,7 @@ struct mom5gpu_domain {
   float* mixed_scr = nullptr;  // precision-form scratch
   size_t mixed_cap = 0;
   double* bt = nullptr;        // barotropic scratch
+  int* kmt_d = nullptr;        // device copy of kmt (uploaded on first use)
   double* red = nullptr;       // reduction scratch (device)
   double* red_h = nullptr;     // pinned host result
   int* flag = nullptr;         // device flag word
@@ -162,7 +163,10 @@ struct BtArgs {
   double* ca;  // coriolis_accel_bt, 2 planes
   double *eta_bar, *udrho_u, *udrho_v;  // taup1 accumulators
   double *uhb, *vhb;  // B grid: ubt*dyu and vbt*dxu, 2 levels like ubt (reuse the C-grid Coriolis planes)
+  double* btf;        // precision form, B grid: folded step coefficients (bt_fast_body.cuh), else nullptr
 };
+// planes of barotropic scratch: 16 for the exact path, 9 more for the precision form
+constexpr int kBtPlanes = 16, kBtFastPlanes = 9;
 struct BtExtra {
   const double *eta_bar_tau, *eta_tau, *ud_tau, *vd_tau, *pme, *river, *source, *eta_smooth;
   double *conv, *eta_u, *ps_out, *gxo, *gyo;
@@ -214,6 +218,13 @@ int launch_tmask_limit(mom5gpu_domain* d, int n, int tau);
 int launch_tmask_limit_ts_same(mom5gpu_domain* d, int nt, int ns);
 int launch_eta_tendency(mom5gpu_domain* d, int tau);
 int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
+// precision-form barotropic subcycle (k_mixed.cu, k_batch.cu)
+void launch_btf_prep(const BtArgs& a, cudaStream_t s);
+void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, cudaStream_t s);
+int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz);
+int ensure_kmt_device(mom5gpu_domain* d);
+int launch_tracer_boundary(mom5gpu_domain* d, int n);
+int launch_barotropic_forcing(mom5gpu_domain* d);
 int launch_advection_velocity(mom5gpu_domain* d, int tau);
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);
 int launch_content(mom5gpu_domain* d, int n, int level, double* out_host);
@@ -242,8 +253,11 @@ void launch_batch_fp64_advection(const MdflArgs* mdfl, const UpdArgs* upd, const
                                  int TJ, cudaStream_t s);
 // the barotropic step (init, nts x (pred, mom, corr), post) for every entry; halo fills of
 // cyclic domains are issued by the caller between the post phases
-void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB,
+void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, bool fast,
                                   cudaStream_t s);
+// precision form: folded subcycle over the work list (k_batch.cu)
+void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s);
+void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, cudaStream_t s);
 void launch_batch_barotropic_post(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, int phase,
                                   cudaStream_t s);
 // precision form: persistent kernel over (entry, tile) items

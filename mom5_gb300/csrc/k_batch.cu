@@ -3,6 +3,7 @@
 // running the same tile body as the one-domain kernel (mixed_body.cuh).
 #include "internal.h"
 #include "mixed_body.cuh"
+#include "bt_fast_body.cuh"
 
 namespace mom5 {
 
@@ -40,6 +41,31 @@ __global__ void __launch_bounds__(NT, ZR == 16 ? 3 : 2) kb_mixed(const MixArgs* 
   }
 }
 
+// precision-form barotropic subcycle over a work list of (domain, 2-D block) items
+#define BTF_ENTRY                                    \
+  int e = find_entry_m(w.pb2, w.count, blockIdx.x);  \
+  const BtArgs& a = d[w.entries[e]];                 \
+  int local = blockIdx.x - w.pb2[e];                 \
+  int nb = (a.g.ni + 2 + 127) / 128;                 \
+  int bx = local % nb, by = local / nb;
+
+__global__ void __launch_bounds__(128) kb_btf_prep(const BtArgs* d, BatchWork w) {
+  BTF_ENTRY
+  btfast::prep_body(a, bx, by);
+}
+__global__ void __launch_bounds__(128) kb_btf_pred(const BtArgs* d, BatchWork w, int so, int sn) {
+  BTF_ENTRY
+  btfast::pred_body(a, so, sn, bx, by);
+}
+__global__ void __launch_bounds__(128) kb_btf_mom(const BtArgs* d, BatchWork w, int so, int sn) {
+  BTF_ENTRY
+  btfast::mom_body(a, so, sn, bx, by);
+}
+__global__ void __launch_bounds__(128) kb_btf_corr(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+  BTF_ENTRY
+  btfast::corr_body(a, so, sn, wgt, bx, by);
+}
+
 template <int NC, int ZR>
 int configure() {
   return cudaFuncSetAttribute(kb_mixed<NC, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemT<ZR>)) ==
@@ -65,6 +91,17 @@ int run_nc(const MixArgs* m, const BatchWork& w, int ntr, int blocks, int* count
 }
 
 }  // namespace
+
+void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s) {
+  if (w.tb2 > 0) kb_btf_prep<<<w.tb2, 128, 0, s>>>(bt, w);
+}
+
+void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, cudaStream_t s) {
+  if (w.tb2 <= 0) return;
+  kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
+  kb_btf_mom<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
+  kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
+}
 
 int prepare_batch_mixed() {
   int rc = 0;

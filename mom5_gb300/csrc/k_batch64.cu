@@ -152,10 +152,15 @@ void launch_batch_fp64_advection(const MdflArgs* m, const UpdArgs* u, const Batc
 }
 
 void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB,
-                                  cudaStream_t s) {
+                                  bool fast, cudaStream_t s) {
   kb_bt_init<<<w.tb1, 256, 0, s>>>(bt, x, w);
+  if (fast) launch_batch_btf_prep(bt, w, s);
   for (int itime = 1; itime <= nts; ++itime) {
     int so = (itime + 0) % 2, sn = (itime + 1) % 2;
+    if (fast) {  // precision form: folded FP64 subcycle
+      launch_batch_btf_subcycle(bt, w, so, sn, (double)(nts - itime + 1), s);
+      continue;
+    }
     kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
     kb_bt_mom_b<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
     kb_bt_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));

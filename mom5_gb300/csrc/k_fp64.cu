@@ -454,6 +454,147 @@ int launch_quicker_vert(mom5gpu_domain* d, int n, int taum1, int tau) {
 }
 
 // ---------------------------------------------------------------------------
+// Centred schemes: 2nd order (ocean_tracer_advect.F90:2306-2352, :2836-2864),
+// 4th order (:2361-2435, :2873-2907), 6th order (:2444-2529, :2916-2972).
+// tracer_fourth/sixth and tmask_fourth/sixth are read through tq (the
+// compute-domain value after a halo update of width 2/3: periodic image or 0).
+// ---------------------------------------------------------------------------
+constexpr double kA4 = 7.0 / 12.0, kB4 = -1.0 / 12.0;                    // :349
+constexpr double kA6 = 37.0 / 60.0, kB6 = -2.0 / 15.0, kC6 = 1.0 / 60.0;  // :350
+
+struct CenArgs {
+  Geo g;
+  const double *tmask, *dyte, *dxtn, *datr, *uh, *vh, *w, *T;
+  const int* kmt;
+  double* th;
+};
+
+template <int ORDER>
+DEVI double cen_fx(const CenArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  double du = a.dyte[I2(g, i, j)] * a.uh[I3(g, i, j, k)];
+  if (ORDER == 2) return du * 0.5 * (a.T[I3(g, i + 1, j, k)] + a.T[I3(g, i, j, k)]);
+  auto TM = [&](int ii) { return tq(g, a.tmask, ii, j, k); };
+  auto TT = [&](int ii) { return tq(g, a.T, ii, j, k); };
+  if (ORDER == 4 || TM(i - 2) * TM(i - 1) == 0.0 || TM(i + 3) * TM(i + 2) == 0.0) {
+    double tm1 = TM(i - 1), tp2 = TM(i + 2);
+    int im1 = (int)(tm1 * (i - 1) + (1.0 - tm1) * i);
+    int ip2 = (int)(tp2 * (i + 2) + (1.0 - tp2) * (i + 1));
+    return du * (kA4 * (TT(i + 1) + TT(i)) + kB4 * (TT(ip2) + TT(im1)));
+  }
+  return du * (kA6 * (TT(i + 1) + TT(i)) + kB6 * (TT(i + 2) + TT(i - 1)) + kC6 * (TT(i + 3) + TT(i - 2)));
+}
+
+template <int ORDER>
+DEVI double cen_fy(const CenArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  double dv = a.dxtn[I2(g, i, j)] * a.vh[I3(g, i, j, k)];
+  if (ORDER == 2) return dv * 0.5 * (a.T[I3(g, i, j + 1, k)] + a.T[I3(g, i, j, k)]);
+  auto TM = [&](int jj) { return tq(g, a.tmask, i, jj, k); };
+  auto TT = [&](int jj) { return tq(g, a.T, i, jj, k); };
+  if (ORDER == 4 || TM(j - 2) * TM(j - 1) == 0.0 || TM(j + 3) * TM(j + 2) == 0.0) {
+    double tm1 = TM(j - 1), tp2 = TM(j + 2);
+    int jm1 = (int)(tm1 * (j - 1) + (1.0 - tm1) * j);
+    int jp2 = (int)(tp2 * (j + 2) + (1.0 - tp2) * (j + 1));
+    return dv * (kA4 * (TT(j + 1) + TT(j)) + kB4 * (TT(jp2) + TT(jm1)));
+  }
+  return dv * (kA6 * (TT(j + 1) + TT(j)) + kB6 * (TT(j + 2) + TT(j - 1)) + kC6 * (TT(j + 3) + TT(j - 2)));
+}
+
+template <int ORDER>
+__global__ void k_centred_horz(CenArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  if (i > g.ni) return;
+  long p = I3(g, i, j, k);
+  double r = a.tmask[p] *
+             (cen_fx<ORDER>(a, i, j, k) - cen_fx<ORDER>(a, i - 1, j, k) + cen_fy<ORDER>(a, i, j, k) -
+              cen_fy<ORDER>(a, i, j - 1, k)) *
+             a.datr[I2(g, i, j)];
+  a.th[p] = a.th[p] + (-r);
+}
+
+template <int ORDER>
+__global__ void k_centred_vert(CenArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+  if (i > g.ni) return;
+  const int nk = g.nk;
+  const int kmt = ORDER == 6 ? a.kmt[I2(g, i, j)] : 0;
+  double ft1 = 0.0;
+  for (int K = 1; K <= nk; ++K) {  // Fortran level numbers
+    double w = a.w[I3(g, i, j, K)];
+    int p1 = K + 1 < nk ? K + 1 : nk, p2 = K + 2 < nk ? K + 2 : nk, km1 = K - 1 > 1 ? K - 1 : 1;
+    auto TV = [&](int L) { return a.T[I3(g, i, j, L - 1)]; };
+    double ft2;
+    if (ORDER == 2) {
+      ft2 = w * 0.5 * (TV(K) + TV(p1));
+    } else {
+      double tp2 = a.tmask[I3(g, i, j, p2 - 1)];
+      int kp2 = (int)rint(tp2 * p2 + (1.0 - tp2) * p1);
+      if (ORDER == 6 && !(K <= 2 || K >= nk - 1) && K < kmt - 2)
+        ft2 = w * (kA6 * (TV(K) + TV(p1)) + kB6 * (TV(km1) + TV(kp2)) + kC6 * (TV(K - 2) + TV(K + 3)));
+      else
+        ft2 = w * (kA4 * (TV(K) + TV(p1)) + kB4 * (TV(km1) + TV(kp2)));
+    }
+    long p = I3(g, i, j, K - 1);
+    double r = a.tmask[p] * (ft1 - ft2);
+    a.th[p] = a.th[p] + (-r);
+    ft1 = ft2;
+  }
+}
+
+int ensure_kmt_device(mom5gpu_domain* d) {
+  if (d->kmt_d) return MOM5GPU_OK;
+  const Geo& g = d->geo;
+  if ((long)d->kmt_h.size() != g.n2) return fail(d, MOM5GPU_ESTATE, "kmt needed: call mom5gpu_set_vertical_grid");
+  cudaError_t e = cudaMalloc(&d->kmt_d, sizeof(int) * g.n2);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d->kmt_d, d->kmt_h.data(), sizeof(int) * g.n2, cudaMemcpyHostToDevice, d->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+  if (e != cudaSuccess) return cuda_fail(d, e, "kmt upload");
+  d->bytes += sizeof(int) * g.n2;
+  return MOM5GPU_OK;
+}
+
+int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz) {
+  const Geo& g = d->geo;
+  CenArgs a;
+  a.g = g;
+  a.tmask = fptr(d, MOM5GPU_TMASK, 0, 0);
+  a.dyte = fptr(d, MOM5GPU_DYTE, 0, 0);
+  a.dxtn = fptr(d, MOM5GPU_DXTN, 0, 0);
+  a.datr = fptr(d, MOM5GPU_DATR, 0, 0);
+  a.uh = fptr(d, MOM5GPU_UHRHO_ET, 0, 0);
+  a.vh = fptr(d, MOM5GPU_VHRHO_NT, 0, 0);
+  a.w = fptr(d, MOM5GPU_WRHO_BT, 0, 0);
+  a.T = fptr(d, MOM5GPU_TRACER, n, tau);
+  a.th = fptr(d, MOM5GPU_TH_TENDENCY, n, 0);
+  a.kmt = nullptr;
+  if (!a.tmask || !a.dyte || !a.dxtn || !a.datr || !a.uh || !a.vh || !a.w || !a.T || !a.th)
+    return fail(d, MOM5GPU_ESTATE, "centred advection: a required field was never set");
+  if (!horz && order == 6) {
+    int rc = ensure_kmt_device(d);
+    if (rc) return rc;
+    a.kmt = d->kmt_d;
+  }
+  count_launches(d, 1);
+  if (horz) {
+    dim3 grid((g.ni + 127) / 128, g.nj, g.nk);
+    if (order == 2) k_centred_horz<2><<<grid, 128, 0, d->stream>>>(a);
+    else if (order == 4) k_centred_horz<4><<<grid, 128, 0, d->stream>>>(a);
+    else k_centred_horz<6><<<grid, 128, 0, d->stream>>>(a);
+  } else {
+    dim3 grid((g.ni + 127) / 128, g.nj);
+    if (order == 2) k_centred_vert<2><<<grid, 128, 0, d->stream>>>(a);
+    else if (order == 4) k_centred_vert<4><<<grid, 128, 0, d->stream>>>(a);
+    else k_centred_vert<6><<<grid, 128, 0, d->stream>>>(a);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "centred advection");
+}
+
+// ---------------------------------------------------------------------------
 // explicit tracer update (ocean_tracer.F90:2341-2350)
 // ---------------------------------------------------------------------------
 __global__ void k_update_tracer(UpdArgs u) {
@@ -671,6 +812,7 @@ int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp)
   a.ca = d->bt + 14 * n2;
   a.uhb = a.cgrid ? nullptr : d->bt + 8 * n2;
   a.vhb = a.cgrid ? nullptr : d->bt + 10 * n2;
+  a.btf = (!a.cgrid && d->opt.precision == MOM5GPU_PRECISION_MIXED) ? d->bt + kBtPlanes * n2 : nullptr;
   a.eta_bar = fptr(d, MOM5GPU_ETA_T_BAR, 0, taup1);
   a.udrho_u = fptr(d, MOM5GPU_UDRHO_U, 0, taup1);
   a.udrho_v = fptr(d, MOM5GPU_UDRHO_V, 0, taup1);
@@ -712,7 +854,8 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   cudaStream_t s = d->stream;
   ClockScope clk(d, SEC_BAROTROPIC);
   int halo = (g.cx || g.cy) ? 1 : 0;
-  count_launches(d, 1 + (a.cgrid ? 1 : 0) + (long)a.nts * (3 + (a.cgrid ? 2 * halo : 0)) + 4 + 5 * halo);
+  count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) + (long)a.nts * (3 + (a.cgrid ? 2 * halo : 0)) + 4 +
+                       5 * halo);
   k_bt_init<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, src,
                                                           esm, d->opt.initsum_with_bar);
   dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
@@ -721,8 +864,13 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
     dim3 gc((g.ni + 127) / 128, g.nj);
     k_bt_cgrid_init<<<gc, 128, 0, s>>>(a);
   }
+  if (a.btf) launch_btf_prep(a, s);
   for (int itime = 1; itime <= a.nts; ++itime) {
     int so = (itime + 0) % 2, sn = (itime + 1) % 2;
+    if (a.btf) {  // precision form: folded FP64 subcycle
+      launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), s);
+      continue;
+    }
     k_bt_pred<<<g2, 128, 0, s>>>(a, so, sn);
     if (!a.cgrid) {
       k_bt_mom_b<<<g2, 128, 0, s>>>(a, so, sn);
@@ -844,6 +992,101 @@ int launch_advection_velocity(mom5gpu_domain* d, int tau) {
   k_adv_vel_w<<<g2, 128, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "ocean_advection_velocity");
+}
+
+// ---------------------------------------------------------------------------
+// surface and bottom source terms of the explicit tracer step (ocean_tracer.F90:2318-2336)
+// ---------------------------------------------------------------------------
+__global__ void k_tracer_boundary(Geo g, const double* tmask, const int* kmt, const double* pme, const double* tpme,
+                                  const double* esm, const double* pbs, double* th) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+  if (i > g.ni) return;
+  long q = I2(g, i, j);
+  th[q] = th[q] + tmask[q] * (pme[q] * tpme[q] + esm[q]);
+  int kbot = kmt[q];
+  if (kbot > 0) {
+    long p = (long)(kbot - 1) * g.n2 + q;
+    th[p] = th[p] + tmask[p] * pbs[q];
+  }
+}
+
+int launch_tracer_boundary(mom5gpu_domain* d, int n) {
+  const Geo& g = d->geo;
+  int krc = ensure_kmt_device(d);
+  if (krc) return krc;
+  const double* tmask = fptr(d, MOM5GPU_TMASK, 0, 0);
+  const double* pme = fptr(d, MOM5GPU_PME, 0, 0);
+  const double* tpme = fptr(d, MOM5GPU_TPME, n, 0);
+  const double* esm = fptr(d, MOM5GPU_TRACER_ETA_SMOOTH, n, 0);
+  const double* pbs = fptr(d, MOM5GPU_PBOT_SMOOTH, n, 0);
+  double* th = fptr(d, MOM5GPU_TH_TENDENCY, n, 0);
+  if (!tmask || !pme || !tpme || !esm || !pbs || !th)
+    return fail(d, MOM5GPU_ESTATE, "tracer_boundary_terms: a field could not be allocated");
+  count_launches(d, 1);
+  dim3 grid((g.ni + 127) / 128, g.nj);
+  k_tracer_boundary<<<grid, 128, 0, d->stream>>>(g, tmask, d->kmt_d, pme, tpme, esm, pbs, th);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "tracer_boundary_terms");
+}
+
+// ---------------------------------------------------------------------------
+// ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141), no barotropic friction
+// ---------------------------------------------------------------------------
+__global__ void k_baro_forcing(Geo g, const double* tmen, const double* accel, const double* smf, const double* bmf,
+                               int nonlinear, double* f) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double v = 0.0;  // forcing_bt = 0.0 on the data domain
+  if (i >= 1 && i <= g.ni && j >= 1 && j <= g.nj) {
+    double w = 0.0;
+    if (nonlinear)
+      for (int k = 0; k < g.nk; ++k) w = w + tmen[(long)k * g.n2 + q] * accel[(long)k * g.n2 + q];
+    v = w + tmen[q] * (smf[q] - bmf[q]);
+  }
+  f[q] = v;
+}
+
+// forcing_bt + friction_lap + friction_bih with both frictions 0.0 (:3109-3117)
+__global__ void k_plus_zero_2d(long n2, double* f) {
+  long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (q < n2) f[q] = plus_zero(plus_zero(f[q]));
+}
+
+int launch_barotropic_forcing(mom5gpu_domain* d) {
+  const Geo& g = d->geo;
+  double* fu = fptr(d, MOM5GPU_FORCING_BT_U, 0, 0);
+  double* fv = fptr(d, MOM5GPU_FORCING_BT_V, 0, 0);
+  if (!fu || !fv) return fail(d, MOM5GPU_ESTATE, "ocean_barotropic_forcing: a field could not be allocated");
+  cudaStream_t s = d->stream;
+  if (d->opt.zero_forcing_bt) {  // (:3126-3134)
+    count_launches(d, 0);
+    cudaMemsetAsync(fu, 0, sizeof(double) * g.n2, s);
+    cudaMemsetAsync(fv, 0, sizeof(double) * g.n2, s);
+  } else {
+    const double* te = fptr(d, MOM5GPU_TMASKEN_E, 0, 0);
+    const double* tn = fptr(d, MOM5GPU_TMASKEN_N, 0, 0);
+    const double* au = fptr(d, MOM5GPU_ACCEL_U, 0, 0);
+    const double* av = fptr(d, MOM5GPU_ACCEL_V, 0, 0);
+    const double* su = fptr(d, MOM5GPU_SMF_U, 0, 0);
+    const double* sv = fptr(d, MOM5GPU_SMF_V, 0, 0);
+    const double* bu = fptr(d, MOM5GPU_BMF_U, 0, 0);
+    const double* bv = fptr(d, MOM5GPU_BMF_V, 0, 0);
+    if (!te || !tn || !au || !av || !su || !sv || !bu || !bv)
+      return fail(d, MOM5GPU_ESTATE, "ocean_barotropic_forcing: a field could not be allocated");
+    int nl = d->opt.zero_nonlinear_forcing_bt ? 0 : 1;
+    dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
+    count_launches(d, 4 + ((g.cx || g.cy) ? 2 : 0));
+    k_baro_forcing<<<g2, 128, 0, s>>>(g, te, au, su, bu, nl, fu);
+    k_baro_forcing<<<g2, 128, 0, s>>>(g, tn, av, sv, bv, nl, fv);
+    launch_halo_fill(g, fu, 1, 3, s);
+    launch_halo_fill(g, fv, 1, 3, s);
+    unsigned nb = (unsigned)((g.n2 + 255) / 256);
+    k_plus_zero_2d<<<nb, 256, 0, s>>>(g.n2, fu);
+    k_plus_zero_2d<<<nb, 256, 0, s>>>(g.n2, fv);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "ocean_barotropic_forcing");
 }
 
 // ---------------------------------------------------------------------------

@@ -79,13 +79,10 @@ struct SmemT {
   // z pass, per z-column (32x32)
   float zmf[ZR * ZW], zd0[ZR * ZW], zd1[ZR * ZW], zc[ZR * ZW], zdtr[ZR * ZW], zwd[ZR * ZW], zdatr[ZR * ZW];
   uint8_t zmask[ZR * ZW];  // bit0..3 = wet at k-1, k, k+1, k+2
-  float tz[ZR * ZW];       // tracer after z
-  float tf[ZR * ZW];       // tracer at taum1 (FP32)
-  float fz[ZR * ZW];       // z flux-divergence increment
   // x pass: faces between columns zi and zi+1 (index zj*ZW+zi), cells
   float xmf[ZR * ZW], xd0[ZR * ZW], xd1[ZR * ZW], xc[ZR * ZW];
   float xcoef[ZR * ZW], xdiv[ZR * ZW];
-  float fx[ZR * ZW], tx[ZR * ZW], fxi[ZR * ZW];
+  float tx[ZR * ZW];  // tracer after x
   // y pass: faces between rows zj and zj+1
   float ymf[ZR * ZW], yd0[ZR * ZW], yd1[ZR * ZW], yc[ZR * ZW];
   float fy[ZR * ZW];
@@ -214,12 +211,16 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
     for (int n = 0; n < NC; ++n) {
       if (n >= a.ntr) break;
       const double* T = a.T + (long)n * g.n3;
-      // ---- z pass ----
+      // A tile row (32 columns) is one warp: the z pass, the x fluxes and the x
+      // update of a row exchange neighbours with warp shuffles; only the y pass
+      // reads other rows (shared memory, two barriers per tracer).
+      float tkr[ROWS_PER_WARP], fzr[ROWS_PER_WARP], fir[ROWS_PER_WARP];
 #pragma unroll
       for (int m = 0; m < ROWS_PER_WARP; ++m) {
         const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        // ---- z pass ----
         const int o = s.off[c];
-        uint8_t mb = s.zmask[c];
+        const uint8_t mb = s.zmask[c];
         float tzv = 0.f, tk = 0.f, fzv = 0.f;
         if (o >= 0) {
           tk = d2f(T[(long)k * g.n2 + o]);
@@ -237,41 +238,32 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
           tzv = tk + dtr * (adiv + tk * s.zwd[c]);
           ftp[n][m] = fbt;
         }
-        s.tz[c] = tzv;
-        s.tf[c] = tk;
-        s.fz[c] = fzv;
-      }
-      __syncthreads();
-      // ---- x fluxes: face zi (between zi and zi+1), zi = 1..29 ----
-#pragma unroll
-      for (int m = 0; m < ROWS_PER_WARP; ++m) {
-        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        // ---- x fluxes: face zi (between zi and zi+1), zi = 1..29 ----
+        const unsigned full = 0xffffffffu;
+        float tA = __shfl_up_sync(full, tzv, 1), tC = __shfl_down_sync(full, tzv, 1);
+        float tD = __shfl_down_sync(full, tzv, 2);
+        unsigned wet = (mb >> 1) & 1u;
+        unsigned wA = __shfl_up_sync(full, wet, 1), wC = __shfl_down_sync(full, wet, 1);
+        unsigned wD = __shfl_down_sync(full, wet, 2);
         float f = 0.f;
-        if (zi >= 1 && zi <= ZW - 3) {
-          bool m0 = s.zmask[c - 1] & 2, m1 = s.zmask[c] & 2, m2 = s.zmask[c + 1] & 2, m3 = s.zmask[c + 2] & 2;
-          if (m1 && m2) {
-            float tA = s.tz[c - 1], tB = s.tz[c], tC = s.tz[c + 1], tD = s.tz[c + 2];
-            float Rjp = (m3 && m2) ? tD - tC : 0.f;
-            float Rj = tC - tB;
-            float Rjm = (m1 && m0) ? tB - tA : 0.f;
-            f = face_flux(s.xmf[c], Rjm, Rj, Rjp, tB, tC, s.xd0[c], s.xd1[c], s.xc[c]);
-          }
+        if (zi >= 1 && zi <= ZW - 3 && wet && wC) {
+          float Rjp = wD ? tD - tC : 0.f;
+          float Rj = tC - tzv;
+          float Rjm = wA ? tzv - tA : 0.f;
+          f = face_flux(s.xmf[c], Rjm, Rj, Rjp, tzv, tC, s.xd0[c], s.xd1[c], s.xc[c]);
         }
-        s.fx[c] = f;
-      }
-      __syncthreads();
-      // ---- x update: cells zi = 2..29 of every row ----
-#pragma unroll
-      for (int m = 0; m < ROWS_PER_WARP; ++m) {
-        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        // ---- x update: cells zi = 2..29 ----
+        float fw = __shfl_up_sync(full, f, 1);
         float t = 0.f, fi = 0.f;
         if (s.xin[c]) {
           float coef = s.xcoef[c];
-          fi = coef * (s.fx[c - 1] - s.fx[c]);
-          t = s.tz[c] + (fi + coef * (s.tf[c] * s.xdiv[c]));
+          fi = coef * (fw - f);
+          t = tzv + (fi + coef * (tk * s.xdiv[c]));
         }
         s.tx[c] = t;
-        s.fxi[c] = fi;
+        tkr[m] = tk;
+        fzr[m] = fzv;
+        fir[m] = fi;
       }
       __syncthreads();
       // ---- y fluxes: face zj (between rows zj and zj+1), zj = 1..29, zi = 2..29 ----
@@ -302,11 +294,11 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
         bool wet = s.zmask[c] & 2;
         if (!wet && !a.fused) continue;
         float fy = s.xcoef[c] * (s.fy[c - ZW] - s.fy[c]);
-        float dT = s.fz[c] + s.fxi[c] + fy;
+        float dT = fzr[m] + fir[m] + fy;
         long p = I3(g, i, j, k);
         if (a.fused) {
           // T(taup1) = T + (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT
-          float inc = s.uq[c] * s.tf[c] + s.ur[c] * dT;
+          float inc = s.uq[c] * tkr[m] + s.ur[c] * dT;
           double tn = T[p] + f2d(inc);
           double* o = a.out + (long)(n0 + n) * g.n3;
           o[p] = tn;
@@ -321,7 +313,8 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
           o[p] = o[p] + f2d(s.ur[c] * dT);
         }
       }
-      __syncthreads();
+      // the next tracer writes tx only after this tracer's y fluxes were read
+      // (second barrier above) and fy only after its own first barrier
     }
   }
 }

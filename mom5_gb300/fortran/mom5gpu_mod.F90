@@ -39,7 +39,9 @@ module mom5gpu_c
        F_PATM = 100, F_PME = 101, F_RIVER = 102, F_RHO_G = 103, &
        F_DXT_DXTER = 24, F_DYT_DYTER = 25, F_DXT_DXTNR = 26, F_DYT_DYTNR = 27, F_DIVERGE_T = 53, &
        F_RHO_DZU = 65, F_RHO_DZTEN_E = 66, F_RHO_DZTEN_N = 67, F_RHO_DZT_TENDENCY = 68, &
-       F_MASS_SOURCE = 69, F_U_VEL = 110, F_V_VEL = 111
+       F_MASS_SOURCE = 69, F_U_VEL = 110, F_V_VEL = 111, F_TMASKEN_E = 41, F_TMASKEN_N = 42, &
+       F_TPME = 73, F_TRACER_ETA_SMOOTH = 74, F_PBOT_SMOOTH = 75, F_ACCEL_U = 112, F_ACCEL_V = 113, &
+       F_SMF_U = 114, F_SMF_V = 115, F_BMF_U = 116, F_BMF_V = 117
 
   type, bind(C) :: mom5gpu_dims
      integer(c_int) :: ni, nj, nk, cyclic_x, cyclic_y, num_prog_tracers, horz_grid
@@ -50,6 +52,7 @@ module mom5gpu_c
      integer(c_int) :: barotropic_time_stepping_A, barotropic_time_stepping_B, initsum_with_bar
      real(c_double) :: pred_corr_gamma, rho0, grav
      integer(c_int) :: precision
+     integer(c_int) :: zero_forcing_bt, zero_nonlinear_forcing_bt
   end type mom5gpu_options
 
   interface
@@ -162,6 +165,15 @@ module mom5gpu_c
        type(c_ptr), value :: dom
        integer(c_int), value :: tau
      end function
+     integer(c_int) function mom5gpu_tracer_boundary_terms(dom, n) bind(C, name="mom5gpu_tracer_boundary_terms")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n
+     end function
+     integer(c_int) function mom5gpu_ocean_barotropic_forcing(dom) bind(C, name="mom5gpu_ocean_barotropic_forcing")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+     end function
      integer(c_int) function mom5gpu_global_tracer_content(dom, n, level, total) &
           bind(C, name="mom5gpu_global_tracer_content")
        import :: c_int, c_ptr, c_double
@@ -189,7 +201,7 @@ module mom5gpu_mod
   public :: mom5gpu_attach, mom5gpu_mark_velocity_changed, mom5gpu_mark_state_changed
   public :: horz_advect_tracer, vert_advect_tracer
   public :: update_ocean_barotropic, eta_and_pbot_tendency, eta_and_pbot_update
-  public :: ocean_advection_velocity
+  public :: ocean_advection_velocity, ocean_barotropic_forcing
 
   type(c_ptr), save :: dom = c_null_ptr
   logical, save :: velocity_dirty = .true.
@@ -375,5 +387,23 @@ contains
     ! not push them again (thickness is still pushed)
     velocity_on_device = .true.
   end subroutine ocean_advection_velocity
+
+  ! ocean_barotropic.F90:3058-3062.  Velocity%accel, smf and bmf go to the device,
+  ! Ext_mode%forcing_bt comes back (it also stays on the device for the subcycle).
+  ! Grd%tmasken is copied once by the host driver (fields F_TMASKEN_E/N).
+  subroutine ocean_barotropic_forcing(Time, Velocity, Ext_mode)
+    type(ocean_time_type),          intent(in)    :: Time
+    type(ocean_velocity_type),      intent(inout) :: Velocity
+    type(ocean_external_mode_type), intent(inout) :: Ext_mode
+    call check(mom5gpu_set_field(dom, F_ACCEL_U, 0, 0, Velocity%accel(:,:,:,1), 0), 'accel')
+    call check(mom5gpu_set_field(dom, F_ACCEL_V, 0, 0, Velocity%accel(:,:,:,2), 0), 'accel')
+    call check(mom5gpu_set_field(dom, F_SMF_U, 0, 0, Velocity%smf(:,:,1), 0), 'smf')
+    call check(mom5gpu_set_field(dom, F_SMF_V, 0, 0, Velocity%smf(:,:,2), 0), 'smf')
+    call check(mom5gpu_set_field(dom, F_BMF_U, 0, 0, Velocity%bmf(:,:,1), 0), 'bmf')
+    call check(mom5gpu_set_field(dom, F_BMF_V, 0, 0, Velocity%bmf(:,:,2), 0), 'bmf')
+    call check(mom5gpu_ocean_barotropic_forcing(dom), 'ocean_barotropic_forcing')
+    call check(mom5gpu_get_field(dom, F_FORCING_BT_U, 0, 0, Ext_mode%forcing_bt(:,:,1), 0), 'forcing_bt')
+    call check(mom5gpu_get_field(dom, F_FORCING_BT_V, 0, 0, Ext_mode%forcing_bt(:,:,2), 0), 'forcing_bt')
+  end subroutine ocean_barotropic_forcing
 
 end module mom5gpu_mod

@@ -192,6 +192,122 @@ void orc_vert_advect_upwind(const orc_dims* d, const double* tmask, const double
 }
 
 /* ------------------------------------------------------------------------- */
+/* Centred schemes: 2nd order (:2306-2352, :2836-2864), 4th order            */
+/* (:2361-2435, :2873-2907), 6th order (:2444-2529, :2916-2972), with        */
+/* a4, b4, a6, b6, c6 (:349-350).  The 4th/6th-order horizontal schemes read */
+/* tracer_fourth/sixth and tmask_fourth/sixth (fourth_sixth_init             */
+/* :1597-1636): the compute-domain values with a halo of 2/3 filled by the   */
+/* single-PE halo update (periodic image in cyclic directions, else 0).      */
+/* Outputs wrk1 = -scheme(...) on the compute domain, zero elsewhere.        */
+/* ------------------------------------------------------------------------- */
+static const double c_a4 = 7.0 / 12.0, c_b4 = -1.0 / 12.0;
+static const double c_a6 = 37.0 / 60.0, c_b6 = -2.0 / 15.0, c_c6 = 1.0 / 60.0;
+
+/* value of a compute-domain field at (i,j,k) after a halo update of any width */
+static double halo_value(const orc_dims* d, const double* a, int i, int j, int k) {
+  if (i < 1 || i > d->ni) {
+    if (!d->cyclic_x) return 0.0;
+    i = i < 1 ? i + d->ni : i - d->ni;
+  }
+  if (j < 1 || j > d->nj) {
+    if (!d->cyclic_y) return 0.0;
+    j = j < 1 ? j + d->nj : j - d->nj;
+  }
+  return a[I3(d, i, j, k)];
+}
+
+void orc_horz_advect_centred(const orc_dims* d, int order, const double* tmask, const double* dyte,
+                             const double* dxtn, const double* datr, const double* uhrho_et, const double* vhrho_nt,
+                             const double* T, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* fx = (double*)calloc(n2, sizeof(double));
+  double* fy = (double*)calloc(n2, sizeof(double));
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+#define TT(i, j) halo_value(d, T, (i), (j), k)
+#define TM(i, j) halo_value(d, tmask, (i), (j), k)
+  for (int k = 0; k < nk; ++k) {
+    memset(fx, 0, sizeof(double) * n2);
+    memset(fy, 0, sizeof(double) * n2);
+    for (int j = (order == 2 ? 0 : 1); j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        double u = uhrho_et[I3(d, i, j, k)], f;
+        if (order == 2) {
+          f = dyte[I2(d, i, j)] * u * 0.5 * (T[I3(d, i + 1, j, k)] + T[I3(d, i, j, k)]);
+        } else if (order == 4 || TM(i - 2, j) * TM(i - 1, j) == 0.0 || TM(i + 3, j) * TM(i + 2, j) == 0.0) {
+          int im1 = (int)(TM(i - 1, j) * (i - 1) + (1.0 - TM(i - 1, j)) * i);
+          int ip2 = (int)(TM(i + 2, j) * (i + 2) + (1.0 - TM(i + 2, j)) * (i + 1));
+          f = dyte[I2(d, i, j)] * u * (c_a4 * (TT(i + 1, j) + TT(i, j)) + c_b4 * (TT(ip2, j) + TT(im1, j)));
+        } else {
+          f = dyte[I2(d, i, j)] * u *
+              (c_a6 * (TT(i + 1, j) + TT(i, j)) + c_b6 * (TT(i + 2, j) + TT(i - 1, j)) +
+               c_c6 * (TT(i + 3, j) + TT(i - 2, j)));
+        }
+        fx[I2(d, i, j)] = f;
+      }
+    for (int j = 0; j <= nj; ++j)
+      for (int i = (order == 2 ? 0 : 1); i <= ni; ++i) {
+        double v = vhrho_nt[I3(d, i, j, k)], f;
+        if (order == 2) {
+          f = dxtn[I2(d, i, j)] * v * 0.5 * (T[I3(d, i, j + 1, k)] + T[I3(d, i, j, k)]);
+        } else if (order == 4 || TM(i, j - 2) * TM(i, j - 1) == 0.0 || TM(i, j + 3) * TM(i, j + 2) == 0.0) {
+          int jm1 = (int)(TM(i, j - 1) * (j - 1) + (1.0 - TM(i, j - 1)) * j);
+          int jp2 = (int)(TM(i, j + 2) * (j + 2) + (1.0 - TM(i, j + 2)) * (j + 1));
+          f = dxtn[I2(d, i, j)] * v * (c_a4 * (TT(i, j + 1) + TT(i, j)) + c_b4 * (TT(i, jp2) + TT(i, jm1)));
+        } else {
+          f = dxtn[I2(d, i, j)] * v *
+              (c_a6 * (TT(i, j + 1) + TT(i, j)) + c_b6 * (TT(i, j + 2) + TT(i, j - 1)) +
+               c_c6 * (TT(i, j + 3) + TT(i, j - 2)));
+        }
+        fy[I2(d, i, j)] = f;
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double r = tmask[I3(d, i, j, k)] *
+                   (fx[I2(d, i, j)] - fx[I2(d, i - 1, j)] + fy[I2(d, i, j)] - fy[I2(d, i, j - 1)]) *
+                   datr[I2(d, i, j)];
+        wrk1[I3(d, i, j, k)] = -r;
+      }
+  }
+#undef TT
+#undef TM
+  free(fx);
+  free(fy);
+}
+
+void orc_vert_advect_centred(const orc_dims* d, int order, const double* tmask, const int* kmt,
+                             const double* wrho_bt, const double* T, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  for (int j = 1; j <= nj; ++j)
+    for (int i = 1; i <= ni; ++i) {
+      double ft1 = 0.0;
+      for (int K = 1; K <= nk; ++K) { /* Fortran level numbers */
+        int k = K - 1;
+        double w = wrho_bt[I3(d, i, j, K)];
+        int p1 = K + 1 < nk ? K + 1 : nk, p2 = K + 2 < nk ? K + 2 : nk, km1 = K - 1 > 1 ? K - 1 : 1;
+#define TV(L) T[I3(d, i, j, (L) - 1)]
+        double ft2;
+        if (order == 2) {
+          ft2 = w * 0.5 * (TV(K) + TV(p1));
+        } else {
+          double tp2 = tmask[I3(d, i, j, p2 - 1)];
+          int kp2 = (int)nearbyint(tp2 * p2 + (1.0 - tp2) * p1);
+          if (order == 6 && !(K <= 2 || K >= nk - 1) && K < kmt[I2(d, i, j)] - 2)
+            ft2 = w * (c_a6 * (TV(K) + TV(p1)) + c_b6 * (TV(km1) + TV(kp2)) + c_c6 * (TV(K - 2) + TV(K + 3)));
+          else
+            ft2 = w * (c_a4 * (TV(K) + TV(p1)) + c_b4 * (TV(km1) + TV(kp2)));
+        }
+#undef TV
+        double r = tmask[I3(d, i, j, k)] * (ft1 - ft2);
+        wrk1[I3(d, i, j, k)] = -r;
+        ft1 = ft2;
+      }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* Quicker: quicker_init :1442-1586, horz :2538-2653, vert :2981-3031.       */
 /* Weight arrays are data-domain 2-D arrays with a trailing component index: */
 /* quick_x(·,·,2), curv_xp(·,·,3) ...; quick_z(nk,2), curv_zp(nk,3).         */
@@ -1223,6 +1339,53 @@ void orc_ocean_advection_velocity(const orc_dims* d, int cgrid, const double* u,
   free(a);
   free(bdx);
   free(bdy);
+}
+
+/* Surface and bottom source terms of the explicit tracer step, one tracer
+ * (ocean_tracer.F90:2318-2336). kmt is the 2-D array of deepest wet levels. */
+void orc_tracer_boundary_terms(const orc_dims* d, const double* tmask, const int* kmt, const double* pme,
+                               const double* tpme, const double* eta_smooth, const double* pbot_smooth, double* th) {
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) {
+      size_t q = I2(d, i, j);
+      th[q] = th[q] + tmask[q] * (pme[q] * tpme[q] + eta_smooth[q]);
+    }
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) {
+      size_t q = I2(d, i, j);
+      int kbot = kmt[q];
+      if (kbot > 0) {
+        size_t p = (size_t)(kbot - 1) * n2 + q;
+        th[p] = th[p] + tmask[p] * pbot_smooth[q];
+      }
+    }
+}
+
+/* ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141) with udrho_lap =
+ * udrho_bih = .false. (their default): one component; tmasken and accel are 3-D. */
+void orc_ocean_barotropic_forcing(const orc_dims* d, int zero_nonlinear, int zero_forcing, const double* tmasken,
+                                  const double* accel, const double* smf, const double* bmf, double* forcing) {
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* wrk = (double*)calloc(n2, sizeof(double));
+  for (size_t q = 0; q < n2; ++q) forcing[q] = 0.0;
+  if (!zero_nonlinear)
+    for (int k = 0; k < d->nk; ++k)
+      for (int j = 1; j <= d->nj; ++j)
+        for (int i = 1; i <= d->ni; ++i) {
+          size_t q = I2(d, i, j);
+          wrk[q] = wrk[q] + tmasken[(size_t)k * n2 + q] * accel[(size_t)k * n2 + q];
+        }
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) {
+      size_t q = I2(d, i, j);
+      forcing[q] = wrk[q] + tmasken[q] * (smf[q] - bmf[q]);
+    }
+  orc_halo_update_2d(d, forcing, 3);
+  for (size_t q = 0; q < n2; ++q) forcing[q] = forcing[q] + 0.0 + 0.0; /* + friction_lap + friction_bih */
+  if (zero_forcing)
+    for (size_t q = 0; q < n2; ++q) forcing[q] = 0.0;
+  free(wrk);
 }
 
 /* total_tracer (ocean_tracer_diag.F90:2395-2412) with conversion = 1: the

@@ -95,6 +95,22 @@ def vert_advect_upwind(d: Dims, g, T):
     return out
 
 
+def horz_advect_centred(d: Dims, g, T, order):
+    """wrk1 of the 2nd/4th/6th-order horizontal schemes (T at tau)."""
+    out = np.zeros_like(T)
+    lib().orc_horz_advect_centred(C.byref(d), int(order), p(g["tmask"]), p(g["dyte"]), p(g["dxtn"]), p(g["datr"]),
+                                  p(g["uhrho_et"]), p(g["vhrho_nt"]), p(T), p(out))
+    return out
+
+
+def vert_advect_centred(d: Dims, g, T, order, kmt):
+    out = np.zeros_like(T)
+    k = np.ascontiguousarray(kmt, dtype=np.int32)
+    lib().orc_vert_advect_centred(C.byref(d), int(order), p(g["tmask"]), k.ctypes.data_as(C.POINTER(C.c_int)),
+                                  p(g["wrho_bt"]), p(T), p(out))
+    return out
+
+
 def quicker_init(d: Dims, g, dzt: np.ndarray):
     nxd, nyd, nk = d.ni + 2, d.nj + 2, d.nk
     q = {"quick_x": np.zeros((2, nyd, nxd)), "quick_y": np.zeros((2, nyd, nxd)),
@@ -189,6 +205,24 @@ def ocean_advection_velocity(d, g, u, v, rho_dzu=None, rho_dzten_e=None, rho_dzt
         (rho_dzt_tendency, z3), (mass_source, z3), (pme, z2), (river, z2))]
     lib().orc_ocean_advection_velocity(C.byref(d), int(cgrid), *[p(a) for a in keep], p(ue), p(vn), p(dv), p(w))
     return ue, vn, dv, w
+
+
+def tracer_boundary_terms(d, g, kmt, pme, tpme, eta_smooth, pbot_smooth, th):
+    """th (one tracer) after the surface and bottom source terms; returns a new array."""
+    out = np.ascontiguousarray(th, dtype=np.float64).copy()
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (pme, tpme, eta_smooth, pbot_smooth)]
+    k = np.ascontiguousarray(kmt, dtype=np.int32)
+    lib().orc_tracer_boundary_terms(C.byref(d), p(g["tmask"]), k.ctypes.data_as(C.POINTER(C.c_int)),
+                                    *[p(a) for a in keep], p(out))
+    return out
+
+
+def ocean_barotropic_forcing(d, tmasken, accel, smf, bmf, zero_nonlinear=False, zero_forcing=False):
+    out = np.zeros((d.nj + 2, d.ni + 2))
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (tmasken, accel, smf, bmf)]
+    lib().orc_ocean_barotropic_forcing(C.byref(d), int(zero_nonlinear), int(zero_forcing), *[p(a) for a in keep],
+                                       p(out))
+    return out
 
 
 def total_tracer(d, g, T):

@@ -106,6 +106,32 @@ def test_upwind_matches(env, cyclic_x):
         assert equal(got, ref), diff_report(got, ref)
 
 
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("cyclic_x,cyclic_y", [(False, False), (True, False), (True, True)])
+def test_centred_schemes_match(env, order, cyclic_x, cyclic_y):
+    """ADVECT_2ND/4TH/6TH_ORDER (ocean_tracer_advect.F90:2306-2529 horizontal,
+    :2836-2972 vertical) on T(tau), with the 4th/6th-order land substitutions
+    next to the continent and the halo-2/3 copies of cyclic domains."""
+    capi, O = env
+    scheme = {2: capi.ADVECT_2ND_ORDER, 4: capi.ADVECT_4TH_ORDER, 6: capi.ADVECT_6TH_ORDER}[order]
+    sp = spec(cyclic_x=cyclic_x, cyclic_y=cyclic_y, ntr=2, seed=13 + order)
+    dom, d, g, dims = setup(env, sp, scheme=scheme)
+    rng = np.random.default_rng(order)
+    kmt = dom["kmt"].numpy()
+    for n in (1, 2):
+        T0 = np.ascontiguousarray(g["T"][n - 1] * (1.0 + 0.01 * rng.standard_normal(g["T"][n - 1].shape)))
+        d.set(capi.F.TRACER, T0, n=n, level=2)  # tau = 2 differs from taum1 = 1
+        d.zero_th_tendency(n)
+        d.horz_advect_tracer(n, 1, 2, 3600.0)
+        got_h = d.get(capi.F.TH_TENDENCY, n=n)
+        ref_h = O.horz_advect_centred(dims, g, T0, order)
+        assert equal(got_h, ref_h), f"horz tracer {n}: {diff_report(got_h, ref_h)}"
+        d.vert_advect_tracer(n, 1, 2, 3600.0)
+        got = d.get(capi.F.TH_TENDENCY, n=n)
+        ref = ref_h + O.vert_advect_centred(dims, g, T0, order, kmt)
+        assert equal(got, ref), f"vert tracer {n}: {diff_report(got, ref)}"
+
+
 @pytest.mark.parametrize("limit_with_upwind", [0, 1])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_quicker_matches(env, cyclic_x, limit_with_upwind):
@@ -186,6 +212,25 @@ def test_tracer_chunks_match(env, ntr):
         tau = 3 - tau
     ref = _oracle_steps(O, dims, g, 3, dt)
     for n in range(1, ntr + 1):
+        got = d.get(capi.F.TRACER, n=n, level=tau)
+        assert equal(got, ref[n - 1]), f"tracer {n}: {diff_report(got, ref[n - 1])}"
+
+
+def test_autotune_keeps_parity(env):
+    """mom5gpu_autotune changes only launch shapes: after it, steps still equal
+    the oracle (its trials overwrite time level 2, which the next step rewrites)."""
+    capi, O = env
+    sp = spec(cyclic_x=True, ntr=3, seed=23)
+    dom, d, g, dims = setup(env, sp)
+    dt = 6 * 3600.0
+    report = d.autotune(dt)
+    assert "chosen tj=" in report, report
+    tau = 1
+    for s in range(4):
+        d.tracer_advection_step(tau, tau, 3 - tau, dt)
+        tau = 3 - tau
+    ref = _oracle_steps(O, dims, g, 4, dt)
+    for n in range(1, sp.ntracers + 1):
         got = d.get(capi.F.TRACER, n=n, level=tau)
         assert equal(got, ref[n - 1]), f"tracer {n}: {diff_report(got, ref[n - 1])}"
 

@@ -66,7 +66,32 @@ def test_advection_velocity_restatements_agree(O):
     assert np.array_equal(ue, u * rz) and np.array_equal(vn, v * (2 * rz))
 
 
-@pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker"])
+def test_step_terms_restatements(O):
+    """Source terms of the tracer step (ocean_tracer.F90:2318-2336) add exactly
+    tmask*(pme*tpme + eta_smooth) at k=1 and tmask*pbot_smooth at kmt; the
+    barotropic forcing (ocean_barotropic.F90:3058-3141) of a fluid at rest with
+    equal surface and bottom stress is +0 everywhere, halo included."""
+    dom, g, d = load(O, small(seed=6))
+    rng = np.random.default_rng(2)
+    kmt = dom["kmt"].numpy()
+    shp2 = kmt.shape
+    pme, tp, es, pb = (rng.standard_normal(shp2) for _ in range(4))
+    th = np.zeros_like(g["tmask"])
+    out = O.tracer_boundary_terms(d, g, kmt, pme, tp, es, pb, th)
+    exp = np.zeros_like(th)
+    exp[0, 1:-1, 1:-1] = (g["tmask"][0] * (pme * tp + es))[1:-1, 1:-1]
+    for j in range(1, d.nj + 1):
+        for i in range(1, d.ni + 1):
+            if kmt[j, i] > 0:
+                exp[kmt[j, i] - 1, j, i] += g["tmask"][kmt[j, i] - 1, j, i] * pb[j, i]
+    assert np.array_equal(out, exp)
+    z3 = np.zeros_like(g["tmask"])
+    s = rng.standard_normal(shp2)
+    f = O.ocean_barotropic_forcing(d, g["tmask"], z3, s, s)
+    assert np.all(f.view(np.uint64) == 0)
+
+
+@pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker", "c2", "c4", "c6"])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
     """A uniform tracer in a non-divergent flow has zero advective tendency
@@ -81,6 +106,9 @@ def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
         th = O.advect_sweby_all(d, g, np.ascontiguousarray(U[None]), 3600.0)[0]
     elif scheme == "upwind":
         th = O.horz_advect_upwind(d, g, U) + O.vert_advect_upwind(d, g, U)
+    elif scheme.startswith("c"):
+        order = int(scheme[1])
+        th = O.horz_advect_centred(d, g, U, order) + O.vert_advect_centred(d, g, U, order, dom["kmt"].numpy())
     else:
         q = O.quicker_init(d, g, dom.dzt.numpy())
         th = O.horz_advect_quicker(d, g, q, U, U) + O.vert_advect_quicker(d, g, q, U, U)
