@@ -68,6 +68,12 @@ def adv_bytes(ni, nj, nk, ntr):
     return 8 * ni * nj * nk * (2 * ntr + 5) + 8 * ni * nj * 7
 
 
+# DRAM bytes per tracer-cell of the advection launch set, from the ncu capture of the
+# 360x270x50 block (profiles/traffic_advection_c2block.md): FP64 5.199 GB, precision form
+# 0.975 GB for 360*270*50*10 tracer-cells.
+TRAFFIC_PER_TRACER_CELL = {"fp64": 5.199e9 / (360 * 270 * 50 * 10), "mixed": 0.975e9 / (360 * 270 * 50 * 10)}
+
+
 def bt_bytes(ni, nj, nts):
     """Streaming bytes of the barotropic subcycles: 28 FP64 arrays per column per subcycle."""
     return 224 * ni * nj * nts
@@ -262,7 +268,8 @@ def run_ours(args, rank, world):
     d.set_stream(stream.cuda_stream)
 
     state = {"tau": 1}
-    tune = d.autotune(DTTS) if ntr > 0 else None  # trial steps 1 -> 2; the timed steps start at level 1
+    # trial steps 1 -> 2; the timed steps start at level 1
+    tune = d.autotune(DTTS) if ntr > 0 and not args.no_autotune else None
     if world > 1:
         torch.distributed.barrier()
     r = _time_domain(d, stream, ntr, args.steps, args.warmup, state, local)
@@ -286,7 +293,10 @@ def run_ours(args, rank, world):
         roofline = {"bound": "hbm", "kernel": "tracer advection step (mdfl passes + explicit update)",
                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                    "algorithmic_bytes_per_launch": bytes_adv, "ms_per_launch": round(per, 3), "traffic": None}
+                    "algorithmic_bytes_per_launch": bytes_adv, "ms_per_launch": round(per, 3),
+                    "traffic": round(TRAFFIC_PER_TRACER_CELL[args.precision] * cells * ntr),
+                    "traffic_source": "ncu DRAM bytes of the 360x270x50 block scaled by tracer-cells "
+                                      "(profiles/traffic_advection_c2block.md)"}
     else:
         roofline = None
     bt_ms = sec["barotropic"][0] / max(1, sec["barotropic"][1])
@@ -573,6 +583,7 @@ def main():
     ap.add_argument("--config", choices=["c2", "c0", "c1", "c2s"], default="c2")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the precision, batched and serving forms reported beside the FP64 headline")
     args = ap.parse_args()
