@@ -74,6 +74,14 @@ def adv_bytes(ni, nj, nk, ntr):
 TRAFFIC_PER_TRACER_CELL = {"fp64": 5.199e9 / (360 * 270 * 50 * 10), "mixed": 0.975e9 / (360 * 270 * 50 * 10)}
 
 
+# FP64 thread-instructions per tracer-cell of the exact MDFL passes (z + x + y) and per
+# column of one exact barotropic subcycle, from ncu (profiles/fp64_ops_c2block.md); the
+# FP64 rate of GB300 measured on this machine with a probe kernel.
+FP64_OPS_PER_TRACER_CELL = 97.3
+FP64_OPS_PER_COLUMN_SUBCYCLE = 62.5
+FP64_PEAK_OPS = 5.05e11
+
+
 def bt_bytes(ni, nj, nts):
     """Streaming bytes of the barotropic subcycles: 28 FP64 arrays per column per subcycle."""
     return 224 * ni * nj * nts
@@ -225,6 +233,39 @@ def _time_domain(d, stream, ntr, steps, warmup, state, clock_index=0):
     return {"ms": ms, "sec": sec, "launches": d.launches - launches0, "clocks": clk, "step": step}
 
 
+def _fp64_roofline(prec, sec, steps, cells, ntr, ni, nj, nts):
+    """The FP64-pipe roofline of the exact path (the bound of the drop-in)."""
+    from mom5_gb300 import capi
+    if prec != capi.PRECISION_FP64 or ntr == 0 or sec["mdfl"][0] <= 0:
+        return None
+    mdfl_s = sec["mdfl"][0] / steps / 1e3
+    bt_s = sec["barotropic"][0] / steps / 1e3
+    a = FP64_OPS_PER_TRACER_CELL * cells * ntr / mdfl_s
+    b = FP64_OPS_PER_COLUMN_SUBCYCLE * (ni + 2) * (nj + 2) * nts / bt_s
+    return {"bound": "fp64 pipe", "unit": "FP64 instructions/s", "peak": FP64_PEAK_OPS,
+            "peak_source": "probe kernel on this pool (FP64 FMA rate)",
+            "mdfl": {"achieved": round(a, -6), "frac": round(a / FP64_PEAK_OPS, 3),
+                     "ops_per_tracer_cell": FP64_OPS_PER_TRACER_CELL},
+            "barotropic": {"achieved": round(b, -6), "frac": round(b / FP64_PEAK_OPS, 3),
+                           "ops_per_column_subcycle": FP64_OPS_PER_COLUMN_SUBCYCLE},
+            "source": "instruction counts from ncu (profiles/fp64_ops_c2block.md)"}
+
+
+def max_over_ranks(ms: float, device) -> float:
+    """The slowest rank's time (each rank steps its own replica of the workload)."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def whole_job_rate(cells: int, world: int, steps: int, ms: float) -> float:
+    """Cell-updates per second of the whole job: every rank advances `cells` cells
+    per step (replicas, weak scaling), timed by the slowest rank."""
+    return cells * world * steps / (ms / 1e3)
+
+
 def _device_copy(d, fid, n, level):
     """A field of a library domain copied into a new CUDA tensor (device to device)."""
     import torch
@@ -275,12 +316,9 @@ def run_ours(args, rank, world):
     r = _time_domain(d, stream, ntr, args.steps, args.warmup, state, local)
     ms, sec, launches, clk, step = r["ms"], r["sec"], r["launches"], r["clocks"], r["step"]
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
+        ms = max_over_ranks(ms, "cuda")
     ms_step = ms / args.steps
-    value = cells * world * args.steps / (ms / 1e3)
+    value = whole_job_rate(cells, world, args.steps, ms)
 
     # dominant kernel group: the advection step (MDFL passes + explicit update)
     adv_ms = sec["mdfl"][0] + sec["mdfl_mixed"][0] + sec["tracer_update"][0]
@@ -355,6 +393,7 @@ def run_ours(args, rank, world):
            "sections_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sec.items()},
            "barotropic_roofline": {"achieved": round(bt_achieved, 1), "unit": "GB/s", "peak": peak,
                                    "frac": round(bt_achieved / peak, 4), "note": "streaming model, 224 B/column/subcycle"},
+           "fp64_roofline": _fp64_roofline(prec, sec, args.steps, cells, ntr, ni, nj, nts),
            "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline and ntr > 0:
         # bounded sample of the same workload on one host core: one block of 1/16 of the domain

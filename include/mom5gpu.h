@@ -52,6 +52,8 @@ extern "C" {
 #define MOM5GPU_ADVECT_4TH_ORDER 3
 #define MOM5GPU_ADVECT_6TH_ORDER 4
 #define MOM5GPU_ADVECT_QUICKER 5
+#define MOM5GPU_ADVECT_MDFL_SUP_B 7
+#define MOM5GPU_ADVECT_MDPPM 8
 #define MOM5GPU_ADVECT_MDFL_SWEBY 9
 #define MOM5GPU_ADVECT_DST_LINEAR 10
 
@@ -196,6 +198,10 @@ int mom5gpu_set_vertical_grid(mom5gpu_domain* d, const double* dzt, const double
 /* Per-tracer field_table choices (ocean_tracer.F90:982-1066). */
 int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz_scheme, int vert_scheme,
                               double min_tracer_limit, double max_tracer_limit);
+/* Edge limiter of the MDPPM scheme for tracer n (field_table ppm_hlimiter,
+ * default 2): 1 Colella-Woodward 1984, 2 improved full constraint (Lin 2004),
+ * 3 Suresh-Huynh 1997. */
+int mom5gpu_set_ppm_limiter(mom5gpu_domain* d, int n, int ppm_hlimiter);
 
 /* ---- initialisation (after the grid fields are set) ---------------------- */
 /* ocean_tracer_advect_init's scheme set-up: quicker_init (:1442-1586) and

@@ -24,7 +24,7 @@ OK = 0
 EINVAL, ENOMEM, ECUDA, ESTATE, ECFL, ENUMERIC, ETIMEDOUT, EUNSUPPORTED, EFULL = range(-1, -10, -1)
 BGRID, CGRID = 1, 2
 ADVECT_UPWIND, ADVECT_QUICKER, ADVECT_MDFL_SWEBY, ADVECT_DST_LINEAR = 1, 5, 9, 10
-ADVECT_2ND_ORDER, ADVECT_4TH_ORDER, ADVECT_6TH_ORDER = 2, 3, 4
+ADVECT_2ND_ORDER, ADVECT_4TH_ORDER, ADVECT_6TH_ORDER, ADVECT_MDFL_SUP_B, ADVECT_MDPPM = 2, 3, 4, 7, 8
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 
@@ -112,6 +112,7 @@ def lib() -> C.CDLL:
             "mom5gpu_ocean_advection_velocity": (C.c_int, [vp, C.c_int]),
             "mom5gpu_autotune": (C.c_int, [vp, C.c_double, C.c_char_p, C.c_size_t]),
             "mom5gpu_tracer_boundary_terms": (C.c_int, [vp, C.c_int]),
+            "mom5gpu_set_ppm_limiter": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
@@ -272,6 +273,9 @@ class Domain:
         buf = C.create_string_buffer(1024)
         self.check(lib().mom5gpu_autotune(self.h, float(dtime), buf, 1024))
         return buf.value.decode()
+
+    def set_ppm_limiter(self, n, limiter):
+        self.check(lib().mom5gpu_set_ppm_limiter(self.h, n, limiter))
 
     def tracer_boundary_terms(self, n=0):
         self.check(lib().mom5gpu_tracer_boundary_terms(self.h, n))

@@ -478,10 +478,10 @@ int mom5gpu_batch_autotune(mom5gpu_batch* b, double dtime, char* report, size_t 
   struct Cand {
     int rows, tj, bps;
   };
-  static const Cand kMixed[] = {{32, 0, 1}, {32, 0, 2}, {16, 0, 2}, {16, 0, 3}};
+  static const Cand kMixed[] = {{32, 0, 1}, {32, 0, 2}, {16, 0, 2}, {16, 0, 3}, {16, 0, 4}};
   static const Cand kFp64[] = {{32, 2, 2}, {32, 4, 2}, {32, 8, 2}, {32, 16, 2}};
-  const Cand* first = b->prec == MOM5GPU_PRECISION_MIXED ? kMixed : kFp64;
-  std::vector<Cand> cands(first, first + 4);
+  std::vector<Cand> cands = b->prec == MOM5GPU_PRECISION_MIXED ? std::vector<Cand>(kMixed, kMixed + 5)
+                                                                 : std::vector<Cand>(kFp64, kFp64 + 4);
   std::vector<int> idx(b->doms.size()), par(b->doms.size(), 0);
   for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
   std::string rep;

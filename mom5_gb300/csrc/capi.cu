@@ -248,7 +248,7 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
   QuickerWeights& q = d->qw;
   for (double* p : {q.quick_x, q.quick_y, q.curv_xp, q.curv_xn, q.curv_yp, q.curv_yn, q.quick_z, q.curv_zp, q.curv_zn})
     if (p) cudaFree(p);
-  for (double* p : {d->cori1, d->cori2, d->mdfl_a, d->mdfl_b, d->bt, d->red})
+  for (double* p : {d->cori1, d->cori2, d->mdfl_a, d->mdfl_b, d->bt, d->red, d->ppm_scr})
     if (p) cudaFree(p);
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
@@ -311,6 +311,15 @@ int mom5gpu_set_field(mom5gpu_domain* d, int field, int n, int level, const doub
   return MOM5GPU_OK;
 }
 
+int mom5gpu_set_ppm_limiter(mom5gpu_domain* d, int n, int lim) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (n < 1 || n > d->dims.num_prog_tracers) return fail(d, MOM5GPU_EINVAL, "set_ppm_limiter: tracer %d", n);
+  if (lim < 1 || lim > 3)
+    return fail(d, MOM5GPU_EINVAL, "set_ppm_limiter: must choose ppm_hlimiter=1,2 or 3 (got %d)", lim);
+  d->scheme[n - 1].ppm_limiter = lim;
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_get_field(mom5gpu_domain* d, int field, int n, int level, double* dst, int on_device) {
   if (!d || !dst) return d ? fail(d, MOM5GPU_EINVAL, "get_field: null destination") : MOM5GPU_EINVAL;
   double* p;
@@ -342,21 +351,28 @@ int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz, int vert, doub
   if (n < 1 || n > d->dims.num_prog_tracers) return fail(d, MOM5GPU_EINVAL, "set_tracer_scheme: tracer %d", n);
   auto ok = [](int s) {
     return s == MOM5GPU_ADVECT_UPWIND || s == MOM5GPU_ADVECT_2ND_ORDER || s == MOM5GPU_ADVECT_4TH_ORDER ||
-           s == MOM5GPU_ADVECT_6TH_ORDER || s == MOM5GPU_ADVECT_QUICKER || s == MOM5GPU_ADVECT_MDFL_SWEBY ||
-           s == MOM5GPU_ADVECT_DST_LINEAR;
+           s == MOM5GPU_ADVECT_6TH_ORDER || s == MOM5GPU_ADVECT_QUICKER || s == MOM5GPU_ADVECT_MDPPM ||
+           s == MOM5GPU_ADVECT_MDFL_SUP_B || s == MOM5GPU_ADVECT_MDFL_SWEBY || s == MOM5GPU_ADVECT_DST_LINEAR;
   };
   if (!ok(horz) || !ok(vert))
     return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: scheme %d/%d is outside upwind, 2nd/4th/6th order, "
-                                          "quicker, mdfl_sweby, dst_linear", horz, vert);
+                                          "quicker, mdfl_sup_b, mdppm, mdfl_sweby, dst_linear", horz, vert);
+  // MDPPM reads a halo of 4: at least 4 compute points across a cyclic direction
+  if (horz == MOM5GPU_ADVECT_MDPPM && ((d->geo.cx && d->geo.ni < 4) || (d->geo.cy && d->geo.nj < 4)))
+    return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: mdppm needs ni, nj >= 4 across cyclic edges");
   // a halo of 3 (6th order) needs at least 3 compute points across a cyclic direction
   if ((horz == MOM5GPU_ADVECT_6TH_ORDER || horz == MOM5GPU_ADVECT_4TH_ORDER) &&
       ((d->geo.cx && d->geo.ni < 3) || (d->geo.cy && d->geo.nj < 3)))
     return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: 4th/6th order needs ni, nj >= 3 across cyclic edges");
   // ocean_tracer.F90:1076-1087: a 3-D scheme must be chosen for both directions
-  bool h3 = horz == MOM5GPU_ADVECT_MDFL_SWEBY || horz == MOM5GPU_ADVECT_DST_LINEAR;
-  bool v3 = vert == MOM5GPU_ADVECT_MDFL_SWEBY || vert == MOM5GPU_ADVECT_DST_LINEAR;
+  auto three_d = [](int s) {
+    return s == MOM5GPU_ADVECT_MDFL_SWEBY || s == MOM5GPU_ADVECT_DST_LINEAR || s == MOM5GPU_ADVECT_MDPPM ||
+           s == MOM5GPU_ADVECT_MDFL_SUP_B;
+  };
+  bool h3 = three_d(horz), v3 = three_d(vert);
   if (h3 != v3 || (h3 && horz != vert))
-    return fail(d, MOM5GPU_EINVAL, "tracer %d: MDFL/DST must be used for both horizontal and vertical advection", n);
+    return fail(d, MOM5GPU_EINVAL, "tracer %d: a 3-D scheme (MDFL, Super-B, DST, MDPPM) must be used for both horizontal and "
+                                   "vertical advection", n);
   d->scheme[n - 1].horz = horz;
   d->scheme[n - 1].vert = vert;
   d->scheme[n - 1].min_limit = tmin;
@@ -659,6 +675,8 @@ int mom5gpu_horz_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
       if (d->opt.precision == MOM5GPU_PRECISION_MIXED) return launch_mdfl_mixed(d, n, 1, taum1, tau, 0, dtime, false);
       return launch_mdfl(d, false, n, 1, taum1, tau, dtime, 1.0);
     case MOM5GPU_ADVECT_DST_LINEAR: return launch_mdfl(d, false, n, 1, taum1, tau, dtime, 0.0);
+    case MOM5GPU_ADVECT_MDPPM: return launch_mdppm(d, n, taum1, tau, dtime);
+    case MOM5GPU_ADVECT_MDFL_SUP_B: return launch_mdfl_sup_b(d, n, taum1, tau, dtime);
   }
   return fail(d, MOM5GPU_EINVAL, "horz_advect_tracer: invalid horz advection scheme");
 }
@@ -680,7 +698,9 @@ int mom5gpu_vert_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
       if (!d->qw.quick_z) return fail(d, MOM5GPU_ESTATE, "quicker needs mom5gpu_set_vertical_grid before init");
       return launch_quicker_vert(d, n, taum1, tau);
     case MOM5GPU_ADVECT_MDFL_SWEBY:
-    case MOM5GPU_ADVECT_DST_LINEAR: return MOM5GPU_OK;  // 3-D schemes: done in horz_advect_tracer
+    case MOM5GPU_ADVECT_DST_LINEAR:
+    case MOM5GPU_ADVECT_MDFL_SUP_B:
+    case MOM5GPU_ADVECT_MDPPM: return MOM5GPU_OK;  // 3-D schemes: done in horz_advect_tracer
   }
   return fail(d, MOM5GPU_EINVAL, "vert_advect_tracer: invalid advection scheme");
 }

@@ -37,6 +37,7 @@ struct TracerScheme {
   int vert = MOM5GPU_ADVECT_MDFL_SWEBY;
   double min_limit = -1.0e10;
   double max_limit = 1.0e10;
+  int ppm_limiter = 2;  // ppm_hlimiter (ocean_tpm_util.F90:87): 1 cw84, 2 ifc, 3 sh
 };
 
 // Quicker weights on the device (quicker_init, ocean_tracer_advect.F90:1442-1586).
@@ -85,6 +86,7 @@ struct mom5gpu_domain {
   size_t mixed_cap = 0;
   double* bt = nullptr;        // barotropic scratch
   int* kmt_d = nullptr;        // device copy of kmt (uploaded on first use)
+  double* ppm_scr = nullptr;   // MDPPM slope and vertical-flux scratch, 2 x n3
   double* red = nullptr;       // reduction scratch (device)
   double* red_h = nullptr;     // pinned host result
   int* flag = nullptr;         // device flag word
@@ -223,6 +225,8 @@ void launch_btf_prep(const BtArgs& a, cudaStream_t s);
 void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, cudaStream_t s);
 int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz);
 int ensure_kmt_device(mom5gpu_domain* d);
+int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
+int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
 int launch_tracer_boundary(mom5gpu_domain* d, int n);
 int launch_barotropic_forcing(mom5gpu_domain* d);
 int launch_advection_velocity(mom5gpu_domain* d, int tau);

@@ -22,7 +22,7 @@ DEVI int find_entry_m(const int* prefix, int count, int b) {
 }
 
 template <int NC, int ZR>
-__global__ void __launch_bounds__(NT, ZR == 16 ? 3 : 2) kb_mixed(const MixArgs* d, BatchWork w, int* counter) {
+__global__ void __launch_bounds__(NT, ZR == 16 ? 4 : 2) kb_mixed(const MixArgs* d, BatchWork w, int* counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
   __shared__ int item;

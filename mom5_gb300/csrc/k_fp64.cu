@@ -13,6 +13,7 @@
 
 #include "internal.h"
 #include "fp64_bodies.cuh"
+#include "mdppm_body.cuh"
 
 namespace mom5 {
 
@@ -592,6 +593,330 @@ int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz) {
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "centred advection");
+}
+
+// ---------------------------------------------------------------------------
+// MDFL Super-B (advect_tracer_mdfl_sup_b, ocean_tracer_advect.F90:3189-3466):
+// level by level z, x, y with the superbee limiter.  Levels are independent
+// (the z flux of the level above is recomputed), so each pass is one kernel
+// over all cells: z (tracer -> tz), x (tz with its halo image -> tx), y and
+// the tendency.  tmask_mdfl is the halo-2 byte mask.
+// ---------------------------------------------------------------------------
+struct SupbArgs {
+  Geo g;
+  double dtime;
+  const uint8_t* mask2;
+  const double *tmask, *dat, *datr, *dxte, *dyte, *dxtn, *dytn, *uh, *vh, *w, *rdz, *T;
+  double *tz, *tx, *th;
+};
+
+DEVI double m2d(const SupbArgs& a, int i, int j, int k) { return a.mask2[IM(a.g, i, j, k)] ? 1.0 : 0.0; }
+
+// face flux 0.5*(mf*(Ta+Tb) - |mf|*(1 + (cfl-1)*Cr)*Rj)*m0*m1 with the superbee limiter (:3244-3263)
+DEVI double supb_flux(double mf, double cfl, double Rjm, double Rj, double Rjp, double Ta, double Tb, double m0,
+                      double m1) {
+  double Cr;
+  if (Rj != 0.0) Cr = mf > 0.0 ? Rjm / Rj : Rjp / Rj;
+  else Cr = mf > 0.0 ? Rjm * 1.0e20 : Rjp * 1.0e20;
+  double c2 = 2.0 * Cr;
+  double lo = 1.0 < c2 ? 1.0 : c2, hi = 2.0 < Cr ? 2.0 : Cr;
+  double mx = lo > hi ? lo : hi;
+  Cr = 0.0 > mx ? 0.0 : mx;
+  return 0.5 * (mf * (Ta + Tb) - fabs(mf) * (1.0 + (cfl - 1.0) * Cr) * Rj) * m0 * m1;
+}
+
+DEVI double supb_zflux(const SupbArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1, kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1, km1 = k > 0 ? k - 1 : 0;
+  double Tk = a.T[I3(g, i, j, k)], Tkp1 = a.T[I3(g, i, j, kp1)];
+  double Rjp = (a.T[I3(g, i, j, km1)] - Tk) * m2d(a, i, j, km1) * m2d(a, i, j, k);
+  double Rj = (Tk - Tkp1) * m2d(a, i, j, k) * m2d(a, i, j, kp1);
+  double Rjm = (Tkp1 - a.T[I3(g, i, j, kp2)]) * m2d(a, i, j, kp1) * m2d(a, i, j, kp2);
+  double w = a.w[I3(g, i, j, k + 1)];
+  double cfl = fabs(w * a.dtime / a.rdz[I3(g, i, j, k)]);
+  return supb_flux(a.dat[I2(g, i, j)] * w, cfl, Rjm, Rj, Rjp, Tk, Tkp1, m2d(a, i, j, kp1), m2d(a, i, j, k));
+}
+
+__global__ void k_supb_z(SupbArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  if (i > g.ni) return;
+  long p = I3(g, i, j, k);
+  double fbt = supb_zflux(a, i, j, k);
+  double ftp = k > 0 ? supb_zflux(a, i, j, k - 1) : 0.0;
+  double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
+  double Tk = a.T[p];
+  a.tz[p] = Tk + a.dtime / a.rdz[p] * (a.datr[I2(g, i, j)] * (fbt - ftp) + Tk * (wkm1 - a.w[I3(g, i, j, k + 1)]));
+}
+
+DEVI double supb_xflux(const SupbArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  auto t = [&](int ii) { return tq(g, a.tz, ii, j, k); };
+  double Rjp = (t(i + 2) - t(i + 1)) * m2d(a, i + 2, j, k) * m2d(a, i + 1, j, k);
+  double Rj = (t(i + 1) - t(i)) * m2d(a, i + 1, j, k) * m2d(a, i, j, k);
+  double Rjm = (t(i) - t(i - 1)) * m2d(a, i, j, k) * m2d(a, i - 1, j, k);
+  double u = a.uh[I3(g, i, j, k)];
+  double cfl = fabs(u * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
+  return supb_flux(a.dyte[I2(g, i, j)] * u, cfl, Rjm, Rj, Rjp, t(i + 1), t(i), m2d(a, i, j, k), m2d(a, i + 1, j, k));
+}
+
+__global__ void k_supb_x(SupbArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  if (i > g.ni) return;
+  long p = I3(g, i, j, k);
+  double div = a.dyte[I2(g, i, j)] * a.uh[p] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
+  a.tx[p] = a.tz[p] + a.dtime * m2d(a, i, j, k) * a.datr[I2(g, i, j)] / a.rdz[p] *
+                          (supb_xflux(a, i - 1, j, k) - supb_xflux(a, i, j, k) + a.T[p] * div);
+}
+
+DEVI double supb_yflux(const SupbArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  auto t = [&](int jj) { return tq(g, a.tx, i, jj, k); };
+  double Rjp = (t(j + 2) - t(j + 1)) * m2d(a, i, j + 2, k) * m2d(a, i, j + 1, k);
+  double Rj = (t(j + 1) - t(j)) * m2d(a, i, j + 1, k) * m2d(a, i, j, k);
+  double Rjm = (t(j) - t(j - 1)) * m2d(a, i, j, k) * m2d(a, i, j - 1, k);
+  double v = a.vh[I3(g, i, j, k)];
+  double cfl = fabs(v * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
+  return supb_flux(a.dxtn[I2(g, i, j)] * v, cfl, Rjm, Rj, Rjp, t(j + 1), t(j), m2d(a, i, j, k), m2d(a, i, j + 1, k));
+}
+
+__global__ void k_supb_y(SupbArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  if (i > g.ni) return;
+  long p = I3(g, i, j, k);
+  double rdz = a.rdz[p], datr = a.datr[I2(g, i, j)], T = a.T[p];
+  double t = a.tx[p] + a.dtime * a.tmask[p] * datr / rdz * (supb_yflux(a, i, j - 1, k) - supb_yflux(a, i, j, k));
+  double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
+  t = t + a.dtime * T / rdz *
+              (a.w[I3(g, i, j, k + 1)] - wkm1 +
+               datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] - a.dyte[I2(g, i, j)] * a.uh[p]));
+  double advect = -rdz * (t - T) / a.dtime * m2d(a, i, j, k);
+  a.th[p] = a.th[p] + (-advect);
+}
+
+int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
+  const Geo& g = d->geo;
+  int rc = ensure_mdfl_scratch(d, 1);
+  if (rc) return rc;
+  SupbArgs a;
+  a.g = g;
+  a.dtime = dtime;
+  a.mask2 = d->mask2;
+  a.tmask = fptr(d, MOM5GPU_TMASK, 0, 0);
+  a.dat = fptr(d, MOM5GPU_DAT, 0, 0);
+  a.datr = fptr(d, MOM5GPU_DATR, 0, 0);
+  a.dxte = fptr(d, MOM5GPU_DXTE, 0, 0);
+  a.dyte = fptr(d, MOM5GPU_DYTE, 0, 0);
+  a.dxtn = fptr(d, MOM5GPU_DXTN, 0, 0);
+  a.dytn = fptr(d, MOM5GPU_DYTN, 0, 0);
+  a.uh = fptr(d, MOM5GPU_UHRHO_ET, 0, 0);
+  a.vh = fptr(d, MOM5GPU_VHRHO_NT, 0, 0);
+  a.w = fptr(d, MOM5GPU_WRHO_BT, 0, 0);
+  a.rdz = fptr(d, MOM5GPU_RHO_DZT, 0, tau);
+  a.T = fptr(d, MOM5GPU_TRACER, n, taum1);
+  a.th = fptr(d, MOM5GPU_TH_TENDENCY, n, 0);
+  a.tz = d->mdfl_a;
+  a.tx = d->mdfl_b;
+  const void* need[] = {a.mask2, a.tmask, a.dat, a.datr, a.dxte, a.dyte, a.dxtn, a.dytn, a.uh, a.vh, a.w, a.rdz,
+                        a.T, a.th};
+  for (const void* p : need)
+    if (!p) return fail(d, MOM5GPU_ESTATE, "mdfl_sup_b: a required field was never set");
+  ClockScope clk(d, SEC_MDFL);
+  count_launches(d, 3);
+  dim3 g3((g.ni + 127) / 128, g.nj, g.nk);
+  k_supb_z<<<g3, 128, 0, d->stream>>>(a);
+  k_supb_x<<<g3, 128, 0, d->stream>>>(a);
+  k_supb_y<<<g3, 128, 0, d->stream>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "mdfl_sup_b");
+}
+
+// ---------------------------------------------------------------------------
+// MDPPM (ocean_tracer_advect.F90:5990-6507): vertical pass in three kernels
+// (slopes, fluxes by a march down each column, update), then the x and y
+// passes streaming along lines (mdppm_body.cuh).
+// ---------------------------------------------------------------------------
+struct PpmArgs {
+  Geo g;
+  int lim;
+  double dtime;
+  const double *tmask, *dat, *datr, *dxte, *dyte, *dxtn, *dytn, *uh, *vh, *w, *rdz, *T;
+  double *dak, *fz, *tz, *tx, *th;
+};
+
+// vertical slope dak of every cell with the clamped neighbour levels and their
+// collapse factors real(kp1-k) ... (:6064-6099)
+__global__ void k_ppm_dak(PpmArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  if (i > g.ni) return;
+  const int nk = g.nk, K = k + 1;
+  int km2 = K - 2 > 1 ? K - 2 : 1, km1 = K - 1 > 1 ? K - 1 : 1, kp1 = K + 1 < nk ? K + 1 : nk,
+      kp2 = K + 2 < nk ? K + 2 : nk;
+  auto at = [&](const double* f, int L) { return f[I3(g, i, j, L - 1)]; };
+  double S[5] = {at(a.T, km2), at(a.T, km1), at(a.T, K), at(a.T, kp1), at(a.T, kp2)};
+  double M[5] = {at(a.tmask, km2) * (double)(km1 - km2), at(a.tmask, km1) * (double)(K - km1), at(a.tmask, K),
+                 at(a.tmask, kp1) * (double)(kp1 - K), at(a.tmask, kp2) * (double)(kp2 - kp1)};
+  double t0, t1, t2, t3;
+  ppm::slope(S, M, a.dak[I3(g, i, j, k)], t0, t1, t2, t3);
+}
+
+// edge values, limiter and the fluxes through the bottom (massflux <= 0) and top
+// (massflux > 0) faces of every cell of a column (:6101-6170)
+__global__ void k_ppm_zflux(PpmArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+  if (i > g.ni) return;
+  const int nk = g.nk;
+  const long q = I2(g, i, j);
+  auto at = [&](const double* f, int L) { return f[I3(g, i, j, L - 1)]; };
+  const double dat = a.dat[q];
+  for (int K = 1; K <= nk; ++K) {
+    int km2 = K - 2 > 1 ? K - 2 : 1, km1 = K - 1 > 1 ? K - 1 : 1, kp1 = K + 1 < nk ? K + 1 : nk,
+        kp2 = K + 2 < nk ? K + 2 : nk;
+    double mskp2 = at(a.tmask, kp2) * (double)(kp2 - kp1), mskp1 = at(a.tmask, kp1) * (double)(kp1 - K);
+    double msk0 = at(a.tmask, K), mskm1 = at(a.tmask, km1) * (double)(K - km1);
+    double mskm2 = at(a.tmask, km2) * (double)(km1 - km2);
+    double Sip2 = at(a.T, kp2), Sip1 = at(a.T, kp1), Si = at(a.T, K), Sim1 = at(a.T, km1), Sim2 = at(a.T, km2);
+    double d1m = (Si - Sim1) * mskm1, d1p = (Sip1 - Si) * mskp1;
+    double d1mm = (Sim1 - Sim2) * mskm1 * mskm2, d1pp = (Sip2 - Sip1) * mskp1 * mskp2;
+    Sim1 = Si - d1m;
+    Sip1 = Si + d1p;
+    double dk = at(a.dak, K);
+    double al = 0.5 * (Sim1 + Si) + ppm::kSixth * (at(a.dak, km1) - dk);
+    double ar = 0.5 * (Si + Sip1) + ppm::kSixth * (dk - at(a.dak, kp1));
+    ppm::limit(a.lim, Si, dk, d1m, d1p, d1mm, d1pp, al, ar);
+    double c6 = 6. * Si - 3. * (ar + al);
+    double wk = a.w[I3(g, i, j, K)];
+    double massflux = dat * wk * msk0 * mskp1;
+    if (massflux <= 0.0) {
+      double cfl = fabs(wk * a.dtime / at(a.rdz, K));
+      a.fz[I3(g, i, j, K - 1)] = massflux * (ar + 0.5 * cfl * ((al - ar) + (1. - ppm::kTwoThirds * cfl) * c6));
+    }
+    double wkm1 = a.w[I3(g, i, j, km1)];
+    massflux = dat * wkm1 * msk0 * mskm1;
+    if (massflux > 0.0) {
+      double cfl = fabs(wkm1 * a.dtime / at(a.rdz, km1));
+      a.fz[I3(g, i, j, km1 - 1)] = massflux * (al + 0.5 * cfl * ((ar - al) + (1. - ppm::kTwoThirds * cfl) * c6));
+    }
+  }
+}
+
+// vertical update of tracer_mdppm (:6173-6182)
+__global__ void k_ppm_zupd(PpmArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  if (i > g.ni) return;
+  const int K = k + 1, km1 = K - 1 > 1 ? K - 1 : 1;
+  const double mskm1 = (double)(K - km1);
+  long p = I3(g, i, j, k), pm = I3(g, i, j, km1 - 1);
+  double T = a.T[p];
+  a.tz[p] = T + a.dtime / a.rdz[p] *
+                    (a.datr[I2(g, i, j)] * (a.fz[p] - mskm1 * a.fz[pm]) +
+                     T * (mskm1 * a.w[I3(g, i, j, km1)] - a.w[I3(g, i, j, K)]));
+}
+
+// x pass along each row (:6193-6325): tracer_mdppm after the x halo update
+__global__ void k_ppm_x(PpmArgs a) {
+  const Geo& g = a.g;
+  int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= g.nj * g.nk) return;
+  const int j = line % g.nj + 1, k = line / g.nj;
+  const double dt = a.dtime;
+  auto S = [&](int i) { return tq(g, a.tz, i, j, k); };
+  auto M = [&](int i) { return tq(g, a.tmask, i, j, k); };
+  auto face = [&](int i, double m0, double m1, double aL0, double aR0, double a60, double aL1, double aR1,
+                  double a61) {
+    double u = a.uh[I3(g, i, j, k)];
+    double massflux = a.dyte[I2(g, i, j)] * u;
+    double cfl = u * dt * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]);
+    return ppm::hflux(massflux, m0, m1, cfl, aL0, aR0, a60, aL1, aR1, a61);
+  };
+  auto upd = [&](int i, double Sv, double m, double Fw, double Fe) {
+    long p = I3(g, i, j, k);
+    double div = a.dyte[I2(g, i, j)] * a.uh[p] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
+    a.tx[p] = Sv + dt * m * a.datr[I2(g, i, j)] / a.rdz[p] * (Fw - Fe + a.T[p] * div);
+  };
+  ppm::stream_line(g.ni, a.lim, S, M, face, upd);
+}
+
+// y pass along each column (:6330-6502) and the tendency: th += -advect_tracer_mdppm
+__global__ void k_ppm_y(PpmArgs a) {
+  const Geo& g = a.g;
+  int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= g.ni * g.nk) return;
+  const int i = line % g.ni + 1, k = line / g.ni;
+  const double dt = a.dtime;
+  auto S = [&](int j) { return tq(g, a.tx, i, j, k); };
+  auto M = [&](int j) { return tq(g, a.tmask, i, j, k); };
+  auto face = [&](int j, double m0, double m1, double aL0, double aR0, double a60, double aL1, double aR1,
+                  double a61) {
+    double v = a.vh[I3(g, i, j, k)];
+    double massflux = a.dxtn[I2(g, i, j)] * v;
+    double cfl = v * dt * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]);
+    return ppm::hflux(massflux, m0, m1, cfl, aL0, aR0, a60, aL1, aR1, a61);
+  };
+  auto upd = [&](int j, double Sv, double m, double Fs, double Fn) {
+    long p = I3(g, i, j, k);
+    double rdz = a.rdz[p], datr = a.datr[I2(g, i, j)], T = a.T[p];
+    double t = Sv + dt * a.tmask[p] * datr / rdz * (Fs - Fn);
+    double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
+    t = t + dt * T / rdz *
+                (a.w[I3(g, i, j, k + 1)] - wkm1 +
+                 datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] - a.dyte[I2(g, i, j)] * a.uh[p]));
+    double advect = -rdz * (t - T) / dt * m;
+    a.th[p] = a.th[p] + (-advect);
+  };
+  ppm::stream_line(g.nj, a.lim, S, M, face, upd);
+}
+
+int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
+  const Geo& g = d->geo;
+  int rc = ensure_mdfl_scratch(d, 1);
+  if (rc) return rc;
+  if (!d->ppm_scr) {
+    cudaError_t e = cudaMalloc(&d->ppm_scr, sizeof(double) * 2 * (size_t)g.n3);
+    if (e != cudaSuccess) return fail(d, MOM5GPU_ENOMEM, "mdppm scratch: %s", cudaGetErrorString(e));
+    d->bytes += sizeof(double) * 2 * (size_t)g.n3;
+    cudaMemsetAsync(d->ppm_scr, 0, sizeof(double) * 2 * (size_t)g.n3, d->stream);
+  }
+  PpmArgs a;
+  a.g = g;
+  a.lim = d->scheme[n - 1].ppm_limiter;
+  a.dtime = dtime;
+  a.tmask = fptr(d, MOM5GPU_TMASK, 0, 0);
+  a.dat = fptr(d, MOM5GPU_DAT, 0, 0);
+  a.datr = fptr(d, MOM5GPU_DATR, 0, 0);
+  a.dxte = fptr(d, MOM5GPU_DXTE, 0, 0);
+  a.dyte = fptr(d, MOM5GPU_DYTE, 0, 0);
+  a.dxtn = fptr(d, MOM5GPU_DXTN, 0, 0);
+  a.dytn = fptr(d, MOM5GPU_DYTN, 0, 0);
+  a.uh = fptr(d, MOM5GPU_UHRHO_ET, 0, 0);
+  a.vh = fptr(d, MOM5GPU_VHRHO_NT, 0, 0);
+  a.w = fptr(d, MOM5GPU_WRHO_BT, 0, 0);
+  a.rdz = fptr(d, MOM5GPU_RHO_DZT, 0, tau);
+  a.T = fptr(d, MOM5GPU_TRACER, n, taum1);
+  a.th = fptr(d, MOM5GPU_TH_TENDENCY, n, 0);
+  a.dak = d->ppm_scr;
+  a.fz = d->ppm_scr + g.n3;
+  a.tz = d->mdfl_a;
+  a.tx = d->mdfl_b;
+  const void* need[] = {a.tmask, a.dat, a.datr, a.dxte, a.dyte, a.dxtn, a.dytn, a.uh, a.vh, a.w, a.rdz, a.T, a.th};
+  for (const void* p : need)
+    if (!p) return fail(d, MOM5GPU_ESTATE, "mdppm: a required field was never set");
+  ClockScope clk(d, SEC_MDFL);
+  count_launches(d, 5);
+  cudaStream_t s = d->stream;
+  dim3 g3((g.ni + 127) / 128, g.nj, g.nk), g2((g.ni + 127) / 128, g.nj);
+  k_ppm_dak<<<g3, 128, 0, s>>>(a);
+  k_ppm_zflux<<<g2, 128, 0, s>>>(a);
+  k_ppm_zupd<<<g3, 128, 0, s>>>(a);
+  k_ppm_x<<<(unsigned)((g.nj * g.nk + 127) / 128), 128, 0, s>>>(a);
+  k_ppm_y<<<(unsigned)((g.ni * g.nk + 127) / 128), 128, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "mdppm");
 }
 
 // ---------------------------------------------------------------------------

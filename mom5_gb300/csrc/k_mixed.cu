@@ -29,7 +29,7 @@ using namespace mixed;
 namespace {
 
 template <int NC, int ZR>
-__global__ void __launch_bounds__(NT, ZR == 16 ? 3 : 2) k_mdfl_mixed(MixArgs a, int n0) {
+__global__ void __launch_bounds__(NT, ZR == 16 ? 4 : 2) k_mdfl_mixed(MixArgs a, int n0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
   mixed_tile<NC, ZR>(a, n0, blockIdx.x, blockIdx.y, s);

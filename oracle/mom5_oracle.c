@@ -216,6 +216,19 @@ static double halo_value(const orc_dims* d, const double* a, int i, int j, int k
   return a[I3(d, i, j, k)];
 }
 
+/* 2-D version (one level of a data-domain array) */
+static double halo_value2d(const orc_dims* d, const double* a, int i, int j) {
+  if (i < 1 || i > d->ni) {
+    if (!d->cyclic_x) return 0.0;
+    i = i < 1 ? i + d->ni : i - d->ni;
+  }
+  if (j < 1 || j > d->nj) {
+    if (!d->cyclic_y) return 0.0;
+    j = j < 1 ? j + d->nj : j - d->nj;
+  }
+  return a[I2(d, i, j)];
+}
+
 void orc_horz_advect_centred(const orc_dims* d, int order, const double* tmask, const double* dyte,
                              const double* dxtn, const double* datr, const double* uhrho_et, const double* vhrho_nt,
                              const double* T, double* wrk1) {
@@ -305,6 +318,381 @@ void orc_vert_advect_centred(const orc_dims* d, int order, const double* tmask, 
         ft1 = ft2;
       }
     }
+}
+
+/* ------------------------------------------------------------------------- */
+/* MDFL Super-B: advect_tracer_mdfl_sup_b (ocean_tracer_advect.F90:3189-3466),*/
+/* split level by level: z flux on the tracer, update, halo update of the    */
+/* level, x fluxes on the z-updated level, update, halo update, y fluxes,    */
+/* update, divergence correction.  Superbee limiter on Cr = R/Rj (R*1e20 for */
+/* Rj = 0).  tmask_mdfl is the halo-2 mask.  Returns wrk1 = -advect.        */
+/* ------------------------------------------------------------------------- */
+static double superbee(double Cr) { return fmaxd(0.0, fmaxd(fmind(1.0, 2.0 * Cr), fmind(2.0, Cr))); }
+
+void orc_advect_mdfl_sup_b(const orc_dims* d, double dtime, const double* tmask, const double* dat,
+                           const double* datr, const double* dxte, const double* dyte, const double* dxtn,
+                           const double* dytn, const double* uhrho_et, const double* vhrho_nt, const double* wrho_bt,
+                           const double* rho_dzt, const double* T, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d), n3 = n2 * nk;
+  double* mk = (double*)calloc((size_t)NX2(d) * NY2(d) * nk, sizeof(double)); /* tmask_mdfl, halo 2 */
+  orc_mask_halo2(d, tmask, mk);
+#define TM2(i, j, k) mk[H3(d, i, j, k)]
+  double* ftp = (double*)calloc(n2, sizeof(double));
+  double* wkm1 = (double*)calloc(n2, sizeof(double));
+  double* tz = (double*)calloc(n2, sizeof(double)); /* tmp_updated_tracer, one level */
+  double* tx = (double*)calloc(n2, sizeof(double));
+  double* fe = (double*)calloc(n2, sizeof(double));
+  double* fn = (double*)calloc(n2, sizeof(double));
+  memset(wrk1, 0, sizeof(double) * n3);
+  for (int k = 0; k < nk; ++k) {
+    int kp1 = k + 1 < nk ? k + 1 : nk - 1, kp2 = k + 2 < nk ? k + 2 : nk - 1, km1 = k > 0 ? k - 1 : 0;
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        size_t q = I2(d, i, j);
+        double Tk = T[I3(d, i, j, k)], Tkp1 = T[I3(d, i, j, kp1)];
+        double Rjp = (T[I3(d, i, j, km1)] - Tk) * TM2(i, j, km1) * TM2(i, j, k);
+        double Rj = (Tk - Tkp1) * TM2(i, j, k) * TM2(i, j, kp1);
+        double Rjm = (Tkp1 - T[I3(d, i, j, kp2)]) * TM2(i, j, kp1) * TM2(i, j, kp2);
+        double w = wrho_bt[I3(d, i, j, k + 1)];
+        double massflux = dat[q] * w;
+        double cfl = fabs(w * dtime / rho_dzt[I3(d, i, j, k)]);
+        double Cr;
+        if (Rj != 0.0) Cr = massflux > 0.0 ? Rjm / Rj : Rjp / Rj;
+        else Cr = massflux > 0.0 ? Rjm * 1.0e20 : Rjp * 1.0e20;
+        Cr = superbee(Cr);
+        double fbt = 0.5 * (massflux * (Tk + Tkp1) - fabs(massflux) * (1.0 + (cfl - 1) * Cr) * Rj) *
+                     TM2(i, j, kp1) * TM2(i, j, k);
+        tz[q] = Tk + dtime / rho_dzt[I3(d, i, j, k)] * (datr[q] * (fbt - ftp[q]) + Tk * (wkm1[q] - w));
+        ftp[q] = fbt;
+      }
+    /* halo update of the level: periodic image of the compute values, else the
+     * (zero) halo the array was created with */
+#define HV(a, i, j) halo_value2d(d, a, i, j)
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        double Rjp = (HV(tz, i + 2, j) - HV(tz, i + 1, j)) * TM2(i + 2, j, k) * TM2(i + 1, j, k);
+        double Rj = (HV(tz, i + 1, j) - HV(tz, i, j)) * TM2(i + 1, j, k) * TM2(i, j, k);
+        double Rjm = (HV(tz, i, j) - HV(tz, i - 1, j)) * TM2(i, j, k) * TM2(i - 1, j, k);
+        double u = uhrho_et[I3(d, i, j, k)];
+        double massflux = dyte[I2(d, i, j)] * u;
+        double cfl = fabs(u * dtime * 2.0 / ((rho_dzt[I3(d, i, j, k)] + rho_dzt[I3(d, i + 1, j, k)]) * dxte[I2(d, i, j)]));
+        double Cr;
+        if (Rj != 0.0) Cr = massflux > 0.0 ? Rjm / Rj : Rjp / Rj;
+        else Cr = massflux > 0.0 ? Rjm * 1.0e20 : Rjp * 1.0e20;
+        Cr = superbee(Cr);
+        fe[I2(d, i, j)] = 0.5 * (massflux * (HV(tz, i + 1, j) + HV(tz, i, j)) -
+                                 fabs(massflux) * (1.0 + (cfl - 1) * Cr) * Rj) *
+                          TM2(i, j, k) * TM2(i + 1, j, k);
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        size_t q = I2(d, i, j);
+        size_t p = I3(d, i, j, k);
+        tx[q] = tz[q] + dtime * TM2(i, j, k) * datr[q] / rho_dzt[p] *
+                            (fe[I2(d, i - 1, j)] - fe[q] +
+                             T[p] * (dyte[q] * uhrho_et[p] - dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)]));
+      }
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double Rjp = (HV(tx, i, j + 2) - HV(tx, i, j + 1)) * TM2(i, j + 2, k) * TM2(i, j + 1, k);
+        double Rj = (HV(tx, i, j + 1) - HV(tx, i, j)) * TM2(i, j + 1, k) * TM2(i, j, k);
+        double Rjm = (HV(tx, i, j) - HV(tx, i, j - 1)) * TM2(i, j, k) * TM2(i, j - 1, k);
+        double v = vhrho_nt[I3(d, i, j, k)];
+        double massflux = dxtn[I2(d, i, j)] * v;
+        double cfl = fabs(v * dtime * 2.0 / ((rho_dzt[I3(d, i, j, k)] + rho_dzt[I3(d, i, j + 1, k)]) * dytn[I2(d, i, j)]));
+        double Cr;
+        if (Rj != 0.0) Cr = massflux > 0.0 ? Rjm / Rj : Rjp / Rj;
+        else Cr = massflux > 0.0 ? Rjm * 1.0e20 : Rjp * 1.0e20;
+        Cr = superbee(Cr);
+        fn[I2(d, i, j)] = 0.5 * (massflux * (HV(tx, i, j + 1) + HV(tx, i, j)) -
+                                 fabs(massflux) * (1.0 + (cfl - 1.0) * Cr) * Rj) *
+                          TM2(i, j, k) * TM2(i, j + 1, k);
+      }
+#undef HV
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        size_t q = I2(d, i, j);
+        size_t p = I3(d, i, j, k);
+        double t = tx[q] + dtime * tmask[p] * datr[q] / rho_dzt[p] * (fn[I2(d, i, j - 1)] - fn[q]);
+        t = t + dtime * T[p] / rho_dzt[p] *
+                    (wrho_bt[I3(d, i, j, k + 1)] - wkm1[q] +
+                     datr[q] * ((dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)] - dyte[q] * uhrho_et[p])));
+        double advect = -rho_dzt[p] * (t - T[p]) / dtime * TM2(i, j, k);
+        wrk1[p] = -advect;
+        wkm1[q] = wrho_bt[I3(d, i, j, k + 1)];
+      }
+  }
+#undef TM2
+  free(mk);
+  free(ftp);
+  free(wkm1);
+  free(tz);
+  free(tx);
+  free(fe);
+  free(fn);
+}
+
+/* ------------------------------------------------------------------------- */
+/* MDPPM: advect_tracer_mdppm (ocean_tracer_advect.F90:5990-6507) with the   */
+/* edge limiters ppm_limit_cw84 (:6510-6538), ppm_limit_ifc (:6555-6580) and */
+/* ppm_limit_sh (:6601-6660) selected by ppm_hlimiter (1, 2, 3) for all      */
+/* three directions, as the reference does; tracer_mdppm and tmask_mdppm     */
+/* carry a halo of 4 (mdppm_init :1702-1735).  Returns wrk1 = -advect.       */
+/* ------------------------------------------------------------------------- */
+static const double ppm_r12 = 1.0 / 12.0, ppm_sixth = 1.0 / 6.0, ppm_2_3 = 2.0 / 3.0, ppm_4_3 = 4.0 / 3.0;
+
+static double fmax3(double a, double b, double c) { return fmaxd(fmaxd(a, b), c); }
+static double fmin3(double a, double b, double c) { return fmind(fmind(a, b), c); }
+static double fmax4(double a, double b, double c, double e) { return fmaxd(fmaxd(fmaxd(a, b), c), e); }
+static double fmin4(double a, double b, double c, double e) { return fmind(fmind(fmind(a, b), c), e); }
+
+/* slope da (Lin 1994 B2 with the masked 3rd/2nd-order estimate) and the differences d1* of cell S[2] */
+static void ppm_slope(const double* S, const double* M, double* da, double* d1m, double* d1p, double* d1mm,
+                      double* d1pp) {
+  /* S, M: values at offsets -2..+2 (index 0..4); M already includes the level-collapse factors */
+  double Sim2 = S[0], Sim1 = S[1], Si = S[2], Sip1 = S[3], Sip2 = S[4];
+  double mskm2 = M[0], mskm1 = M[1], msk0 = M[2], mskp1 = M[3], mskp2 = M[4];
+  double da2 = 0.5 * (Sip1 - Sim1);
+  double da3m = ppm_r12 * (2. * Sim2 - 12. * Sim1 + 6. * Si + 4. * Sip1);
+  double da3p = ppm_r12 * (-(4. * Sim1) - 6. * Si + 12. * Sip1 - 2. * Sip2);
+  double a = ((mskm2 * (1. - 0.5 * mskp2) * da3m + mskp2 * (1. - 0.5 * mskm2) * da3p) +
+              (1. - mskm2) * (1. - mskp2) * da2);
+  double dMx = fmax3(Sip1, Sim1, Si) - Si;
+  double dMn = Si - fmin3(Sip1, Sim1, Si);
+  *da = copysign(1., a) * fmind(fabs(a), 2. * fmind(dMx, dMn)) * mskm1 * mskp1 * msk0;
+  *d1m = (Si - Sim1) * mskm1;
+  *d1p = (Sip1 - Si) * mskp1;
+  *d1mm = (Sim1 - Sim2) * mskm1 * mskm2;
+  *d1pp = (Sip2 - Sip1) * mskp1 * mskp2;
+}
+
+static void ppm_limit(int lim, double Si, double da, double d1m, double d1p, double d1mm, double d1pp, double* aL,
+                      double* aR) {
+  if (lim == 1) { /* Colella and Woodward 1984, Eq. 1.10 */
+    if ((*aR - Si) * (Si - *aL) <= 0.) {
+      *aL = Si;
+      *aR = Si;
+    }
+    double da2 = *aR - *aL, da4 = 0.5 * (*aR + *aL);
+    double da3m = 6. * da2 * (Si - da4), da3p = da2 * da2;
+    if (da3m > da3p) *aL = 3. * Si - 2. * *aR;
+    if (da3m < -da3p) *aR = 3. * Si - 2. * *aL;
+  } else if (lim == 2) { /* improved full constraint, Lin 2004 */
+    double ada = fabs(da), sda = copysign(1., da);
+    *aL = Si - sda * fmind(ada, fabs(*aL - Si));
+    *aR = Si + sda * fmind(ada, fabs(*aR - Si));
+  } else { /* Suresh and Huynh 1997 */
+    double Sim1 = Si - d1m, Sip1 = Si + d1p;
+    double z = d1m - d1mm, w = d1p - d1m;
+    double x = 4. * w - z, y = 4. * z - w;
+    double dM4m = fmaxd(0., fmin4(x, y, z, w)) + fmind(0., fmax4(x, y, z, w));
+    z = d1pp - d1p;
+    x = 4. * w - z;
+    y = 4. * z - w;
+    double dM4p = fmaxd(0., fmin4(x, y, z, w)) + fmind(0., fmax4(x, y, z, w));
+    double qAV = 0.5 * (Si + Sip1);
+    x = d1p;
+    y = 3. * d1m;
+    double qMP = Si + fmaxd(0., fmind(x, y)) + fmind(0., fmaxd(x, y));
+    double qUL = Si + y;
+    double qLC = (Si + 0.5 * d1m) + ppm_4_3 * dM4m;
+    double qMD = qAV - 0.5 * dM4p;
+    double qMin = fmaxd(fmin3(qMD, Si, Sip1), fmin3(Si, qUL, qLC));
+    double qMax = fmind(fmax3(qMD, Si, Sip1), fmax3(Si, qUL, qLC));
+    if ((*aR - Si) * (*aR - qMP) > 1.e-10) *aR = fmind(fmaxd(*aR, qMin), qMax);
+    qAV = 0.5 * (Si + Sim1);
+    x = -d1m;
+    y = -3. * d1p;
+    qMP = Si + fmaxd(0., fmind(x, y)) + fmind(0., fmaxd(x, y));
+    qUL = Si + y;
+    qLC = (Si - 0.5 * d1p) + ppm_4_3 * dM4p;
+    qMD = qAV - 0.5 * dM4m;
+    qMin = fmaxd(fmin3(qMD, Si, Sim1), fmin3(Si, qUL, qLC));
+    qMax = fmind(fmax3(qMD, Si, Sim1), fmax3(Si, qUL, qLC));
+    if ((*aL - Si) * (*aL - qMP) > 1.e-10) *aL = fmind(fmaxd(*aL, qMin), qMax);
+  }
+}
+
+/* edge values, limited, and the curvature of a line of cells; S and M are indexed by
+ * position p = 0..n-1 with a 4-cell margin at each end; results for p = 3..n-4 */
+static void ppm_line(int n, int lim, const double* S, const double* M, double* aL, double* aR, double* a6) {
+  double *da = calloc(n, sizeof(double)), *d1m = calloc(n, sizeof(double)), *d1p = calloc(n, sizeof(double));
+  double *d1mm = calloc(n, sizeof(double)), *d1pp = calloc(n, sizeof(double));
+  for (int q = 2; q < n - 2; ++q) ppm_slope(S + q - 2, M + q - 2, &da[q], &d1m[q], &d1p[q], &d1mm[q], &d1pp[q]);
+  for (int q = 3; q < n - 3; ++q) {
+    double Si = S[q], Sim1 = Si - d1m[q], Sip1 = Si + d1p[q];
+    aL[q] = 0.5 * (Sim1 + Si) + ppm_sixth * (da[q - 1] - da[q]);
+    aR[q] = 0.5 * (Si + Sip1) + ppm_sixth * (da[q] - da[q + 1]);
+    ppm_limit(lim, Si, da[q], d1m[q], d1p[q], d1mm[q], d1pp[q], &aL[q], &aR[q]);
+    a6[q] = 6. * Si - 3. * (aR[q] + aL[q]);
+  }
+  free(da);
+  free(d1m);
+  free(d1p);
+  free(d1mm);
+  free(d1pp);
+}
+
+void orc_advect_mdppm(const orc_dims* d, int lim, double dtime, const double* tmask, const double* dat,
+                      const double* datr, const double* dxte, const double* dyte, const double* dxtn,
+                      const double* dytn, const double* uhrho_et, const double* vhrho_nt, const double* wrho_bt,
+                      const double* rho_dzt, const double* T, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d), n3 = n2 * nk;
+  double* tm = (double*)malloc(sizeof(double) * n3); /* tracer_mdppm on the compute domain (+ halo by image) */
+  double* fz = (double*)calloc(n3, sizeof(double));
+  memset(wrk1, 0, sizeof(double) * n3);
+  memcpy(tm, T, sizeof(double) * n3);
+#define W(i, j, K) wrho_bt[I3(d, i, j, K)] /* Fortran face index K = 0..nk */
+#define MK(i, j, K) tmask[I3(d, i, j, (K) - 1)] /* Fortran level K = 1..nk */
+#define TV(i, j, K) T[I3(d, i, j, (K) - 1)]
+  int L = nk + 8;
+  double *S = calloc(L, sizeof(double)), *M = calloc(L, sizeof(double));
+  double *aL = calloc(L, sizeof(double)), *aR = calloc(L, sizeof(double)), *a6 = calloc(L, sizeof(double));
+  double* dak = calloc(L, sizeof(double));
+  /* ---- vertical ---- */
+  for (int j = 1; j <= nj; ++j)
+    for (int i = 1; i <= ni; ++i) {
+      /* slopes dak(k) for all k (:6064-6099); positions q = K + 3 */
+      for (int K = 1; K <= nk; ++K) {
+        int km2 = K - 2 > 1 ? K - 2 : 1, km1 = K - 1 > 1 ? K - 1 : 1, kp1 = K + 1 < nk ? K + 1 : nk,
+            kp2 = K + 2 < nk ? K + 2 : nk;
+        double Sv[5] = {TV(i, j, km2), TV(i, j, km1), TV(i, j, K), TV(i, j, kp1), TV(i, j, kp2)};
+        double Mv[5] = {MK(i, j, km2) * (double)(km1 - km2), MK(i, j, km1) * (double)(K - km1), MK(i, j, K),
+                        MK(i, j, kp1) * (double)(kp1 - K), MK(i, j, kp2) * (double)(kp2 - kp1)};
+        double t0, t1, t2, t3;
+        ppm_slope(Sv, Mv, &dak[K], &t0, &t1, &t2, &t3);
+      }
+      for (int K = 1; K <= nk; ++K) {
+        int km2 = K - 2 > 1 ? K - 2 : 1, km1 = K - 1 > 1 ? K - 1 : 1, kp1 = K + 1 < nk ? K + 1 : nk,
+            kp2 = K + 2 < nk ? K + 2 : nk;
+        double mskp2 = MK(i, j, kp2) * (double)(kp2 - kp1), mskp1 = MK(i, j, kp1) * (double)(kp1 - K);
+        double msk0 = MK(i, j, K), mskm1 = MK(i, j, km1) * (double)(K - km1);
+        double mskm2 = MK(i, j, km2) * (double)(km1 - km2);
+        double Sip2 = TV(i, j, kp2), Sip1 = TV(i, j, kp1), Si = TV(i, j, K), Sim1 = TV(i, j, km1),
+               Sim2 = TV(i, j, km2);
+        double d1m = (Si - Sim1) * mskm1, d1p = (Sip1 - Si) * mskp1;
+        double d1mm = (Sim1 - Sim2) * mskm1 * mskm2, d1pp = (Sip2 - Sip1) * mskp1 * mskp2;
+        Sim1 = Si - d1m;
+        Sip1 = Si + d1p;
+        double al = 0.5 * (Sim1 + Si) + ppm_sixth * (dak[km1] - dak[K]);
+        double ar = 0.5 * (Si + Sip1) + ppm_sixth * (dak[K] - dak[kp1]);
+        ppm_limit(lim, Si, dak[K], d1m, d1p, d1mm, d1pp, &al, &ar);
+        double c6 = 6. * Si - 3. * (ar + al);
+        double massflux = dat[I2(d, i, j)] * W(i, j, K) * msk0 * mskp1;
+        if (massflux <= 0.0) {
+          double cfl = fabs(W(i, j, K) * dtime / rho_dzt[I3(d, i, j, K - 1)]);
+          fz[I3(d, i, j, K - 1)] = massflux * (ar + 0.5 * cfl * ((al - ar) + (1. - ppm_2_3 * cfl) * c6));
+        }
+        massflux = dat[I2(d, i, j)] * W(i, j, km1) * msk0 * mskm1;
+        if (massflux > 0.0) {
+          double cfl = fabs(W(i, j, km1) * dtime / rho_dzt[I3(d, i, j, km1 - 1)]);
+          fz[I3(d, i, j, km1 - 1)] = massflux * (al + 0.5 * cfl * ((ar - al) + (1. - ppm_2_3 * cfl) * c6));
+        }
+      }
+      for (int K = 1; K <= nk; ++K) {
+        int km1 = K - 1 > 1 ? K - 1 : 1;
+        double mskm1 = (double)(K - km1);
+        size_t p = I3(d, i, j, K - 1);
+        tm[p] = tm[p] + dtime / rho_dzt[p] *
+                            (datr[I2(d, i, j)] * (fz[p] - mskm1 * fz[I3(d, i, j, km1 - 1)]) +
+                             T[p] * (mskm1 * W(i, j, km1) - W(i, j, K)));
+      }
+    }
+  /* ---- x: lines along i of compute rows, halo of 4 by image (XUPDATE) ---- */
+  int Lx = ni + 8;
+  double *Sx = calloc(Lx, sizeof(double)), *Mx = calloc(Lx, sizeof(double)), *fx = calloc(Lx, sizeof(double));
+  double *aLx = calloc(Lx, sizeof(double)), *aRx = calloc(Lx, sizeof(double)), *a6x = calloc(Lx, sizeof(double));
+  double* tx = (double*)malloc(sizeof(double) * n3);
+  memcpy(tx, tm, sizeof(double) * n3);
+  for (int k = 0; k < nk; ++k)
+    for (int j = 1; j <= nj; ++j) {
+      for (int q = 0; q < Lx; ++q) { /* position q <-> i = q - 3 */
+        Sx[q] = halo_value(d, tm, q - 3, j, k);
+        Mx[q] = halo_value(d, tmask, q - 3, j, k);
+      }
+      ppm_line(Lx, lim, Sx, Mx, aLx, aRx, a6x);
+      for (int i = 0; i <= ni; ++i) { /* face i+1/2, q = i + 3 */
+        int q = i + 3;
+        double u = uhrho_et[I3(d, i, j, k)];
+        double massflux = dyte[I2(d, i, j)] * u;
+        double cfl = u * dtime * 2.0 / ((rho_dzt[I3(d, i, j, k)] + rho_dzt[I3(d, i + 1, j, k)]) * dxte[I2(d, i, j)]);
+        if (massflux >= 0.0)
+          fx[q] = massflux * Mx[q] * Mx[q + 1] *
+                  (aRx[q] + 0.5 * cfl * ((aLx[q] - aRx[q]) + (1. - ppm_2_3 * cfl) * a6x[q]));
+        else
+          fx[q] = massflux * Mx[q] * Mx[q + 1] *
+                  (aLx[q + 1] - 0.5 * cfl * ((aRx[q + 1] - aLx[q + 1]) + (1. + ppm_2_3 * cfl) * a6x[q + 1]));
+      }
+      for (int i = 1; i <= ni; ++i) {
+        size_t p = I3(d, i, j, k);
+        int q = i + 3;
+        tx[p] = tm[p] + dtime * Mx[q] * datr[I2(d, i, j)] / rho_dzt[p] *
+                            (fx[q - 1] - fx[q] +
+                             T[p] * (dyte[I2(d, i, j)] * uhrho_et[p] - dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)]));
+      }
+    }
+  /* ---- y: lines along j of compute columns, halo of 4 by image (YUPDATE) ---- */
+  int Ly = nj + 8;
+  double *Sy = calloc(Ly, sizeof(double)), *My = calloc(Ly, sizeof(double)), *fy = calloc(Ly, sizeof(double));
+  double *aLy = calloc(Ly, sizeof(double)), *aRy = calloc(Ly, sizeof(double)), *a6y = calloc(Ly, sizeof(double));
+  for (int k = 0; k < nk; ++k)
+    for (int i = 1; i <= ni; ++i) {
+      for (int q = 0; q < Ly; ++q) {
+        Sy[q] = halo_value(d, tx, i, q - 3, k);
+        My[q] = halo_value(d, tmask, i, q - 3, k);
+      }
+      ppm_line(Ly, lim, Sy, My, aLy, aRy, a6y);
+      for (int j = 0; j <= nj; ++j) {
+        int q = j + 3;
+        double v = vhrho_nt[I3(d, i, j, k)];
+        double massflux = dxtn[I2(d, i, j)] * v;
+        double cfl = v * dtime * 2.0 / ((rho_dzt[I3(d, i, j, k)] + rho_dzt[I3(d, i, j + 1, k)]) * dytn[I2(d, i, j)]);
+        if (massflux >= 0.0)
+          fy[q] = massflux * My[q] * My[q + 1] *
+                  (aRy[q] + 0.5 * cfl * ((aLy[q] - aRy[q]) + (1. - 2. / 3. * cfl) * a6y[q]));
+        else
+          fy[q] = massflux * My[q] * My[q + 1] *
+                  (aLy[q + 1] - 0.5 * cfl * ((aRy[q + 1] - aLy[q + 1]) + (1. + 2. / 3. * cfl) * a6y[q + 1]));
+      }
+      for (int j = 1; j <= nj; ++j) {
+        size_t p = I3(d, i, j, k);
+        int q = j + 3;
+        double t = tx[p] + dtime * tmask[p] * datr[I2(d, i, j)] / rho_dzt[p] * (fy[q - 1] - fy[q]);
+        double wkm1 = k > 0 ? wrho_bt[I3(d, i, j, k)] : 0.0;
+        t = t + dtime * T[p] / rho_dzt[p] *
+                    (wrho_bt[I3(d, i, j, k + 1)] - wkm1 +
+                     datr[I2(d, i, j)] * ((dyte[I2(d, i - 1, j)] * uhrho_et[I3(d, i - 1, j, k)] -
+                                           dyte[I2(d, i, j)] * uhrho_et[p])));
+        double advect = -rho_dzt[p] * (t - T[p]) / dtime * My[q];
+        wrk1[p] = -advect;
+      }
+    }
+#undef W
+#undef MK
+#undef TV
+  free(tm);
+  free(tx);
+  free(fz);
+  free(S);
+  free(M);
+  free(aL);
+  free(aR);
+  free(a6);
+  free(dak);
+  free(Sx);
+  free(Mx);
+  free(fx);
+  free(aLx);
+  free(aRx);
+  free(a6x);
+  free(Sy);
+  free(My);
+  free(fy);
+  free(aLy);
+  free(aRy);
+  free(a6y);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -111,6 +111,24 @@ def vert_advect_centred(d: Dims, g, T, order, kmt):
     return out
 
 
+def advect_mdfl_sup_b(d: Dims, g, T, dtime):
+    """wrk1 = -advect_tracer_mdfl_sup_b(...)."""
+    out = np.zeros_like(T)
+    lib().orc_advect_mdfl_sup_b(C.byref(d), C.c_double(dtime), p(g["tmask"]), p(g["dat"]), p(g["datr"]),
+                                p(g["dxte"]), p(g["dyte"]), p(g["dxtn"]), p(g["dytn"]), p(g["uhrho_et"]),
+                                p(g["vhrho_nt"]), p(g["wrho_bt"]), p(g["rho_dzt"]), p(np.ascontiguousarray(T)), p(out))
+    return out
+
+
+def advect_mdppm(d: Dims, g, T, dtime, limiter=2):
+    """wrk1 = -advect_tracer_mdppm(...) for ppm_hlimiter = limiter (1 cw84, 2 ifc, 3 sh)."""
+    out = np.zeros_like(T)
+    lib().orc_advect_mdppm(C.byref(d), int(limiter), C.c_double(dtime), p(g["tmask"]), p(g["dat"]), p(g["datr"]),
+                           p(g["dxte"]), p(g["dyte"]), p(g["dxtn"]), p(g["dytn"]), p(g["uhrho_et"]),
+                           p(g["vhrho_nt"]), p(g["wrho_bt"]), p(g["rho_dzt"]), p(np.ascontiguousarray(T)), p(out))
+    return out
+
+
 def quicker_init(d: Dims, g, dzt: np.ndarray):
     nxd, nyd, nk = d.ni + 2, d.nj + 2, d.nk
     q = {"quick_x": np.zeros((2, nyd, nxd)), "quick_y": np.zeros((2, nyd, nxd)),

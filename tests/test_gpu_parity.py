@@ -132,6 +132,64 @@ def test_centred_schemes_match(env, order, cyclic_x, cyclic_y):
         assert equal(got, ref), f"vert tracer {n}: {diff_report(got, ref)}"
 
 
+@pytest.mark.parametrize("cyclic_x,cyclic_y", [(False, False), (True, False), (True, True)])
+def test_mdfl_sup_b_matches(env, cyclic_x, cyclic_y):
+    """ADVECT_MDFL_SUP_B (advect_tracer_mdfl_sup_b, ocean_tracer_advect.F90:3189-3466):
+    the tendency of two tracers, then three whole steps, every value equal."""
+    capi, O = env
+    sp = spec(cyclic_x=cyclic_x, cyclic_y=cyclic_y, ntr=2, seed=44)
+    dom, d, g, dims = setup(env, sp, scheme=capi.ADVECT_MDFL_SUP_B)
+    dt = 6 * 3600.0
+    for n in (1, 2):
+        d.zero_th_tendency(n)
+        d.horz_advect_tracer(n, 1, 1, dt)
+        d.vert_advect_tracer(n, 1, 1, dt)
+        got = d.get(capi.F.TH_TENDENCY, n=n)
+        ref = O.advect_mdfl_sup_b(dims, g, g["T"][n - 1].copy(), dt)
+        assert equal(got, ref), f"tracer {n}: {diff_report(got, ref)}"
+    tau = 1
+    T = [g["T"][n].copy() for n in range(2)]
+    for s in range(3):
+        d.tracer_advection_step(tau, tau, 3 - tau, dt)
+        tau = 3 - tau
+        for n in range(2):
+            T[n] = O.update_tracer(dims, g, T[n], O.advect_mdfl_sup_b(dims, g, T[n], dt), dt)
+    for n in (1, 2):
+        got = d.get(capi.F.TRACER, n=n, level=tau)
+        assert equal(got, T[n - 1]), f"step 3 tracer {n}: {diff_report(got, T[n - 1])}"
+
+
+@pytest.mark.parametrize("limiter", [1, 2, 3])
+@pytest.mark.parametrize("cyclic_x,cyclic_y", [(False, False), (True, False), (True, True)])
+def test_mdppm_matches(env, limiter, cyclic_x, cyclic_y):
+    """ADVECT_MDPPM (advect_tracer_mdppm, ocean_tracer_advect.F90:5990-6507) with
+    each edge limiter (ppm_hlimiter 1, 2, 3: :6510-6660): the tendency of two
+    tracers, then three whole steps, every value equal."""
+    capi, O = env
+    sp = spec(cyclic_x=cyclic_x, cyclic_y=cyclic_y, ntr=2, seed=30 + limiter)
+    dom, d, g, dims = setup(env, sp, scheme=capi.ADVECT_MDPPM)
+    dt = 6 * 3600.0
+    for n in (1, 2):
+        d.set_ppm_limiter(n, limiter)
+        d.zero_th_tendency(n)
+        d.horz_advect_tracer(n, 1, 1, dt)
+        d.vert_advect_tracer(n, 1, 1, dt)
+        got = d.get(capi.F.TH_TENDENCY, n=n)
+        ref = O.advect_mdppm(dims, g, g["T"][n - 1].copy(), dt, limiter)
+        assert equal(got, ref), f"tracer {n}: {diff_report(got, ref)}"
+    tau = 1
+    T = [g["T"][n].copy() for n in range(2)]
+    for s in range(3):
+        d.tracer_advection_step(tau, tau, 3 - tau, dt)
+        tau = 3 - tau
+        for n in range(2):
+            th = O.advect_mdppm(dims, g, T[n], dt, limiter)
+            T[n] = O.update_tracer(dims, g, T[n], th, dt)
+    for n in (1, 2):
+        got = d.get(capi.F.TRACER, n=n, level=tau)
+        assert equal(got, T[n - 1]), f"step 3 tracer {n}: {diff_report(got, T[n - 1])}"
+
+
 @pytest.mark.parametrize("limit_with_upwind", [0, 1])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_quicker_matches(env, cyclic_x, limit_with_upwind):

@@ -91,7 +91,8 @@ def test_step_terms_restatements(O):
     assert np.all(f.view(np.uint64) == 0)
 
 
-@pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker", "c2", "c4", "c6"])
+@pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker", "c2", "c4", "c6", "ppm1", "ppm2", "ppm3",
+                                    "supb"])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
     """A uniform tracer in a non-divergent flow has zero advective tendency
@@ -106,6 +107,10 @@ def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
         th = O.advect_sweby_all(d, g, np.ascontiguousarray(U[None]), 3600.0)[0]
     elif scheme == "upwind":
         th = O.horz_advect_upwind(d, g, U) + O.vert_advect_upwind(d, g, U)
+    elif scheme.startswith("ppm"):
+        th = O.advect_mdppm(d, g, U, 3600.0, int(scheme[3]))
+    elif scheme == "supb":
+        th = O.advect_mdfl_sup_b(d, g, U, 3600.0)
     elif scheme.startswith("c"):
         order = int(scheme[1])
         th = O.horz_advect_centred(d, g, U, order) + O.vert_advect_centred(d, g, U, order, dom["kmt"].numpy())
@@ -116,7 +121,7 @@ def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
     assert np.abs(th).max() <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("scheme", ["mdfl", "upwind", "quicker"])
+@pytest.mark.parametrize("scheme", ["mdfl", "upwind", "quicker", "c4", "ppm1", "ppm2", "ppm3", "supb"])
 def test_global_content_conserved(O, scheme):
     """sum(dat*rho_dzt*T*tmask) (ocean_tracer_diag.F90:2395-2412) is unchanged by
     advection plus the explicit update, to FP64 roundoff."""
@@ -129,6 +134,12 @@ def test_global_content_conserved(O, scheme):
             th = O.advect_mdfl_sweby(d, g, T, 3600.0 * 6)
         elif scheme == "upwind":
             th = O.horz_advect_upwind(d, g, T) + O.vert_advect_upwind(d, g, T)
+        elif scheme.startswith("ppm"):
+            th = O.advect_mdppm(d, g, T, 3600.0 * 6, int(scheme[3]))
+        elif scheme == "supb":
+            th = O.advect_mdfl_sup_b(d, g, T, 3600.0 * 6)
+        elif scheme == "c4":
+            th = O.horz_advect_centred(d, g, T, 4) + O.vert_advect_centred(d, g, T, 4, dom["kmt"].numpy())
         else:
             th = O.horz_advect_quicker(d, g, q, T, T) + O.vert_advect_quicker(d, g, q, T, T)
         T = O.update_tracer(d, g, T, th, 3600.0 * 6)
