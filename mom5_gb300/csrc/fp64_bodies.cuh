@@ -142,22 +142,34 @@ constexpr int kMdflThreads = 128;
 // z pass: one thread per column, march down k.
 template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
-  __shared__ double ftp[MAXN][kMdflThreads];
+  // ftp: flux through the top face; Rp, Rc: the masked differences R(k-1), R(k),
+  // R(k) = (m(k) && m(k1)) ? T(k) - T(k1) : 0 with k1 = min(k+1, nk-1).  The
+  // reference's Rjp at level k is R(k-1) (+0 at k = 0) and its Rjm is R(k+1), so
+  // each difference is formed once and carried down the column.
+  __shared__ double ftp[MAXN][kMdflThreads], Rp[MAXN][kMdflThreads], Rc[MAXN][kMdflThreads];
   const Geo& g = a.g;
   const int t = threadIdx.x;
   int i = bx * blockDim.x + t + 1;
   int j = by + 1;
   if (i > g.ni) return;
+  {
+    const int k1 = g.nk > 1 ? 1 : 0;
+    const bool m0 = a.mask2[IM(g, i, j, 0)], m1 = a.mask2[IM(g, i, j, k1)];
 #pragma unroll 1
-  for (int n = 0; n < a.ntr; ++n) ftp[n][t] = 0.0;
+    for (int n = 0; n < a.ntr; ++n) {
+      const double* T = a.T + n * a.tstride;
+      ftp[n][t] = 0.0;
+      Rp[n][t] = 0.0;
+      Rc[n][t] = (m0 && m1) ? Ar::sub(T[I3(g, i, j, 0)], T[I3(g, i, j, k1)]) : 0.0;
+    }
+  }
   double wkm1 = 0.0;
   const double dat = a.dat[I2(g, i, j)];
   const double datr = a.datr[I2(g, i, j)];
   for (int k = 0; k < g.nk; ++k) {
     int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
     int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
-    int km1 = k > 0 ? k - 1 : 0;
-    bool mkm1 = a.mask2[IM(g, i, j, km1)], mk = a.mask2[IM(g, i, j, k)];
+    bool mk = a.mask2[IM(g, i, j, k)];
     bool mkp1 = a.mask2[IM(g, i, j, kp1)], mkp2 = a.mask2[IM(g, i, j, kp2)];
     double wk = a.w[I3(g, i, j, k + 1)];
     double rdz = a.rdz[I3(g, i, j, k)];
@@ -174,10 +186,12 @@ DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
     for (int n = 0; n < a.ntr; ++n) {
       const double* T = a.T + n * a.tstride;
       double Tk = T[p];
-      double Tkm1 = T[I3(g, i, j, km1)], Tkp1 = T[I3(g, i, j, kp1)], Tkp2 = T[I3(g, i, j, kp2)];
-      double Rjp = (mkm1 && mk) ? Ar::sub(Tkm1, Tk) : 0.0;
-      double Rj = (mk && mkp1) ? Ar::sub(Tk, Tkp1) : 0.0;
+      double Tkp1 = T[I3(g, i, j, kp1)], Tkp2 = T[I3(g, i, j, kp2)];
+      double Rjp = Rp[n][t];
+      double Rj = Rc[n][t];
       double Rjm = (mkp1 && mkp2) ? Ar::sub(Tkp1, Tkp2) : 0.0;
+      Rp[n][t] = Rj;
+      Rc[n][t] = Rjm;
       double fbt = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, Tkp1, Tk, d0, d1, c) : 0.0;
       double div = Au::add(Au::mul(datr, Au::sub(fbt, ftp[n][t])), Au::mul(Tk, wdiff));
       double tm;
@@ -217,12 +231,14 @@ DEVI double tm_yhalo(const Geo& g, const double* a, int i, int j, int k) {
 
 constexpr int kTX = 128;
 
-// x-face i of row (j,k): fluxes of every tracer into sm[n][slot].
+// x-face i of row (j,k): fluxes of every tracer into sm[n][slot].  Rs[n][r-1..r+1]
+// hold the masked differences R of faces i-1, i, i+1 (the reference's Rjm, Rj,
+// Rjp), each formed once per block.
 template <bool SWEBY, int MAXN, class Ar>
-DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], int slot) {
+DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], int slot,
+                 const double (*Rs)[kTX + 3], int r) {
   const Geo& g = a.g;
-  bool m0 = a.mask2[IM(g, i - 1, j, k)], m1 = a.mask2[IM(g, i, j, k)];
-  bool m2 = a.mask2[IM(g, i + 1, j, k)], m3 = a.mask2[IM(g, i + 2, j, k)];
+  bool m1 = a.mask2[IM(g, i, j, k)], m2 = a.mask2[IM(g, i + 1, j, k)];
   double u = a.uh[I3(g, i, j, k)];
   double massflux = a.dyte[I2(g, i, j)] * u;
   double cfl = fabs(u * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
@@ -233,26 +249,34 @@ DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], 
 #pragma unroll 1
   for (int n = 0; n < a.ntr; ++n) {
     const double* tz = a.tz + n * g.n3;
-    double tA = tm_xhalo(g, tz, i - 1, j, k), tB = tm_xhalo(g, tz, i, j, k);
-    double tC = tm_xhalo(g, tz, i + 1, j, k), tD = tm_xhalo(g, tz, i + 2, j, k);
-    double Rjp = (m3 && m2) ? Ar::sub(tD, tC) : 0.0;
-    double Rj = (m2 && m1) ? Ar::sub(tC, tB) : 0.0;
-    double Rjm = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
-    sm[n][slot] = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
+    double tB = tm_xhalo(g, tz, i, j, k), tC = tm_xhalo(g, tz, i + 1, j, k);
+    sm[n][slot] = fm ? face_flux<SWEBY, Ar>(massflux, Rs[n][r - 1], Rs[n][r], Rs[n][r + 1], tB, tC, d0, d1, c) : 0.0;
   }
 }
 
 template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
-  __shared__ double sm[MAXN][kTX + 1];
+  __shared__ double sm[MAXN][kTX + 1], Rs[MAXN][kTX + 3];
   const Geo& g = a.g;
   int i0 = bx * kTX + 1;
   int j = by + 1;
   int k = bz;
   int t = threadIdx.x;
   int i = i0 + t;
-  if (i <= g.ni) x_face<SWEBY, MAXN, Ar>(a, i, j, k, sm, t + 1);
-  if (t == 0) x_face<SWEBY, MAXN, Ar>(a, i0 - 1, j, k, sm, 0);
+  // R(f) = (m(f) && m(f+1)) ? tz(f+1) - tz(f) : 0 for faces f = i0-2 .. i0+128 (slot f-i0+2)
+  for (int sl = t; sl < kTX + 3; sl += kTX) {
+    int f = i0 - 2 + sl;
+    if (f > g.ni + 1) continue;
+    bool ma = a.mask2[IM(g, f, j, k)], mb = a.mask2[IM(g, f + 1, j, k)];
+#pragma unroll 1
+    for (int n = 0; n < a.ntr; ++n) {
+      const double* tz = a.tz + n * g.n3;
+      Rs[n][sl] = (mb && ma) ? Ar::sub(tm_xhalo(g, tz, f + 1, j, k), tm_xhalo(g, tz, f, j, k)) : 0.0;
+    }
+  }
+  __syncthreads();
+  if (i <= g.ni) x_face<SWEBY, MAXN, Ar>(a, i, j, k, sm, t + 1, Rs, t + 2);
+  if (t == 0) x_face<SWEBY, MAXN, Ar>(a, i0 - 1, j, k, sm, 0, Rs, 1);
   __syncthreads();
   if (i > g.ni) return;
   bool mk = a.mask2[IM(g, i, j, k)];
@@ -278,9 +302,13 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
 }
 
 // y pass + closing divergence correction + tendency: one thread per (i,k) and a
-// strip of TJ rows, marching north; th_tendency += result.
+// strip of TJ rows, marching north; th_tendency += result.  Ra, Rb carry the
+// masked differences R of faces j-1 and j (R(f) = (m(f) && m(f+1)) ?
+// tx(f+1) - tx(f) : 0, the reference's Rjm and Rj of face j); face j forms only
+// R(j+1), its Rjp.  With `first` the two carried values are formed as well.
 template <bool SWEBY, int MAXN, class Ar>
-DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThreads], int t) {
+DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThreads], int t, double (*Ra)[kMdflThreads],
+                 double (*Rb)[kMdflThreads], bool first) {
   const Geo& g = a.g;
   bool m0 = a.mask2[IM(g, i, j - 1, k)], m1 = a.mask2[IM(g, i, j, k)];
   bool m2 = a.mask2[IM(g, i, j + 1, k)], m3 = a.mask2[IM(g, i, j + 2, k)];
@@ -294,11 +322,17 @@ DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThread
 #pragma unroll 1
   for (int n = 0; n < a.ntr; ++n) {
     const double* tx = a.tx + n * g.n3;
-    double tA = tm_yhalo(g, tx, i, j - 1, k), tB = tm_yhalo(g, tx, i, j, k);
-    double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
+    double tB = tm_yhalo(g, tx, i, j, k), tC = tm_yhalo(g, tx, i, j + 1, k);
+    if (first) {
+      double tA = tm_yhalo(g, tx, i, j - 1, k);
+      Ra[n][t] = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
+      Rb[n][t] = (m2 && m1) ? Ar::sub(tC, tB) : 0.0;
+    }
+    double tD = tm_yhalo(g, tx, i, j + 2, k);
+    double Rjm = Ra[n][t], Rj = Rb[n][t];
     double Rjp = (m3 && m2) ? Ar::sub(tD, tC) : 0.0;
-    double Rj = (m2 && m1) ? Ar::sub(tC, tB) : 0.0;
-    double Rjm = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
+    Ra[n][t] = Rj;
+    Rb[n][t] = Rjp;
     f[n][t] = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
   }
 }
@@ -306,6 +340,7 @@ DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThread
 template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
   __shared__ double fprev[MAXN][kMdflThreads], fcur[MAXN][kMdflThreads];
+  __shared__ double Ra[MAXN][kMdflThreads], Rb[MAXN][kMdflThreads];
   const Geo& g = a.g;
   const int t = threadIdx.x;
   int i = bx * blockDim.x + t + 1;
@@ -315,9 +350,9 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
   int j1 = j0 + TJ - 1;
   if (j1 > g.nj) j1 = g.nj;
   const double rdtime = 1.0 / a.dtime;
-  y_face<SWEBY, MAXN, Ar>(a, i, j0 - 1, k, fprev, t);
+  y_face<SWEBY, MAXN, Ar>(a, i, j0 - 1, k, fprev, t, Ra, Rb, true);
   for (int j = j0; j <= j1; ++j) {
-    y_face<SWEBY, MAXN, Ar>(a, i, j, k, fcur, t);
+    y_face<SWEBY, MAXN, Ar>(a, i, j, k, fcur, t, Ra, Rb, false);
     long p = I3(g, i, j, k);
     bool mk = a.mask2[IM(g, i, j, k)];
     double datr = a.datr[I2(g, i, j)];

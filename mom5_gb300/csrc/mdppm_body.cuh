@@ -91,9 +91,9 @@ DEVI void limit(int lim, double Si, double da, double d1m, double d1p, double d1
   }
 }
 
-// flux through the face between cells with edge data (aL0, aR0, a60) and (aL1, aR1, a61)
-// for horizontal passes (:6293-6305, :6470-6482); `mm` = mask(left)*mask(right) applied
-// in the reference's order
+// flux through the face between a cell with edge data (aL0, aR0, a60) and mask m0 and
+// its neighbour (aL1, aR1, a61), mask m1, in the horizontal passes (:6293-6305,
+// :6470-6482); the masks multiply in the reference's order
 DEVI double hflux(double massflux, double m0, double m1, double cfl, double aL0, double aR0, double a60, double aL1,
                   double aR1, double a61) {
   if (massflux >= 0.0)
