@@ -56,6 +56,7 @@ extern "C" {
 #define MOM5GPU_ADVECT_MDPPM 8
 #define MOM5GPU_ADVECT_MDFL_SWEBY 9
 #define MOM5GPU_ADVECT_DST_LINEAR 10
+#define MOM5GPU_ADVECT_PSOM 11
 
 /* arithmetic of the advection kernels */
 #define MOM5GPU_PRECISION_FP64 0  /* drop-in: IEEE FP64 in the reference's operation order */
@@ -131,6 +132,12 @@ enum mom5gpu_field {
   MOM5GPU_SMF_V,
   MOM5GPU_BMF_U,         /* 2D, Velocity%bmf(:,:,1) */
   MOM5GPU_BMF_V,
+  /* second-order moments of the PSOM scheme (ocean_types.F90 T_prog(n)%s0..syz,
+   * allocated by psom_init, ocean_tracer_advect.F90:1798-1819); per tracer, 3D,
+   * compute domain meaningful (the halo is not maintained) */
+  MOM5GPU_PSOM_S0 = 120, /* 3D (n), mass-weighted tracer after the last sweep */
+  MOM5GPU_PSOM_SX, MOM5GPU_PSOM_SXX, MOM5GPU_PSOM_SY, MOM5GPU_PSOM_SYY, MOM5GPU_PSOM_SZ, MOM5GPU_PSOM_SZZ,
+  MOM5GPU_PSOM_SXY, MOM5GPU_PSOM_SXZ, MOM5GPU_PSOM_SYZ,
   MOM5GPU_FIELD_END
 };
 
@@ -161,6 +168,8 @@ typedef struct mom5gpu_options {
   /* ocean_barotropic_nml, ocean_barotropic.F90:528-529 */
   int zero_forcing_bt;            /* default 0 */
   int zero_nonlinear_forcing_bt;  /* default 0 */
+  /* ocean_tracer_advect_nml psom_limit_prather, ocean_tracer_advect.F90:489 */
+  int psom_limit_prather;         /* default 0: Merryfield-Holloway limiter */
 } mom5gpu_options;
 
 typedef struct mom5gpu_domain mom5gpu_domain;
@@ -202,6 +211,13 @@ int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz_scheme, int ver
  * default 2): 1 Colella-Woodward 1984, 2 improved full constraint (Lin 2004),
  * 3 Suresh-Huynh 1997. */
 int mom5gpu_set_ppm_limiter(mom5gpu_domain* d, int n, int ppm_hlimiter);
+/* Moment limiter of the PSOM scheme for tracer n (field_table psom_limit,
+ * ocean_tracer.F90:1013-1016; default 0, ocean_tpm_util.F90:86). */
+int mom5gpu_set_psom_limit(mom5gpu_domain* d, int n, int psom_limit);
+/* Time%itt0, the time-step counter whose value mod 6 orders the PSOM sweeps
+ * (ocean_tracer_advect.F90:4592-4621); >= 0, default 0.  The library does not
+ * advance it: the host sets it each step, as ocean_model does. */
+int mom5gpu_set_itt0(mom5gpu_domain* d, long itt0);
 
 /* ---- initialisation (after the grid fields are set) ---------------------- */
 /* ocean_tracer_advect_init's scheme set-up: quicker_init (:1442-1586) and

@@ -25,6 +25,7 @@ EINVAL, ENOMEM, ECUDA, ESTATE, ECFL, ENUMERIC, ETIMEDOUT, EUNSUPPORTED, EFULL = 
 BGRID, CGRID = 1, 2
 ADVECT_UPWIND, ADVECT_QUICKER, ADVECT_MDFL_SWEBY, ADVECT_DST_LINEAR = 1, 5, 9, 10
 ADVECT_2ND_ORDER, ADVECT_4TH_ORDER, ADVECT_6TH_ORDER, ADVECT_MDFL_SUP_B, ADVECT_MDPPM = 2, 3, 4, 7, 8
+ADVECT_PSOM = 11
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 
@@ -64,7 +65,7 @@ class Options(C.Structure):
                 ("barotropic_time_stepping_A", C.c_int), ("barotropic_time_stepping_B", C.c_int),
                 ("initsum_with_bar", C.c_int), ("pred_corr_gamma", C.c_double), ("rho0", C.c_double),
                 ("grav", C.c_double), ("precision", C.c_int), ("zero_forcing_bt", C.c_int),
-                ("zero_nonlinear_forcing_bt", C.c_int)]
+                ("zero_nonlinear_forcing_bt", C.c_int), ("psom_limit_prather", C.c_int)]
 
 
 class Mom5GpuError(RuntimeError):
@@ -113,6 +114,8 @@ def lib() -> C.CDLL:
             "mom5gpu_autotune": (C.c_int, [vp, C.c_double, C.c_char_p, C.c_size_t]),
             "mom5gpu_tracer_boundary_terms": (C.c_int, [vp, C.c_int]),
             "mom5gpu_set_ppm_limiter": (C.c_int, [vp, C.c_int, C.c_int]),
+            "mom5gpu_set_psom_limit": (C.c_int, [vp, C.c_int, C.c_int]),
+            "mom5gpu_set_itt0": (C.c_int, [vp, C.c_long]),
             "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
@@ -276,6 +279,12 @@ class Domain:
 
     def set_ppm_limiter(self, n, limiter):
         self.check(lib().mom5gpu_set_ppm_limiter(self.h, n, limiter))
+
+    def set_psom_limit(self, n, on):
+        self.check(lib().mom5gpu_set_psom_limit(self.h, n, int(bool(on))))
+
+    def set_itt0(self, itt0):
+        self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))
 
     def tracer_boundary_terms(self, n=0):
         self.check(lib().mom5gpu_tracer_boundary_terms(self.h, n))

@@ -57,6 +57,11 @@ const FieldInfo kFields[] = {
     {MOM5GPU_ACCEL_V, S3D, false, false},     {MOM5GPU_SMF_U, S2D, false, false},
     {MOM5GPU_SMF_V, S2D, false, false},       {MOM5GPU_BMF_U, S2D, false, false},
     {MOM5GPU_BMF_V, S2D, false, false},
+    {MOM5GPU_PSOM_S0, S3D, true, false},      {MOM5GPU_PSOM_SX, S3D, true, false},
+    {MOM5GPU_PSOM_SXX, S3D, true, false},     {MOM5GPU_PSOM_SY, S3D, true, false},
+    {MOM5GPU_PSOM_SYY, S3D, true, false},     {MOM5GPU_PSOM_SZ, S3D, true, false},
+    {MOM5GPU_PSOM_SZZ, S3D, true, false},     {MOM5GPU_PSOM_SXY, S3D, true, false},
+    {MOM5GPU_PSOM_SXZ, S3D, true, false},     {MOM5GPU_PSOM_SYZ, S3D, true, false},
 };
 
 // field storage: one block per (field, level) holding every tracer of that level
@@ -183,6 +188,7 @@ void mom5gpu_default_options(mom5gpu_options* o) {
   o->precision = MOM5GPU_PRECISION_FP64;
   o->zero_forcing_bt = 0;
   o->zero_nonlinear_forcing_bt = 0;
+  o->psom_limit_prather = 0;
 }
 
 const char* mom5gpu_strerror(int s) {
@@ -248,7 +254,7 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
   QuickerWeights& q = d->qw;
   for (double* p : {q.quick_x, q.quick_y, q.curv_xp, q.curv_xn, q.curv_yp, q.curv_yn, q.quick_z, q.curv_zp, q.curv_zn})
     if (p) cudaFree(p);
-  for (double* p : {d->cori1, d->cori2, d->mdfl_a, d->mdfl_b, d->bt, d->red, d->ppm_scr})
+  for (double* p : {d->cori1, d->cori2, d->mdfl_a, d->mdfl_b, d->bt, d->red, d->ppm_scr, d->psom_scr})
     if (p) cudaFree(p);
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
@@ -320,6 +326,21 @@ int mom5gpu_set_ppm_limiter(mom5gpu_domain* d, int n, int lim) {
   return MOM5GPU_OK;
 }
 
+int mom5gpu_set_psom_limit(mom5gpu_domain* d, int n, int on) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (n < 1 || n > d->dims.num_prog_tracers) return fail(d, MOM5GPU_EINVAL, "set_psom_limit: tracer %d", n);
+  d->scheme[n - 1].psom_limit = on ? 1 : 0;
+  return MOM5GPU_OK;
+}
+
+int mom5gpu_set_itt0(mom5gpu_domain* d, long itt0) {
+  if (!d) return MOM5GPU_EINVAL;
+  // mod(itt0, 6) of a negative counter matches none of the sweep orders
+  if (itt0 < 0) return fail(d, MOM5GPU_EINVAL, "set_itt0: the time-step counter must be >= 0 (got %ld)", itt0);
+  d->itt0 = itt0;
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_get_field(mom5gpu_domain* d, int field, int n, int level, double* dst, int on_device) {
   if (!d || !dst) return d ? fail(d, MOM5GPU_EINVAL, "get_field: null destination") : MOM5GPU_EINVAL;
   double* p;
@@ -352,11 +373,12 @@ int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz, int vert, doub
   auto ok = [](int s) {
     return s == MOM5GPU_ADVECT_UPWIND || s == MOM5GPU_ADVECT_2ND_ORDER || s == MOM5GPU_ADVECT_4TH_ORDER ||
            s == MOM5GPU_ADVECT_6TH_ORDER || s == MOM5GPU_ADVECT_QUICKER || s == MOM5GPU_ADVECT_MDPPM ||
-           s == MOM5GPU_ADVECT_MDFL_SUP_B || s == MOM5GPU_ADVECT_MDFL_SWEBY || s == MOM5GPU_ADVECT_DST_LINEAR;
+           s == MOM5GPU_ADVECT_MDFL_SUP_B || s == MOM5GPU_ADVECT_MDFL_SWEBY || s == MOM5GPU_ADVECT_DST_LINEAR ||
+           s == MOM5GPU_ADVECT_PSOM;
   };
   if (!ok(horz) || !ok(vert))
     return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: scheme %d/%d is outside upwind, 2nd/4th/6th order, "
-                                          "quicker, mdfl_sup_b, mdppm, mdfl_sweby, dst_linear", horz, vert);
+                                          "quicker, mdfl_sup_b, mdppm, mdfl_sweby, dst_linear, psom", horz, vert);
   // MDPPM reads a halo of 4: at least 4 compute points across a cyclic direction
   if (horz == MOM5GPU_ADVECT_MDPPM && ((d->geo.cx && d->geo.ni < 4) || (d->geo.cy && d->geo.nj < 4)))
     return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: mdppm needs ni, nj >= 4 across cyclic edges");
@@ -367,11 +389,11 @@ int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz, int vert, doub
   // ocean_tracer.F90:1076-1087: a 3-D scheme must be chosen for both directions
   auto three_d = [](int s) {
     return s == MOM5GPU_ADVECT_MDFL_SWEBY || s == MOM5GPU_ADVECT_DST_LINEAR || s == MOM5GPU_ADVECT_MDPPM ||
-           s == MOM5GPU_ADVECT_MDFL_SUP_B;
+           s == MOM5GPU_ADVECT_MDFL_SUP_B || s == MOM5GPU_ADVECT_PSOM;
   };
   bool h3 = three_d(horz), v3 = three_d(vert);
   if (h3 != v3 || (h3 && horz != vert))
-    return fail(d, MOM5GPU_EINVAL, "tracer %d: a 3-D scheme (MDFL, Super-B, DST, MDPPM) must be used for both horizontal and "
+    return fail(d, MOM5GPU_EINVAL, "tracer %d: a 3-D scheme (MDFL, Super-B, DST, MDPPM, PSOM) must be used for both horizontal and "
                                    "vertical advection", n);
   d->scheme[n - 1].horz = horz;
   d->scheme[n - 1].vert = vert;
@@ -677,6 +699,7 @@ int mom5gpu_horz_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
     case MOM5GPU_ADVECT_DST_LINEAR: return launch_mdfl(d, false, n, 1, taum1, tau, dtime, 0.0);
     case MOM5GPU_ADVECT_MDPPM: return launch_mdppm(d, n, taum1, tau, dtime);
     case MOM5GPU_ADVECT_MDFL_SUP_B: return launch_mdfl_sup_b(d, n, taum1, tau, dtime);
+    case MOM5GPU_ADVECT_PSOM: return launch_psom(d, n, taum1, dtime);
   }
   return fail(d, MOM5GPU_EINVAL, "horz_advect_tracer: invalid horz advection scheme");
 }
@@ -700,6 +723,7 @@ int mom5gpu_vert_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
     case MOM5GPU_ADVECT_MDFL_SWEBY:
     case MOM5GPU_ADVECT_DST_LINEAR:
     case MOM5GPU_ADVECT_MDFL_SUP_B:
+    case MOM5GPU_ADVECT_PSOM:
     case MOM5GPU_ADVECT_MDPPM: return MOM5GPU_OK;  // 3-D schemes: done in horz_advect_tracer
   }
   return fail(d, MOM5GPU_EINVAL, "vert_advect_tracer: invalid advection scheme");

@@ -38,6 +38,7 @@ struct TracerScheme {
   double min_limit = -1.0e10;
   double max_limit = 1.0e10;
   int ppm_limiter = 2;  // ppm_hlimiter (ocean_tpm_util.F90:87): 1 cw84, 2 ifc, 3 sh
+  int psom_limit = 0;   // psom_limit (ocean_tpm_util.F90:86)
 };
 
 // Quicker weights on the device (quicker_init, ocean_tracer_advect.F90:1442-1586).
@@ -87,6 +88,8 @@ struct mom5gpu_domain {
   double* bt = nullptr;        // barotropic scratch
   int* kmt_d = nullptr;        // device copy of kmt (uploaded on first use)
   double* ppm_scr = nullptr;   // MDPPM slope and vertical-flux scratch, 2 x n3
+  double* psom_scr = nullptr;  // PSOM mass and x/y/z face fluxes, 4 x n3
+  long itt0 = 0;               // Time%itt0 (orders the PSOM sweeps)
   double* red = nullptr;       // reduction scratch (device)
   double* red_h = nullptr;     // pinned host result
   int* flag = nullptr;         // device flag word
@@ -227,6 +230,7 @@ int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz);
 int ensure_kmt_device(mom5gpu_domain* d);
 int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
 int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
+int launch_psom(mom5gpu_domain* d, int n, int taum1, double dtime);
 int launch_tracer_boundary(mom5gpu_domain* d, int n);
 int launch_barotropic_forcing(mom5gpu_domain* d);
 int launch_advection_velocity(mom5gpu_domain* d, int tau);

@@ -41,7 +41,10 @@ module mom5gpu_c
        F_RHO_DZU = 65, F_RHO_DZTEN_E = 66, F_RHO_DZTEN_N = 67, F_RHO_DZT_TENDENCY = 68, &
        F_MASS_SOURCE = 69, F_U_VEL = 110, F_V_VEL = 111, F_TMASKEN_E = 41, F_TMASKEN_N = 42, &
        F_TPME = 73, F_TRACER_ETA_SMOOTH = 74, F_PBOT_SMOOTH = 75, F_ACCEL_U = 112, F_ACCEL_V = 113, &
-       F_SMF_U = 114, F_SMF_V = 115, F_BMF_U = 116, F_BMF_V = 117
+       F_SMF_U = 114, F_SMF_V = 115, F_BMF_U = 116, F_BMF_V = 117, &
+       F_PSOM_S0 = 120, F_PSOM_SX = 121, F_PSOM_SXX = 122, F_PSOM_SY = 123, F_PSOM_SYY = 124, &
+       F_PSOM_SZ = 125, F_PSOM_SZZ = 126, F_PSOM_SXY = 127, F_PSOM_SXZ = 128, F_PSOM_SYZ = 129
+  integer(c_int), parameter :: MOM5GPU_ADVECT_PSOM = 11
 
   type, bind(C) :: mom5gpu_dims
      integer(c_int) :: ni, nj, nk, cyclic_x, cyclic_y, num_prog_tracers, horz_grid
@@ -53,6 +56,7 @@ module mom5gpu_c
      real(c_double) :: pred_corr_gamma, rho0, grav
      integer(c_int) :: precision
      integer(c_int) :: zero_forcing_bt, zero_nonlinear_forcing_bt
+     integer(c_int) :: psom_limit_prather
   end type mom5gpu_options
 
   interface
@@ -100,6 +104,21 @@ module mom5gpu_c
        type(c_ptr), value :: dom
        integer(c_int), value :: n, horz, vert
        real(c_double), value :: tmin, tmax
+     end function
+     integer(c_int) function mom5gpu_set_ppm_limiter(dom, n, lim) bind(C, name="mom5gpu_set_ppm_limiter")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, lim
+     end function
+     integer(c_int) function mom5gpu_set_psom_limit(dom, n, on) bind(C, name="mom5gpu_set_psom_limit")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, on
+     end function
+     integer(c_int) function mom5gpu_set_itt0(dom, itt0) bind(C, name="mom5gpu_set_itt0")
+       import :: c_int, c_ptr, c_long
+       type(c_ptr), value :: dom
+       integer(c_long), value :: itt0
      end function
      integer(c_int) function mom5gpu_tracer_advect_init(dom) bind(C, name="mom5gpu_tracer_advect_init")
        import :: c_int, c_ptr

@@ -321,6 +321,316 @@ void orc_vert_advect_centred(const orc_dims* d, int order, const double* tmask, 
 }
 
 /* ------------------------------------------------------------------------- */
+/* PSOM: advect_tracer_psom (ocean_tracer_advect.F90:4549-4660) with psom_x  */
+/* (:4662-4917), psom_y (:4919-5174), psom_z (:5176-5420): Prather's second- */
+/* order moments, direction order by mod(itt0, 6), optional moment limiters. */
+/* The nine moments sx..syz are prognostic (in/out); s0 and the mass sm are  */
+/* formed from the tracer at lag = taum1.  Every array is data-domain sized. */
+/* Returns wrk1 = -advect.                                                    */
+/* ------------------------------------------------------------------------- */
+enum { P_SX, P_SXX, P_SY, P_SYY, P_SZ, P_SZZ, P_SXY, P_SXZ, P_SYZ, P_N };
+static const double psom_epsln = 1.0e-20; /* constants_mod epsln */
+
+typedef struct {
+  double *sm, *s0, *m[P_N];
+} psom_state;
+
+static void psom_full_update(const orc_dims* d, psom_state* st) {
+  orc_halo_update_3d(d, st->sm, d->nk, 3);
+  orc_halo_update_3d(d, st->s0, d->nk, 3);
+  for (int q = 0; q < P_N; ++q) orc_halo_update_3d(d, st->m[q], d->nk, 3);
+}
+
+/* limiter of the moments along one direction before transport (:4676-4748 and the
+ * y/z analogues); a = first moment along the direction, aa = second, c1, c2 = the
+ * two cross moments with it; nb selects the neighbours (1 x, 2 y, 3 z). */
+static void psom_limit(const orc_dims* d, int prather, int dir, const double* tmask, const double* field,
+                       psom_state* st, int a, int aa, int c1, int c2) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  double *A = st->m[a], *AA = st->m[aa], *C1 = st->m[c1], *C2 = st->m[c2];
+  if (prather) {
+    for (int k = 0; k < nk; ++k)
+      for (int j = 0; j <= nj + 1; ++j)
+        for (int i = 0; i <= ni + 1; ++i) {
+          size_t p = I3(d, i, j, k);
+          double slpmax = 0.0;
+          if (st->s0[p] > 0.0) slpmax = st->s0[p];
+          double s1max = 1.5 * slpmax;
+          double s1new = fmind(s1max, fmaxd(-s1max, A[p]));
+          double s2new = fmind(slpmax + slpmax - 0.3334 * fabs(s1new), fmaxd(fabs(s1new) - slpmax, AA[p]));
+          C1[p] = fmind(slpmax, fmaxd(-slpmax, C1[p]));
+          C2[p] = fmind(slpmax, fmaxd(-slpmax, C2[p]));
+          A[p] = s1new;
+          AA[p] = s2new;
+        }
+    return;
+  }
+  int i0 = dir == 1 ? 1 : 0, i1 = dir == 1 ? ni : ni + 1;
+  int j0 = dir == 2 ? 1 : 0, j1 = dir == 2 ? nj : nj + 1;
+  for (int k = 0; k < nk; ++k) {
+    int km1 = k - 1 > 0 ? k - 1 : 0, kp1 = k + 1 < nk ? k + 1 : nk - 1;
+    for (int j = j0; j <= j1; ++j)
+      for (int i = i0; i <= i1; ++i) {
+        size_t p = I3(d, i, j, k), pm, pp;
+        if (dir == 1) {
+          pm = I3(d, i - 1, j, k);
+          pp = I3(d, i + 1, j, k);
+        } else if (dir == 2) {
+          pm = I3(d, i, j - 1, k);
+          pp = I3(d, i, j + 1, k);
+        } else {
+          pm = I3(d, i, j, km1);
+          pp = I3(d, i, j, kp1);
+        }
+        double s0max1 = field[p] * tmask[p];
+        if (tmask[pm] > 0.) s0max1 = fmaxd(field[pm], s0max1);
+        if (tmask[pp] > 0.) s0max1 = fmaxd(field[pp], s0max1);
+        s0max1 = s0max1 * st->sm[p];
+        double slpmax = -st->s0[p] + s0max1;
+        double s1max = 1.5 * slpmax;
+        double s1new = fmind(s1max, fmaxd(-s1max, -A[p]));
+        double s2new = fmind(slpmax + slpmax - 0.3334 * fabs(s1new), fmaxd(fabs(s1new) - slpmax, -AA[p]));
+        C1[p] = -fmind(slpmax, fmaxd(-slpmax, -C1[p]));
+        C2[p] = -fmind(slpmax, fmaxd(-slpmax, -C2[p]));
+        A[p] = -s1new;
+        AA[p] = -s2new;
+        double s0min1 = field[p] * tmask[p];
+        if (tmask[pm] > 0.) s0min1 = fmind(field[pm], s0min1);
+        if (tmask[pp] > 0.) s0min1 = fmind(field[pp], s0min1);
+        s0min1 = s0min1 * st->sm[p];
+        slpmax = st->s0[p] - s0min1;
+        s1max = 1.5 * slpmax;
+        s1new = fmind(s1max, fmaxd(-s1max, A[p]));
+        s2new = fmind(slpmax + slpmax - 0.3334 * fabs(s1new), fmaxd(fabs(s1new) - slpmax, AA[p]));
+        C1[p] = fmind(slpmax, fmaxd(-slpmax, C1[p]));
+        C2[p] = fmind(slpmax, fmaxd(-slpmax, C2[p]));
+        A[p] = s1new;
+        AA[p] = s2new;
+      }
+  }
+  if (dir != 3) { /* Dom_flux full halo update of the four limited moments */
+    orc_halo_update_3d(d, A, nk, 3);
+    orc_halo_update_3d(d, AA, nk, 3);
+    orc_halo_update_3d(d, C1, nk, 3);
+    orc_halo_update_3d(d, C2, nk, 3);
+  }
+}
+
+/* One face of a transport sweep.  Along the direction: a, aa (first and second
+ * moment), cross moments c1 = (a x other1), c2 = (a x other2) with the other two
+ * first moments b1, b2 and their second moments bb1, bb2, and the cross moment
+ * between the two others bc.  fl[0..10] = f0, fa, faa, fb1, fb2, fc1, fc2, fbb1, fbb2, fbc, fm. */
+enum { F0, FA, FAA, FB1, FB2, FC1, FC2, FBB1, FBB2, FBC, FM, NF };
+
+static void psom_out(double velocity, double dv, double dtime, psom_state* st, size_t up, int sgn, const int* ix,
+                     double* fl) {
+  /* ix: indices of a, aa, b1, b2, c1, c2, bb1, bb2, bc in st->m */
+  double *sm = st->sm, *s0 = st->s0;
+  double *A = st->m[ix[0]], *AA = st->m[ix[1]], *B1 = st->m[ix[2]], *B2 = st->m[ix[3]];
+  double *C1 = st->m[ix[4]], *C2 = st->m[ix[5]], *BB1 = st->m[ix[6]], *BB2 = st->m[ix[7]], *BC = st->m[ix[8]];
+  fl[FM] = sgn > 0 ? velocity * dtime * dv : -velocity * dtime * dv;
+  double alf = fl[FM] / (sm[up] + psom_epsln), alfq = alf * alf, alf1 = 1.0 - alf, alf1q = alf1 * alf1;
+  if (sgn > 0) {
+    fl[F0] = alf * (s0[up] + alf1 * (A[up] + (alf1 - alf) * AA[up]));
+    fl[FA] = alfq * (A[up] + 3.0 * alf1 * AA[up]);
+    fl[FB1] = alf * (B1[up] + alf1 * C1[up]);
+    fl[FB2] = alf * (B2[up] + alf1 * C2[up]);
+  } else {
+    fl[F0] = alf * (s0[up] - alf1 * (A[up] - (alf1 - alf) * AA[up]));
+    fl[FA] = alfq * (A[up] - 3.0 * alf1 * AA[up]);
+    fl[FB1] = alf * (B1[up] - alf1 * C1[up]);
+    fl[FB2] = alf * (B2[up] - alf1 * C2[up]);
+  }
+  fl[FAA] = alf * alfq * AA[up];
+  fl[FC1] = alfq * C1[up];
+  fl[FC2] = alfq * C2[up];
+  fl[FBB1] = alf * BB1[up];
+  fl[FBB2] = alf * BB2[up];
+  fl[FBC] = alf * BC[up];
+  sm[up] = sm[up] - fl[FM];
+  s0[up] = s0[up] - fl[F0];
+  if (sgn > 0) A[up] = alf1q * (A[up] - 3.0 * alf * AA[up]);
+  else A[up] = alf1q * (A[up] + 3.0 * alf * AA[up]);
+  AA[up] = alf1 * alf1q * AA[up];
+  B1[up] = B1[up] - fl[FB1];
+  BB1[up] = BB1[up] - fl[FBB1];
+  B2[up] = B2[up] - fl[FB2];
+  BB2[up] = BB2[up] - fl[FBB2];
+  C1[up] = alf1q * C1[up];
+  C2[up] = alf1q * C2[up];
+  BC[up] = BC[up] - fl[FBC];
+}
+
+static void psom_in(psom_state* st, size_t dn, int sgn, const int* ix, const double* fl) {
+  double *sm = st->sm, *s0 = st->s0;
+  double *A = st->m[ix[0]], *AA = st->m[ix[1]], *B1 = st->m[ix[2]], *B2 = st->m[ix[3]];
+  double *C1 = st->m[ix[4]], *C2 = st->m[ix[5]], *BB1 = st->m[ix[6]], *BB2 = st->m[ix[7]], *BC = st->m[ix[8]];
+  sm[dn] = sm[dn] + fl[FM];
+  double alf = fl[FM] / (sm[dn] + psom_epsln), alf1 = 1.0 - alf;
+  if (sgn > 0) {
+    double temptm = alf * s0[dn] - alf1 * fl[F0];
+    s0[dn] = s0[dn] + fl[F0];
+    AA[dn] = alf * alf * fl[FAA] + alf1 * alf1 * AA[dn] + 5.0 * (alf * alf1 * (A[dn] - fl[FA]) - (alf1 - alf) * temptm);
+    A[dn] = alf * fl[FA] + alf1 * A[dn] + 3.0 * temptm;
+    C1[dn] = alf * fl[FC1] + alf1 * C1[dn] + 3.0 * (-alf1 * fl[FB1] + alf * B1[dn]);
+    C2[dn] = alf * fl[FC2] + alf1 * C2[dn] + 3.0 * (-alf1 * fl[FB2] + alf * B2[dn]);
+  } else {
+    double temptm = -alf * s0[dn] + alf1 * fl[F0];
+    s0[dn] = s0[dn] + fl[F0];
+    AA[dn] = alf * alf * fl[FAA] + alf1 * alf1 * AA[dn] + 5.0 * (alf * alf1 * (-A[dn] + fl[FA]) + (alf1 - alf) * temptm);
+    A[dn] = alf * fl[FA] + alf1 * A[dn] + 3.0 * temptm;
+    C1[dn] = alf * fl[FC1] + alf1 * C1[dn] + 3.0 * (alf1 * fl[FB1] - alf * B1[dn]);
+    C2[dn] = alf * fl[FC2] + alf1 * C2[dn] + 3.0 * (alf1 * fl[FB2] - alf * B2[dn]);
+  }
+  B1[dn] = B1[dn] + fl[FB1];
+  BB1[dn] = BB1[dn] + fl[FBB1];
+  B2[dn] = B2[dn] + fl[FB2];
+  BB2[dn] = BB2[dn] + fl[FBB2];
+  BC[dn] = BC[dn] + fl[FBC];
+}
+
+/* moment roles per direction: along (a, aa), other firsts (b1, b2), cross (c1 = a*b1,
+ * c2 = a*b2), other seconds (bb1, bb2), other cross (bc) */
+static const int psom_roles[3][9] = {
+    {P_SX, P_SXX, P_SY, P_SZ, P_SXY, P_SXZ, P_SYY, P_SZZ, P_SYZ}, /* psom_x */
+    {P_SY, P_SYY, P_SX, P_SZ, P_SXY, P_SYZ, P_SXX, P_SZZ, P_SXZ}, /* psom_y */
+    {P_SZ, P_SZZ, P_SX, P_SY, P_SXZ, P_SYZ, P_SXX, P_SYY, P_SXY}, /* psom_z */
+};
+
+/* Transport sweeps of one direction.  A face joins cell a (upstream when the
+ * velocity is >= 0) and cell b: x (i, i+1), y (j, j+1), z (k+1, k) with k the
+ * upper cell.  Outflow sweep over every face, halo update of the in-transit
+ * moments (XUPDATE without fm in x, YUPDATE with fm in y, none in z), inflow
+ * sweep in the same face order, full halo update. */
+static void psom_sweep(const orc_dims* d, int dir, double dtime, const double* tmask, const double* dat,
+                       const double* dxtn, const double* dyte, const double* uhrho_et, const double* vhrho_nt,
+                       const double* wrho_bt, psom_state* st, double* flux, double* fb) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n3 = (size_t)NXD(d) * NYD(d) * nk;
+  const int* ix = psom_roles[dir - 1];
+  double dtimer = 1.0 / dtime, fl[NF];
+  for (int pass = 0; pass < 2; ++pass) {
+    if (dir == 3) {
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i)
+          for (int kf = nk - 2; kf >= 0; --kf) {
+            size_t pa = I3(d, i, j, kf + 1), pb = I3(d, i, j, kf), pf = I3(d, i, j, kf);
+            double velocity = wrho_bt[I3(d, i, j, kf + 1)] * tmask[I3(d, i, j, kf + 1)];
+            if (pass == 0) {
+              if (velocity >= 0.0) {
+                psom_out(velocity, dat[I2(d, i, j)], dtime, st, pa, 1, ix, fl);
+                flux[pf] = fl[F0] * dtimer;
+              } else {
+                psom_out(velocity, dat[I2(d, i, j)], dtime, st, pb, -1, ix, fl);
+                flux[pf] = -fl[F0] * dtimer;
+              }
+              for (int q = 0; q < NF; ++q) fb[q * n3 + pf] = fl[q];
+            } else {
+              for (int q = 0; q < NF; ++q) fl[q] = fb[q * n3 + pf];
+              if (velocity >= 0.0) psom_in(st, pb, 1, ix, fl);
+              else psom_in(st, pa, -1, ix, fl);
+            }
+          }
+    } else {
+      int i0 = dir == 1 ? 0 : 1, j0 = dir == 2 ? 0 : 1;
+      for (int k = 0; k < nk; ++k)
+        for (int j = j0; j <= nj; ++j)
+          for (int i = i0; i <= ni; ++i) {
+            size_t pa = I3(d, i, j, k), pf = pa;
+            size_t pb = dir == 1 ? I3(d, i + 1, j, k) : I3(d, i, j + 1, k);
+            double velocity, dv;
+            if (dir == 1) {
+              velocity = uhrho_et[pa] * fmind(tmask[pa], tmask[pb]);
+              dv = dyte[I2(d, i, j)];
+            } else {
+              velocity = vhrho_nt[pa] * fmind(tmask[pa], tmask[pb]);
+              dv = dxtn[I2(d, i, j)];
+            }
+            if (pass == 0) {
+              if (velocity >= 0.0) {
+                psom_out(velocity, dv, dtime, st, pa, 1, ix, fl);
+                flux[pf] = fl[F0] * dtimer;
+              } else {
+                psom_out(velocity, dv, dtime, st, pb, -1, ix, fl);
+                flux[pf] = -fl[F0] * dtimer;
+              }
+              for (int q = 0; q < NF; ++q) fb[q * n3 + pf] = fl[q];
+            } else {
+              for (int q = 0; q < NF; ++q) fl[q] = fb[q * n3 + pf];
+              if (velocity >= 0.0) psom_in(st, pb, 1, ix, fl);
+              else psom_in(st, pa, -1, ix, fl);
+            }
+          }
+    }
+    if (pass == 0 && dir != 3) {
+      int fl_flag = dir == 1 ? 1 : 2;
+      for (int q = 0; q < NF; ++q)
+        if (q != FM || dir == 2) orc_halo_update_3d(d, fb + q * n3, nk, fl_flag);
+      orc_halo_update_3d(d, flux, nk, fl_flag);
+      orc_halo_update_3d(d, st->sm, nk, fl_flag);
+      orc_halo_update_3d(d, st->s0, nk, fl_flag);
+      for (int q = 0; q < P_N; ++q) orc_halo_update_3d(d, st->m[q], nk, fl_flag);
+    }
+  }
+  psom_full_update(d, st);
+}
+
+/* mom: the nine moments sx, sxx, sy, syy, sz, szz, sxy, sxz, syz (each data-domain
+ * sized, in/out); s0: out; rho_dzt and field at taum1. */
+void orc_advect_psom(const orc_dims* d, long itt0, int limit, int prather, double dtime, const double* tmask,
+                     const double* dat, const double* datr, const double* dxtn, const double* dyte,
+                     const double* uhrho_et, const double* vhrho_nt, const double* wrho_bt, const double* rho_dzt,
+                     const double* field, double* s0, double* mom, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d), n3 = n2 * nk;
+  psom_state st;
+  st.sm = (double*)calloc(n3, sizeof(double));
+  st.s0 = s0;
+  for (int q = 0; q < P_N; ++q) st.m[q] = mom + q * n3;
+  double* fx = (double*)calloc(n3, sizeof(double));
+  double* fy = (double*)calloc(n3, sizeof(double));
+  double* fz = (double*)calloc(n3, sizeof(double));
+  double* fb = (double*)calloc(NF * n3, sizeof(double));
+  for (int k = 0; k < nk; ++k)
+    for (int j = 0; j <= nj + 1; ++j)
+      for (int i = 0; i <= ni + 1; ++i) {
+        size_t p = I3(d, i, j, k);
+        st.sm[p] = rho_dzt[p] * dat[I2(d, i, j)];
+        s0[p] = field[p] * st.sm[p] * tmask[p];
+      }
+  static const int order[6][3] = {{1, 2, 3}, {3, 1, 2}, {2, 3, 1}, {1, 3, 2}, {2, 1, 3}, {3, 2, 1}};
+  const int* o = order[itt0 % 6];
+  for (int s = 0; s < 3; ++s) {
+    int dir = o[s];
+    if (limit) {
+      if (dir == 1) psom_limit(d, prather, 1, tmask, field, &st, P_SX, P_SXX, P_SXY, P_SXZ);
+      else if (dir == 2) psom_limit(d, prather, 2, tmask, field, &st, P_SY, P_SYY, P_SXY, P_SYZ);
+      else psom_limit(d, prather, 3, tmask, field, &st, P_SZ, P_SZZ, P_SXZ, P_SYZ);
+    }
+    double* flux = dir == 1 ? fx : dir == 2 ? fy : fz;
+    psom_sweep(d, dir, dtime, tmask, dat, dxtn, dyte, uhrho_et, vhrho_nt, wrho_bt, &st, flux, fb);
+  }
+  memset(wrk1, 0, sizeof(double) * n3);
+  for (int j = 1; j <= nj; ++j)
+    for (int i = 1; i <= ni; ++i) {
+      double ft1 = 0.0;
+      for (int k = 0; k < nk; ++k) {
+        size_t p = I3(d, i, j, k);
+        double fzk = k < nk - 1 ? fz[p] : 0.0; /* flux_z = 0 on entry; the bottom face is never written */
+        double advect = tmask[p] * (fx[p] - fx[I3(d, i - 1, j, k)] + fy[p] - fy[I3(d, i, j - 1, k)] + ft1 - fzk) *
+                        datr[I2(d, i, j)];
+        wrk1[p] = -advect;
+        ft1 = fzk;
+      }
+    }
+  free(st.sm);
+  free(fx);
+  free(fy);
+  free(fz);
+  free(fb);
+}
+
+/* ------------------------------------------------------------------------- */
 /* MDFL Super-B: advect_tracer_mdfl_sup_b (ocean_tracer_advect.F90:3189-3466),*/
 /* split level by level: z flux on the tracer, update, halo update of the    */
 /* level, x fluxes on the z-updated level, update, halo update, y fluxes,    */

@@ -129,6 +129,24 @@ def advect_mdppm(d: Dims, g, T, dtime, limiter=2):
     return out
 
 
+PSOM_MOMENTS = ("sx", "sxx", "sy", "syy", "sz", "szz", "sxy", "sxz", "syz")
+
+
+def advect_psom(d: Dims, g, T, dtime, moments, itt0=0, limit=True, prather=False, rho_dzt=None):
+    """wrk1 = -advect_tracer_psom(...) (T and rho_dzt at taum1).  ``moments`` is the
+    (9, nk, nj+2, ni+2) array of Tracer%sx..syz in PSOM_MOMENTS order, updated in
+    place; returns (wrk1, s0)."""
+    assert moments.dtype == np.float64 and moments.flags["C_CONTIGUOUS"] and moments.shape[0] == 9
+    out = np.zeros_like(T)
+    s0 = np.zeros_like(T)
+    rdz = g["rho_dzt"] if rho_dzt is None else np.ascontiguousarray(rho_dzt)
+    lib().orc_advect_psom(C.byref(d), C.c_long(int(itt0)), int(bool(limit)), int(bool(prather)), C.c_double(dtime),
+                          p(g["tmask"]), p(g["dat"]), p(g["datr"]), p(g["dxtn"]), p(g["dyte"]), p(g["uhrho_et"]),
+                          p(g["vhrho_nt"]), p(g["wrho_bt"]), p(rdz), p(np.ascontiguousarray(T)), p(s0),
+                          p(moments), p(out))
+    return out, s0
+
+
 def quicker_init(d: Dims, g, dzt: np.ndarray):
     nxd, nyd, nk = d.ni + 2, d.nj + 2, d.nk
     q = {"quick_x": np.zeros((2, nyd, nxd)), "quick_y": np.zeros((2, nyd, nxd)),

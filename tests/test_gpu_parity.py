@@ -190,6 +190,52 @@ def test_mdppm_matches(env, limiter, cyclic_x, cyclic_y):
         assert equal(got, T[n - 1]), f"step 3 tracer {n}: {diff_report(got, T[n - 1])}"
 
 
+@pytest.mark.parametrize("mode", ["merryfield_holloway", "prather", "unlimited"])
+@pytest.mark.parametrize("cyclic_x,cyclic_y", [(False, False), (True, False), (True, True)])
+def test_psom_matches(env, mode, cyclic_x, cyclic_y):
+    """ADVECT_PSOM (advect_tracer_psom, ocean_tracer_advect.F90:4549-4660; psom_x/y/z
+    :4662-5420) with the Merryfield-Holloway limiter, Prather's limiter
+    (psom_limit_prather) or none: the tendency of two tracers at itt0 = 0, then
+    six whole steps through every sweep order (mod(itt0, 6)), every tracer value
+    and every moment equal."""
+    capi, O = env
+    opts = capi.default_options(psom_limit_prather=int(mode == "prather"))
+    sp = spec(cyclic_x=cyclic_x, cyclic_y=cyclic_y, ntr=2, seed=50 + cyclic_x + 2 * cyclic_y)
+    dom, d, g, dims = setup(env, sp, scheme=capi.ADVECT_PSOM, options=opts)
+    limit, prather = mode != "unlimited", mode == "prather"
+    dt = 6 * 3600.0
+    mom = [np.zeros((9,) + g["T"][0].shape) for _ in range(2)]
+    for n in (1, 2):
+        d.set_psom_limit(n, limit)
+        d.zero_th_tendency(n)
+        d.horz_advect_tracer(n, 1, 1, dt)
+        d.vert_advect_tracer(n, 1, 1, dt)
+        got = d.get(capi.F.TH_TENDENCY, n=n)
+        ref, _ = O.advect_psom(dims, g, g["T"][n - 1].copy(), dt, mom[n - 1], itt0=0, limit=limit, prather=prather)
+        assert equal(got, ref), f"tracer {n}: {diff_report(got, ref)}"
+    tau = 1
+    T = [g["T"][n].copy() for n in range(2)]
+    s0 = [None, None]
+    for itt0 in range(1, 7):
+        d.set_itt0(itt0)
+        d.tracer_advection_step(tau, tau, 3 - tau, dt)
+        tau = 3 - tau
+        for n in range(2):
+            th, s0[n] = O.advect_psom(dims, g, T[n], dt, mom[n], itt0=itt0, limit=limit, prather=prather)
+            T[n] = O.update_tracer(dims, g, T[n], th, dt)
+    inner = (slice(None), slice(1, -1), slice(1, -1))
+    shp = g["T"][0].shape
+    for n in (1, 2):
+        got = d.get(capi.F.TRACER, n=n, level=tau)
+        assert equal(got, T[n - 1]), f"step 6 tracer {n}: {diff_report(got, T[n - 1])}"
+        got = d.get(capi.F.PSOM_S0, n=n).reshape(shp)[inner]
+        assert equal(got, s0[n - 1][inner]), f"s0 tracer {n}: {diff_report(got, s0[n - 1][inner])}"
+        for q, name in enumerate(O.PSOM_MOMENTS):
+            got = d.get(capi.F.PSOM_SX + q, n=n).reshape(shp)[inner]
+            ref = mom[n - 1][q][inner]
+            assert equal(got, ref), f"{name} tracer {n}: {diff_report(got, ref)}"
+
+
 @pytest.mark.parametrize("limit_with_upwind", [0, 1])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_quicker_matches(env, cyclic_x, limit_with_upwind):

@@ -92,7 +92,7 @@ def test_step_terms_restatements(O):
 
 
 @pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker", "c2", "c4", "c6", "ppm1", "ppm2", "ppm3",
-                                    "supb"])
+                                    "supb", "psom", "psom_prather", "psom_nolimit"])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
     """A uniform tracer in a non-divergent flow has zero advective tendency
@@ -111,6 +111,8 @@ def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
         th = O.advect_mdppm(d, g, U, 3600.0, int(scheme[3]))
     elif scheme == "supb":
         th = O.advect_mdfl_sup_b(d, g, U, 3600.0)
+    elif scheme.startswith("psom"):
+        th = psom_steps(O, d, g, U, 3600.0, scheme, 1)
     elif scheme.startswith("c"):
         order = int(scheme[1])
         th = O.horz_advect_centred(d, g, U, order) + O.vert_advect_centred(d, g, U, order, dom["kmt"].numpy())
@@ -121,7 +123,20 @@ def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
     assert np.abs(th).max() <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("scheme", ["mdfl", "upwind", "quicker", "c4", "ppm1", "ppm2", "ppm3", "supb"])
+def psom_steps(O, d, g, T, dtime, scheme, nsteps, moments=None):
+    """nsteps calls of advect_tracer_psom on the same T (itt0 = 0, 1, ...); the
+    tendency of the last."""
+    if moments is None:
+        moments = np.zeros((9,) + T.shape)
+    th = None
+    for itt0 in range(nsteps):
+        th, _ = O.advect_psom(d, g, T, dtime, moments, itt0=itt0, limit=scheme != "psom_nolimit",
+                              prather=scheme == "psom_prather")
+    return th
+
+
+@pytest.mark.parametrize("scheme", ["mdfl", "upwind", "quicker", "c4", "ppm1", "ppm2", "ppm3", "supb", "psom",
+                                    "psom_prather"])
 def test_global_content_conserved(O, scheme):
     """sum(dat*rho_dzt*T*tmask) (ocean_tracer_diag.F90:2395-2412) is unchanged by
     advection plus the explicit update, to FP64 roundoff."""
@@ -129,8 +144,11 @@ def test_global_content_conserved(O, scheme):
     q = O.quicker_init(d, g, dom.dzt.numpy())
     T = g["T"][0].copy()
     c0 = O.total_tracer(d, g, T)[0]
-    for _ in range(10):
-        if scheme == "mdfl":
+    moments = np.zeros((9,) + T.shape)
+    for step in range(10):
+        if scheme.startswith("psom"):
+            th, _ = O.advect_psom(d, g, T, 3600.0 * 6, moments, itt0=step, prather=scheme == "psom_prather")
+        elif scheme == "mdfl":
             th = O.advect_mdfl_sweby(d, g, T, 3600.0 * 6)
         elif scheme == "upwind":
             th = O.horz_advect_upwind(d, g, T) + O.vert_advect_upwind(d, g, T)
