@@ -216,6 +216,11 @@ def make_domain(spec: DomainSpec, device="cpu", with_barotropic: bool = True) ->
     F["dus"] = 0.5 * F["dyu"]
     F["dun"] = 0.5 * F["dyu"]
     F["f"] = (2.0 * OMEGA * torch.sin(phi_u)).contiguous()
+    # the metrics' halos hold the periodic images, as after the grid's halo
+    # updates (ocean_grids.F90:2083-2165)
+    for name in ("dxt", "dyt", "dxu", "dyu", "dxte", "dyte", "dxtn", "dytn", "dat", "datr", "dau", "daur", "dxur",
+                 "dyur", "dxter", "dytnr", "dte", "dtw", "dus", "dun", "f"):
+        F[name] = _periodic_fill(F[name].contiguous().clone(), spec.cyclic_x, spec.cyclic_y)
 
     # vertical grid
     dz = stretched_dz(nk, spec.dz_top, spec.dz_bot, spec.depth)

@@ -165,6 +165,34 @@ def test_global_content_conserved(O, scheme):
     assert abs(c1 - c0) <= 1e-13 * abs(c0)
 
 
+def test_psom_limiters_on_a_square_pulse(O):
+    """Torus pulse under PSOM for 20 steps through every sweep order: with the
+    Merryfield-Holloway limiter (the default, ocean_tracer_advect.F90:112-117)
+    and with Prather's limiter the tracer stays non-negative (Prather's limiter
+    is documented as positive definite but not monotonic, :4542-4547); without
+    a limiter the second-order moments undershoot below zero."""
+    sp = small(ni=32, nj=24, nk=4, continent=None, ntr=1, seed=3, cyclic_x=True, hmin=None, depth=400.0,
+               dz_top=80.0, dz_bot=120.0)
+    dom, g, d = load(O, sp)
+    T0 = np.zeros_like(g["T"][0])
+    T0[:, 8:16, 10:20] = 1.0
+    T0 *= g["tmask"]
+    O.halo_update(d, T0)
+    dt = 3600.0 * 6
+    wet = g["tmask"] > 0
+    ext = {}
+    for mode in ("mh", "prather", "none"):
+        T = T0.copy()
+        mom = np.zeros((9,) + T.shape)
+        for step in range(20):
+            th, _ = O.advect_psom(d, g, T, dt, mom, itt0=step, limit=mode != "none", prather=mode == "prather")
+            T = O.update_tracer(d, g, T, th, dt)
+        ext[mode] = (T[wet].min(), T[wet].max())
+    assert ext["mh"][0] >= 0.0 and ext["prather"][0] >= 0.0
+    assert ext["none"][0] < -1e-3
+    assert ext["mh"][1] < 1.01 and ext["mh"][1] < ext["prather"][1]
+
+
 def test_sweby_is_monotone_and_quicker_is_not(O):
     """Torus pulse test (testcase_ocean_solo.pdf section 2), qualitative: Quicker
     over/undershoots a square pulse, MDFL Sweby's extrema are far smaller.  The
