@@ -448,6 +448,7 @@ def run_forms(args, dom, d64, plain_value, stream):
         "max_rel_err_vs_fp64_1step": max(errs), "content_rel_change_1step": {"fp64": drift64, "precision": driftm},
         "gpu_launches": r["launches"], "clocks": r["clocks"], "autotune": tune}
     dm.close()
+    forms["schemes"] = scheme_sweep(d64, stream, ntr, cells)
     d64.close()
     del dom
     torch.cuda.empty_cache()
@@ -455,6 +456,43 @@ def run_forms(args, dom, d64, plain_value, stream):
     forms["batched"] = form_batched(args, stream)
     forms["serving"] = form_serving(args, stream, forms["batched"])
     return forms
+
+
+SCHEMES = (("upwind", "ADVECT_UPWIND"), ("2nd_order", "ADVECT_2ND_ORDER"), ("4th_order", "ADVECT_4TH_ORDER"),
+           ("6th_order", "ADVECT_6TH_ORDER"), ("quicker", "ADVECT_QUICKER"), ("mdfl_sup_b", "ADVECT_MDFL_SUP_B"),
+           ("mdppm", "ADVECT_MDPPM"), ("psom", "ADVECT_PSOM"), ("mdfl_sweby", "ADVECT_MDFL_SWEBY"))
+
+
+def scheme_sweep(d, stream, ntr, cells, steps=2):
+    """FP64 tracer advection step (every tracer on one scheme, explicit update
+    included, no barotropic) for each scheme on the headline domain."""
+    import torch
+
+    from mom5_gb300 import capi
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, const in SCHEMES:
+        sid = getattr(capi, const)
+        for n in range(1, ntr + 1):
+            d.set_tracer_scheme(n, sid, sid, -1.0e10, 1.0e10)
+            if name == "psom":
+                d.set_psom_limit(n, True)
+        launches0 = d.launches
+        d.tracer_advection_step(1, 1, 2, DTTS)  # warm-up (allocates the scheme's fields)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            d.tracer_advection_step(1, 1, 2, DTTS)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"ms_per_step": round(ms, 3), "cell_updates_per_s": round(cells / (ms / 1e3), 1),
+                     "launches_per_step": (d.launches - launches0) // (steps + 1)}
+    for n in range(1, ntr + 1):
+        d.set_tracer_scheme(n, capi.ADVECT_MDFL_SWEBY, capi.ADVECT_MDFL_SWEBY, -1.0e10, 1.0e10)
+    return {"workload": "headline domain, every tracer on one scheme, FP64 drop-in, advection + explicit update "
+                        "(no barotropic), from the same state each step; psom with the Merryfield-Holloway limiter",
+            "steps": steps, "schemes": out}
 
 
 def _load_set(specs, precisions):

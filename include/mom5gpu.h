@@ -219,6 +219,27 @@ int mom5gpu_set_psom_limit(mom5gpu_domain* d, int n, int psom_limit);
  * advance it: the host sets it each step, as ocean_model does. */
 int mom5gpu_set_itt0(mom5gpu_domain* d, long itt0);
 
+/* Name and restart file of tracer n (T_prog(n)%name and %restart_file; default
+ * "tracer<n>" in "ocean_tracer.res.nc", ocean_tpm_util.F90:76). */
+int mom5gpu_set_tracer_name(mom5gpu_domain* d, int n, const char* name, const char* restart_file);
+
+/* ---- restarts ------------------------------------------------------------ */
+/* Write the prognostic state at time level `level` into directory dir as the
+ * netCDF files fms_io save_restart writes (fms_io.F90:2996-3260, 64-bit offset
+ * format): each tracer into its restart file (ocean_tracer.F90:2658-2681);
+ * eta_t, conv_rho_ud_t, eta_t_bar, eta_u, patm_t, udrho, vdrho, forcing_u_bt,
+ * forcing_v_bt into ocean_barotropic.res.nc (ocean_barotropic.F90:5240-5294,
+ * two-level layout) when the barotropic state was set; the moments of PSOM
+ * tracers into ocean_psom_moments.res.nc (ocean_tracer_advect.F90:1795-1843).
+ * Compute-domain data, one time record, an fms checksum attribute per field. */
+int mom5gpu_write_restart(mom5gpu_domain* d, const char* dir, int level);
+/* Read those files back into time level `level` (restore_state): tracer files
+ * are required; the barotropic file when the barotropic mode is initialised;
+ * PSOM moments stay zero without their file (psom_init).  Dimensions must match
+ * the domain; a checksum attribute that disagrees with the data is
+ * MOM5GPU_ENUMERIC.  Halos are filled with the periodic images (0 elsewhere). */
+int mom5gpu_read_restart(mom5gpu_domain* d, const char* dir, int level);
+
 /* ---- initialisation (after the grid fields are set) ---------------------- */
 /* ocean_tracer_advect_init's scheme set-up: quicker_init (:1442-1586) and
  * mdfl_init (:1644-1691). */

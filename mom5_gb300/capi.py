@@ -116,6 +116,9 @@ def lib() -> C.CDLL:
             "mom5gpu_set_ppm_limiter": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_psom_limit": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_itt0": (C.c_int, [vp, C.c_long]),
+            "mom5gpu_set_tracer_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p]),
+            "mom5gpu_write_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
+            "mom5gpu_read_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
             "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
@@ -285,6 +288,16 @@ class Domain:
 
     def set_itt0(self, itt0):
         self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))
+
+    def set_tracer_name(self, n, name, restart_file=None):
+        self.check(lib().mom5gpu_set_tracer_name(self.h, n, name.encode(),
+                                                 restart_file.encode() if restart_file else None))
+
+    def write_restart(self, directory, level):
+        self.check(lib().mom5gpu_write_restart(self.h, os.fsencode(directory), level))
+
+    def read_restart(self, directory, level):
+        self.check(lib().mom5gpu_read_restart(self.h, os.fsencode(directory), level))
 
     def tracer_boundary_terms(self, n=0):
         self.check(lib().mom5gpu_tracer_boundary_terms(self.h, n))

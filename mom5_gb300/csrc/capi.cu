@@ -101,6 +101,18 @@ int cuda_fail(mom5gpu_domain* d, cudaError_t e, const char* where) {
   return fail(d, MOM5GPU_ECUDA, "%s: %s", where, cudaGetErrorString(e));
 }
 
+// Device pointer of (field, tracer n, level) if its block was ever allocated.
+double* fptr_if_set(mom5gpu_domain* d, int id, int n, int level) {
+  const FieldInfo* fi = field_info(id);
+  if (!fi) return nullptr;
+  int ntr = d->dims.num_prog_tracers;
+  if (fi->per_tracer && (n < 1 || n > ntr)) return nullptr;
+  if (fi->per_level && (level < 1 || level > 3)) return nullptr;
+  int slot = slot_of(id, fi->per_level ? level : 0);
+  if ((size_t)slot >= d->field.size() || !d->field[slot]) return nullptr;
+  return d->field[slot] + (fi->per_tracer ? (size_t)(n - 1) * field_count(d->geo, fi->shape) : 0);
+}
+
 // Device pointer of (field, tracer n, level); the block is allocated (zeroed)
 // on first use.  Returns nullptr on a bad index or allocation failure.
 double* fptr(mom5gpu_domain* d, int id, int n, int level) {
@@ -235,6 +247,10 @@ int mom5gpu_create(const mom5gpu_dims* dims, const mom5gpu_options* opt, mom5gpu
   g.n2 = (long)g.nxd * g.nyd;
   g.n3 = g.n2 * g.nk;
   d->scheme.resize(dims->num_prog_tracers);
+  for (int n = 1; n <= dims->num_prog_tracers; ++n) {
+    d->tracer_name.push_back("tracer" + std::to_string(n));
+    d->tracer_file.push_back("ocean_tracer.res.nc");  // default_restart_file, ocean_tpm_util.F90:76
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete d;

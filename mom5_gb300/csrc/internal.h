@@ -67,6 +67,7 @@ struct mom5gpu_domain {
   // one allocation per field id; nullptr until first set/used
   std::vector<double*> field;  // indexed by field id
   std::vector<mom5::TracerScheme> scheme;
+  std::vector<std::string> tracer_name, tracer_file;  // T_prog(n)%name, %restart_file
   // host copies needed at init time
   std::vector<double> dzt_h, zw_h;
   std::vector<int> kmt_h;
@@ -115,6 +116,7 @@ namespace mom5 {
 int fail(mom5gpu_domain* d, int code, const char* fmt, ...);
 int cuda_fail(mom5gpu_domain* d, cudaError_t e, const char* where);
 double* fptr(mom5gpu_domain* d, int id, int n, int level);  // nullptr if absent
+double* fptr_if_set(mom5gpu_domain* d, int id, int n, int level);  // nullptr if never allocated
 size_t field_count(const Geo& g, Shape s);
 
 // profiling sections
