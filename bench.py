@@ -292,10 +292,16 @@ def run_ours(args, rank, world):
     build.build()
     spec = config_spec(args.config)
     prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_FP64
-    forms = (not args.no_forms) and world == 1 and prec == capi.PRECISION_FP64 and args.config == "c2"
+    headline = args.scheme == "mdfl_sweby"
+    forms = (not args.no_forms) and world == 1 and prec == capi.PRECISION_FP64 and args.config == "c2" and headline
     dom = grid.make_domain(spec, device="cuda")
     opts = capi.default_options(barotropic_time_stepping_B=1, precision=prec)
     d = harness.load(dom, options=opts)
+    if not headline:
+        sid = getattr(capi, dict(SCHEMES)[args.scheme])
+        for n in range(1, spec.ntracers + 1):
+            d.set_tracer_scheme(n, sid, sid, -1.0e10, 1.0e10)
+            d.set_psom_limit(n, True)
     nts = d.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
     ni, nj, nk, ntr = spec.ni, spec.nj, spec.nk, spec.ntracers
     cells = ni * nj * nk
@@ -328,11 +334,11 @@ def run_ours(args, rank, world):
         bytes_adv = adv_bytes(ni, nj, nk, ntr)
         per = adv_ms / adv_calls
         achieved = bytes_adv / (per / 1e3) / 1e9
-        roofline = {"bound": "hbm", "kernel": "tracer advection step (mdfl passes + explicit update)",
+        roofline = {"bound": "hbm", "kernel": f"tracer advection step ({args.scheme} + explicit update)",
                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_launch": bytes_adv, "ms_per_launch": round(per, 3),
-                    "traffic": round(TRAFFIC_PER_TRACER_CELL[args.precision] * cells * ntr),
+                    "traffic": round(TRAFFIC_PER_TRACER_CELL[args.precision] * cells * ntr) if headline else None,
                     "traffic_source": "ncu DRAM bytes of the 360x270x50 block scaled by tracer-cells "
                                       "(profiles/traffic_advection_c2block.md)"}
     else:
@@ -384,7 +390,8 @@ def run_ours(args, rank, world):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == capi.PRECISION_FP64 else "f32+f64",
            "data": "synthetic (seeded streamfunction flow, partial-cell bathymetry)",
-           "config": {"workload": f"{args.config.upper()}: {ni}x{nj}x{nk}, {ntr} tracers, MDFL Sweby + {nts}-subcycle "
+           "config": {"workload": f"{args.config.upper()}: {ni}x{nj}x{nk}, {ntr} tracers, "
+                                  f"{'MDFL Sweby' if headline else args.scheme} + {nts}-subcycle "
                                   f"B-grid barotropic, dtts={DTTS:g}s dtbt={DTBT:g}s, "
                                   f"{'FP64 drop-in' if prec == capi.PRECISION_FP64 else 'precision form'}",
                       "cells": cells, "tracers": ntr, "subcycles": nts, "parallelism": f"replicas x{world}",
@@ -393,7 +400,7 @@ def run_ours(args, rank, world):
            "sections_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sec.items()},
            "barotropic_roofline": {"achieved": round(bt_achieved, 1), "unit": "GB/s", "peak": peak,
                                    "frac": round(bt_achieved / peak, 4), "note": "streaming model, 224 B/column/subcycle"},
-           "fp64_roofline": _fp64_roofline(prec, sec, args.steps, cells, ntr, ni, nj, nts),
+           "fp64_roofline": _fp64_roofline(prec, sec, args.steps, cells, ntr, ni, nj, nts) if headline else None,
            "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline and ntr > 0:
         # bounded sample of the same workload on one host core: one block of 1/16 of the domain
@@ -658,6 +665,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--config", choices=["c2", "c0", "c1", "c2s"], default="c2")
+    ap.add_argument("--scheme", choices=[n for n, _ in SCHEMES], default="mdfl_sweby",
+                    help="advection scheme of every tracer (the headline is mdfl_sweby)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")

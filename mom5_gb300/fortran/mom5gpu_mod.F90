@@ -120,6 +120,25 @@ module mom5gpu_c
        type(c_ptr), value :: dom
        integer(c_long), value :: itt0
      end function
+     integer(c_int) function mom5gpu_set_tracer_name(dom, n, name, restart_file) &
+          bind(C, name="mom5gpu_set_tracer_name")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n
+       character(kind=c_char), intent(in) :: name(*), restart_file(*)
+     end function
+     integer(c_int) function mom5gpu_write_restart(dom, dir, level) bind(C, name="mom5gpu_write_restart")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value :: dom
+       character(kind=c_char), intent(in) :: dir(*)
+       integer(c_int), value :: level
+     end function
+     integer(c_int) function mom5gpu_read_restart(dom, dir, level) bind(C, name="mom5gpu_read_restart")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value :: dom
+       character(kind=c_char), intent(in) :: dir(*)
+       integer(c_int), value :: level
+     end function
      integer(c_int) function mom5gpu_tracer_advect_init(dom) bind(C, name="mom5gpu_tracer_advect_init")
        import :: c_int, c_ptr
        type(c_ptr), value :: dom
@@ -220,7 +239,7 @@ module mom5gpu_mod
   public :: mom5gpu_attach, mom5gpu_mark_velocity_changed, mom5gpu_mark_state_changed
   public :: horz_advect_tracer, vert_advect_tracer
   public :: update_ocean_barotropic, eta_and_pbot_tendency, eta_and_pbot_update
-  public :: ocean_advection_velocity, ocean_barotropic_forcing
+  public :: ocean_advection_velocity, ocean_barotropic_forcing, device_restart_write
 
   type(c_ptr), save :: dom = c_null_ptr
   logical, save :: velocity_dirty = .true.
@@ -424,5 +443,14 @@ contains
     call check(mom5gpu_get_field(dom, F_FORCING_BT_U, 0, 0, Ext_mode%forcing_bt(:,:,1), 0), 'forcing_bt')
     call check(mom5gpu_get_field(dom, F_FORCING_BT_V, 0, 0, Ext_mode%forcing_bt(:,:,2), 0), 'forcing_bt')
   end subroutine ocean_barotropic_forcing
+
+  ! The restart files of the device-resident state at Time%taup1, in the layout
+  ! save_restart writes (ocean_tracer_restart, ocean_tracer.F90:2658-2681, and the
+  ! barotropic and PSOM files); directory is usually 'RESTART'.
+  subroutine device_restart_write(Time, directory)
+    type(ocean_time_type), intent(in) :: Time
+    character(len=*),      intent(in) :: directory
+    call check(mom5gpu_write_restart(dom, trim(directory)//c_null_char, int(Time%taup1, c_int)), 'write_restart')
+  end subroutine device_restart_write
 
 end module mom5gpu_mod
