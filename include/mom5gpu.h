@@ -199,6 +199,14 @@ size_t mom5gpu_field_count(const mom5gpu_domain* d, int field);
  * n: tracer 1..num_prog_tracers or 0; level: time level 1..3 or 0. */
 int mom5gpu_set_field(mom5gpu_domain* d, int field, int n, int level, const double* src, int on_device);
 int mom5gpu_get_field(mom5gpu_domain* d, int field, int n, int level, double* dst, int on_device);
+/* Queue a copy of field (n, level) between its device storage and host memory
+ * on `stream` (a cudaStream_t; NULL = the domain's stream) and return without
+ * waiting: to_device = 1 copies host -> device, 0 device -> host.  The host
+ * buffer must stay valid until the stream has passed the copy, and must be
+ * pinned for the copy to overlap other work.  Ordering against the domain's
+ * stream is the caller's (events), as for any stream-ordered copy. */
+int mom5gpu_copy_field_async(mom5gpu_domain* d, int field, int n, int level, double* host, int to_device,
+                             void* stream);
 /* Device address of a field (for aliasing by a caller that owns device code). */
 int mom5gpu_field_device_ptr(mom5gpu_domain* d, int field, int n, int level, double** dptr);
 /* Vertical grid for quicker_init and the barotropic CFL check: nominal dzt(nk),

@@ -116,6 +116,7 @@ def lib() -> C.CDLL:
             "mom5gpu_set_ppm_limiter": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_psom_limit": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_itt0": (C.c_int, [vp, C.c_long]),
+            "mom5gpu_copy_field_async": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
             "mom5gpu_set_tracer_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p]),
             "mom5gpu_write_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
             "mom5gpu_read_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
@@ -288,6 +289,12 @@ class Domain:
 
     def set_itt0(self, itt0):
         self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))
+
+    def copy_field_async(self, field, host_ptr, to_device, stream=None, n=0, level=0):
+        """Stream-ordered copy between the field and host memory at host_ptr (an
+        address; pinned for overlap); stream is a cudaStream_t handle or None."""
+        self.check(lib().mom5gpu_copy_field_async(self.h, field, n, level, C.c_void_p(host_ptr), int(to_device),
+                                                  C.c_void_p(stream) if stream else None))
 
     def set_tracer_name(self, n, name, restart_file=None):
         self.check(lib().mom5gpu_set_tracer_name(self.h, n, name.encode(),

@@ -369,6 +369,21 @@ int mom5gpu_get_field(mom5gpu_domain* d, int field, int n, int level, double* ds
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "get_field copy");
 }
 
+int mom5gpu_copy_field_async(mom5gpu_domain* d, int field, int n, int level, double* host, int to_device,
+                             void* stream) {
+  if (!d || !host) return d ? fail(d, MOM5GPU_EINVAL, "copy_field_async: null host buffer") : MOM5GPU_EINVAL;
+  double* p;
+  size_t cnt;
+  int rc = check_field(d, field, n, level, &p, &cnt);
+  if (rc) return rc;
+  cudaStream_t s = stream ? (cudaStream_t)stream : d->stream;
+  cudaError_t e = to_device ? cudaMemcpyAsync(p, host, sizeof(double) * cnt, cudaMemcpyDefault, s)
+                            : cudaMemcpyAsync(host, p, sizeof(double) * cnt, cudaMemcpyDefault, s);
+  if (e != cudaSuccess) return cuda_fail(d, e, "copy_field_async");
+  if (to_device && field == MOM5GPU_TMASK) d->advect_ready = false;
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_field_device_ptr(mom5gpu_domain* d, int field, int n, int level, double** dptr) {
   if (!d || !dptr) return MOM5GPU_EINVAL;
   size_t cnt;

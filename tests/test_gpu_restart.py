@@ -122,3 +122,28 @@ def test_restart_checksum_and_shape_are_checked(gpu_lib, tmp_path):
         d.read_restart(str(tmp_path), 1)
     d.close()
     d2.close()
+
+
+def test_copy_field_async_on_caller_streams(gpu_lib):
+    """mom5gpu_copy_field_async: host -> device on one stream, device -> host on
+    another after an event; the values arrive unchanged (pinned buffers)."""
+    import torch
+    capi = gpu_lib
+    F = capi.F
+    dom = grid.make_domain(_spec())
+    d = _make(capi, dom)
+    n3 = d.count(F.TRACER)
+    src = torch.randn(n3, dtype=torch.float64).pin_memory()
+    dst = torch.zeros(n3, dtype=torch.float64).pin_memory()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    d.copy_field_async(F.TRACER, src.data_ptr(), 1, up.cuda_stream, n=2, level=3)
+    e = torch.cuda.Event()
+    e.record(up)
+    down.wait_event(e)
+    d.copy_field_async(F.TRACER, dst.data_ptr(), 0, down.cuda_stream, n=2, level=3)
+    down.synchronize()
+    assert torch.equal(src, dst)
+    assert np.array_equal(d.get(F.TRACER, n=2, level=3), src.numpy())
+    with pytest.raises(capi.Mom5GpuError):
+        d.copy_field_async(F.TRACER, src.data_ptr(), 1, up.cuda_stream, n=9, level=1)
+    d.close()
