@@ -368,10 +368,10 @@ def run_ours(args, rank, world):
             d.set(fid, d.get(fid, level=1), level=3)
         oT = [pin(n3) for _ in range(ntr)]
         oE, oU, oV = pin(n2), pin(n2), pin(n2)
-        ke = max(3, min(args.steps, 6))
+        ke = max(3, min(args.steps, 10))
         h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
         ev = lambda: torch.cuda.Event()
-        h2d_done, comp_done, d2h_done = [ev() for _ in range(ke)], [ev() for _ in range(ke)], [ev() for _ in range(ke)]
+        h2d_done, adv_done, comp_done, d2h_done = ([ev() for _ in range(ke)] for _ in range(4))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for s_ in range(ke):
@@ -380,13 +380,14 @@ def run_ours(args, rank, world):
                 h2d.wait_event(d2h_done[s_ - 2])
             for n in range(ntr):
                 d.copy_field_async(F.TRACER, hT[n].data_ptr(), 1, h2d.cuda_stream, n=n + 1, level=lin)
-            if s_ >= 1:  # the velocity is read by step s-1
-                h2d.wait_event(comp_done[s_ - 1])
+            if s_ >= 1:  # the velocity is read by the tracer advection of step s-1 (not by its barotropic part)
+                h2d.wait_event(adv_done[s_ - 1])
             for fid, buf in ((F.UHRHO_ET, hU), (F.VHRHO_NT, hV), (F.WRHO_BT, hW)):
                 d.copy_field_async(fid, buf.data_ptr(), 1, h2d.cuda_stream)
             h2d_done[s_].record(h2d)
             stream.wait_event(h2d_done[s_])
             d.tracer_advection_step(lin, lin, lout, DTTS)
+            adv_done[s_].record(stream)
             d.update_ocean_barotropic(lin, lout)
             comp_done[s_].record(stream)
             d2h.wait_event(comp_done[s_])
