@@ -818,12 +818,14 @@ __global__ void k_ppm_zupd(PpmArgs a) {
                      T * (mskm1 * a.w[I3(g, i, j, km1)] - a.w[I3(g, i, j, K)]));
 }
 
-// x pass along each row (:6193-6325): tracer_mdppm after the x halo update
-__global__ void k_ppm_x(PpmArgs a) {
+// x pass along the rows (:6193-6325): tracer_mdppm after the x halo update;
+// segments of PPM_LX - 8 cells, one thread per position
+constexpr int PPM_LX = 128, PPM_BY = 8, PPM_LY = 64;
+
+__global__ void __launch_bounds__(PPM_LX) k_ppm_x(PpmArgs a) {
+  __shared__ double sm[7][PPM_LX][1];
   const Geo& g = a.g;
-  int line = blockIdx.x * blockDim.x + threadIdx.x;
-  if (line >= g.nj * g.nk) return;
-  const int j = line % g.nj + 1, k = line / g.nj;
+  const int j = blockIdx.y + 1, k = blockIdx.z;
   const double dt = a.dtime;
   auto S = [&](int i) { return tq(g, a.tz, i, j, k); };
   auto M = [&](int i) { return tq(g, a.tmask, i, j, k); };
@@ -839,15 +841,16 @@ __global__ void k_ppm_x(PpmArgs a) {
     double div = a.dyte[I2(g, i, j)] * a.uh[p] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
     a.tx[p] = Sv + dt * m * a.datr[I2(g, i, j)] / a.rdz[p] * (Fw - Fe + a.T[p] * div);
   };
-  ppm::stream_line(g.ni, a.lim, S, M, face, upd);
+  ppm::tile_line<PPM_LX, 1>(g.ni, a.lim, (int)blockIdx.x * (PPM_LX - 8) - 3, threadIdx.x, 0, true, sm, S, M, face,
+                            upd);
 }
 
-// y pass along each column (:6330-6502) and the tendency: th += -advect_tracer_mdppm
-__global__ void k_ppm_y(PpmArgs a) {
+// y pass along the columns (:6330-6502) and the tendency: th += -advect_tracer_mdppm;
+// PPM_BY columns per block, segments of PPM_LY - 8 cells
+__global__ void __launch_bounds__(PPM_BY* PPM_LY) k_ppm_y(PpmArgs a) {
+  __shared__ double sm[7][PPM_LY][PPM_BY];
   const Geo& g = a.g;
-  int line = blockIdx.x * blockDim.x + threadIdx.x;
-  if (line >= g.ni * g.nk) return;
-  const int i = line % g.ni + 1, k = line / g.ni;
+  const int i = blockIdx.x * PPM_BY + threadIdx.x + 1, k = blockIdx.z;
   const double dt = a.dtime;
   auto S = [&](int j) { return tq(g, a.tx, i, j, k); };
   auto M = [&](int j) { return tq(g, a.tmask, i, j, k); };
@@ -869,7 +872,8 @@ __global__ void k_ppm_y(PpmArgs a) {
     double advect = -rdz * (t - T) / dt * m;
     a.th[p] = a.th[p] + (-advect);
   };
-  ppm::stream_line(g.nj, a.lim, S, M, face, upd);
+  ppm::tile_line<PPM_LY, PPM_BY>(g.nj, a.lim, (int)blockIdx.y * (PPM_LY - 8) - 3, threadIdx.y, threadIdx.x,
+                                 i <= g.ni, sm, S, M, face, upd);
 }
 
 int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
@@ -913,8 +917,9 @@ int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
   k_ppm_dak<<<g3, 128, 0, s>>>(a);
   k_ppm_zflux<<<g2, 128, 0, s>>>(a);
   k_ppm_zupd<<<g3, 128, 0, s>>>(a);
-  k_ppm_x<<<(unsigned)((g.nj * g.nk + 127) / 128), 128, 0, s>>>(a);
-  k_ppm_y<<<(unsigned)((g.ni * g.nk + 127) / 128), 128, 0, s>>>(a);
+  k_ppm_x<<<dim3((g.ni + PPM_LX - 9) / (PPM_LX - 8), g.nj, g.nk), PPM_LX, 0, s>>>(a);
+  k_ppm_y<<<dim3((g.ni + PPM_BY - 1) / PPM_BY, (g.nj + PPM_LY - 9) / (PPM_LY - 8), g.nk), dim3(PPM_BY, PPM_LY), 0, s>>>(
+      a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "mdppm");
 }

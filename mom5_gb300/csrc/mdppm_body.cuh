@@ -160,5 +160,63 @@ DEVI void stream_line(int n, int lim, FS S, FM M, FF face, FU upd) {
   }
 }
 
+// The same computation as stream_line with one thread per position: a segment
+// of L positions p0 .. p0+L-1 of BI lines (lane = the line's slot) forms, stage
+// by stage with a barrier between stages, the slopes, the limited edge values,
+// the fluxes and the updates; cells p0+4 .. p0+L-5 are updated (the first and
+// last four positions only supply their neighbours).  sm holds the stages'
+// values: tracer, mask, slope, edge values, curvature and face flux.
+template <int L, int BI, class FS, class FM, class FF, class FU>
+DEVI void tile_line(int n, int lim, int p0, int t, int lane, bool lane_ok, double (*sm)[L][BI], FS S, FM M, FF face,
+                    FU upd) {
+  enum { QS, QM, QDA, QL, QR, Q6, QF };
+  const int p = p0 + t;
+  double sv = 0.0, mv = 0.0;
+  if (lane_ok && p >= -3 && p <= n + 4) {
+    sv = S(p);
+    mv = M(p);
+  }
+  sm[QS][t][lane] = sv;
+  sm[QM][t][lane] = mv;
+  __syncthreads();
+  // slope and one-sided differences of positions -1 .. n+2
+  double da = 0.0, d1m = 0.0, d1p = 0.0, d1mm = 0.0, d1pp = 0.0;
+  if (lane_ok && t >= 2 && t <= L - 3 && p >= -1 && p <= n + 2) {
+    double Sw[5], Mw[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      Sw[q] = sm[QS][t - 2 + q][lane];
+      Mw[q] = sm[QM][t - 2 + q][lane];
+    }
+    slope(Sw, Mw, da, d1m, d1p, d1mm, d1pp);
+  }
+  sm[QDA][t][lane] = da;
+  __syncthreads();
+  // limited edge values and curvature of cells 0 .. n+1
+  double el = 0.0, er = 0.0, e6 = 0.0;
+  if (lane_ok && t >= 3 && t <= L - 4 && p >= 0 && p <= n + 1) {
+    double Si = sv;
+    double Sim1 = Si - d1m, Sip1 = Si + d1p;
+    double al = 0.5 * (Sim1 + Si) + kSixth * (sm[QDA][t - 1][lane] - da);
+    double ar = 0.5 * (Si + Sip1) + kSixth * (da - sm[QDA][t + 1][lane]);
+    limit(lim, Si, da, d1m, d1p, d1mm, d1pp, al, ar);
+    el = al;
+    er = ar;
+    e6 = 6. * Si - 3. * (ar + al);
+  }
+  sm[QL][t][lane] = el;
+  sm[QR][t][lane] = er;
+  sm[Q6][t][lane] = e6;
+  __syncthreads();
+  // flux through face p (between positions p and p+1), faces 0 .. n
+  double f = 0.0;
+  if (lane_ok && t >= 3 && t <= L - 5 && p >= 0 && p <= n)
+    f = face(p, mv, sm[QM][t + 1][lane], el, er, e6, sm[QL][t + 1][lane], sm[QR][t + 1][lane], sm[Q6][t + 1][lane]);
+  sm[QF][t][lane] = f;
+  __syncthreads();
+  // update of cells 1 .. n
+  if (lane_ok && t >= 4 && t <= L - 5 && p >= 1 && p <= n) upd(p, sv, mv, sm[QF][t - 1][lane], f);
+}
+
 }  // namespace ppm
 }  // namespace mom5
