@@ -178,6 +178,61 @@ int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, in
 }
 
 // ---------------------------------------------------------------------------
+// Launch shapes shared by the flux-form schemes (upwind, centred, Quicker).
+// Horizontal: th += -tmask*(fx(i) - fx(i-1) + fy(j) - fy(j-1))*datr with each
+// face flux formed once: a block of HB threads along i covers the cells
+// i0 .. i0+HB-2 and the x faces i0-1 .. i0+HB-2 (thread t: face i0-1+t, through
+// shared memory) and marches a strip of HR rows carrying the southern y flux.
+// Vertical: th += -tmask*(fz(k-1) - fz(k)) with fz(k) the flux through the
+// bottom of level k (0 above the first), VS levels per thread and the flux
+// above a segment formed again by its thread.
+// ---------------------------------------------------------------------------
+constexpr int HB = 128, HR = 8, VS = 8;
+
+inline dim3 horz_grid(const Geo& g) { return dim3((g.ni + HB - 2) / (HB - 1), (g.nj + HR - 1) / HR, g.nk); }
+inline dim3 vert_grid(const Geo& g) { return dim3((g.ni + 127) / 128, g.nj, (g.nk + VS - 1) / VS); }
+
+template <class FX, class FY>
+DEVI void horz_faces_once(const Geo& g, const double* tmask, const double* datr, double* th, FX fx, FY fy) {
+  __shared__ double sfx[HB];
+  const int t = threadIdx.x;
+  const int i0 = blockIdx.x * (HB - 1) + 1, j0 = blockIdx.y * HR + 1, k = blockIdx.z;
+  const int iface = i0 - 1 + t, i = i0 + t;
+  const bool cell = t <= HB - 2 && i <= g.ni, face_ok = iface <= g.ni;
+  double fs = 0.0;  // y flux through the south face of the current row
+  if (cell) fs = fy(i, j0 - 1, k);
+  for (int r = 0; r < HR; ++r) {
+    const int j = j0 + r;
+    if (j > g.nj) break;  // the same j for the whole block
+    __syncthreads();      // the previous row's x fluxes are read
+    sfx[t] = face_ok ? fx(iface, j, k) : 0.0;
+    __syncthreads();
+    if (cell) {
+      double fn = fy(i, j, k);
+      long p = I3(g, i, j, k);
+      double rr = tmask[p] * (sfx[t + 1] - sfx[t] + fn - fs) * datr[I2(g, i, j)];
+      th[p] = th[p] + (-rr);
+      fs = fn;
+    }
+  }
+}
+
+template <class FZ>
+DEVI void vert_segment(const Geo& g, const double* tmask, double* th, FZ fz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+  if (i > g.ni) return;
+  const int k0 = blockIdx.z * VS, k1 = k0 + VS < g.nk ? k0 + VS : g.nk;
+  double ft1 = k0 > 0 ? fz(i, j, k0 - 1) : 0.0;
+  for (int k = k0; k < k1; ++k) {
+    double ft2 = fz(i, j, k);
+    long p = I3(g, i, j, k);
+    double r = tmask[p] * (ft1 - ft2);
+    th[p] = th[p] + (-r);
+    ft1 = ft2;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Upwind: ocean_tracer_advect.F90:2238-2294 and :2792-2824.
 // ---------------------------------------------------------------------------
 struct UpwArgs {
@@ -207,35 +262,26 @@ DEVI double upw_fn(const UpwArgs& a, int i, int j, int k) {
              : 0.0;
 }
 
-__global__ void k_upwind_horz(UpwArgs a) {
+__global__ void __launch_bounds__(HB) k_upwind_horz(UpwArgs a) {
+  horz_faces_once(
+      a.g, a.tmask, a.datr, a.th, [&](int i, int j, int k) { return upw_fe(a, i, j, k); },
+      [&](int i, int j, int k) { return upw_fn(a, i, j, k); });
+}
+
+// flux through the bottom of level k (:2800-2815)
+DEVI double upw_fz(const UpwArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j = blockIdx.y + 1, k = blockIdx.z;
-  if (i > g.ni) return;
-  long p = I3(g, i, j, k);
-  double r = a.tmask[p] * (upw_fe(a, i, j, k) - upw_fe(a, i - 1, j, k) + upw_fn(a, i, j, k) - upw_fn(a, i, j - 1, k)) *
-             a.datr[I2(g, i, j)];
-  a.th[p] = a.th[p] + (-r);
+  int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
+  long p = I3(g, i, j, k), pp = I3(g, i, j, kp1);
+  double velocity = 0.5 * a.w[I3(g, i, j, k + 1)];
+  double wpos = velocity + fabs(velocity);
+  double wneg = velocity - fabs(velocity);
+  double ft2 = (wneg * a.T[p] + wpos * a.T[pp]);
+  return (a.tmask[p] != 0.0 && a.tmask[pp] != 0.0) ? ft2 * a.tmask[p] * a.tmask[pp] : 0.0;
 }
 
 __global__ void k_upwind_vert(UpwArgs a) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j = blockIdx.y + 1;
-  if (i > g.ni) return;
-  double ft1 = 0.0;
-  for (int k = 0; k < g.nk; ++k) {
-    int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
-    long p = I3(g, i, j, k), pp = I3(g, i, j, kp1);
-    double velocity = 0.5 * a.w[I3(g, i, j, k + 1)];
-    double wpos = velocity + fabs(velocity);
-    double wneg = velocity - fabs(velocity);
-    double ft2 = (wneg * a.T[p] + wpos * a.T[pp]);
-    ft2 = (a.tmask[p] != 0.0 && a.tmask[pp] != 0.0) ? ft2 * a.tmask[p] * a.tmask[pp] : 0.0;
-    double r = a.tmask[p] * (ft1 - ft2);
-    a.th[p] = a.th[p] + (-r);
-    ft1 = ft2;
-  }
+  vert_segment(a.g, a.tmask, a.th, [&](int i, int j, int k) { return upw_fz(a, i, j, k); });
 }
 
 static UpwArgs upw_args(mom5gpu_domain* d, int n, int level) {
@@ -261,8 +307,7 @@ int launch_upwind_horz(mom5gpu_domain* d, int n, int taum1) {
     return fail(d, MOM5GPU_ESTATE, "upwind: a required field was never set");
   ClockScope clk(d, SEC_UPWIND);
   count_launches(d, 1);
-  dim3 grid((g.ni + 127) / 128, g.nj, g.nk);
-  k_upwind_horz<<<grid, 128, 0, d->stream>>>(a);
+  k_upwind_horz<<<horz_grid(g), HB, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "upwind horz");
 }
@@ -273,8 +318,7 @@ int launch_upwind_vert(mom5gpu_domain* d, int n, int taum1) {
   if (!a.tmask || !a.w || !a.T || !a.th) return fail(d, MOM5GPU_ESTATE, "upwind: a required field was never set");
   ClockScope clk(d, SEC_UPWIND);
   count_launches(d, 1);
-  dim3 grid((g.ni + 127) / 128, g.nj);
-  k_upwind_vert<<<grid, 128, 0, d->stream>>>(a);
+  k_upwind_vert<<<vert_grid(g), 128, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "upwind vert");
 }
@@ -360,50 +404,38 @@ DEVI double quk_fy(const QukArgs& a, int i, int j, int k) {
          uneg * (a.q.curv_yn[q] * (soutmsk ? tq1 : tq2) + a.q.curv_yn[n2 + q] * tq1 + a.q.curv_yn[2 * n2 + q] * tq0);
 }
 
-__global__ void k_quicker_horz(QukArgs a) {
+__global__ void __launch_bounds__(HB) k_quicker_horz(QukArgs a) {
+  horz_faces_once(
+      a.g, a.tmask, a.datr, a.th, [&](int i, int j, int k) { return quk_fx(a, i, j, k); },
+      [&](int i, int j, int k) { return quk_fy(a, i, j, k); });
+}
+
+// flux through the bottom of level k (:2981-3031)
+DEVI double quk_fz(const QukArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j = blockIdx.y + 1, k = blockIdx.z;
-  if (i > g.ni) return;
+  const int nk = g.nk;
+  int km1 = k > 0 ? k - 1 : 0;
+  int kp1 = k + 1 < nk ? k + 1 : nk - 1;
+  int p2 = k + 2 < nk ? k + 2 : nk - 1;
   long p = I3(g, i, j, k);
-  double r = a.tmask[p] * (quk_fx(a, i, j, k) - quk_fx(a, i - 1, j, k) + quk_fy(a, i, j, k) - quk_fy(a, i, j - 1, k)) *
-             a.datr[I2(g, i, j)];
-  a.th[p] = a.th[p] + (-r);
+  double vel = a.w[I3(g, i, j, k + 1)];
+  double upos = 0.5 * (vel + fabs(vel));
+  double uneg = 0.5 * (vel - fabs(vel));
+  const double* Tm = a.Tm1;
+  if (a.tmask_limit[p] == 1.0)
+    return (uneg * Tm[p] + upos * Tm[I3(g, i, j, kp1)]) * a.tmask[p] * a.tmask[I3(g, i, j, kp1)];
+  // kp2 = nint(tmask(p2)*p2 + (1-tmask(p2))*kp1): p2 when level p2 is wet, else kp1
+  int kp2 = a.tmask[I3(g, i, j, p2)] != 0.0 ? p2 : kp1;
+  bool upmsk = a.tmask[p] != 0.0 && a.tmask[I3(g, i, j, km1)] == 0.0;
+  return vel * (a.q.quick_z[k] * a.T0[p] + a.q.quick_z[nk + k] * a.T0[I3(g, i, j, kp1)]) -
+         uneg * (a.q.curv_zp[k] * Tm[I3(g, i, j, kp1)] + a.q.curv_zp[nk + k] * Tm[p] +
+                 a.q.curv_zp[2 * nk + k] * Tm[I3(g, i, j, km1)]) -
+         upos * (a.q.curv_zn[k] * Tm[I3(g, i, j, kp2)] + a.q.curv_zn[nk + k] * Tm[I3(g, i, j, kp1)] +
+                 a.q.curv_zn[2 * nk + k] * (upmsk ? Tm[I3(g, i, j, kp1)] : Tm[p]));
 }
 
 __global__ void k_quicker_vert(QukArgs a) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  int j = blockIdx.y + 1;
-  if (i > g.ni) return;
-  int nk = g.nk;
-  double ft1 = 0.0;
-  for (int k = 0; k < nk; ++k) {
-    int km1 = k > 0 ? k - 1 : 0;
-    int kp1 = k + 1 < nk ? k + 1 : nk - 1;
-    int p2 = k + 2 < nk ? k + 2 : nk - 1;
-    long p = I3(g, i, j, k);
-    double vel = a.w[I3(g, i, j, k + 1)];
-    double upos = 0.5 * (vel + fabs(vel));
-    double uneg = 0.5 * (vel - fabs(vel));
-    double ft2;
-    const double* Tm = a.Tm1;
-    if (a.tmask_limit[p] == 1.0) {
-      ft2 = (uneg * Tm[p] + upos * Tm[I3(g, i, j, kp1)]) * a.tmask[p] * a.tmask[I3(g, i, j, kp1)];
-    } else {
-      // kp2 = nint(tmask(p2)*p2 + (1-tmask(p2))*kp1): p2 when level p2 is wet, else kp1
-      int kp2 = a.tmask[I3(g, i, j, p2)] != 0.0 ? p2 : kp1;
-      bool upmsk = a.tmask[p] != 0.0 && a.tmask[I3(g, i, j, km1)] == 0.0;
-      ft2 = vel * (a.q.quick_z[k] * a.T0[p] + a.q.quick_z[nk + k] * a.T0[I3(g, i, j, kp1)]) -
-            uneg * (a.q.curv_zp[k] * Tm[I3(g, i, j, kp1)] + a.q.curv_zp[nk + k] * Tm[p] +
-                    a.q.curv_zp[2 * nk + k] * Tm[I3(g, i, j, km1)]) -
-            upos * (a.q.curv_zn[k] * Tm[I3(g, i, j, kp2)] + a.q.curv_zn[nk + k] * Tm[I3(g, i, j, kp1)] +
-                    a.q.curv_zn[2 * nk + k] * (upmsk ? Tm[I3(g, i, j, kp1)] : Tm[p]));
-    }
-    double r = a.tmask[p] * (ft1 - ft2);
-    a.th[p] = a.th[p] + (-r);
-    ft1 = ft2;
-  }
+  vert_segment(a.g, a.tmask, a.th, [&](int i, int j, int k) { return quk_fz(a, i, j, k); });
 }
 
 static int quk_args(mom5gpu_domain* d, int n, int taum1, int tau, QukArgs* a) {
@@ -435,8 +467,7 @@ int launch_quicker_horz(mom5gpu_domain* d, int n, int taum1, int tau) {
   ClockScope clk(d, SEC_QUICKER);
   count_launches(d, 1);
   const Geo& g = d->geo;
-  dim3 grid((g.ni + 127) / 128, g.nj, g.nk);
-  k_quicker_horz<<<grid, 128, 0, d->stream>>>(a);
+  k_quicker_horz<<<horz_grid(g), HB, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "quicker horz");
 }
@@ -448,8 +479,7 @@ int launch_quicker_vert(mom5gpu_domain* d, int n, int taum1, int tau) {
   ClockScope clk(d, SEC_QUICKER);
   count_launches(d, 1);
   const Geo& g = d->geo;
-  dim3 grid((g.ni + 127) / 128, g.nj);
-  k_quicker_vert<<<grid, 128, 0, d->stream>>>(a);
+  k_quicker_vert<<<vert_grid(g), 128, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "quicker vert");
 }
@@ -503,46 +533,31 @@ DEVI double cen_fy(const CenArgs& a, int i, int j, int k) {
 }
 
 template <int ORDER>
-__global__ void k_centred_horz(CenArgs a) {
+__global__ void __launch_bounds__(HB) k_centred_horz(CenArgs a) {
+  horz_faces_once(
+      a.g, a.tmask, a.datr, a.th, [&](int i, int j, int k) { return cen_fx<ORDER>(a, i, j, k); },
+      [&](int i, int j, int k) { return cen_fy<ORDER>(a, i, j, k); });
+}
+
+// flux through the bottom of level k (Fortran level K = k+1)
+template <int ORDER>
+DEVI double cen_fz(const CenArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
-  if (i > g.ni) return;
-  long p = I3(g, i, j, k);
-  double r = a.tmask[p] *
-             (cen_fx<ORDER>(a, i, j, k) - cen_fx<ORDER>(a, i - 1, j, k) + cen_fy<ORDER>(a, i, j, k) -
-              cen_fy<ORDER>(a, i, j - 1, k)) *
-             a.datr[I2(g, i, j)];
-  a.th[p] = a.th[p] + (-r);
+  const int nk = g.nk, K = k + 1;
+  double w = a.w[I3(g, i, j, K)];
+  int p1 = K + 1 < nk ? K + 1 : nk, p2 = K + 2 < nk ? K + 2 : nk, km1 = K - 1 > 1 ? K - 1 : 1;
+  auto TV = [&](int L) { return a.T[I3(g, i, j, L - 1)]; };
+  if (ORDER == 2) return w * 0.5 * (TV(K) + TV(p1));
+  double tp2 = a.tmask[I3(g, i, j, p2 - 1)];
+  int kp2 = (int)rint(tp2 * p2 + (1.0 - tp2) * p1);
+  if (ORDER == 6 && !(K <= 2 || K >= nk - 1) && K < a.kmt[I2(g, i, j)] - 2)
+    return w * (kA6 * (TV(K) + TV(p1)) + kB6 * (TV(km1) + TV(kp2)) + kC6 * (TV(K - 2) + TV(K + 3)));
+  return w * (kA4 * (TV(K) + TV(p1)) + kB4 * (TV(km1) + TV(kp2)));
 }
 
 template <int ORDER>
 __global__ void k_centred_vert(CenArgs a) {
-  const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
-  if (i > g.ni) return;
-  const int nk = g.nk;
-  const int kmt = ORDER == 6 ? a.kmt[I2(g, i, j)] : 0;
-  double ft1 = 0.0;
-  for (int K = 1; K <= nk; ++K) {  // Fortran level numbers
-    double w = a.w[I3(g, i, j, K)];
-    int p1 = K + 1 < nk ? K + 1 : nk, p2 = K + 2 < nk ? K + 2 : nk, km1 = K - 1 > 1 ? K - 1 : 1;
-    auto TV = [&](int L) { return a.T[I3(g, i, j, L - 1)]; };
-    double ft2;
-    if (ORDER == 2) {
-      ft2 = w * 0.5 * (TV(K) + TV(p1));
-    } else {
-      double tp2 = a.tmask[I3(g, i, j, p2 - 1)];
-      int kp2 = (int)rint(tp2 * p2 + (1.0 - tp2) * p1);
-      if (ORDER == 6 && !(K <= 2 || K >= nk - 1) && K < kmt - 2)
-        ft2 = w * (kA6 * (TV(K) + TV(p1)) + kB6 * (TV(km1) + TV(kp2)) + kC6 * (TV(K - 2) + TV(K + 3)));
-      else
-        ft2 = w * (kA4 * (TV(K) + TV(p1)) + kB4 * (TV(km1) + TV(kp2)));
-    }
-    long p = I3(g, i, j, K - 1);
-    double r = a.tmask[p] * (ft1 - ft2);
-    a.th[p] = a.th[p] + (-r);
-    ft1 = ft2;
-  }
+  vert_segment(a.g, a.tmask, a.th, [&](int i, int j, int k) { return cen_fz<ORDER>(a, i, j, k); });
 }
 
 int ensure_kmt_device(mom5gpu_domain* d) {
@@ -581,12 +596,12 @@ int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz) {
   }
   count_launches(d, 1);
   if (horz) {
-    dim3 grid((g.ni + 127) / 128, g.nj, g.nk);
-    if (order == 2) k_centred_horz<2><<<grid, 128, 0, d->stream>>>(a);
-    else if (order == 4) k_centred_horz<4><<<grid, 128, 0, d->stream>>>(a);
-    else k_centred_horz<6><<<grid, 128, 0, d->stream>>>(a);
+    dim3 grid = horz_grid(g);
+    if (order == 2) k_centred_horz<2><<<grid, HB, 0, d->stream>>>(a);
+    else if (order == 4) k_centred_horz<4><<<grid, HB, 0, d->stream>>>(a);
+    else k_centred_horz<6><<<grid, HB, 0, d->stream>>>(a);
   } else {
-    dim3 grid((g.ni + 127) / 128, g.nj);
+    dim3 grid = vert_grid(g);
     if (order == 2) k_centred_vert<2><<<grid, 128, 0, d->stream>>>(a);
     else if (order == 4) k_centred_vert<4><<<grid, 128, 0, d->stream>>>(a);
     else k_centred_vert<6><<<grid, 128, 0, d->stream>>>(a);
@@ -637,16 +652,21 @@ DEVI double supb_zflux(const SupbArgs& a, int i, int j, int k) {
   return supb_flux(a.dat[I2(g, i, j)] * w, cfl, Rjm, Rj, Rjp, Tk, Tkp1, m2d(a, i, j, kp1), m2d(a, i, j, k));
 }
 
+// z step down a segment of VS levels carrying the flux through the top of the level
 __global__ void k_supb_z(SupbArgs a) {
   const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
   if (i > g.ni) return;
-  long p = I3(g, i, j, k);
-  double fbt = supb_zflux(a, i, j, k);
-  double ftp = k > 0 ? supb_zflux(a, i, j, k - 1) : 0.0;
-  double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
-  double Tk = a.T[p];
-  a.tz[p] = Tk + a.dtime / a.rdz[p] * (a.datr[I2(g, i, j)] * (fbt - ftp) + Tk * (wkm1 - a.w[I3(g, i, j, k + 1)]));
+  const int k0 = blockIdx.z * VS, k1 = k0 + VS < g.nk ? k0 + VS : g.nk;
+  double ftp = k0 > 0 ? supb_zflux(a, i, j, k0 - 1) : 0.0;
+  for (int k = k0; k < k1; ++k) {
+    long p = I3(g, i, j, k);
+    double fbt = supb_zflux(a, i, j, k);
+    double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
+    double Tk = a.T[p];
+    a.tz[p] = Tk + a.dtime / a.rdz[p] * (a.datr[I2(g, i, j)] * (fbt - ftp) + Tk * (wkm1 - a.w[I3(g, i, j, k + 1)]));
+    ftp = fbt;
+  }
 }
 
 DEVI double supb_xflux(const SupbArgs& a, int i, int j, int k) {
@@ -660,14 +680,18 @@ DEVI double supb_xflux(const SupbArgs& a, int i, int j, int k) {
   return supb_flux(a.dyte[I2(g, i, j)] * u, cfl, Rjm, Rj, Rjp, t(i + 1), t(i), m2d(a, i, j, k), m2d(a, i + 1, j, k));
 }
 
-__global__ void k_supb_x(SupbArgs a) {
+// x step of one row: thread t forms the flux through face i0-1+t once (shared memory)
+__global__ void __launch_bounds__(HB) k_supb_x(SupbArgs a) {
+  __shared__ double sfx[HB];
   const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
-  if (i > g.ni) return;
+  const int t = threadIdx.x, i0 = blockIdx.x * (HB - 1) + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  const int iface = i0 - 1 + t, i = i0 + t;
+  sfx[t] = iface <= g.ni ? supb_xflux(a, iface, j, k) : 0.0;
+  __syncthreads();
+  if (t > HB - 2 || i > g.ni) return;
   long p = I3(g, i, j, k);
   double div = a.dyte[I2(g, i, j)] * a.uh[p] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
-  a.tx[p] = a.tz[p] + a.dtime * m2d(a, i, j, k) * a.datr[I2(g, i, j)] / a.rdz[p] *
-                          (supb_xflux(a, i - 1, j, k) - supb_xflux(a, i, j, k) + a.T[p] * div);
+  a.tx[p] = a.tz[p] + a.dtime * m2d(a, i, j, k) * a.datr[I2(g, i, j)] / a.rdz[p] * (sfx[t] - sfx[t + 1] + a.T[p] * div);
 }
 
 DEVI double supb_yflux(const SupbArgs& a, int i, int j, int k) {
@@ -681,19 +705,25 @@ DEVI double supb_yflux(const SupbArgs& a, int i, int j, int k) {
   return supb_flux(a.dxtn[I2(g, i, j)] * v, cfl, Rjm, Rj, Rjp, t(j + 1), t(j), m2d(a, i, j, k), m2d(a, i, j + 1, k));
 }
 
+// y step and tendency along a strip of HR rows carrying the flux through the south face
 __global__ void k_supb_y(SupbArgs a) {
   const Geo& g = a.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j0 = blockIdx.y * HR + 1, k = blockIdx.z;
   if (i > g.ni) return;
-  long p = I3(g, i, j, k);
-  double rdz = a.rdz[p], datr = a.datr[I2(g, i, j)], T = a.T[p];
-  double t = a.tx[p] + a.dtime * a.tmask[p] * datr / rdz * (supb_yflux(a, i, j - 1, k) - supb_yflux(a, i, j, k));
-  double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
-  t = t + a.dtime * T / rdz *
-              (a.w[I3(g, i, j, k + 1)] - wkm1 +
-               datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] - a.dyte[I2(g, i, j)] * a.uh[p]));
-  double advect = -rdz * (t - T) / a.dtime * m2d(a, i, j, k);
-  a.th[p] = a.th[p] + (-advect);
+  double fs = supb_yflux(a, i, j0 - 1, k);
+  for (int j = j0; j < j0 + HR && j <= g.nj; ++j) {
+    long p = I3(g, i, j, k);
+    double fn = supb_yflux(a, i, j, k);
+    double rdz = a.rdz[p], datr = a.datr[I2(g, i, j)], T = a.T[p];
+    double t = a.tx[p] + a.dtime * a.tmask[p] * datr / rdz * (fs - fn);
+    double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
+    t = t + a.dtime * T / rdz *
+                (a.w[I3(g, i, j, k + 1)] - wkm1 +
+                 datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] - a.dyte[I2(g, i, j)] * a.uh[p]));
+    double advect = -rdz * (t - T) / a.dtime * m2d(a, i, j, k);
+    a.th[p] = a.th[p] + (-advect);
+    fs = fn;
+  }
 }
 
 int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
@@ -725,10 +755,9 @@ int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime
     if (!p) return fail(d, MOM5GPU_ESTATE, "mdfl_sup_b: a required field was never set");
   ClockScope clk(d, SEC_MDFL);
   count_launches(d, 3);
-  dim3 g3((g.ni + 127) / 128, g.nj, g.nk);
-  k_supb_z<<<g3, 128, 0, d->stream>>>(a);
-  k_supb_x<<<g3, 128, 0, d->stream>>>(a);
-  k_supb_y<<<g3, 128, 0, d->stream>>>(a);
+  k_supb_z<<<vert_grid(g), 128, 0, d->stream>>>(a);
+  k_supb_x<<<dim3((g.ni + HB - 2) / (HB - 1), g.nj, g.nk), HB, 0, d->stream>>>(a);
+  k_supb_y<<<dim3((g.ni + 127) / 128, (g.nj + HR - 1) / HR, g.nk), 128, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "mdfl_sup_b");
 }
