@@ -793,7 +793,10 @@ __global__ void k_ppm_dak(PpmArgs a) {
 }
 
 // edge values, limiter and the fluxes through the bottom (massflux <= 0) and top
-// (massflux > 0) faces of every cell of a column (:6101-6170)
+// (massflux > 0) faces of a cell (:6101-6170).  The reference's loop over the
+// levels carries nothing from one level to the next, and a face is written by
+// exactly one of its two cells (the same mask-product massflux, <= 0 from above,
+// > 0 from below), so every cell runs in its own thread.
 __global__ void k_ppm_zflux(PpmArgs a) {
   const Geo& g = a.g;
   int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
@@ -802,7 +805,8 @@ __global__ void k_ppm_zflux(PpmArgs a) {
   const long q = I2(g, i, j);
   auto at = [&](const double* f, int L) { return f[I3(g, i, j, L - 1)]; };
   const double dat = a.dat[q];
-  for (int K = 1; K <= nk; ++K) {
+  {
+    const int K = blockIdx.z + 1;
     int km2 = K - 2 > 1 ? K - 2 : 1, km1 = K - 1 > 1 ? K - 1 : 1, kp1 = K + 1 < nk ? K + 1 : nk,
         kp2 = K + 2 < nk ? K + 2 : nk;
     double mskp2 = at(a.tmask, kp2) * (double)(kp2 - kp1), mskp1 = at(a.tmask, kp1) * (double)(kp1 - K);
@@ -942,9 +946,9 @@ int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
   ClockScope clk(d, SEC_MDFL);
   count_launches(d, 5);
   cudaStream_t s = d->stream;
-  dim3 g3((g.ni + 127) / 128, g.nj, g.nk), g2((g.ni + 127) / 128, g.nj);
+  dim3 g3((g.ni + 127) / 128, g.nj, g.nk);
   k_ppm_dak<<<g3, 128, 0, s>>>(a);
-  k_ppm_zflux<<<g2, 128, 0, s>>>(a);
+  k_ppm_zflux<<<g3, 128, 0, s>>>(a);
   k_ppm_zupd<<<g3, 128, 0, s>>>(a);
   k_ppm_x<<<dim3((g.ni + PPM_LX - 9) / (PPM_LX - 8), g.nj, g.nk), PPM_LX, 0, s>>>(a);
   k_ppm_y<<<dim3((g.ni + PPM_BY - 1) / PPM_BY, (g.nj + PPM_LY - 9) / (PPM_LY - 8), g.nk), dim3(PPM_BY, PPM_LY), 0, s>>>(
