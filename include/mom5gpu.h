@@ -286,6 +286,12 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
  * taup1 = 2: time level 2 of the tracers and th_tendency are overwritten.
  * A summary is written to report (may be NULL). */
 int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len);
+/* The launch shape autotune chose, or one to pin: precision-form tile height
+ * (16 or 32 rows incl. halo), tracer prefetch into shared memory (height 16
+ * only), FP64 y-pass rows per thread (0 = built-in choice, 2, 4, 8, 16).
+ * Every shape gives the same results bit for bit. */
+int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
+int mom5gpu_get_tuning(const mom5gpu_domain* d, int* rows, int* prefetch, int* tj);
 /* eta_and_pbot_tendency (ocean_barotropic.F90:2668-2734), depth-based. */
 int mom5gpu_eta_and_pbot_tendency(mom5gpu_domain* d, int tau);
 /* eta_and_pbot_update (ocean_barotropic.F90:2290-2385), depth-based, no OBC. */

@@ -116,6 +116,8 @@ def lib() -> C.CDLL:
             "mom5gpu_set_ppm_limiter": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_psom_limit": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_itt0": (C.c_int, [vp, C.c_long]),
+            "mom5gpu_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+            "mom5gpu_get_tuning": (C.c_int, [vp, ip, ip, ip]),
             "mom5gpu_copy_field_async": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
             "mom5gpu_set_tracer_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p]),
             "mom5gpu_write_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
@@ -286,6 +288,17 @@ class Domain:
 
     def set_psom_limit(self, n, on):
         self.check(lib().mom5gpu_set_psom_limit(self.h, n, int(bool(on))))
+
+    @property
+    def tuning(self):
+        r, p, t = C.c_int(), C.c_int(), C.c_int()
+        self.check(lib().mom5gpu_get_tuning(self.h, C.byref(r), C.byref(p), C.byref(t)))
+        return r.value, p.value, t.value
+
+    @tuning.setter
+    def tuning(self, v):
+        rows, prefetch, tj = v
+        self.check(lib().mom5gpu_set_tuning(self.h, rows, int(prefetch), tj))
 
     def set_itt0(self, itt0):
         self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))

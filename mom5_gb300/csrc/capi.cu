@@ -821,14 +821,33 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
   return launch_update_tracer(d, 1, ntr, taum1, taup1, dtime);
 }
 
+int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj) {
+  if (!d) return MOM5GPU_EINVAL;
+  if ((rows != 16 && rows != 32) || (prefetch && rows != 16) || !(tj == 0 || tj == 2 || tj == 4 || tj == 8 || tj == 16))
+    return fail(d, MOM5GPU_EINVAL, "set_tuning: rows 16|32 (prefetch only with 16), tj 0|2|4|8|16");
+  d->tune_mixed_rows = rows;
+  d->tune_mixed_pf = prefetch ? 1 : 0;
+  d->tune_y_tj = tj;
+  return MOM5GPU_OK;
+}
+
+int mom5gpu_get_tuning(const mom5gpu_domain* d, int* rows, int* prefetch, int* tj) {
+  if (!d || !rows || !prefetch || !tj) return MOM5GPU_EINVAL;
+  *rows = d->tune_mixed_rows;
+  *prefetch = d->tune_mixed_pf;
+  *tj = d->tune_y_tj;
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len) {
   if (!d) return MOM5GPU_EINVAL;
   if (!d->advect_ready) return fail(d, MOM5GPU_ESTATE, "autotune before mom5gpu_tracer_advect_init");
   bool mixed = d->opt.precision == MOM5GPU_PRECISION_MIXED;
-  // candidate launch shapes: precision-form tile height; FP64 y-pass rows per thread
-  const int kRows[] = {32, 16};
+  // candidate launch shapes: precision-form tile height (and tracer prefetch); FP64 y-pass rows per thread
+  const int kRows[] = {32, 16, 16};
+  const int kPf[] = {0, 0, 1};
   const int kTj[] = {2, 4, 8, 16};
-  int ncand = mixed ? 2 : 4;
+  int ncand = mixed ? 3 : 4;
   cudaEvent_t t0, t1;
   if (cudaEventCreate(&t0) != cudaSuccess) return fail(d, MOM5GPU_ECUDA, "autotune events");
   if (cudaEventCreate(&t1) != cudaSuccess) {
@@ -839,8 +858,12 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   double best = 1e30;
   int bestc = 0, rc = MOM5GPU_OK;
   for (int c = 0; c < ncand && rc == MOM5GPU_OK; ++c) {
-    if (mixed) d->tune_mixed_rows = kRows[c];
-    else d->tune_y_tj = kTj[c];
+    if (mixed) {
+      d->tune_mixed_rows = kRows[c];
+      d->tune_mixed_pf = kPf[c];
+    } else {
+      d->tune_y_tj = kTj[c];
+    }
     rc = mom5gpu_tracer_advection_step(d, 1, 1, 2, dtime);  // warm-up
     cudaEventRecord(t0, d->stream);
     for (int r = 0; r < 3 && rc == MOM5GPU_OK; ++r) rc = mom5gpu_tracer_advection_step(d, 1, 1, 2, dtime);
@@ -855,7 +878,8 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
     cudaEventElapsedTime(&ms, t0, t1);
     ms /= 3.f;
     char line[96];
-    snprintf(line, sizeof(line), mixed ? "rows=%d: %.3f ms; " : "tj=%d: %.3f ms; ", mixed ? kRows[c] : kTj[c], ms);
+    if (mixed) snprintf(line, sizeof(line), "rows=%d%s: %.3f ms; ", kRows[c], kPf[c] ? "+prefetch" : "", ms);
+    else snprintf(line, sizeof(line), "tj=%d: %.3f ms; ", kTj[c], ms);
     rep += line;
     if (ms < best) {
       best = ms;
@@ -864,11 +888,16 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
-  if (mixed) d->tune_mixed_rows = kRows[bestc];
-  else d->tune_y_tj = kTj[bestc];
+  if (mixed) {
+    d->tune_mixed_rows = kRows[bestc];
+    d->tune_mixed_pf = kPf[bestc];
+  } else {
+    d->tune_y_tj = kTj[bestc];
+  }
   if (rc) return rc;
   char line[64];
-  snprintf(line, sizeof(line), mixed ? "chosen rows=%d" : "chosen tj=%d", mixed ? kRows[bestc] : kTj[bestc]);
+  if (mixed) snprintf(line, sizeof(line), "chosen rows=%d%s", kRows[bestc], kPf[bestc] ? "+prefetch" : "");
+  else snprintf(line, sizeof(line), "chosen tj=%d", kTj[bestc]);
   rep += line;
   if (report && report_len) {
     strncpy(report, rep.c_str(), report_len - 1);

@@ -28,33 +28,44 @@ using namespace mixed;
 
 namespace {
 
-template <int NC, int ZR>
-__global__ void __launch_bounds__(NT, ZR == 16 ? 4 : 2) k_mdfl_mixed(MixArgs a, int n0) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
-  mixed_tile<NC, ZR>(a, n0, blockIdx.x, blockIdx.y, s);
+// shared memory: the tile arrays, then (prefetch variant) the tracer buffers
+template <int ZR, bool PF>
+constexpr size_t mixed_smem() {
+  return ((sizeof(SmemT<ZR>) + 15) & ~(size_t)15) + (PF ? sizeof(PrefetchT<ZR>) : 0);
 }
 
-template <int NC, int ZR>
+template <int NC, int ZR, bool PF>
+__global__ void __launch_bounds__(NT, PF ? 2 : (ZR == 16 ? 4 : 2)) k_mdfl_mixed(MixArgs a, int n0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
+  PrefetchT<ZR>* pf =
+      PF ? reinterpret_cast<PrefetchT<ZR>*>(smem_raw + ((sizeof(SmemT<ZR>) + 15) & ~(size_t)15)) : nullptr;
+  mixed_tile<NC, ZR, PF>(a, n0, blockIdx.x, blockIdx.y, s, pf);
+}
+
+template <int NC, int ZR, bool PF>
 int run_mixed_zr(mom5gpu_domain* d, MixArgs a, int n0) {
   const Geo& g = d->geo;
-  size_t smem = sizeof(SmemT<ZR>);
+  constexpr size_t smem = mixed_smem<ZR, PF>();
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_mdfl_mixed<NC, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_mdfl_mixed<NC, ZR, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(d, e, "mixed kernel attribute");
     configured = true;
   }
   constexpr int TJ = ZR - 4;
   dim3 grid((g.ni + TI - 1) / TI, (g.nj + TJ - 1) / TJ);
-  k_mdfl_mixed<NC, ZR><<<grid, NT, smem, d->stream>>>(a, n0);
+  k_mdfl_mixed<NC, ZR, PF><<<grid, NT, smem, d->stream>>>(a, n0);
   count_launches(d, 1);
   return MOM5GPU_OK;
 }
 
 template <int NC>
 int run_mixed(mom5gpu_domain* d, MixArgs a, int n0) {
-  return d->tune_mixed_rows == 16 ? run_mixed_zr<NC, 16>(d, a, n0) : run_mixed_zr<NC, 32>(d, a, n0);
+  if (d->tune_mixed_rows == 16)
+    return d->tune_mixed_pf ? run_mixed_zr<NC, 16, true>(d, a, n0) : run_mixed_zr<NC, 16, false>(d, a, n0);
+  return run_mixed_zr<NC, 32, false>(d, a, n0);
 }
 
 }  // namespace

@@ -92,8 +92,24 @@ struct SmemT {
   int off[ZR * ZW];      // 2-D offset j*nxd+i of the position's image; -1 outside a wall
 };
 
-template <int NC, int ZR>
-DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>& s) {
+// Stream-ordered 8-byte copy global -> shared (cp.async, L1-allocating); src_size 0
+// fills the destination with zeros and reads nothing.
+DEVI void cp_async8(void* dst, const void* src, int src_size) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(src_size) : "memory");
+}
+DEVI void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+DEVI void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Shared memory of the tracer prefetch: two buffers of the four levels
+// km1, k, kp1, kp2 of one tracer over the tile (FP64, as stored).
+template <int ZR>
+struct PrefetchT {
+  double tb[2][4][ZR * ZW];
+};
+
+template <int NC, int ZR, bool PF = false>
+DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>& s, PrefetchT<ZR>* pf = nullptr) {
   constexpr int TJ = ZR - 4;
   constexpr int ROWS_PER_WARP = ZR / NW;
   const Geo& g = a.g;
@@ -101,6 +117,28 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
   const int i0 = 1 + tile_x * TI, j0 = 1 + tile_y * TJ;
   const float dt = a.dtime;
   const float sixth = 1.0f / 6.0f;
+  // image offsets of this thread's tile positions (the same at every level)
+  int offr[ROWS_PER_WARP];
+#pragma unroll
+  for (int m = 0; m < ROWS_PER_WARP; ++m) {
+    int i = i0 - 2 + lane, j = j0 - 2 + warp + NW * m;
+    offr[m] = image(g, i, j) ? (int)I2(g, i, j) : -1;
+  }
+  // queue the four levels of tracer n into prefetch buffer b (zeros outside a wall)
+  auto prefetch = [&](int n, int b, int km1, int k, int kp1, int kp2) {
+    const double* T = a.T + (long)n * g.n3;
+    const int lev[4] = {km1, k, kp1, kp2};
+#pragma unroll
+    for (int m = 0; m < ROWS_PER_WARP; ++m) {
+      const int c = (warp + NW * m) * ZW + lane, o = offr[m];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double* src = o >= 0 ? T + (long)lev[q] * g.n2 + o : T;
+        cp_async8(&pf->tb[b][q][c], src, o >= 0 ? 8 : 0);
+      }
+    }
+    cp_async_commit();
+  };
 
   // per-thread z columns: zi = lane, zj = warp + NW*m
   float ftp[NC][ROWS_PER_WARP];
@@ -114,6 +152,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
     const int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
     const int km1 = k > 0 ? k - 1 : 0;
     __syncthreads();  // previous level done with every tile array
+    if (PF && a.ntr > 0) prefetch(0, 0, km1, k, kp1, kp2);  // overlaps the level terms
     // ---- level terms: z columns, x faces/cells, y faces ----
 #pragma unroll
     for (int m = 0; m < ROWS_PER_WARP; ++m) {
@@ -205,12 +244,20 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
       s.uq[c] = uq;
       s.ur[c] = ur;
     }
+    if (PF) cp_async_wait_all();
     __syncthreads();
 
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
       if (n >= a.ntr) break;
       const double* T = a.T + (long)n * g.n3;
+      if (PF) {
+        if (n > 0) {  // tracer n has arrived and every thread is done with tracer n-1
+          cp_async_wait_all();
+          __syncthreads();
+        }
+        if (n + 1 < a.ntr && n + 1 < NC) prefetch(n + 1, (n + 1) & 1, km1, k, kp1, kp2);
+      }
       // A tile row (32 columns) is one warp: the z pass, the x fluxes and the x
       // update of a row exchange neighbours with warp shuffles; only the y pass
       // reads other rows (shared memory, two barriers per tracer).
@@ -223,10 +270,19 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
         const uint8_t mb = s.zmask[c];
         float tzv = 0.f, tk = 0.f, fzv = 0.f;
         if (o >= 0) {
-          tk = d2f(T[(long)k * g.n2 + o]);
-          float tkm1 = d2f(T[(long)km1 * g.n2 + o]);
-          float tkp1 = d2f(T[(long)kp1 * g.n2 + o]);
-          float tkp2 = d2f(T[(long)kp2 * g.n2 + o]);
+          float tkm1, tkp1, tkp2;
+          if (PF) {
+            const int b = n & 1;
+            tkm1 = d2f(pf->tb[b][0][c]);
+            tk = d2f(pf->tb[b][1][c]);
+            tkp1 = d2f(pf->tb[b][2][c]);
+            tkp2 = d2f(pf->tb[b][3][c]);
+          } else {
+            tk = d2f(T[(long)k * g.n2 + o]);
+            tkm1 = d2f(T[(long)km1 * g.n2 + o]);
+            tkp1 = d2f(T[(long)kp1 * g.n2 + o]);
+            tkp2 = d2f(T[(long)kp2 * g.n2 + o]);
+          }
           bool mkm1 = mb & 1, mk = mb & 2, mkp1 = mb & 4, mkp2 = mb & 8;
           float Rjp = (mkm1 && mk) ? tkm1 - tk : 0.f;
           float Rj = (mk && mkp1) ? tk - tkp1 : 0.f;
@@ -299,7 +355,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
         if (a.fused) {
           // T(taup1) = T + (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT
           float inc = s.uq[c] * tkr[m] + s.ur[c] * dT;
-          double tn = T[p] + f2d(inc);
+          double tn = (PF ? pf->tb[n & 1][1][c] : T[p]) + f2d(inc);
           double* o = a.out + (long)(n0 + n) * g.n3;
           o[p] = tn;
           // halo update of T(taup1) in cyclic directions (ocean_model.F90:1903-1911)

@@ -127,6 +127,38 @@ def test_mixed_multi_tile_and_partial_tiles(gpu_lib, case):
         assert err <= REL_TOL, (ni, nj, cx, cy, n, err)
 
 
+@pytest.mark.parametrize("case", [(False, False, 61, 45, 10), (True, True, 30, 29, 3), (True, False, 57, 30, 1)])
+def test_precision_form_launch_shapes_agree(gpu_lib, case):
+    """Every launch shape of the precision form (tile height 32, 16, 16 with the
+    tracer prefetch through cp.async) gives the same tracers bit for bit."""
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    cx, cy, ni, nj, ntr = case
+    sp = grid.DomainSpec(ni=ni, nj=nj, nk=7, lon0=0.0, lon1=float(ni), lat0=-20.0, lat1=20.0, cyclic_x=cx,
+                         cyclic_y=cy, continent=(10, 8, 5, 6), wavelength_cells=6.0, ntracers=ntr, seed=ni + 1)
+    dom = grid.make_domain(sp)
+    out = {}
+    for shape in ((32, 0, 0), (16, 0, 0), (16, 1, 0)):
+        d = harness.load(dom, options=capi.default_options(precision=capi.PRECISION_MIXED))
+        d.tuning = shape
+        assert d.tuning == shape
+        tau = 1
+        for _ in range(3):
+            d.tracer_advection_step(tau, tau, 3 - tau, 6 * 3600.0)
+            tau = 3 - tau
+        out[shape] = [d.get(capi.F.TRACER, n=n, level=tau) for n in range(1, ntr + 1)]
+        d.close()
+    for shape, T in out.items():
+        for n in range(ntr):
+            assert np.array_equal(T[n], out[(32, 0, 0)][n]), (shape, n)
+    with pytest.raises(capi.Mom5GpuError):
+        d = harness.load(dom, options=capi.default_options(precision=capi.PRECISION_MIXED))
+        try:
+            d.tuning = (32, 1, 0)
+        finally:
+            d.close()
+
+
 @pytest.mark.parametrize("stepping_B", [True, False])
 @pytest.mark.parametrize("cyclic_x", [True, False])
 def test_precision_form_barotropic_is_fp64_accurate(gpu_lib, oracle_lib, cyclic_x, stepping_B):
