@@ -52,6 +52,7 @@ extern "C" {
 #define MOM5GPU_ADVECT_4TH_ORDER 3
 #define MOM5GPU_ADVECT_6TH_ORDER 4
 #define MOM5GPU_ADVECT_QUICKER 5
+#define MOM5GPU_ADVECT_QUICKMOM3 6 /* horizontal only (the vertical routine is undefined at k = nk) */
 #define MOM5GPU_ADVECT_MDFL_SUP_B 7
 #define MOM5GPU_ADVECT_MDPPM 8
 #define MOM5GPU_ADVECT_MDFL_SWEBY 9

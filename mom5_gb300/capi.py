@@ -26,6 +26,7 @@ BGRID, CGRID = 1, 2
 ADVECT_UPWIND, ADVECT_QUICKER, ADVECT_MDFL_SWEBY, ADVECT_DST_LINEAR = 1, 5, 9, 10
 ADVECT_2ND_ORDER, ADVECT_4TH_ORDER, ADVECT_6TH_ORDER, ADVECT_MDFL_SUP_B, ADVECT_MDPPM = 2, 3, 4, 7, 8
 ADVECT_PSOM = 11
+ADVECT_QUICKMOM3 = 6
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 

@@ -407,9 +407,14 @@ int mom5gpu_set_tracer_scheme(mom5gpu_domain* d, int n, int horz, int vert, doub
            s == MOM5GPU_ADVECT_MDFL_SUP_B || s == MOM5GPU_ADVECT_MDFL_SWEBY || s == MOM5GPU_ADVECT_DST_LINEAR ||
            s == MOM5GPU_ADVECT_PSOM;
   };
-  if (!ok(horz) || !ok(vert))
+  if (vert == MOM5GPU_ADVECT_QUICKMOM3)
+    return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: vertical quickmom3 reads levels nk+1 and nk+2 at the "
+                                          "bottom level and, under tmask_limit, upos/uneg before it sets them "
+                                          "(ocean_tracer_advect.F90:3060-3150): its result is undefined there");
+  if (!(ok(horz) || horz == MOM5GPU_ADVECT_QUICKMOM3) || !ok(vert))
     return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: scheme %d/%d is outside upwind, 2nd/4th/6th order, "
-                                          "quicker, mdfl_sup_b, mdppm, mdfl_sweby, dst_linear, psom", horz, vert);
+                                          "quicker, quickmom3 (horizontal), mdfl_sup_b, mdppm, mdfl_sweby, "
+                                          "dst_linear, psom", horz, vert);
   // MDPPM reads a halo of 4: at least 4 compute points across a cyclic direction
   if (horz == MOM5GPU_ADVECT_MDPPM && ((d->geo.cx && d->geo.ni < 4) || (d->geo.cy && d->geo.nj < 4)))
     return fail(d, MOM5GPU_EUNSUPPORTED, "set_tracer_scheme: mdppm needs ni, nj >= 4 across cyclic edges");
@@ -724,6 +729,9 @@ int mom5gpu_horz_advect_tracer(mom5gpu_domain* d, int n, int taum1, int tau, dou
     case MOM5GPU_ADVECT_QUICKER:
       if (!d->qw.quick_x) return fail(d, MOM5GPU_ESTATE, "quicker needs mom5gpu_set_vertical_grid before init");
       return launch_quicker_horz(d, n, taum1, tau);
+    case MOM5GPU_ADVECT_QUICKMOM3:
+      if (!d->qw.quick_x) return fail(d, MOM5GPU_ESTATE, "quickmom3 needs mom5gpu_set_vertical_grid before init");
+      return launch_quickmom3_horz(d, n, taum1, tau);
     case MOM5GPU_ADVECT_MDFL_SWEBY:
       if (d->opt.precision == MOM5GPU_PRECISION_MIXED) return launch_mdfl_mixed(d, n, 1, taum1, tau, 0, dtime, false);
       return launch_mdfl(d, false, n, 1, taum1, tau, dtime, 1.0);

@@ -234,6 +234,7 @@ int ensure_kmt_device(mom5gpu_domain* d);
 int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
 int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
 int launch_psom(mom5gpu_domain* d, int n, int taum1, double dtime);
+int launch_quickmom3_horz(mom5gpu_domain* d, int n, int taum1, int tau);
 int launch_tracer_boundary(mom5gpu_domain* d, int n);
 int launch_barotropic_forcing(mom5gpu_domain* d);
 int launch_advection_velocity(mom5gpu_domain* d, int tau);

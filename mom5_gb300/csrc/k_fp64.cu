@@ -438,6 +438,59 @@ __global__ void k_quicker_vert(QukArgs a) {
   vert_segment(a.g, a.tmask, a.th, [&](int i, int j, int k) { return quk_fz(a, i, j, k); });
 }
 
+// QuickMOM3, horizontal (:2665-2780): the Quicker weights with mask products in
+// place of the coast masks and the northern second neighbour clamped to nj
+DEVI double qm3_fx(const QukArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  long q = I2(g, i, j);
+  long n2 = g.n2;
+  if (a.limit_with_upwind && a.tmask_limit[I3(g, i, j, k)] == 1.0) {
+    double vel = a.uh[I3(g, i, j, k)];
+    double upos = 0.5 * (vel + fabs(vel));
+    double uneg = 0.5 * (vel - fabs(vel));
+    double f = a.dyte[q] * (upos * a.Tm1[I3(g, i, j, k)] + uneg * a.Tm1[I3(g, i + 1, j, k)]);
+    return f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i + 1, j, k)];
+  }
+  auto mq = [&](int ii) { return a.mask2[IM(g, ii, j, k)] ? 1.0 : 0.0; };
+  double vel = a.dyte[q] * a.uh[I3(g, i, j, k)];
+  double upos = 0.5 * (vel + fabs(vel)) * mq(i - 1) * mq(i) * mq(i + 1);
+  double uneg = 0.5 * (vel - fabs(vel)) * mq(i + 2) * mq(i + 1) * mq(i);
+  double tqm = tq(g, a.Tm1, i - 1, j, k), tq0 = tq(g, a.Tm1, i, j, k);
+  double tq1 = tq(g, a.Tm1, i + 1, j, k), tq2 = tq(g, a.Tm1, i + 2, j, k);
+  return vel * (a.q.quick_x[q] * a.T0[I3(g, i, j, k)] + a.q.quick_x[n2 + q] * a.T0[I3(g, i + 1, j, k)]) -
+         upos * (a.q.curv_xp[q] * tq1 + a.q.curv_xp[n2 + q] * tq0 + a.q.curv_xp[2 * n2 + q] * tqm) -
+         uneg * (a.q.curv_xn[q] * tq2 + a.q.curv_xn[n2 + q] * tq1 + a.q.curv_xn[2 * n2 + q] * tq0);
+}
+
+DEVI double qm3_fy(const QukArgs& a, int i, int j, int k) {
+  const Geo& g = a.g;
+  long q = I2(g, i, j);
+  long n2 = g.n2;
+  if (a.limit_with_upwind && a.tmask_limit[I3(g, i, j, k)] == 1.0) {
+    double vel = a.vh[I3(g, i, j, k)];
+    double upos = 0.5 * (vel + fabs(vel));
+    double uneg = 0.5 * (vel - fabs(vel));
+    double f = a.dxtn[q] * (upos * a.Tm1[I3(g, i, j, k)] + uneg * a.Tm1[I3(g, i, j + 1, k)]);
+    return f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i, j + 1, k)];
+  }
+  const int jp2 = j + 2 < g.nj ? j + 2 : g.nj;  // min(j+2, jec)
+  auto mq = [&](int jj) { return a.mask2[IM(g, i, jj, k)] ? 1.0 : 0.0; };
+  double vel = a.dxtn[q] * a.vh[I3(g, i, j, k)];
+  double upos = 0.5 * (vel + fabs(vel)) * mq(j - 1) * mq(j) * mq(j + 1);
+  double uneg = 0.5 * (vel - fabs(vel)) * mq(jp2) * mq(j + 1) * mq(j);
+  double tqm = tq(g, a.Tm1, i, j - 1, k), tq0 = tq(g, a.Tm1, i, j, k);
+  double tq1 = tq(g, a.Tm1, i, j + 1, k), tq2 = tq(g, a.Tm1, i, jp2, k);
+  return vel * (a.q.quick_y[q] * a.T0[I3(g, i, j, k)] + a.q.quick_y[n2 + q] * a.T0[I3(g, i, j + 1, k)]) -
+         upos * (a.q.curv_yp[q] * tq1 + a.q.curv_yp[n2 + q] * tq0 + a.q.curv_yp[2 * n2 + q] * tqm) -
+         uneg * (a.q.curv_yn[q] * tq2 + a.q.curv_yn[n2 + q] * tq1 + a.q.curv_yn[2 * n2 + q] * tq0);
+}
+
+__global__ void __launch_bounds__(HB) k_quickmom3_horz(QukArgs a) {
+  horz_faces_once(
+      a.g, a.tmask, a.datr, a.th, [&](int i, int j, int k) { return qm3_fx(a, i, j, k); },
+      [&](int i, int j, int k) { return qm3_fy(a, i, j, k); });
+}
+
 static int quk_args(mom5gpu_domain* d, int n, int taum1, int tau, QukArgs* a) {
   a->g = d->geo;
   a->limit_with_upwind = d->opt.limit_with_upwind;
@@ -470,6 +523,17 @@ int launch_quicker_horz(mom5gpu_domain* d, int n, int taum1, int tau) {
   k_quicker_horz<<<horz_grid(g), HB, 0, d->stream>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "quicker horz");
+}
+
+int launch_quickmom3_horz(mom5gpu_domain* d, int n, int taum1, int tau) {
+  QukArgs a;
+  int rc = quk_args(d, n, taum1, tau, &a);
+  if (rc) return rc;
+  ClockScope clk(d, SEC_QUICKER);
+  count_launches(d, 1);
+  k_quickmom3_horz<<<horz_grid(d->geo), HB, 0, d->stream>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "quickmom3 horz");
 }
 
 int launch_quicker_vert(mom5gpu_domain* d, int n, int taum1, int tau) {

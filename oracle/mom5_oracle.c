@@ -1124,6 +1124,92 @@ void orc_quicker_init(const orc_dims* d, const double* dxt, const double* dyt, c
   free(dyq);
 }
 
+/* horz_advect_tracer_quickmom3 (ocean_tracer_advect.F90:2665-2780): the Quicker
+ * weights with the upwind-biased terms switched off by mask products instead of
+ * the coast masks, and the northern second neighbour clamped to jec (jp2 =
+ * min(j+2, jec), :2703-2705) for a single-PE domain. */
+void orc_horz_advect_quickmom3(const orc_dims* d, int limit_with_upwind, const orc_quicker* q, const double* tmask,
+                               const double* tmask_limit, const double* dyte, const double* dxtn, const double* datr,
+                               const double* uhrho_et, const double* vhrho_nt, const double* T_taum1,
+                               const double* T_tau, double* wrk1) {
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  size_t nh = (size_t)NX2(d) * NY2(d) * nk;
+  double* tq = (double*)calloc(nh, sizeof(double));
+  double* fx = (double*)calloc(n2 * nk, sizeof(double));
+  double* fy = (double*)calloc(n2 * nk, sizeof(double));
+  const double* tmq = q->tmask_quick;
+  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  for (int k = 0; k < nk; ++k)
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) tq[H3(d, i, j, k)] = T_taum1[I3(d, i, j, k)];
+  halo2_update(d, tq, 3);
+#define TQ(i, j, k) tq[H3(d, (i), (j), (k))]
+#define MQ(i, j, k) tmq[H3(d, (i), (j), (k))]
+  for (int k = 0; k < nk; ++k) {
+    for (int j = 0; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        int jp2 = j + 2 < nj ? j + 2 : nj;
+        double vel = dxtn[I2(d, i, j)] * vhrho_nt[I3(d, i, j, k)];
+        double upos = 0.5 * (vel + fabs(vel)) * MQ(i, j - 1, k) * MQ(i, j, k) * MQ(i, j + 1, k);
+        double uneg = 0.5 * (vel - fabs(vel)) * MQ(i, jp2, k) * MQ(i, j + 1, k) * MQ(i, j, k);
+        fy[I3(d, i, j, k)] =
+            vel * (W2(q->quick_y, i, j, 0) * T_tau[I3(d, i, j, k)] + W2(q->quick_y, i, j, 1) * T_tau[I3(d, i, j + 1, k)]) -
+            upos * (W2(q->curv_yp, i, j, 0) * TQ(i, j + 1, k) + W2(q->curv_yp, i, j, 1) * TQ(i, j, k) +
+                    W2(q->curv_yp, i, j, 2) * TQ(i, j - 1, k)) -
+            uneg * (W2(q->curv_yn, i, j, 0) * TQ(i, jp2, k) + W2(q->curv_yn, i, j, 1) * TQ(i, j + 1, k) +
+                    W2(q->curv_yn, i, j, 2) * TQ(i, j, k));
+      }
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 0; i <= ni; ++i) {
+        double vel = dyte[I2(d, i, j)] * uhrho_et[I3(d, i, j, k)];
+        double upos = 0.5 * (vel + fabs(vel)) * MQ(i - 1, j, k) * MQ(i, j, k) * MQ(i + 1, j, k);
+        double uneg = 0.5 * (vel - fabs(vel)) * MQ(i + 2, j, k) * MQ(i + 1, j, k) * MQ(i, j, k);
+        fx[I3(d, i, j, k)] =
+            vel * (W2(q->quick_x, i, j, 0) * T_tau[I3(d, i, j, k)] + W2(q->quick_x, i, j, 1) * T_tau[I3(d, i + 1, j, k)]) -
+            upos * (W2(q->curv_xp, i, j, 0) * TQ(i + 1, j, k) + W2(q->curv_xp, i, j, 1) * TQ(i, j, k) +
+                    W2(q->curv_xp, i, j, 2) * TQ(i - 1, j, k)) -
+            uneg * (W2(q->curv_xn, i, j, 0) * TQ(i + 2, j, k) + W2(q->curv_xn, i, j, 1) * TQ(i + 1, j, k) +
+                    W2(q->curv_xn, i, j, 2) * TQ(i, j, k));
+      }
+    if (limit_with_upwind) {
+      for (int j = 1; j <= nj; ++j)
+        for (int i = 0; i <= ni; ++i)
+          if (tmask_limit[I3(d, i, j, k)] == 1.0) {
+            double vel = uhrho_et[I3(d, i, j, k)];
+            double upos = 0.5 * (vel + fabs(vel));
+            double uneg = 0.5 * (vel - fabs(vel));
+            fx[I3(d, i, j, k)] = dyte[I2(d, i, j)] *
+                                 (upos * T_taum1[I3(d, i, j, k)] + uneg * T_taum1[I3(d, i + 1, j, k)]) *
+                                 tmask[I3(d, i, j, k)] * tmask[I3(d, i + 1, j, k)];
+          }
+      for (int j = 0; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i)
+          if (tmask_limit[I3(d, i, j, k)] == 1.0) {
+            double vel = vhrho_nt[I3(d, i, j, k)];
+            double upos = 0.5 * (vel + fabs(vel));
+            double uneg = 0.5 * (vel - fabs(vel));
+            fy[I3(d, i, j, k)] = dxtn[I2(d, i, j)] *
+                                 (upos * T_taum1[I3(d, i, j, k)] + uneg * T_taum1[I3(d, i, j + 1, k)]) *
+                                 tmask[I3(d, i, j, k)] * tmask[I3(d, i, j + 1, k)];
+          }
+    }
+  }
+#undef TQ
+#undef MQ
+  for (int k = 0; k < nk; ++k)
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) {
+        double r = tmask[I3(d, i, j, k)] *
+                   (fx[I3(d, i, j, k)] - fx[I3(d, i - 1, j, k)] + fy[I3(d, i, j, k)] - fy[I3(d, i, j - 1, k)]) *
+                   datr[I2(d, i, j)];
+        wrk1[I3(d, i, j, k)] = -r;
+      }
+  free(tq);
+  free(fx);
+  free(fy);
+}
+
 void orc_horz_advect_quicker(const orc_dims* d, int limit_with_upwind, const orc_quicker* q, const double* tmask,
                              const double* tmask_limit, const double* dyte, const double* dxtn, const double* datr,
                              const double* uhrho_et, const double* vhrho_nt, const double* T_taum1,

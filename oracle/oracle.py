@@ -169,6 +169,16 @@ def horz_advect_quicker(d, g, q, Tm1, T0, tmask_limit=None, limit_with_upwind=Fa
     return out
 
 
+def horz_advect_quickmom3(d, g, q, Tm1, T0, tmask_limit=None, limit_with_upwind=False):
+    """wrk1 = -horz_advect_tracer_quickmom3(...) (weights from quicker_init)."""
+    out = np.zeros_like(Tm1)
+    tl = tmask_limit if tmask_limit is not None else np.zeros_like(Tm1)
+    lib().orc_horz_advect_quickmom3(C.byref(d), int(limit_with_upwind), C.byref(q["_struct"]), p(g["tmask"]), p(tl),
+                                    p(g["dyte"]), p(g["dxtn"]), p(g["datr"]), p(g["uhrho_et"]), p(g["vhrho_nt"]),
+                                    p(Tm1), p(T0), p(out))
+    return out
+
+
 def vert_advect_quicker(d, g, q, Tm1, T0, tmask_limit=None):
     out = np.zeros_like(Tm1)
     tl = tmask_limit if tmask_limit is not None else np.zeros_like(Tm1)

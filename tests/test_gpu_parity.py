@@ -272,6 +272,43 @@ def test_quicker_matches(env, cyclic_x, limit_with_upwind):
         assert equal(got, ref), diff_report(got, ref)
 
 
+@pytest.mark.parametrize("limit_with_upwind", [0, 1])
+@pytest.mark.parametrize("cyclic_x,cyclic_y", [(False, False), (True, False), (True, True)])
+def test_quickmom3_matches(env, cyclic_x, cyclic_y, limit_with_upwind):
+    """Horizontal ADVECT_QUICKMOM3 (horz_advect_tracer_quickmom3, ocean_tracer_advect.F90:
+    2665-2780; the northern second neighbour clamped to jec) with vertical Quicker,
+    tmask_limit non-trivial; the vertical QuickMOM3 is refused (undefined at k = nk)."""
+    capi, O = env
+    sp = spec(cyclic_x=cyclic_x, cyclic_y=cyclic_y, ntr=2, seed=6)
+    opts = capi.default_options(limit_with_upwind=limit_with_upwind)
+    limits = [(2.0, 20.0), (34.6, 35.3)]
+    dom, d, g, dims = setup(env, sp, scheme=capi.ADVECT_QUICKER, options=opts, limits=limits)
+    for n, lim in zip((1, 2), limits):
+        d.set_tracer_scheme(n, capi.ADVECT_QUICKMOM3, capi.ADVECT_QUICKER, *lim)
+    with pytest.raises(capi.Mom5GpuError) as e:
+        d.set_tracer_scheme(1, capi.ADVECT_QUICKMOM3, capi.ADVECT_QUICKMOM3, *limits[0])
+    assert e.value.status == capi.EUNSUPPORTED
+    q = O.quicker_init(dims, g, dom.dzt.numpy())
+    d.compute_tmask_limit(1, 1, 2)
+    tl = [O.compute_tmask_limit(dims, g, g["T"][n].copy(), *limits[n]) for n in range(2)]
+    O.tmask_limit_ts_same(dims, tl[0], tl[1])
+    T0 = g["T"] * 1.01 + 0.003
+    for n in (1, 2):
+        d.set(capi.F.TRACER, np.ascontiguousarray(T0[n - 1]), n=n, level=2)
+    for n in (1, 2):
+        Tm1 = g["T"][n - 1].copy()
+        Tt = np.ascontiguousarray(T0[n - 1])
+        d.zero_th_tendency(n)
+        d.horz_advect_tracer(n, 1, 2, 3600.0)
+        got_h = d.get(capi.F.TH_TENDENCY, n=n)
+        ref_h = O.horz_advect_quickmom3(dims, g, q, Tm1, Tt, tl[n - 1], bool(limit_with_upwind))
+        assert equal(got_h, ref_h), diff_report(got_h, ref_h)
+        d.vert_advect_tracer(n, 1, 2, 3600.0)
+        got = d.get(capi.F.TH_TENDENCY, n=n)
+        ref = ref_h + O.vert_advect_quicker(dims, g, q, Tm1, Tt, tl[n - 1])
+        assert equal(got, ref), diff_report(got, ref)
+
+
 def _oracle_steps(O, dims, g, nsteps, dt, limiter=1.0):
     T = [g["T"][n].copy() for n in range(g["T"].shape[0])]
     for _ in range(nsteps):

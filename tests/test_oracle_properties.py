@@ -92,7 +92,7 @@ def test_step_terms_restatements(O):
 
 
 @pytest.mark.parametrize("scheme", ["mdfl", "dst", "all", "upwind", "quicker", "c2", "c4", "c6", "ppm1", "ppm2", "ppm3",
-                                    "supb", "psom", "psom_prather", "psom_nolimit"])
+                                    "supb", "psom", "psom_prather", "psom_nolimit", "qm3"])
 @pytest.mark.parametrize("cyclic_x", [False, True])
 def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
     """A uniform tracer in a non-divergent flow has zero advective tendency
@@ -113,6 +113,9 @@ def test_uniform_tracer_stays_uniform(O, scheme, cyclic_x):
         th = O.advect_mdfl_sup_b(d, g, U, 3600.0)
     elif scheme.startswith("psom"):
         th = psom_steps(O, d, g, U, 3600.0, scheme, 1)
+    elif scheme == "qm3":
+        q = O.quicker_init(d, g, dom.dzt.numpy())
+        th = O.horz_advect_quickmom3(d, g, q, U, U) + O.vert_advect_quicker(d, g, q, U, U)
     elif scheme.startswith("c"):
         order = int(scheme[1])
         th = O.horz_advect_centred(d, g, U, order) + O.vert_advect_centred(d, g, U, order, dom["kmt"].numpy())
@@ -136,7 +139,7 @@ def psom_steps(O, d, g, T, dtime, scheme, nsteps, moments=None):
 
 
 @pytest.mark.parametrize("scheme", ["mdfl", "upwind", "quicker", "c4", "ppm1", "ppm2", "ppm3", "supb", "psom",
-                                    "psom_prather"])
+                                    "psom_prather", "qm3"])
 def test_global_content_conserved(O, scheme):
     """sum(dat*rho_dzt*T*tmask) (ocean_tracer_diag.F90:2395-2412) is unchanged by
     advection plus the explicit update, to FP64 roundoff."""
@@ -158,6 +161,8 @@ def test_global_content_conserved(O, scheme):
             th = O.advect_mdfl_sup_b(d, g, T, 3600.0 * 6)
         elif scheme == "c4":
             th = O.horz_advect_centred(d, g, T, 4) + O.vert_advect_centred(d, g, T, 4, dom["kmt"].numpy())
+        elif scheme == "qm3":
+            th = O.horz_advect_quickmom3(d, g, q, T, T) + O.vert_advect_quicker(d, g, q, T, T)
         else:
             th = O.horz_advect_quicker(d, g, q, T, T) + O.vert_advect_quicker(d, g, q, T, T)
         T = O.update_tracer(d, g, T, th, 3600.0 * 6)
