@@ -687,6 +687,7 @@ def main():
     ap.add_argument("--config", choices=["c2", "c0", "c1", "c2s"], default="c2")
     ap.add_argument("--scheme", choices=[n for n, _ in SCHEMES], default="mdfl_sweby",
                     help="advection scheme of every tracer (the headline is mdfl_sweby)")
+    ap.add_argument("--metrics-jsonl", default=None, help="also append the figures to this JSON-lines file")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
@@ -724,6 +725,9 @@ def main():
     out = run_ours(args, rank, world)
     if rank == 0:
         print(json.dumps(out))
+        if args.metrics_jsonl:
+            from mom5_gb300 import metrics
+            metrics.from_bench_line(out, metrics.MetricsLog(args.metrics_jsonl))
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()

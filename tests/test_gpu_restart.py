@@ -147,3 +147,29 @@ def test_copy_field_async_on_caller_streams(gpu_lib):
     with pytest.raises(capi.Mom5GpuError):
         d.copy_field_async(F.TRACER, src.data_ptr(), 1, up.cuda_stream, n=9, level=1)
     d.close()
+
+
+def test_run_configuration_drives_a_domain(gpu_lib, tmp_path):
+    """A JSON run configuration (namelists and field_table choices) sets the
+    domain's options, schemes, limiters and restart names."""
+    capi = gpu_lib
+    from mom5_gb300 import config
+    doc = {"ocean_barotropic_nml": {"barotropic_time_stepping_B": True},
+           "tracers": [{"name": "temp", "horiz_advect_scheme": "quickMOM3", "vert_advect_scheme": "quicker",
+                        "restart_file": "ocean_temp_salt.res.nc"},
+                       {"name": "salt", "horiz_advect_scheme": "mdppm", "vert_advect_scheme": "mdppm",
+                        "ppm_hlimiter": 3, "restart_file": "ocean_temp_salt.res.nc"},
+                       {"name": "age", "horiz_advect_scheme": "psom", "vert_advect_scheme": "psom",
+                        "psom_limit": True}]}
+    cfg = config.parse(doc)
+    dom = grid.make_domain(_spec())
+    d = config.load_domain(dom, cfg)
+    d.barotropic_init(dtuv=DT, dtbt=60.0)
+    _step(d, 1, 0)
+    assert d.check_finite(0, 2)
+    d.write_restart(str(tmp_path), 2)
+    with netcdf(str(tmp_path / "ocean_temp_salt.res.nc"), "r", mmap=False) as f:
+        assert {"temp", "salt"} <= set(f.variables)
+    with netcdf(str(tmp_path / "ocean_psom_moments.res.nc"), "r", mmap=False) as f:
+        assert "age_prather_sxx" in f.variables
+    d.close()
