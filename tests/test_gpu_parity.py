@@ -272,6 +272,30 @@ def test_quicker_matches(env, cyclic_x, limit_with_upwind):
         assert equal(got, ref), diff_report(got, ref)
 
 
+@pytest.mark.parametrize("case", [(6, 5, 1, False, False), (2, 3, 2, True, True), (5, 4, 3, True, False),
+                                  (130, 7, 33, True, False)])
+def test_psom_small_and_odd_domains(env, case):
+    """PSOM on one-level columns, two-cell periodic rings, and a row longer than one
+    x segment with more levels than one z segment: every value equal after three calls."""
+    capi, O = env
+    ni, nj, nk, cx, cy = case
+    sp = spec(ni=ni, nj=nj, nk=nk, cyclic_x=cx, cyclic_y=cy, ntr=1, seed=ni * 7 + nk, continent=None)
+    dom, d, g, dims = setup(env, sp, scheme=capi.ADVECT_PSOM)
+    d.set_psom_limit(1, True)
+    mom = np.zeros((9,) + g["T"][0].shape)
+    for itt0 in range(3):
+        d.set_itt0(itt0)
+        d.zero_th_tendency(1)
+        d.horz_advect_tracer(1, 1, 1, 3600.0)
+        got = d.get(capi.F.TH_TENDENCY, n=1)
+        ref, _ = O.advect_psom(dims, g, g["T"][0].copy(), 3600.0, mom, itt0=itt0)
+        assert equal(got, ref), f"call {itt0}: {diff_report(got, ref)}"
+    inner = (slice(None), slice(1, -1), slice(1, -1))
+    for q in range(9):
+        got = d.get(capi.F.PSOM_SX + q, n=1).reshape(g["T"][0].shape)[inner]
+        assert equal(got, mom[q][inner]), q
+
+
 @pytest.mark.parametrize("limit_with_upwind", [0, 1])
 @pytest.mark.parametrize("cyclic_x,cyclic_y", [(False, False), (True, False), (True, True)])
 def test_quickmom3_matches(env, cyclic_x, cyclic_y, limit_with_upwind):
