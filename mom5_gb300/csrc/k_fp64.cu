@@ -694,13 +694,15 @@ DEVI double m2d(const SupbArgs& a, int i, int j, int k) { return a.mask2[IM(a.g,
 // face flux 0.5*(mf*(Ta+Tb) - |mf|*(1 + (cfl-1)*Cr)*Rj)*m0*m1 with the superbee limiter (:3244-3263)
 DEVI double supb_flux(double mf, double cfl, double Rjm, double Rj, double Rjp, double Ta, double Tb, double m0,
                       double m1) {
+  // the comparisons on the integer pipe (sel::), same selections as the FP ones
+  const bool pos = sel::gt0(mf);
   double Cr;
-  if (Rj != 0.0) Cr = mf > 0.0 ? Rjm / Rj : Rjp / Rj;
-  else Cr = mf > 0.0 ? Rjm * 1.0e20 : Rjp * 1.0e20;
+  if ((__double_as_longlong(Rj) << 1) != 0) Cr = (pos ? Rjm : Rjp) / Rj;
+  else Cr = (pos ? Rjm : Rjp) * 1.0e20;
   double c2 = 2.0 * Cr;
-  double lo = 1.0 < c2 ? 1.0 : c2, hi = 2.0 < Cr ? 2.0 : Cr;
-  double mx = lo > hi ? lo : hi;
-  Cr = 0.0 > mx ? 0.0 : mx;
+  double lo = sel::lt_min(1.0, c2), hi = sel::lt_min(2.0, Cr);
+  double mx = sel::gt_max(lo, hi);
+  Cr = sel::gt_max(0.0, mx);
   return 0.5 * (mf * (Ta + Tb) - fabs(mf) * (1.0 + (cfl - 1.0) * Cr) * Rj) * m0 * m1;
 }
 
@@ -888,13 +890,13 @@ __global__ void k_ppm_zflux(PpmArgs a) {
     double c6 = 6. * Si - 3. * (ar + al);
     double wk = a.w[I3(g, i, j, K)];
     double massflux = dat * wk * msk0 * mskp1;
-    if (massflux <= 0.0) {
+    if (!sel::gt0(massflux)) {
       double cfl = fabs(wk * a.dtime / at(a.rdz, K));
       a.fz[I3(g, i, j, K - 1)] = massflux * (ar + 0.5 * cfl * ((al - ar) + (1. - ppm::kTwoThirds * cfl) * c6));
     }
     double wkm1 = a.w[I3(g, i, j, km1)];
     massflux = dat * wkm1 * msk0 * mskm1;
-    if (massflux > 0.0) {
+    if (sel::gt0(massflux)) {
       double cfl = fabs(wkm1 * a.dtime / at(a.rdz, km1));
       a.fz[I3(g, i, j, km1 - 1)] = massflux * (al + 0.5 * cfl * ((ar - al) + (1. - ppm::kTwoThirds * cfl) * c6));
     }

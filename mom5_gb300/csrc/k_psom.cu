@@ -27,6 +27,7 @@
 // are per-domain scratch.
 #include <math.h>
 
+#include "fp64_select.cuh"
 #include "internal.h"
 
 namespace mom5 {
@@ -36,8 +37,9 @@ namespace psom {
 
 DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
 DEVI long I3(const Geo& g, int i, int j, int k) { return (long)k * g.n2 + (long)j * g.nxd + i; }
-DEVI double mx(double a, double b) { return a > b ? a : b; }
-DEVI double mn(double a, double b) { return a < b ? a : b; }
+// a > b ? a : b and a < b ? a : b, compared on the integer pipe
+DEVI double mx(double a, double b) { return sel::gt_max(a, b); }
+DEVI double mn(double a, double b) { return sel::lt_min(a, b); }
 
 constexpr double kEpsln = 1.0e-20;  // constants_mod epsln
 
@@ -87,7 +89,7 @@ DEVI double tq(const Geo& g, const double* T, int i, int j, int k) {
 // Prather's limiter (psom_x :4676-4692)
 DEVI void limit_prather(Cell& c) {
   double slpmax = 0.0;
-  if (c.s0 > 0.0) slpmax = c.s0;
+  if (sel::gt0(c.s0)) slpmax = c.s0;
   double s1max = 1.5 * slpmax;
   double s1new = mn(s1max, mx(-s1max, c.a));
   double s2new = mn(slpmax + slpmax - 0.3334 * fabs(s1new), mx(fabs(s1new) - slpmax, c.aa));
@@ -101,8 +103,8 @@ DEVI void limit_prather(Cell& c) {
 // (fc, mc) and its two neighbours along the direction (fm, mm), (fp, mp)
 DEVI void limit_mh(Cell& c, double fc, double mc, double fm, double mm, double fp, double mp) {
   double s0max1 = fc * mc;
-  if (mm > 0.) s0max1 = mx(fm, s0max1);
-  if (mp > 0.) s0max1 = mx(fp, s0max1);
+  if (sel::gt0(mm)) s0max1 = mx(fm, s0max1);
+  if (sel::gt0(mp)) s0max1 = mx(fp, s0max1);
   s0max1 = s0max1 * c.sm;
   double slpmax = -c.s0 + s0max1;
   double s1max = 1.5 * slpmax;
@@ -113,8 +115,8 @@ DEVI void limit_mh(Cell& c, double fc, double mc, double fm, double mm, double f
   c.a = -s1new;
   c.aa = -s2new;
   double s0min1 = fc * mc;
-  if (mm > 0.) s0min1 = mn(fm, s0min1);
-  if (mp > 0.) s0min1 = mn(fp, s0min1);
+  if (sel::gt0(mm)) s0min1 = mn(fm, s0min1);
+  if (sel::gt0(mp)) s0min1 = mn(fp, s0min1);
   s0min1 = s0min1 * c.sm;
   slpmax = c.s0 - s0min1;
   s1max = 1.5 * slpmax;
@@ -319,7 +321,7 @@ __global__ void __launch_bounds__(BI* L) k_psom_dir(Args a) {
   if (he) ln.face_vel(a, fec, ve, dve);
   double f[NF];
   // outflow sweep: low face first, then high face
-  if (hw && vw < 0.0) {
+  if (hw && sel::lt0(vw)) {
     if (valid) out_op(c, vw, dvw, a.dtime, false, f);
     else
       for (int q = 0; q < NF; ++q) f[q] = 0.0;
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(BI* L) k_psom_dir(Args a) {
     if (sl >= 0 && sl <= L - 2)
       for (int q = 0; q < NF; ++q) slot[q][sl][lane] = f[q];
   }
-  if (he && ve >= 0.0) {
+  if (he && sel::ge0(ve)) {
     if (valid) out_op(c, ve, dve, a.dtime, true, f);
     else
       for (int q = 0; q < NF; ++q) f[q] = 0.0;  // halo cell of a closed edge: nothing in transit
@@ -338,11 +340,11 @@ __global__ void __launch_bounds__(BI* L) k_psom_dir(Args a) {
   __syncthreads();
   if (!valid || t < 1 || t > L - 2 || s < 1 || s > ln.N) return;
   // inflow sweep: low face first, then high face
-  if (hw && vw >= 0.0) {
+  if (hw && sel::ge0(vw)) {
     for (int q = 0; q < NF; ++q) f[q] = slot[q][t - 1][lane];
     in_op(c, true, f);
   }
-  if (he && ve < 0.0) {
+  if (he && sel::lt0(ve)) {
     for (int q = 0; q < NF; ++q) f[q] = slot[q][t][lane];
     in_op(c, false, f);
   }
@@ -355,11 +357,11 @@ __global__ void __launch_bounds__(BI* L) k_psom_dir(Args a) {
   double* flux = DIR == 1 ? a.fx : DIR == 2 ? a.fy : a.fz;
   if (he) {
     double f0 = slot[F0][t][lane];
-    flux[ln.flux_index(s)] = ve >= 0.0 ? f0 * a.dtimer : -f0 * a.dtimer;
+    flux[ln.flux_index(s)] = sel::ge0(ve) ? f0 * a.dtimer : -f0 * a.dtimer;
   }
   if (DIR != 3 && s == 1 && hw) {
     double f0 = slot[F0][t - 1][lane];
-    flux[ln.flux_index(0)] = vw >= 0.0 ? f0 * a.dtimer : -f0 * a.dtimer;
+    flux[ln.flux_index(0)] = sel::ge0(vw) ? f0 * a.dtimer : -f0 * a.dtimer;
   }
 }
 

@@ -14,6 +14,7 @@
 // tmask_mdppm hold them (mdppm_init :1702-1735).
 #pragma once
 
+#include "fp64_select.cuh"
 #include "internal.h"
 
 namespace mom5 {
@@ -23,8 +24,9 @@ namespace ppm {
 
 constexpr double kR12 = 1.0 / 12.0, kSixth = 1.0 / 6.0, kTwoThirds = 2.0 / 3.0, kFourThirds = 4.0 / 3.0;
 
-DEVI double mx(double a, double b) { return a > b ? a : b; }
-DEVI double mn(double a, double b) { return a < b ? a : b; }
+// a > b ? a : b and a < b ? a : b, compared on the integer pipe
+DEVI double mx(double a, double b) { return sel::gt_max(a, b); }
+DEVI double mn(double a, double b) { return sel::lt_min(a, b); }
 
 // slope of the centre cell of S[0..4] (offsets -2..+2) and its one-sided differences
 DEVI void slope(const double* S, const double* M, double& da, double& d1m, double& d1p, double& d1mm, double& d1pp) {
@@ -47,14 +49,14 @@ DEVI void slope(const double* S, const double* M, double& da, double& d1m, doubl
 DEVI void limit(int lim, double Si, double da, double d1m, double d1p, double d1mm, double d1pp, double& aL,
                 double& aR) {
   if (lim == 1) {
-    if ((aR - Si) * (Si - aL) <= 0.) {
+    if (!sel::gt0((aR - Si) * (Si - aL))) {
       aL = Si;
       aR = Si;
     }
     double da2 = aR - aL, da4 = 0.5 * (aR + aL);
     double da3m = 6. * da2 * (Si - da4), da3p = da2 * da2;
-    if (da3m > da3p) aL = 3. * Si - 2. * aR;
-    if (da3m < -da3p) aR = 3. * Si - 2. * aL;
+    if (sel::ord0(da3m) > sel::ord0(da3p)) aL = 3. * Si - 2. * aR;
+    if (sel::ord0(da3m) < sel::ord0(-da3p)) aR = 3. * Si - 2. * aL;
   } else if (lim == 2) {
     double ada = fabs(da), sda = copysign(1., da);
     aL = Si - sda * mn(ada, fabs(aL - Si));
@@ -77,7 +79,7 @@ DEVI void limit(int lim, double Si, double da, double d1m, double d1p, double d1
     double qMD = qAV - 0.5 * dM4p;
     double qMin = mx(mn(mn(qMD, Si), Sip1), mn(mn(Si, qUL), qLC));
     double qMax = mn(mx(mx(qMD, Si), Sip1), mx(mx(Si, qUL), qLC));
-    if ((aR - Si) * (aR - qMP) > 1.e-10) aR = mn(mx(aR, qMin), qMax);
+    if (sel::ord0((aR - Si) * (aR - qMP)) > sel::ord0(1.e-10)) aR = mn(mx(aR, qMin), qMax);
     qAV = 0.5 * (Si + Sim1);
     x = -d1m;
     y = -3. * d1p;
@@ -87,7 +89,7 @@ DEVI void limit(int lim, double Si, double da, double d1m, double d1p, double d1
     qMD = qAV - 0.5 * dM4m;
     qMin = mx(mn(mn(qMD, Si), Sim1), mn(mn(Si, qUL), qLC));
     qMax = mn(mx(mx(qMD, Si), Sim1), mx(mx(Si, qUL), qLC));
-    if ((aL - Si) * (aL - qMP) > 1.e-10) aL = mn(mx(aL, qMin), qMax);
+    if (sel::ord0((aL - Si) * (aL - qMP)) > sel::ord0(1.e-10)) aL = mn(mx(aL, qMin), qMax);
   }
 }
 
@@ -96,7 +98,7 @@ DEVI void limit(int lim, double Si, double da, double d1m, double d1p, double d1
 // :6470-6482); the masks multiply in the reference's order
 DEVI double hflux(double massflux, double m0, double m1, double cfl, double aL0, double aR0, double a60, double aL1,
                   double aR1, double a61) {
-  if (massflux >= 0.0)
+  if (sel::ge0(massflux))
     return massflux * m0 * m1 * (aR0 + 0.5 * cfl * ((aL0 - aR0) + (1. - kTwoThirds * cfl) * a60));
   return massflux * m0 * m1 * (aL1 - 0.5 * cfl * ((aR1 - aL1) + (1. + kTwoThirds * cfl) * a61));
 }
