@@ -210,7 +210,7 @@ DEVI void horz_faces_once(const Geo& g, const double* tmask, const double* datr,
     if (cell) {
       double fn = fy(i, j, k);
       long p = I3(g, i, j, k);
-      double rr = tmask[p] * (sfx[t + 1] - sfx[t] + fn - fs) * datr[I2(g, i, j)];
+      double rr = mask_mul(sfx[t + 1] - sfx[t] + fn - fs, tmask[p]) * datr[I2(g, i, j)];
       th[p] = th[p] + (-rr);
       fs = fn;
     }
@@ -226,7 +226,7 @@ DEVI void vert_segment(const Geo& g, const double* tmask, double* th, FZ fz) {
   for (int k = k0; k < k1; ++k) {
     double ft2 = fz(i, j, k);
     long p = I3(g, i, j, k);
-    double r = tmask[p] * (ft1 - ft2);
+    double r = mask_mul(ft1 - ft2, tmask[p]);
     th[p] = th[p] + (-r);
     ft1 = ft2;
   }
@@ -241,25 +241,25 @@ struct UpwArgs {
   double* th;
 };
 
+// 0.5*u, the mask tests and the products by a mask of 1.0 run on the integer pipe
+// (exact: the same values as the FP64 operations).
 DEVI double upw_fe(const UpwArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
-  double velocity = 0.5 * a.uh[I3(g, i, j, k)];
+  double velocity = half_exact(a.uh[I3(g, i, j, k)]);
   double upos = velocity + fabs(velocity);
   double uneg = velocity - fabs(velocity);
   double f = a.dyte[I2(g, i, j)] * (upos * a.T[I3(g, i, j, k)] + uneg * a.T[I3(g, i + 1, j, k)]);
-  return (a.tmask[I3(g, i, j, k)] != 0.0 && a.tmask[I3(g, i + 1, j, k)] != 0.0)
-             ? f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i + 1, j, k)]
-             : 0.0;
+  double m0 = a.tmask[I3(g, i, j, k)], m1 = a.tmask[I3(g, i + 1, j, k)];
+  return (!is_zero(m0) && !is_zero(m1)) ? mask_mul(mask_mul(f, m0), m1) : 0.0;
 }
 DEVI double upw_fn(const UpwArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
-  double velocity = 0.5 * a.vh[I3(g, i, j, k)];
+  double velocity = half_exact(a.vh[I3(g, i, j, k)]);
   double upos = velocity + fabs(velocity);
   double uneg = velocity - fabs(velocity);
   double f = a.dxtn[I2(g, i, j)] * (upos * a.T[I3(g, i, j, k)] + uneg * a.T[I3(g, i, j + 1, k)]);
-  return (a.tmask[I3(g, i, j, k)] != 0.0 && a.tmask[I3(g, i, j + 1, k)] != 0.0)
-             ? f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i, j + 1, k)]
-             : 0.0;
+  double m0 = a.tmask[I3(g, i, j, k)], m1 = a.tmask[I3(g, i, j + 1, k)];
+  return (!is_zero(m0) && !is_zero(m1)) ? mask_mul(mask_mul(f, m0), m1) : 0.0;
 }
 
 __global__ void __launch_bounds__(HB) k_upwind_horz(UpwArgs a) {
@@ -273,11 +273,11 @@ DEVI double upw_fz(const UpwArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
   long p = I3(g, i, j, k), pp = I3(g, i, j, kp1);
-  double velocity = 0.5 * a.w[I3(g, i, j, k + 1)];
+  double velocity = half_exact(a.w[I3(g, i, j, k + 1)]);
   double wpos = velocity + fabs(velocity);
   double wneg = velocity - fabs(velocity);
   double ft2 = (wneg * a.T[p] + wpos * a.T[pp]);
-  return (a.tmask[p] != 0.0 && a.tmask[pp] != 0.0) ? ft2 * a.tmask[p] * a.tmask[pp] : 0.0;
+  return (!is_zero(a.tmask[p]) && !is_zero(a.tmask[pp])) ? mask_mul(mask_mul(ft2, a.tmask[p]), a.tmask[pp]) : 0.0;
 }
 
 __global__ void k_upwind_vert(UpwArgs a) {
@@ -358,16 +358,16 @@ DEVI double quk_fx(const QukArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   long q = I2(g, i, j);
   long n2 = g.n2;
-  if (a.limit_with_upwind && a.tmask_limit[I3(g, i, j, k)] == 1.0) {
+  if (a.limit_with_upwind && is_one(a.tmask_limit[I3(g, i, j, k)])) {
     double vel = a.uh[I3(g, i, j, k)];
-    double upos = 0.5 * (vel + fabs(vel));
-    double uneg = 0.5 * (vel - fabs(vel));
+    double upos = half_exact(vel + fabs(vel));
+    double uneg = half_exact(vel - fabs(vel));
     double f = a.dyte[q] * (upos * a.Tm1[I3(g, i, j, k)] + uneg * a.Tm1[I3(g, i + 1, j, k)]);
-    return f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i + 1, j, k)];
+    return mask_mul(mask_mul(f, a.tmask[I3(g, i, j, k)]), a.tmask[I3(g, i + 1, j, k)]);
   }
   double vel = a.dyte[q] * a.uh[I3(g, i, j, k)];
-  double upos = 0.5 * (vel + fabs(vel));
-  double uneg = 0.5 * (vel - fabs(vel));
+  double upos = half_exact(vel + fabs(vel));
+  double uneg = half_exact(vel - fabs(vel));
   bool mm = a.mask2[IM(g, i - 1, j, k)], m0 = a.mask2[IM(g, i, j, k)];
   bool m1 = a.mask2[IM(g, i + 1, j, k)], m2 = a.mask2[IM(g, i + 2, j, k)];
   bool eastmsk = m0 && !mm;
@@ -383,16 +383,16 @@ DEVI double quk_fy(const QukArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   long q = I2(g, i, j);
   long n2 = g.n2;
-  if (a.limit_with_upwind && a.tmask_limit[I3(g, i, j, k)] == 1.0) {
+  if (a.limit_with_upwind && is_one(a.tmask_limit[I3(g, i, j, k)])) {
     double vel = a.vh[I3(g, i, j, k)];
-    double upos = 0.5 * (vel + fabs(vel));
-    double uneg = 0.5 * (vel - fabs(vel));
+    double upos = half_exact(vel + fabs(vel));
+    double uneg = half_exact(vel - fabs(vel));
     double f = a.dxtn[q] * (upos * a.Tm1[I3(g, i, j, k)] + uneg * a.Tm1[I3(g, i, j + 1, k)]);
-    return f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i, j + 1, k)];
+    return mask_mul(mask_mul(f, a.tmask[I3(g, i, j, k)]), a.tmask[I3(g, i, j + 1, k)]);
   }
   double vel = a.dxtn[q] * a.vh[I3(g, i, j, k)];
-  double upos = 0.5 * (vel + fabs(vel));
-  double uneg = 0.5 * (vel - fabs(vel));
+  double upos = half_exact(vel + fabs(vel));
+  double uneg = half_exact(vel - fabs(vel));
   bool mm = a.mask2[IM(g, i, j - 1, k)], m0 = a.mask2[IM(g, i, j, k)];
   bool m1 = a.mask2[IM(g, i, j + 1, k)], m2 = a.mask2[IM(g, i, j + 2, k)];
   bool rnormsk = m0 && !mm;
@@ -419,14 +419,14 @@ DEVI double quk_fz(const QukArgs& a, int i, int j, int k) {
   int p2 = k + 2 < nk ? k + 2 : nk - 1;
   long p = I3(g, i, j, k);
   double vel = a.w[I3(g, i, j, k + 1)];
-  double upos = 0.5 * (vel + fabs(vel));
-  double uneg = 0.5 * (vel - fabs(vel));
+  double upos = half_exact(vel + fabs(vel));
+  double uneg = half_exact(vel - fabs(vel));
   const double* Tm = a.Tm1;
-  if (a.tmask_limit[p] == 1.0)
-    return (uneg * Tm[p] + upos * Tm[I3(g, i, j, kp1)]) * a.tmask[p] * a.tmask[I3(g, i, j, kp1)];
+  if (is_one(a.tmask_limit[p]))
+    return mask_mul(mask_mul(uneg * Tm[p] + upos * Tm[I3(g, i, j, kp1)], a.tmask[p]), a.tmask[I3(g, i, j, kp1)]);
   // kp2 = nint(tmask(p2)*p2 + (1-tmask(p2))*kp1): p2 when level p2 is wet, else kp1
-  int kp2 = a.tmask[I3(g, i, j, p2)] != 0.0 ? p2 : kp1;
-  bool upmsk = a.tmask[p] != 0.0 && a.tmask[I3(g, i, j, km1)] == 0.0;
+  int kp2 = !is_zero(a.tmask[I3(g, i, j, p2)]) ? p2 : kp1;
+  bool upmsk = !is_zero(a.tmask[p]) && is_zero(a.tmask[I3(g, i, j, km1)]);
   return vel * (a.q.quick_z[k] * a.T0[p] + a.q.quick_z[nk + k] * a.T0[I3(g, i, j, kp1)]) -
          uneg * (a.q.curv_zp[k] * Tm[I3(g, i, j, kp1)] + a.q.curv_zp[nk + k] * Tm[p] +
                  a.q.curv_zp[2 * nk + k] * Tm[I3(g, i, j, km1)]) -
@@ -444,17 +444,17 @@ DEVI double qm3_fx(const QukArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   long q = I2(g, i, j);
   long n2 = g.n2;
-  if (a.limit_with_upwind && a.tmask_limit[I3(g, i, j, k)] == 1.0) {
+  if (a.limit_with_upwind && is_one(a.tmask_limit[I3(g, i, j, k)])) {
     double vel = a.uh[I3(g, i, j, k)];
-    double upos = 0.5 * (vel + fabs(vel));
-    double uneg = 0.5 * (vel - fabs(vel));
+    double upos = half_exact(vel + fabs(vel));
+    double uneg = half_exact(vel - fabs(vel));
     double f = a.dyte[q] * (upos * a.Tm1[I3(g, i, j, k)] + uneg * a.Tm1[I3(g, i + 1, j, k)]);
-    return f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i + 1, j, k)];
+    return mask_mul(mask_mul(f, a.tmask[I3(g, i, j, k)]), a.tmask[I3(g, i + 1, j, k)]);
   }
   auto mq = [&](int ii) { return a.mask2[IM(g, ii, j, k)] ? 1.0 : 0.0; };
   double vel = a.dyte[q] * a.uh[I3(g, i, j, k)];
-  double upos = 0.5 * (vel + fabs(vel)) * mq(i - 1) * mq(i) * mq(i + 1);
-  double uneg = 0.5 * (vel - fabs(vel)) * mq(i + 2) * mq(i + 1) * mq(i);
+  double upos = mask_mul(mask_mul(mask_mul(half_exact(vel + fabs(vel)), mq(i - 1)), mq(i)), mq(i + 1));
+  double uneg = mask_mul(mask_mul(mask_mul(half_exact(vel - fabs(vel)), mq(i + 2)), mq(i + 1)), mq(i));
   double tqm = tq(g, a.Tm1, i - 1, j, k), tq0 = tq(g, a.Tm1, i, j, k);
   double tq1 = tq(g, a.Tm1, i + 1, j, k), tq2 = tq(g, a.Tm1, i + 2, j, k);
   return vel * (a.q.quick_x[q] * a.T0[I3(g, i, j, k)] + a.q.quick_x[n2 + q] * a.T0[I3(g, i + 1, j, k)]) -
@@ -466,18 +466,18 @@ DEVI double qm3_fy(const QukArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   long q = I2(g, i, j);
   long n2 = g.n2;
-  if (a.limit_with_upwind && a.tmask_limit[I3(g, i, j, k)] == 1.0) {
+  if (a.limit_with_upwind && is_one(a.tmask_limit[I3(g, i, j, k)])) {
     double vel = a.vh[I3(g, i, j, k)];
-    double upos = 0.5 * (vel + fabs(vel));
-    double uneg = 0.5 * (vel - fabs(vel));
+    double upos = half_exact(vel + fabs(vel));
+    double uneg = half_exact(vel - fabs(vel));
     double f = a.dxtn[q] * (upos * a.Tm1[I3(g, i, j, k)] + uneg * a.Tm1[I3(g, i, j + 1, k)]);
-    return f * a.tmask[I3(g, i, j, k)] * a.tmask[I3(g, i, j + 1, k)];
+    return mask_mul(mask_mul(f, a.tmask[I3(g, i, j, k)]), a.tmask[I3(g, i, j + 1, k)]);
   }
   const int jp2 = j + 2 < g.nj ? j + 2 : g.nj;  // min(j+2, jec)
   auto mq = [&](int jj) { return a.mask2[IM(g, i, jj, k)] ? 1.0 : 0.0; };
   double vel = a.dxtn[q] * a.vh[I3(g, i, j, k)];
-  double upos = 0.5 * (vel + fabs(vel)) * mq(j - 1) * mq(j) * mq(j + 1);
-  double uneg = 0.5 * (vel - fabs(vel)) * mq(jp2) * mq(j + 1) * mq(j);
+  double upos = mask_mul(mask_mul(mask_mul(half_exact(vel + fabs(vel)), mq(j - 1)), mq(j)), mq(j + 1));
+  double uneg = mask_mul(mask_mul(mask_mul(half_exact(vel - fabs(vel)), mq(jp2)), mq(j + 1)), mq(j));
   double tqm = tq(g, a.Tm1, i, j - 1, k), tq0 = tq(g, a.Tm1, i, j, k);
   double tq1 = tq(g, a.Tm1, i, j + 1, k), tq2 = tq(g, a.Tm1, i, jp2, k);
   return vel * (a.q.quick_y[q] * a.T0[I3(g, i, j, k)] + a.q.quick_y[n2 + q] * a.T0[I3(g, i, j + 1, k)]) -
@@ -568,13 +568,13 @@ template <int ORDER>
 DEVI double cen_fx(const CenArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   double du = a.dyte[I2(g, i, j)] * a.uh[I3(g, i, j, k)];
-  if (ORDER == 2) return du * 0.5 * (a.T[I3(g, i + 1, j, k)] + a.T[I3(g, i, j, k)]);
-  auto TM = [&](int ii) { return tq(g, a.tmask, ii, j, k); };
+  if (ORDER == 2) return half_exact(du) * (a.T[I3(g, i + 1, j, k)] + a.T[I3(g, i, j, k)]);
+  // the masks are 0.0 or 1.0: products, == 0 tests and the index selections exactly as integers
+  auto TM = [&](int ii) { return !is_zero(tq(g, a.tmask, ii, j, k)); };
   auto TT = [&](int ii) { return tq(g, a.T, ii, j, k); };
-  if (ORDER == 4 || TM(i - 2) * TM(i - 1) == 0.0 || TM(i + 3) * TM(i + 2) == 0.0) {
-    double tm1 = TM(i - 1), tp2 = TM(i + 2);
-    int im1 = (int)(tm1 * (i - 1) + (1.0 - tm1) * i);
-    int ip2 = (int)(tp2 * (i + 2) + (1.0 - tp2) * (i + 1));
+  if (ORDER == 4 || !(TM(i - 2) && TM(i - 1)) || !(TM(i + 3) && TM(i + 2))) {
+    int im1 = TM(i - 1) ? i - 1 : i;
+    int ip2 = TM(i + 2) ? i + 2 : i + 1;
     return du * (kA4 * (TT(i + 1) + TT(i)) + kB4 * (TT(ip2) + TT(im1)));
   }
   return du * (kA6 * (TT(i + 1) + TT(i)) + kB6 * (TT(i + 2) + TT(i - 1)) + kC6 * (TT(i + 3) + TT(i - 2)));
@@ -584,13 +584,12 @@ template <int ORDER>
 DEVI double cen_fy(const CenArgs& a, int i, int j, int k) {
   const Geo& g = a.g;
   double dv = a.dxtn[I2(g, i, j)] * a.vh[I3(g, i, j, k)];
-  if (ORDER == 2) return dv * 0.5 * (a.T[I3(g, i, j + 1, k)] + a.T[I3(g, i, j, k)]);
-  auto TM = [&](int jj) { return tq(g, a.tmask, i, jj, k); };
+  if (ORDER == 2) return half_exact(dv) * (a.T[I3(g, i, j + 1, k)] + a.T[I3(g, i, j, k)]);
+  auto TM = [&](int jj) { return !is_zero(tq(g, a.tmask, i, jj, k)); };
   auto TT = [&](int jj) { return tq(g, a.T, i, jj, k); };
-  if (ORDER == 4 || TM(j - 2) * TM(j - 1) == 0.0 || TM(j + 3) * TM(j + 2) == 0.0) {
-    double tm1 = TM(j - 1), tp2 = TM(j + 2);
-    int jm1 = (int)(tm1 * (j - 1) + (1.0 - tm1) * j);
-    int jp2 = (int)(tp2 * (j + 2) + (1.0 - tp2) * (j + 1));
+  if (ORDER == 4 || !(TM(j - 2) && TM(j - 1)) || !(TM(j + 3) && TM(j + 2))) {
+    int jm1 = TM(j - 1) ? j - 1 : j;
+    int jp2 = TM(j + 2) ? j + 2 : j + 1;
     return dv * (kA4 * (TT(j + 1) + TT(j)) + kB4 * (TT(jp2) + TT(jm1)));
   }
   return dv * (kA6 * (TT(j + 1) + TT(j)) + kB6 * (TT(j + 2) + TT(j - 1)) + kC6 * (TT(j + 3) + TT(j - 2)));
@@ -611,9 +610,8 @@ DEVI double cen_fz(const CenArgs& a, int i, int j, int k) {
   double w = a.w[I3(g, i, j, K)];
   int p1 = K + 1 < nk ? K + 1 : nk, p2 = K + 2 < nk ? K + 2 : nk, km1 = K - 1 > 1 ? K - 1 : 1;
   auto TV = [&](int L) { return a.T[I3(g, i, j, L - 1)]; };
-  if (ORDER == 2) return w * 0.5 * (TV(K) + TV(p1));
-  double tp2 = a.tmask[I3(g, i, j, p2 - 1)];
-  int kp2 = (int)rint(tp2 * p2 + (1.0 - tp2) * p1);
+  if (ORDER == 2) return half_exact(w) * (TV(K) + TV(p1));
+  int kp2 = is_zero(a.tmask[I3(g, i, j, p2 - 1)]) ? p1 : p2;  // nint(tp2*p2 + (1-tp2)*p1), tp2 0 or 1
   if (ORDER == 6 && !(K <= 2 || K >= nk - 1) && K < a.kmt[I2(g, i, j)] - 2)
     return w * (kA6 * (TV(K) + TV(p1)) + kB6 * (TV(km1) + TV(kp2)) + kC6 * (TV(K - 2) + TV(K + 3)));
   return w * (kA4 * (TV(K) + TV(p1)) + kB4 * (TV(km1) + TV(kp2)));
