@@ -14,6 +14,12 @@ server keeps every domain's state on the device and never copies it back.
   in at most one batch at a time; requests for a busy domain wait.
 * Completion is detected with CUDA events; a request's latency runs from its
   arrival to the moment the host sees its batch complete.
+* Failures are contained on the host: a request for a domain that does not exist
+  or is quarantined is rejected at arrival; a batched step that the library
+  refuses (a non-zero status) fails the requests of that batch, quarantines their
+  domains and leaves every other domain serving; with ``check_every`` > 0 the
+  state of a domain is checked for non-finite values after every ``check_every``
+  of its steps, and a domain that fails the check is quarantined.
 
 All kernels come from libmom5gpu.so through the batch API
 (``mom5gpu_batch_step``); this module only schedules.
@@ -42,6 +48,8 @@ class Request:
     arrival: float
     start: float = 0.0
     done: float = 0.0
+    status: str = "ok"  # ok | failed | rejected
+    error: str = ""
 
 
 @dataclass
@@ -65,7 +73,7 @@ def bytes_per_domain(ni, nj, nk, ntr, precision) -> int:
 
 class Server:
     def __init__(self, dtime: float, precision=capi.PRECISION_MIXED, slots: int = 3, max_batch: int = 64,
-                 reserve_bytes: int = 8 << 30, memory_limit: Optional[int] = None):
+                 reserve_bytes: int = 8 << 30, memory_limit: Optional[int] = None, check_every: int = 0):
         import torch
         self.torch = torch
         self.dtime = dtime
@@ -81,6 +89,8 @@ class Server:
         self.steps_done: List[int] = []
         self.slots: List[Slot] = []
         self.used_bytes = 0
+        self.check_every = check_every
+        self.quarantined: Dict[int, str] = {}  # domain -> reason
 
     # ---- admission ----
     def free_bytes(self) -> int:
@@ -142,8 +152,14 @@ class Server:
                 raise TimeoutError(f"serving loop exceeded {timeout} s with {len(reqs) - len(done)} requests left")
             while nxt < len(reqs) and reqs[nxt].arrival <= now:
                 r = reqs[nxt]
-                waiting.setdefault(self.bucket(r.domain), deque()).append(r)
                 nxt += 1
+                if not 0 <= r.domain < len(self.domains) or r.domain in self.quarantined:
+                    r.status = "rejected"
+                    r.error = self.quarantined.get(r.domain, f"no domain {r.domain}")
+                    r.start = r.done = now
+                    done.append(r)
+                    continue
+                waiting.setdefault(self.bucket(r.domain), deque()).append(r)
             # completions
             for si in list(inflight):
                 s = self.slots[si]
@@ -155,6 +171,8 @@ class Server:
                         self.parity[r.domain] ^= 1
                         self.steps_done[r.domain] += 1
                         done.append(r)
+                        if self.check_every and self.steps_done[r.domain] % self.check_every == 0:
+                            self.health_check(r.domain)
                     s.requests = []
                     inflight.remove(si)
                     free_slots.append(si)
@@ -169,6 +187,11 @@ class Server:
                     take, keep, seen = [], deque(), set()
                     while q:
                         r = q.popleft()
+                        if r.domain in self.quarantined:  # quarantined while the request waited
+                            r.status, r.error = "rejected", self.quarantined[r.domain]
+                            r.start = r.done = time.perf_counter() - t0
+                            done.append(r)
+                            continue
                         if (len(take) < self.max_batch and not self.busy[r.domain] and r.domain not in seen):
                             take.append(r)
                             seen.add(r.domain)
@@ -183,7 +206,19 @@ class Server:
                     for r in take:
                         r.start = t
                         self.busy[r.domain] = True
-                    s.batch.step(self.dtime, index=[r.domain for r in take], parity=[self.parity[r.domain] for r in take])
+                    try:
+                        s.batch.step(self.dtime, index=[r.domain for r in take],
+                                     parity=[self.parity[r.domain] for r in take])
+                    except capi.Mom5GpuError as e:
+                        # the library refused the step: fail these requests, keep the others serving
+                        for r in take:
+                            r.status, r.error, r.done = "failed", str(e), time.perf_counter() - t0
+                            self.busy[r.domain] = False
+                            self.quarantined[r.domain] = f"step failed: {e}"
+                            done.append(r)
+                        free_slots.append(si)
+                        launched = True
+                        break
                     s.event = torch.cuda.Event()
                     s.event.record(s.stream)
                     s.requests = take
@@ -196,13 +231,28 @@ class Server:
                     break
             if not free_slots or (nxt < len(reqs) and not any(waiting.values())):
                 time.sleep(20e-6)
-        wall = max(r.done for r in done) - min(r.arrival for r in done)
-        lat = np.array([r.done - r.arrival for r in done])
-        cells = sum(self.cells[r.domain] for r in done)
-        return {"requests": len(done), "wall_s": wall, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+        ok = [r for r in done if r.status == "ok"]
+        wall = max(r.done for r in done) - min(r.arrival for r in done) if done else 0.0
+        lat = np.array([r.done - r.arrival for r in ok]) if ok else np.zeros(1)
+        cells = sum(self.cells[r.domain] for r in ok)
+        wall = max(wall, 1e-9)
+        return {"requests": len(ok), "wall_s": wall, "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
-                "cell_updates_per_s": cells / wall, "requests_per_s": len(done) / wall, "batches": batches,
-                "mean_batch": float(np.mean(batch_sizes)) if batch_sizes else 0.0}
+                "cell_updates_per_s": cells / wall, "requests_per_s": len(ok) / wall, "batches": batches,
+                "mean_batch": float(np.mean(batch_sizes)) if batch_sizes else 0.0,
+                "failed": sum(r.status == "failed" for r in done),
+                "rejected": sum(r.status == "rejected" for r in done),
+                "errors": {r.rid: r.error for r in done if r.status != "ok"},
+                "quarantined": dict(self.quarantined)}
+
+    def health_check(self, i: int) -> bool:
+        """Quarantine domain i if any tracer at its current time level is not finite."""
+        d = self.domains[i]
+        level = self.parity[i] + 1
+        if d.check_finite(0, level):
+            return True
+        self.quarantined[i] = f"non-finite tracer after {self.steps_done[i]} steps"
+        return False
 
 
 def poisson_arrivals(rate: float, n: int, seed: int = 0) -> List[float]:

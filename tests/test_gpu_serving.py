@@ -86,3 +86,54 @@ def test_admission_by_free_memory(gpu_lib):
     srv.add_domain(grid.make_domain(specs[0]), load)
     with pytest.raises(serving.AdmissionError):
         srv.add_domain(grid.make_domain(specs[1]), load)
+
+
+def test_failures_are_contained(gpu_lib):
+    """Host-side fault injection: a request for a domain that does not exist is
+    rejected; a batched step the library refuses fails only the requests of that
+    batch and quarantines their domains; a domain whose tracer turns non-finite is
+    quarantined by the health check; every other domain keeps serving and ends
+    equal to the same domain stepped alone."""
+    capi = gpu_lib
+    from mom5_gb300 import serving
+    specs = small_specs(5, seed=9)
+    doms = [grid.make_domain(s) for s in specs]
+    srv = serving.Server(DT, precision=1, slots=2, max_batch=1, reserve_bytes=1 << 30, check_every=1)
+    load = loader(capi, 1)
+    for dom in doms:
+        srv.add_domain(dom, load)
+    srv.start()
+    poisoned, blown = 1, 3
+    # a library refusal whenever the poisoned domain is stepped
+    for slot in srv.slots:
+        real = slot.batch.step
+
+        def step(dtime, index=None, parity=None, _real=real):
+            if index is not None and poisoned in index:
+                raise capi.Mom5GpuError(capi.EINVAL, "injected refusal")
+            return _real(dtime, index=index, parity=parity)
+        slot.batch.step = step
+    # a non-finite value in the blown domain's tracer
+    T = srv.domains[blown].get(capi.F.TRACER, n=1, level=1)
+    T[T.size // 2] = np.nan
+    srv.domains[blown].set(capi.F.TRACER, T, n=1, level=1)
+    targets = [0, 1, 2, 3, 4, 99, 0, 1, 2, 3, 4, 0, 2, 4]
+    arrivals = [0.001 * i for i in range(len(targets))]
+    stats = srv.run(arrivals, targets)
+    assert stats["rejected"] >= 1 + 1  # the unknown domain, and later requests to a quarantined one
+    assert stats["failed"] == 1 and "injected refusal" in srv.quarantined[poisoned]
+    assert blown in srv.quarantined and "non-finite" in srv.quarantined[blown]
+    assert srv.steps_done[poisoned] == 0 and srv.steps_done[blown] == 1
+    for i in (0, 2, 4):
+        k = srv.steps_done[i]
+        assert k == targets.count(i)
+        alone = load(doms[i])
+        tau = 1
+        for _ in range(k):
+            alone.tracer_advection_step(tau, tau, 3 - tau, DT)
+            alone.update_ocean_barotropic(tau, 3 - tau)
+            tau = 3 - tau
+        for n in range(1, specs[i].ntracers + 1):
+            assert np.array_equal(alone.get(capi.F.TRACER, n=n, level=tau), srv.domains[i].get(capi.F.TRACER, n=n, level=tau))
+        alone.close()
+    srv.close()
