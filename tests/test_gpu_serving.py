@@ -114,9 +114,10 @@ def test_failures_are_contained(gpu_lib):
             return _real(dtime, index=index, parity=parity)
         slot.batch.step = step
     # a non-finite value in the blown domain's tracer
-    T = srv.domains[blown].get(capi.F.TRACER, n=1, level=1)
-    T[T.size // 2] = np.nan
-    srv.domains[blown].set(capi.F.TRACER, T, n=1, level=1)
+    sb = specs[blown]
+    T = srv.domains[blown].get(capi.F.TRACER, n=1, level=1).reshape(sb.nk, sb.nj + 2, sb.ni + 2)
+    T[0, 2, 2] = np.nan  # a compute cell away from the continent
+    srv.domains[blown].set(capi.F.TRACER, np.ascontiguousarray(T), n=1, level=1)
     targets = [0, 1, 2, 3, 4, 99, 0, 1, 2, 3, 4, 0, 2, 4]
     arrivals = [0.001 * i for i in range(len(targets))]
     stats = srv.run(arrivals, targets)
