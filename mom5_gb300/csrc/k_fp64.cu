@@ -1024,16 +1024,21 @@ int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime) {
 // ---------------------------------------------------------------------------
 // explicit tracer update (ocean_tracer.F90:2341-2350)
 // ---------------------------------------------------------------------------
+// The time levels and th_tendency are distinct arrays (restrict), so the loads of
+// several tracers are issued before their stores.
 __global__ void k_update_tracer(UpdArgs u) {
   const Geo& g = u.g;
   int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   int j = blockIdx.y + 1, k = blockIdx.z;
   if (i > g.ni) return;
   long p = I3(g, i, j, k);
+  const double* __restrict__ Tm1 = u.Tm1 + p;
+  const double* __restrict__ th = u.th + p;
+  double* __restrict__ Tp1 = u.Tp1 + p;
+  const long ts = u.tstride, hs = g.n3;
   double a = u.rdz_m1[p], r = u.rdzr[p];
-  for (int n = 0; n < u.ntr; ++n) {
-    u.Tp1[n * u.tstride + p] = (a * u.Tm1[n * u.tstride + p] + u.dtime * u.th[n * g.n3 + p]) * r;
-  }
+#pragma unroll 5
+  for (int n = 0; n < u.ntr; ++n) Tp1[n * ts] = (a * Tm1[n * ts] + u.dtime * th[n * hs]) * r;
 }
 
 int make_upd_args(mom5gpu_domain* d, int taum1, int taup1, double dtime, UpdArgs* u) {
