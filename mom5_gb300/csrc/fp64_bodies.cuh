@@ -6,6 +6,7 @@
 #include <math.h>
 
 #include "internal.h"
+#include "fp64_div.cuh"
 
 namespace mom5 {
 namespace fp64 {
@@ -48,13 +49,13 @@ DEVI double plus_zero(double x) {
 // Inf and NaN take the multiply (decided per warp, so the common case issues no
 // FP64 instruction).
 DEVI double half_exact(double x) {
-  long long b = __double_as_longlong(x);
+  long long b = bits_of(x);
   unsigned e = (unsigned)((unsigned long long)b >> 52) & 0x7ffu;
   bool normal = e - 2u < 0x7fdu;  // 2 <= e <= 0x7fe
   bool fast = normal || (b << 1) == 0;
   long long r = normal ? b - (1LL << 52) : b;
-  if (__all_sync(__activemask(), fast)) return __longlong_as_double(r);
-  return fast ? __longlong_as_double(r) : 0.5 * x;
+  if (__all_sync(__activemask(), fast)) return double_of(r);
+  return fast ? double_of(r) : 0.5 * x;
 }
 
 // Arithmetic policy of the MDFL bodies: the FP64 instructions.  (Integer-pipe
@@ -67,42 +68,6 @@ struct HwArith {
 };
 using MdflFaceArith = HwArith;
 using MdflUpdArith = HwArith;
-
-// a / b from y = RN(1/b), for a divisor shared by many quotients (Markstein's
-// correction: P. Markstein, IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al.,
-// Handbook of Floating-Point Arithmetic, ch. 5): q = RN(a*y), r = a - b*q
-// (one FMA), q1 = RN(q + r*y).  The result is then proven correctly rounded
-// at run time: with r1 = a - b*q1 from one more FMA (exact when q1 is within
-// an ulp), q1 = RN(a/b) when |r1| < |b|*ulp(q1)/2 and q1 is normal and not a
-// power of two.  A lane that cannot prove it (a tie, a binade edge, extreme
-// exponents) takes the division instruction, so the result always equals a / b.
-DEVI double div_recip(double a, double b, double y) {
-  const long long kAbsMask = 0x7fffffffffffffffLL;
-  long long ab = __double_as_longlong(a) & kAbsMask, bb = __double_as_longlong(b) & kAbsMask;
-  int ea = (int)(ab >> 52), eb = (int)(bb >> 52);
-  double q1;
-  bool ok;
-  if (ab == 0) {  // 0 / b = +-0 for finite non-zero b
-    q1 = __longlong_as_double((__double_as_longlong(a) ^ __double_as_longlong(b)) & (long long)0x8000000000000000ULL);
-    ok = eb >= 1 && eb <= 2046;
-  } else {
-    double q = a * y;
-    double r = fma(-q, b, a);
-    q1 = fma(r, y, q);
-    double r1 = fma(-q1, b, a);
-    long long qb = __double_as_longlong(q1) & kAbsMask;
-    int eq = (int)(qb >> 52);
-    int et = eb + eq - 1076;  // exponent of |b| * ulp(q1) / 2
-    ok = ea >= 64 && ea <= 1980 && eb >= 64 && eb <= 1980 && eq >= 64 && eq <= 1980 &&
-         (qb & 0x000fffffffffffffLL) != 0 && et >= 1 && et <= 2046;
-    long long thr = (bb & 0x000fffffffffffffLL) | ((long long)et << 52);
-    ok = ok && (__double_as_longlong(r1) & kAbsMask) < thr;
-  }
-  if (!__all_sync(__activemask(), ok)) {
-    if (!ok) q1 = a / b;
-  }
-  return q1;
-}
 
 // Sweby limiter psi (ocean_tracer_advect.F90:3868-3878).  With the limiter on
 // the reference forms psi*(1-1) + max(...)*1, with it off psi*1 + max(...)*0;
@@ -128,7 +93,7 @@ DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, d
   long long b = __double_as_longlong(mf);
   bool pos = b > 0;                                                 // mf > 0
   bool neg = b < 0 && b != (long long)0x8000000000000000ULL;        // mf < 0
-  double theta = (pos ? Rjm : Rjp) / Ar::add(1.0e-30, Rj);
+  double theta = div_seeded(pos ? Rjm : Rjp, add_1em30(Rj));
   double psi = limiter<SWEBY, Ar>(theta, d0, d1, c);
   double p = Ar::mul(psi, Rj);
   double r = Ar::mul(mf, Ar::add(pos ? Tp : Tm, pos ? p : -p));
@@ -174,11 +139,11 @@ DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
     double wk = a.w[I3(g, i, j, k + 1)];
     double rdz = a.rdz[I3(g, i, j, k)];
     double massflux = dat * wk;
-    double cfl = fabs(wk * a.dtime / rdz);
+    double cfl = fabs(div_seeded(wk * a.dtime, rdz));
     double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
     double d1 = (1.0 - cfl * cfl) * kOneSixth;
-    double c = (1.0 - cfl) / (1.0e-30 + cfl);
-    double dtr = ALL ? 0.0 : a.dtime / rdz;
+    double c = div_seeded(1.0 - cfl, add_1em30(cfl));
+    double dtr = ALL ? 0.0 : div_seeded(a.dtime, rdz);
     double wdiff = wkm1 - wk;
     bool fm = mkp1 && mk;
     long p = I3(g, i, j, k);
@@ -198,7 +163,7 @@ DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
       if (!ALL) {
         tm = Au::add(Tk, Au::mul(dtr, div));
       } else {
-        tm = Au::add(Tk, Au::mul(div, a.dtime) / rdz);
+        tm = Au::add(Tk, div_seeded(Au::mul(div, a.dtime), rdz));
       }
       a.tz[n * g.n3 + p] = tm;
       ftp[n][t] = fbt;
@@ -241,10 +206,10 @@ DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], 
   bool m1 = a.mask2[IM(g, i, j, k)], m2 = a.mask2[IM(g, i + 1, j, k)];
   double u = a.uh[I3(g, i, j, k)];
   double massflux = a.dyte[I2(g, i, j)] * u;
-  double cfl = fabs(u * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
+  double cfl = fabs(div_seeded(u * a.dtime * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
   double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
   double d1 = (1.0 - cfl * cfl) * kOneSixth;
-  double c = (1.0 - cfl) / (1.0e-30 + cfl);
+  double c = div_seeded(1.0 - cfl, add_1em30(cfl));
   bool fm = m1 && m2;
 #pragma unroll 1
   for (int n = 0; n < a.ntr; ++n) {
@@ -284,7 +249,7 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
   double rdz = a.rdz[I3(g, i, j, k)];
   double divx = a.dyte[I2(g, i, j)] * a.uh[I3(g, i, j, k)] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
   // dtime*tmask*datr/rho_dzt (:3960-3961); tmask_mdfl*datr (:4277)
-  double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
+  double coef = ALL ? 0.0 : (mk ? div_seeded(a.dtime * datr, rdz) : 0.0);
   long p = I3(g, i, j, k);
 #pragma unroll 1
   for (int n = 0; n < a.ntr; ++n) {
@@ -295,7 +260,7 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
       tm = Au::add(tm, Au::mul(coef, s));
     } else {
       double w1 = mk ? Au::mul(datr, s) : 0.0;
-      tm = Au::add(tm, Au::mul(w1, a.dtime) / rdz);
+      tm = Au::add(tm, div_seeded(Au::mul(w1, a.dtime), rdz));
     }
     a.tx[n * g.n3 + p] = tm;
   }
@@ -314,10 +279,10 @@ DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThread
   bool m2 = a.mask2[IM(g, i, j + 1, k)], m3 = a.mask2[IM(g, i, j + 2, k)];
   double v = a.vh[I3(g, i, j, k)];
   double massflux = a.dxtn[I2(g, i, j)] * v;
-  double cfl = fabs(v * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
+  double cfl = fabs(div_seeded(v * a.dtime * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
   double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
   double d1 = (1.0 - cfl * cfl) * kOneSixth;
-  double c = (1.0 - cfl) / (1.0e-30 + cfl);
+  double c = div_seeded(1.0 - cfl, add_1em30(cfl));
   bool fm = m1 && m2;
 #pragma unroll 1
   for (int n = 0; n < a.ntr; ++n) {
@@ -361,8 +326,8 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
     double wkm1j = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;  // bottom face of level k-1; 0 at the surface
     double corr = (wk - wkm1j) + datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] -
                                          a.dyte[I2(g, i, j)] * a.uh[p]);
-    double coef = ALL ? 0.0 : (mk ? a.dtime * datr / rdz : 0.0);
-    const double rrdz = 1.0 / rdz;  // shared by every tracer's division by rho_dzt
+    double coef = ALL ? 0.0 : (mk ? div_seeded(a.dtime * datr, rdz) : 0.0);
+    const double rrdz = recip_seed(rdz);  // shared by every tracer's division by rho_dzt
 #pragma unroll 1
     for (int n = 0; n < a.ntr; ++n) {
       double Tk = a.T[n * a.tstride + p];
