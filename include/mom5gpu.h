@@ -288,7 +288,7 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
  * A summary is written to report (may be NULL). */
 int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len);
 /* The launch shape autotune chose, or one to pin: precision-form tile height
- * (16 or 32 rows incl. halo), tracer prefetch into shared memory (height 16
+ * (16, 24 or 32 rows incl. halo), tracer prefetch into shared memory (height 16
  * only), FP64 y-pass rows per thread (0 = built-in choice, 2, 4, 8, 16).
  * Every shape gives the same results bit for bit. */
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
