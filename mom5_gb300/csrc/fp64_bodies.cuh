@@ -21,28 +21,35 @@ DEVI long IM(const Geo& g, int i, int j, int k) { return ((long)k * (g.nj + 4) +
 constexpr double kOneSixth = 1.0 / 6.0;  // ocean_parameters.F90:92
 
 // max(0, x) and min(a, b) on the integer pipe (ordered-integer comparison of
-// the bit patterns; equal to the FP comparison for all non-NaN operands).
+// the bit patterns; equal to the FP comparison for all non-NaN operands).  The
+// bit patterns are taken through bits_of so that the compiler keeps the tests
+// integer.
 DEVI long long ordbits(double x) {
-  long long b = __double_as_longlong(x);
+  long long b = bits_of(x);
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
 }
 DEVI double dmin(double a, double b) { return ordbits(a) <= ordbits(b) ? a : b; }
-DEVI double dmax0(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
-DEVI bool dpos(double x) { return __double_as_longlong(x) > 0; }   // x > 0
+DEVI double dmax0(double x) { return bits_of(x) > 0 ? x : 0.0; }
+DEVI bool dpos(double x) {  // x > 0 (false for NaN)
+  long long b = bits_of(x);
+  return b > 0 && b <= 0x7ff0000000000000LL;
+}
 
 // Exact shortcuts that keep work off the FP64 pipe (GB300 issues FP64 at
 // 1/64 of the FP32 rate; integer operations are cheap).  Each returns the
 // bit pattern the FP64 operation would produce.
-DEVI bool is_one(double m) { return __double_as_longlong(m) == 0x3ff0000000000000LL; }
-DEVI bool is_zero(double m) { return (__double_as_longlong(m) << 1) == 0; }
+DEVI bool is_one(double m) { return bits_of(m) == 0x3ff0000000000000LL; }
+DEVI bool is_zero(double m) { return (bits_of(m) << 1) == 0; }
 // x*m for a mask value m: 1 -> x (x*1 == x), +-0 -> 0.0 as the callers' selects do
 DEVI double mask_mul(double x, double m) {
   if (is_one(m)) return x;
   return x * m;
 }
 // x + 0.0: the same value except that -0 becomes +0
-DEVI double plus_zero(double x) {
-  return __double_as_longlong(x) == (long long)0x8000000000000000ULL ? 0.0 : x;
+DEVI double plus_zero(double x) { return bits_of(x) == (long long)0x8000000000000000ULL ? 0.0 : x; }
+// -x (the sign bit flipped) when flip, on the integer pipe
+DEVI double neg_if(double x, bool flip) {
+  return double_of(bits_of(x) ^ (flip ? (long long)0x8000000000000000ULL : 0LL));
 }
 // 0.5*x: for a normal x whose exponent field is at least 2 the product is the
 // exponent lowered by one; +-0 is unchanged.  Subnormals, the smallest normals,
@@ -86,17 +93,18 @@ DEVI double limiter(double theta, double d0, double d1, double c) {
 // the first is.  Both signs share one division and one limiter evaluation (the
 // operands are selected first), so a warp whose faces carry both signs runs
 // the division once, not once per branch; Tdn - p is computed as Tdn + (-p),
-// which IEEE defines to be the same operation.
+// which IEEE defines to be the same operation, with -p formed on the integer
+// pipe.
 template <bool SWEBY, class Ar>
 DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, double Tm, double d0, double d1,
                       double c) {
-  long long b = __double_as_longlong(mf);
+  long long b = bits_of(mf);
   bool pos = b > 0;                                                 // mf > 0
   bool neg = b < 0 && b != (long long)0x8000000000000000ULL;        // mf < 0
   double theta = div_seeded(pos ? Rjm : Rjp, add_1em30(Rj));
   double psi = limiter<SWEBY, Ar>(theta, d0, d1, c);
   double p = Ar::mul(psi, Rj);
-  double r = Ar::mul(mf, Ar::add(pos ? Tp : Tm, pos ? p : -p));
+  double r = Ar::mul(mf, Ar::add(pos ? Tp : Tm, neg_if(p, !pos)));
   return (pos || neg) ? r : 0.0;
 }
 
@@ -314,7 +322,8 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
   if (i > g.ni) return;
   int j1 = j0 + TJ - 1;
   if (j1 > g.nj) j1 = g.nj;
-  const double rdtime = 1.0 / a.dtime;
+  double rdt_h, rdt_l;  // two-term reciprocal of dtime
+  recip_pair(a.dtime, rdt_h, rdt_l);
   y_face<SWEBY, MAXN, Ar>(a, i, j0 - 1, k, fprev, t, Ra, Rb, true);
   for (int j = j0; j <= j1; ++j) {
     y_face<SWEBY, MAXN, Ar>(a, i, j, k, fcur, t, Ra, Rb, false);
@@ -327,7 +336,8 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
     double corr = (wk - wkm1j) + datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] -
                                          a.dyte[I2(g, i, j)] * a.uh[p]);
     double coef = ALL ? 0.0 : (mk ? div_seeded(a.dtime * datr, rdz) : 0.0);
-    const double rrdz = recip_seed(rdz);  // shared by every tracer's division by rho_dzt
+    double rr_h, rr_l;  // two-term reciprocal of rho_dzt, shared by every tracer's divisions
+    recip_pair(rdz, rr_h, rr_l);
 #pragma unroll 1
     for (int n = 0; n < a.ntr; ++n) {
       double Tk = a.T[n * a.tstride + p];
@@ -336,12 +346,12 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
       double out;
       if (!ALL) {
         tm = Au::add(tm, Au::mul(coef, Au::sub(fp, fc)));
-        tm = Au::add(tm, Au::mul(div_recip(Au::mul(a.dtime, Tk), rdz, rrdz), corr));
+        tm = Au::add(tm, Au::mul(div_pair(Au::mul(a.dtime, Tk), rdz, rr_h, rr_l), corr));
       } else {
         double w1 = Au::add(mk ? Au::mul(datr, Au::sub(fp, fc)) : 0.0, Au::mul(Tk, corr));
-        tm = Au::add(tm, div_recip(Au::mul(w1, a.dtime), rdz, rrdz));
+        tm = Au::add(tm, div_pair(Au::mul(w1, a.dtime), rdz, rr_h, rr_l));
       }
-      out = mk ? div_recip(Au::mul(rdz, Au::sub(tm, Tk)), a.dtime, rdtime) : 0.0;
+      out = mk ? div_pair(Au::mul(rdz, Au::sub(tm, Tk)), a.dtime, rdt_h, rdt_l) : 0.0;
       double* th = a.th + n * g.n3;
       th[p] = Au::add(th[p], out);
       fprev[n][t] = fc;
@@ -472,7 +482,7 @@ DEVI void bt_pred_body(BtArgs a, int so, int sn, int bx, int by) {
   const double* eo = a.eta_bt + so * g.n2;
   long q = I2(g, i, j);
   double en;
-  if (a.gamma > 0.0) {
+  if (dpos(a.gamma)) {
     double dv = a.cgrid ? div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j)
                         : div_ud_bh(a, a.uhb + so * g.n2, a.vhb + so * g.n2, i, j);
     double tm = a.tmask1[q];

@@ -695,7 +695,7 @@ DEVI double supb_flux(double mf, double cfl, double Rjm, double Rj, double Rjp, 
   // the comparisons on the integer pipe (sel::), same selections as the FP ones
   const bool pos = sel::gt0(mf);
   double Cr;
-  if ((__double_as_longlong(Rj) << 1) != 0) Cr = (pos ? Rjm : Rjp) / Rj;
+  if ((__double_as_longlong(Rj) << 1) != 0) Cr = div_seeded(pos ? Rjm : Rjp, Rj);
   else Cr = (pos ? Rjm : Rjp) * 1.0e20;
   double c2 = 2.0 * Cr;
   double lo = sel::lt_min(1.0, c2), hi = sel::lt_min(2.0, Cr);
@@ -712,7 +712,7 @@ DEVI double supb_zflux(const SupbArgs& a, int i, int j, int k) {
   double Rj = (Tk - Tkp1) * m2d(a, i, j, k) * m2d(a, i, j, kp1);
   double Rjm = (Tkp1 - a.T[I3(g, i, j, kp2)]) * m2d(a, i, j, kp1) * m2d(a, i, j, kp2);
   double w = a.w[I3(g, i, j, k + 1)];
-  double cfl = fabs(w * a.dtime / a.rdz[I3(g, i, j, k)]);
+  double cfl = fabs(div_seeded(w * a.dtime, a.rdz[I3(g, i, j, k)]));
   return supb_flux(a.dat[I2(g, i, j)] * w, cfl, Rjm, Rj, Rjp, Tk, Tkp1, m2d(a, i, j, kp1), m2d(a, i, j, k));
 }
 
@@ -728,7 +728,7 @@ __global__ void k_supb_z(SupbArgs a) {
     double fbt = supb_zflux(a, i, j, k);
     double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
     double Tk = a.T[p];
-    a.tz[p] = Tk + a.dtime / a.rdz[p] * (a.datr[I2(g, i, j)] * (fbt - ftp) + Tk * (wkm1 - a.w[I3(g, i, j, k + 1)]));
+    a.tz[p] = Tk + div_seeded(a.dtime, a.rdz[p]) * (a.datr[I2(g, i, j)] * (fbt - ftp) + Tk * (wkm1 - a.w[I3(g, i, j, k + 1)]));
     ftp = fbt;
   }
 }
@@ -740,7 +740,7 @@ DEVI double supb_xflux(const SupbArgs& a, int i, int j, int k) {
   double Rj = (t(i + 1) - t(i)) * m2d(a, i + 1, j, k) * m2d(a, i, j, k);
   double Rjm = (t(i) - t(i - 1)) * m2d(a, i, j, k) * m2d(a, i - 1, j, k);
   double u = a.uh[I3(g, i, j, k)];
-  double cfl = fabs(u * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
+  double cfl = fabs(div_seeded(u * a.dtime * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]));
   return supb_flux(a.dyte[I2(g, i, j)] * u, cfl, Rjm, Rj, Rjp, t(i + 1), t(i), m2d(a, i, j, k), m2d(a, i + 1, j, k));
 }
 
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(HB) k_supb_x(SupbArgs a) {
   if (t > HB - 2 || i > g.ni) return;
   long p = I3(g, i, j, k);
   double div = a.dyte[I2(g, i, j)] * a.uh[p] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
-  a.tx[p] = a.tz[p] + a.dtime * m2d(a, i, j, k) * a.datr[I2(g, i, j)] / a.rdz[p] * (sfx[t] - sfx[t + 1] + a.T[p] * div);
+  a.tx[p] = a.tz[p] + div_seeded(a.dtime * m2d(a, i, j, k) * a.datr[I2(g, i, j)], a.rdz[p]) * (sfx[t] - sfx[t + 1] + a.T[p] * div);
 }
 
 DEVI double supb_yflux(const SupbArgs& a, int i, int j, int k) {
@@ -765,7 +765,7 @@ DEVI double supb_yflux(const SupbArgs& a, int i, int j, int k) {
   double Rj = (t(j + 1) - t(j)) * m2d(a, i, j + 1, k) * m2d(a, i, j, k);
   double Rjm = (t(j) - t(j - 1)) * m2d(a, i, j, k) * m2d(a, i, j - 1, k);
   double v = a.vh[I3(g, i, j, k)];
-  double cfl = fabs(v * a.dtime * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
+  double cfl = fabs(div_seeded(v * a.dtime * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
   return supb_flux(a.dxtn[I2(g, i, j)] * v, cfl, Rjm, Rj, Rjp, t(j + 1), t(j), m2d(a, i, j, k), m2d(a, i, j + 1, k));
 }
 
@@ -779,12 +779,12 @@ __global__ void k_supb_y(SupbArgs a) {
     long p = I3(g, i, j, k);
     double fn = supb_yflux(a, i, j, k);
     double rdz = a.rdz[p], datr = a.datr[I2(g, i, j)], T = a.T[p];
-    double t = a.tx[p] + a.dtime * a.tmask[p] * datr / rdz * (fs - fn);
+    double t = a.tx[p] + div_seeded(a.dtime * a.tmask[p] * datr, rdz) * (fs - fn);
     double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
-    t = t + a.dtime * T / rdz *
+    t = t + div_seeded(a.dtime * T, rdz) *
                 (a.w[I3(g, i, j, k + 1)] - wkm1 +
                  datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] - a.dyte[I2(g, i, j)] * a.uh[p]));
-    double advect = -rdz * (t - T) / a.dtime * m2d(a, i, j, k);
+    double advect = div_seeded(-rdz * (t - T), a.dtime) * m2d(a, i, j, k);
     a.th[p] = a.th[p] + (-advect);
     fs = fn;
   }
@@ -889,13 +889,13 @@ __global__ void k_ppm_zflux(PpmArgs a) {
     double wk = a.w[I3(g, i, j, K)];
     double massflux = dat * wk * msk0 * mskp1;
     if (!sel::gt0(massflux)) {
-      double cfl = fabs(wk * a.dtime / at(a.rdz, K));
+      double cfl = fabs(div_seeded(wk * a.dtime, at(a.rdz, K)));
       a.fz[I3(g, i, j, K - 1)] = massflux * (ar + 0.5 * cfl * ((al - ar) + (1. - ppm::kTwoThirds * cfl) * c6));
     }
     double wkm1 = a.w[I3(g, i, j, km1)];
     massflux = dat * wkm1 * msk0 * mskm1;
     if (sel::gt0(massflux)) {
-      double cfl = fabs(wkm1 * a.dtime / at(a.rdz, km1));
+      double cfl = fabs(div_seeded(wkm1 * a.dtime, at(a.rdz, km1)));
       a.fz[I3(g, i, j, km1 - 1)] = massflux * (al + 0.5 * cfl * ((ar - al) + (1. - ppm::kTwoThirds * cfl) * c6));
     }
   }
@@ -910,7 +910,7 @@ __global__ void k_ppm_zupd(PpmArgs a) {
   const double mskm1 = (double)(K - km1);
   long p = I3(g, i, j, k), pm = I3(g, i, j, km1 - 1);
   double T = a.T[p];
-  a.tz[p] = T + a.dtime / a.rdz[p] *
+  a.tz[p] = T + div_seeded(a.dtime, a.rdz[p]) *
                     (a.datr[I2(g, i, j)] * (a.fz[p] - mskm1 * a.fz[pm]) +
                      T * (mskm1 * a.w[I3(g, i, j, km1)] - a.w[I3(g, i, j, K)]));
 }
@@ -930,13 +930,13 @@ __global__ void __launch_bounds__(PPM_LX) k_ppm_x(PpmArgs a) {
                   double a61) {
     double u = a.uh[I3(g, i, j, k)];
     double massflux = a.dyte[I2(g, i, j)] * u;
-    double cfl = u * dt * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]);
+    double cfl = div_seeded(u * dt * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i + 1, j, k)]) * a.dxte[I2(g, i, j)]);
     return ppm::hflux(massflux, m0, m1, cfl, aL0, aR0, a60, aL1, aR1, a61);
   };
   auto upd = [&](int i, double Sv, double m, double Fw, double Fe) {
     long p = I3(g, i, j, k);
     double div = a.dyte[I2(g, i, j)] * a.uh[p] - a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)];
-    a.tx[p] = Sv + dt * m * a.datr[I2(g, i, j)] / a.rdz[p] * (Fw - Fe + a.T[p] * div);
+    a.tx[p] = Sv + div_seeded(dt * m * a.datr[I2(g, i, j)], a.rdz[p]) * (Fw - Fe + a.T[p] * div);
   };
   ppm::tile_line<PPM_LX, 1>(g.ni, a.lim, (int)blockIdx.x * (PPM_LX - 8) - 3, threadIdx.x, 0, true, sm, S, M, face,
                             upd);
@@ -955,18 +955,18 @@ __global__ void __launch_bounds__(PPM_BY* PPM_LY) k_ppm_y(PpmArgs a) {
                   double a61) {
     double v = a.vh[I3(g, i, j, k)];
     double massflux = a.dxtn[I2(g, i, j)] * v;
-    double cfl = v * dt * 2.0 / ((a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]);
+    double cfl = div_seeded(v * dt * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]);
     return ppm::hflux(massflux, m0, m1, cfl, aL0, aR0, a60, aL1, aR1, a61);
   };
   auto upd = [&](int j, double Sv, double m, double Fs, double Fn) {
     long p = I3(g, i, j, k);
     double rdz = a.rdz[p], datr = a.datr[I2(g, i, j)], T = a.T[p];
-    double t = Sv + dt * a.tmask[p] * datr / rdz * (Fs - Fn);
+    double t = Sv + div_seeded(dt * a.tmask[p] * datr, rdz) * (Fs - Fn);
     double wkm1 = k > 0 ? a.w[I3(g, i, j, k)] : 0.0;
-    t = t + dt * T / rdz *
+    t = t + div_seeded(dt * T, rdz) *
                 (a.w[I3(g, i, j, k + 1)] - wkm1 +
                  datr * (a.dyte[I2(g, i - 1, j)] * a.uh[I3(g, i - 1, j, k)] - a.dyte[I2(g, i, j)] * a.uh[p]));
-    double advect = -rdz * (t - T) / dt * m;
+    double advect = div_seeded(-rdz * (t - T), dt) * m;
     a.th[p] = a.th[p] + (-advect);
   };
   ppm::tile_line<PPM_LY, PPM_BY>(g.nj, a.lim, (int)blockIdx.y * (PPM_LY - 8) - 3, threadIdx.y, threadIdx.x,
@@ -1352,8 +1352,8 @@ __global__ void k_adv_vel_faces(AdvVelArgs a) {
       bay = half_exact(a.u[p] * a.dyu[q] * a.rdzu[p] + a.u[ps] * a.dyu[qs] * a.rdzu[ps]);
     }
     if (i >= 1) bax = half_exact(a.v[p] * a.dxu[q] * a.rdzu[p] + a.v[p - 1] * a.dxu[q - 1] * a.rdzu[p - 1]);
-    a.ue[p] = bay / a.dyte[q];
-    a.vn[p] = bax / a.dxtn[q];
+    a.ue[p] = div_seeded(bay, a.dyte[q]);
+    a.vn[p] = div_seeded(bax, a.dxtn[q]);
   } else {
     a.ue[p] = a.u[p] * a.rdzten_e[p] * a.dxt_dxter[q] * a.dyt_dyter[q];
     a.vn[p] = a.v[p] * a.rdzten_n[p] * a.dxt_dxtnr[q] * a.dyt_dytnr[q];

@@ -27,6 +27,7 @@
 // are per-domain scratch.
 #include <math.h>
 
+#include "fp64_div.cuh"
 #include "fp64_select.cuh"
 #include "internal.h"
 
@@ -132,7 +133,7 @@ DEVI void limit_mh(Cell& c, double fc, double mc, double fm, double mm, double f
 // (velocity >= 0), else through the low face
 DEVI void out_op(Cell& c, double velocity, double dv, double dtime, bool pos, double* f) {
   f[FM] = pos ? velocity * dtime * dv : -velocity * dtime * dv;
-  double alf = f[FM] / (c.sm + kEpsln);
+  double alf = fp64::div_seeded(f[FM], c.sm + kEpsln);
   double alfq = alf * alf, alf1 = 1.0 - alf, alf1q = alf1 * alf1;
   if (pos) {
     f[F0] = alf * (c.s0 + alf1 * (c.a + (alf1 - alf) * c.aa));
@@ -169,7 +170,7 @@ DEVI void out_op(Cell& c, double velocity, double dv, double dtime, bool pos, do
 // (velocity >= 0), else through the high face
 DEVI void in_op(Cell& c, bool pos, const double* f) {
   c.sm = c.sm + f[FM];
-  double alf = f[FM] / (c.sm + kEpsln), alf1 = 1.0 - alf;
+  double alf = fp64::div_seeded(f[FM], c.sm + kEpsln), alf1 = 1.0 - alf;
   if (pos) {
     double temptm = alf * c.s0 - alf1 * f[F0];
     c.s0 = c.s0 + f[F0];

@@ -1,7 +1,8 @@
 // Exactness check of the FP64 division and 1e-30 + x shortcuts of the exact
-// schemes (mom5_gb300/csrc/fp64_div.cuh): for every case the shortcut's bit
-// pattern must equal the FP64 division / addition instruction's, and the host's
-// IEEE division (NaN payloads aside).  Cases: uniformly random bit patterns
+// schemes (mom5_gb300/csrc/fp64_div.cuh): for every case the bit pattern of
+// each shortcut (the seeded division, the division by a two-term reciprocal,
+// 1e-30 + x) must equal the FP64 division / addition instruction's, and the
+// host's IEEE division (NaN payloads aside).  Cases: uniformly random bit patterns
 // (every exponent, subnormals, Inf, NaN), random operands of moderate exponent,
 // limiter-like ratios of tracer differences, exact quotients, quotients next
 // to rounding midpoints, and the binade edges of the 1e-30 + x shortcut.
@@ -16,10 +17,14 @@
 
 #include "fp64_div.cuh"
 
-__global__ void k_div(const double* a, const double* b, double* qf, double* qr, double* sf, double* sr, long n) {
+__global__ void k_div(const double* a, const double* b, double* qf, double* qp, double* qr, double* sf, double* sr,
+                      long n) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   qf[i] = mom5::fp64::div_seeded(a[i], b[i]);
+  double yh, yl;
+  mom5::fp64::recip_pair(b[i], yh, yl);
+  qp[i] = mom5::fp64::div_pair(a[i], b[i], yh, yl);
   qr[i] = a[i] / b[i];
   sf[i] = mom5::fp64::add_1em30(b[i]);
   sr[i] = 1.0e-30 + b[i];
@@ -96,22 +101,23 @@ int main() {
 
   long n = (long)A.size();
   size_t bytes = sizeof(double) * n;
-  double *dA, *dB, *qf, *qr, *sf, *sr;
-  if (cudaMalloc(&dA, bytes) || cudaMalloc(&dB, bytes) || cudaMalloc(&qf, bytes) || cudaMalloc(&qr, bytes) ||
-      cudaMalloc(&sf, bytes) || cudaMalloc(&sr, bytes)) {
+  double *dA, *dB, *qf, *qp, *qr, *sf, *sr;
+  if (cudaMalloc(&dA, bytes) || cudaMalloc(&dB, bytes) || cudaMalloc(&qf, bytes) || cudaMalloc(&qp, bytes) ||
+      cudaMalloc(&qr, bytes) || cudaMalloc(&sf, bytes) || cudaMalloc(&sr, bytes)) {
     printf("cudaMalloc failed\n");
     return 2;
   }
   cudaMemcpy(dA, A.data(), bytes, cudaMemcpyHostToDevice);
   cudaMemcpy(dB, B.data(), bytes, cudaMemcpyHostToDevice);
-  k_div<<<(unsigned)((n + 255) / 256), 256>>>(dA, dB, qf, qr, sf, sr, n);
+  k_div<<<(unsigned)((n + 255) / 256), 256>>>(dA, dB, qf, qp, qr, sf, sr, n);
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
     printf("kernel: %s\n", cudaGetErrorString(e));
     return 2;
   }
-  std::vector<double> QF(n), QR(n), SF(n), SR(n);
+  std::vector<double> QF(n), QP(n), QR(n), SF(n), SR(n);
   cudaMemcpy(QF.data(), qf, bytes, cudaMemcpyDeviceToHost);
+  cudaMemcpy(QP.data(), qp, bytes, cudaMemcpyDeviceToHost);
   cudaMemcpy(QR.data(), qr, bytes, cudaMemcpyDeviceToHost);
   cudaMemcpy(SF.data(), sf, bytes, cudaMemcpyDeviceToHost);
   cudaMemcpy(SR.data(), sr, bytes, cudaMemcpyDeviceToHost);
@@ -119,16 +125,17 @@ int main() {
   for (long i = 0; i < n; ++i) {
     double host = A[i] / B[i];
     bool host_ok = isnan(host) ? isnan(QF[i]) : bits(host) == bits(QF[i]);
-    if (bits(QF[i]) != bits(QR[i]) || !host_ok || bits(SF[i]) != bits(SR[i])) {
+    if (bits(QF[i]) != bits(QR[i]) || bits(QP[i]) != bits(QR[i]) || !host_ok || bits(SF[i]) != bits(SR[i])) {
       if (bad < 20)
-        printf("case %ld: a=%a b=%a  div %a (instr %a, host %a)  add %a (instr %a)\n", i, A[i], B[i], QF[i], QR[i],
-               host, SF[i], SR[i]);
+        printf("case %ld: a=%a b=%a  div %a pair %a (instr %a, host %a)  add %a (instr %a)\n", i, A[i], B[i], QF[i],
+               QP[i], QR[i], host, SF[i], SR[i]);
       ++bad;
     }
   }
   cudaFree(dA);
   cudaFree(dB);
   cudaFree(qf);
+  cudaFree(qp);
   cudaFree(qr);
   cudaFree(sf);
   cudaFree(sr);

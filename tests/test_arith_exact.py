@@ -1,8 +1,8 @@
 """The FP64 shortcuts of the exact schemes return the FP64 instruction's result:
-tests/arith/div_check.cu compares the seeded Markstein division and the
-1e-30 + x shortcut with the division and addition instructions (and the host's
-division) over about four million operand pairs (GPU); it compiles for sm_103a
-here (CPU)."""
+tests/arith/div_check.cu compares the seeded Markstein division, the division
+by a two-term reciprocal and the 1e-30 + x shortcut with the division and
+addition instructions (and the host's division) over about four million operand
+pairs (GPU); it compiles for sm_103a here (CPU)."""
 import os
 import shutil
 import subprocess
