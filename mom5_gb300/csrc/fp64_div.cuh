@@ -130,19 +130,17 @@ DEVI double div_recip(double a, double b, double y) {
 DEVI double div_seeded(double a, double b) { return div_recip(a, b, recip_seed(b)); }
 
 // Two-term reciprocal yh + yl of b for a divisor shared by many quotients:
-// recip_seed refined by one FP64 Newton-Raphson step to within an ulp of 1/b,
-// then yl = yh*(1 - b*yh), so that yh + yl is within about 2^-100 of 1/b
-// (relative) for b in the FP32 normal range (else NaN).
+// yh = recip_seed(b) and yl = yh*(1 - b*yh) (two FP64 instructions), so that
+// yh + yl is within about 2^-84 of 1/b (relative; the square of yh's error)
+// where recip_seed is usable, else unusable.
 DEVI void recip_pair(double b, double& yh, double& yl) {
-  double y = recip_seed(b);
-  y = fma(y, fma(-b, y, 1.0), y);
-  yh = y;
-  yl = y * fma(-b, y, 1.0);
+  yh = recip_seed(b);
+  yl = yh * fma(-b, yh, 1.0);
 }
 
 // a / b from a two-term reciprocal (recip_pair): q1 = RN(a*yh + RN(a*yl))
 // (N. Brisebarre, J.-M. Muller, S. K. Raina, IEEE Trans. Computers 53(8),
-// 2004) is within about 2^-100 of a/b before its rounding; it is proven
+// 2004) is within about 2^-84 of a/b before its rounding; it is proven
 // correctly rounded as in div_recip, else the lane takes the division
 // instruction.  Three FP64 instructions.
 DEVI double div_pair(double a, double b, double yh, double yl) {
