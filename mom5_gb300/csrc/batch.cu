@@ -87,6 +87,7 @@ int build_descriptors(mom5gpu_batch* b, double dtime) {
         if ((rc = make_mdfl_args(d, 1, b->ntr, taum1, tau, dtime, &m[2 * i + p])) ||
             (rc = make_upd_args(d, taum1, taup1, dtime, &u[2 * i + p])))
           return bfail(b, rc, "domain %d: %s", i, d->err.c_str());
+        m[2 * i + p].th_fresh = 1;  // the step zeroes only the halo ring of th_tendency
       } else if ((rc = make_mix_args(d, taum1, tau, taup1, dtime, &mx[2 * i + p]))) {
         return bfail(b, rc, "domain %d: %s", i, d->err.c_str());
       }
@@ -163,7 +164,8 @@ int enqueue_step(mom5gpu_batch* b, const BatchWork& w, const std::vector<std::pa
       for (auto& it : list) {
         mom5gpu_domain* d = b->doms[it.first];
         double* th = fptr(d, MOM5GPU_TH_TENDENCY, 1, 0);
-        cudaMemsetAsync(th, 0, sizeof(double) * d->geo.n3 * b->ntr, s);
+        launch_zero_ring(d->geo, th, (long)b->ntr * d->geo.nk, s);
+        ++launches;
       }
       launch_batch_fp64_advection(b->d_mdfl, b->d_upd, w, b->ntr, true, tj_of(b), s);
       launches += 4;

@@ -816,11 +816,17 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
     if (d->scheme[n].horz != MOM5GPU_ADVECT_MDFL_SWEBY) all_mdfl = false;
   if (all_mdfl && !d->opt.zero_tracer_advect_horz && d->opt.precision == MOM5GPU_PRECISION_MIXED)
     return launch_mdfl_mixed(d, 1, ntr, taum1, tau, taup1, dtime, true);
-  if ((rc = mom5gpu_zero_th_tendency(d, 0))) return rc;
   if (all_mdfl && !d->opt.zero_tracer_advect_horz) {
-    rc = launch_mdfl(d, d->opt.advect_sweby_all != 0, 1, ntr, taum1, tau, dtime, 1.0);
+    // th_tendency starts at +0: the y pass writes every compute cell, only the
+    // halo ring is zeroed here
+    double* th = fptr(d, MOM5GPU_TH_TENDENCY, 1, 0);
+    if (!th) return MOM5GPU_ENOMEM;
+    launch_zero_ring(d->geo, th, (long)ntr * d->geo.nk, d->stream);
+    count_launches(d, 1);
+    rc = launch_mdfl(d, d->opt.advect_sweby_all != 0, 1, ntr, taum1, tau, dtime, 1.0, true);
     if (rc) return rc;
   } else {
+    if ((rc = mom5gpu_zero_th_tendency(d, 0))) return rc;
     for (int n = 1; n <= ntr; ++n) {
       if ((rc = mom5gpu_horz_advect_tracer(d, n, taum1, tau, dtime))) return rc;
       if ((rc = mom5gpu_vert_advect_tracer(d, n, taum1, tau, dtime))) return rc;

@@ -353,7 +353,7 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
       }
       out = mk ? div_pair(Au::mul(rdz, Au::sub(tm, Tk)), a.dtime, rdt_h, rdt_l) : 0.0;
       double* th = a.th + n * g.n3;
-      th[p] = Au::add(th[p], out);
+      th[p] = a.th_fresh ? plus_zero(out) : Au::add(th[p], out);  // +0 + out == plus_zero(out)
       fprev[n][t] = fc;
     }
   }

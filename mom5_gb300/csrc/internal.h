@@ -147,6 +147,7 @@ struct MdflArgs {
   double* tx;                 // after x
   double* th;                 // th_tendency of tracer 0, tracer n at th + n*g.n3
   int tj = 0;                 // y-pass rows per thread (0 = choose from the domain size)
+  int th_fresh = 0;           // th is +0 at every compute cell: the y pass writes out + 0.0 instead of th + out
 };
 
 
@@ -215,8 +216,9 @@ int make_mix_args(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime
 // (at most 8 per call); scratch a.tz/a.tx and a.mask2 are the caller's.
 void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s);
 void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t s);
+void launch_zero_ring(const Geo& g, double* a, long nlev, cudaStream_t s);
 int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,
-                double sweby_limiter);
+                double sweby_limiter, bool th_fresh = false);
 int launch_upwind_horz(mom5gpu_domain* d, int n, int taum1);
 int launch_upwind_vert(mom5gpu_domain* d, int n, int taum1);
 int launch_quicker_horz(mom5gpu_domain* d, int n, int taum1, int tau);

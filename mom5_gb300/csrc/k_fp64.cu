@@ -51,6 +51,33 @@ void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t
   k_halo_fill<<<grid, 256, 0, s>>>(g, a, nlev, flags);
 }
 
+// zero the halo ring (i in {0, ni+1} or j in {0, nj+1}) of nlev data-domain levels
+__global__ void k_zero_ring(Geo g, double* a, long nlev) {
+  const long r = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long row = g.ni + 2;
+  if (r >= 2 * row + 2L * g.nj) return;
+  int i, j;
+  if (r < row) {
+    i = (int)r;
+    j = 0;
+  } else if (r < 2 * row) {
+    i = (int)(r - row);
+    j = g.nj + 1;
+  } else {
+    const long q = r - 2 * row;
+    i = q < g.nj ? 0 : g.ni + 1;
+    j = 1 + (int)(q % g.nj);
+  }
+  for (long k = blockIdx.y; k < nlev; k += gridDim.y) a[k * g.n2 + I2(g, i, j)] = 0.0;
+}
+
+void launch_zero_ring(const Geo& g, double* a, long nlev, cudaStream_t s) {
+  if (nlev <= 0) return;
+  const long nring = 2L * (g.ni + 2) + 2L * g.nj;
+  dim3 grid((unsigned)((nring + 255) / 256), (unsigned)(nlev < 1024 ? nlev : 1024));
+  k_zero_ring<<<grid, 256, 0, s>>>(g, a, nlev);
+}
+
 // ---------------------------------------------------------------------------
 // MDFL Sweby / DST-linear: ocean_tracer_advect.F90:3806-4066 (ALL = false) and
 // advect_tracer_sweby_all :4104-4511 (ALL = true).  Three passes with the
@@ -157,7 +184,7 @@ int make_mdfl_args(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, 
 }
 
 int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,
-                double sweby_limiter) {
+                double sweby_limiter, bool th_fresh) {
   // tracers per launch set: at most kMdflChunk, in chunks of equal size (the
   // tracer-independent face terms are computed once per chunk)
   int nchunks = (ntr + kMdflChunk - 1) / kMdflChunk;
@@ -170,6 +197,7 @@ int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, in
     MdflArgs a;
     rc = make_mdfl_args(d, n_first + c0, cn, taum1, tau, dtime, &a);
     if (rc) return rc;
+    a.th_fresh = th_fresh ? 1 : 0;
     count_launches(d, 3);
     run_mdfl_kernels(a, all, sweby_limiter != 0.0, d->stream);
   }
