@@ -77,7 +77,8 @@ DEVI void prep_body(const BtArgs& a, int bx, int by) {
   c[FV * n2 + q] = a.dtbt * a.forcing_v[q];
 }
 
-DEVI void pred_body(const BtArgs& a, int so, int sn, int bx, int by) {
+// with reuse, D of level so is the previous corrector's D of the same arrays (dvs)
+DEVI void pred_body(const BtArgs& a, int so, int sn, int reuse, int bx, int by) {
   const Geo& g = a.g;
   int i0 = bx * blockDim.x + threadIdx.x, j0 = by;
   if (i0 > g.ni + 1) return;
@@ -89,7 +90,7 @@ DEVI void pred_body(const BtArgs& a, int so, int sn, int bx, int by) {
   long q = I2(g, i, j), n2 = g.n2;
   double en = a.eta_bt[so * n2 + q];
   if (a.gamma > 0.0) {
-    double D = div_num(g, a.uhb + so * n2, a.vhb + so * n2, i, j);
+    double D = reuse ? a.dvs[q] : div_num(g, a.uhb + so * n2, a.vhb + so * n2, i, j);
     en = fma(a.btf[KG * n2 + q], D, en + a.btf[SG * n2 + q]);
   }
   long q0 = I2(g, i0, j0);
@@ -129,6 +130,7 @@ DEVI void corr_body(const BtArgs& a, int so, int sn, double wgt, int bx, int by)
   if (i > g.ni + 1) return;
   long q = I2(g, i, j), n2 = g.n2;
   double D = div_num(g, a.uhb + sn * n2, a.vhb + sn * n2, i, j);
+  a.dvs[q] = D;
   double en = fma(a.btf[KC * n2 + q], D, a.eta_bt[so * n2 + q] + a.btf[SC * n2 + q]);
   a.eta_bt[sn * n2 + q] = en;
   a.eta_bar[q] += en;

@@ -464,8 +464,10 @@ DEVI void bt_cgrid_init_body(BtArgs a, int bx, int by) {
   a.ca[n2 + q] = abm0 * c1 + abm1 * c1 + abm2 * c1;
 }
 
-// predictor + ps (both grids)
-DEVI void bt_pred_body(BtArgs a, int so, int sn, int bx, int by) {
+// predictor + ps (both grids).  With reuse the divergence of the transports at
+// level so is the one the previous subcycle's corrector formed from the same
+// arrays (its level sn), stored in dvs: the same values, read instead of formed.
+DEVI void bt_pred_body(BtArgs a, int so, int sn, int reuse, int bx, int by) {
   const Geo& g = a.g;
   int i0 = bx * blockDim.x + threadIdx.x;
   int j0 = by;
@@ -483,8 +485,9 @@ DEVI void bt_pred_body(BtArgs a, int so, int sn, int bx, int by) {
   long q = I2(g, i, j);
   double en;
   if (dpos(a.gamma)) {
-    double dv = a.cgrid ? div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j)
-                        : div_ud_bh(a, a.uhb + so * g.n2, a.vhb + so * g.n2, i, j);
+    double dv = reuse ? a.dvs[q]
+                      : (a.cgrid ? div_ud(a, a.ubt + so * g.n2, a.vbt + so * g.n2, i, j)
+                                 : div_ud_bh(a, a.uhb + so * g.n2, a.vhb + so * g.n2, i, j));
     double tm = a.tmask1[q];
     double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
     en = eo[q] + a.dtbt_gamma_rho0r * (tmp + a.steady[q]);
@@ -573,6 +576,7 @@ DEVI void bt_corr_body(BtArgs a, int so, int sn, double wgt, int bx, int by) {
   long q = I2(g, i, j);
   double dv = a.cgrid ? div_ud(a, a.ubt + sn * g.n2, a.vbt + sn * g.n2, i, j)
                       : div_ud_bh(a, a.uhb + sn * g.n2, a.vhb + sn * g.n2, i, j);
+  a.dvs[q] = dv;
   double tm = a.tmask1[q];
   double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
   double en = a.eta_bt[so * g.n2 + q] + a.dtbt_rho0r * (tmp + a.steady[q]);

@@ -173,9 +173,10 @@ struct BtArgs {
   double *eta_bar, *udrho_u, *udrho_v;  // taup1 accumulators
   double *uhb, *vhb;  // B grid: ubt*dyu and vbt*dxu, 2 levels like ubt (reuse the C-grid Coriolis planes)
   double* btf;        // precision form, B grid: folded step coefficients (bt_fast_body.cuh), else nullptr
+  double* dvs;        // divergence of the corrector's transports, reused by the next subcycle's predictor
 };
-// planes of barotropic scratch: 16 for the exact path, 9 more for the precision form
-constexpr int kBtPlanes = 16, kBtFastPlanes = 9;
+// planes of barotropic scratch: 17 for the exact path, 9 more for the precision form
+constexpr int kBtPlanes = 17, kBtFastPlanes = 9;
 struct BtExtra {
   const double *eta_bar_tau, *eta_tau, *ud_tau, *vd_tau, *pme, *river, *source, *eta_smooth;
   double *conv, *eta_u, *ps_out, *gxo, *gyo;
@@ -230,7 +231,7 @@ int launch_eta_tendency(mom5gpu_domain* d, int tau);
 int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
 // precision-form barotropic subcycle (k_mixed.cu, k_batch.cu)
 void launch_btf_prep(const BtArgs& a, cudaStream_t s);
-void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, cudaStream_t s);
+void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, bool reuse, cudaStream_t s);
 int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz);
 int ensure_kmt_device(mom5gpu_domain* d);
 int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
@@ -271,7 +272,8 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
                                   cudaStream_t s);
 // precision form: folded subcycle over the work list (k_batch.cu)
 void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s);
-void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, cudaStream_t s);
+void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, bool reuse,
+                               cudaStream_t s);
 void launch_batch_barotropic_post(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, int phase,
                                   cudaStream_t s);
 // precision form: persistent kernel over (entry, tile) items

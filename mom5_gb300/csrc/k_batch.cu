@@ -53,9 +53,9 @@ __global__ void __launch_bounds__(128) kb_btf_prep(const BtArgs* d, BatchWork w)
   BTF_ENTRY
   btfast::prep_body(a, bx, by);
 }
-__global__ void __launch_bounds__(128) kb_btf_pred(const BtArgs* d, BatchWork w, int so, int sn) {
+__global__ void __launch_bounds__(128) kb_btf_pred(const BtArgs* d, BatchWork w, int so, int sn, int reuse) {
   BTF_ENTRY
-  btfast::pred_body(a, so, sn, bx, by);
+  btfast::pred_body(a, so, sn, reuse, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_btf_mom(const BtArgs* d, BatchWork w, int so, int sn) {
   BTF_ENTRY
@@ -96,9 +96,10 @@ void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s)
   if (w.tb2 > 0) kb_btf_prep<<<w.tb2, 128, 0, s>>>(bt, w);
 }
 
-void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, cudaStream_t s) {
+void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, bool reuse,
+                               cudaStream_t s) {
   if (w.tb2 <= 0) return;
-  kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
+  kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, reuse);
   kb_btf_mom<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
   kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
 }

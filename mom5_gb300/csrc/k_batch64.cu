@@ -80,9 +80,9 @@ __global__ void __launch_bounds__(256) kb_bt_init(const BtArgs* d, const BtExtra
   int nb = (a.g.ni + 2 + 127) / 128;                 \
   int bx = local % nb, by = local / nb;
 
-__global__ void __launch_bounds__(128) kb_bt_pred(const BtArgs* d, BatchWork w, int so, int sn) {
+__global__ void __launch_bounds__(128) kb_bt_pred(const BtArgs* d, BatchWork w, int so, int sn, int reuse) {
   BT2D_ENTRY
-  bt_pred_body(a, so, sn, bx, by);
+  bt_pred_body(a, so, sn, reuse, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_bt_mom_b(const BtArgs* d, BatchWork w, int so, int sn) {
   BT2D_ENTRY
@@ -158,10 +158,10 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
   for (int itime = 1; itime <= nts; ++itime) {
     int so = (itime + 0) % 2, sn = (itime + 1) % 2;
     if (fast) {  // precision form: folded FP64 subcycle
-      launch_batch_btf_subcycle(bt, w, so, sn, (double)(nts - itime + 1), s);
+      launch_batch_btf_subcycle(bt, w, so, sn, (double)(nts - itime + 1), itime > 1, s);
       continue;
     }
-    kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
+    kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, itime > 1);
     kb_bt_mom_b<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
     kb_bt_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));
   }

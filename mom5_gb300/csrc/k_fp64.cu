@@ -1214,7 +1214,7 @@ __global__ void k_bt_init(BtArgs a, const double* eta_bar_tau, const double* eta
                           const double* vd_tau, const double* pme, const double* river, const double* source,
                           const double* eta_smooth, int initsum_with_bar) { bt_init_body(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, source, eta_smooth, initsum_with_bar, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_cgrid_init(BtArgs a) { bt_cgrid_init_body(a, blockIdx.x, blockIdx.y); }
-__global__ void k_bt_pred(BtArgs a, int so, int sn) { bt_pred_body(a, so, sn, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_pred(BtArgs a, int so, int sn, int reuse) { bt_pred_body(a, so, sn, reuse, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_mom_b(BtArgs a, int so, int sn) { bt_mom_b_body(a, so, sn, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_mom_c(BtArgs a, int so, int sn, int itime) { bt_mom_c_body(a, so, sn, itime, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) { bt_corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y); }
@@ -1271,6 +1271,7 @@ int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp)
   a.cf = d->bt + 8 * n2;
   a.ca = d->bt + 14 * n2;
   a.uhb = a.cgrid ? nullptr : d->bt + 8 * n2;
+  a.dvs = d->bt + 16 * n2;
   a.vhb = a.cgrid ? nullptr : d->bt + 10 * n2;
   a.btf = (!a.cgrid && d->opt.precision == MOM5GPU_PRECISION_MIXED) ? d->bt + kBtPlanes * n2 : nullptr;
   a.eta_bar = fptr(d, MOM5GPU_ETA_T_BAR, 0, taup1);
@@ -1328,10 +1329,10 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   for (int itime = 1; itime <= a.nts; ++itime) {
     int so = (itime + 0) % 2, sn = (itime + 1) % 2;
     if (a.btf) {  // precision form: folded FP64 subcycle
-      launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), s);
+      launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), itime > 1, s);
       continue;
     }
-    k_bt_pred<<<g2, 128, 0, s>>>(a, so, sn);
+    k_bt_pred<<<g2, 128, 0, s>>>(a, so, sn, itime > 1);
     if (!a.cgrid) {
       k_bt_mom_b<<<g2, 128, 0, s>>>(a, so, sn);
     } else {

@@ -72,8 +72,8 @@ int run_mixed(mom5gpu_domain* d, MixArgs a, int n0) {
 }  // namespace
 
 __global__ void __launch_bounds__(128) k_btf_prep(BtArgs a) { btfast::prep_body(a, blockIdx.x, blockIdx.y); }
-__global__ void __launch_bounds__(128) k_btf_pred(BtArgs a, int so, int sn) {
-  btfast::pred_body(a, so, sn, blockIdx.x, blockIdx.y);
+__global__ void __launch_bounds__(128) k_btf_pred(BtArgs a, int so, int sn, int reuse) {
+  btfast::pred_body(a, so, sn, reuse, blockIdx.x, blockIdx.y);
 }
 __global__ void __launch_bounds__(128) k_btf_mom(BtArgs a, int so, int sn) {
   btfast::mom_body(a, so, sn, blockIdx.x, blockIdx.y);
@@ -87,9 +87,9 @@ void launch_btf_prep(const BtArgs& a, cudaStream_t s) {
   k_btf_prep<<<g2, 128, 0, s>>>(a);
 }
 
-void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, cudaStream_t s) {
+void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, bool reuse, cudaStream_t s) {
   dim3 g2((a.g.ni + 2 + 127) / 128, a.g.nj + 2);
-  k_btf_pred<<<g2, 128, 0, s>>>(a, so, sn);
+  k_btf_pred<<<g2, 128, 0, s>>>(a, so, sn, reuse);
   k_btf_mom<<<g2, 128, 0, s>>>(a, so, sn);
   k_btf_corr<<<g2, 128, 0, s>>>(a, so, sn, wgt);
 }

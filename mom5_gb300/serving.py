@@ -67,7 +67,7 @@ def bytes_per_domain(ni, nj, nk, ntr, precision) -> int:
     f3 = 2 * ntr + ntr + 6  # tracers at 2 levels, th_tendency, tmask/u/v/w/rho_dzt x2/rho_dztr
     if precision == capi.PRECISION_FP64:
         f3 += 2 * ntr  # MDFL scratch
-    f2 = 60  # metrics, barotropic state and scratch
+    f2 = 61  # metrics, barotropic state and scratch
     return 8 * (f3 * n3 + f2 * n2) + (ni + 4) * (nj + 4) * nk
 
 
