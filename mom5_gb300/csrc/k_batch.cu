@@ -22,7 +22,8 @@ DEVI int find_entry_m(const int* prefix, int count, int b) {
 }
 
 template <int NC, int ZR>
-__global__ void __launch_bounds__(NT, ZR == 16 ? 4 : 2) kb_mixed(const MixArgs* d, BatchWork w, int* counter) {
+__global__ void __launch_bounds__(tile_threads(ZR), ZR == 16 ? 4 : 2) kb_mixed(const MixArgs* d, BatchWork w,
+                                                                              int* counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
   __shared__ int item;
@@ -37,7 +38,7 @@ __global__ void __launch_bounds__(NT, ZR == 16 ? 4 : 2) kb_mixed(const MixArgs* 
     const MixArgs& a = d[w.entries[e]];
     int local = it - w.pm[e];
     int ntx = (a.g.ni + TI - 1) / TI;
-    mixed_tile<NC, ZR>(a, 0, local % ntx, local / ntx, s);
+    mixed_tile<NC, ZR, false, tile_threads(ZR)>(a, 0, local % ntx, local / ntx, s);
   }
 }
 
@@ -78,7 +79,7 @@ template <int NC, int ZR>
 int run(const MixArgs* m, const BatchWork& w, int blocks, int* counter, cudaStream_t s) {
   size_t smem = sizeof(SmemT<ZR>);
   cudaMemsetAsync(counter, 0, sizeof(int), s);
-  kb_mixed<NC, ZR><<<blocks, NT, smem, s>>>(m, w, counter);
+  kb_mixed<NC, ZR><<<blocks, tile_threads(ZR), smem, s>>>(m, w, counter);
   return MOM5GPU_OK;
 }
 

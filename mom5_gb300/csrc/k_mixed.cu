@@ -1,10 +1,11 @@
 // Precision form of MDFL Sweby: fluxes and limiters in FP32, tracer state in FP64.
 //
 // One fused kernel does the z, x and y passes of advect_tracer_mdfl_sweby
-// (ocean_tracer_advect.F90:3806-4066) for a 28x28 tile of columns, marching
-// down k, with the tile's 2-cell halo recomputed instead of exchanged: the
-// z pass runs on the 32x32 tile-plus-halo, the x pass on 32 rows x 28 columns,
-// the y pass on the 28x28 interior.  Face terms (mass flux, Courant number,
+// (ocean_tracer_advect.F90:3806-4066) for a tile of 28 columns by ZR-4 rows
+// (ZR = 16, 24 or 32, autotuned), marching down k, with the tile's 2-cell halo
+// recomputed instead of exchanged: the z pass runs on the 32 x ZR
+// tile-plus-halo, the x pass on ZR rows x 28 columns, the y pass on the
+// interior.  Face terms (mass flux, Courant number,
 // d0, d1, the limiter slope) are computed once per level and shared by every
 // tracer of the launch.
 //
@@ -35,12 +36,13 @@ constexpr size_t mixed_smem() {
 }
 
 template <int NC, int ZR, bool PF>
-__global__ void __launch_bounds__(NT, PF ? 2 : (ZR == 16 ? 4 : ZR == 24 ? 3 : 2)) k_mdfl_mixed(MixArgs a, int n0) {
+__global__ void __launch_bounds__(tile_threads(ZR), PF ? 2 : (ZR == 16 ? 4 : ZR == 24 ? 3 : 2))
+    k_mdfl_mixed(MixArgs a, int n0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
   PrefetchT<ZR>* pf =
       PF ? reinterpret_cast<PrefetchT<ZR>*>(smem_raw + ((sizeof(SmemT<ZR>) + 15) & ~(size_t)15)) : nullptr;
-  mixed_tile<NC, ZR, PF>(a, n0, blockIdx.x, blockIdx.y, s, pf);
+  mixed_tile<NC, ZR, PF, tile_threads(ZR)>(a, n0, blockIdx.x, blockIdx.y, s, pf);
 }
 
 template <int NC, int ZR, bool PF>
@@ -56,7 +58,7 @@ int run_mixed_zr(mom5gpu_domain* d, MixArgs a, int n0) {
   }
   constexpr int TJ = ZR - 4;
   dim3 grid((g.ni + TI - 1) / TI, (g.nj + TJ - 1) / TJ);
-  k_mdfl_mixed<NC, ZR, PF><<<grid, NT, smem, d->stream>>>(a, n0);
+  k_mdfl_mixed<NC, ZR, PF><<<grid, tile_threads(ZR), smem, d->stream>>>(a, n0);
   count_launches(d, 1);
   return MOM5GPU_OK;
 }

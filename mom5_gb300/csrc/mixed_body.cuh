@@ -17,6 +17,10 @@ constexpr int TI = ZW - 4;   // interior width
 constexpr int NT = 256;      // threads
 constexpr int NW = NT / 32;  // warps
 // ZR (template): tile height incl. halo; interior height ZR - 4
+// Threads per block of a tile height: 8 warps, 16 for the 32-row tile, so that
+// every shape holds two tile rows per thread and two blocks of the tallest
+// tile still give 32 warps per SM.
+__host__ __device__ constexpr int tile_threads(int ZR) { return ZR == 32 ? 512 : NT; }
 
 DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
 DEVI long I3(const Geo& g, int i, int j, int k) { return (long)k * g.n2 + (long)j * g.nxd + i; }
@@ -108,10 +112,12 @@ struct PrefetchT {
   double tb[2][4][ZR * ZW];
 };
 
-template <int NC, int ZR, bool PF = false>
+template <int NC, int ZR, bool PF = false, int NTH = NT>
 DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>& s, PrefetchT<ZR>* pf = nullptr) {
   constexpr int TJ = ZR - 4;
-  constexpr int ROWS_PER_WARP = ZR / NW;
+  constexpr int NWT = NTH / 32;  // warps of the block; tile row zj belongs to warp zj % NWT
+  static_assert(ZR % NWT == 0, "tile height must be a multiple of the warps per block");
+  constexpr int ROWS_PER_WARP = ZR / NWT;
   const Geo& g = a.g;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i0 = 1 + tile_x * TI, j0 = 1 + tile_y * TJ;
@@ -121,7 +127,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
   int offr[ROWS_PER_WARP];
 #pragma unroll
   for (int m = 0; m < ROWS_PER_WARP; ++m) {
-    int i = i0 - 2 + lane, j = j0 - 2 + warp + NW * m;
+    int i = i0 - 2 + lane, j = j0 - 2 + warp + NWT * m;
     offr[m] = image(g, i, j) ? (int)I2(g, i, j) : -1;
   }
   // queue the four levels of tracer n into prefetch buffer b (zeros outside a wall)
@@ -130,7 +136,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
     const int lev[4] = {km1, k, kp1, kp2};
 #pragma unroll
     for (int m = 0; m < ROWS_PER_WARP; ++m) {
-      const int c = (warp + NW * m) * ZW + lane, o = offr[m];
+      const int c = (warp + NWT * m) * ZW + lane, o = offr[m];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const double* src = o >= 0 ? T + (long)lev[q] * g.n2 + o : T;
@@ -140,7 +146,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
     cp_async_commit();
   };
 
-  // per-thread z columns: zi = lane, zj = warp + NW*m
+  // per-thread z columns: zi = lane, zj = warp + NWT*m
   float ftp[NC][ROWS_PER_WARP];
 #pragma unroll
   for (int n = 0; n < NC; ++n)
@@ -156,7 +162,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
     // ---- level terms: z columns, x faces/cells, y faces ----
 #pragma unroll
     for (int m = 0; m < ROWS_PER_WARP; ++m) {
-      const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+      const int zj = warp + NWT * m, zi = lane, c = zj * ZW + zi;
       int i = i0 - 2 + zi, j = j0 - 2 + zj;
       const int pi = i, pj = j;
       bool in = image(g, i, j);
@@ -264,7 +270,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
       float tkr[ROWS_PER_WARP], fzr[ROWS_PER_WARP], fir[ROWS_PER_WARP];
 #pragma unroll
       for (int m = 0; m < ROWS_PER_WARP; ++m) {
-        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        const int zj = warp + NWT * m, zi = lane, c = zj * ZW + zi;
         // ---- z pass ----
         const int o = s.off[c];
         const uint8_t mb = s.zmask[c];
@@ -325,7 +331,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
       // ---- y fluxes: face zj (between rows zj and zj+1), zj = 1..29, zi = 2..29 ----
 #pragma unroll
       for (int m = 0; m < ROWS_PER_WARP; ++m) {
-        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        const int zj = warp + NWT * m, zi = lane, c = zj * ZW + zi;
         float f = 0.f;
         if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3) {
           bool m0 = s.zmask[c - ZW] & 2, m1 = s.zmask[c] & 2, m2 = s.zmask[c + ZW] & 2, m3 = s.zmask[c + 2 * ZW] & 2;
@@ -343,7 +349,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
       // ---- interior: total increment and output ----
 #pragma unroll
       for (int m = 0; m < ROWS_PER_WARP; ++m) {
-        const int zj = warp + NW * m, zi = lane, c = zj * ZW + zi;
+        const int zj = warp + NWT * m, zi = lane, c = zj * ZW + zi;
         if (zj < 2 || zj > ZR - 3 || zi < 2 || zi > ZW - 3) continue;
         const int i = i0 - 2 + zi, j = j0 - 2 + zj;
         if (i > g.ni || j > g.nj) continue;
