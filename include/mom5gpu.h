@@ -282,13 +282,13 @@ int mom5gpu_update_tracer(mom5gpu_domain* d, int n, int taum1, int taup1, double
  * halo update. */
 int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime);
 /* Time the candidate launch shapes of mom5gpu_tracer_advection_step on this
- * domain (precision form: tile height 32 or 16 rows; FP64: y-pass rows per
+ * domain (precision form: tile height 16, 24, 32 or 64 rows; FP64: y-pass rows per
  * thread 2..16) and keep the fastest.  The trials step taum1 = tau = 1 to
  * taup1 = 2: time level 2 of the tracers and th_tendency are overwritten.
  * A summary is written to report (may be NULL). */
 int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len);
 /* The launch shape autotune chose, or one to pin: precision-form tile height
- * (16, 24 or 32 rows incl. halo), tracer prefetch into shared memory (height 16
+ * (16, 24, 32 or 64 rows incl. halo), tracer prefetch into shared memory (height 16
  * only), FP64 y-pass rows per thread (0 = built-in choice, 2, 4, 8, 16).
  * Every shape gives the same results bit for bit. */
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);

@@ -837,9 +837,9 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
 
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj) {
   if (!d) return MOM5GPU_EINVAL;
-  if ((rows != 16 && rows != 24 && rows != 32) || (prefetch && rows != 16) ||
+  if ((rows != 16 && rows != 24 && rows != 32 && rows != 64) || (prefetch && rows != 16) ||
       !(tj == 0 || tj == 2 || tj == 4 || tj == 8 || tj == 16))
-    return fail(d, MOM5GPU_EINVAL, "set_tuning: rows 16|24|32 (prefetch only with 16), tj 0|2|4|8|16");
+    return fail(d, MOM5GPU_EINVAL, "set_tuning: rows 16|24|32|64 (prefetch only with 16), tj 0|2|4|8|16");
   d->tune_mixed_rows = rows;
   d->tune_mixed_pf = prefetch ? 1 : 0;
   d->tune_y_tj = tj;
@@ -859,10 +859,10 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   if (!d->advect_ready) return fail(d, MOM5GPU_ESTATE, "autotune before mom5gpu_tracer_advect_init");
   bool mixed = d->opt.precision == MOM5GPU_PRECISION_MIXED;
   // candidate launch shapes: precision-form tile height (and tracer prefetch); FP64 y-pass rows per thread
-  const int kRows[] = {32, 24, 16, 16};
-  const int kPf[] = {0, 0, 0, 1};
+  const int kRows[] = {32, 64, 24, 16, 16};
+  const int kPf[] = {0, 0, 0, 0, 1};
   const int kTj[] = {2, 4, 8, 16};
-  int ncand = 4;
+  int ncand = mixed ? 5 : 4;
   cudaEvent_t t0, t1;
   if (cudaEventCreate(&t0) != cudaSuccess) return fail(d, MOM5GPU_ECUDA, "autotune events");
   if (cudaEventCreate(&t1) != cudaSuccess) {

@@ -106,7 +106,7 @@ struct mom5gpu_domain {
   long clock_calls[8] = {0};
   long launches = 0;
   // autotuned launch shapes (0 = built-in heuristic)
-  int tune_mixed_rows = 32;  // precision-form tile height incl. halo: 32, 24 or 16
+  int tune_mixed_rows = 32;  // precision-form tile height incl. halo: 16, 24, 32 or 64
   int tune_mixed_pf = 0;     // precision form, height 16: tracer levels prefetched into shared memory
   int tune_y_tj = 0;         // FP64 y-pass rows per thread
 };

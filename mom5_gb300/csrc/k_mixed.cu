@@ -36,7 +36,7 @@ constexpr size_t mixed_smem() {
 }
 
 template <int NC, int ZR, bool PF>
-__global__ void __launch_bounds__(tile_threads(ZR), PF ? 2 : (ZR == 16 ? 4 : ZR == 24 ? 3 : 2))
+__global__ void __launch_bounds__(tile_threads(ZR), PF ? 2 : (ZR == 16 ? 4 : ZR == 24 ? 3 : ZR == 64 ? 1 : 2))
     k_mdfl_mixed(MixArgs a, int n0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemT<ZR>& s = *reinterpret_cast<SmemT<ZR>*>(smem_raw);
@@ -68,6 +68,7 @@ int run_mixed(mom5gpu_domain* d, MixArgs a, int n0) {
   if (d->tune_mixed_rows == 16)
     return d->tune_mixed_pf ? run_mixed_zr<NC, 16, true>(d, a, n0) : run_mixed_zr<NC, 16, false>(d, a, n0);
   if (d->tune_mixed_rows == 24) return run_mixed_zr<NC, 24, false>(d, a, n0);
+  if (d->tune_mixed_rows == 64) return run_mixed_zr<NC, 64, false>(d, a, n0);
   return run_mixed_zr<NC, 32, false>(d, a, n0);
 }
 

@@ -17,10 +17,10 @@ constexpr int TI = ZW - 4;   // interior width
 constexpr int NT = 256;      // threads
 constexpr int NW = NT / 32;  // warps
 // ZR (template): tile height incl. halo; interior height ZR - 4
-// Threads per block of a tile height: 8 warps, 16 for the 32-row tile, so that
-// every shape holds two tile rows per thread and two blocks of the tallest
-// tile still give 32 warps per SM.
-__host__ __device__ constexpr int tile_threads(int ZR) { return ZR == 32 ? 512 : NT; }
+// Threads per block of a tile height: 8 warps, 16 for the 32-row tile and 32
+// for the 64-row tile, so that every shape holds two tile rows per thread and
+// the tall tiles still give 32 warps per SM (two blocks of 32 rows, one of 64).
+__host__ __device__ constexpr int tile_threads(int ZR) { return ZR == 64 ? 1024 : ZR == 32 ? 512 : NT; }
 
 DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
 DEVI long I3(const Geo& g, int i, int j, int k) { return (long)k * g.n2 + (long)j * g.nxd + i; }

@@ -129,7 +129,7 @@ def test_mixed_multi_tile_and_partial_tiles(gpu_lib, case):
 
 @pytest.mark.parametrize("case", [(False, False, 61, 45, 10), (True, True, 30, 29, 3), (True, False, 57, 30, 1)])
 def test_precision_form_launch_shapes_agree(gpu_lib, case):
-    """Every launch shape of the precision form (tile height 32, 24, 16, 16 with the
+    """Every launch shape of the precision form (tile height 32, 64, 24, 16, 16 with the
     tracer prefetch through cp.async) gives the same tracers bit for bit."""
     capi = gpu_lib
     from mom5_gb300 import harness
@@ -138,7 +138,7 @@ def test_precision_form_launch_shapes_agree(gpu_lib, case):
                          cyclic_y=cy, continent=(10, 8, 5, 6), wavelength_cells=6.0, ntracers=ntr, seed=ni + 1)
     dom = grid.make_domain(sp)
     out = {}
-    for shape in ((32, 0, 0), (24, 0, 0), (16, 0, 0), (16, 1, 0)):
+    for shape in ((32, 0, 0), (64, 0, 0), (24, 0, 0), (16, 0, 0), (16, 1, 0)):
         d = harness.load(dom, options=capi.default_options(precision=capi.PRECISION_MIXED))
         d.tuning = shape
         assert d.tuning == shape
