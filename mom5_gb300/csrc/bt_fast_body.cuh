@@ -1,34 +1,52 @@
 // Barotropic subcycle of the precision form (B grid): the same predictor,
 // momentum and corrector as pred_corr_tropic_depth_bgrid
-// (ocean_barotropic.F90:3255-3575), in FP64 but with the step constants folded
-// into per-column coefficients once per baroclinic step and the products
-// contracted into FMAs.  The result is FP64-accurate (not bit-identical to the
-// reference order); the exact drop-in keeps the bodies of fp64_bodies.cuh.
-// Included by translation units built with FMA contraction on.
+// (ocean_barotropic.F90:3255-3575) with the state (eta, udrho, the transports
+// u*dyu, v*dxu and the time sums) in FP64 and each subcycle's increments in
+// FP32, the form's "FP32 fluxes, FP64 state" split.  The exact drop-in keeps
+// the bodies of fp64_bodies.cuh.
 //
-// Coefficients (planes of BtArgs::btf, each (ni+2)(nj+2)):
-//   KG = -dtbt_gamma_rho0r*tmask*datr   SG = dtbt_gamma_rho0r*steady   (predictor)
-//   KC = -dtbt_rho0r*tmask*datr         SC = dtbt_rho0r*steady         (corrector)
+// Step coefficients, FP32 planes of BtArgs::btf (each (ni+2)(nj+2) floats),
+// formed in FP64 once per baroclinic step and rounded to FP32:
+//   KG = -dtbt_gamma_rho0r*tmask*datr/2   SG = dtbt_gamma_rho0r*steady   (predictor)
+//   KC = -dtbt_rho0r*tmask*datr/2         SC = dtbt_rho0r*steady         (corrector)
 //   A  = dtbt*f/2
 //   BX = -dtbt*thicku*dxur*umask/2, BY = -dtbt*thicku*dyur*umask/2 on compute
 //        points (0 elsewhere: no pressure gradient there)
 //   FU = dtbt*forcing_u, FV = dtbt*forcing_v
-// so that, with D the undivided DIV_UD numerator and P the undivided corner
-// differences of ps,
-//   eta(new) = eta(old) + S + K*D
-//   u(new)   = cori2*(t1 + cori1*t2), t1 = u + A*v + BX*Px + FU, t2 = v - A*u + BY*Py + FV.
+//   G1 = cori2 - 1, G2 = cori2*cori1            (the Coriolis rotation as an increment)
+//   PX = BX*Px(patm + rho_g*E), PY = BY*Py(patm + rho_g*E)
+//        (the pressure gradient of the step's initial surface E, an FP64 plane)
+//   RG = rho_g
+// With D the undivided DIV_UD numerator of the transports and Px, Py the
+// undivided corner differences of rho_g*(eta - E) (a float plane PS written by
+// the predictor: the departure from E, small, keeps its FP32 rounding small
+// against the gradient), a subcycle is
+//   eta(new) = eta(old) + [S + K*D]
+//   u(new)   = u + [d1 + G1*t1 + G2*t2],  v(new) = v + [d2 + G1*t2 - G2*t1]
+//   d1 = A*v + BX*Px + PX + FU,  d2 = -A*u + BY*Py + PY + FV,  t1 = u + d1,  t2 = v + d2
+// (algebraically u(new) = cori2*(t1 + cori1*t2), v(new) = cori2*(t2 - cori1*t1)),
+// the brackets in FP32 and each added to the FP64 state with one FP64 add.  D
+// is formed from four FP64 differences of neighbouring transports summed in
+// FP32.  The increments are small against the state (Coriolis and pressure
+// terms of one short subcycle), so their FP32 rounding stays near 1e-7 of the
+// increment and far below the form's 1e-6 bound on the state.
 #pragma once
 
 #include "internal.h"
+#include "mixed_body.cuh"
 
 namespace mom5 {
 namespace btfast {
 
 #define DEVI __device__ __forceinline__
 
-enum { KG = 0, SG, KC, SC, A, BX, BY, FU, FV, NPLANES };
+enum { KG = 0, SG, KC, SC, A, BX, BY, FU, FV, G1, G2, PX, PY, RG, PS, DV, E0, E1, NPLANES };
+static_assert(NPLANES <= 2 * kBtFastPlanes, "float planes of the precision-form subcycle");
 
 DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
+DEVI float* plane(const BtArgs& a, int p) { return reinterpret_cast<float*>(a.btf) + (long)p * a.g.n2; }
+// E: the FP64 plane over float planes E0, E1 (8-byte aligned: n2 floats per plane, E0 even)
+DEVI double* eref(const BtArgs& a) { return reinterpret_cast<double*>(plane(a, E0)); }
 
 // same rule as the exact path: a halo point takes its periodic image's value
 // when the single-PE halo update would copy it, else it keeps its own
@@ -49,35 +67,53 @@ DEVI bool halo_image(const Geo& g, int& i, int& j) {
   return true;
 }
 
-// undivided DIV_UD numerator from the stored products uh = u*dyu, vh = v*dxu
-// (the backward averages' 1/2 is folded into the coefficients K)
-DEVI double div_num(const Geo& g, const double* uh, const double* vh, int i, int j) {
-  if (i < 1 || j < 1) return 0.0;
+// undivided DIV_UD numerator from the stored transports uh = u*dyu, vh = v*dxu
+// (the backward averages' 1/2 is folded into K): four FP64 differences of
+// neighbours, rounded to FP32 and summed
+DEVI float div_num(const Geo& g, const double* uh, const double* vh, int i, int j) {
+  if (i < 1 || j < 1) return 0.0f;
   long q = I2(g, i, j), qw = q - 1, qs = q - g.nxd, qsw = qs - 1;
-  return ((uh[q] + uh[qs]) - (uh[qw] + uh[qsw])) + ((vh[q] + vh[qw]) - (vh[qs] + vh[qsw]));
+  float d1 = mixed::d2f_rn(uh[q] - uh[qw]), d2 = mixed::d2f_rn(uh[qs] - uh[qsw]);
+  float d3 = mixed::d2f_rn(vh[q] - vh[qs]), d4 = mixed::d2f_rn(vh[qw] - vh[qsw]);
+  return (d1 + d2) + (d3 + d4);
 }
 
 DEVI void prep_body(const BtArgs& a, int bx, int by) {
   const Geo& g = a.g;
   int i = bx * blockDim.x + threadIdx.x, j = by;
   if (i > g.ni + 1) return;
-  long q = I2(g, i, j), n2 = g.n2;
-  double* c = a.btf;
+  long q = I2(g, i, j);
   double tmd = a.tmask1[q] * a.datr[q];
-  c[KG * n2 + q] = -a.dtbt_gamma_rho0r * tmd * 0.5;
-  c[SG * n2 + q] = a.dtbt_gamma_rho0r * a.steady[q];
-  c[KC * n2 + q] = -a.dtbt_rho0r * tmd * 0.5;
-  c[SC * n2 + q] = a.dtbt_rho0r * a.steady[q];
-  c[A * n2 + q] = a.dtbt * a.f[q] * 0.5;
+  plane(a, KG)[q] = (float)(-a.dtbt_gamma_rho0r * tmd * 0.5);
+  plane(a, SG)[q] = (float)(a.dtbt_gamma_rho0r * a.steady[q]);
+  plane(a, KC)[q] = (float)(-a.dtbt_rho0r * tmd * 0.5);
+  plane(a, SC)[q] = (float)(a.dtbt_rho0r * a.steady[q]);
+  plane(a, A)[q] = (float)(a.dtbt * a.f[q] * 0.5);
   bool comp = i <= g.ni && j <= g.nj;
   double th = a.dtbt * a.thicku[q] * a.umask1[q] * 0.5;
-  c[BX * n2 + q] = comp ? -th * a.dxur[q] : 0.0;
-  c[BY * n2 + q] = comp ? -th * a.dyur[q] : 0.0;
-  c[FU * n2 + q] = a.dtbt * a.forcing_u[q];
-  c[FV * n2 + q] = a.dtbt * a.forcing_v[q];
+  double bxq = comp ? -th * a.dxur[q] : 0.0, byq = comp ? -th * a.dyur[q] : 0.0;
+  plane(a, BX)[q] = (float)bxq;
+  plane(a, BY)[q] = (float)byq;
+  plane(a, FU)[q] = (float)(a.dtbt * a.forcing_u[q]);
+  plane(a, FV)[q] = (float)(a.dtbt * a.forcing_v[q]);
+  plane(a, G1)[q] = (float)(a.cori2[q] - 1.0);
+  plane(a, G2)[q] = (float)(a.cori2[q] * a.cori1[q]);
+  // E = eta_bt at the first subcycle's old level (eta_t_bar(tau), set by the init kernel)
+  const double* e = a.eta_bt + g.n2;
+  eref(a)[q] = e[q];
+  double pxa = 0.0, pya = 0.0;
+  if (comp) {
+    auto P = [&](long r) { return a.patm[r] + a.rho_g[r] * e[r]; };
+    double p00 = P(q), p10 = P(q + 1), p01 = P(q + g.nxd), p11 = P(q + g.nxd + 1);
+    pxa = bxq * ((p10 + p11) - (p00 + p01));
+    pya = byq * ((p01 + p11) - (p00 + p10));
+  }
+  plane(a, PX)[q] = (float)pxa;
+  plane(a, PY)[q] = (float)pya;
+  plane(a, RG)[q] = (float)a.rho_g[q];
 }
 
-// with reuse, D of level so is the previous corrector's D of the same arrays (dvs)
+// with reuse, D of level so is the previous corrector's D of the same arrays
 DEVI void pred_body(const BtArgs& a, int so, int sn, int reuse, int bx, int by) {
   const Geo& g = a.g;
   int i0 = bx * blockDim.x + threadIdx.x, j0 = by;
@@ -90,12 +126,12 @@ DEVI void pred_body(const BtArgs& a, int so, int sn, int reuse, int bx, int by) 
   long q = I2(g, i, j), n2 = g.n2;
   double en = a.eta_bt[so * n2 + q];
   if (a.gamma > 0.0) {
-    double D = reuse ? a.dvs[q] : div_num(g, a.uhb + so * n2, a.vhb + so * n2, i, j);
-    en = fma(a.btf[KG * n2 + q], D, en + a.btf[SG * n2 + q]);
+    float D = reuse ? plane(a, DV)[q] : div_num(g, a.uhb + so * n2, a.vhb + so * n2, i, j);
+    en += mixed::f2d(fmaf(plane(a, KG)[q], D, plane(a, SG)[q]));
   }
   long q0 = I2(g, i0, j0);
   a.eta_bt[sn * n2 + q0] = en;
-  a.ps[q0] = fma(a.rho_g[q0], en, a.patm[q0]);
+  plane(a, PS)[q0] = plane(a, RG)[q0] * mixed::d2f_rn(en - eref(a)[q0]);
 }
 
 DEVI void mom_body(const BtArgs& a, int so, int sn, int bx, int by) {
@@ -103,21 +139,20 @@ DEVI void mom_body(const BtArgs& a, int so, int sn, int bx, int by) {
   int i = bx * blockDim.x + threadIdx.x, j = by;
   if (i > g.ni + 1) return;
   long q = I2(g, i, j), n2 = g.n2;
-  const double* c = a.btf;
-  double px = 0.0, py = 0.0;
+  float px = 0.0f, py = 0.0f;
   if (i <= g.ni && j <= g.nj) {
-    const double* ps = a.ps;
-    double p00 = ps[q], p10 = ps[q + 1], p01 = ps[q + g.nxd], p11 = ps[q + g.nxd + 1];
+    const float* ps = plane(a, PS);
+    float p00 = ps[q], p10 = ps[q + 1], p01 = ps[q + g.nxd], p11 = ps[q + g.nxd + 1];
     px = (p10 + p11) - (p00 + p01);
     py = (p01 + p11) - (p00 + p10);
   }
   double uo = a.ubt[so * n2 + q], vo = a.vbt[so * n2 + q];
-  double hf = c[A * n2 + q];
-  double t1 = uo + fma(hf, vo, fma(c[BX * n2 + q], px, c[FU * n2 + q]));
-  double t2 = vo + fma(-hf, uo, fma(c[BY * n2 + q], py, c[FV * n2 + q]));
-  double c1 = a.cori1[q], c2 = a.cori2[q];
-  double un = c2 * fma(c1, t2, t1);
-  double vn = c2 * fma(-c1, t1, t2);
+  float uf = mixed::d2f_rn(uo), vf = mixed::d2f_rn(vo), hf = plane(a, A)[q];
+  float d1 = fmaf(hf, vf, fmaf(plane(a, BX)[q], px, plane(a, PX)[q] + plane(a, FU)[q]));
+  float d2 = fmaf(-hf, uf, fmaf(plane(a, BY)[q], py, plane(a, PY)[q] + plane(a, FV)[q]));
+  float t1 = uf + d1, t2 = vf + d2, g1 = plane(a, G1)[q], g2 = plane(a, G2)[q];
+  double un = uo + mixed::f2d(d1 + fmaf(g1, t1, g2 * t2));
+  double vn = vo + mixed::f2d(d2 + fmaf(g1, t2, -g2 * t1));
   a.ubt[sn * n2 + q] = un;
   a.vbt[sn * n2 + q] = vn;
   a.uhb[sn * n2 + q] = un * a.dyu[q];
@@ -129,9 +164,9 @@ DEVI void corr_body(const BtArgs& a, int so, int sn, double wgt, int bx, int by)
   int i = bx * blockDim.x + threadIdx.x, j = by;
   if (i > g.ni + 1) return;
   long q = I2(g, i, j), n2 = g.n2;
-  double D = div_num(g, a.uhb + sn * n2, a.vhb + sn * n2, i, j);
-  a.dvs[q] = D;
-  double en = fma(a.btf[KC * n2 + q], D, a.eta_bt[so * n2 + q] + a.btf[SC * n2 + q]);
+  float D = div_num(g, a.uhb + sn * n2, a.vhb + sn * n2, i, j);
+  plane(a, DV)[q] = D;
+  double en = a.eta_bt[so * n2 + q] + mixed::f2d(fmaf(plane(a, KC)[q], D, plane(a, SC)[q]));
   a.eta_bt[sn * n2 + q] = en;
   a.eta_bar[q] += en;
   double un = a.ubt[sn * n2 + q], vn = a.vbt[sn * n2 + q];

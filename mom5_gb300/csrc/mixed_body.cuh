@@ -34,6 +34,9 @@ DEVI float d2f(double x) {
   if (mag >= (1151u << 20)) return __uint_as_float(sign | 0x7f800000u);
   return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
 }
+// FP64 -> FP32 rounded to nearest (ties away from zero): half an FP32 ulp added
+// to the bit pattern, then truncated.
+DEVI float d2f_rn(double x) { return d2f(__longlong_as_double(__double_as_longlong(x) + (1LL << 28))); }
 // FP32 -> FP64, exact, with integer operations (subnormal floats read as zero).
 DEVI double f2d(float f) {
   unsigned b = __float_as_uint(f);

