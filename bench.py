@@ -77,8 +77,8 @@ TRAFFIC_PER_TRACER_CELL = {"fp64": 5.199e9 / (360 * 270 * 50 * 10), "mixed": 0.9
 # FP64 thread-instructions per tracer-cell of the exact MDFL passes (z + x + y) and per
 # column of one exact barotropic subcycle, from ncu (profiles/fp64_ops_c2block.md); the
 # FP64 rate of GB300 measured on this machine with a probe kernel.
-FP64_OPS_PER_TRACER_CELL = 63.4
-FP64_OPS_PER_COLUMN_SUBCYCLE = 60.6
+FP64_OPS_PER_TRACER_CELL = 62.4
+FP64_OPS_PER_COLUMN_SUBCYCLE = 52.8
 FP64_PEAK_OPS = 5.05e11
 
 
