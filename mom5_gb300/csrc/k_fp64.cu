@@ -10,6 +10,7 @@
 // 1.7 instructions per clock per SM against ~119 for FP32.
 #include <math.h>
 #include <stdio.h>
+#include <string.h>
 
 #include "internal.h"
 #include "fp64_bodies.cuh"
@@ -1226,6 +1227,7 @@ int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp)
   if (!d->baro_ready) return fail(d, MOM5GPU_ESTATE, "update_ocean_barotropic before mom5gpu_barotropic_init");
   BtArgs& a = *ap;
   BtExtra& x = *xp;
+  memset(&a, 0, sizeof(BtArgs));  // padding too: the bytes key the subcycle graph
   a.g = g;
   a.cgrid = d->dims.horz_grid == MOM5GPU_CGRID;
   a.nts = d->nts;
@@ -1302,6 +1304,38 @@ int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp)
   return MOM5GPU_OK;
 }
 
+// Replays the domain's graph of the subcycle loop when it was captured with the
+// same BtArgs bytes, else captures enqueue(stream) into a new graph and launches
+// it.  Returns false (nothing enqueued) when the stream cannot be captured (the
+// caller then launches directly).
+template <class F>
+bool replay_subcycle_graph(mom5gpu_domain* d, const BtArgs& a, F&& enqueue) {
+  const unsigned char* key = reinterpret_cast<const unsigned char*>(&a);
+  bool same = d->bt_graph && d->bt_graph_key.size() == sizeof(BtArgs) &&
+              memcmp(d->bt_graph_key.data(), key, sizeof(BtArgs)) == 0;
+  if (!same) {
+    if (d->bt_graph) cudaGraphExecDestroy(d->bt_graph);
+    d->bt_graph = nullptr;
+    d->bt_graph_key.clear();
+    if (cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    enqueue(d->stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
+    if (e == cudaSuccess && graph) e = cudaGraphInstantiate(&d->bt_graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess || !d->bt_graph) {
+      d->bt_graph = nullptr;
+      cudaGetLastError();
+      return false;
+    }
+    d->bt_graph_key.assign(key, key + sizeof(BtArgs));
+  }
+  return cudaGraphLaunch(d->bt_graph, d->stream) == cudaSuccess;
+}
+
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   const Geo& g = d->geo;
   BtArgs a;
@@ -1326,22 +1360,27 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
     k_bt_cgrid_init<<<gc, 128, 0, s>>>(a);
   }
   if (a.btf) launch_btf_prep(a, s);
-  for (int itime = 1; itime <= a.nts; ++itime) {
-    int so = (itime + 0) % 2, sn = (itime + 1) % 2;
-    if (a.btf) {  // precision form: folded FP64 subcycle
-      launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), itime > 1, s);
-      continue;
+  // the nts subcycles (3 to 5 launches each, all arguments in a): one CUDA graph,
+  // captured on first use and replayed while a is unchanged
+  auto subcycles = [&](cudaStream_t st) {
+    for (int itime = 1; itime <= a.nts; ++itime) {
+      int so = (itime + 0) % 2, sn = (itime + 1) % 2;
+      if (a.btf) {  // precision form: FP32 increments
+        launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), itime > 1, st);
+        continue;
+      }
+      k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, itime > 1);
+      if (!a.cgrid) {
+        k_bt_mom_b<<<g2, 128, 0, st>>>(a, so, sn);
+      } else {
+        k_bt_mom_c<<<g2, 128, 0, st>>>(a, so, sn, itime);
+        launch_halo_fill(g, a.ubt + sn * n2, 1, 3, st);
+        launch_halo_fill(g, a.vbt + sn * n2, 1, 3, st);
+      }
+      k_bt_corr<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
     }
-    k_bt_pred<<<g2, 128, 0, s>>>(a, so, sn, itime > 1);
-    if (!a.cgrid) {
-      k_bt_mom_b<<<g2, 128, 0, s>>>(a, so, sn);
-    } else {
-      k_bt_mom_c<<<g2, 128, 0, s>>>(a, so, sn, itime);
-      launch_halo_fill(g, a.ubt + sn * n2, 1, 3, s);
-      launch_halo_fill(g, a.vbt + sn * n2, 1, 3, s);
-    }
-    k_bt_corr<<<g2, 128, 0, s>>>(a, so, sn, (double)(a.nts - itime + 1));
-  }
+  };
+  if (!replay_subcycle_graph(d, a, subcycles)) subcycles(s);
   double rntsp1 = 1.0 / ((double)a.nts + 1.0);
   double rnts = a.stepB ? 2.0 / ((double)a.nts * (double)(a.nts + 1)) : 1.0 / (double)a.nts;
   k_bt_post1<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(n2, rntsp1, rnts, a.eta_bar, a.udrho_u, a.udrho_v);
