@@ -275,7 +275,8 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
   if (d->kmt_d) cudaFree(d->kmt_d);
-  if (d->bt_graph) cudaGraphExecDestroy(d->bt_graph);
+  for (auto& gr : d->bt_graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
   if (d->red_h) cudaFreeHost(d->red_h);
   for (auto& c : d->clocks) {
     cudaEventDestroy(c.a);

@@ -109,10 +109,14 @@ struct mom5gpu_domain {
   int tune_mixed_rows = 32;  // precision-form tile height incl. halo: 16, 24, 32 or 64
   int tune_mixed_pf = 0;     // precision form, height 16: tracer levels prefetched into shared memory
   int tune_y_tj = 0;         // FP64 y-pass rows per thread
-  // CUDA graph of the barotropic subcycle loop, replayed while its kernel arguments
-  // (the bytes of the BtArgs it was captured with) are unchanged
-  cudaGraphExec_t bt_graph = nullptr;
-  std::vector<unsigned char> bt_graph_key;
+  // CUDA graphs of the barotropic subcycle loop, one per set of kernel arguments
+  // (the bytes of the BtArgs it was captured with: time levels rotate), at most
+  // kBtGraphs, the oldest replaced first
+  struct BtGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> key;
+  };
+  std::vector<BtGraph> bt_graphs;
 };
 
 namespace mom5 {

@@ -1304,36 +1304,43 @@ int make_bt_args(mom5gpu_domain* d, int tau, int taup1, BtArgs* ap, BtExtra* xp)
   return MOM5GPU_OK;
 }
 
-// Replays the domain's graph of the subcycle loop when it was captured with the
-// same BtArgs bytes, else captures enqueue(stream) into a new graph and launches
-// it.  Returns false (nothing enqueued) when the stream cannot be captured (the
-// caller then launches directly).
+// Replays the domain's graph of the subcycle loop captured with the same BtArgs
+// bytes, else captures enqueue(stream) into a new graph (kept with the last few:
+// the time levels rotate) and launches it.  Returns false (nothing enqueued)
+// when the stream cannot be captured; the caller then launches directly.
+constexpr size_t kBtGraphs = 6;
 template <class F>
 bool replay_subcycle_graph(mom5gpu_domain* d, const BtArgs& a, F&& enqueue) {
-  const unsigned char* key = reinterpret_cast<const unsigned char*>(&a);
-  bool same = d->bt_graph && d->bt_graph_key.size() == sizeof(BtArgs) &&
-              memcmp(d->bt_graph_key.data(), key, sizeof(BtArgs)) == 0;
-  if (!same) {
-    if (d->bt_graph) cudaGraphExecDestroy(d->bt_graph);
-    d->bt_graph = nullptr;
-    d->bt_graph_key.clear();
-    if (cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    enqueue(d->stream);
-    cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
-    if (e == cudaSuccess && graph) e = cudaGraphInstantiate(&d->bt_graph, graph, 0);
-    if (graph) cudaGraphDestroy(graph);
-    if (e != cudaSuccess || !d->bt_graph) {
-      d->bt_graph = nullptr;
-      cudaGetLastError();
-      return false;
-    }
-    d->bt_graph_key.assign(key, key + sizeof(BtArgs));
+  // inside a capture the caller runs (its own graph), launch directly
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(d->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return false;
   }
-  return cudaGraphLaunch(d->bt_graph, d->stream) == cudaSuccess;
+  const unsigned char* key = reinterpret_cast<const unsigned char*>(&a);
+  for (auto& gr : d->bt_graphs)
+    if (gr.exec && gr.key.size() == sizeof(BtArgs) && memcmp(gr.key.data(), key, sizeof(BtArgs)) == 0)
+      return cudaGraphLaunch(gr.exec, d->stream) == cudaSuccess;
+  if (cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  enqueue(d->stream);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaStreamEndCapture(d->stream, &graph);
+  if (e == cudaSuccess && graph) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess || !exec) {
+    cudaGetLastError();
+    return false;
+  }
+  if (d->bt_graphs.size() >= kBtGraphs) {
+    cudaGraphExecDestroy(d->bt_graphs.front().exec);
+    d->bt_graphs.erase(d->bt_graphs.begin());
+  }
+  d->bt_graphs.push_back({exec, std::vector<unsigned char>(key, key + sizeof(BtArgs))});
+  return cudaGraphLaunch(exec, d->stream) == cudaSuccess;
 }
 
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {

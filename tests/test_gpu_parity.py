@@ -471,6 +471,34 @@ def test_barotropic_matches(env, cyclic_x, stepping_B, cgrid):
     assert np.abs(out["eta_t_bar"]).max() > 0 and np.abs(out["udrho_u"]).max() > 0
 
 
+def test_barotropic_graph_follows_arguments(env):
+    """The subcycle loop is replayed from a CUDA graph keyed by its kernel
+    arguments: repeated level pairs replay, a new dtbt (new nts and step
+    constants) captures a new graph; every call equals the restatement."""
+    capi, O = env
+    sp = grid.DomainSpec(ni=40, nj=30, nk=1, lon0=0.0, lon1=40.0, lat0=-50.0, lat1=50.0, cyclic_x=True,
+                         hmin=None, ridge_amp=1000.0, ntracers=0, seed=21)
+    from mom5_gb300 import harness
+    dom = grid.make_domain(sp)
+    d = harness.load(dom, options=capi.default_options(barotropic_time_stepping_B=1))
+    g = O.domain_arrays(dom)
+    dims = O.dims(sp)
+    st = _baro_state(dom)
+    tau = 1
+    for step, dtbt in enumerate((30.0, 30.0, 30.0, 20.0, 20.0, 30.0)):
+        nts = d.barotropic_init(dtuv=300.0, dtbt=dtbt)
+        taup1 = 3 - tau
+        d.update_ocean_barotropic(tau, taup1)
+        out = O.update_ocean_barotropic(dims, g, st, nts, dtbt, time_stepping_B=True)
+        for k, fid in (("eta_t_bar", capi.F.ETA_T_BAR), ("udrho_u", capi.F.UDRHO_U), ("udrho_v", capi.F.UDRHO_V)):
+            got = d.get(fid, level=taup1)
+            assert equal(got, out[k]), f"step {step} dtbt {dtbt} {k}: {diff_report(got, out[k])}"
+        st = {"eta_t": st["eta_t"], "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"],
+              "udrho_v": out["udrho_v"]}
+        d.set(capi.F.ETA_T, np.ascontiguousarray(st["eta_t"]), level=taup1)
+        tau = taup1
+
+
 def test_barotropic_cfl_check(env):
     """The gravity-wave check of ocean_barotropic_init (:1595-1662) rejects a
     step above the limit and accepts one below it."""
