@@ -350,7 +350,10 @@ def run_ours(args, rank, world):
     # inputs (tracers, advection velocity) from pinned host memory and reads its
     # results back, pipelined over three time levels so that the uploads of step
     # s+1 and the read-back of step s overlap the compute (stream-ordered copies,
-    # mom5gpu_copy_field_async, ordered by events)
+    # mom5gpu_copy_field_async, ordered by events).  The velocity has one device
+    # field, read by the advection: step s+1's velocity is uploaded into a device
+    # staging buffer while step s advects and copied into the field (device to
+    # device) while step s runs its barotropic subcycle.
     e2e = None
     if not args.no_e2e and ntr > 0:
         pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True)
@@ -368,7 +371,8 @@ def run_ours(args, rank, world):
             d.set(fid, d.get(fid, level=1), level=3)
         oT = [pin(n3) for _ in range(ntr)]
         oE, oU, oV = pin(n2), pin(n2), pin(n2)
-        ke = max(3, min(args.steps, 10))
+        sU, sV, sW = (torch.empty(n, dtype=torch.float64, device="cuda") for n in (n3, n3, nw))
+        ke = max(3, min(args.steps, 30))
         h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
         ev = lambda: torch.cuda.Event()
         h2d_done, adv_done, comp_done, d2h_done = ([ev() for _ in range(ke)] for _ in range(4))
@@ -380,9 +384,12 @@ def run_ours(args, rank, world):
                 h2d.wait_event(d2h_done[s_ - 2])
             for n in range(ntr):
                 d.copy_field_async(F.TRACER, hT[n].data_ptr(), 1, h2d.cuda_stream, n=n + 1, level=lin)
-            if s_ >= 1:  # the velocity is read by the tracer advection of step s-1 (not by its barotropic part)
+            with torch.cuda.stream(h2d):  # the staging buffer is free: its last copy is earlier on h2d
+                for buf, dst in ((hU, sU), (hV, sV), (hW, sW)):
+                    dst.copy_(buf, non_blocking=True)
+            if s_ >= 1:  # the velocity field is read by the advection of step s-1 (not by its barotropic part)
                 h2d.wait_event(adv_done[s_ - 1])
-            for fid, buf in ((F.UHRHO_ET, hU), (F.VHRHO_NT, hV), (F.WRHO_BT, hW)):
+            for fid, buf in ((F.UHRHO_ET, sU), (F.VHRHO_NT, sV), (F.WRHO_BT, sW)):
                 d.copy_field_async(fid, buf.data_ptr(), 1, h2d.cuda_stream)
             h2d_done[s_].record(h2d)
             stream.wait_event(h2d_done[s_])
@@ -403,8 +410,8 @@ def run_ours(args, rank, world):
                "steps": ke, "api": "mom5gpu_copy_field_async (pinned host buffers, upload and read-back streams) / "
                                    "mom5gpu_tracer_advection_step / mom5gpu_update_ocean_barotropic",
                "timing": "host wall clock over the steps, every copy inside; copies of neighbouring steps overlap "
-                         "the compute (three time levels rotate)"}
-        del hT, oT, hU, hV, hW
+                         "the compute (three time levels rotate; the velocity goes through a device staging buffer)"}
+        del hT, oT, hU, hV, hW, sU, sV, sW
 
     out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-updates/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
