@@ -278,41 +278,51 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
 // strip of TJ rows, marching north; th_tendency += result.  Ra, Rb carry the
 // masked differences R of faces j-1 and j (R(f) = (m(f) && m(f+1)) ?
 // tx(f+1) - tx(f) : 0, the reference's Rjm and Rj of face j); face j forms only
-// R(j+1), its Rjp.  With `first` the two carried values are formed as well.
-template <bool SWEBY, int MAXN, class Ar>
-DEVI void y_face(const MdflArgs& a, int i, int j, int k, double (*f)[kMdflThreads], int t, double (*Ra)[kMdflThreads],
-                 double (*Rb)[kMdflThreads], bool first) {
+// R(j+1), its Rjp.
+//
+// Tracer-independent terms of face j (between rows j and j+1).
+struct YFace {
+  bool m2, m3, fm;
+  double massflux, d0, d1, c;
+};
+DEVI YFace y_geom(const MdflArgs& a, int i, int j, int k, bool& m0, bool& m1) {
   const Geo& g = a.g;
-  bool m0 = a.mask2[IM(g, i, j - 1, k)], m1 = a.mask2[IM(g, i, j, k)];
-  bool m2 = a.mask2[IM(g, i, j + 1, k)], m3 = a.mask2[IM(g, i, j + 2, k)];
+  YFace f;
+  m0 = a.mask2[IM(g, i, j - 1, k)];
+  m1 = a.mask2[IM(g, i, j, k)];
+  f.m2 = a.mask2[IM(g, i, j + 1, k)];
+  f.m3 = a.mask2[IM(g, i, j + 2, k)];
   double v = a.vh[I3(g, i, j, k)];
-  double massflux = a.dxtn[I2(g, i, j)] * v;
+  f.massflux = a.dxtn[I2(g, i, j)] * v;
   double cfl = fabs(div_seeded(v * a.dtime * 2.0, (a.rdz[I3(g, i, j, k)] + a.rdz[I3(g, i, j + 1, k)]) * a.dytn[I2(g, i, j)]));
-  double d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
-  double d1 = (1.0 - cfl * cfl) * kOneSixth;
-  double c = div_seeded(1.0 - cfl, add_1em30(cfl));
-  bool fm = m1 && m2;
-#pragma unroll 1
-  for (int n = 0; n < a.ntr; ++n) {
-    const double* tx = a.tx + n * g.n3;
-    double tB = tm_yhalo(g, tx, i, j, k), tC = tm_yhalo(g, tx, i, j + 1, k);
-    if (first) {
-      double tA = tm_yhalo(g, tx, i, j - 1, k);
-      Ra[n][t] = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
-      Rb[n][t] = (m2 && m1) ? Ar::sub(tC, tB) : 0.0;
-    }
-    double tD = tm_yhalo(g, tx, i, j + 2, k);
-    double Rjm = Ra[n][t], Rj = Rb[n][t];
-    double Rjp = (m3 && m2) ? Ar::sub(tD, tC) : 0.0;
-    Ra[n][t] = Rj;
-    Rb[n][t] = Rjp;
-    f[n][t] = fm ? face_flux<SWEBY, Ar>(massflux, Rjm, Rj, Rjp, tB, tC, d0, d1, c) : 0.0;
-  }
+  f.d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
+  f.d1 = (1.0 - cfl * cfl) * kOneSixth;
+  f.c = div_seeded(1.0 - cfl, add_1em30(cfl));
+  f.fm = m1 && f.m2;
+  return f;
+}
+// Flux of tracer n through face j, carrying Ra/Rb; tB returns tx at row j.
+template <bool SWEBY, class Ar>
+DEVI double y_flux(const MdflArgs& a, const YFace& f, int i, int j, int k, int n, int t, double (*Ra)[kMdflThreads],
+                   double (*Rb)[kMdflThreads], double& tB) {
+  const Geo& g = a.g;
+  const double* tx = a.tx + n * g.n3;
+  tB = tm_yhalo(g, tx, i, j, k);
+  double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
+  double Rjm = Ra[n][t], Rj = Rb[n][t];
+  double Rjp = (f.m3 && f.m2) ? Ar::sub(tD, tC) : 0.0;
+  Ra[n][t] = Rj;
+  Rb[n][t] = Rjp;
+  return f.fm ? face_flux<SWEBY, Ar>(f.massflux, Rjm, Rj, Rjp, tB, tC, f.d0, f.d1, f.c) : 0.0;
 }
 
+// Each tracer's face flux is formed and used in the same iteration (the
+// flux of the row's north face in a register, the south face's from the
+// previous row in shared memory), so the per-tracer shared state is fprev, Ra
+// and Rb only.
 template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
 DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
-  __shared__ double fprev[MAXN][kMdflThreads], fcur[MAXN][kMdflThreads];
+  __shared__ double fprev[MAXN][kMdflThreads];
   __shared__ double Ra[MAXN][kMdflThreads], Rb[MAXN][kMdflThreads];
   const Geo& g = a.g;
   const int t = threadIdx.x;
@@ -324,9 +334,24 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
   if (j1 > g.nj) j1 = g.nj;
   double rdt_h, rdt_l;  // two-term reciprocal of dtime
   recip_pair(a.dtime, rdt_h, rdt_l);
-  y_face<SWEBY, MAXN, Ar>(a, i, j0 - 1, k, fprev, t, Ra, Rb, true);
+  {
+    // the face below the strip: its flux and the two carried differences
+    bool m0, m1;
+    const YFace f = y_geom(a, i, j0 - 1, k, m0, m1);
+#pragma unroll 1
+    for (int n = 0; n < a.ntr; ++n) {
+      const double* tx = a.tx + n * g.n3;
+      double tA = tm_yhalo(g, tx, i, j0 - 2, k), tB = tm_yhalo(g, tx, i, j0 - 1, k);
+      double tC = tm_yhalo(g, tx, i, j0, k);
+      Ra[n][t] = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
+      Rb[n][t] = (f.m2 && m1) ? Ar::sub(tC, tB) : 0.0;
+      double tb;
+      fprev[n][t] = y_flux<SWEBY, Ar>(a, f, i, j0 - 1, k, n, t, Ra, Rb, tb);
+    }
+  }
   for (int j = j0; j <= j1; ++j) {
-    y_face<SWEBY, MAXN, Ar>(a, i, j, k, fcur, t, Ra, Rb, false);
+    bool m0, m1;
+    const YFace f = y_geom(a, i, j, k, m0, m1);
     long p = I3(g, i, j, k);
     bool mk = a.mask2[IM(g, i, j, k)];
     double datr = a.datr[I2(g, i, j)];
@@ -340,9 +365,10 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
     recip_pair(rdz, rr_h, rr_l);
 #pragma unroll 1
     for (int n = 0; n < a.ntr; ++n) {
+      double tm;  // tracer_mdfl after the x pass at (i, j, k)
+      double fc = y_flux<SWEBY, Ar>(a, f, i, j, k, n, t, Ra, Rb, tm);
       double Tk = a.T[n * a.tstride + p];
-      double tm = a.tx[n * g.n3 + p];
-      double fp = fprev[n][t], fc = fcur[n][t];
+      double fp = fprev[n][t];
       double out;
       if (!ALL) {
         tm = Au::add(tm, Au::mul(coef, Au::sub(fp, fc)));
