@@ -14,8 +14,7 @@ namespace mixed {
 
 constexpr int ZW = 32;       // tile width incl. the 2-cell halo on each side (one warp)
 constexpr int TI = ZW - 4;   // interior width
-constexpr int NT = 256;      // threads
-constexpr int NW = NT / 32;  // warps
+constexpr int NT = 256;      // threads of the 16- and 24-row tiles
 // ZR (template): tile height incl. halo; interior height ZR - 4
 // Threads per block of a tile height: 8 warps, 16 for the 32-row tile and 32
 // for the 64-row tile, so that every shape holds two tile rows per thread and
