@@ -17,8 +17,9 @@ constexpr int TI = ZW - 4;   // interior width
 constexpr int NT = 256;      // threads of the 16- and 24-row tiles
 // ZR (template): tile height incl. halo; interior height ZR - 4
 // Threads per block of a tile height: 8 warps, 16 for the 32-row tile and 32
-// for the 64-row tile, so that every shape holds two tile rows per thread and
-// the tall tiles still give 32 warps per SM (two blocks of 32 rows, one of 64).
+// for the 64-row tile, so that the 16-, 32- and 64-row tiles hold two tile rows
+// per thread (the 24-row tile three) and the tall tiles still give 32 warps per
+// SM (two blocks of 32 rows, one of 64).
 __host__ __device__ constexpr int tile_threads(int ZR) { return ZR == 64 ? 1024 : ZR == 32 ? 512 : NT; }
 
 DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
