@@ -69,9 +69,9 @@ def adv_bytes(ni, nj, nk, ntr):
 
 
 # DRAM bytes per tracer-cell of the advection launch set, from the ncu capture of the
-# 360x270x50 block (profiles/traffic_advection_c2block.md): FP64 5.199 GB, precision form
+# 360x270x50 block (profiles/traffic_advection_c2block.md): FP64 4.740 GB, precision form
 # 0.975 GB for 360*270*50*10 tracer-cells.
-TRAFFIC_PER_TRACER_CELL = {"fp64": 5.199e9 / (360 * 270 * 50 * 10), "mixed": 0.975e9 / (360 * 270 * 50 * 10)}
+TRAFFIC_PER_TRACER_CELL = {"fp64": 4.740e9 / (360 * 270 * 50 * 10), "mixed": 0.975e9 / (360 * 270 * 50 * 10)}
 
 
 # FP64 thread-instructions per tracer-cell of the exact MDFL passes (z + x + y) and per
