@@ -139,6 +139,23 @@ enum mom5gpu_field {
   MOM5GPU_PSOM_S0 = 120, /* 3D (n), mass-weighted tracer after the last sweep */
   MOM5GPU_PSOM_SX, MOM5GPU_PSOM_SXX, MOM5GPU_PSOM_SY, MOM5GPU_PSOM_SYY, MOM5GPU_PSOM_SZ, MOM5GPU_PSOM_SZZ,
   MOM5GPU_PSOM_SXY, MOM5GPU_PSOM_SXZ, MOM5GPU_PSOM_SYZ,
+  /* thickness fields of update_ucell_thickness (ocean_thickness.F90:3507-3886),
+   * ocean_thickness_type (ocean_types.F90:134-203) and Grd%umask */
+  MOM5GPU_UMASK = 130,   /* 3D, Grd%umask (1 down to kmu, 0 below) */
+  MOM5GPU_DZT,           /* 3D, Thickness%dzt */
+  MOM5GPU_DZWT,          /* 3DW, Thickness%dzwt(:,:,0:nk) */
+  MOM5GPU_DZU,           /* 3D, Thickness%dzu */
+  MOM5GPU_DZWU,          /* 3DW, Thickness%dzwu(:,:,0:nk) */
+  MOM5GPU_RHO_DZUR,      /* 3D, Thickness%rho_dzur */
+  MOM5GPU_DZTEN_E,       /* 3D, Thickness%dzten(:,:,:,1) */
+  MOM5GPU_DZTEN_N,       /* 3D, Thickness%dzten(:,:,:,2) */
+  MOM5GPU_DEPTH_ZT,      /* 3D, Thickness%depth_zt */
+  MOM5GPU_DEPTH_ZWT,     /* 3D, Thickness%depth_zwt */
+  MOM5GPU_DEPTH_ZU,      /* 3D, Thickness%depth_zu */
+  MOM5GPU_DEPTH_ZWU,     /* 3D, Thickness%depth_zwu */
+  MOM5GPU_MASS_U,        /* 2D (t), Thickness%mass_u */
+  MOM5GPU_MASS_EN_E,     /* 2D, Thickness%mass_en(:,:,1) */
+  MOM5GPU_MASS_EN_N,     /* 2D, Thickness%mass_en(:,:,2) */
   MOM5GPU_FIELD_END
 };
 
@@ -314,6 +331,23 @@ int mom5gpu_ocean_advection_velocity(mom5gpu_domain* d, int tau);
  * n (0 = every tracer).  Reads PME and the per-tracer TPME, TRACER_ETA_SMOOTH
  * and PBOT_SMOOTH (zero until set); needs mom5gpu_set_vertical_grid (kmt). */
 int mom5gpu_tracer_boundary_terms(mom5gpu_domain* d, int n);
+/* Vertical coordinates (ocean_parameters.F90:107-112). */
+#define MOM5GPU_GEOPOTENTIAL 1
+#define MOM5GPU_ZSTAR 2
+#define MOM5GPU_ZSIGMA 3
+#define MOM5GPU_PRESSURE 4
+#define MOM5GPU_PSTAR 5
+#define MOM5GPU_PSIGMA 6
+/* update_ucell_thickness (ocean_thickness.F90:3507-3886), without blobs: U-cell
+ * and face thicknesses of time level taup1 from the T cells (geopotential: the
+ * top U cell from eta_u(taup1) only; zsigma/psigma: copies; other coordinates:
+ * the minimum of the neighbouring T cells, halos updated), rho_dzur, depth_zu,
+ * depth_zwu, thicku(taup1), thicken, mass_u(taup1), mass_en.  kmu is the number
+ * of wet levels of MOM5GPU_UMASK.  linear_free_surface and update_dzwu_k0 are
+ * the ocean_thickness_nml switches (defaults 0 and 1).  The inputs of the
+ * branch taken must have been set (MOM5GPU_ESTATE otherwise). */
+int mom5gpu_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vert_coordinate, int linear_free_surface,
+                                   int update_dzwu_k0);
 /* ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141) without the
  * optional barotropic friction: FORCING_BT_U/V = sum_k tmasken*accel +
  * tmasken(k=1)*(smf - bmf) on the compute domain, zero halo then the single-PE

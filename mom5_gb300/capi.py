@@ -28,6 +28,7 @@ ADVECT_2ND_ORDER, ADVECT_4TH_ORDER, ADVECT_6TH_ORDER, ADVECT_MDFL_SUP_B, ADVECT_
 ADVECT_PSOM = 11
 ADVECT_QUICKMOM3 = 6
 PRECISION_FP64, PRECISION_MIXED = 0, 1
+GEOPOTENTIAL, ZSTAR, ZSIGMA, PRESSURE, PSTAR, PSIGMA = 1, 2, 3, 4, 5, 6
 
 
 def _enum_values() -> dict:
@@ -124,6 +125,7 @@ def lib() -> C.CDLL:
             "mom5gpu_write_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
             "mom5gpu_read_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
             "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
+            "mom5gpu_update_ucell_thickness": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_check_finite": (C.c_int, [vp, C.c_int, C.c_int, ip]),
@@ -325,6 +327,11 @@ class Domain:
 
     def ocean_barotropic_forcing(self):
         self.check(lib().mom5gpu_ocean_barotropic_forcing(self.h))
+
+    def update_ucell_thickness(self, taup1, vert_coordinate=GEOPOTENTIAL, linear_free_surface=False,
+                               update_dzwu_k0=True):
+        self.check(lib().mom5gpu_update_ucell_thickness(self.h, taup1, vert_coordinate, int(linear_free_surface),
+                                                        int(update_dzwu_k0)))
 
     def ocean_advection_velocity(self, tau):
         self.check(lib().mom5gpu_ocean_advection_velocity(self.h, tau))

@@ -62,6 +62,14 @@ const FieldInfo kFields[] = {
     {MOM5GPU_PSOM_SYY, S3D, true, false},     {MOM5GPU_PSOM_SZ, S3D, true, false},
     {MOM5GPU_PSOM_SZZ, S3D, true, false},     {MOM5GPU_PSOM_SXY, S3D, true, false},
     {MOM5GPU_PSOM_SXZ, S3D, true, false},     {MOM5GPU_PSOM_SYZ, S3D, true, false},
+    {MOM5GPU_UMASK, S3D, false, false},       {MOM5GPU_DZT, S3D, false, false},
+    {MOM5GPU_DZWT, S3DW, false, false},       {MOM5GPU_DZU, S3D, false, false},
+    {MOM5GPU_DZWU, S3DW, false, false},       {MOM5GPU_RHO_DZUR, S3D, false, false},
+    {MOM5GPU_DZTEN_E, S3D, false, false},     {MOM5GPU_DZTEN_N, S3D, false, false},
+    {MOM5GPU_DEPTH_ZT, S3D, false, false},    {MOM5GPU_DEPTH_ZWT, S3D, false, false},
+    {MOM5GPU_DEPTH_ZU, S3D, false, false},    {MOM5GPU_DEPTH_ZWU, S3D, false, false},
+    {MOM5GPU_MASS_U, S2D, false, true},       {MOM5GPU_MASS_EN_E, S2D, false, false},
+    {MOM5GPU_MASS_EN_N, S2D, false, false},
 };
 
 // field storage: one block per (field, level) holding every tracer of that level
@@ -951,6 +959,15 @@ int mom5gpu_tracer_boundary_terms(mom5gpu_domain* d, int n) {
   int rc = MOM5GPU_OK;
   for (int m = (n == 0 ? 1 : n); m <= (n == 0 ? ntr : n) && rc == MOM5GPU_OK; ++m) rc = launch_tracer_boundary(d, m);
   return rc;
+}
+
+int mom5gpu_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vert_coordinate, int linear_free_surface,
+                                   int update_dzwu_k0) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (taup1 < 1 || taup1 > 3) return fail(d, MOM5GPU_EINVAL, "update_ucell_thickness: taup1 %d", taup1);
+  if (vert_coordinate < MOM5GPU_GEOPOTENTIAL || vert_coordinate > MOM5GPU_PSIGMA)
+    return fail(d, MOM5GPU_EINVAL, "update_ucell_thickness: vertical coordinate %d", vert_coordinate);
+  return launch_update_ucell_thickness(d, taup1, vert_coordinate, linear_free_surface != 0, update_dzwu_k0 != 0);
 }
 
 int mom5gpu_ocean_barotropic_forcing(mom5gpu_domain* d) {

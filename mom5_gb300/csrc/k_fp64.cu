@@ -1597,6 +1597,186 @@ int launch_barotropic_forcing(mom5gpu_domain* d) {
 }
 
 // ---------------------------------------------------------------------------
+// update_ucell_thickness (ocean_thickness.F90:3507-3886), no blobs
+// ---------------------------------------------------------------------------
+struct UThkArgs {
+  Geo g;
+  double rho0;
+  int linear_fs, dzwu_k0;
+  const double *umask, *tme, *tmn, *dzt, *dzwt, *rho_dzt, *depth_zt, *depth_zwt, *eta_u;
+  double *dzu, *dzwu, *rho_dzu, *rho_dzur, *dzten_e, *dzten_n, *rho_dzten_e, *rho_dzten_n, *depth_zu, *depth_zwu;
+  double *thicku, *thicken_e, *thicken_n, *mass_u, *mass_en_e, *mass_en_n;
+};
+constexpr double kEpslnThk = 1.0e-20;  // constants_mod epsln
+DEVI double min2(double a, double b) { return a < b ? a : b; }  // Fortran min, evaluated left to right
+
+// geopotential (:3617-3635): only the top U cell moves, with eta_u(taup1)
+__global__ void k_uthk_geo(UThkArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double zt = a.depth_zt[q], zwt = a.depth_zwt[q];  // level 1
+  a.dzwu[q] = a.linear_fs ? zt : zt + a.eta_u[q];   // dzwu(:,:,0)
+  double dzu1 = a.linear_fs ? zwt : zwt + a.eta_u[q];
+  a.dzu[q] = dzu1;
+  double r = a.rho0 * dzu1;
+  a.rho_dzu[q] = r;
+  a.rho_dzur[q] = div_seeded(1.0, r + kEpslnThk);
+}
+
+// zsigma / psigma (:3663-3683): the T-cell thicknesses
+__global__ void k_uthk_sigma(UThkArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  for (int k = 0; k < g.nk; ++k) {
+    long p = (long)k * g.n2 + q;
+    double t = a.dzt[p];
+    a.dzu[p] = t;
+    a.dzten_e[p] = t;
+    a.dzten_n[p] = t;
+    a.dzwu[p + g.n2] = a.dzwt[p + g.n2];
+    a.rho_dzu[p] = a.rho_dzt[p];
+  }
+  a.dzwu[q] = a.dzwt[q];
+}
+
+// other coordinates (:3735-3763): minimum of the neighbouring T cells over isd:iec, jsd:jec
+__global__ void k_uthk_min(UThkArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni || j > g.nj) return;
+  long q = I2(g, i, j), qe = q + 1, qn = q + g.nxd, qne = qn + 1;
+  for (int k = 0; k < g.nk; ++k) {
+    long o = (long)k * g.n2, w = o + g.n2;  // 3-D level k; level k+1 of the 0..nk arrays
+    const double *t = a.dzt + o, *r = a.rho_dzt + o, *zw = a.dzwt + w;
+    a.dzu[o + q] = min2(min2(min2(t[q], t[qe]), t[qn]), t[qne]);
+    a.dzwu[w + q] = min2(min2(min2(zw[q], zw[qe]), zw[qn]), zw[qne]);
+    a.rho_dzu[o + q] = min2(min2(min2(r[q], r[qe]), r[qn]), r[qne]);
+    a.dzten_e[o + q] = min2(t[q], t[qe]);
+    a.dzten_n[o + q] = min2(t[q], t[qn]);
+    a.rho_dzten_e[o + q] = min2(r[q], r[qe]);
+    a.rho_dzten_n[o + q] = min2(r[q], r[qn]);
+  }
+  if (a.dzwu_k0) a.dzwu[q] = min2(min2(min2(a.dzwt[q], a.dzwt[qe]), a.dzwt[qn]), a.dzwt[qne]);
+}
+
+// non-geopotential tail (:3771-3827): rho_dzur and the cumulative depths
+__global__ void k_uthk_depths(UThkArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  for (int k = 0; k < g.nk; ++k) {
+    long p = (long)k * g.n2 + q;
+    a.rho_dzur[p] = div_seeded(a.umask[p], a.rho_dzu[p] + kEpslnThk);
+  }
+  double zu = a.dzwu[q], zwu = a.dzu[q];
+  a.depth_zu[q] = zu;
+  a.depth_zwu[q] = zwu;
+  for (int k = 1; k < g.nk; ++k) {
+    long p = (long)k * g.n2 + q;
+    zu = zu + a.dzwu[p];  // + dzwu(k-1) of the 0..nk array
+    zwu = zwu + a.dzu[p];
+    a.depth_zu[p] = zu;
+    a.depth_zwu[p] = zwu;
+  }
+}
+
+// every coordinate (:3817-3858): thicku, thicken, mass_u, mass_en; kmu counted from umask
+__global__ void k_uthk_sums(UThkArgs a) {
+  const Geo& g = a.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  int kmu = 0;
+  double te = 0.0, tn = 0.0, mu = 0.0, me = 0.0, mn = 0.0;
+  for (int k = 0; k < g.nk; ++k) {
+    long p = (long)k * g.n2 + q;
+    kmu += a.umask[p] != 0.0 ? 1 : 0;
+    te = te + a.dzten_e[p];
+    tn = tn + a.dzten_n[p];
+    mu = mu + a.umask[p] * a.rho_dzu[p];
+    me = me + a.tme[p] * a.rho_dzten_e[p];
+    mn = mn + a.tmn[p] * a.rho_dzten_n[p];
+  }
+  a.thicku[q] = kmu > 1 ? a.depth_zwu[(long)(kmu - 1) * g.n2 + q] : 0.0;
+  a.thicken_e[q] = te;
+  a.thicken_n[q] = tn;
+  a.mass_u[q] = mu;
+  a.mass_en_e[q] = me;
+  a.mass_en_n[q] = mn;
+}
+
+int launch_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vcoord, bool linear_fs, bool dzwu_k0) {
+  const Geo& g = d->geo;
+  UThkArgs a;
+  a.g = g;
+  a.rho0 = d->opt.rho0;
+  a.linear_fs = linear_fs;
+  a.dzwu_k0 = dzwu_k0;
+  const bool geo = vcoord == MOM5GPU_GEOPOTENTIAL, sigma = vcoord == MOM5GPU_ZSIGMA || vcoord == MOM5GPU_PSIGMA;
+  a.umask = fptr_if_set(d, MOM5GPU_UMASK, 0, 0);
+  a.tme = fptr_if_set(d, MOM5GPU_TMASKEN_E, 0, 0);
+  a.tmn = fptr_if_set(d, MOM5GPU_TMASKEN_N, 0, 0);
+  a.dzt = geo ? nullptr : fptr_if_set(d, MOM5GPU_DZT, 0, 0);
+  a.dzwt = geo ? nullptr : fptr_if_set(d, MOM5GPU_DZWT, 0, 0);
+  a.rho_dzt = geo ? nullptr : fptr_if_set(d, MOM5GPU_RHO_DZT, 0, taup1);
+  a.depth_zt = geo ? fptr_if_set(d, MOM5GPU_DEPTH_ZT, 0, 0) : nullptr;
+  a.depth_zwt = geo ? fptr_if_set(d, MOM5GPU_DEPTH_ZWT, 0, 0) : nullptr;
+  a.eta_u = geo && !linear_fs ? fptr_if_set(d, MOM5GPU_ETA_U, 0, taup1) : nullptr;
+  if (!a.umask || !a.tme || !a.tmn || (!geo && (!a.dzt || !a.dzwt || !a.rho_dzt)) ||
+      (geo && (!a.depth_zt || !a.depth_zwt || (!linear_fs && !a.eta_u))))
+    return fail(d, MOM5GPU_ESTATE, "update_ucell_thickness: an input field was never set");
+  a.dzu = fptr(d, MOM5GPU_DZU, 0, 0);
+  a.dzwu = fptr(d, MOM5GPU_DZWU, 0, 0);
+  a.rho_dzu = fptr(d, MOM5GPU_RHO_DZU, 0, taup1);
+  a.rho_dzur = fptr(d, MOM5GPU_RHO_DZUR, 0, 0);
+  a.dzten_e = fptr(d, MOM5GPU_DZTEN_E, 0, 0);
+  a.dzten_n = fptr(d, MOM5GPU_DZTEN_N, 0, 0);
+  a.rho_dzten_e = fptr(d, MOM5GPU_RHO_DZTEN_E, 0, 0);
+  a.rho_dzten_n = fptr(d, MOM5GPU_RHO_DZTEN_N, 0, 0);
+  a.depth_zu = fptr(d, MOM5GPU_DEPTH_ZU, 0, 0);
+  a.depth_zwu = fptr(d, MOM5GPU_DEPTH_ZWU, 0, 0);
+  a.thicku = fptr(d, MOM5GPU_THICKU, 0, taup1);
+  a.thicken_e = fptr(d, MOM5GPU_THICKEN_E, 0, 0);
+  a.thicken_n = fptr(d, MOM5GPU_THICKEN_N, 0, 0);
+  a.mass_u = fptr(d, MOM5GPU_MASS_U, 0, taup1);
+  a.mass_en_e = fptr(d, MOM5GPU_MASS_EN_E, 0, 0);
+  a.mass_en_n = fptr(d, MOM5GPU_MASS_EN_N, 0, 0);
+  const void* outs[] = {a.dzu, a.dzwu, a.rho_dzu, a.rho_dzur, a.dzten_e, a.dzten_n, a.rho_dzten_e, a.rho_dzten_n,
+                        a.depth_zu, a.depth_zwu, a.thicku, a.thicken_e, a.thicken_n, a.mass_u, a.mass_en_e,
+                        a.mass_en_n};
+  for (const void* p : outs)
+    if (!p) return MOM5GPU_ENOMEM;
+  cudaStream_t s = d->stream;
+  dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
+  if (geo) {
+    k_uthk_geo<<<g2, 128, 0, s>>>(a);
+    count_launches(d, 1);
+  } else {
+    if (sigma) {
+      k_uthk_sigma<<<g2, 128, 0, s>>>(a);
+      count_launches(d, 1);
+    } else {
+      k_uthk_min<<<dim3((g.ni + 1 + 127) / 128, g.nj + 1), 128, 0, s>>>(a);
+      for (double* p : {a.dzu, a.rho_dzu, a.dzten_e, a.dzten_n, a.rho_dzten_e, a.rho_dzten_n})
+        launch_halo_fill(g, p, g.nk, 3, s);
+      launch_halo_fill(g, a.dzwu, g.nk + 1, 3, s);
+      count_launches(d, 1 + ((g.cx || g.cy) ? 7 : 0));
+    }
+    k_uthk_depths<<<g2, 128, 0, s>>>(a);
+    count_launches(d, 1);
+  }
+  k_uthk_sums<<<g2, 128, 0, s>>>(a);
+  count_launches(d, 1);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "update_ucell_thickness");
+}
+
+// ---------------------------------------------------------------------------
 // compensated, fixed-order reductions
 // ---------------------------------------------------------------------------
 DEVI void two_sum(double a, double b, double& s, double& e) {

@@ -404,3 +404,52 @@ def barotropic_cfl_limit(dom: Domain) -> float:
     gridsp = torch.sqrt(1.0 / (1.0 / (dxt * dxt) + 1.0 / (dyt * dyt)))
     dtcg = torch.where(wet, gridsp / cg, torch.full_like(cg, 1.0e6))
     return float(int(float(dtcg.min())))
+
+
+def thickness_state(ni: int, nj: int, nk: int, cyclic_x: bool = False, cyclic_y: bool = False, seed: int = 0,
+                    rho0: float = 1035.0) -> dict:
+    """Seeded thickness fields of a partial-cell domain for update_ucell_thickness
+    (ocean_thickness.F90:3507-3886), data-domain arrays [k][j][i] (numpy):
+    T-cell dzt with partial bottom cells and a time-varying top cell, dzwt
+    (levels 0..nk, half-cell distances), rho_dzt = rho0*dzt (perturbed, as a
+    non-Boussinesq density would), depth_zt/zwt (cumulative), kmt; the U-cell
+    kmu = min of the four surrounding kmt with umask(k) = (k <= kmu); tmasken
+    of the east and north faces; eta_u; and the current U-cell and face
+    fields the routine updates, filled with values it must overwrite or keep."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    nx, ny = ni + 2, nj + 2
+    dz0 = 10.0 + 40.0 * np.arange(nk) / max(nk - 1, 1)
+    kmt = rng.integers(0, nk + 1, size=(ny, nx))
+    kmt[rng.random((ny, nx)) < 0.6] = nk
+    dzt = np.zeros((nk, ny, nx))
+    for k in range(nk):
+        dzt[k] = dz0[k] * np.where(kmt - 1 == k, 0.3 + 0.7 * rng.random((ny, nx)), 1.0)
+    dzt[0] += rng.normal(0.0, 0.3, size=(ny, nx))
+    dzwt = np.zeros((nk + 1, ny, nx))
+    dzwt[0] = 0.5 * dzt[0]
+    for k in range(1, nk):
+        dzwt[k] = 0.5 * (dzt[k - 1] + dzt[k])
+    dzwt[nk] = 0.5 * dzt[nk - 1]
+    rho_dzt = rho0 * dzt * (1.0 + 1e-3 * rng.standard_normal((nk, ny, nx)))
+    depth_zwt = np.cumsum(dzt, axis=0)
+    depth_zt = np.cumsum(dzwt[:nk], axis=0)
+    kp = np.pad(kmt, 1, mode="edge")
+    kmu = np.minimum(np.minimum(kmt, kp[1:-1, 2:]), np.minimum(kp[2:, 1:-1], kp[2:, 2:]))
+    if cyclic_x:
+        kmu[:, 0], kmu[:, -1] = kmu[:, -2], kmu[:, 1]
+    if cyclic_y:
+        kmu[0, :], kmu[-1, :] = kmu[-2, :], kmu[1, :]
+    lev = np.arange(nk)[:, None, None]
+    umask = (lev < kmu[None]).astype(np.float64)
+    tmask = (lev < kmt[None]).astype(np.float64)
+    tme = tmask * np.concatenate([tmask[:, :, 1:], tmask[:, :, -1:]], axis=2)
+    tmn = tmask * np.concatenate([tmask[:, 1:, :], tmask[:, -1:, :]], axis=1)
+    junk = lambda shape: rng.normal(5.0, 1.0, size=shape)
+    return {"dzt": dzt, "dzwt": dzwt, "rho_dzt": rho_dzt, "depth_zt": depth_zt, "depth_zwt": depth_zwt,
+            "kmt": kmt.astype(np.int32), "kmu": kmu.astype(np.int32), "umask": umask, "tmasken_e": tme,
+            "tmasken_n": tmn, "eta_u": rng.normal(0.0, 0.5, size=(ny, nx)),
+            "dzu": junk((nk, ny, nx)), "dzwu": junk((nk + 1, ny, nx)), "rho_dzu": junk((nk, ny, nx)),
+            "rho_dzur": junk((nk, ny, nx)), "dzten_e": dzt * 0.9, "dzten_n": dzt * 0.8,
+            "rho_dzten_e": rho_dzt * 0.9, "rho_dzten_n": rho_dzt * 0.8,
+            "depth_zu": depth_zt.copy(), "depth_zwu": depth_zwt.copy()}

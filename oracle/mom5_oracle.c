@@ -2215,3 +2215,123 @@ double orc_area_integral(const orc_dims* d, const double* tmask1, const double* 
     }
   return s + c;
 }
+
+/* update_ucell_thickness (ocean_thickness.F90:3507-3886), no blobs.
+ * vcoord: 1 GEOPOTENTIAL, 3 ZSIGMA, 6 PSIGMA, any other value (ZSTAR, PRESSURE,
+ * PSTAR) the branch that takes U-cell and face thicknesses as the minimum of
+ * the neighbouring T cells (:3735-3763).  Arrays are data-domain [k][j][i];
+ * dzwt and dzwu hold levels 0..nk (nk+1 planes).  kmu (Grid%kmu) is given.
+ * Updated in place: dzu, dzwu, rho_dzu (level taup1), rho_dzur, dzten_e/n,
+ * rho_dzten_e/n, depth_zu, depth_zwu; written: thicku and mass_u (level
+ * taup1), thicken_e/n, mass_en_e/n.  Fortran min(a,b,c,d) is evaluated left to
+ * right with a < b ? a : b; single-PE mpp_update_domains halos. */
+void orc_update_ucell_thickness(const orc_dims* d, int vcoord, int linear_free_surface, int update_dzwu_k0,
+                                double rho0, const double* umask, const double* tmasken_e, const double* tmasken_n,
+                                const double* dzt, const double* dzwt, const double* rho_dzt, const double* depth_zt1,
+                                const double* depth_zwt1, const double* eta_u, const int* kmu, double* dzu,
+                                double* dzwu, double* rho_dzu, double* rho_dzur, double* dzten_e, double* dzten_n,
+                                double* rho_dzten_e, double* rho_dzten_n, double* depth_zu, double* depth_zwu,
+                                double* thicku, double* thicken_e, double* thicken_n, double* mass_u,
+                                double* mass_en_e, double* mass_en_n) {
+  const double epsln = 1.0e-20; /* constants_mod epsln */
+  int ni = d->ni, nj = d->nj, nk = d->nk;
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+#define MIN4(a, b, c, e) fmind(fmind(fmind((a), (b)), (c)), (e))
+  if (vcoord == 1) {
+    for (int j = 0; j <= nj + 1; ++j)
+      for (int i = 0; i <= ni + 1; ++i) {
+        size_t q = I2(d, i, j);
+        double eu = linear_free_surface ? 0.0 : eta_u[q];
+        dzwu[q] = linear_free_surface ? depth_zt1[q] : depth_zt1[q] + eu;             /* dzwu(:,:,0) */
+        dzu[q] = linear_free_surface ? depth_zwt1[q] : depth_zwt1[q] + eu;            /* dzu(:,:,1) */
+        rho_dzu[q] = rho0 * dzu[q];
+        rho_dzur[q] = 1.0 / (rho_dzu[q] + epsln);
+      }
+  } else {
+    if (vcoord == 3 || vcoord == 6) {
+      for (int k = 0; k < nk; ++k)
+        for (size_t q = 0; q < n2; ++q) {
+          size_t p = (size_t)k * n2 + q;
+          dzu[p] = dzt[p];
+          dzten_e[p] = dzt[p];
+          dzten_n[p] = dzt[p];
+          dzwu[p + n2] = dzwt[p + n2];
+          rho_dzu[p] = rho_dzt[p];
+        }
+      for (size_t q = 0; q < n2; ++q) dzwu[q] = dzwt[q];
+    } else {
+      for (int k = 0; k < nk; ++k)
+        for (int j = 0; j <= nj; ++j)
+          for (int i = 0; i <= ni; ++i) {
+            size_t p = I3(d, i, j, k), pe = I3(d, i + 1, j, k), pn = I3(d, i, j + 1, k), pne = I3(d, i + 1, j + 1, k);
+            dzu[p] = MIN4(dzt[p], dzt[pe], dzt[pn], dzt[pne]);
+            dzwu[p + n2] = MIN4(dzwt[p + n2], dzwt[pe + n2], dzwt[pn + n2], dzwt[pne + n2]);
+            rho_dzu[p] = MIN4(rho_dzt[p], rho_dzt[pe], rho_dzt[pn], rho_dzt[pne]);
+            dzten_e[p] = fmind(dzt[p], dzt[pe]);
+            dzten_n[p] = fmind(dzt[p], dzt[pn]);
+            rho_dzten_e[p] = fmind(rho_dzt[p], rho_dzt[pe]);
+            rho_dzten_n[p] = fmind(rho_dzt[p], rho_dzt[pn]);
+          }
+      if (update_dzwu_k0)
+        for (int j = 0; j <= nj; ++j)
+          for (int i = 0; i <= ni; ++i)
+            dzwu[I2(d, i, j)] = MIN4(dzwt[I2(d, i, j)], dzwt[I2(d, i + 1, j)], dzwt[I2(d, i, j + 1)],
+                                     dzwt[I2(d, i + 1, j + 1)]);
+      orc_halo_update_3d(d, dzu, nk, 3);
+      orc_halo_update_3d(d, dzwu, nk + 1, 3);
+      orc_halo_update_3d(d, rho_dzu, nk, 3);
+      orc_halo_update_3d(d, dzten_e, nk, 3);
+      orc_halo_update_3d(d, dzten_n, nk, 3);
+      orc_halo_update_3d(d, rho_dzten_e, nk, 3);
+      orc_halo_update_3d(d, rho_dzten_n, nk, 3);
+    }
+    for (int k = 0; k < nk; ++k)
+      for (size_t q = 0; q < n2; ++q) {
+        size_t p = (size_t)k * n2 + q;
+        rho_dzur[p] = umask[p] / (rho_dzu[p] + epsln);
+      }
+    for (size_t q = 0; q < n2; ++q) {
+      depth_zu[q] = dzwu[q];
+      depth_zwu[q] = dzu[q];
+    }
+    for (int k = 1; k < nk; ++k)
+      for (size_t q = 0; q < n2; ++q) {
+        size_t p = (size_t)k * n2 + q;
+        depth_zu[p] = depth_zu[p - n2] + dzwu[p];          /* + dzwu(k-1): level k-1 of 0..nk is plane k */
+        depth_zwu[p] = depth_zwu[p - n2] + dzu[p];
+      }
+  }
+#undef MIN4
+  for (size_t q = 0; q < n2; ++q) {
+    int k = kmu[q];
+    thicku[q] = k > 1 ? depth_zwu[(size_t)(k - 1) * n2 + q] : 0.0;
+  }
+  for (size_t q = 0; q < n2; ++q) {
+    thicken_e[q] = 0.0;
+    thicken_n[q] = 0.0;
+    mass_u[q] = 0.0;
+    mass_en_e[q] = 0.0;
+    mass_en_n[q] = 0.0;
+  }
+  for (int k = 0; k < nk; ++k)
+    for (size_t q = 0; q < n2; ++q) {
+      size_t p = (size_t)k * n2 + q;
+      thicken_e[q] = thicken_e[q] + dzten_e[p];
+      thicken_n[q] = thicken_n[q] + dzten_n[p];
+    }
+  for (int k = 0; k < nk; ++k)
+    for (size_t q = 0; q < n2; ++q) {
+      size_t p = (size_t)k * n2 + q;
+      mass_u[q] = mass_u[q] + umask[p] * rho_dzu[p];
+    }
+  for (int k = 0; k < nk; ++k)
+    for (size_t q = 0; q < n2; ++q) {
+      size_t p = (size_t)k * n2 + q;
+      mass_en_e[q] = mass_en_e[q] + tmasken_e[p] * rho_dzten_e[p];
+    }
+  for (int k = 0; k < nk; ++k)
+    for (size_t q = 0; q < n2; ++q) {
+      size_t p = (size_t)k * n2 + q;
+      mass_en_n[q] = mass_en_n[q] + tmasken_n[p] * rho_dzten_n[p];
+    }
+}

@@ -340,3 +340,29 @@ def update_ocean_barotropic(d, g, state, nts, dtbt, gamma=0.2, rho0=1035.0, time
 def domain_arrays(dom) -> Dict[str, np.ndarray]:
     """numpy copies of a grid.Domain's arrays (the oracle's inputs)."""
     return {k: np64(v) for k, v in dom.f.items() if k != "kmt"}
+
+
+def update_ucell_thickness(d, vcoord, state, rho0=1035.0, linear_free_surface=False, update_dzwu_k0=True):
+    """update_ucell_thickness (ocean_thickness.F90:3507-3886), no blobs.  state maps
+    umask, tmasken_e, tmasken_n, dzt, dzwt (nk+1 levels), rho_dzt (level taup1),
+    depth_zt, depth_zwt (level 1 used), eta_u (level taup1), kmu and the fields it
+    updates: dzu, dzwu, rho_dzu (level taup1), rho_dzur, dzten_e/n, rho_dzten_e/n,
+    depth_zu, depth_zwu.  Returns new arrays of those plus thicku, mass_u,
+    thicken_e/n, mass_en_e/n."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    out = {k: f(state[k]).copy() for k in ("dzu", "dzwu", "rho_dzu", "rho_dzur", "dzten_e", "dzten_n", "rho_dzten_e",
+                                           "rho_dzten_n", "depth_zu", "depth_zwu")}
+    n2 = (d.nj + 2, d.ni + 2)
+    for k in ("thicku", "thicken_e", "thicken_n", "mass_u", "mass_en_e", "mass_en_n"):
+        out[k] = np.zeros(n2)
+    ins = [f(state[k]) for k in ("umask", "tmasken_e", "tmasken_n", "dzt", "dzwt", "rho_dzt")]
+    ins += [f(np.asarray(state["depth_zt"]).reshape(d.nk, *n2)[0]), f(np.asarray(state["depth_zwt"]).reshape(d.nk, *n2)[0]),
+            f(state["eta_u"])]
+    kmu = np.ascontiguousarray(state["kmu"], dtype=np.int32)
+    lib().orc_update_ucell_thickness(C.byref(d), int(vcoord), int(linear_free_surface), int(update_dzwu_k0),
+                                     C.c_double(rho0), *[p(a) for a in ins], kmu.ctypes.data_as(C.POINTER(C.c_int)),
+                                     *[p(out[k]) for k in ("dzu", "dzwu", "rho_dzu", "rho_dzur", "dzten_e", "dzten_n",
+                                                           "rho_dzten_e", "rho_dzten_n", "depth_zu", "depth_zwu",
+                                                           "thicku", "thicken_e", "thicken_n", "mass_u", "mass_en_e",
+                                                           "mass_en_n")])
+    return out

@@ -84,3 +84,44 @@ def test_barotropic_forcing_matches(gpu_lib, oracle_lib, cyclic_x, opt):
         got = d.get(fid)
         assert np.array_equal(got.view(np.uint64), ref.ravel().view(np.uint64)), f"{fid}: bits differ"
     d.close()
+
+
+@pytest.mark.parametrize("case", [(1, False, False, False), (1, True, False, True), (2, False, False, False),
+                                  (2, True, True, False), (5, True, False, False), (3, False, True, False),
+                                  (6, True, False, False)])
+def test_update_ucell_thickness_matches(gpu_lib, oracle_lib, case):
+    """update_ucell_thickness (ocean_thickness.F90:3507-3886) through
+    mom5gpu_update_ucell_thickness: the geopotential branch (also with
+    linear_free_surface), the minimum-of-neighbours branch of zstar and pstar
+    (also with update_dzwu_k0 off, on cyclic and walled domains) and the sigma
+    copies; every field it writes equal to the restatement on the data domain."""
+    capi, O = gpu_lib, oracle_lib
+    from mom5_gb300 import harness
+    F = capi.F
+    vcoord, cyclic, cyclic_y, linear = case
+    sp = grid.DomainSpec(ni=35, nj=27, nk=8, lon0=0.0, lon1=35.0, lat0=-30.0, lat1=30.0, cyclic_x=cyclic,
+                         cyclic_y=cyclic_y, continent=None, wavelength_cells=6.0, ntracers=1, seed=61)
+    dom = grid.make_domain(sp)
+    d = harness.load(dom)
+    st = grid.thickness_state(sp.ni, sp.nj, sp.nk, cyclic_x=cyclic, cyclic_y=cyclic_y, seed=7 + vcoord)
+    dzwu_k0 = vcoord != 5
+    taup1 = 2
+    fields = {"umask": (F.UMASK, 0), "tmasken_e": (F.TMASKEN_E, 0), "tmasken_n": (F.TMASKEN_N, 0),
+              "dzt": (F.DZT, 0), "dzwt": (F.DZWT, 0), "rho_dzt": (F.RHO_DZT, taup1), "depth_zt": (F.DEPTH_ZT, 0),
+              "depth_zwt": (F.DEPTH_ZWT, 0), "eta_u": (F.ETA_U, taup1), "dzu": (F.DZU, 0), "dzwu": (F.DZWU, 0),
+              "rho_dzu": (F.RHO_DZU, taup1), "rho_dzur": (F.RHO_DZUR, 0), "dzten_e": (F.DZTEN_E, 0),
+              "dzten_n": (F.DZTEN_N, 0), "rho_dzten_e": (F.RHO_DZTEN_E, 0), "rho_dzten_n": (F.RHO_DZTEN_N, 0),
+              "depth_zu": (F.DEPTH_ZU, 0), "depth_zwu": (F.DEPTH_ZWU, 0)}
+    for k, (fid, lev) in fields.items():
+        d.set(fid, np.ascontiguousarray(st[k]), level=lev)
+    d.update_ucell_thickness(taup1, vcoord, linear_free_surface=linear, update_dzwu_k0=dzwu_k0)
+    ref = O.update_ucell_thickness(O.dims(sp), vcoord, st, rho0=1035.0, linear_free_surface=linear,
+                                   update_dzwu_k0=dzwu_k0)
+    outs = dict(fields)
+    outs.update({"thicku": (F.THICKU, taup1), "thicken_e": (F.THICKEN_E, 0), "thicken_n": (F.THICKEN_N, 0),
+                 "mass_u": (F.MASS_U, taup1), "mass_en_e": (F.MASS_EN_E, 0), "mass_en_n": (F.MASS_EN_N, 0)})
+    for k in ref:
+        fid, lev = outs[k]
+        got = d.get(fid, level=lev)
+        assert np.array_equal(got, ref[k].ravel()), f"{k}: {np.abs(got - ref[k].ravel()).max():.3e}"
+    d.close()

@@ -395,3 +395,41 @@ def test_halo_update_semantics(O):
     O.halo_update(d, b)
     assert np.array_equal(b[0, 1:4, 0], a[0, 1:4, 4]) and np.array_equal(b[0, 1:4, 5], a[0, 1:4, 1])
     assert np.array_equal(b[0, 0, :], a[0, 0, :]) and np.array_equal(b[0, 4, :], a[0, 4, :])
+
+
+@pytest.mark.parametrize("vcoord", [1, 2, 3])
+def test_ucell_thickness_rules(O, vcoord):
+    """update_ucell_thickness (ocean_thickness.F90:3507-3886): the geopotential
+    branch moves only the top U cell with eta_u (:3617-3635); the sigma branch
+    copies the T-cell thicknesses (:3663-3683); the others take the minimum of
+    the neighbouring T cells (:3735-3763); depths are cumulative sums
+    (:3811-3827), thicku the depth of the bottom U level (:3817-3826), mass_u
+    and thicken vertical sums (:3829-3858)."""
+    ni, nj, nk = 10, 8, 5
+    st = grid.thickness_state(ni, nj, nk, seed=4)
+    d = O.dims(small(ni=ni, nj=nj, nk=nk))
+    out = O.update_ucell_thickness(d, vcoord, st)
+    rho0 = 1035.0
+    sl = (slice(None), slice(0, nj + 1), slice(0, ni + 1))  # computed by the min loops (isd:iec, jsd:jec)
+    if vcoord == 1:
+        assert np.array_equal(out["dzu"][0], st["depth_zwt"][0] + st["eta_u"])
+        assert np.array_equal(out["dzwu"][0], st["depth_zt"][0] + st["eta_u"])
+        assert np.array_equal(out["dzu"][1:], st["dzu"][1:]) and np.array_equal(out["depth_zwu"], st["depth_zwu"])
+        assert np.array_equal(out["rho_dzur"][0], 1.0 / (rho0 * out["dzu"][0] + 1e-20))
+    elif vcoord == 3:
+        assert np.array_equal(out["dzu"], st["dzt"]) and np.array_equal(out["rho_dzu"], st["rho_dzt"])
+        assert np.array_equal(out["dzwu"], st["dzwt"]) and np.array_equal(out["rho_dzten_e"], st["rho_dzten_e"])
+    else:
+        t = st["dzt"]
+        m4 = np.minimum(np.minimum(np.minimum(t[:, :-1, :-1], t[:, :-1, 1:]), t[:, 1:, :-1]), t[:, 1:, 1:])
+        assert np.array_equal(out["dzu"][sl], m4)
+        assert np.array_equal(out["dzten_e"][sl], np.minimum(t[:, :-1, :-1], t[:, :-1, 1:]))
+        assert np.array_equal(out["dzu"][:, :, ni + 1], st["dzu"][:, :, ni + 1])  # walled halo kept
+    if vcoord != 1:
+        assert np.allclose(out["depth_zwu"], np.cumsum(out["dzu"], axis=0), rtol=1e-14, atol=0)
+        assert np.array_equal(out["rho_dzur"], st["umask"] / (out["rho_dzu"] + 1e-20))
+    kmu = st["kmu"]
+    want = np.where(kmu > 1, np.take_along_axis(out["depth_zwu"], np.maximum(kmu - 1, 0)[None], 0)[0], 0.0)
+    assert np.array_equal(out["thicku"], want)
+    assert np.allclose(out["mass_u"], (st["umask"] * out["rho_dzu"]).sum(0), rtol=1e-14, atol=0)
+    assert np.allclose(out["thicken_n"], out["dzten_n"].sum(0), rtol=1e-14, atol=0)
