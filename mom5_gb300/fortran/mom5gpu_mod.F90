@@ -43,7 +43,10 @@ module mom5gpu_c
        F_TPME = 73, F_TRACER_ETA_SMOOTH = 74, F_PBOT_SMOOTH = 75, F_ACCEL_U = 112, F_ACCEL_V = 113, &
        F_SMF_U = 114, F_SMF_V = 115, F_BMF_U = 116, F_BMF_V = 117, &
        F_PSOM_S0 = 120, F_PSOM_SX = 121, F_PSOM_SXX = 122, F_PSOM_SY = 123, F_PSOM_SYY = 124, &
-       F_PSOM_SZ = 125, F_PSOM_SZZ = 126, F_PSOM_SXY = 127, F_PSOM_SXZ = 128, F_PSOM_SYZ = 129
+       F_PSOM_SZ = 125, F_PSOM_SZZ = 126, F_PSOM_SXY = 127, F_PSOM_SXZ = 128, F_PSOM_SYZ = 129, &
+       F_UMASK = 130, F_DZT = 131, F_DZWT = 132, F_DZU = 133, F_DZWU = 134, F_RHO_DZUR = 135, &
+       F_DZTEN_E = 136, F_DZTEN_N = 137, F_DEPTH_ZT = 138, F_DEPTH_ZWT = 139, F_DEPTH_ZU = 140, &
+       F_DEPTH_ZWU = 141, F_MASS_U = 142, F_MASS_EN_E = 143, F_MASS_EN_N = 144
   integer(c_int), parameter :: MOM5GPU_ADVECT_PSOM = 11
 
   type, bind(C) :: mom5gpu_dims
@@ -212,6 +215,12 @@ module mom5gpu_c
        import :: c_int, c_ptr
        type(c_ptr), value :: dom
      end function
+     integer(c_int) function mom5gpu_update_ucell_thickness(dom, taup1, vert_coordinate, linear_free_surface, &
+          update_dzwu_k0) bind(C, name="mom5gpu_update_ucell_thickness")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: taup1, vert_coordinate, linear_free_surface, update_dzwu_k0
+     end function
      integer(c_int) function mom5gpu_global_tracer_content(dom, n, level, total) &
           bind(C, name="mom5gpu_global_tracer_content")
        import :: c_int, c_ptr, c_double
@@ -232,7 +241,7 @@ module mom5gpu_mod
   use mpp_mod,          only: mpp_error, FATAL
   use ocean_types_mod,  only: ocean_time_type, ocean_adv_vel_type, ocean_thickness_type, ocean_density_type, &
                               ocean_prog_tracer_type, ocean_external_mode_type, ocean_velocity_type, &
-                              ocean_lagrangian_type
+                              ocean_lagrangian_type, ocean_grid_type
   implicit none
   private
 
@@ -240,6 +249,12 @@ module mom5gpu_mod
   public :: horz_advect_tracer, vert_advect_tracer
   public :: update_ocean_barotropic, eta_and_pbot_tendency, eta_and_pbot_update
   public :: ocean_advection_velocity, ocean_barotropic_forcing, device_restart_write
+  public :: update_ucell_thickness, device_thickness_options
+
+  ! ocean_thickness_nml switches and the vertical coordinate (ocean_parameters.F90:107-112)
+  ! used by update_ucell_thickness; set once by the host driver
+  integer(c_int), save :: thk_vert_coordinate = 1
+  integer(c_int), save :: thk_linear_free_surface = 0, thk_update_dzwu_k0 = 1
 
   type(c_ptr), save :: dom = c_null_ptr
   logical, save :: velocity_dirty = .true.
@@ -443,6 +458,46 @@ contains
     call check(mom5gpu_get_field(dom, F_FORCING_BT_U, 0, 0, Ext_mode%forcing_bt(:,:,1), 0), 'forcing_bt')
     call check(mom5gpu_get_field(dom, F_FORCING_BT_V, 0, 0, Ext_mode%forcing_bt(:,:,2), 0), 'forcing_bt')
   end subroutine ocean_barotropic_forcing
+
+  subroutine device_thickness_options(vert_coordinate, linear_free_surface, update_dzwu_k0)
+    integer, intent(in) :: vert_coordinate
+    logical, intent(in) :: linear_free_surface, update_dzwu_k0
+    thk_vert_coordinate = vert_coordinate
+    thk_linear_free_surface = merge(1, 0, linear_free_surface)
+    thk_update_dzwu_k0 = merge(1, 0, update_dzwu_k0)
+  end subroutine device_thickness_options
+
+  ! ocean_thickness.F90:3507-3512, no blobs.  The T-cell thickness fields
+  ! (F_DZT, F_DZWT, F_RHO_DZT, F_DEPTH_ZT, F_DEPTH_ZWT), Grd%umask (F_UMASK) and
+  ! Grd%tmasken are on the device (copied by the host driver); eta_u(taup1) goes
+  ! to the device and the U-cell and face thicknesses come back.
+  subroutine update_ucell_thickness(Time, Grid, Ext_mode, Thickness)
+    type(ocean_time_type),          intent(in)    :: Time
+    type(ocean_grid_type),          intent(in)    :: Grid
+    type(ocean_external_mode_type), intent(in)    :: Ext_mode
+    type(ocean_thickness_type),     intent(inout) :: Thickness
+    integer :: taup1
+    taup1 = Time%taup1
+    call check(mom5gpu_set_field(dom, F_ETA_U, 0, taup1, Ext_mode%eta_u(:,:,taup1), 0), 'eta_u')
+    call check(mom5gpu_update_ucell_thickness(dom, taup1, thk_vert_coordinate, thk_linear_free_surface, &
+         thk_update_dzwu_k0), 'update_ucell_thickness')
+    call check(mom5gpu_get_field(dom, F_DZU, 0, 0, Thickness%dzu, 0), 'dzu')
+    call check(mom5gpu_get_field(dom, F_DZWU, 0, 0, Thickness%dzwu, 0), 'dzwu')
+    call check(mom5gpu_get_field(dom, F_RHO_DZU, 0, taup1, Thickness%rho_dzu(:,:,:,taup1), 0), 'rho_dzu')
+    call check(mom5gpu_get_field(dom, F_RHO_DZUR, 0, 0, Thickness%rho_dzur, 0), 'rho_dzur')
+    call check(mom5gpu_get_field(dom, F_DZTEN_E, 0, 0, Thickness%dzten(:,:,:,1), 0), 'dzten')
+    call check(mom5gpu_get_field(dom, F_DZTEN_N, 0, 0, Thickness%dzten(:,:,:,2), 0), 'dzten')
+    call check(mom5gpu_get_field(dom, F_RHO_DZTEN_E, 0, 0, Thickness%rho_dzten(:,:,:,1), 0), 'rho_dzten')
+    call check(mom5gpu_get_field(dom, F_RHO_DZTEN_N, 0, 0, Thickness%rho_dzten(:,:,:,2), 0), 'rho_dzten')
+    call check(mom5gpu_get_field(dom, F_DEPTH_ZU, 0, 0, Thickness%depth_zu, 0), 'depth_zu')
+    call check(mom5gpu_get_field(dom, F_DEPTH_ZWU, 0, 0, Thickness%depth_zwu, 0), 'depth_zwu')
+    call check(mom5gpu_get_field(dom, F_THICKU, 0, taup1, Thickness%thicku(:,:,taup1), 0), 'thicku')
+    call check(mom5gpu_get_field(dom, F_THICKEN_E, 0, 0, Thickness%thicken(:,:,1), 0), 'thicken')
+    call check(mom5gpu_get_field(dom, F_THICKEN_N, 0, 0, Thickness%thicken(:,:,2), 0), 'thicken')
+    call check(mom5gpu_get_field(dom, F_MASS_U, 0, taup1, Thickness%mass_u(:,:,taup1), 0), 'mass_u')
+    call check(mom5gpu_get_field(dom, F_MASS_EN_E, 0, 0, Thickness%mass_en(:,:,1), 0), 'mass_en')
+    call check(mom5gpu_get_field(dom, F_MASS_EN_N, 0, 0, Thickness%mass_en(:,:,2), 0), 'mass_en')
+  end subroutine update_ucell_thickness
 
   ! The restart files of the device-resident state at Time%taup1, in the layout
   ! save_restart writes (ocean_tracer_restart, ocean_tracer.F90:2658-2681, and the
