@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kTX) kb_mdfl_x(const MdflArgs* d, BatchWork w)
 }
 
 template <bool SWEBY, int MAXN>
-__global__ void __launch_bounds__(128) kb_mdfl_y(const MdflArgs* d, BatchWork w, int TJ) {
+__global__ void __launch_bounds__(128, 6) kb_mdfl_y(const MdflArgs* d, BatchWork w, int TJ) {
   int e = find_entry(w.py, w.count, blockIdx.x);
   const MdflArgs& a = d[w.entries[e]];
   int local = blockIdx.x - w.py[e];

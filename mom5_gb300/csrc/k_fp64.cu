@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kTX) k_mdfl_x(MdflArgs a) {
 }
 
 template <bool ALL, bool SWEBY, int MAXN>
-__global__ void __launch_bounds__(128) k_mdfl_y(MdflArgs a, int TJ) {
+__global__ void __launch_bounds__(128, 6) k_mdfl_y(MdflArgs a, int TJ) {
   mdfl_y_body<ALL, SWEBY, MAXN>(a, TJ, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
