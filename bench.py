@@ -7,15 +7,18 @@ update_ocean_barotropic (predictor-corrector subcycles + time averages).
 
 Workload (N=1): 1440x1080x50, 0.25 degree, lat -80..80, cyclic in x, 10 tracers,
 MDFL Sweby + 60 barotropic subcycles, dtts = dtuv = 600 s, dtbt = 20 s; seeded
-synthetic inputs.  Metric: cell-updates/s (cells x steps / s).
+synthetic inputs.  Metric: cell-updates/s (cells x steps / s).  The other
+workloads (--config) keep their own time steps: c0 120x80x30 advection at
+dt = 3600 s; c1 360x300 barotropic, 80 subcycles of 67.5 s (dtuv = 2700 s).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed] [--config c2|c0|c1]
+                  [--precision fp64|mixed] [--config c2|c0|c1|c2s]
 
 --impl reference times the reference's CPU algorithm (the C restatement in
 oracle/, the reference Fortran cannot be compiled on these hosts) on all host
-cores: the domain is split into one block per process, as MPI ranks would hold
-it, each block stepped independently (no halo exchange is charged).
+cores: the whole workload grid, stepped by the restatement's C loop with its
+scratch held across steps and its loops spread over the cores with OpenMP
+(one block per process when the compiler has no OpenMP).
 """
 from __future__ import annotations
 
@@ -33,9 +36,42 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s (1 GB300): FP64 drop-in vs batched mixed-precision; p99 latency"
-DTTS = 600.0
-DTBT = 20.0
-NTS = 60
+
+
+class Workload:
+    """A named workload: its domain, baroclinic step and barotropic subcycle.
+    nts = nint(2*dtuv/dtbt) with dtuv = dtts (ocean_barotropic.F90:1109-1115)."""
+
+    def __init__(self, name, spec_fn, dtts, dtbt=None):
+        self.name, self.spec_fn, self.dtts, self.dtbt = name, spec_fn, dtts, dtbt
+
+    @property
+    def barotropic(self):
+        return self.dtbt is not None
+
+    @property
+    def nts(self):
+        return int(round(2.0 * self.dtts / self.dtbt)) if self.barotropic else 0
+
+    def spec(self):
+        from mom5_gb300 import grid
+        return getattr(grid, self.spec_fn)()
+
+    def describe(self, spec):
+        parts = [f"{spec.ni}x{spec.nj}x{spec.nk}"]
+        if spec.ntracers:
+            parts.append(f"{spec.ntracers} tracers, MDFL Sweby, dtts={self.dtts:g}s")
+        if self.barotropic:
+            parts.append(f"{self.nts}-subcycle B-grid barotropic, dtbt={self.dtbt:g}s (dtuv={self.dtts:g}s)")
+        return ", ".join(parts)
+
+
+WORKLOADS = {
+    "c2": Workload("c2", "config_c2", 600.0, 20.0),
+    "c2s": Workload("c2s", "config_c2_block", 600.0, 20.0),
+    "c0": Workload("c0", "config_c0", 3600.0),
+    "c1": Workload("c1", "config_c1", 2700.0, 67.5),
+}
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 HBM_FALLBACK = 6800.0  # GB/s
 
@@ -48,19 +84,6 @@ def hbm_peak():
         return HBM_FALLBACK, "fallback"
 
 
-def config_spec(name: str, ntr_override=None):
-    from mom5_gb300 import grid
-    if name == "c2":
-        return grid.config_c2(ntracers=ntr_override or 10)
-    if name == "c0":
-        return grid.config_c0()
-    if name == "c1":
-        return grid.config_c1()
-    if name == "c2s":
-        return grid.config_c2_block()
-    raise SystemExit(f"unknown config {name}")
-
-
 def adv_bytes(ni, nj, nk, ntr):
     """Algorithmic bytes of one fused advection step incl. the state update:
     read T and write T(taup1) per tracer, read u, v, w, rho_dzt, rho_dztr per cell,
@@ -68,15 +91,14 @@ def adv_bytes(ni, nj, nk, ntr):
     return 8 * ni * nj * nk * (2 * ntr + 5) + 8 * ni * nj * 7
 
 
-# DRAM bytes per tracer-cell of the advection launch set, from the ncu capture of the
-# 360x270x50 block (profiles/traffic_advection_c2block.md): FP64 4.740 GB, precision form
-# 0.975 GB for 360*270*50*10 tracer-cells.
+# DRAM bytes per tracer-cell of the advection launch set, from an ncu capture of the
+# 360x270x50 block: FP64 4.740 GB, precision form 0.975 GB for 360*270*50*10 tracer-cells.
 TRAFFIC_PER_TRACER_CELL = {"fp64": 4.740e9 / (360 * 270 * 50 * 10), "mixed": 0.975e9 / (360 * 270 * 50 * 10)}
 
 
 # FP64 thread-instructions per tracer-cell of the exact MDFL passes (z + x + y) and per
-# column of one exact barotropic subcycle, from ncu (profiles/fp64_ops_c2block.md); the
-# FP64 rate of GB300 measured on this machine with a probe kernel.
+# column of one exact barotropic subcycle, counted by ncu on the 360x270x50 block; the
+# FP64 instruction rate of GB300 measured with a probe kernel.
 FP64_OPS_PER_TRACER_CELL = 62.4
 FP64_OPS_PER_COLUMN_SUBCYCLE = 52.8
 FP64_PEAK_OPS = 5.05e11
@@ -138,68 +160,95 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------- CPU side (reference algorithm)
-def _ref_worker(args):
-    """One host process: one block of the workload stepped with the C restatement."""
-    (ni, nj, nk, ntr, lat0, lat1, lon0, lon1, seed, warmup, steps, nts) = args
+def _oracle_inputs(spec):
+    """The restatement's inputs for `spec`: grid arrays, tracers and barotropic state (numpy)."""
     import numpy as np
     import torch
-    torch.set_num_threads(1)
     from mom5_gb300 import grid
     from oracle import oracle as O
-    sp = grid.DomainSpec(ni=ni, nj=nj, nk=nk, lon0=lon0, lon1=lon1, lat0=lat0, lat1=lat1, cyclic_x=False,
-                         continent=None, hmin=2000.0, ntracers=ntr, seed=seed)
-    dom = grid.make_domain(sp)
+    dom = grid.make_domain(spec)
     g = O.domain_arrays(dom)
-    d = O.dims(sp)
-    T = [g["T"][n].copy() for n in range(ntr)]
+    del dom
+    if spec.ntracers > 0:
+        T = g.pop("T")
+    else:
+        T = np.zeros((0, spec.nk, spec.nj + 2, spec.ni + 2))
     st = {k: g[k].copy() for k in ("eta_t", "eta_t_bar", "udrho_u", "udrho_v")}
-
-    def step():
-        nonlocal st
-        for n in range(ntr):
-            th = O.advect_mdfl_sweby(d, g, T[n], DTTS)
-            T[n] = O.update_tracer(d, g, T[n], th, DTTS)
-        out = O.update_ocean_barotropic(d, g, st, nts, DTBT)
-        st = {"eta_t": st["eta_t"], "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"],
-              "udrho_v": out["udrho_v"]}
-
-    for _ in range(warmup):
-        step()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        step()
-    return time.perf_counter() - t0, ni * nj * nk * steps
+    return O, g, T, st
 
 
-def cpu_reference(spec, warmup, steps, procs, block_frac=1.0):
-    """Time the reference algorithm on `procs` host processes, one block each."""
-    import multiprocessing as mp
+def _ref_worker(args):
+    """One host process: `spec` stepped by the restatement's C loop (orc_run_steps),
+    single-threaded or with OpenMP over `threads` cores.  One untimed step sizes
+    the sample: then min(steps, budget_s / its time) timed steps from there on.
+    Returns (seconds, cells x timed steps, timed steps)."""
+    spec, wl, steps, threads, budget_s = args
+    import torch
+    if threads == 1:
+        torch.set_num_threads(1)
+    O, g, T, st = _oracle_inputs(spec)
+    d = O.dims(spec)
+    kw = dict(nts=wl.nts, dtbt=wl.dtbt or 0.0, threaded=threads > 1, threads=threads)
+    t1, res = O.run_steps(d, g, T, wl.dtts, warmup=0, steps=1, state=st, **kw)
+    if res is not None:
+        st = {"eta_t": st["eta_t"], "eta_t_bar": res["eta_t_bar"], "udrho_u": res["udrho_u"],
+              "udrho_v": res["udrho_v"]}
+    n = max(1, min(steps, int(budget_s / max(t1, 1e-6))))
+    sec, _ = O.run_steps(d, g, T, wl.dtts, warmup=0, steps=n, state=st, **kw)
+    return sec, spec.ni * spec.nj * spec.nk * n, n
+
+
+def _block_specs(spec, procs):
+    """One walled block per process (an MPI-rank-like split of the grid)."""
+    import dataclasses
     px = int(round(math.sqrt(procs)))
     while procs % px:
         px -= 1
     py = procs // px
-    bi = max(8, int(spec.ni / px * math.sqrt(block_frac)))
-    bj = max(8, int(spec.nj / py * math.sqrt(block_frac)))
+    bi, bj = max(8, spec.ni // px), max(8, spec.nj // py)
     dlon = (spec.lon1 - spec.lon0) / spec.ni
     dlat = (spec.lat1 - spec.lat0) / spec.nj
-    jobs = []
+    out = []
     for b in range(procs):
         ix, iy = b % px, b // px
-        lon0 = spec.lon0 + ix * (spec.ni // px) * dlon
-        lat0 = spec.lat0 + iy * (spec.nj // py) * dlat
-        jobs.append((bi, bj, spec.nk, spec.ntracers, lat0, lat0 + bj * dlat, lon0, lon0 + bi * dlon,
-                     1000 + b, warmup, steps, NTS))
+        lon0 = spec.lon0 + ix * bi * dlon
+        lat0 = spec.lat0 + iy * bj * dlat
+        out.append(dataclasses.replace(spec, ni=bi, nj=bj, lon0=lon0, lon1=lon0 + bi * dlon, lat0=lat0,
+                                       lat1=lat0 + bj * dlat, cyclic_x=False, cyclic_y=False, continent=None,
+                                       seed=1000 + b))
+    return out
+
+
+def cpu_reference(wl, spec, steps, cores, budget_s=150.0):
+    """The reference algorithm on `cores` host cores: the whole grid in one
+    process with OpenMP (the C loop's scratch held across steps); when the
+    compiler has no OpenMP, one walled block per process.  Timed steps are
+    capped so that the run stays within about budget_s seconds."""
+    import multiprocessing as mp
     ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        res = pool.map(_ref_worker, jobs)
-    tmax = max(r[0] for r in res)
-    cells = sum(r[1] for r in res)
-    return cells / tmax, {"block": [bi, bj, spec.nk], "procs": procs, "seconds": tmax,
-                          "cells_per_step": bi * bj * spec.nk * procs}
+    try:
+        from oracle import oracle as O
+        O.build_omp()
+        omp = True
+    except Exception:
+        omp = False
+    if omp:
+        with ctx.Pool(1) as pool:
+            sec, cells, n = pool.apply(_ref_worker, ((spec, wl, steps, cores, budget_s),))
+        return cells / sec, {"grid": [spec.ni, spec.nj, spec.nk], "threads": cores, "steps_timed": n,
+                             "seconds": round(sec, 3), "parallelism": "OpenMP over rows and levels",
+                             "same_config": True}
+    blocks = _block_specs(spec, cores)
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_worker, [(b, wl, steps, 1, budget_s) for b in blocks])
+    rate = sum(c / s for s, c, _ in res)
+    return rate, {"block": [blocks[0].ni, blocks[0].nj, spec.nk], "procs": cores,
+                  "steps_timed": min(r[2] for r in res), "seconds": round(max(r[0] for r in res), 3),
+                  "parallelism": "one walled block per process", "same_config": False}
 
 
 # --------------------------------------------------------------------------- GPU side
-def _time_domain(d, stream, ntr, steps, warmup, state, clock_index=0):
+def _time_domain(d, stream, wl, ntr, steps, warmup, state, clock_index=0):
     """Warm up, then time `steps` whole steps of one domain on `stream` (CUDA events)."""
     import torch
 
@@ -207,8 +256,9 @@ def _time_domain(d, stream, ntr, steps, warmup, state, clock_index=0):
         tau = state["tau"]
         taup1 = 3 - tau
         if ntr > 0:
-            d.tracer_advection_step(tau, tau, taup1, DTTS)
-        d.update_ocean_barotropic(tau, taup1)
+            d.tracer_advection_step(tau, tau, taup1, wl.dtts)
+        if wl.barotropic:
+            d.update_ocean_barotropic(tau, taup1)
         state["tau"] = taup1
 
     for _ in range(warmup):
@@ -241,14 +291,15 @@ def _fp64_roofline(prec, sec, steps, cells, ntr, ni, nj, nts):
     mdfl_s = sec["mdfl"][0] / steps / 1e3
     bt_s = sec["barotropic"][0] / steps / 1e3
     a = FP64_OPS_PER_TRACER_CELL * cells * ntr / mdfl_s
-    b = FP64_OPS_PER_COLUMN_SUBCYCLE * (ni + 2) * (nj + 2) * nts / bt_s
+    b = FP64_OPS_PER_COLUMN_SUBCYCLE * (ni + 2) * (nj + 2) * nts / bt_s if bt_s > 0 else 0.0
     return {"bound": "fp64 pipe", "unit": "FP64 instructions/s", "peak": FP64_PEAK_OPS,
             "peak_source": "probe kernel on this pool (FP64 FMA rate)",
             "mdfl": {"achieved": round(a, -6), "frac": round(a / FP64_PEAK_OPS, 3),
                      "ops_per_tracer_cell": FP64_OPS_PER_TRACER_CELL},
             "barotropic": {"achieved": round(b, -6), "frac": round(b / FP64_PEAK_OPS, 3),
                            "ops_per_column_subcycle": FP64_OPS_PER_COLUMN_SUBCYCLE},
-            "source": "instruction counts from ncu (profiles/fp64_ops_c2block.md)"}
+            "source": "FP64 instruction counts per tracer-cell and per column-subcycle from ncu on a "
+                      "360x270x50 block"}
 
 
 def max_over_ranks(ms: float, device) -> float:
@@ -281,16 +332,114 @@ def _rel_err(a, b):
     return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
 
 
+def run_e2e(d, stream, wl, ntr, steps, warm=3):
+    """End to end through the C ABI with host buffers: every step uploads its
+    inputs from pinned host memory (tracers and advection velocity; the
+    barotropic forcing) and reads its results back (tracers; eta_t_bar, udrho),
+    stream-ordered copies (mom5gpu_copy_field_async) on an upload and a
+    read-back stream, ordered by events.  Three time levels rotate so that the
+    uploads of step s+1 and the read-back of step s overlap the compute of step
+    s.  Single-level inputs (velocity, forcing) are uploaded into a device
+    staging buffer while the previous step still reads the field and copied
+    into it (device to device) once that step is past it.  `warm` untimed
+    steps first (first-touch allocations, graph captures); the timed steps are
+    timed on the host wall clock and each stream's work by CUDA events."""
+    import numpy as np
+    import torch
+    from mom5_gb300.capi import F
+    pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True)
+    n3, nw = d.count(F.TRACER), d.count(F.WRHO_BT)
+    n2 = d.count(F.ETA_T_BAR)
+    ups, downs = [], []  # (field, n, host buffer) per step
+    stage = []           # (field, host buffer, device staging buffer, read by advection?)
+    if ntr > 0:
+        for n in range(1, ntr + 1):
+            h = pin(n3)
+            h.copy_(torch.from_numpy(d.get(F.TRACER, n=n, level=1)))
+            ups.append((F.TRACER, n, h))
+            downs.append((F.TRACER, n, pin(n3)))
+        for fid, cnt in ((F.UHRHO_ET, n3), (F.VHRHO_NT, n3), (F.WRHO_BT, nw)):
+            h = pin(cnt)
+            h.copy_(torch.from_numpy(d.get(fid)))
+            stage.append((fid, h, torch.empty(cnt, dtype=torch.float64, device="cuda"), True))
+        for fid in (F.RHO_DZT,):  # the third level of the rotation
+            d.set(fid, d.get(fid, level=1), level=3)
+    if wl.barotropic:
+        for fid in (F.FORCING_BT_U, F.FORCING_BT_V):
+            h = pin(n2)
+            h.copy_(torch.from_numpy(d.get(fid)))
+            stage.append((fid, h, torch.empty(n2, dtype=torch.float64, device="cuda"), False))
+        for fid in (F.ETA_T_BAR, F.UDRHO_U, F.UDRHO_V):
+            downs.append((fid, 0, pin(n2)))
+        d.set(F.THICKU, d.get(F.THICKU, level=1), level=3)
+        for fid in (F.ETA_T_BAR, F.UDRHO_U, F.UDRHO_V, F.CONV_RHO_UD_T):
+            d.set(fid, d.get(fid, level=1), level=3)
+    h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
+    total = warm + steps
+    tev = lambda: torch.cuda.Event(enable_timing=True)
+    ev = {k: [tev() for _ in range(total)] for k in ("h2d0", "h2d1", "c0", "adv", "c1", "d2h0", "d2h1")}
+    torch.cuda.synchronize()
+    t0 = None
+    for s_ in range(total):
+        if s_ == warm:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        lin, lout = (1, 2, 3)[(2 * s_) % 3], (1, 2, 3)[(2 * s_ + 1) % 3]
+        if s_ >= 2:  # lin was read back by step s-2
+            h2d.wait_event(ev["d2h1"][s_ - 2])
+        ev["h2d0"][s_].record(h2d)
+        for fid, n, h in ups:
+            d.copy_field_async(fid, h.data_ptr(), 1, h2d.cuda_stream, n=n, level=lin)
+        with torch.cuda.stream(h2d):  # the staging buffers' last reader is earlier on h2d
+            for fid, h, buf, _ in stage:
+                buf.copy_(h, non_blocking=True)
+        for phase in (True, False):  # fields the advection reads, then the barotropic forcing
+            if s_ >= 1:
+                h2d.wait_event(ev["adv"][s_ - 1] if phase else ev["c1"][s_ - 1])
+            for fid, h, buf, adv in stage:
+                if adv == phase:
+                    d.copy_field_async(fid, buf.data_ptr(), 1, h2d.cuda_stream)
+        ev["h2d1"][s_].record(h2d)
+        stream.wait_event(ev["h2d1"][s_])
+        ev["c0"][s_].record(stream)
+        if ntr > 0:
+            d.tracer_advection_step(lin, lin, lout, wl.dtts)
+        ev["adv"][s_].record(stream)
+        if wl.barotropic:
+            d.update_ocean_barotropic(lin, lout)
+        ev["c1"][s_].record(stream)
+        d2h.wait_event(ev["c1"][s_])
+        ev["d2h0"][s_].record(d2h)
+        for fid, n, h in downs:
+            d.copy_field_async(fid, h.data_ptr(), 0, d2h.cuda_stream, n=n, level=lout)
+        ev["d2h1"][s_].record(d2h)
+    torch.cuda.synchronize()
+    te = (time.perf_counter() - t0) / steps
+    rng = range(warm, total)
+    mean = lambda a, b: float(np.mean([ev[a][s].elapsed_time(ev[b][s]) for s in rng]))
+    wait = float(np.mean([ev["c1"][s - 1].elapsed_time(ev["c0"][s]) for s in rng]))
+    span = ev["c0"][warm].elapsed_time(ev["c1"][total - 1]) / steps
+    hb = 8 * (sum(h.numel() for _, _, h in ups) + sum(h.numel() for _, h, _, _ in stage))
+    db = 8 * sum(h.numel() for _, _, h in downs)
+    timeline = {"unit": "ms per step (means over the timed steps, CUDA events)",
+                "host_wall": round(te * 1e3, 3), "compute_span": round(span, 3),
+                "upload": round(mean("h2d0", "h2d1"), 3), "compute": round(mean("c0", "c1"), 3),
+                "readback": round(mean("d2h0", "d2h1"), 3), "compute_waits_for_upload": round(wait, 3),
+                "upload_GBps": round(hb / mean("h2d0", "h2d1") / 1e6, 1),
+                "readback_GBps": round(db / mean("d2h0", "d2h1") / 1e6, 1)}
+    return te, hb, db, timeline
+
+
 def run_ours(args, rank, world):
     import torch
 
     from mom5_gb300 import build, capi, grid, harness
-    from mom5_gb300.capi import F
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     build.build()
-    spec = config_spec(args.config)
+    wl = WORKLOADS[args.config]
+    spec = wl.spec()
     prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_FP64
     headline = args.scheme == "mdfl_sweby"
     forms = (not args.no_forms) and world == 1 and prec == capi.PRECISION_FP64 and args.config == "c2" and headline
@@ -302,7 +451,8 @@ def run_ours(args, rank, world):
         for n in range(1, spec.ntracers + 1):
             d.set_tracer_scheme(n, sid, sid, -1.0e10, 1.0e10)
             d.set_psom_limit(n, True)
-    nts = d.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
+    nts = d.barotropic_init(dtuv=wl.dtts, dtbt=wl.dtbt) if wl.barotropic else 0
+    assert nts == wl.nts
     ni, nj, nk, ntr = spec.ni, spec.nj, spec.nk, spec.ntracers
     cells = ni * nj * nk
     if not forms:
@@ -316,11 +466,11 @@ def run_ours(args, rank, world):
 
     state = {"tau": 1}
     # trial steps 1 -> 2; the timed steps start at level 1
-    tune = d.autotune(DTTS) if ntr > 0 and not args.no_autotune else None
+    tune = d.autotune(wl.dtts) if ntr > 0 and not args.no_autotune else None
     if world > 1:
         torch.distributed.barrier()
-    r = _time_domain(d, stream, ntr, args.steps, args.warmup, state, local)
-    ms, sec, launches, clk, step = r["ms"], r["sec"], r["launches"], r["clocks"], r["step"]
+    r = _time_domain(d, stream, wl, ntr, args.steps, args.warmup, state, local)
+    ms, sec, launches, clk = r["ms"], r["sec"], r["launches"], r["clocks"]
     if world > 1:
         ms = max_over_ranks(ms, "cuda")
     ms_step = ms / args.steps
@@ -330,6 +480,12 @@ def run_ours(args, rank, world):
     adv_ms = sec["mdfl"][0] + sec["mdfl_mixed"][0] + sec["tracer_update"][0]
     adv_calls = max(1, max(sec["mdfl"][1], sec["mdfl_mixed"][1]))
     peak, peak_kind = hbm_peak()
+    bt_ms = sec["barotropic"][0] / max(1, sec["barotropic"][1])
+    bt_roof = None
+    if wl.barotropic and bt_ms > 0:
+        bt_achieved = bt_bytes(ni, nj, nts) / (bt_ms / 1e3) / 1e9
+        bt_roof = {"achieved": round(bt_achieved, 1), "unit": "GB/s", "peak": peak,
+                   "frac": round(bt_achieved / peak, 4), "note": "streaming model, 224 B/column/subcycle"}
     if ntr > 0:
         bytes_adv = adv_bytes(ni, nj, nk, ntr)
         per = adv_ms / adv_calls
@@ -339,103 +495,49 @@ def run_ours(args, rank, world):
                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_launch": bytes_adv, "ms_per_launch": round(per, 3),
                     "traffic": round(TRAFFIC_PER_TRACER_CELL[args.precision] * cells * ntr) if headline else None,
-                    "traffic_source": "ncu DRAM bytes of the 360x270x50 block scaled by tracer-cells "
-                                      "(profiles/traffic_advection_c2block.md)"}
+                    "traffic_source": "ncu DRAM bytes of the advection launch set on a 360x270x50 block, "
+                                      "scaled by tracer-cells"}
+    elif bt_roof is not None:
+        roofline = dict(bt_roof, bound="hbm", kernel="barotropic subcycle loop (streaming model)",
+                        peak_source=peak_kind, algorithmic_bytes_per_launch=bt_bytes(ni, nj, nts),
+                        ms_per_launch=round(bt_ms, 3), traffic=None)
     else:
         roofline = None
-    bt_ms = sec["barotropic"][0] / max(1, sec["barotropic"][1])
-    bt_achieved = bt_bytes(ni, nj, nts) / (bt_ms / 1e3) / 1e9
 
-    # end to end through the C ABI with host buffers: every step uploads its
-    # inputs (tracers, advection velocity) from pinned host memory and reads its
-    # results back, pipelined over three time levels so that the uploads of step
-    # s+1 and the read-back of step s overlap the compute (stream-ordered copies,
-    # mom5gpu_copy_field_async, ordered by events).  The velocity has one device
-    # field, read by the advection: step s+1's velocity is uploaded into a device
-    # staging buffer while step s advects and copied into the field (device to
-    # device) while step s runs its barotropic subcycle.
     e2e = None
-    if not args.no_e2e and ntr > 0:
-        pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True)
-        n3 = d.count(F.TRACER)
-        n2 = d.count(F.ETA_T_BAR)
-        nw = d.count(F.WRHO_BT)
-        hT = [pin(n3) for _ in range(ntr)]
-        hU, hV, hW = pin(n3), pin(n3), pin(nw)
-        for n in range(ntr):
-            hT[n].copy_(torch.from_numpy(d.get(F.TRACER, n=n + 1, level=state["tau"])))
-        hU.copy_(torch.from_numpy(d.get(F.UHRHO_ET)))
-        hV.copy_(torch.from_numpy(d.get(F.VHRHO_NT)))
-        hW.copy_(torch.from_numpy(d.get(F.WRHO_BT)))
-        for fid in (F.RHO_DZT, F.THICKU):  # the third time level of the rotation
-            d.set(fid, d.get(fid, level=1), level=3)
-        oT = [pin(n3) for _ in range(ntr)]
-        oE, oU, oV = pin(n2), pin(n2), pin(n2)
-        sU, sV, sW = (torch.empty(n, dtype=torch.float64, device="cuda") for n in (n3, n3, nw))
-        ke = max(3, min(args.steps, 30))
-        h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
-        ev = lambda: torch.cuda.Event()
-        h2d_done, adv_done, comp_done, d2h_done = ([ev() for _ in range(ke)] for _ in range(4))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for s_ in range(ke):
-            lin, lout = (1, 2, 3)[(2 * s_) % 3], (1, 2, 3)[(2 * s_ + 1) % 3]
-            if s_ >= 2:  # lin was read back by step s-2
-                h2d.wait_event(d2h_done[s_ - 2])
-            for n in range(ntr):
-                d.copy_field_async(F.TRACER, hT[n].data_ptr(), 1, h2d.cuda_stream, n=n + 1, level=lin)
-            with torch.cuda.stream(h2d):  # the staging buffer is free: its last copy is earlier on h2d
-                for buf, dst in ((hU, sU), (hV, sV), (hW, sW)):
-                    dst.copy_(buf, non_blocking=True)
-            if s_ >= 1:  # the velocity field is read by the advection of step s-1 (not by its barotropic part)
-                h2d.wait_event(adv_done[s_ - 1])
-            for fid, buf in ((F.UHRHO_ET, sU), (F.VHRHO_NT, sV), (F.WRHO_BT, sW)):
-                d.copy_field_async(fid, buf.data_ptr(), 1, h2d.cuda_stream)
-            h2d_done[s_].record(h2d)
-            stream.wait_event(h2d_done[s_])
-            d.tracer_advection_step(lin, lin, lout, DTTS)
-            adv_done[s_].record(stream)
-            d.update_ocean_barotropic(lin, lout)
-            comp_done[s_].record(stream)
-            d2h.wait_event(comp_done[s_])
-            for n in range(ntr):
-                d.copy_field_async(F.TRACER, oT[n].data_ptr(), 0, d2h.cuda_stream, n=n + 1, level=lout)
-            for fid, buf in ((F.ETA_T_BAR, oE), (F.UDRHO_U, oU), (F.UDRHO_V, oV)):
-                d.copy_field_async(fid, buf.data_ptr(), 0, d2h.cuda_stream, level=lout)
-            d2h_done[s_].record(d2h)
-        torch.cuda.synchronize()
-        te = (time.perf_counter() - t0) / ke
-        e2e = {"value": round(cells / te, 1), "unit": "cell-updates/s",
-               "h2d_bytes_per_step": 8 * (ntr * n3 + 2 * n3 + nw), "d2h_bytes_per_step": 8 * (ntr * n3 + 3 * n2),
-               "steps": ke, "api": "mom5gpu_copy_field_async (pinned host buffers, upload and read-back streams) / "
-                                   "mom5gpu_tracer_advection_step / mom5gpu_update_ocean_barotropic",
+    if not args.no_e2e:
+        te, hb, db, timeline = run_e2e(d, stream, wl, ntr, max(3, min(args.steps, 30)))
+        e2e = {"value": round(cells / te, 1), "unit": "cell-updates/s", "h2d_bytes_per_step": hb,
+               "d2h_bytes_per_step": db, "steps": max(3, min(args.steps, 30)),
+               "api": "mom5gpu_copy_field_async (pinned host buffers, upload and read-back streams) / "
+                      "mom5gpu_tracer_advection_step / mom5gpu_update_ocean_barotropic",
                "timing": "host wall clock over the steps, every copy inside; copies of neighbouring steps overlap "
-                         "the compute (three time levels rotate; the velocity goes through a device staging buffer)"}
-        del hT, oT, hU, hV, hW, sU, sV, sW
+                         "the compute (three time levels rotate; single-level inputs go through device staging "
+                         "buffers)", "timeline": timeline}
 
+    l2note = ("inputs larger than L2 (tracer state alone %.1f GB)" % (2 * ntr * cells * 8 / 1e9)
+              if 2 * ntr * cells * 8 > 129e6 else "inputs smaller than L2, not flushed (launch/latency-bound case)")
     out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-updates/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == capi.PRECISION_FP64 else "f32+f64",
            "data": "synthetic (seeded streamfunction flow, partial-cell bathymetry)",
-           "config": {"workload": f"{args.config.upper()}: {ni}x{nj}x{nk}, {ntr} tracers, "
-                                  f"{'MDFL Sweby' if headline else args.scheme} + {nts}-subcycle "
-                                  f"B-grid barotropic, dtts={DTTS:g}s dtbt={DTBT:g}s, "
-                                  f"{'FP64 drop-in' if prec == capi.PRECISION_FP64 else 'precision form'}",
-                      "cells": cells, "tracers": ntr, "subcycles": nts, "parallelism": f"replicas x{world}",
-                      "l2": "inputs larger than L2 (tracer state alone %.1f GB)" % (2 * ntr * cells * 8 / 1e9)},
+           "config": {"workload": f"{args.config.upper()}: {wl.describe(spec)}"
+                                  + ("" if headline else f" ({args.scheme} for every tracer)")
+                                  + (", FP64 drop-in" if prec == capi.PRECISION_FP64 else ", precision form"),
+                      "cells": cells, "tracers": ntr, "subcycles": nts, "dtts": wl.dtts, "dtbt": wl.dtbt,
+                      "parallelism": f"replicas x{world}", "l2": l2note},
            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "autotune": tune,
            "sections_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in sec.items()},
-           "barotropic_roofline": {"achieved": round(bt_achieved, 1), "unit": "GB/s", "peak": peak,
-                                   "frac": round(bt_achieved / peak, 4), "note": "streaming model, 224 B/column/subcycle"},
+           "barotropic_roofline": bt_roof,
            "fp64_roofline": _fp64_roofline(prec, sec, args.steps, cells, ntr, ni, nj, nts) if headline else None,
            "clocks": clk}
-    if rank == 0 and not args.no_cpu_baseline and ntr > 0:
-        # bounded sample of the same workload on one host core: one block of 1/16 of the domain
-        v, info = _cpu_sample(spec)
+    if rank == 0 and not args.no_cpu_baseline:
+        # bounded sample of the same workload on one host core
+        v, info = _cpu_sample(wl, spec)
         out["cpu_baseline"] = {"value": round(v, 1), "unit": "cell-updates/s", "cores": 1, "kind": "port",
                                "sample": info}
     if forms:
-        out["forms"] = run_forms(args, dom, d, value, stream)
+        out["forms"] = run_forms(args, wl, dom, d, value, stream)
     return out
 
 
@@ -444,7 +546,7 @@ FORM_DT = 400.0     # baroclinic step of the ensemble and serving domains (s)
 FORM_DTBT = 20.0    # barotropic step: nts = 2 * 400 / 20 = 40 subcycles
 
 
-def run_forms(args, dom, d64, plain_value, stream):
+def run_forms(args, wl, dom, d64, plain_value, stream):
     """Precision form on the same 1440x1080x50 domain, then the batched ensemble
     (64 domains) and the serving loop (256 resident domains)."""
     import torch
@@ -457,10 +559,10 @@ def run_forms(args, dom, d64, plain_value, stream):
     forms = {}
     # ---- precision form, same workload
     dm = harness.load(dom, options=capi.default_options(barotropic_time_stepping_B=1, precision=capi.PRECISION_MIXED))
-    dm.barotropic_init(dtuv=NTS * DTBT / 2.0, dtbt=DTBT)
+    dm.barotropic_init(dtuv=wl.dtts, dtbt=wl.dtbt)
     dm.set_stream(stream.cuda_stream)
-    tune = dm.autotune(DTTS)
-    r = _time_domain(dm, stream, ntr, args.steps, args.warmup, {"tau": 1})
+    tune = dm.autotune(wl.dtts)
+    r = _time_domain(dm, stream, wl, ntr, args.steps, args.warmup, {"tau": 1})
     v = cells * args.steps / (r["ms"] / 1e3)
     # error against the FP64 drop-in (equal to the oracle bit for bit), one step from the same state
     errs, drift64, driftm = [], 0.0, 0.0
@@ -468,8 +570,8 @@ def run_forms(args, dom, d64, plain_value, stream):
         d64.set(F.TRACER, dom["T"][n - 1].contiguous(), n=n, level=1)
         dm.set(F.TRACER, dom["T"][n - 1].contiguous(), n=n, level=1)
     c0 = [d64.global_tracer_content(n, 1) for n in range(1, ntr + 1)]
-    d64.tracer_advection_step(1, 1, 2, DTTS)
-    dm.tracer_advection_step(1, 1, 2, DTTS)
+    d64.tracer_advection_step(1, 1, 2, wl.dtts)
+    dm.tracer_advection_step(1, 1, 2, wl.dtts)
     for n in range(1, ntr + 1):
         errs.append(_rel_err(_device_copy(dm, F.TRACER, n, 2), _device_copy(d64, F.TRACER, n, 2)))
         drift64 = max(drift64, abs(d64.global_tracer_content(n, 2) - c0[n - 1]) / abs(c0[n - 1]))
@@ -482,7 +584,7 @@ def run_forms(args, dom, d64, plain_value, stream):
         "max_rel_err_vs_fp64_1step": max(errs), "content_rel_change_1step": {"fp64": drift64, "precision": driftm},
         "gpu_launches": r["launches"], "clocks": r["clocks"], "autotune": tune}
     dm.close()
-    forms["schemes"] = scheme_sweep(d64, stream, ntr, cells)
+    forms["schemes"] = scheme_sweep(d64, stream, ntr, cells, wl.dtts)
     d64.close()
     del dom
     torch.cuda.empty_cache()
@@ -497,7 +599,7 @@ SCHEMES = (("upwind", "ADVECT_UPWIND"), ("2nd_order", "ADVECT_2ND_ORDER"), ("4th
            ("mdppm", "ADVECT_MDPPM"), ("psom", "ADVECT_PSOM"), ("mdfl_sweby", "ADVECT_MDFL_SWEBY"))
 
 
-def scheme_sweep(d, stream, ntr, cells, steps=2):
+def scheme_sweep(d, stream, ntr, cells, dtts, steps=2):
     """FP64 tracer advection step (every tracer on one scheme, explicit update
     included, no barotropic) for each scheme on the headline domain."""
     import torch
@@ -512,11 +614,11 @@ def scheme_sweep(d, stream, ntr, cells, steps=2):
             if name == "psom":
                 d.set_psom_limit(n, True)
         launches0 = d.launches
-        d.tracer_advection_step(1, 1, 2, DTTS)  # warm-up (allocates the scheme's fields)
+        d.tracer_advection_step(1, 1, 2, dtts)  # warm-up (allocates the scheme's fields)
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(steps):
-            d.tracer_advection_step(1, 1, 2, DTTS)
+            d.tracer_advection_step(1, 1, 2, dtts)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
@@ -678,10 +780,14 @@ def form_serving(args, stream, batched):
             "vs_plain_fp64": round(sat["cell_updates_per_s"] / plain["value"], 3)}
 
 
-def _cpu_sample(spec):
-    """One host core, one 360x270 block (1/16) of the workload's grid, four steps (about 10 s)."""
-    res = _ref_worker((360, 270, spec.nk, spec.ntracers, -40.0, 27.5, 0.0, 90.0, 77, 0, 4, NTS))
-    return res[1] / res[0], f"C restatement, 1 core, 360x270x{spec.nk} block, {spec.ntracers} tracers, 4 steps"
+def _cpu_sample(wl, spec):
+    """One host core on a bounded sample of the workload: one walled block of
+    1/16 of its grid, one untimed and three timed steps of the restatement's
+    C loop (about 15 s for the global config)."""
+    blk = _block_specs(spec, 16)[0]
+    sec, cells, _ = _ref_worker((blk, wl, 3, 1, 1e9))
+    return cells / sec, (f"C restatement, 1 core, {blk.ni}x{blk.nj}x{blk.nk} block of the grid, "
+                         f"{spec.ntracers} tracers, 3 steps ({wl.describe(blk)})")
 
 
 def main():
@@ -707,20 +813,20 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        spec = config_spec(args.config)
-        procs = os.cpu_count() or 1
-        # bound the run to a few minutes: shrink each block when many steps are asked for
-        est_step = 3.5
-        frac = min(1.0, 150.0 / max(1.0, est_step * (args.steps + args.warmup)))
-        v, info = cpu_reference(spec, args.warmup, args.steps, procs, block_frac=frac)
+        wl = WORKLOADS[args.config]
+        spec = wl.spec()
+        cores = os.cpu_count() or 1
+        v, info = cpu_reference(wl, spec, args.steps, cores)
+        how = (f"whole grid, OpenMP on {cores} threads" if info["same_config"]
+               else f"{cores} processes x walled block {info['block']}")
         out = {"metric": METRIC, "value": round(v, 1), "unit": "cell-updates/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-               "config": {"workload": f"{args.config.upper()} ({spec.ni}x{spec.nj}x{spec.nk}, {spec.ntracers} tracers, "
-                                      f"MDFL Sweby + {NTS}-subcycle barotropic), one block per host process",
-                          "sample": info},
-               "cpu_baseline": {"value": round(v, 1), "unit": "cell-updates/s", "cores": procs, "kind": "port",
-                                "sample": f"{procs} processes x block {info['block']}, {args.steps} steps"},
+               "config": {"workload": f"{args.config.upper()}: {wl.describe(spec)}, reference algorithm on the "
+                                      f"host cores ({how})", "sample": info},
+               "cpu_baseline": {"value": round(v, 1), "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                                "sample": f"C restatement stepping loop, {how}, {info['steps_timed']} timed steps "
+                                          f"after one untimed step"},
                "e2e": {"value": round(v, 1), "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}
         print(json.dumps(out))

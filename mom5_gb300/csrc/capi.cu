@@ -141,7 +141,17 @@ double* fptr(mom5gpu_domain* d, int id, int n, int level) {
       fail(d, MOM5GPU_ENOMEM, "allocating field %d (%zu bytes)", id, sizeof(double) * cnt * per);
       return nullptr;
     }
-    cudaMemsetAsync(p, 0, sizeof(double) * cnt * per, d->stream);
+    // The first use of a field may be a copy queued on another stream
+    // (mom5gpu_copy_field_async): the zeroing must be complete before this
+    // returns, not merely queued behind the domain stream's pending work.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(d->stream, &cs);
+    if (cs == cudaStreamCaptureStatusNone) {
+      cudaMemset(p, 0, sizeof(double) * cnt * per);
+      cudaDeviceSynchronize();
+    } else {
+      cudaMemsetAsync(p, 0, sizeof(double) * cnt * per, d->stream);
+    }
     d->bytes += sizeof(double) * cnt * per;
     d->field[slot] = p;
   }

@@ -100,6 +100,15 @@ def config_c2_block(seed: int = 3, ntracers: int = 10) -> DomainSpec:
                       cyclic_x=False, continent=(150, 100, 40, 30), hmin=2000.0, ntracers=ntracers, seed=seed)
 
 
+def config_c2_polar_block(seed: int = 4, ntracers: int = 10) -> DomainSpec:
+    """A 360x270x50 block of the 0.25 degree grid reaching the global grid's
+    poleward edge (lon 0-90, lat 12.5..80), periodic in x, 10 tracers: the
+    metrics where the global config is most extreme (dxt = 4.8 km at 80 deg,
+    the barotropic CFL limit about 24 s) at an oracle-checkable size."""
+    return DomainSpec(ni=360, nj=270, nk=50, lon0=0.0, lon1=90.0, lat0=12.5, lat1=80.0,
+                      cyclic_x=True, continent=(150, 100, 40, 30), hmin=2000.0, ntracers=ntracers, seed=seed)
+
+
 def stretched_dz(nk: int, top: float, bot: float, total: float) -> torch.Tensor:
     """Level thicknesses growing from ``top`` to ``bot`` as a power law whose
     exponent is solved so that the levels sum to ``total``."""

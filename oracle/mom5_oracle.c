@@ -28,14 +28,22 @@
  * Build with -O2 -ffp-contract=off so that no multiply-add is fused: the
  * reference's gfortran build evaluates every product and sum separately.
  */
+#define _POSIX_C_SOURCE 199309L
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 typedef struct {
   int ni, nj, nk;
   int cyclic_x, cyclic_y;
 } orc_dims;
+
+typedef struct orc_mdfl_ws orc_mdfl_ws;
+void orc_advect_mdfl_sweby_ws(orc_mdfl_ws* ws, double sweby_limiter, double dtime, const double* dat,
+                              const double* datr, const double* dxte, const double* dyte, const double* dxtn,
+                              const double* dytn, const double* uhrho_et, const double* vhrho_nt,
+                              const double* wrho_bt, const double* rho_dzt, const double* T, double* wrk1);
 
 #define NXD(d) ((d)->ni + 2)
 #define NYD(d) ((d)->nj + 2)
@@ -44,6 +52,38 @@ typedef struct {
 
 static inline double fmaxd(double a, double b) { return a > b ? a : b; }
 static inline double fmind(double a, double b) { return a < b ? a : b; }
+
+/* Built with -fopenmp (the CPU baseline's build only), the loops marked
+ * OMP_FOR run their iterations on all host cores; every marked loop has
+ * independent iterations, so the results are those of the serial build. */
+#ifdef _OPENMP
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define OMP_FOR
+#endif
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Threads of the OpenMP build's parallel loops (no effect in the serial build). */
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+static void zero_par(double* a, size_t n) {
+  const size_t chunk = 1 << 16;
+  long nc = (long)((n + chunk - 1) / chunk);
+  OMP_FOR
+  for (long c = 0; c < nc; ++c) {
+    size_t lo = (size_t)c * chunk, hi = lo + chunk < n ? lo + chunk : n;
+    memset(a + lo, 0, sizeof(double) * (hi - lo));
+  }
+}
 
 /* ocean_parameters.F90:92 onesixth = 1.0/6.0; :194-195 rho0, rho0r */
 static const double onesixth = 1.0 / 6.0;
@@ -1345,34 +1385,90 @@ void orc_vert_advect_quicker(const orc_dims* d, const orc_quicker* q, const doub
 /* wrk1 receives -advect_tracer_mdfl_sweby (horz_advect_tracer :1953-1959).  */
 /* sweby_limiter = 1 for ADVECT_MDFL_SWEBY, 0 for ADVECT_DST_LINEAR.         */
 /* ------------------------------------------------------------------------- */
+/* The module scratch of the MDFL scheme, allocated once as mdfl_init does
+ * (ocean_tracer_advect.F90:1644-1669; flux_x/flux_y :548-553): tmask_mdfl is
+ * built once, the rest is zeroed at the top of every call (:3833-3838). */
+struct orc_mdfl_ws {
+  orc_dims d;
+  double *tm, *mk, *ftp, *fbt, *wkm1, *fx, *fy;
+};
+
+orc_mdfl_ws* orc_mdfl_ws_create(const orc_dims* d, const double* tmask) {
+  orc_mdfl_ws* ws = (orc_mdfl_ws*)calloc(1, sizeof(orc_mdfl_ws));
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  size_t nh = (size_t)NX2(d) * NY2(d) * d->nk;
+  ws->d = *d;
+  ws->tm = (double*)calloc(nh, sizeof(double)); /* tracer_mdfl */
+  ws->mk = (double*)calloc(nh, sizeof(double)); /* tmask_mdfl  */
+  ws->ftp = (double*)calloc(n2, sizeof(double));
+  ws->fbt = (double*)calloc(n2, sizeof(double));
+  ws->wkm1 = (double*)calloc(n2, sizeof(double));
+  ws->fx = (double*)calloc(n2 * d->nk, sizeof(double)); /* flux_x */
+  ws->fy = (double*)calloc(n2 * d->nk, sizeof(double)); /* flux_y */
+  orc_mask_halo2(d, tmask, ws->mk);
+  return ws;
+}
+
+void orc_mdfl_ws_destroy(orc_mdfl_ws* ws) {
+  if (!ws) return;
+  free(ws->tm);
+  free(ws->mk);
+  free(ws->ftp);
+  free(ws->fbt);
+  free(ws->wkm1);
+  free(ws->fx);
+  free(ws->fy);
+  free(ws);
+}
+
 void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime, const double* tmask,
                            const double* dat, const double* datr, const double* dxte, const double* dyte,
                            const double* dxtn, const double* dytn, const double* uhrho_et,
                            const double* vhrho_nt, const double* wrho_bt, const double* rho_dzt,
                            const double* T, double* wrk1) {
+  orc_mdfl_ws* ws = orc_mdfl_ws_create(d, tmask);
+  orc_advect_mdfl_sweby_ws(ws, sweby_limiter, dtime, dat, datr, dxte, dyte, dxtn, dytn, uhrho_et, vhrho_nt,
+                           wrho_bt, rho_dzt, T, wrk1);
+  orc_mdfl_ws_destroy(ws);
+}
+
+void orc_advect_mdfl_sweby_ws(orc_mdfl_ws* ws, double sweby_limiter, double dtime, const double* dat,
+                              const double* datr, const double* dxte, const double* dyte, const double* dxtn,
+                              const double* dytn, const double* uhrho_et, const double* vhrho_nt,
+                              const double* wrho_bt, const double* rho_dzt, const double* T, double* wrk1) {
+  const orc_dims* d = &ws->d;
   int ni = d->ni, nj = d->nj, nk = d->nk;
   size_t n2 = (size_t)NXD(d) * NYD(d);
   size_t nh = (size_t)NX2(d) * NY2(d) * nk;
-  double* tm = (double*)calloc(nh, sizeof(double)); /* tracer_mdfl */
-  double* mk = (double*)calloc(nh, sizeof(double)); /* tmask_mdfl  */
-  double* ftp = (double*)calloc(n2, sizeof(double));
-  double* fbt = (double*)calloc(n2, sizeof(double));
-  double* wkm1 = (double*)calloc(n2, sizeof(double));
-  double* fx = (double*)calloc(n2 * nk, sizeof(double));
-  double* fy = (double*)calloc(n2 * nk, sizeof(double));
-  orc_mask_halo2(d, tmask, mk);
-  memset(wrk1, 0, sizeof(double) * n2 * nk);
+  double* tm = ws->tm;
+  const double* mk = ws->mk;
+  double* ftp = ws->ftp;
+  double* fbt = ws->fbt;
+  double* wkm1 = ws->wkm1;
+  double* fx = ws->fx;
+  double* fy = ws->fy;
+  /* :3833-3838 */
+  zero_par(ftp, n2);
+  zero_par(fbt, n2);
+  zero_par(wkm1, n2);
+  zero_par(tm, nh);
+  zero_par(fx, n2 * nk);
+  zero_par(fy, n2 * nk);
+  /* horz_advect_tracer :1925-1931 */
+  zero_par(wrk1, n2 * nk);
 #define TM(i, j, k) tm[H3(d, (i), (j), (k))]
 #define MK(i, j, k) mk[H3(d, (i), (j), (k))]
 #define TF(i, j, k) T[I3(d, (i), (j), (k))]
 #define RDZ(i, j, k) rho_dzt[I3(d, (i), (j), (k))]
 #define WB(i, j, k) wrho_bt[I3(d, (i), (j), (k) + 1)]
   for (int k = 0; k < nk; ++k) {
+    OMP_FOR
     for (int j = 1; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i) TM(i, j, k) = TF(i, j, k);
     int kp1 = k + 1 < nk ? k + 1 : nk - 1;
     int kp2 = k + 2 < nk ? k + 2 : nk - 1;
     int km1 = k - 1 > 0 ? k - 1 : 0;
+    OMP_FOR
     for (int j = 1; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i) {
         double Rjp = (TF(i, j, km1) - TF(i, j, k)) * MK(i, j, km1) * MK(i, j, k);
@@ -1398,11 +1494,13 @@ void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime
                                          TF(i, j, k) * (wkm1[I2(d, i, j)] - WB(i, j, k)));
         ftp[I2(d, i, j)] = fbt[I2(d, i, j)];
       }
+    OMP_FOR
     for (int j = 1; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i) wkm1[I2(d, i, j)] = WB(i, j, k);
   }
   halo2_update(d, tm, 1); /* XUPDATE :3912 */
 
+  OMP_FOR
   for (int k = 0; k < nk; ++k) {
     for (int j = 1; j <= nj; ++j)
       for (int i = 0; i <= ni; ++i) {
@@ -1438,6 +1536,7 @@ void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime
 
   memset(wkm1, 0, sizeof(double) * n2);
   for (int k = 0; k < nk; ++k) {
+    OMP_FOR
     for (int j = 0; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i) {
         double Rjp = (TM(i, j + 2, k) - TM(i, j + 1, k)) * MK(i, j + 2, k) * MK(i, j + 1, k);
@@ -1460,10 +1559,12 @@ void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime
                                     (massflux - fabs(massflux)) * (TM(i, j + 1, k) - psiM * Rj)) *
                              MK(i, j, k) * MK(i, j + 1, k);
       }
+    OMP_FOR
     for (int j = 1; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i)
         TM(i, j, k) = TM(i, j, k) + dtime * MK(i, j, k) * datr[I2(d, i, j)] / RDZ(i, j, k) *
                                         (fy[I3(d, i, j - 1, k)] - fy[I3(d, i, j, k)]);
+    OMP_FOR
     for (int j = 1; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i) {
         TM(i, j, k) = TM(i, j, k) + dtime * TF(i, j, k) / RDZ(i, j, k) *
@@ -1473,6 +1574,7 @@ void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime
         double adv = -RDZ(i, j, k) * (TM(i, j, k) - TF(i, j, k)) / dtime * MK(i, j, k);
         wrk1[I3(d, i, j, k)] = -adv;
       }
+    OMP_FOR
     for (int j = 1; j <= nj; ++j)
       for (int i = 1; i <= ni; ++i) wkm1[I2(d, i, j)] = WB(i, j, k);
   }
@@ -1481,13 +1583,6 @@ void orc_advect_mdfl_sweby(const orc_dims* d, double sweby_limiter, double dtime
 #undef TF
 #undef RDZ
 #undef WB
-  free(tm);
-  free(mk);
-  free(ftp);
-  free(fbt);
-  free(wkm1);
-  free(fx);
-  free(fy);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1657,6 +1752,7 @@ void orc_advect_sweby_all(const orc_dims* d, int ntr, double dtime, const double
 /* ------------------------------------------------------------------------- */
 void orc_update_tracer(const orc_dims* d, double dtime, const double* rho_dzt_taum1, const double* rho_dztr,
                        const double* T_taum1, const double* th_tendency, double* T_taup1) {
+  OMP_FOR
   for (int k = 0; k < d->nk; ++k)
     for (int j = 1; j <= d->nj; ++j)
       for (int i = 1; i <= d->ni; ++i) {
@@ -1711,7 +1807,8 @@ void orc_div_ud_bgrid(const orc_dims* d, const double* udu, const double* udv, c
                       const double* dxu, const double* datr, double* out) {
   int ni = d->ni, nj = d->nj;
   size_t n2 = (size_t)NXD(d) * NYD(d);
-  memset(out, 0, sizeof(double) * n2);
+  zero_par(out, n2);
+  OMP_FOR
   for (int j = 1; j <= nj + 1; ++j) {
     int i = 1;
     double uhim = udu[I2(d, i - 1, j)] * dyu[I2(d, i - 1, j)];
@@ -1742,7 +1839,8 @@ void orc_div_ud_cgrid(const orc_dims* d, const double* udu, const double* udv, c
                       const double* dxter, const double* dytnr, const double* datr, double* out) {
   int ni = d->ni, nj = d->nj;
   size_t n2 = (size_t)NXD(d) * NYD(d);
-  memset(out, 0, sizeof(double) * n2);
+  zero_par(out, n2);
+  OMP_FOR
   for (int j = 1; j <= nj + 1; ++j)
     for (int i = 1; i <= ni + 1; ++i) {
       double uhim = udu[I2(d, i - 1, j)] * dat[I2(d, i - 1, j)] * dxter[I2(d, i - 1, j)];
@@ -1758,8 +1856,9 @@ void orc_grad_baro_p(const orc_dims* d, int cgrid, const double* press, const do
                      const double* mx, const double* my, double* gx, double* gy) {
   int ni = d->ni, nj = d->nj;
   size_t n2 = (size_t)NXD(d) * NYD(d);
-  memset(gx, 0, sizeof(double) * n2);
-  memset(gy, 0, sizeof(double) * n2);
+  zero_par(gx, n2);
+  zero_par(gy, n2);
+  OMP_FOR
   for (int j = 0; j <= nj; ++j)
     for (int i = 0; i <= ni; ++i) {
       if (!cgrid) {
@@ -1820,6 +1919,9 @@ typedef struct {
   double *eta_t_bar, *udrho_u, *udrho_v, *conv_rho_ud_t, *eta_u, *ps, *grad_ps_x, *grad_ps_y;
 } orc_baro_io;
 
+typedef struct orc_baro_ws orc_baro_ws;
+void orc_update_ocean_barotropic_ws(orc_baro_ws* ws, const orc_baro_params* p, const orc_baro_io* io);
+
 static void div_ud_any(const orc_dims* d, const orc_baro_params* p, const orc_baro_io* io, const double* u,
                        const double* v, double* out) {
   if (p->cgrid)
@@ -1828,7 +1930,34 @@ static void div_ud_any(const orc_dims* d, const orc_baro_params* p, const orc_ba
     orc_div_ud_bgrid(d, u, v, io->dyu, io->dxu, io->datr, out);
 }
 
+/* The barotropic module arrays, allocated once as ocean_barotropic_init does
+ * (ocean_barotropic.F90:1249-1256); every call starts them from zero. */
+struct orc_baro_ws {
+  orc_dims d;
+  double* buf;
+};
+
+orc_baro_ws* orc_baro_ws_create(const orc_dims* d) {
+  orc_baro_ws* ws = (orc_baro_ws*)calloc(1, sizeof(orc_baro_ws));
+  ws->d = *d;
+  ws->buf = (double*)calloc((size_t)NXD(d) * NYD(d) * 21, sizeof(double));
+  return ws;
+}
+
+void orc_baro_ws_destroy(orc_baro_ws* ws) {
+  if (!ws) return;
+  free(ws->buf);
+  free(ws);
+}
+
 void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, const orc_baro_io* io) {
+  orc_baro_ws* ws = orc_baro_ws_create(d);
+  orc_update_ocean_barotropic_ws(ws, p, io);
+  orc_baro_ws_destroy(ws);
+}
+
+void orc_update_ocean_barotropic_ws(orc_baro_ws* ws, const orc_baro_params* p, const orc_baro_io* io) {
+  const orc_dims* d = &ws->d;
   int ni = d->ni, nj = d->nj, nts = p->nts;
   size_t n2 = (size_t)NXD(d) * NYD(d);
   double rho0r = 1.0 / p->rho0;
@@ -1839,18 +1968,19 @@ void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, co
   /* AB3 weights :617-619, onefourth */
   const double abtau_m0 = 23.0 / 12.0, abtau_m1 = -16.0 / 12.0, abtau_m2 = 5.0 / 12.0, onefourth = 0.25;
 
-  double* eta_bt = (double*)calloc(n2 * 2, sizeof(double));
-  double* ubt = (double*)calloc(n2 * 2, sizeof(double));
-  double* vbt = (double*)calloc(n2 * 2, sizeof(double));
-  double* steady = (double*)calloc(n2, sizeof(double));
-  double* tmp = (double*)calloc(n2, sizeof(double));
-  double* ps = (double*)calloc(n2, sizeof(double));
-  double* gx = (double*)calloc(n2, sizeof(double));
-  double* gy = (double*)calloc(n2, sizeof(double));
-  double* cori1 = (double*)calloc(n2, sizeof(double));
-  double* cori2 = (double*)calloc(n2, sizeof(double));
-  double* cf = (double*)calloc(n2 * 2 * 3, sizeof(double)); /* coriolis_force_bt(·,·,2,3) */
-  double* ca = (double*)calloc(n2 * 2, sizeof(double));     /* coriolis_accel_bt(·,·,2) */
+  memset(ws->buf, 0, sizeof(double) * n2 * 21);
+  double* eta_bt = ws->buf;
+  double* ubt = eta_bt + n2 * 2;
+  double* vbt = ubt + n2 * 2;
+  double* steady = vbt + n2 * 2;
+  double* tmp = steady + n2;
+  double* ps = tmp + n2;
+  double* gx = ps + n2;
+  double* gy = gx + n2;
+  double* cori1 = gy + n2;
+  double* cori2 = cori1 + n2;
+  double* cf = cori2 + n2; /* coriolis_force_bt(·,·,2,3) */
+  double* ca = cf + n2 * 6; /* coriolis_accel_bt(·,·,2) */
 #define CF(i, j, c, l) cf[((size_t)(l) * 2 + (c)) * n2 + I2(d, (i), (j))]
 #define CA(i, j, c) ca[(size_t)(c) * n2 + I2(d, (i), (j))]
   /* :1283-1288 */
@@ -1904,15 +2034,20 @@ void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, co
     /* predictor */
     if (p->pred_corr_gamma > 0.0) {
       div_ud_any(d, p, io, uo, vo, tmp);
+      OMP_FOR
       for (size_t q = 0; q < n2; ++q) tmp[q] = -tmp[q] * io->tmask1[q];
+      OMP_FOR
       for (size_t q = 0; q < n2; ++q) en[q] = eo[q] + dtbt_gamma_rho0r * (tmp[q] + steady[q]);
     } else {
+      OMP_FOR
       for (size_t q = 0; q < n2; ++q) en[q] = eo[q];
     }
     if (!p->cgrid) orc_halo_update_2d(d, en, 3); /* use_legacy_barotropic_halos (B-grid only) */
+    OMP_FOR
     for (size_t q = 0; q < n2; ++q) ps[q] = io->rho_g[q] * en[q] + io->patm[q];
     if (!p->cgrid) {
       orc_grad_baro_p(d, 0, ps, io->dxur, io->dyur, io->umask1, io->umask1, gx, gy);
+      OMP_FOR
       for (int j = 0; j <= nj + 1; ++j)
         for (int i = 0; i <= ni + 1; ++i) {
           size_t q = I2(d, i, j);
@@ -1926,6 +2061,7 @@ void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, co
     } else {
       int m2 = (itime + 0) % 3, m1 = (itime + 1) % 3, m0 = (itime + 2) % 3;
       memset(ca, 0, sizeof(double) * n2 * 2);
+      OMP_FOR
       for (int j = 1; j <= nj; ++j)
         for (int i = 1; i <= ni; ++i) {
           CF(i, j, 0, m0) = onefourth * (io->f[I2(d, i, j)] * (vo[I2(d, i, j)] + vo[I2(d, i + 1, j)]) +
@@ -1936,6 +2072,7 @@ void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, co
           CA(i, j, 1) = abtau_m0 * CF(i, j, 1, m0) + abtau_m1 * CF(i, j, 1, m1) + abtau_m2 * CF(i, j, 1, m2);
         }
       orc_grad_baro_p(d, 1, ps, io->dxter, io->dytnr, io->tmasken_e, io->tmasken_n, gx, gy);
+      OMP_FOR
       for (int j = 0; j <= nj + 1; ++j)
         for (int i = 0; i <= ni + 1; ++i) {
           size_t q = I2(d, i, j);
@@ -1949,10 +2086,13 @@ void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, co
     }
     /* corrector */
     div_ud_any(d, p, io, un, vn, tmp);
+    OMP_FOR
     for (size_t q = 0; q < n2; ++q) tmp[q] = -tmp[q] * io->tmask1[q];
+    OMP_FOR
     for (size_t q = 0; q < n2; ++q) en[q] = eo[q] + dtbt_rho0r * (tmp[q] + steady[q]);
     /* accumulate */
     double wgt = p->time_stepping_B ? (double)(nts - itime + 1) : 1.0;
+    OMP_FOR
     for (size_t q = 0; q < n2; ++q) {
       io->eta_t_bar[q] = io->eta_t_bar[q] + en[q];
       if (p->time_stepping_B) {
@@ -1988,18 +2128,6 @@ void orc_update_ocean_barotropic(const orc_dims* d, const orc_baro_params* p, co
   else
     orc_grad_baro_p(d, 1, io->ps, io->dxter, io->dytnr, io->tmasken_e, io->tmasken_n, io->grad_ps_x,
                     io->grad_ps_y);
-  free(eta_bt);
-  free(ubt);
-  free(vbt);
-  free(steady);
-  free(tmp);
-  free(ps);
-  free(gx);
-  free(gy);
-  free(cori1);
-  free(cori2);
-  free(cf);
-  free(ca);
 }
 
 /* eta_and_pbot_tendency, depth-based: ocean_barotropic.F90:2683-2690. */
@@ -2334,4 +2462,70 @@ void orc_update_ucell_thickness(const orc_dims* d, int vcoord, int linear_free_s
       size_t p = (size_t)k * n2 + q;
       mass_en_n[q] = mass_en_n[q] + tmasken_n[p] * rho_dzten_n[p];
     }
+}
+
+/* ------------------------------------------------------------------------- */
+/* The CPU baseline's timed loop: warmup + steps two-level baroclinic steps  */
+/* of one block with no host language in between.  Each step advects every  */
+/* tracer by MDFL Sweby into a zeroed th_tendency (update_advection_only,    */
+/* ocean_tracer.F90:2618-2649; horz_advect_tracer :1925-1936), updates it    */
+/* explicitly (:2341-2350) and halo-updates T(taup1) (ocean_model.F90:       */
+/* 1903-1911), then runs update_ocean_barotropic when p is not NULL.  The    */
+/* scratch lives across steps as the reference's module arrays do (mdfl_init */
+/* ocean_tracer_advect.F90:1644-1669, ocean_barotropic_init :1249-1256).  T  */
+/* holds ntr data-domain blocks and ends at the last step's values; the      */
+/* barotropic *_tau inputs and out_* outputs of io swap roles every step (a  */
+/* local copy of io; the caller's arrays hold the last two steps).  Returns  */
+/* the seconds of the timed steps (CLOCK_MONOTONIC).                         */
+/* ------------------------------------------------------------------------- */
+double orc_run_steps(const orc_dims* d, int ntr, int warmup, int steps, double dtts, const double* tmask,
+                     const double* dat, const double* datr, const double* dxte, const double* dyte,
+                     const double* dxtn, const double* dytn, const double* uhrho_et, const double* vhrho_nt,
+                     const double* wrho_bt, const double* rho_dzt, const double* rho_dztr, double* T,
+                     const orc_baro_params* p, const orc_baro_io* io_in) {
+  size_t n3 = (size_t)NXD(d) * NYD(d) * d->nk;
+  orc_mdfl_ws* ws = ntr > 0 ? orc_mdfl_ws_create(d, tmask) : NULL;
+  orc_baro_ws* bws = p ? orc_baro_ws_create(d) : NULL;
+  orc_baro_io io;
+  if (io_in) io = *io_in;
+  double* th = (double*)malloc(sizeof(double) * (n3 > 0 ? n3 : 1));
+  double* wrk1 = (double*)malloc(sizeof(double) * (n3 > 0 ? n3 : 1));
+  double* other = (double*)malloc(sizeof(double) * (n3 * (size_t)ntr + 1));
+  if (ntr > 0) memcpy(other, T, sizeof(double) * n3 * (size_t)ntr);
+  double* cur = T;
+  double* nxt = other;
+  struct timespec t0 = {0, 0}, t1;
+  for (int s = 0; s < warmup + steps; ++s) {
+    if (s == warmup) clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int n = 0; n < ntr; ++n) {
+      zero_par(th, n3);
+      orc_advect_mdfl_sweby_ws(ws, 1.0, dtts, dat, datr, dxte, dyte, dxtn, dytn, uhrho_et, vhrho_nt, wrho_bt,
+                               rho_dzt, cur + n * n3, wrk1);
+      OMP_FOR
+      for (int k = 0; k < d->nk; ++k)
+        for (int j = 1; j <= d->nj; ++j)
+          for (int i = 1; i <= d->ni; ++i) th[I3(d, i, j, k)] = th[I3(d, i, j, k)] + wrk1[I3(d, i, j, k)];
+      orc_update_tracer(d, dtts, rho_dzt, rho_dztr, cur + n * n3, th, nxt + n * n3);
+      orc_halo_update_3d(d, nxt + n * n3, d->nk, 3);
+    }
+    double* sw = cur;
+    cur = nxt;
+    nxt = sw;
+    if (p) {
+      orc_update_ocean_barotropic_ws(bws, p, &io);
+      /* the outputs become the next step's inputs; the old inputs take the next outputs */
+      double* a;
+      a = (double*)io.eta_t_bar_tau; io.eta_t_bar_tau = io.eta_t_bar; io.eta_t_bar = a;
+      a = (double*)io.udrho_u_tau; io.udrho_u_tau = io.udrho_u; io.udrho_u = a;
+      a = (double*)io.udrho_v_tau; io.udrho_v_tau = io.udrho_v; io.udrho_v = a;
+    }
+  }
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  if (ntr > 0 && cur != T) memcpy(T, cur, sizeof(double) * n3 * (size_t)ntr);
+  free(th);
+  free(wrk1);
+  free(other);
+  orc_mdfl_ws_destroy(ws);
+  orc_baro_ws_destroy(bws);
+  return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }

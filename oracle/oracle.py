@@ -50,9 +50,20 @@ class BaroIO(C.Structure):
     _fields_ = [(n, DP) for n in BARO_IO_FIELDS]
 
 
+_OMP_PATH = os.path.join(_HERE, "_build", "libmom5oracle_omp.so")
+_lib_omp = None
+
+
 def build() -> str:
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
+
+
+def build_omp() -> str:
+    """The OpenMP build of the same source (the CPU baseline's); raises if the
+    compiler has no OpenMP."""
+    subprocess.run(["make", "-s", "-C", _HERE, "omp"], check=True)
+    return _OMP_PATH
 
 
 def lib():
@@ -63,6 +74,15 @@ def lib():
         _lib = C.CDLL(_LIB_PATH)
         _lib.orc_area_integral.restype = C.c_double
     return _lib
+
+
+def lib_omp():
+    global _lib_omp
+    if _lib_omp is None:
+        if not os.path.exists(_OMP_PATH):
+            build_omp()
+        _lib_omp = C.CDLL(_OMP_PATH)
+    return _lib_omp
 
 
 def p(a: np.ndarray):
@@ -335,6 +355,54 @@ def update_ocean_barotropic(d, g, state, nts, dtbt, gamma=0.2, rho0=1035.0, time
                      int(cgrid))
     lib().orc_update_ocean_barotropic(C.byref(d), C.byref(prm), C.byref(io))
     return out
+
+
+def run_steps(d, g, T, dtts, warmup=0, steps=1, nts=0, dtbt=0.0, state=None, gamma=0.2, rho0=1035.0,
+              threaded=False, threads=None):
+    """The CPU baseline's loop (orc_run_steps): warmup + steps baroclinic steps of
+    one block in C with the scheme scratch held across steps -- every tracer of
+    ``T`` (ntr, nk, nj+2, ni+2) by MDFL Sweby with the explicit update, then,
+    with nts > 0, update_ocean_barotropic from ``state`` (eta_t, eta_t_bar,
+    udrho_u, udrho_v at tau).  ``T`` is updated in place.  threaded=True runs
+    the OpenMP build on ``threads`` threads (default: every host core).  Returns (seconds of the timed
+    steps, the last barotropic outputs or None)."""
+    T = np.ascontiguousarray(T)
+    assert T.dtype == np.float64 and T.ndim == 4
+    ntr = int(T.shape[0])
+    io = out = prm = None
+    keep = []
+    if nts > 0:
+        shp = g["tmask1"].shape
+        out = {k: np.zeros(shp) for k in ("eta_t_bar", "udrho_u", "udrho_v", "conv_rho_ud_t", "eta_u", "ps",
+                                          "grad_ps_x", "grad_ps_y")}
+        src = dict(g)
+        src["eta_t_tau"] = state["eta_t"]
+        for k in ("eta_t_bar", "udrho_u", "udrho_v"):
+            src[k + "_tau"] = np.ascontiguousarray(state[k]).copy()
+        keep = [src, out]
+        io = BaroIO(*[p(out[n[4:]]) if n.startswith("out_") else p(src[n]) for n in BARO_IO_FIELDS])
+        prm = BaroParams(int(nts), float(dtbt), float(gamma), float(rho0), 1, 1, 0)
+    z = np.zeros(1)
+    arr = lambda k: p(g[k]) if ntr > 0 else p(z)
+    L = lib_omp() if threaded else lib()
+    if threaded:
+        L.orc_set_threads(int(os.cpu_count() if threads is None else threads))
+    f = L.orc_run_steps
+    f.restype = C.c_double
+    sec = f(C.byref(d), ntr, int(warmup), int(steps), C.c_double(dtts), arr("tmask"), arr("dat"), arr("datr"),
+            arr("dxte"), arr("dyte"), arr("dxtn"), arr("dytn"), arr("uhrho_et"), arr("vhrho_nt"), arr("wrho_bt"),
+            arr("rho_dzt"), arr("rho_dztr"), p(T) if ntr > 0 else p(z),
+            C.byref(prm) if prm is not None else None, C.byref(io) if io is not None else None)
+    if nts > 0:
+        # the last step's outputs sit in whichever buffer that step wrote
+        last = (warmup + steps) % 2
+        src = keep[0]
+        res = dict(out)
+        if last == 0:
+            for k in ("eta_t_bar", "udrho_u", "udrho_v"):
+                res[k] = src[k + "_tau"]
+        return sec, res
+    return sec, None
 
 
 def domain_arrays(dom) -> Dict[str, np.ndarray]:

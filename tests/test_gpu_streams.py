@@ -1,0 +1,34 @@
+"""Stream ordering at the C ABI: a field whose first use is a copy queued on a
+caller's stream (mom5gpu_copy_field_async) while the domain's own stream is
+busy keeps the copied values -- the zeroing of a newly allocated field is
+complete before the entry point returns, not queued behind the domain's work."""
+import numpy as np
+import pytest
+
+from mom5_gb300 import grid
+
+pytestmark = pytest.mark.gpu
+
+
+def test_first_touch_copy_on_another_stream(gpu_lib):
+    capi = gpu_lib
+    import torch
+    from mom5_gb300 import harness
+    sp = grid.DomainSpec(ni=180, nj=120, nk=30, lon0=0.0, lon1=90.0, lat0=-30.0, lat1=30.0, cyclic_x=True,
+                         continent=(60, 40, 10, 8), ntracers=3, seed=12)
+    d = harness.load(grid.make_domain(sp), options=capi.default_options(barotropic_time_stepping_B=1))
+    own = torch.cuda.Stream()
+    other = torch.cuda.Stream()
+    d.set_stream(own.cuda_stream)
+    n3 = d.count(capi.F.TRACER)
+    src = torch.empty(n3, dtype=torch.float64, pin_memory=True)
+    src.copy_(torch.linspace(1.0, 2.0, n3, dtype=torch.float64))
+    torch.cuda.synchronize()
+    for _ in range(4):  # keep the domain's stream busy
+        d.tracer_advection_step(1, 1, 2, 3600.0)
+    # time level 3 of tracer 2 has never been used: this copy allocates it
+    d.copy_field_async(capi.F.TRACER, src.data_ptr(), 1, other.cuda_stream, n=2, level=3)
+    torch.cuda.synchronize()
+    got = d.get(capi.F.TRACER, n=2, level=3)
+    assert np.array_equal(got, src.numpy())
+    d.close()
