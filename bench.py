@@ -69,6 +69,7 @@ class Workload:
 WORKLOADS = {
     "c2": Workload("c2", "config_c2", 600.0, 20.0),
     "c2s": Workload("c2s", "config_c2_block", 600.0, 20.0),
+    "c2w": Workload("c2w", "config_c2_band", 600.0, 20.0),
     "c0": Workload("c0", "config_c0", 3600.0),
     "c1": Workload("c1", "config_c1", 2700.0, 67.5),
 }
@@ -198,6 +199,26 @@ def _ref_worker(args):
     return sec, spec.ni * spec.nj * spec.nk * n, n
 
 
+def _block_proc(idx, spec, wl, steps, budget_s, barrier, t1s, q):
+    """One block of the per-process split: an untimed step, then the same
+    number of timed steps in every process, all started together."""
+    import torch
+    torch.set_num_threads(1)
+    O, g, T, st = _oracle_inputs(spec)
+    d = O.dims(spec)
+    kw = dict(nts=wl.nts, dtbt=wl.dtbt or 0.0)
+    t1, res = O.run_steps(d, g, T, wl.dtts, warmup=0, steps=1, state=st, **kw)
+    if res is not None:
+        st = {"eta_t": st["eta_t"], "eta_t_bar": res["eta_t_bar"], "udrho_u": res["udrho_u"],
+              "udrho_v": res["udrho_v"]}
+    t1s[idx] = t1
+    barrier.wait()
+    n = max(1, min(steps, int(budget_s / max(max(t1s[:]), 1e-6))))
+    barrier.wait()
+    sec, _ = O.run_steps(d, g, T, wl.dtts, warmup=0, steps=n, state=st, **kw)
+    q.put((sec, spec.ni * spec.nj * spec.nk * n, n))
+
+
 def _block_specs(spec, procs):
     """One walled block per process (an MPI-rank-like split of the grid)."""
     import dataclasses
@@ -219,32 +240,42 @@ def _block_specs(spec, procs):
     return out
 
 
-def cpu_reference(wl, spec, steps, cores, budget_s=150.0):
-    """The reference algorithm on `cores` host cores: the whole grid in one
-    process with OpenMP (the C loop's scratch held across steps); when the
-    compiler has no OpenMP, one walled block per process.  Timed steps are
-    capped so that the run stays within about budget_s seconds."""
+def cpu_reference(wl, spec, steps, cores, budget_s=75.0):
+    """The reference algorithm on `cores` host cores, two ways, the faster one
+    reported: (1) the whole grid in one process with OpenMP over rows and
+    levels (the same configuration as the GPU's); (2) one walled block per
+    process, as MPI ranks hold the grid, each stepped on its own (no halo
+    exchange charged, so an upper bound for the decomposed reference).  The
+    C loop holds its scratch across steps; timed steps are capped so that each
+    way stays within about budget_s seconds."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
+    runs = {}
     try:
         from oracle import oracle as O
         O.build_omp()
-        omp = True
-    except Exception:
-        omp = False
-    if omp:
         with ctx.Pool(1) as pool:
             sec, cells, n = pool.apply(_ref_worker, ((spec, wl, steps, cores, budget_s),))
-        return cells / sec, {"grid": [spec.ni, spec.nj, spec.nk], "threads": cores, "steps_timed": n,
-                             "seconds": round(sec, 3), "parallelism": "OpenMP over rows and levels",
-                             "same_config": True}
+        runs["openmp"] = {"value": cells / sec, "grid": [spec.ni, spec.nj, spec.nk], "threads": cores,
+                          "steps_timed": n, "seconds": round(sec, 3), "same_config": True}
+    except Exception as e:  # a compiler without OpenMP
+        runs["openmp"] = {"unavailable": str(e)[:200]}
     blocks = _block_specs(spec, cores)
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_ref_worker, [(b, wl, steps, 1, budget_s) for b in blocks])
-    rate = sum(c / s for s, c, _ in res)
-    return rate, {"block": [blocks[0].ni, blocks[0].nj, spec.nk], "procs": cores,
-                  "steps_timed": min(r[2] for r in res), "seconds": round(max(r[0] for r in res), 3),
-                  "parallelism": "one walled block per process", "same_config": False}
+    barrier, t1s, q = ctx.Barrier(len(blocks)), ctx.Array("d", len(blocks)), ctx.Queue()
+    procs = [ctx.Process(target=_block_proc, args=(i, b, wl, steps, budget_s, barrier, t1s, q))
+             for i, b in enumerate(blocks)]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    sec = max(r[0] for r in res)
+    runs["blocks"] = {"value": sum(r[1] for r in res) / sec, "block": [blocks[0].ni, blocks[0].nj, spec.nk],
+                      "procs": cores, "steps_timed": res[0][2], "seconds": round(sec, 3), "same_config": False}
+    best = max((k for k in runs if "value" in runs[k]), key=lambda k: runs[k]["value"])
+    info = {"reported": best, "runs": {k: {q: (round(x, 1) if isinstance(x, float) else x) for q, x in r.items()}
+                                       for k, r in runs.items()}}
+    return runs[best]["value"], info
 
 
 # --------------------------------------------------------------------------- GPU side
@@ -336,48 +367,51 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     """End to end through the C ABI with host buffers: every step uploads its
     inputs from pinned host memory (tracers and advection velocity; the
     barotropic forcing) and reads its results back (tracers; eta_t_bar, udrho),
-    stream-ordered copies (mom5gpu_copy_field_async) on an upload and a
-    read-back stream, ordered by events.  Three time levels rotate so that the
-    uploads of step s+1 and the read-back of step s overlap the compute of step
-    s.  Single-level inputs (velocity, forcing) are uploaded into a device
-    staging buffer while the previous step still reads the field and copied
-    into it (device to device) once that step is past it.  `warm` untimed
-    steps first (first-touch allocations, graph captures); the timed steps are
-    timed on the host wall clock and each stream's work by CUDA events."""
+    stream-ordered copies (mom5gpu_copy_field_async) ordered by events.
+
+    Uploads go into device staging buffers on the upload stream as soon as the
+    previous step's staging copies are done, so they run beside the previous
+    step's read-back; a staging stream then copies them into their fields
+    (device to device) once the field is free: a tracer time level after its
+    read-back two steps earlier (three time levels rotate), the velocity after
+    the previous step's advection, the forcing after its barotropic step.
+    `warm` untimed steps first (first-touch allocations, graph captures); the
+    timed steps are timed on the host wall clock and each stream's work by
+    CUDA events."""
     import numpy as np
     import torch
     from mom5_gb300.capi import F
     pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True)
+    dev = lambda n: torch.empty(n, dtype=torch.float64, device="cuda")
     n3, nw = d.count(F.TRACER), d.count(F.WRHO_BT)
     n2 = d.count(F.ETA_T_BAR)
-    ups, downs = [], []  # (field, n, host buffer) per step
-    stage = []           # (field, host buffer, device staging buffer, read by advection?)
+    ups = []    # (field, n, host buffer, device staging buffer, when the field is free: "level", "adv", "step")
+    downs = []  # (field, n, host buffer)
     if ntr > 0:
         for n in range(1, ntr + 1):
             h = pin(n3)
             h.copy_(torch.from_numpy(d.get(F.TRACER, n=n, level=1)))
-            ups.append((F.TRACER, n, h))
+            ups.append((F.TRACER, n, h, dev(n3), "level"))
             downs.append((F.TRACER, n, pin(n3)))
         for fid, cnt in ((F.UHRHO_ET, n3), (F.VHRHO_NT, n3), (F.WRHO_BT, nw)):
             h = pin(cnt)
             h.copy_(torch.from_numpy(d.get(fid)))
-            stage.append((fid, h, torch.empty(cnt, dtype=torch.float64, device="cuda"), True))
-        for fid in (F.RHO_DZT,):  # the third level of the rotation
-            d.set(fid, d.get(fid, level=1), level=3)
+            ups.append((fid, 0, h, dev(cnt), "adv"))
+        d.set(F.RHO_DZT, d.get(F.RHO_DZT, level=1), level=3)  # the third level of the rotation
     if wl.barotropic:
         for fid in (F.FORCING_BT_U, F.FORCING_BT_V):
             h = pin(n2)
             h.copy_(torch.from_numpy(d.get(fid)))
-            stage.append((fid, h, torch.empty(n2, dtype=torch.float64, device="cuda"), False))
+            ups.append((fid, 0, h, dev(n2), "step"))
         for fid in (F.ETA_T_BAR, F.UDRHO_U, F.UDRHO_V):
             downs.append((fid, 0, pin(n2)))
-        d.set(F.THICKU, d.get(F.THICKU, level=1), level=3)
-        for fid in (F.ETA_T_BAR, F.UDRHO_U, F.UDRHO_V, F.CONV_RHO_UD_T):
+        for fid in (F.THICKU, F.ETA_T_BAR, F.UDRHO_U, F.UDRHO_V, F.CONV_RHO_UD_T):
             d.set(fid, d.get(fid, level=1), level=3)
-    h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
+    h2d, stg, d2h = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
     total = warm + steps
     tev = lambda: torch.cuda.Event(enable_timing=True)
-    ev = {k: [tev() for _ in range(total)] for k in ("h2d0", "h2d1", "c0", "adv", "c1", "d2h0", "d2h1")}
+    names = ("up0", "up1", "stg1", "c0", "adv", "c1", "d2h0", "d2h1")
+    ev = {k: [tev() for _ in range(total)] for k in names}
     torch.cuda.synchronize()
     t0 = None
     for s_ in range(total):
@@ -385,22 +419,26 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
         lin, lout = (1, 2, 3)[(2 * s_) % 3], (1, 2, 3)[(2 * s_ + 1) % 3]
-        if s_ >= 2:  # lin was read back by step s-2
-            h2d.wait_event(ev["d2h1"][s_ - 2])
-        ev["h2d0"][s_].record(h2d)
-        for fid, n, h in ups:
-            d.copy_field_async(fid, h.data_ptr(), 1, h2d.cuda_stream, n=n, level=lin)
-        with torch.cuda.stream(h2d):  # the staging buffers' last reader is earlier on h2d
-            for fid, h, buf, _ in stage:
+        # host -> staging, once the previous step's staging copies have read the buffers
+        if s_ >= 1:
+            h2d.wait_event(ev["stg1"][s_ - 1])
+        ev["up0"][s_].record(h2d)
+        with torch.cuda.stream(h2d):
+            for _, _, h, buf, _ in ups:
                 buf.copy_(h, non_blocking=True)
-        for phase in (True, False):  # fields the advection reads, then the barotropic forcing
-            if s_ >= 1:
-                h2d.wait_event(ev["adv"][s_ - 1] if phase else ev["c1"][s_ - 1])
-            for fid, h, buf, adv in stage:
-                if adv == phase:
-                    d.copy_field_async(fid, buf.data_ptr(), 1, h2d.cuda_stream)
-        ev["h2d1"][s_].record(h2d)
-        stream.wait_event(ev["h2d1"][s_])
+        ev["up1"][s_].record(h2d)
+        # staging -> fields, each once its field is free
+        stg.wait_event(ev["up1"][s_])
+        for when, after in (("level", "d2h1"), ("adv", "adv"), ("step", "c1")):
+            back = 2 if when == "level" else 1
+            if s_ >= back:
+                stg.wait_event(ev[after][s_ - back])
+            for fid, n, _, buf, w in ups:
+                if w == when:
+                    d.copy_field_async(fid, buf.data_ptr(), 1, stg.cuda_stream, n=n,
+                                       level=lin if fid == F.TRACER else 0)
+        ev["stg1"][s_].record(stg)
+        stream.wait_event(ev["stg1"][s_])
         ev["c0"][s_].record(stream)
         if ntr > 0:
             d.tracer_advection_step(lin, lin, lout, wl.dtts)
@@ -419,14 +457,15 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     mean = lambda a, b: float(np.mean([ev[a][s].elapsed_time(ev[b][s]) for s in rng]))
     wait = float(np.mean([ev["c1"][s - 1].elapsed_time(ev["c0"][s]) for s in rng]))
     span = ev["c0"][warm].elapsed_time(ev["c1"][total - 1]) / steps
-    hb = 8 * (sum(h.numel() for _, _, h in ups) + sum(h.numel() for _, h, _, _ in stage))
+    hb = 8 * sum(h.numel() for _, _, h, _, _ in ups)
     db = 8 * sum(h.numel() for _, _, h in downs)
+    up, rb = mean("up0", "up1"), mean("d2h0", "d2h1")
     timeline = {"unit": "ms per step (means over the timed steps, CUDA events)",
-                "host_wall": round(te * 1e3, 3), "compute_span": round(span, 3),
-                "upload": round(mean("h2d0", "h2d1"), 3), "compute": round(mean("c0", "c1"), 3),
-                "readback": round(mean("d2h0", "d2h1"), 3), "compute_waits_for_upload": round(wait, 3),
-                "upload_GBps": round(hb / mean("h2d0", "h2d1") / 1e6, 1),
-                "readback_GBps": round(db / mean("d2h0", "d2h1") / 1e6, 1)}
+                "host_wall": round(te * 1e3, 3), "compute_span": round(span, 3), "compute": round(mean("c0", "c1"), 3),
+                "upload": round(up, 3), "readback": round(rb, 3), "staging_to_fields": round(mean("up1", "stg1"), 3),
+                "compute_waits_for_inputs": round(wait, 3),
+                "upload_GBps": round(hb / up / 1e6, 1) if up > 0 else None,
+                "readback_GBps": round(db / rb / 1e6, 1) if rb > 0 else None}
     return te, hb, db, timeline
 
 
@@ -511,9 +550,9 @@ def run_ours(args, rank, world):
                "d2h_bytes_per_step": db, "steps": max(3, min(args.steps, 30)),
                "api": "mom5gpu_copy_field_async (pinned host buffers, upload and read-back streams) / "
                       "mom5gpu_tracer_advection_step / mom5gpu_update_ocean_barotropic",
-               "timing": "host wall clock over the steps, every copy inside; copies of neighbouring steps overlap "
-                         "the compute (three time levels rotate; single-level inputs go through device staging "
-                         "buffers)", "timeline": timeline}
+               "timing": "host wall clock over the steps, every copy inside; uploads land in device staging "
+                         "buffers beside the previous step's read-back and compute, then are copied into their "
+                         "fields (three time levels rotate)", "timeline": timeline}
 
     l2note = ("inputs larger than L2 (tracer state alone %.1f GB)" % (2 * ntr * cells * 8 / 1e9)
               if 2 * ntr * cells * 8 > 129e6 else "inputs smaller than L2, not flushed (launch/latency-bound case)")
@@ -797,7 +836,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--config", choices=["c2", "c0", "c1", "c2s"], default="c2")
+    ap.add_argument("--config", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--scheme", choices=[n for n, _ in SCHEMES], default="mdfl_sweby",
                     help="advection scheme of every tracer (the headline is mdfl_sweby)")
     ap.add_argument("--metrics-jsonl", default=None, help="also append the figures to this JSON-lines file")
@@ -817,15 +856,17 @@ def main():
         spec = wl.spec()
         cores = os.cpu_count() or 1
         v, info = cpu_reference(wl, spec, args.steps, cores)
-        how = (f"whole grid, OpenMP on {cores} threads" if info["same_config"]
-               else f"{cores} processes x walled block {info['block']}")
+        r = info["runs"][info["reported"]]
+        how = (f"whole grid, OpenMP on {cores} threads" if info["reported"] == "openmp"
+               else f"{cores} processes x walled block {r['block']}")
         out = {"metric": METRIC, "value": round(v, 1), "unit": "cell-updates/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
                "config": {"workload": f"{args.config.upper()}: {wl.describe(spec)}, reference algorithm on the "
-                                      f"host cores ({how})", "sample": info},
+                                      f"host cores (the faster of: whole grid with OpenMP; one walled block per "
+                                      f"process)", "sample": info, "same_config": r["same_config"]},
                "cpu_baseline": {"value": round(v, 1), "unit": "cell-updates/s", "cores": cores, "kind": "port",
-                                "sample": f"C restatement stepping loop, {how}, {info['steps_timed']} timed steps "
+                                "sample": f"C restatement stepping loop, {how}, {r['steps_timed']} timed steps "
                                           f"after one untimed step"},
                "e2e": {"value": round(v, 1), "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}

@@ -100,6 +100,15 @@ def config_c2_block(seed: int = 3, ntracers: int = 10) -> DomainSpec:
                       cyclic_x=False, continent=(150, 100, 40, 30), hmin=2000.0, ntracers=ntracers, seed=seed)
 
 
+def config_c2_band(seed: int = 5, ntracers: int = 10) -> DomainSpec:
+    """A 1440x360x50 band of the 0.25 degree global grid (lat -40..50, periodic
+    in x), 10 tracers: one third of the global config's rows, for profiling
+    captures that fill more than two waves of the precision-form kernel while
+    holding about 6 GB on the device."""
+    return DomainSpec(ni=1440, nj=360, nk=50, lon0=0.0, lon1=360.0, lat0=-40.0, lat1=50.0,
+                      cyclic_x=True, continent=(600, 120, 160, 120), hmin=2000.0, ntracers=ntracers, seed=seed)
+
+
 def config_c2_polar_block(seed: int = 4, ntracers: int = 10) -> DomainSpec:
     """A 360x270x50 block of the 0.25 degree grid reaching the global grid's
     poleward edge (lon 0-90, lat 12.5..80), periodic in x, 10 tracers: the
