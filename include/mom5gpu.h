@@ -412,6 +412,97 @@ double mom5gpu_batch_last_ms(mom5gpu_batch* b);
 /* Kernels launched by the batch since creation (graph replays count their kernels). */
 long mom5gpu_batch_launch_count(const mom5gpu_batch* b);
 
+/* ---- domain decomposition -------------------------------------------------
+ * The reference runs one domain as a 2-D layout of blocks, one per processor
+ * element, each with a one-cell halo kept current by mpp_update_domains
+ * (set_ocean_domain, ocean_domains.F90:123-; halo updates of the MDFL
+ * intermediates ocean_tracer_advect.F90:3912, :3970, of T(taup1)
+ * ocean_model.F90:1903-1911, of the predicted eta ocean_barotropic.F90:3383
+ * and of the barotropic outputs :2846-2901).  Here each block is its own
+ * mom5gpu_domain, created NON-cyclic with the block's compute size (ni, nj >= 2)
+ * and with its grid and inputs set on the whole data domain (halo included,
+ * as after the reference's halo updates).  The entry points below split a step
+ * into the phases between which the reference exchanges halos; the caller moves
+ * each halo region from the neighbour that owns it (mom5gpu_copy_boxes on one
+ * GPU; a send/receive between processes otherwise).  Decomposed stepping covers
+ * the FP64 MDFL Sweby / DST-linear step with the explicit update (at most 10
+ * tracers, advect_sweby_all or not) and the B-grid barotropic step. */
+
+/* Sides of a block: halos of the four faces and the four corners. */
+#define MOM5GPU_WEST 0
+#define MOM5GPU_EAST 1
+#define MOM5GPU_SOUTH 2
+#define MOM5GPU_NORTH 3
+#define MOM5GPU_SOUTHWEST 4
+#define MOM5GPU_SOUTHEAST 5
+#define MOM5GPU_NORTHWEST 6
+#define MOM5GPU_NORTHEAST 7
+/* What is exchanged (mom5gpu_halo_region / mom5gpu_halo_base). */
+#define MOM5GPU_HALO_FIELD 1   /* one-cell halo of a field (all tracers when n = 0), faces and corners */
+#define MOM5GPU_HALO_MDFL_Z 2  /* tracer_mdfl after the z pass: two columns, west and east */
+#define MOM5GPU_HALO_MDFL_X 3  /* tracer_mdfl after the x pass: two rows, south and north */
+#define MOM5GPU_HALO_BT_ETA 4  /* predicted eta of a subcycle (plane level = 0 or 1), faces and corners */
+#define MOM5GPU_HALO_BT_PS 5   /* the surface pressure formed from it, faces and corners */
+/* Roles: the region a block sends to its neighbour on `side`, or the region it
+ * receives from that neighbour.  A block's SEND region for side s pairs with
+ * its neighbour's RECV region for the opposite side. */
+#define MOM5GPU_SEND 0
+#define MOM5GPU_RECV 1
+
+/* A strided 3-D box of doubles: n[0] x n[1] x n[2] elements, element (x,y,z) at
+ * src + x*src_stride[0] + y*src_stride[1] + z*src_stride[2] (likewise dst). */
+typedef struct mom5gpu_box {
+  const double* src;
+  double* dst;
+  long src_stride[3];
+  long dst_stride[3];
+  int n[3];
+} mom5gpu_box;
+
+/* Declare which sides of d face a neighbouring block (1) or the edge of the
+ * whole domain (0).  Allocates the MDFL halo strips.  A side facing a
+ * neighbour takes its halo from the exchanges; a side at the edge keeps the
+ * single-PE rule of a non-cyclic boundary (the halo holds zero). */
+int mom5gpu_set_neighbours(mom5gpu_domain* d, int west, int east, int south, int north);
+/* tmask_mdfl of a block with its two-cell halo from the neighbours, as
+ * mdfl_init's halo update builds it (ocean_tracer_advect.F90:1660-1668): a host
+ * array of (ni+4)*(nj+4)*nk values 0 or 1, i fastest, i = -1..ni+2.  Call
+ * after mom5gpu_tracer_advect_init, which builds the single-PE mask. */
+int mom5gpu_set_mask_halo2(mom5gpu_domain* d, const double* tmask_halo2);
+/* Geometry of a halo region, relative to the base of its array
+ * (mom5gpu_halo_base): offset of element (0,0,0), strides and extents.  Pure
+ * host arithmetic on dims (no device call): level count nlev for
+ * MOM5GPU_HALO_FIELD (nk, nk+1, 1, or ntr*nk for all tracers), ignored for the
+ * other kinds.  MOM5GPU_EINVAL for a side the kind does not exchange. */
+int mom5gpu_halo_region(const mom5gpu_dims* dims, int kind, int nlev, int side, int role, long* offset,
+                        long stride[3], int n[3]);
+/* Device base address of the array a halo region lives in: the field (field,
+ * n, level) for MOM5GPU_HALO_FIELD; for the MDFL kinds the intermediate
+ * (SEND) or its strip (RECV); for the barotropic kinds the scratch plane. */
+int mom5gpu_halo_base(mom5gpu_domain* d, int kind, int field, int n, int level, int role, double** base);
+/* Copy count boxes (device memory, same extents on both sides) in one launch on
+ * `stream` (a cudaStream_t; NULL = the default stream). */
+int mom5gpu_copy_boxes(const mom5gpu_box* boxes, int count, void* stream);
+/* One pass of the FP64 MDFL step over every tracer (taum1 = tau, two-level):
+ * pass 1 zeroes th_tendency's halo ring and runs the z pass, then exchange
+ * MOM5GPU_HALO_MDFL_Z; pass 2 the x pass, then exchange MOM5GPU_HALO_MDFL_X;
+ * pass 3 the y pass and th_tendency.  mom5gpu_update_tracer(d, 0, ...) then
+ * updates every tracer; exchange MOM5GPU_HALO_FIELD of MOM5GPU_TRACER (n = 0)
+ * at taup1 closes the step. */
+int mom5gpu_mdfl_pass(mom5gpu_domain* d, int pass, int taum1, int tau, double dtime);
+/* One phase of update_ocean_barotropic (B grid, FP64) for a decomposed block:
+ *   0 start (time-average accumulators, subcycle state from tau),
+ *   1 predictor of subcycle itime, then exchange MOM5GPU_HALO_BT_ETA with
+ *     level = (itime + 1) % 2 (the plane the predictor wrote) and
+ *     MOM5GPU_HALO_BT_PS,
+ *   2 momentum and corrector of subcycle itime,
+ *   3 time averages, then exchange MOM5GPU_HALO_FIELD of ETA_T_BAR, UDRHO_U,
+ *     UDRHO_V at taup1,
+ *   4 conv_rho_ud_t, eta_u, ps, then exchange CONV_RHO_UD_T and ETA_U at taup1,
+ *   5 grad_ps.
+ * Phases 1 and 2 run for itime = 1..nts in turn. */
+int mom5gpu_barotropic_phase(mom5gpu_domain* d, int tau, int taup1, int phase, int itime);
+
 /* ---- allocation-free variant ---------------------------------------------
  * No counterpart in the reference.  For callers that cannot let the library
  * allocate device memory (a model whose GPU memory is reserved by its own pool,

@@ -70,6 +70,12 @@ class Options(C.Structure):
                 ("zero_nonlinear_forcing_bt", C.c_int), ("psom_limit_prather", C.c_int)]
 
 
+class Box(C.Structure):
+    """mom5gpu_box: a strided 3-D box of doubles, copied src -> dst."""
+    _fields_ = [("src", C.c_void_p), ("dst", C.c_void_p), ("src_stride", C.c_long * 3),
+                ("dst_stride", C.c_long * 3), ("n", C.c_int * 3)]
+
+
 class Mom5GpuError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"[{status}] {msg}")
@@ -133,6 +139,14 @@ def lib() -> C.CDLL:
             "mom5gpu_timing_query": (C.c_int, [vp, C.c_char_p, dp, C.POINTER(C.c_long)]),
             "mom5gpu_launch_count": (C.c_long, [vp]),
             "mom5gpu_mdfl_sweby_noalloc": (C.c_int, [C.POINTER(Dims), C.c_int, C.c_double] + [vp] * 14),
+            "mom5gpu_set_neighbours": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+            "mom5gpu_set_mask_halo2": (C.c_int, [vp, dp]),
+            "mom5gpu_halo_region": (C.c_int, [C.POINTER(Dims), C.c_int, C.c_int, C.c_int, C.c_int,
+                                              C.POINTER(C.c_long), C.c_long * 3, C.c_int * 3]),
+            "mom5gpu_halo_base": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
+            "mom5gpu_copy_boxes": (C.c_int, [C.POINTER(Box), C.c_int, vp]),
+            "mom5gpu_mdfl_pass": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double]),
+            "mom5gpu_barotropic_phase": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
             "mom5gpu_batch_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
             "mom5gpu_batch_destroy": (None, [vp]),
             "mom5gpu_batch_last_error": (C.c_char_p, [vp]),
@@ -249,6 +263,11 @@ class Domain:
         self.check(lib().mom5gpu_barotropic_init(self.h, float(dtuv), float(dtbt)))
         return lib().mom5gpu_barotropic_nts(self.h)
 
+    @property
+    def nts(self) -> int:
+        """Barotropic subcycles per step (0 before barotropic_init)."""
+        return lib().mom5gpu_barotropic_nts(self.h)
+
     # ---- hot path (reference names) ----
     def horz_advect_tracer(self, n, taum1, tau, dtime):
         self.check(lib().mom5gpu_horz_advect_tracer(self.h, n, taum1, tau, float(dtime)))
@@ -305,6 +324,25 @@ class Domain:
 
     def set_itt0(self, itt0):
         self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))
+
+    # ---- decomposed blocks (decomp.py) ----
+    def set_neighbours(self, west, east, south, north):
+        self.check(lib().mom5gpu_set_neighbours(self.h, int(west), int(east), int(south), int(north)))
+
+    def set_mask_halo2(self, mask):
+        m = np.ascontiguousarray(mask, dtype=np.float64)
+        self.check(lib().mom5gpu_set_mask_halo2(self.h, m.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def halo_base(self, kind, role, field=0, n=0, level=0) -> int:
+        p = C.c_void_p()
+        self.check(lib().mom5gpu_halo_base(self.h, kind, field, n, level, role, C.byref(p)))
+        return p.value
+
+    def mdfl_pass(self, pass_, taum1, tau, dtime):
+        self.check(lib().mom5gpu_mdfl_pass(self.h, int(pass_), taum1, tau, float(dtime)))
+
+    def barotropic_phase(self, tau, taup1, phase, itime=0):
+        self.check(lib().mom5gpu_barotropic_phase(self.h, tau, taup1, int(phase), int(itime)))
 
     def copy_field_async(self, field, host_ptr, to_device, stream=None, n=0, level=0):
         """Stream-ordered copy between the field and host memory at host_ptr (an
@@ -433,3 +471,23 @@ def header_symbols():
     """Every function the header declares."""
     txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
     return sorted(set(re.findall(r"\b(mom5gpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+def halo_region(dims: Dims, kind: int, nlev: int, side: int, role: int):
+    """(offset, strides, extents) of a halo region relative to its array's base
+    (mom5gpu_halo_region: host arithmetic only, no device needed)."""
+    off, st, n = C.c_long(), (C.c_long * 3)(), (C.c_int * 3)()
+    r = lib().mom5gpu_halo_region(C.byref(dims), kind, nlev, side, role, C.byref(off), st, n)
+    if r != OK:
+        raise Mom5GpuError(r, f"halo_region(kind={kind}, side={side}, role={role})")
+    return off.value, tuple(st), tuple(n)
+
+
+def copy_boxes(boxes, stream=None):
+    """One launch copying every Box in `boxes` (device memory)."""
+    if not boxes:
+        return
+    arr = (Box * len(boxes))(*boxes)
+    r = lib().mom5gpu_copy_boxes(arr, len(boxes), C.c_void_p(stream) if stream else None)
+    if r != OK:
+        raise Mom5GpuError(r, lib().mom5gpu_last_error(None).decode())

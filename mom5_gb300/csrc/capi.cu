@@ -292,6 +292,8 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
     if (p) cudaFree(p);
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
+  if (d->hz) cudaFree(d->hz);
+  if (d->hx) cudaFree(d->hx);
   if (d->kmt_d) cudaFree(d->kmt_d);
   for (auto& gr : d->bt_graphs)
     if (gr.exec) cudaGraphExecDestroy(gr.exec);

@@ -202,6 +202,26 @@ DEVI double tm_yhalo(const Geo& g, const double* a, int i, int j, int k) {
   return a[I3(g, i, j, k)];
 }
 
+// tracer_mdfl of tracer n at a halo column or row: from the strip a
+// neighbouring subdomain's exchange filled (decomposed domains), else by the
+// single-PE rule above.
+DEVI double tz_halo(const MdflArgs& a, int n, int i, int j, int k) {
+  const Geo& g = a.g;
+  if ((i < 1 || i > g.ni) && (a.nbr & (i < 1 ? 1 : 2))) {
+    const int s = i < 1 ? i + 1 : i - g.ni + 1;  // -1, 0, ni+1, ni+2 -> 0..3
+    return a.hz[(((long)n * g.nk + k) * g.nj + (j - 1)) * 4 + s];
+  }
+  return tm_xhalo(g, a.tz + n * g.n3, i, j, k);
+}
+DEVI double tx_halo(const MdflArgs& a, int n, int i, int j, int k) {
+  const Geo& g = a.g;
+  if ((j < 1 || j > g.nj) && (a.nbr & (j < 1 ? 4 : 8))) {
+    const int s = j < 1 ? j + 1 : j - g.nj + 1;
+    return a.hx[(((long)n * g.nk + k) * 4 + s) * g.ni + (i - 1)];
+  }
+  return tm_yhalo(g, a.tx + n * g.n3, i, j, k);
+}
+
 constexpr int kTX = 128;
 
 // x-face i of row (j,k): fluxes of every tracer into sm[n][slot].  Rs[n][r-1..r+1]
@@ -221,8 +241,7 @@ DEVI void x_face(const MdflArgs& a, int i, int j, int k, double (*sm)[kTX + 1], 
   bool fm = m1 && m2;
 #pragma unroll 1
   for (int n = 0; n < a.ntr; ++n) {
-    const double* tz = a.tz + n * g.n3;
-    double tB = tm_xhalo(g, tz, i, j, k), tC = tm_xhalo(g, tz, i + 1, j, k);
+    double tB = tz_halo(a, n, i, j, k), tC = tz_halo(a, n, i + 1, j, k);
     sm[n][slot] = fm ? face_flux<SWEBY, Ar>(massflux, Rs[n][r - 1], Rs[n][r], Rs[n][r + 1], tB, tC, d0, d1, c) : 0.0;
   }
 }
@@ -243,8 +262,7 @@ DEVI void mdfl_x_body(MdflArgs a, int bx, int by, int bz) {
     bool ma = a.mask2[IM(g, f, j, k)], mb = a.mask2[IM(g, f + 1, j, k)];
 #pragma unroll 1
     for (int n = 0; n < a.ntr; ++n) {
-      const double* tz = a.tz + n * g.n3;
-      Rs[n][sl] = (mb && ma) ? Ar::sub(tm_xhalo(g, tz, f + 1, j, k), tm_xhalo(g, tz, f, j, k)) : 0.0;
+      Rs[n][sl] = (mb && ma) ? Ar::sub(tz_halo(a, n, f + 1, j, k), tz_halo(a, n, f, j, k)) : 0.0;
     }
   }
   __syncthreads();
@@ -305,10 +323,8 @@ DEVI YFace y_geom(const MdflArgs& a, int i, int j, int k, bool& m0, bool& m1) {
 template <bool SWEBY, class Ar>
 DEVI double y_flux(const MdflArgs& a, const YFace& f, int i, int j, int k, int n, int t, double (*Ra)[kMdflThreads],
                    double (*Rb)[kMdflThreads], double& tB) {
-  const Geo& g = a.g;
-  const double* tx = a.tx + n * g.n3;
-  tB = tm_yhalo(g, tx, i, j, k);
-  double tC = tm_yhalo(g, tx, i, j + 1, k), tD = tm_yhalo(g, tx, i, j + 2, k);
+  tB = tx_halo(a, n, i, j, k);
+  double tC = tx_halo(a, n, i, j + 1, k), tD = tx_halo(a, n, i, j + 2, k);
   double Rjm = Ra[n][t], Rj = Rb[n][t];
   double Rjp = (f.m3 && f.m2) ? Ar::sub(tD, tC) : 0.0;
   Ra[n][t] = Rj;
@@ -340,9 +356,8 @@ DEVI void mdfl_y_body(MdflArgs a, int TJ, int bx, int by, int bz) {
     const YFace f = y_geom(a, i, j0 - 1, k, m0, m1);
 #pragma unroll 1
     for (int n = 0; n < a.ntr; ++n) {
-      const double* tx = a.tx + n * g.n3;
-      double tA = tm_yhalo(g, tx, i, j0 - 2, k), tB = tm_yhalo(g, tx, i, j0 - 1, k);
-      double tC = tm_yhalo(g, tx, i, j0, k);
+      double tA = tx_halo(a, n, i, j0 - 2, k), tB = tx_halo(a, n, i, j0 - 1, k);
+      double tC = tx_halo(a, n, i, j0, k);
       Ra[n][t] = (m1 && m0) ? Ar::sub(tB, tA) : 0.0;
       Rb[n][t] = (f.m2 && m1) ? Ar::sub(tC, tB) : 0.0;
       double tb;

@@ -117,6 +117,11 @@ struct mom5gpu_domain {
     std::vector<unsigned char> key;
   };
   std::vector<BtGraph> bt_graphs;
+  // domain decomposition (decomp.cu): sides facing a neighbouring subdomain
+  // (bits 1 west, 2 east, 4 south, 8 north) and the MDFL halo strips
+  int nbr = 0;
+  double* hz = nullptr;  // tracer_mdfl after z, columns -1, 0, ni+1, ni+2: ntr*nk*nj*4
+  double* hx = nullptr;  // after x, rows -1, 0, nj+1, nj+2: ntr*nk*4*ni
 };
 
 namespace mom5 {
@@ -156,6 +161,13 @@ struct MdflArgs {
   double* th;                 // th_tendency of tracer 0, tracer n at th + n*g.n3
   int tj = 0;                 // y-pass rows per thread (0 = choose from the domain size)
   int th_fresh = 0;           // th is +0 at every compute cell: the y pass writes out + 0.0 instead of th + out
+  // decomposed domains: sides whose halo comes from a neighbouring subdomain
+  // (bits 1 west, 2 east, 4 south, 8 north) and the strips its exchange filled:
+  // tracer_mdfl after the z pass at i = -1, 0, ni+1, ni+2 (hz[((n*nk + k)*nj + j-1)*4 + slot])
+  // and after the x pass at j = -1, 0, nj+1, nj+2 (hx[((n*nk + k)*4 + slot)*ni + i-1])
+  int nbr = 0;
+  const double* hz = nullptr;
+  const double* hx = nullptr;
 };
 
 
@@ -224,6 +236,8 @@ int make_mix_args(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime
 // the three MDFL passes on the stream, for the tracers described by a
 // (at most 8 per call); scratch a.tz/a.tx and a.mask2 are the caller's.
 void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s);
+void run_mdfl_pass(const MdflArgs& a, bool all, bool sweby, int pass, cudaStream_t s);
+int launch_barotropic_phase(mom5gpu_domain* d, int tau, int taup1, int phase, int itime);
 void launch_halo_fill(const Geo& g, double* a, int nlev, int flags, cudaStream_t s);
 void launch_zero_ring(const Geo& g, double* a, long nlev, cudaStream_t s);
 int launch_mdfl(mom5gpu_domain* d, bool all, int n_first, int ntr, int taum1, int tau, double dtime,

@@ -125,6 +125,44 @@ static void run_mdfl_n(const MdflArgs& a, cudaStream_t s) {
   else run_mdfl<ALL, SWEBY, kMdflChunk>(a, s);
 }
 
+// one pass (1 z, 2 x, 3 y) of run_mdfl: a decomposed domain exchanges halos between them
+template <bool ALL, bool SWEBY, int MAXN>
+static void run_mdfl_one(const MdflArgs& a, int pass, cudaStream_t s) {
+  const Geo& g = a.g;
+  if (pass == 1) {
+    dim3 bz((g.ni + 127) / 128, g.nj);
+    k_mdfl_z<ALL, SWEBY, MAXN><<<bz, 128, 0, s>>>(a);
+  } else if (pass == 2) {
+    dim3 bx((g.ni + kTX - 1) / kTX, g.nj, g.nk);
+    k_mdfl_x<ALL, SWEBY, MAXN><<<bx, kTX, 0, s>>>(a);
+  } else {
+    long cols = (long)g.ni * g.nk;
+    int TJ = 16;
+    while (TJ > 2 && cols * ((g.nj + TJ - 1) / TJ) < 152L * 32 * 16) TJ /= 2;
+    if (a.tj > 0) TJ = a.tj;
+    dim3 by((g.ni + 127) / 128, (g.nj + TJ - 1) / TJ, g.nk);
+    k_mdfl_y<ALL, SWEBY, MAXN><<<by, 128, 0, s>>>(a, TJ);
+  }
+}
+
+template <bool ALL, bool SWEBY>
+static void run_mdfl_one_n(const MdflArgs& a, int pass, cudaStream_t s) {
+  if (a.ntr <= 1) run_mdfl_one<ALL, SWEBY, 1>(a, pass, s);
+  else if (a.ntr <= 2) run_mdfl_one<ALL, SWEBY, 2>(a, pass, s);
+  else if (a.ntr <= 4) run_mdfl_one<ALL, SWEBY, 4>(a, pass, s);
+  else run_mdfl_one<ALL, SWEBY, kMdflChunk>(a, pass, s);
+}
+
+void run_mdfl_pass(const MdflArgs& a, bool all, bool sweby, int pass, cudaStream_t s) {
+  if (all) {
+    if (sweby) run_mdfl_one_n<true, true>(a, pass, s);
+    else run_mdfl_one_n<true, false>(a, pass, s);
+  } else {
+    if (sweby) run_mdfl_one_n<false, true>(a, pass, s);
+    else run_mdfl_one_n<false, false>(a, pass, s);
+  }
+}
+
 void run_mdfl_kernels(const MdflArgs& a, bool all, bool sweby, cudaStream_t s) {
   if (all) {
     if (sweby) run_mdfl_n<true, true>(a, s);
@@ -176,6 +214,9 @@ int make_mdfl_args(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, 
   a.tx = d->mdfl_b;
   a.th = fptr(d, MOM5GPU_TH_TENDENCY, n_first, 0);
   a.tj = d->tune_y_tj;
+  a.nbr = d->nbr;
+  a.hz = d->hz ? d->hz + (size_t)(n_first - 1) * g.nk * g.nj * 4 : nullptr;
+  a.hx = d->hx ? d->hx + (size_t)(n_first - 1) * g.nk * 4 * g.ni : nullptr;
   long thstride = NT > 1 ? (long)(fptr(d, MOM5GPU_TH_TENDENCY, 2, 0) - fptr(d, MOM5GPU_TH_TENDENCY, 1, 0)) : g.n3;
   if (thstride != g.n3 || a.tstride != g.n3) return fail(d, MOM5GPU_ESTATE, "unexpected tracer layout");
   if (!a.dat || !a.datr || !a.dxte || !a.dyte || !a.dxtn || !a.dytn || !a.uh || !a.vh || !a.w || !a.rdz || !a.T ||
@@ -1400,6 +1441,58 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   k_bt_post3<<<g2, 128, 0, s>>>(a, ps_out, gxo, gyo);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "barotropic");
+}
+
+// One phase of launch_barotropic for a decomposed block (B grid, FP64): the
+// same kernels in the same order, with the single-PE halo fills left to the
+// caller's exchanges (a block is created non-cyclic).
+int launch_barotropic_phase(mom5gpu_domain* d, int tau, int taup1, int phase, int itime) {
+  const Geo& g = d->geo;
+  BtArgs a;
+  BtExtra x;
+  int rc = make_bt_args(d, tau, taup1, &a, &x);
+  if (rc) return rc;
+  if (a.cgrid || a.btf) return fail(d, MOM5GPU_EUNSUPPORTED, "decomposed barotropic: B grid, FP64 only");
+  if (phase < 0 || phase > 5) return fail(d, MOM5GPU_EINVAL, "barotropic phase %d (0..5)", phase);
+  if ((phase == 1 || phase == 2) && (itime < 1 || itime > a.nts))
+    return fail(d, MOM5GPU_EINVAL, "barotropic subcycle %d (1..%d)", itime, a.nts);
+  long n2 = g.n2;
+  cudaStream_t s = d->stream;
+  dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
+  int so = (itime + 0) % 2, sn = (itime + 1) % 2;
+  switch (phase) {
+    case 0:
+      k_bt_init<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(a, x.eta_bar_tau, x.eta_tau, x.ud_tau, x.vd_tau, x.pme,
+                                                              x.river, x.source, x.eta_smooth,
+                                                              d->opt.initsum_with_bar);
+      count_launches(d, 1);
+      break;
+    case 1:
+      k_bt_pred<<<g2, 128, 0, s>>>(a, so, sn, itime > 1);
+      count_launches(d, 1);
+      break;
+    case 2:
+      k_bt_mom_b<<<g2, 128, 0, s>>>(a, so, sn);
+      k_bt_corr<<<g2, 128, 0, s>>>(a, so, sn, (double)(a.nts - itime + 1));
+      count_launches(d, 2);
+      break;
+    case 3: {
+      double rntsp1 = 1.0 / ((double)a.nts + 1.0);
+      double rnts = a.stepB ? 2.0 / ((double)a.nts * (double)(a.nts + 1)) : 1.0 / (double)a.nts;
+      k_bt_post1<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(n2, rntsp1, rnts, a.eta_bar, a.udrho_u, a.udrho_v);
+      count_launches(d, 1);
+      break;
+    }
+    case 4:
+      k_bt_post2<<<g2, 128, 0, s>>>(a, x.conv, x.eta_u, x.ps_out);
+      count_launches(d, 1);
+      break;
+    default:
+      k_bt_post3<<<g2, 128, 0, s>>>(a, x.ps_out, x.gxo, x.gyo);
+      count_launches(d, 1);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "barotropic phase");
 }
 
 // ---------------------------------------------------------------------------
