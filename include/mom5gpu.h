@@ -509,9 +509,12 @@ int mom5gpu_barotropic_phase(mom5gpu_domain* d, int tau, int taup1, int phase, i
  * a process under a hard device-memory cap, or code that must not call
  * cudaMalloc/cudaFree because they synchronise the device): adds the MDFL Sweby
  * (scheme 9) or DST-linear (scheme 10) advection tendency of ONE tracer to
- * th_tendency, exactly as mom5gpu_horz_advect_tracer does, without any device
- * allocation.  Every pointer is a caller-owned DEVICE array in the domain
- * layout above: 2-D metrics (dat, datr, dxte, dyte, dxtn, dytn), 3-D tmask,
+ * th_tendency, with the values mom5gpu_horz_advect_tracer gives under the
+ * default options (FP64 precision, advect_sweby_all = 0,
+ * zero_tracer_advect_horz = 0), without any device allocation.  Every pointer
+ * is a caller-owned DEVICE array in the domain layout above: 2-D metrics (dat,
+ * datr, dxte, dyte, dxtn, dytn), 3-D tmask (values 0.0 or 1.0 only: any other
+ * value counts as wet here, where the domain API refuses it),
  * uhrho_et, vhrho_nt, rho_dzt(tau), T(taum1), th_tendency (read and written),
  * and wrho_bt with nk+1 levels.  Work is queued on `stream` (NULL = default).
  * Limit: (ni+2)*(nj+2)*nk <= 2097152 data-domain cells (and
@@ -519,8 +522,10 @@ int mom5gpu_barotropic_phase(mom5gpu_domain* d, int tau, int taup1, int phase, i
  * message in mom5gpu_last_error(NULL).  The scratch is a 36 MB file-scope
  * device array held by every GPU that loads the library until exit; the first
  * call on each device looks up its address, so make that first call before any
- * stream capture.  Calls share the one array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * stream capture.  The address is kept per device number for the process: it
+ * belongs to the device's primary context, so the calls must run in that
+ * context and not after a cudaDeviceReset.  Calls share the one array: calls
+ * that overlap on the GPU race and must be serialised by the caller. */
 int mom5gpu_mdfl_sweby_noalloc(const mom5gpu_dims* dims, int scheme, double dtime, const double* tmask,
                                const double* dat, const double* datr, const double* dxte, const double* dyte,
                                const double* dxtn, const double* dytn, const double* uhrho_et,

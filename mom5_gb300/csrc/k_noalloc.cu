@@ -16,7 +16,9 @@
 // array's device address with cudaGetSymbolAddress while that device is
 // current (in host code the array's name is only a host-side stand-in, not a
 // device address) and caches it; that first call should therefore come before
-// any stream capture.  All calls on a device share the one array: calls that
+// any stream capture.  The cached address is that of the device's primary
+// context (the runtime's): it is not valid in another context made current
+// through the driver API, nor after cudaDeviceReset.  All calls on a device share the one array: calls that
 // overlap on the GPU (on different streams, or from different host threads)
 // race on it and must be serialised by the caller.  Every element a call reads
 // is written earlier in the same call, so nothing needs to be cleared between
@@ -42,7 +44,8 @@ double* g_addr[kMaxDevices] = {nullptr};
 // tmask with a 2-cell halo under the single-domain halo rules: the compute
 // value, its periodic image in a cyclic direction (corners only when both
 // directions are cyclic), or zero beyond a wall (mdfl_init,
-// ocean_tracer_advect.F90:1660-1669).
+// ocean_tracer_advect.F90:1660-1669).  tmask holds 0.0 or 1.0; any non-zero
+// value counts as wet.
 __global__ void k_build_mask2(Geo g, const double* tmask, uint8_t* m2) {
   long n = (long)(g.ni + 4) * (g.nj + 4) * g.nk;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {

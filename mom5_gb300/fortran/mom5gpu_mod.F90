@@ -235,7 +235,8 @@ end module mom5gpu_c
 module mom5gpu_mod
   ! Drop-in wrappers.  ocean_tracer.F90:2300-2303 and ocean_model.F90:1752,
   ! :1819, :1941 call these exactly as they call the reference procedures once
-  ! the use statements point here (see INTEGRATION.md).
+  ! their use statements name this module instead of ocean_tracer_advect_mod
+  ! and ocean_barotropic_mod.
   use, intrinsic :: iso_c_binding
   use mom5gpu_c
   use mpp_mod,          only: mpp_error, FATAL
