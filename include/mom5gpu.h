@@ -299,15 +299,20 @@ int mom5gpu_update_tracer(mom5gpu_domain* d, int n, int taum1, int taup1, double
  * halo update. */
 int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime);
 /* Time the candidate launch shapes of mom5gpu_tracer_advection_step on this
- * domain (precision form: tile height 16, 24, 32 or 64 rows; FP64: y-pass rows per
- * thread 2..16) and keep the fastest.  The trials step taum1 = tau = 1 to
+ * domain (precision form: tile height 16, 24, 32 or 64 rows, plain, with a
+ * cp.async tracer prefetch, or TMA-staged; FP64: y-pass rows per thread 2..16)
+ * and keep the fastest.  The trials step taum1 = tau = 1 to
  * taup1 = 2: time level 2 of the tracers and th_tendency are overwritten.
  * A summary is written to report (may be NULL). */
 int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t report_len);
 /* The launch shape autotune chose, or one to pin: precision-form tile height
- * (16, 24, 32 or 64 rows incl. halo), tracer prefetch into shared memory (height 16
- * only), FP64 y-pass rows per thread (0 = built-in choice, 2, 4, 8, 16).
- * Every shape gives the same results bit for bit. */
+ * (16, 24, 32 or 64 rows incl. halo); staging of the tile's operands: prefetch
+ * 0 = plain loads, 1 = tracer levels prefetched by cp.async (height 16 only),
+ * 2 = tiles staged by TMA with the tracer levels carried down the column in
+ * registers (heights 16, 24, 32; domains of even ni, else the plain kernel);
+ * FP64 y-pass rows per thread (0 = built-in choice, 2, 4, 8, 16).  Every shape
+ * gives the same results bit for bit.  A TMA-staged launch whose bounded wait
+ * gave up is reported by the next mom5gpu_synchronize as MOM5GPU_ETIMEDOUT. */
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
 int mom5gpu_get_tuning(const mom5gpu_domain* d, int* rows, int* prefetch, int* tj);
 /* eta_and_pbot_tendency (ocean_barotropic.F90:2668-2734), depth-based. */

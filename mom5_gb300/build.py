@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, exact FP64)
 UNITS = [("capi.cu", True), ("k_fp64.cu", True), ("k_mixed.cu", False), ("k_batch.cu", False), ("k_batch64.cu", True),
-         ("batch.cu", True), ("k_noalloc.cu", True), ("k_psom.cu", True), ("restart.cu", True), ("decomp.cu", True)]
+         ("batch.cu", True), ("k_noalloc.cu", True), ("k_psom.cu", True), ("restart.cu", True), ("decomp.cu", True),
+         ("k_mixed_tma.cu", False)]
 
 
 def _nvcc() -> str:

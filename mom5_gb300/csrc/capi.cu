@@ -292,6 +292,7 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
     if (p) cudaFree(p);
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
+  if (d->tma_err) cudaFree(d->tma_err);
   if (d->hz) cudaFree(d->hz);
   if (d->hx) cudaFree(d->hx);
   if (d->kmt_d) cudaFree(d->kmt_d);
@@ -318,7 +319,17 @@ int mom5gpu_set_stream(mom5gpu_domain* d, void* stream) {
 int mom5gpu_synchronize(mom5gpu_domain* d) {
   if (!d) return MOM5GPU_EINVAL;
   cudaError_t e = cudaStreamSynchronize(d->stream);
-  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "synchronize");
+  if (e != cudaSuccess) return cuda_fail(d, e, "synchronize");
+  if (d->tma_err) {  // a bounded wait of the TMA-staged precision kernel gave up
+    int v = 0;
+    e = cudaMemcpy(&v, d->tma_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(d, e, "synchronize");
+    if (v) {
+      cudaMemset(d->tma_err, 0, sizeof(int));
+      return fail(d, MOM5GPU_ETIMEDOUT, "precision form: a tile's staged copy did not arrive; its results are void");
+    }
+  }
+  return MOM5GPU_OK;
 }
 
 size_t mom5gpu_device_bytes(const mom5gpu_domain* d) { return d ? d->bytes : 0; }
@@ -859,11 +870,14 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
 
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj) {
   if (!d) return MOM5GPU_EINVAL;
-  if ((rows != 16 && rows != 24 && rows != 32 && rows != 64) || (prefetch && rows != 16) ||
+  if ((rows != 16 && rows != 24 && rows != 32 && rows != 64) || prefetch < 0 || prefetch > 2 ||
+      (prefetch == 1 && rows != 16) || (prefetch == 2 && rows == 64) ||
       !(tj == 0 || tj == 2 || tj == 4 || tj == 8 || tj == 16))
-    return fail(d, MOM5GPU_EINVAL, "set_tuning: rows 16|24|32|64 (prefetch only with 16), tj 0|2|4|8|16");
+    return fail(d, MOM5GPU_EINVAL,
+                "set_tuning: rows 16|24|32|64, prefetch 0, 1 (cp.async, rows 16) or 2 (TMA, rows 16|24|32), "
+                "tj 0|2|4|8|16");
   d->tune_mixed_rows = rows;
-  d->tune_mixed_pf = prefetch ? 1 : 0;
+  d->tune_mixed_pf = prefetch;
   d->tune_y_tj = tj;
   return MOM5GPU_OK;
 }
@@ -881,10 +895,10 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   if (!d->advect_ready) return fail(d, MOM5GPU_ESTATE, "autotune before mom5gpu_tracer_advect_init");
   bool mixed = d->opt.precision == MOM5GPU_PRECISION_MIXED;
   // candidate launch shapes: precision-form tile height (and tracer prefetch); FP64 y-pass rows per thread
-  const int kRows[] = {32, 64, 24, 16, 16};
-  const int kPf[] = {0, 0, 0, 0, 1};
+  const int kRows[] = {32, 64, 24, 16, 16, 16, 24, 32};
+  const int kPf[] = {0, 0, 0, 0, 1, 2, 2, 2};
   const int kTj[] = {2, 4, 8, 16};
-  int ncand = mixed ? 5 : 4;
+  int ncand = mixed ? (d->geo.ni % 2 == 0 ? 8 : 5) : 4;
   cudaEvent_t t0, t1;
   if (cudaEventCreate(&t0) != cudaSuccess) return fail(d, MOM5GPU_ECUDA, "autotune events");
   if (cudaEventCreate(&t1) != cudaSuccess) {
@@ -915,7 +929,9 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
     cudaEventElapsedTime(&ms, t0, t1);
     ms /= 3.f;
     char line[96];
-    if (mixed) snprintf(line, sizeof(line), "rows=%d%s: %.3f ms; ", kRows[c], kPf[c] ? "+prefetch" : "", ms);
+    if (mixed)
+      snprintf(line, sizeof(line), "rows=%d%s: %.3f ms; ", kRows[c], kPf[c] == 2 ? "+tma" : kPf[c] ? "+prefetch" : "",
+               ms);
     else snprintf(line, sizeof(line), "tj=%d: %.3f ms; ", kTj[c], ms);
     rep += line;
     if (ms < best) {
@@ -933,7 +949,9 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   }
   if (rc) return rc;
   char line[64];
-  if (mixed) snprintf(line, sizeof(line), "chosen rows=%d%s", kRows[bestc], kPf[bestc] ? "+prefetch" : "");
+  if (mixed)
+    snprintf(line, sizeof(line), "chosen rows=%d%s", kRows[bestc],
+             kPf[bestc] == 2 ? "+tma" : kPf[bestc] ? "+prefetch" : "");
   else snprintf(line, sizeof(line), "chosen tj=%d", kTj[bestc]);
   rep += line;
   if (report && report_len) {

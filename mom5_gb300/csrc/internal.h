@@ -107,7 +107,8 @@ struct mom5gpu_domain {
   long launches = 0;
   // autotuned launch shapes (0 = built-in heuristic)
   int tune_mixed_rows = 32;  // precision-form tile height incl. halo: 16, 24, 32 or 64
-  int tune_mixed_pf = 0;     // precision form, height 16: tracer levels prefetched into shared memory
+  int tune_mixed_pf = 0;     // precision form: 1 tracer levels prefetched by cp.async (height 16), 2 TMA-staged tiles
+  int* tma_err = nullptr;    // set by the TMA-staged kernel when a bounded wait gave up
   int tune_y_tj = 0;         // FP64 y-pass rows per thread
   // CUDA graphs of the barotropic subcycle loop, one per set of kernel arguments
   // (the bytes of the BtArgs it was captured with: time levels rotate), at most
@@ -308,5 +309,7 @@ int prepare_batch_mixed();
 // ---- precision form (k_mixed.cu) ----
 int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, int taup1, double dtime,
                       bool fused_update);
+// TMA-staged variant of one launch (k_mixed_tma.cu); MOM5GPU_EUNSUPPORTED: use the plain kernel
+int launch_mixed_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all);
 
 }  // namespace mom5

@@ -65,8 +65,8 @@ int run_mixed_zr(mom5gpu_domain* d, MixArgs a, int n0) {
 
 template <int NC>
 int run_mixed(mom5gpu_domain* d, MixArgs a, int n0) {
-  if (d->tune_mixed_rows == 16)
-    return d->tune_mixed_pf ? run_mixed_zr<NC, 16, true>(d, a, n0) : run_mixed_zr<NC, 16, false>(d, a, n0);
+  if (d->tune_mixed_rows == 16 && d->tune_mixed_pf == 1) return run_mixed_zr<NC, 16, true>(d, a, n0);
+  if (d->tune_mixed_rows == 16) return run_mixed_zr<NC, 16, false>(d, a, n0);
   if (d->tune_mixed_rows == 24) return run_mixed_zr<NC, 24, false>(d, a, n0);
   if (d->tune_mixed_rows == 64) return run_mixed_zr<NC, 64, false>(d, a, n0);
   return run_mixed_zr<NC, 32, false>(d, a, n0);
@@ -160,6 +160,11 @@ int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int ta
     }
     if (!a.T || !a.out) return fail(d, MOM5GPU_ENOMEM, "precision form: tracer storage");
     int n0 = fused_update ? n_first - 1 + c0 : 0;
+    if (d->tune_mixed_pf == 2) {
+      rc = launch_mixed_tma(d, a, n0, fptr(d, MOM5GPU_TRACER, 1, taum1), n_first - 1 + c0,
+                            d->dims.num_prog_tracers);
+      if (rc != MOM5GPU_EUNSUPPORTED) continue;
+    }
     if (cn <= 1) rc = run_mixed<1>(d, a, n0);
     else if (cn <= 2) rc = run_mixed<2>(d, a, n0);
     else if (cn <= 4) rc = run_mixed<4>(d, a, n0);

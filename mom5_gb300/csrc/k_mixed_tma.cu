@@ -1,0 +1,448 @@
+// Precision form of MDFL Sweby with its tiles staged into shared memory by TMA.
+//
+// The same method and the same FP32 arithmetic, operation for operation, as the
+// tile kernel of mixed_body.cuh (so every result is bit-identical to it): a
+// tile of 28 columns by ZR-4 rows with its 2-cell halo recomputed, marching
+// down k, the face terms of a level shared by every tracer of the launch.
+// What changes is where the operands come from:
+//   * one tile position per thread (a warp per tile row), the tracers' levels
+//     k-1, k, k+1 carried down the column in registers, so each level of each
+//     tracer is brought on chip once instead of four times;
+//   * the level that enters the window (k+2) arrives by TMA
+//     (cp.async.bulk.tensor, completion on an mbarrier) into one shared-memory
+//     slot per tracer, requested as soon as the slot is free -- one level and
+//     the rest of the tracers ahead of its use;
+//   * the level's fields (uhrho_et, vhrho_nt, wrho_bt, rho_dzt(tau),
+//     rho_dztr, rho_dzt(taum1)) arrive by TMA one level ahead, with the
+//     neighbours the face terms need in the same box;
+//   * the 2-D metrics are read once per tile into registers.
+// A TMA box is 34 columns wide starting at an even column (16-byte aligned for
+// FP64), covering the tile's 32 columns and the +-1 neighbours.  Box cells
+// outside the data domain read as zero; tile positions outside the compute
+// domain (halo columns and rows, periodic images) take their values from
+// global memory at their image, exactly as the plain kernel does, so the seam
+// of a periodic domain needs no special box.  Requires an even ni (row stride
+// a multiple of 16 bytes); the launcher falls back to the plain kernel
+// otherwise.
+//
+// Every wait on an mbarrier is bounded; a wait that gives up sets *err, the
+// block stops at its next barrier (after waiting, again bounded, for the
+// copies it issued) and mom5gpu_synchronize reports MOM5GPU_ETIMEDOUT.
+#include <cuda.h>
+#include <math.h>
+
+#include "mixed_body.cuh"
+
+namespace mom5 {
+
+using namespace mixed;
+
+namespace {
+
+constexpr int BX = 34;  // box width: tile columns i0-3 .. i0+30
+
+struct TmaMaps {
+  CUtensorMap T, f[6];  // tracers (every tracer of the time level), then the fields below
+};
+enum { F_UH = 0, F_VH, F_W, F_RDZ, F_RDZR, F_RDZM1 };
+
+DEVI unsigned su32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+DEVI void mbar_init(uint64_t* b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(b)) : "memory");
+}
+DEVI void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+DEVI void mbar_expect(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+DEVI void tma3(void* dst, const CUtensorMap* m, int x, int y, int z, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(m)), "r"(x), "r"(y), "r"(z), "r"(su32(b))
+      : "memory");
+}
+DEVI bool mbar_test(uint64_t* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for phase `parity` of an mbarrier: false after kSpin polls (each
+// poll itself waits a hardware-chosen while before it reports not ready).
+constexpr unsigned kSpin = 1u << 22;
+DEVI bool mbar_wait(uint64_t* b, unsigned parity) {
+  for (unsigned it = 0; it < kSpin; ++it)
+    if (mbar_test(b, parity)) return true;
+  return false;
+}
+
+template <int NC, int ZR>
+struct TmaSmem {
+  static constexpr int SLOT = ZR * BX;  // doubles per box (a multiple of 16: 128-byte aligned slots)
+  double t[NC][SLOT];                   // level k+2 of each tracer
+  double f[6][SLOT];                    // the level's fields
+  float tx[ZR * 32];                    // tracer after the x pass
+  float fy[ZR * 32];                    // y fluxes
+  uint8_t wet[ZR * 32];                 // tmask at level k
+  alignas(8) uint64_t bar[NC + 1];      // one per tracer slot, one for the fields
+  int pending[NC + 1];                  // 1 + parity of a phase in flight, 0 = none (thread 0's bookkeeping)
+};
+
+template <int NC, int ZR>
+__global__ void __launch_bounds__(32 * ZR, 1)
+    k_mdfl_mixed_tma(MixArgs a, int n0, int zt0, const __grid_constant__ TmaMaps maps, int* err) {
+  using S = TmaSmem<NC, ZR>;
+  constexpr int SLOT = S::SLOT;
+  constexpr int TJ = ZR - 4;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  S& s = *reinterpret_cast<S*>(smem_raw);
+  const Geo& g = a.g;
+  const int zi = threadIdx.x & 31, zj = threadIdx.x >> 5, c = zj * 32 + zi;
+  const int i0 = 1 + blockIdx.x * TI, j0 = 1 + blockIdx.y * TJ;
+  const int bx0 = i0 - 3, by0 = j0 - 2;  // box origin (bx0 even)
+  const int sc = zj * BX + zi + 1;       // this position in a box
+  const float dt = a.dtime;
+  const float sixth = 1.0f / 6.0f;
+  const int ntr = a.ntr < NC ? a.ntr : NC;
+  // this position: raw data-domain coordinates, its image, whether the boxes hold it
+  const int pi = i0 - 2 + zi, pj = j0 - 2 + zj;
+  int i = pi, j = pj;
+  const bool in = image(g, i, j);
+  const bool direct = pi >= 1 && pi <= g.ni && pj >= 1 && pj <= g.nj;
+  const long o = in ? I2(g, i, j) : 0;
+  const bool interior = zj >= 2 && zj <= ZR - 3 && zi >= 2 && zi <= 29 && pi <= g.ni && pj <= g.nj;
+  bool bad = false;
+
+  if (threadIdx.x == 0) {
+    for (int q = 0; q <= NC; ++q) {
+      mbar_init(&s.bar[q]);
+      s.pending[q] = 0;
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  // first loads: the fields of level 0 and level min(2, nk-1) of every tracer
+  if (threadIdx.x == 0) {
+    mbar_expect(&s.bar[NC], 6u * SLOT * 8u);
+    for (int f = 0; f < 6; ++f) tma3(s.f[f], &maps.f[f], bx0, by0, f == F_W ? 1 : 0, &s.bar[NC]);
+    s.pending[NC] = 1;  // phase 0 in flight
+    const int l2 = g.nk > 2 ? 2 : g.nk - 1;
+    for (int n = 0; n < ntr; ++n) {
+      mbar_expect(&s.bar[n], SLOT * 8u);
+      tma3(s.t[n], &maps.T, bx0, by0, (zt0 + n) * g.nk + l2, &s.bar[n]);
+      s.pending[n] = 1;  // phase 0 in flight
+    }
+  }
+  // 2-D metrics of this position, once per tile
+  float m_dat = 0.f, m_datr = 0.f, m_dyte = 0.f, m_dyte_w = 0.f, m_dxte = 0.f, m_dxtn = 0.f, m_dytn = 0.f;
+  if (in) {
+    m_dat = d2f(a.dat[o]);
+    m_datr = d2f(a.datr[o]);
+    m_dyte = d2f(a.dyte[o]);
+    m_dyte_w = d2f(a.dyte[I2(g, i - 1, j)]);
+    m_dxte = d2f(a.dxte[o]);
+    m_dxtn = d2f(a.dxtn[o]);
+    m_dytn = d2f(a.dytn[o]);
+  }
+  // the window of each tracer: levels km1, k, kp1 at k = 0 (0, 0, min(1, nk-1)), and
+  // the flux through the top face
+  float w0[NC], w1[NC], w2[NC], ftp[NC];
+  {
+    const int l1 = g.nk > 1 ? 1 : 0;
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+      w0[n] = w1[n] = w2[n] = ftp[n] = 0.f;
+      if (n < ntr && in) {
+        const double* T = a.T + (long)n * g.n3;
+        w0[n] = w1[n] = d2f(T[o]);
+        w2[n] = d2f(T[(long)l1 * g.n2 + o]);
+      }
+    }
+  }
+  // wet bits of levels km1, k, kp1, kp2 (mask2 at the raw position)
+  unsigned mb = 0;
+  {
+    const int l1 = g.nk > 1 ? 1 : 0, l2 = g.nk > 2 ? 2 : g.nk - 1;
+    mb = (mask_at(g, a.mask2, pi, pj, 0) ? 3u : 0u) | (mask_at(g, a.mask2, pi, pj, l1) ? 4u : 0u) |
+         (mask_at(g, a.mask2, pi, pj, l2) ? 8u : 0u);
+  }
+  float wk_prev = 0.f;  // w at the top face of the level (0 at the surface)
+
+  for (int k = 0; k < g.nk; ++k) {
+    const int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
+    const int kp3 = k + 3 < g.nk ? k + 3 : g.nk - 1;
+    // the wet bit that enters the window at the next level, loaded a level ahead
+    const bool m_next = (k + 1 < g.nk) && mask_at(g, a.mask2, pi, pj, kp3);
+    // ---- level terms of this position ----
+    if (!mbar_wait(&s.bar[NC], (unsigned)(k & 1))) bad = true;
+    const bool wet = (mb & 2u) != 0;
+    float zmf = 0.f, zd0 = 0.f, zd1 = 0.f, zc = 0.f, zdtr = 0.f, zwd = 0.f;
+    float xmf = 0.f, xd0 = 0.f, xd1 = 0.f, xc = 0.f, xcoef = 0.f, xdiv = 0.f;
+    float ymf = 0.f, yd0 = 0.f, yd1 = 0.f, yc = 0.f, uq = 0.f, ur = 0.f;
+    const bool xin = in && zi >= 2 && zi <= 29;
+    if (in) {
+      // own values and the neighbours' (i+1, i-1, j+1): from the boxes for a
+      // compute-domain position, else from global memory at the image
+      const long p = I3(g, i, j, k);
+      const double rdz_c = direct ? s.f[F_RDZ][sc] : a.rdz[p];
+      const double uh_c = direct ? s.f[F_UH][sc] : a.uh[p];
+      const double w_c = direct ? s.f[F_W][sc] : a.w[I3(g, i, j, k + 1)];
+      const float wk = d2f(w_c);
+      const float rr = 1.0f / d2f(rdz_c);
+      zmf = m_dat * wk;
+      float cfl = fabsf(wk * dt * rr);
+      zd0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
+      zd1 = (1.0f - cfl * cfl) * sixth;
+      zc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
+      zdtr = dt * rr;
+      zwd = wk_prev - wk;
+      wk_prev = wk;
+      if (zi >= 1 && zi <= 29) {
+        const double rdz_e = direct ? s.f[F_RDZ][sc + 1] : a.rdz[I3(g, i + 1, j, k)];
+        float u = d2f(uh_c);
+        xmf = m_dyte * u;
+        float den = (d2f(rdz_c) + d2f(rdz_e)) * m_dxte;
+        float cf = fabsf(__fdividef(u * dt * 2.0f, den));
+        xd0 = (2.0f - cf) * (1.0f - cf) * sixth;
+        xd1 = (1.0f - cf * cf) * sixth;
+        xc = __fdividef(1.0f - cf, 1.0e-30f + cf);
+      }
+      if (xin) {
+        const double uh_w = direct ? s.f[F_UH][sc - 1] : a.uh[I3(g, i - 1, j, k)];
+        xcoef = wet ? dt * m_datr / d2f(rdz_c) : 0.0f;
+        xdiv = m_dyte * d2f(uh_c) - m_dyte_w * d2f(uh_w);
+      }
+      if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= 29) {
+        const double rdz_n = direct ? s.f[F_RDZ][sc + BX] : a.rdz[I3(g, i, j + 1, k)];
+        const double vh_c = direct ? s.f[F_VH][sc] : a.vh[p];
+        float v = d2f(vh_c);
+        ymf = m_dxtn * v;
+        float den = (d2f(rdz_c) + d2f(rdz_n)) * m_dytn;
+        float cf = fabsf(__fdividef(v * dt * 2.0f, den));
+        yd0 = (2.0f - cf) * (1.0f - cf) * sixth;
+        yd1 = (1.0f - cf * cf) * sixth;
+        yc = __fdividef(1.0f - cf, 1.0e-30f + cf);
+      }
+      if (zj >= 2 && zj <= ZR - 3 && zi >= 2 && zi <= 29) {
+        if (a.fused) {
+          const double r = direct ? s.f[F_RDZR][sc] : a.rdzr[p];
+          const double m1 = direct ? s.f[F_RDZM1][sc] : a.rdz_m1[p];
+          uq = d2f(fma(m1, r, -1.0));
+          ur = wet ? d2f(rdz_c * r) : 0.0f;
+        } else {
+          ur = wet ? d2f(rdz_c) / dt : 0.0f;
+        }
+      }
+    }
+    s.wet[c] = in && wet;
+    // every thread is done with the level's field boxes: fetch the next level's
+    if (__syncthreads_or(bad)) goto abort;
+    if (threadIdx.x == 0 && k + 1 < g.nk) {
+      mbar_expect(&s.bar[NC], 6u * SLOT * 8u);
+      for (int f = 0; f < 6; ++f) tma3(s.f[f], &maps.f[f], bx0, by0, f == F_W ? k + 2 : k + 1, &s.bar[NC]);
+      s.pending[NC] = 1 + ((k + 1) & 1);
+    } else if (threadIdx.x == 0) {
+      s.pending[NC] = 0;
+    }
+
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+      if (n >= ntr) break;
+      const double* T = a.T + (long)n * g.n3;
+      // T(k) in FP64 for the state update, requested now and used last
+      const double t64 = interior ? T[I3(g, pi, pj, k)] : 0.0;
+      if (!mbar_wait(&s.bar[n], (unsigned)(k & 1))) bad = true;
+      // ---- z pass ----
+      float tzv = 0.f, tk = 0.f, fzv = 0.f;
+      if (in) {
+        const float tkp2 = direct ? d2f(s.t[n][sc]) : d2f(T[(long)kp2 * g.n2 + o]);
+        const float tkm1 = w0[n];
+        tk = w1[n];
+        const float tkp1 = w2[n];
+        const bool mkm1 = mb & 1u, mk = mb & 2u, mkp1 = mb & 4u, mkp2 = mb & 8u;
+        float Rjp = (mkm1 && mk) ? tkm1 - tk : 0.f;
+        float Rj = (mk && mkp1) ? tk - tkp1 : 0.f;
+        float Rjm = (mkp1 && mkp2) ? tkp1 - tkp2 : 0.f;
+        float fbt = (mkp1 && mk) ? face_flux(zmf, Rjm, Rj, Rjp, tkp1, tk, zd0, zd1, zc) : 0.f;
+        float adiv = m_datr * (fbt - ftp[n]);
+        fzv = zdtr * adiv;
+        tzv = tk + zdtr * (adiv + tk * zwd);
+        ftp[n] = fbt;
+        w0[n] = tk;
+        w1[n] = tkp1;
+        w2[n] = tkp2;
+      }
+      // ---- x fluxes (face zi, between zi and zi+1) by warp shuffles ----
+      const unsigned full = 0xffffffffu;
+      float tA = __shfl_up_sync(full, tzv, 1), tC = __shfl_down_sync(full, tzv, 1);
+      float tD = __shfl_down_sync(full, tzv, 2);
+      unsigned wt = (in && (mb & 2u)) ? 1u : 0u;
+      unsigned wA = __shfl_up_sync(full, wt, 1), wC = __shfl_down_sync(full, wt, 1);
+      unsigned wD = __shfl_down_sync(full, wt, 2);
+      float f = 0.f;
+      if (zi >= 1 && zi <= 29 && wt && wC) {
+        float Rjp = wD ? tD - tC : 0.f;
+        float Rj = tC - tzv;
+        float Rjm = wA ? tzv - tA : 0.f;
+        f = face_flux(xmf, Rjm, Rj, Rjp, tzv, tC, xd0, xd1, xc);
+      }
+      // ---- x update (cells zi = 2..29) ----
+      float fw = __shfl_up_sync(full, f, 1);
+      float t = 0.f, fi = 0.f;
+      if (xin) {
+        fi = xcoef * (fw - f);
+        t = tzv + (fi + xcoef * (tk * xdiv));
+      }
+      s.tx[c] = t;
+      // every thread has read slot n and written tx: the slot takes level k+3
+      if (__syncthreads_or(bad)) goto abort;
+      if (threadIdx.x == 0) {
+        if (k + 1 < g.nk) {
+          mbar_expect(&s.bar[n], SLOT * 8u);
+          tma3(s.t[n], &maps.T, bx0, by0, (zt0 + n) * g.nk + kp3, &s.bar[n]);
+          s.pending[n] = 1 + ((k + 1) & 1);
+        } else {
+          s.pending[n] = 0;
+        }
+      }
+      // ---- y fluxes (face zj, between rows zj and zj+1) ----
+      float fyv = 0.f;
+      if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= 29) {
+        bool m0 = s.wet[c - 32], m1 = s.wet[c], m2 = s.wet[c + 32], m3 = s.wet[c + 64];
+        if (m1 && m2) {
+          float ya = s.tx[c - 32], yb = s.tx[c], yc2 = s.tx[c + 32], yd = s.tx[c + 64];
+          float Rjp = (m3 && m2) ? yd - yc2 : 0.f;
+          float Rj = yc2 - yb;
+          float Rjm = (m1 && m0) ? yb - ya : 0.f;
+          fyv = face_flux(ymf, Rjm, Rj, Rjp, yb, yc2, yd0, yd1, yc);
+        }
+      }
+      s.fy[c] = fyv;
+      if (__syncthreads_or(bad)) goto abort;
+      // ---- interior: total increment and output ----
+      if (interior && (wet || a.fused)) {
+        float fyi = xcoef * (s.fy[c - 32] - fyv);
+        float dT = fzv + fi + fyi;
+        const long p = I3(g, pi, pj, k);
+        if (a.fused) {
+          float inc = uq * tk + ur * dT;
+          double tn = t64 + f2d(inc);
+          double* out = a.out + (long)(n0 + n) * g.n3;
+          out[p] = tn;
+          // halo update of T(taup1) in cyclic directions (ocean_model.F90:1903-1911)
+          int hi = (g.cx && pi == g.ni) ? 0 : (g.cx && pi == 1) ? g.ni + 1 : -1;
+          int hj = (g.cy && pj == g.nj) ? 0 : (g.cy && pj == 1) ? g.nj + 1 : -1;
+          if (hi >= 0) out[I3(g, hi, pj, k)] = tn;
+          if (hj >= 0) out[I3(g, pi, hj, k)] = tn;
+          if (hi >= 0 && hj >= 0) out[I3(g, hi, hj, k)] = tn;
+        } else if (wet) {
+          double* out = a.out + (long)n * g.n3;
+          out[p] = out[p] + f2d(ur * dT);
+        }
+      }
+    }
+    // the window of wet bits moves down one level
+    mb = (mb >> 1) | (m_next ? 8u : 0u);
+  }
+  return;
+
+abort:
+  if (threadIdx.x == 0) {
+    atomicOr(err, 1);
+    // wait, bounded, for the copies this block still has in flight
+    for (int q = 0; q <= NC; ++q)
+      if (s.pending[q]) mbar_wait(&s.bar[q], (unsigned)(s.pending[q] - 1));
+  }
+  __syncthreads();
+}
+
+// ---- host side ----
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+  static EncodeTiled fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// a 3-D FP64 tensor [nz][nyd][nxd] at base, boxes of 34 x rows x 1
+bool encode(CUtensorMap* m, const double* base, const Geo& g, long nz, int rows) {
+  EncodeTiled fn = encoder();
+  if (!fn || !base) return false;
+  cuuint64_t dim[3] = {(cuuint64_t)g.nxd, (cuuint64_t)g.nyd, (cuuint64_t)nz};
+  cuuint64_t stride[2] = {(cuuint64_t)g.nxd * 8, (cuuint64_t)g.n2 * 8};
+  cuuint32_t box[3] = {(cuuint32_t)BX, (cuuint32_t)rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dim, stride, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NC, int ZR>
+int run_tma_zr(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
+  const Geo& g = d->geo;
+  constexpr size_t smem = sizeof(TmaSmem<NC, ZR>);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_mdfl_mixed_tma<NC, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return cuda_fail(d, e, "TMA precision kernel attribute");
+    configured = true;
+  }
+  TmaMaps maps;
+  bool ok = encode(&maps.T, Tall, g, (long)ntr_all * g.nk, ZR) && encode(&maps.f[F_UH], a.uh, g, g.nk, ZR) &&
+            encode(&maps.f[F_VH], a.vh, g, g.nk, ZR) && encode(&maps.f[F_W], a.w, g, g.nk + 1, ZR) &&
+            encode(&maps.f[F_RDZ], a.rdz, g, g.nk, ZR) && encode(&maps.f[F_RDZR], a.rdzr, g, g.nk, ZR) &&
+            encode(&maps.f[F_RDZM1], a.rdz_m1, g, g.nk, ZR);
+  if (!ok) return fail(d, MOM5GPU_ECUDA, "TMA precision kernel: tensor-map encoding failed");
+  constexpr int TJ = ZR - 4;
+  dim3 grid((g.ni + TI - 1) / TI, (g.nj + TJ - 1) / TJ);
+  k_mdfl_mixed_tma<NC, ZR><<<grid, 32 * ZR, smem, d->stream>>>(a, n0, zt0, maps, d->tma_err);
+  count_launches(d, 1);
+  return MOM5GPU_OK;
+}
+
+template <int NC>
+int run_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
+  if (d->tune_mixed_rows == 24) return run_tma_zr<NC, 24>(d, a, n0, Tall, zt0, ntr_all);
+  if (d->tune_mixed_rows == 32) return run_tma_zr<NC, 32>(d, a, n0, Tall, zt0, ntr_all);
+  return run_tma_zr<NC, 16>(d, a, n0, Tall, zt0, ntr_all);
+}
+
+}  // namespace
+
+// The TMA variant of one launch of launch_mdfl_mixed (a = the launch's
+// arguments, tracers zt0 .. zt0+a.ntr-1 of the level whose first tracer is
+// Tall, ntr_all tracers in all).  MOM5GPU_EUNSUPPORTED when the domain cannot
+// be described to TMA (odd ni: the row stride is not a multiple of 16 bytes):
+// the caller then launches the plain kernel.
+int launch_mixed_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
+  if (d->geo.ni % 2 != 0) return MOM5GPU_EUNSUPPORTED;
+  if (!d->tma_err) {
+    cudaError_t e = cudaMalloc(&d->tma_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d->tma_err, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(d, e, "TMA precision kernel: error word");
+  }
+  if (a.ntr <= 1) return run_tma<1>(d, a, n0, Tall, zt0, ntr_all);
+  if (a.ntr <= 2) return run_tma<2>(d, a, n0, Tall, zt0, ntr_all);
+  if (a.ntr <= 4) return run_tma<4>(d, a, n0, Tall, zt0, ntr_all);
+  return run_tma<10>(d, a, n0, Tall, zt0, ntr_all);
+}
+
+}  // namespace mom5
