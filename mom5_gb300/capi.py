@@ -331,6 +331,9 @@ class Domain:
 
     def set_mask_halo2(self, mask):
         m = np.ascontiguousarray(mask, dtype=np.float64)
+        dm = self.dims
+        if m.size != (dm.ni + 4) * (dm.nj + 4) * dm.nk:
+            raise ValueError(f"tmask with a two-cell halo has {(dm.ni + 4) * (dm.nj + 4) * dm.nk} values, got {m.size}")
         self.check(lib().mom5gpu_set_mask_halo2(self.h, m.ctypes.data_as(C.POINTER(C.c_double))))
 
     def halo_base(self, kind, role, field=0, n=0, level=0) -> int:

@@ -1,13 +1,17 @@
 // Precision form of MDFL Sweby with its tiles staged into shared memory by TMA.
 //
-// The same method and the same FP32 arithmetic, operation for operation, as the
-// tile kernel of mixed_body.cuh (so every result is bit-identical to it): a
-// tile of 28 columns by ZR-4 rows with its 2-cell halo recomputed, marching
-// down k, the face terms of a level shared by every tracer of the launch.
-// What changes is where the operands come from:
+// The same method and the same FP32 arithmetic, operation for operation (the
+// helpers of mixed_body.cuh, every product and sum rounded on its own), as the
+// plain tile kernel, so every result is bit-identical to it: a tile of 28
+// columns by ZR-4 rows with its 2-cell halo recomputed, marching down k, the
+// face terms of a level shared by every tracer of the launch.  What changes is
+// where the operands come from and how often the block synchronises:
 //   * one tile position per thread (a warp per tile row), the tracers' levels
 //     k-1, k, k+1 carried down the column in registers, so each level of each
 //     tracer is brought on chip once instead of four times;
+//   * three block barriers per level (face terms; z and x passes of every
+//     tracer; y fluxes of every tracer), the per-tracer intermediates in shared
+//     memory, instead of two barriers per tracer;
 //   * the level that enters the window (k+2) arrives by TMA
 //     (cp.async.bulk.tensor, completion on an mbarrier) into one shared-memory
 //     slot per tracer, requested as soon as the slot is free -- one level and
@@ -28,6 +32,8 @@
 // Every wait on an mbarrier is bounded; a wait that gives up sets *err, the
 // block stops at its next barrier (after waiting, again bounded, for the
 // copies it issued) and mom5gpu_synchronize reports MOM5GPU_ETIMEDOUT.
+// Tile heights 16 and 24 (the per-tracer intermediates of 10 tracers at 32 rows
+// would not fit in shared memory).
 #include <cuda.h>
 #include <math.h>
 
@@ -84,13 +90,17 @@ struct TmaSmem {
   static constexpr int SLOT = ZR * BX;  // doubles per box (a multiple of 16: 128-byte aligned slots)
   double t[NC][SLOT];                   // level k+2 of each tracer
   double f[6][SLOT];                    // the level's fields
-  float tx[ZR * 32];                    // tracer after the x pass
-  float fy[ZR * 32];                    // y fluxes
+  float tx[NC][ZR * 32];                // each tracer after the x pass
+  float fzx[NC][ZR * 32];               // its z + x increment
+  float fy[NC][ZR * 32];                // its y fluxes
   uint8_t wet[ZR * 32];                 // tmask at level k
   alignas(8) uint64_t bar[NC + 1];      // one per tracer slot, one for the fields
   int pending[NC + 1];                  // 1 + parity of a phase in flight, 0 = none (thread 0's bookkeeping)
 };
 
+// One level is three phases with a block barrier between them: (1) the level's
+// face terms, (2) the z and x passes of every tracer, (3) the y fluxes of every
+// tracer, then the outputs -- three barriers per level whatever the tracer count.
 template <int NC, int ZR>
 __global__ void __launch_bounds__(32 * ZR, 1)
     k_mdfl_mixed_tma(MixArgs a, int n0, int zt0, const __grid_constant__ TmaMaps maps, int* err) {
@@ -105,7 +115,6 @@ __global__ void __launch_bounds__(32 * ZR, 1)
   const int bx0 = i0 - 3, by0 = j0 - 2;  // box origin (bx0 even)
   const int sc = zj * BX + zi + 1;       // this position in a box
   const float dt = a.dtime;
-  const float sixth = 1.0f / 6.0f;
   const int ntr = a.ntr < NC ? a.ntr : NC;
   // this position: raw data-domain coordinates, its image, whether the boxes hold it
   const int pi = i0 - 2 + zi, pj = j0 - 2 + zj;
@@ -114,6 +123,7 @@ __global__ void __launch_bounds__(32 * ZR, 1)
   const bool direct = pi >= 1 && pi <= g.ni && pj >= 1 && pj <= g.nj;
   const long o = in ? I2(g, i, j) : 0;
   const bool interior = zj >= 2 && zj <= ZR - 3 && zi >= 2 && zi <= 29 && pi <= g.ni && pj <= g.nj;
+  const bool xin = in && zi >= 2 && zi <= 29;
   bool bad = false;
 
   if (threadIdx.x == 0) {
@@ -133,7 +143,7 @@ __global__ void __launch_bounds__(32 * ZR, 1)
     for (int n = 0; n < ntr; ++n) {
       mbar_expect(&s.bar[n], SLOT * 8u);
       tma3(s.t[n], &maps.T, bx0, by0, (zt0 + n) * g.nk + l2, &s.bar[n]);
-      s.pending[n] = 1;  // phase 0 in flight
+      s.pending[n] = 1;
     }
   }
   // 2-D metrics of this position, once per tile
@@ -147,8 +157,8 @@ __global__ void __launch_bounds__(32 * ZR, 1)
     m_dxtn = d2f(a.dxtn[o]);
     m_dytn = d2f(a.dytn[o]);
   }
-  // the window of each tracer: levels km1, k, kp1 at k = 0 (0, 0, min(1, nk-1)), and
-  // the flux through the top face
+  // the window of each tracer: levels km1, k, kp1 (at k = 0: 0, 0, min(1, nk-1)),
+  // and the flux through the top face
   float w0[NC], w1[NC], w2[NC], ftp[NC];
   {
     const int l1 = g.nk > 1 ? 1 : 0;
@@ -176,55 +186,34 @@ __global__ void __launch_bounds__(32 * ZR, 1)
     const int kp3 = k + 3 < g.nk ? k + 3 : g.nk - 1;
     // the wet bit that enters the window at the next level, loaded a level ahead
     const bool m_next = (k + 1 < g.nk) && mask_at(g, a.mask2, pi, pj, kp3);
-    // ---- level terms of this position ----
+    // ---- phase 1: face terms of this position ----
     if (!mbar_wait(&s.bar[NC], (unsigned)(k & 1))) bad = true;
     const bool wet = (mb & 2u) != 0;
     float zmf = 0.f, zd0 = 0.f, zd1 = 0.f, zc = 0.f, zdtr = 0.f, zwd = 0.f;
     float xmf = 0.f, xd0 = 0.f, xd1 = 0.f, xc = 0.f, xcoef = 0.f, xdiv = 0.f;
     float ymf = 0.f, yd0 = 0.f, yd1 = 0.f, yc = 0.f, uq = 0.f, ur = 0.f;
-    const bool xin = in && zi >= 2 && zi <= 29;
     if (in) {
       // own values and the neighbours' (i+1, i-1, j+1): from the boxes for a
       // compute-domain position, else from global memory at the image
       const long p = I3(g, i, j, k);
       const double rdz_c = direct ? s.f[F_RDZ][sc] : a.rdz[p];
       const double uh_c = direct ? s.f[F_UH][sc] : a.uh[p];
-      const double w_c = direct ? s.f[F_W][sc] : a.w[I3(g, i, j, k + 1)];
-      const float wk = d2f(w_c);
-      const float rr = 1.0f / d2f(rdz_c);
-      zmf = m_dat * wk;
-      float cfl = fabsf(wk * dt * rr);
-      zd0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
-      zd1 = (1.0f - cfl * cfl) * sixth;
-      zc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
-      zdtr = dt * rr;
-      zwd = wk_prev - wk;
+      const float wk = d2f(direct ? s.f[F_W][sc] : a.w[I3(g, i, j, k + 1)]);
+      z_terms(wk, wk_prev, d2f(rdz_c), m_dat, dt, zmf, zd0, zd1, zc, zdtr, zwd);
       wk_prev = wk;
       if (zi >= 1 && zi <= 29) {
         const double rdz_e = direct ? s.f[F_RDZ][sc + 1] : a.rdz[I3(g, i + 1, j, k)];
-        float u = d2f(uh_c);
-        xmf = m_dyte * u;
-        float den = (d2f(rdz_c) + d2f(rdz_e)) * m_dxte;
-        float cf = fabsf(__fdividef(u * dt * 2.0f, den));
-        xd0 = (2.0f - cf) * (1.0f - cf) * sixth;
-        xd1 = (1.0f - cf * cf) * sixth;
-        xc = __fdividef(1.0f - cf, 1.0e-30f + cf);
+        h_terms(d2f(uh_c), m_dyte, d2f(rdz_c), d2f(rdz_e), m_dxte, dt, xmf, xd0, xd1, xc);
       }
       if (xin) {
         const double uh_w = direct ? s.f[F_UH][sc - 1] : a.uh[I3(g, i - 1, j, k)];
-        xcoef = wet ? dt * m_datr / d2f(rdz_c) : 0.0f;
-        xdiv = m_dyte * d2f(uh_c) - m_dyte_w * d2f(uh_w);
+        xcoef = x_coef(wet, dt, m_datr, d2f(rdz_c));
+        xdiv = x_div(m_dyte, d2f(uh_c), m_dyte_w, d2f(uh_w));
       }
       if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= 29) {
         const double rdz_n = direct ? s.f[F_RDZ][sc + BX] : a.rdz[I3(g, i, j + 1, k)];
         const double vh_c = direct ? s.f[F_VH][sc] : a.vh[p];
-        float v = d2f(vh_c);
-        ymf = m_dxtn * v;
-        float den = (d2f(rdz_c) + d2f(rdz_n)) * m_dytn;
-        float cf = fabsf(__fdividef(v * dt * 2.0f, den));
-        yd0 = (2.0f - cf) * (1.0f - cf) * sixth;
-        yd1 = (1.0f - cf * cf) * sixth;
-        yc = __fdividef(1.0f - cf, 1.0e-30f + cf);
+        h_terms(d2f(vh_c), m_dxtn, d2f(rdz_c), d2f(rdz_n), m_dytn, dt, ymf, yd0, yd1, yc);
       }
       if (zj >= 2 && zj <= ZR - 3 && zi >= 2 && zi <= 29) {
         if (a.fused) {
@@ -240,66 +229,49 @@ __global__ void __launch_bounds__(32 * ZR, 1)
     s.wet[c] = in && wet;
     // every thread is done with the level's field boxes: fetch the next level's
     if (__syncthreads_or(bad)) goto abort;
-    if (threadIdx.x == 0 && k + 1 < g.nk) {
-      mbar_expect(&s.bar[NC], 6u * SLOT * 8u);
-      for (int f = 0; f < 6; ++f) tma3(s.f[f], &maps.f[f], bx0, by0, f == F_W ? k + 2 : k + 1, &s.bar[NC]);
-      s.pending[NC] = 1 + ((k + 1) & 1);
-    } else if (threadIdx.x == 0) {
-      s.pending[NC] = 0;
+    if (threadIdx.x == 0) {
+      if (k + 1 < g.nk) {
+        mbar_expect(&s.bar[NC], 6u * SLOT * 8u);
+        for (int f = 0; f < 6; ++f) tma3(s.f[f], &maps.f[f], bx0, by0, f == F_W ? k + 2 : k + 1, &s.bar[NC]);
+        s.pending[NC] = 1 + ((k + 1) & 1);
+      } else {
+        s.pending[NC] = 0;
+      }
     }
 
+    // ---- phase 2: z and x passes of every tracer ----
+    const unsigned full = 0xffffffffu;
+    const unsigned wt = (in && wet) ? 1u : 0u;
+    const unsigned wA = __shfl_up_sync(full, wt, 1), wC = __shfl_down_sync(full, wt, 1);
+    const unsigned wD = __shfl_down_sync(full, wt, 2);
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
       if (n >= ntr) break;
-      const double* T = a.T + (long)n * g.n3;
-      // T(k) in FP64 for the state update, requested now and used last
-      const double t64 = interior ? T[I3(g, pi, pj, k)] : 0.0;
       if (!mbar_wait(&s.bar[n], (unsigned)(k & 1))) bad = true;
-      // ---- z pass ----
       float tzv = 0.f, tk = 0.f, fzv = 0.f;
       if (in) {
-        const float tkp2 = direct ? d2f(s.t[n][sc]) : d2f(T[(long)kp2 * g.n2 + o]);
-        const float tkm1 = w0[n];
+        const float tkp2 = d2f(direct ? s.t[n][sc] : a.T[(long)n * g.n3 + (long)kp2 * g.n2 + o]);
         tk = w1[n];
-        const float tkp1 = w2[n];
-        const bool mkm1 = mb & 1u, mk = mb & 2u, mkp1 = mb & 4u, mkp2 = mb & 8u;
-        float Rjp = (mkm1 && mk) ? tkm1 - tk : 0.f;
-        float Rj = (mk && mkp1) ? tk - tkp1 : 0.f;
-        float Rjm = (mkp1 && mkp2) ? tkp1 - tkp2 : 0.f;
-        float fbt = (mkp1 && mk) ? face_flux(zmf, Rjm, Rj, Rjp, tkp1, tk, zd0, zd1, zc) : 0.f;
-        float adiv = m_datr * (fbt - ftp[n]);
-        fzv = zdtr * adiv;
-        tzv = tk + zdtr * (adiv + tk * zwd);
-        ftp[n] = fbt;
+        tzv = z_cell(w0[n], tk, w2[n], tkp2, mb, zmf, zd0, zd1, zc, m_datr, zdtr, zwd, ftp[n], fzv);
         w0[n] = tk;
-        w1[n] = tkp1;
+        w1[n] = w2[n];
         w2[n] = tkp2;
       }
-      // ---- x fluxes (face zi, between zi and zi+1) by warp shuffles ----
-      const unsigned full = 0xffffffffu;
-      float tA = __shfl_up_sync(full, tzv, 1), tC = __shfl_down_sync(full, tzv, 1);
-      float tD = __shfl_down_sync(full, tzv, 2);
-      unsigned wt = (in && (mb & 2u)) ? 1u : 0u;
-      unsigned wA = __shfl_up_sync(full, wt, 1), wC = __shfl_down_sync(full, wt, 1);
-      unsigned wD = __shfl_down_sync(full, wt, 2);
+      // x flux of face zi (between zi and zi+1) by warp shuffles
+      const float tA = __shfl_up_sync(full, tzv, 1), tC = __shfl_down_sync(full, tzv, 1);
+      const float tD = __shfl_down_sync(full, tzv, 2);
       float f = 0.f;
-      if (zi >= 1 && zi <= 29 && wt && wC) {
-        float Rjp = wD ? tD - tC : 0.f;
-        float Rj = tC - tzv;
-        float Rjm = wA ? tzv - tA : 0.f;
-        f = face_flux(xmf, Rjm, Rj, Rjp, tzv, tC, xd0, xd1, xc);
-      }
-      // ---- x update (cells zi = 2..29) ----
-      float fw = __shfl_up_sync(full, f, 1);
+      if (zi >= 1 && zi <= 29 && wt && wC) f = h_flux(tA, tzv, tC, tD, wA, wD, xmf, xd0, xd1, xc);
+      const float fw = __shfl_up_sync(full, f, 1);
       float t = 0.f, fi = 0.f;
-      if (xin) {
-        fi = xcoef * (fw - f);
-        t = tzv + (fi + xcoef * (tk * xdiv));
-      }
-      s.tx[c] = t;
-      // every thread has read slot n and written tx: the slot takes level k+3
-      if (__syncthreads_or(bad)) goto abort;
-      if (threadIdx.x == 0) {
+      if (xin) t = x_cell(tzv, tk, fw, f, xcoef, xdiv, fi);
+      s.tx[n][c] = t;
+      s.fzx[n][c] = fa(fzv, fi);
+    }
+    // every tracer's slot is read: each takes level k+3
+    if (__syncthreads_or(bad)) goto abort;
+    if (threadIdx.x == 0) {
+      for (int n = 0; n < ntr; ++n) {
         if (k + 1 < g.nk) {
           mbar_expect(&s.bar[n], SLOT * 8u);
           tma3(s.t[n], &maps.T, bx0, by0, (zt0 + n) * g.nk + kp3, &s.bar[n]);
@@ -308,39 +280,43 @@ __global__ void __launch_bounds__(32 * ZR, 1)
           s.pending[n] = 0;
         }
       }
-      // ---- y fluxes (face zj, between rows zj and zj+1) ----
+    }
+
+    // ---- phase 3: y fluxes of every tracer (face zj, between rows zj and zj+1) ----
+    const bool yface = zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= 29;
+    const bool m0 = yface && s.wet[c - 32], m1 = yface && s.wet[c];
+    const bool m2 = yface && s.wet[c + 32], m3 = yface && s.wet[c + 64];
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+      if (n >= ntr) break;
       float fyv = 0.f;
-      if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= 29) {
-        bool m0 = s.wet[c - 32], m1 = s.wet[c], m2 = s.wet[c + 32], m3 = s.wet[c + 64];
-        if (m1 && m2) {
-          float ya = s.tx[c - 32], yb = s.tx[c], yc2 = s.tx[c + 32], yd = s.tx[c + 64];
-          float Rjp = (m3 && m2) ? yd - yc2 : 0.f;
-          float Rj = yc2 - yb;
-          float Rjm = (m1 && m0) ? yb - ya : 0.f;
-          fyv = face_flux(ymf, Rjm, Rj, Rjp, yb, yc2, yd0, yd1, yc);
-        }
-      }
-      s.fy[c] = fyv;
-      if (__syncthreads_or(bad)) goto abort;
-      // ---- interior: total increment and output ----
-      if (interior && (wet || a.fused)) {
-        float fyi = xcoef * (s.fy[c - 32] - fyv);
-        float dT = fzv + fi + fyi;
-        const long p = I3(g, pi, pj, k);
+      if (m1 && m2)
+        fyv = h_flux(s.tx[n][c - 32], s.tx[n][c], s.tx[n][c + 32], s.tx[n][c + 64], m1 && m0, m3 && m2, ymf, yd0, yd1,
+                     yc);
+      s.fy[n][c] = fyv;
+    }
+    if (__syncthreads_or(bad)) goto abort;
+    // ---- outputs of the interior cells ----
+    if (interior && (wet || a.fused)) {
+      const long p = I3(g, pi, pj, k);
+#pragma unroll
+      for (int n = 0; n < NC; ++n) {
+        if (n >= ntr) break;
+        const float dT = total_inc(s.fzx[n][c], xcoef, s.fy[n][c - 32], s.fy[n][c]);
         if (a.fused) {
-          float inc = uq * tk + ur * dT;
-          double tn = t64 + f2d(inc);
+          // T(taup1) = T + (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT; T(k) is w0 after the shift
+          const double tn = a.T[(long)n * g.n3 + p] + f2d(update_inc(uq, w0[n], ur, dT));
           double* out = a.out + (long)(n0 + n) * g.n3;
           out[p] = tn;
           // halo update of T(taup1) in cyclic directions (ocean_model.F90:1903-1911)
-          int hi = (g.cx && pi == g.ni) ? 0 : (g.cx && pi == 1) ? g.ni + 1 : -1;
-          int hj = (g.cy && pj == g.nj) ? 0 : (g.cy && pj == 1) ? g.nj + 1 : -1;
+          const int hi = (g.cx && pi == g.ni) ? 0 : (g.cx && pi == 1) ? g.ni + 1 : -1;
+          const int hj = (g.cy && pj == g.nj) ? 0 : (g.cy && pj == 1) ? g.nj + 1 : -1;
           if (hi >= 0) out[I3(g, hi, pj, k)] = tn;
           if (hj >= 0) out[I3(g, pi, hj, k)] = tn;
           if (hi >= 0 && hj >= 0) out[I3(g, hi, hj, k)] = tn;
         } else if (wet) {
           double* out = a.out + (long)n * g.n3;
-          out[p] = out[p] + f2d(ur * dT);
+          out[p] = out[p] + f2d(fm(ur, dT));
         }
       }
     }
@@ -421,7 +397,6 @@ int run_tma_zr(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, 
 template <int NC>
 int run_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
   if (d->tune_mixed_rows == 24) return run_tma_zr<NC, 24>(d, a, n0, Tall, zt0, ntr_all);
-  if (d->tune_mixed_rows == 32) return run_tma_zr<NC, 32>(d, a, n0, Tall, zt0, ntr_all);
   return run_tma_zr<NC, 16>(d, a, n0, Tall, zt0, ntr_all);
 }
 

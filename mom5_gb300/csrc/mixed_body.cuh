@@ -45,20 +45,86 @@ DEVI double f2d(float f) {
   return __hiloint2double((int)(sign | ((mag >> 3) + (896u << 20))), (int)(mag << 29));
 }
 
+// The FP32 arithmetic of the precision form.  Every product and sum is rounded
+// on its own (__fmul_rn / __fadd_rn / __fsub_rn are never contracted into a
+// multiply-add), so the result of a formula does not depend on how the
+// compiler schedules the kernel around it: every tile kernel built on these
+// helpers (plain, prefetching, TMA-staged, batched) gives the same bits.
+DEVI float fm(float a, float b) { return __fmul_rn(a, b); }
+DEVI float fa(float a, float b) { return __fadd_rn(a, b); }
+DEVI float fs(float a, float b) { return __fsub_rn(a, b); }
+
 DEVI float limiter(float theta, float d0, float d1, float c) {
-  float lin = d0 + d1 * theta;
-  return fmaxf(0.0f, fminf(fminf(1.0f, lin), c * theta));
+  float lin = fa(d0, fm(d1, theta));
+  return fmaxf(0.0f, fminf(fminf(1.0f, lin), fm(c, theta)));
 }
 
 // One division and one limiter for either sign of mf (operands selected first);
 // Tm - p is evaluated as Tm + (-p), the same IEEE operation.
 DEVI float face_flux(float mf, float Rjm, float Rj, float Rjp, float Tp, float Tm, float d0, float d1, float c) {
   bool pos = mf > 0.0f;
-  float theta = __fdividef(pos ? Rjm : Rjp, 1.0e-30f + Rj);
-  float p = limiter(theta, d0, d1, c) * Rj;
-  float r = mf * ((pos ? Tp : Tm) + (pos ? p : -p));
+  float theta = __fdividef(pos ? Rjm : Rjp, fa(1.0e-30f, Rj));
+  float p = fm(limiter(theta, d0, d1, c), Rj);
+  float r = fm(mf, fa(pos ? Tp : Tm, pos ? p : -p));
   return (pos || mf < 0.0f) ? r : 0.0f;
 }
+
+// d0, d1 and the limiter slope (1-cfl)/(1e-30+cfl) of a Courant number
+DEVI void cfl_terms(float cfl, float& d0, float& d1, float& c) {
+  const float sixth = 1.0f / 6.0f;
+  d0 = fm(fm(fs(2.0f, cfl), fs(1.0f, cfl)), sixth);
+  d1 = fm(fs(1.0f, fm(cfl, cfl)), sixth);
+  c = __fdividef(fs(1.0f, cfl), fa(1.0e-30f, cfl));
+}
+// vertical face terms of a column: mass flux dat*w, cfl = |w*dt/rho_dzt|
+DEVI void z_terms(float wk, float wkm1, float rdz, float dat, float dt, float& mf, float& d0, float& d1, float& c,
+                  float& dtr, float& wd) {
+  float rr = 1.0f / rdz;
+  mf = fm(dat, wk);
+  cfl_terms(fabsf(fm(fm(wk, dt), rr)), d0, d1, c);
+  dtr = fm(dt, rr);
+  wd = fs(wkm1, wk);
+}
+// horizontal face terms: mass flux len*u, cfl = |u*dt*2/((rdz + rdz_nb)*dist)|
+DEVI void h_terms(float u, float len, float rdz, float rdz_nb, float dist, float dt, float& mf, float& d0, float& d1,
+                  float& c) {
+  mf = fm(len, u);
+  float den = fm(fa(rdz, rdz_nb), dist);
+  cfl_terms(fabsf(__fdividef(fm(fm(u, dt), 2.0f), den)), d0, d1, c);
+}
+// x-cell terms: dtime*datr/rho_dzt where wet, and the x divergence dyte*uh - dyte(i-1)*uh(i-1)
+DEVI float x_coef(bool wet, float dt, float datr, float rdz) { return wet ? fm(dt, datr) / rdz : 0.0f; }
+DEVI float x_div(float dyte, float uh, float dyte_w, float uh_w) { return fs(fm(dyte, uh), fm(dyte_w, uh_w)); }
+// z pass of one column cell: returns tracer_mdfl after z; fz the z increment
+DEVI float z_cell(float tkm1, float tk, float tkp1, float tkp2, unsigned mb, float mf, float d0, float d1, float c,
+                  float datr, float dtr, float wd, float& ftp, float& fz) {
+  const bool mkm1 = mb & 1u, mk = mb & 2u, mkp1 = mb & 4u, mkp2 = mb & 8u;
+  float Rjp = (mkm1 && mk) ? fs(tkm1, tk) : 0.f;
+  float Rj = (mk && mkp1) ? fs(tk, tkp1) : 0.f;
+  float Rjm = (mkp1 && mkp2) ? fs(tkp1, tkp2) : 0.f;
+  float fbt = (mkp1 && mk) ? face_flux(mf, Rjm, Rj, Rjp, tkp1, tk, d0, d1, c) : 0.f;
+  float adiv = fm(datr, fs(fbt, ftp));
+  fz = fm(dtr, adiv);
+  ftp = fbt;
+  return fa(tk, fm(dtr, fa(adiv, fm(tk, wd))));
+}
+// flux of a face between cells B and C given A (upstream of B) and D (beyond C)
+// and their wet flags
+DEVI float h_flux(float tA, float tB, float tC, float tD, bool wA, bool wD, float mf, float d0, float d1, float c) {
+  float Rjp = wD ? fs(tD, tC) : 0.f;
+  float Rj = fs(tC, tB);
+  float Rjm = wA ? fs(tB, tA) : 0.f;
+  return face_flux(mf, Rjm, Rj, Rjp, tB, tC, d0, d1, c);
+}
+// x update of a cell: returns tracer_mdfl after x; fi the x increment
+DEVI float x_cell(float tz, float tk, float fw, float f, float coef, float div, float& fi) {
+  fi = fm(coef, fs(fw, f));
+  return fa(tz, fa(fi, fm(coef, fm(tk, div))));
+}
+// the total increment of a cell from its z + x part and the y fluxes either side
+DEVI float total_inc(float fzx, float coef, float fy_s, float fy_n) { return fa(fzx, fm(coef, fs(fy_s, fy_n))); }
+// state update increment (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT
+DEVI float update_inc(float uq, float tk, float ur, float dT) { return fa(fm(uq, tk), fm(ur, dT)); }
 
 
 
@@ -125,7 +191,6 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i0 = 1 + tile_x * TI, j0 = 1 + tile_y * TJ;
   const float dt = a.dtime;
-  const float sixth = 1.0f / 6.0f;
   // image offsets of this thread's tile positions (the same at every level)
   int offr[ROWS_PER_WARP];
 #pragma unroll
@@ -176,15 +241,8 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
                 (mask_at(g, a.mask2, pi, pj, kp1) ? 4 : 0) | (mask_at(g, a.mask2, pi, pj, kp2) ? 8 : 0);
         float wk = d2f(a.w[I3(g, i, j, k + 1)]);
         float wkm1 = k > 0 ? d2f(a.w[I3(g, i, j, k)]) : 0.0f;
-        float rr = 1.0f / d2f(a.rdz[I3(g, i, j, k)]);
         datr = d2f(a.datr[I2(g, i, j)]);
-        mf = d2f(a.dat[I2(g, i, j)]) * wk;
-        float cfl = fabsf(wk * dt * rr);
-        d0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
-        d1 = (1.0f - cfl * cfl) * sixth;
-        cc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
-        dtr = dt * rr;
-        wd = wkm1 - wk;
+        z_terms(wk, wkm1, d2f(a.rdz[I3(g, i, j, k)]), d2f(a.dat[I2(g, i, j)]), dt, mf, d0, d1, cc, dtr, wd);
       }
       s.zmask[c] = mbits;
       s.off[c] = in ? (int)I2(g, i, j) : -1;
@@ -197,15 +255,9 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
       s.zdatr[c] = datr;
       // x face between zi and zi+1 of row zj (needed for zi = 1..29)
       float xmf = 0.f, xd0 = 0.f, xd1 = 0.f, xc = 0.f;
-      if (in && zi >= 1 && zi <= ZW - 3) {
-        float u = d2f(a.uh[I3(g, i, j, k)]);
-        xmf = d2f(a.dyte[I2(g, i, j)]) * u;
-        float den = (d2f(a.rdz[I3(g, i, j, k)]) + d2f(a.rdz[I3(g, i + 1, j, k)])) * d2f(a.dxte[I2(g, i, j)]);
-        float cfl = fabsf(__fdividef(u * dt * 2.0f, den));
-        xd0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
-        xd1 = (1.0f - cfl * cfl) * sixth;
-        xc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
-      }
+      if (in && zi >= 1 && zi <= ZW - 3)
+        h_terms(d2f(a.uh[I3(g, i, j, k)]), d2f(a.dyte[I2(g, i, j)]), d2f(a.rdz[I3(g, i, j, k)]),
+                d2f(a.rdz[I3(g, i + 1, j, k)]), d2f(a.dxte[I2(g, i, j)]), dt, xmf, xd0, xd1, xc);
       s.xmf[c] = xmf;
       s.xd0[c] = xd0;
       s.xd1[c] = xd1;
@@ -215,24 +267,18 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
       bool xin = in && zi >= 2 && zi <= ZW - 3;
       if (xin) {
         bool wet = (mbits & 2) != 0;
-        coef = wet ? dt * datr / d2f(a.rdz[I3(g, i, j, k)]) : 0.0f;
-        div = d2f(a.dyte[I2(g, i, j)]) * d2f(a.uh[I3(g, i, j, k)]) -
-              d2f(a.dyte[I2(g, i - 1, j)]) * d2f(a.uh[I3(g, i - 1, j, k)]);
+        coef = x_coef(wet, dt, datr, d2f(a.rdz[I3(g, i, j, k)]));
+        div = x_div(d2f(a.dyte[I2(g, i, j)]), d2f(a.uh[I3(g, i, j, k)]), d2f(a.dyte[I2(g, i - 1, j)]),
+                    d2f(a.uh[I3(g, i - 1, j, k)]));
       }
       s.xcoef[c] = coef;
       s.xdiv[c] = div;
       s.xin[c] = xin;
       // y face between rows zj and zj+1 (needed for zj = 1..29, zi = 2..29)
       float ymf = 0.f, yd0 = 0.f, yd1 = 0.f, yc = 0.f;
-      if (in && zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3) {
-        float v = d2f(a.vh[I3(g, i, j, k)]);
-        ymf = d2f(a.dxtn[I2(g, i, j)]) * v;
-        float den = (d2f(a.rdz[I3(g, i, j, k)]) + d2f(a.rdz[I3(g, i, j + 1, k)])) * d2f(a.dytn[I2(g, i, j)]);
-        float cfl = fabsf(__fdividef(v * dt * 2.0f, den));
-        yd0 = (2.0f - cfl) * (1.0f - cfl) * sixth;
-        yd1 = (1.0f - cfl * cfl) * sixth;
-        yc = __fdividef(1.0f - cfl, 1.0e-30f + cfl);
-      }
+      if (in && zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3)
+        h_terms(d2f(a.vh[I3(g, i, j, k)]), d2f(a.dxtn[I2(g, i, j)]), d2f(a.rdz[I3(g, i, j, k)]),
+                d2f(a.rdz[I3(g, i, j + 1, k)]), d2f(a.dytn[I2(g, i, j)]), dt, ymf, yd0, yd1, yc);
       s.ymf[c] = ymf;
       s.yd0[c] = yd0;
       s.yd1[c] = yd1;
@@ -292,16 +338,8 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
             tkp1 = d2f(T[(long)kp1 * g.n2 + o]);
             tkp2 = d2f(T[(long)kp2 * g.n2 + o]);
           }
-          bool mkm1 = mb & 1, mk = mb & 2, mkp1 = mb & 4, mkp2 = mb & 8;
-          float Rjp = (mkm1 && mk) ? tkm1 - tk : 0.f;
-          float Rj = (mk && mkp1) ? tk - tkp1 : 0.f;
-          float Rjm = (mkp1 && mkp2) ? tkp1 - tkp2 : 0.f;
-          float fbt = (mkp1 && mk) ? face_flux(s.zmf[c], Rjm, Rj, Rjp, tkp1, tk, s.zd0[c], s.zd1[c], s.zc[c]) : 0.f;
-          float dtr = s.zdtr[c];
-          float adiv = s.zdatr[c] * (fbt - ftp[n][m]);
-          fzv = dtr * adiv;
-          tzv = tk + dtr * (adiv + tk * s.zwd[c]);
-          ftp[n][m] = fbt;
+          tzv = z_cell(tkm1, tk, tkp1, tkp2, mb, s.zmf[c], s.zd0[c], s.zd1[c], s.zc[c], s.zdatr[c], s.zdtr[c],
+                       s.zwd[c], ftp[n][m], fzv);
         }
         // ---- x fluxes: face zi (between zi and zi+1), zi = 1..29 ----
         const unsigned full = 0xffffffffu;
@@ -311,20 +349,12 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
         unsigned wA = __shfl_up_sync(full, wet, 1), wC = __shfl_down_sync(full, wet, 1);
         unsigned wD = __shfl_down_sync(full, wet, 2);
         float f = 0.f;
-        if (zi >= 1 && zi <= ZW - 3 && wet && wC) {
-          float Rjp = wD ? tD - tC : 0.f;
-          float Rj = tC - tzv;
-          float Rjm = wA ? tzv - tA : 0.f;
-          f = face_flux(s.xmf[c], Rjm, Rj, Rjp, tzv, tC, s.xd0[c], s.xd1[c], s.xc[c]);
-        }
+        if (zi >= 1 && zi <= ZW - 3 && wet && wC)
+          f = h_flux(tA, tzv, tC, tD, wA, wD, s.xmf[c], s.xd0[c], s.xd1[c], s.xc[c]);
         // ---- x update: cells zi = 2..29 ----
         float fw = __shfl_up_sync(full, f, 1);
         float t = 0.f, fi = 0.f;
-        if (s.xin[c]) {
-          float coef = s.xcoef[c];
-          fi = coef * (fw - f);
-          t = tzv + (fi + coef * (tk * s.xdiv[c]));
-        }
+        if (s.xin[c]) t = x_cell(tzv, tk, fw, f, s.xcoef[c], s.xdiv[c], fi);
         s.tx[c] = t;
         tkr[m] = tk;
         fzr[m] = fzv;
@@ -338,13 +368,9 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
         float f = 0.f;
         if (zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= ZW - 3) {
           bool m0 = s.zmask[c - ZW] & 2, m1 = s.zmask[c] & 2, m2 = s.zmask[c + ZW] & 2, m3 = s.zmask[c + 2 * ZW] & 2;
-          if (m1 && m2) {
-            float tA = s.tx[c - ZW], tB = s.tx[c], tC = s.tx[c + ZW], tD = s.tx[c + 2 * ZW];
-            float Rjp = (m3 && m2) ? tD - tC : 0.f;
-            float Rj = tC - tB;
-            float Rjm = (m1 && m0) ? tB - tA : 0.f;
-            f = face_flux(s.ymf[c], Rjm, Rj, Rjp, tB, tC, s.yd0[c], s.yd1[c], s.yc[c]);
-          }
+          if (m1 && m2)
+            f = h_flux(s.tx[c - ZW], s.tx[c], s.tx[c + ZW], s.tx[c + 2 * ZW], m1 && m0, m3 && m2, s.ymf[c], s.yd0[c],
+                       s.yd1[c], s.yc[c]);
         }
         s.fy[c] = f;
       }
@@ -358,12 +384,11 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
         if (i > g.ni || j > g.nj) continue;
         bool wet = s.zmask[c] & 2;
         if (!wet && !a.fused) continue;
-        float fy = s.xcoef[c] * (s.fy[c - ZW] - s.fy[c]);
-        float dT = fzr[m] + fir[m] + fy;
+        float dT = total_inc(fa(fzr[m], fir[m]), s.xcoef[c], s.fy[c - ZW], s.fy[c]);
         long p = I3(g, i, j, k);
         if (a.fused) {
           // T(taup1) = T + (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT
-          float inc = s.uq[c] * tkr[m] + s.ur[c] * dT;
+          float inc = update_inc(s.uq[c], tkr[m], s.ur[c], dT);
           double tn = (PF ? pf->tb[n & 1][1][c] : T[p]) + f2d(inc);
           double* o = a.out + (long)(n0 + n) * g.n3;
           o[p] = tn;
@@ -375,7 +400,7 @@ DEVI void mixed_tile(const MixArgs& a, int n0, int tile_x, int tile_y, SmemT<ZR>
           if (hi >= 0 && hj >= 0) o[I3(g, hi, hj, k)] = tn;
         } else if (wet) {
           double* o = a.out + (long)n * g.n3;
-          o[p] = o[p] + f2d(s.ur[c] * dT);
+          o[p] = o[p] + f2d(fm(s.ur[c], dT));
         }
       }
       // the next tracer writes tx only after this tracer's y fluxes were read

@@ -172,7 +172,7 @@ def split(dom, layout: Layout) -> List:
         f = {k: v[(Ellipsis,) + sl].contiguous().clone() for k, v in dom.f.items()}
         spec = replace(s, ni=ie - is_ + 1, nj=je - js + 1, cyclic_x=False, cyclic_y=False)
         b = Domain(spec, f, dom.dzt, dom.zw)
-        b.mask2 = np.ascontiguousarray(m2[:, js - 1:je + 3, is_ - 1:ie + 3])
+        b.mask2 = np.ascontiguousarray(m2[:, js - 1:je + 4, is_ - 1:ie + 4])
         b.extent = (is_, ie, js, je)
         out.append(b)
     return out

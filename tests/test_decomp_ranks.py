@@ -47,6 +47,28 @@ def test_neighbours_wrap_only_in_periodic_directions():
     assert one.neighbour(1, decomp.WEST) == 1  # its own neighbour across the periodic direction
 
 
+def test_split_cuts_every_array_to_the_block():
+    """Blocks carry their data domain of every array (halo from the neighbours or
+    the domain's own halo) and tmask_mdfl with the two-cell halo; join puts the
+    compute cells back."""
+    from mom5_gb300 import grid
+    sp = grid.DomainSpec(ni=23, nj=17, nk=4, lon0=0.0, lon1=23.0, lat0=-20.0, lat1=20.0, cyclic_x=True,
+                         continent=(6, 5, 4, 3), ntracers=2, seed=8)
+    dom = grid.make_domain(sp)
+    L = decomp.Layout(23, 17, 3, 2, True, False)
+    blocks = decomp.split(dom, L)
+    m2 = decomp.mask_halo2(dom["tmask"].numpy(), True, False)
+    for r, b in enumerate(blocks):
+        s = b.spec
+        is_, ie, js, je = L.extent(r)
+        assert (s.ni, s.nj, s.cyclic_x) == (ie - is_ + 1, je - js + 1, False)
+        assert b.mask2.shape == (sp.nk, s.nj + 4, s.ni + 4)
+        assert np.array_equal(b.mask2, m2[:, js - 1:je + 4, is_ - 1:ie + 4])
+        assert np.array_equal(b["T"].numpy(), dom["T"].numpy()[..., js - 1:je + 2, is_ - 1:ie + 2])
+    T = decomp.join([b["T"].numpy() for b in blocks], L)
+    assert np.array_equal(T, dom["T"].numpy())
+
+
 def _global(ni, nj, nlev, seed):
     rng = np.random.default_rng(seed)
     g = np.zeros((nlev, nj + 2, ni + 2))
