@@ -511,7 +511,11 @@ def run_ours(args, rank, world):
 
     state = {"tau": 1}
     # trial steps 1 -> 2; the timed steps start at level 1
-    tune = d.autotune(wl.dtts) if ntr > 0 and not args.no_autotune else None
+    if args.tuning:
+        d.tuning = tuple(int(x) for x in args.tuning.split(","))
+        tune = f"pinned {args.tuning}"
+    else:
+        tune = d.autotune(wl.dtts) if ntr > 0 and not args.no_autotune else None
     if world > 1:
         torch.distributed.barrier()
     r = _time_domain(d, stream, wl, ntr, args.steps, args.warmup, state, local)
@@ -850,6 +854,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
+    ap.add_argument("--tuning", default=None,
+                    help="pin the launch shape ROWS,PREFETCH,TJ (mom5gpu_set_tuning) instead of autotuning")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the precision, batched and serving forms reported beside the FP64 headline")
     args = ap.parse_args()
