@@ -309,7 +309,9 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
  * (16, 24, 32 or 64 rows incl. halo); staging of the tile's operands: prefetch
  * 0 = plain loads, 1 = tracer levels prefetched by cp.async (height 16 only),
  * 2 = tiles staged by TMA with the tracer levels carried down the column in
- * registers (heights 16 and 24; domains of even ni, else the plain kernel);
+ * registers (heights 16 and 24; domains of even ni, else the plain kernel),
+ * 3 = the same with at most 5 tracers per block and two blocks per SM
+ * (height 16);
  * FP64 y-pass rows per thread (0 = built-in choice, 2, 4, 8, 16).  Every shape
  * gives the same results bit for bit.  A TMA-staged launch whose bounded wait
  * gave up is reported by the next mom5gpu_synchronize as MOM5GPU_ETIMEDOUT. */

@@ -870,11 +870,12 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
 
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj) {
   if (!d) return MOM5GPU_EINVAL;
-  if ((rows != 16 && rows != 24 && rows != 32 && rows != 64) || prefetch < 0 || prefetch > 2 ||
-      (prefetch == 1 && rows != 16) || (prefetch == 2 && rows != 16 && rows != 24) ||
+  if ((rows != 16 && rows != 24 && rows != 32 && rows != 64) || prefetch < 0 || prefetch > 3 ||
+      (prefetch == 1 && rows != 16) || (prefetch == 2 && rows != 16 && rows != 24) || (prefetch == 3 && rows != 16) ||
       !(tj == 0 || tj == 2 || tj == 4 || tj == 8 || tj == 16))
     return fail(d, MOM5GPU_EINVAL,
-                "set_tuning: rows 16|24|32|64, prefetch 0, 1 (cp.async, rows 16) or 2 (TMA, rows 16|24), "
+                "set_tuning: rows 16|24|32|64, prefetch 0, 1 (cp.async, rows 16), 2 (TMA, rows 16|24) or 3 "
+                "(TMA, 5 tracers per block, rows 16), "
                 "tj 0|2|4|8|16");
   d->tune_mixed_rows = rows;
   d->tune_mixed_pf = prefetch;
@@ -895,10 +896,10 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   if (!d->advect_ready) return fail(d, MOM5GPU_ESTATE, "autotune before mom5gpu_tracer_advect_init");
   bool mixed = d->opt.precision == MOM5GPU_PRECISION_MIXED;
   // candidate launch shapes: precision-form tile height (and tracer prefetch); FP64 y-pass rows per thread
-  const int kRows[] = {32, 64, 24, 16, 16, 16, 24};
-  const int kPf[] = {0, 0, 0, 0, 1, 2, 2};
+  const int kRows[] = {32, 64, 24, 16, 16, 16, 24, 16};
+  const int kPf[] = {0, 0, 0, 0, 1, 2, 2, 3};
   const int kTj[] = {2, 4, 8, 16};
-  int ncand = mixed ? (d->geo.ni % 2 == 0 ? 7 : 5) : 4;
+  int ncand = mixed ? (d->geo.ni % 2 == 0 ? 8 : 5) : 4;
   cudaEvent_t t0, t1;
   if (cudaEventCreate(&t0) != cudaSuccess) return fail(d, MOM5GPU_ECUDA, "autotune events");
   if (cudaEventCreate(&t1) != cudaSuccess) {
@@ -930,7 +931,7 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
     ms /= 3.f;
     char line[96];
     if (mixed)
-      snprintf(line, sizeof(line), "rows=%d%s: %.3f ms; ", kRows[c], kPf[c] == 2 ? "+tma" : kPf[c] ? "+prefetch" : "",
+      snprintf(line, sizeof(line), "rows=%d%s: %.3f ms; ", kRows[c], kPf[c] == 3 ? "+tma5" : kPf[c] == 2 ? "+tma" : kPf[c] ? "+prefetch" : "",
                ms);
     else snprintf(line, sizeof(line), "tj=%d: %.3f ms; ", kTj[c], ms);
     rep += line;
@@ -951,7 +952,7 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
   char line[64];
   if (mixed)
     snprintf(line, sizeof(line), "chosen rows=%d%s", kRows[bestc],
-             kPf[bestc] == 2 ? "+tma" : kPf[bestc] ? "+prefetch" : "");
+             kPf[bestc] == 3 ? "+tma5" : kPf[bestc] == 2 ? "+tma" : kPf[bestc] ? "+prefetch" : "");
   else snprintf(line, sizeof(line), "chosen tj=%d", kTj[bestc]);
   rep += line;
   if (report && report_len) {

@@ -160,7 +160,7 @@ int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int ta
     }
     if (!a.T || !a.out) return fail(d, MOM5GPU_ENOMEM, "precision form: tracer storage");
     int n0 = fused_update ? n_first - 1 + c0 : 0;
-    if (d->tune_mixed_pf == 2) {
+    if (d->tune_mixed_pf >= 2) {
       rc = launch_mixed_tma(d, a, n0, fptr(d, MOM5GPU_TRACER, 1, taum1), n_first - 1 + c0,
                             d->dims.num_prog_tracers);
       if (rc != MOM5GPU_EUNSUPPORTED) continue;

@@ -33,7 +33,8 @@
 // block stops at its next barrier (after waiting, again bounded, for the
 // copies it issued) and mom5gpu_synchronize reports MOM5GPU_ETIMEDOUT.
 // Tile heights 16 and 24 (the per-tracer intermediates of 10 tracers at 32 rows
-// would not fit in shared memory).
+// would not fit in shared memory); at height 16 also with at most 5 tracers per
+// block and two blocks per SM.
 #include <cuda.h>
 #include <math.h>
 
@@ -101,8 +102,8 @@ struct TmaSmem {
 // One level is three phases with a block barrier between them: (1) the level's
 // face terms, (2) the z and x passes of every tracer, (3) the y fluxes of every
 // tracer, then the outputs -- three barriers per level whatever the tracer count.
-template <int NC, int ZR>
-__global__ void __launch_bounds__(32 * ZR, 1)
+template <int NC, int ZR, int MINB>
+__global__ void __launch_bounds__(32 * ZR, MINB)
     k_mdfl_mixed_tma(MixArgs a, int n0, int zt0, const __grid_constant__ TmaMaps maps, int* err) {
   using S = TmaSmem<NC, ZR>;
   constexpr int SLOT = S::SLOT;
@@ -370,13 +371,13 @@ bool encode(CUtensorMap* m, const double* base, const Geo& g, long nz, int rows)
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NC, int ZR>
+template <int NC, int ZR, int MINB>
 int run_tma_zr(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
   const Geo& g = d->geo;
   constexpr size_t smem = sizeof(TmaSmem<NC, ZR>);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_mdfl_mixed_tma<NC, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_mdfl_mixed_tma<NC, ZR, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return cuda_fail(d, e, "TMA precision kernel attribute");
     configured = true;
@@ -389,15 +390,32 @@ int run_tma_zr(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, 
   if (!ok) return fail(d, MOM5GPU_ECUDA, "TMA precision kernel: tensor-map encoding failed");
   constexpr int TJ = ZR - 4;
   dim3 grid((g.ni + TI - 1) / TI, (g.nj + TJ - 1) / TJ);
-  k_mdfl_mixed_tma<NC, ZR><<<grid, 32 * ZR, smem, d->stream>>>(a, n0, zt0, maps, d->tma_err);
+  k_mdfl_mixed_tma<NC, ZR, MINB><<<grid, 32 * ZR, smem, d->stream>>>(a, n0, zt0, maps, d->tma_err);
   count_launches(d, 1);
   return MOM5GPU_OK;
 }
 
 template <int NC>
 int run_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
-  if (d->tune_mixed_rows == 24) return run_tma_zr<NC, 24>(d, a, n0, Tall, zt0, ntr_all);
-  return run_tma_zr<NC, 16>(d, a, n0, Tall, zt0, ntr_all);
+  if (d->tune_mixed_rows == 24) return run_tma_zr<NC, 24, 1>(d, a, n0, Tall, zt0, ntr_all);
+  return run_tma_zr<NC, 16, 1>(d, a, n0, Tall, zt0, ntr_all);
+}
+
+// Two resident blocks per SM (16-row tiles, at most 5 tracers per block, 64
+// registers): the tracers of the launch go in sub-launches of up to 5, each
+// recomputing the level's face terms.
+int run_tma_pairs(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
+  for (int q = 0; q < a.ntr; q += 5) {
+    MixArgs b = a;
+    b.ntr = a.ntr - q < 5 ? a.ntr - q : 5;
+    b.T = a.T + (long)q * a.g.n3;
+    if (!a.fused) b.out = a.out + (long)q * a.g.n3;
+    const int m0 = a.fused ? n0 + q : 0;
+    int rc = b.ntr <= 2 ? run_tma_zr<2, 16, 2>(d, b, m0, Tall, zt0 + q, ntr_all)
+                        : run_tma_zr<5, 16, 2>(d, b, m0, Tall, zt0 + q, ntr_all);
+    if (rc) return rc;
+  }
+  return MOM5GPU_OK;
 }
 
 }  // namespace
@@ -414,6 +432,7 @@ int launch_mixed_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* 
     if (e == cudaSuccess) e = cudaMemset(d->tma_err, 0, sizeof(int));
     if (e != cudaSuccess) return cuda_fail(d, e, "TMA precision kernel: error word");
   }
+  if (d->tune_mixed_pf == 3) return run_tma_pairs(d, a, n0, Tall, zt0, ntr_all);
   if (a.ntr <= 1) return run_tma<1>(d, a, n0, Tall, zt0, ntr_all);
   if (a.ntr <= 2) return run_tma<2>(d, a, n0, Tall, zt0, ntr_all);
   if (a.ntr <= 4) return run_tma<4>(d, a, n0, Tall, zt0, ntr_all);

@@ -132,8 +132,9 @@ def test_mixed_multi_tile_and_partial_tiles(gpu_lib, case):
 def test_precision_form_launch_shapes_agree(gpu_lib, case):
     """Every launch shape of the precision form (tile height 32, 64, 24, 16, 16 with the
     tracer prefetch through cp.async, and heights 16 and 24 staged by TMA with the
-    tracer levels carried in registers) gives the same tracers bit for bit; an odd ni
-    takes the plain kernel for the TMA shapes."""
+    tracer levels carried in registers, height 16 also with at most 5 tracers per
+    block) gives the same tracers bit for bit; an odd ni takes the plain kernel for
+    the TMA shapes."""
     capi = gpu_lib
     from mom5_gb300 import harness
     cx, cy, ni, nj, ntr = case
@@ -141,7 +142,7 @@ def test_precision_form_launch_shapes_agree(gpu_lib, case):
                          cyclic_y=cy, continent=(10, 8, 5, 6), wavelength_cells=6.0, ntracers=ntr, seed=ni + 1)
     dom = grid.make_domain(sp)
     out = {}
-    for shape in ((32, 0, 0), (64, 0, 0), (24, 0, 0), (16, 0, 0), (16, 1, 0), (16, 2, 0), (24, 2, 0)):
+    for shape in ((32, 0, 0), (64, 0, 0), (24, 0, 0), (16, 0, 0), (16, 1, 0), (16, 2, 0), (24, 2, 0), (16, 3, 0)):
         d = harness.load(dom, options=capi.default_options(precision=capi.PRECISION_MIXED))
         d.tuning = shape
         assert d.tuning == shape
