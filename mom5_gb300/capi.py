@@ -125,6 +125,7 @@ def lib() -> C.CDLL:
             "mom5gpu_set_psom_limit": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_set_itt0": (C.c_int, [vp, C.c_long]),
             "mom5gpu_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+            "mom5gpu_set_barotropic_fusion": (C.c_int, [vp, C.c_int]),
             "mom5gpu_get_tuning": (C.c_int, [vp, ip, ip, ip]),
             "mom5gpu_copy_field_async": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
             "mom5gpu_set_tracer_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p]),
@@ -321,6 +322,10 @@ class Domain:
     def tuning(self, v):
         rows, prefetch, tj = v
         self.check(lib().mom5gpu_set_tuning(self.h, rows, int(prefetch), tj))
+
+    def set_barotropic_fusion(self, mode: int):
+        """1: one launch per exact B-grid subcycle; 0: three; -1: by domain size."""
+        self.check(lib().mom5gpu_set_barotropic_fusion(self.h, int(mode)))
 
     def set_itt0(self, itt0):
         self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))

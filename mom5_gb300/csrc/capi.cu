@@ -868,6 +868,19 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
   return launch_update_tracer(d, 1, ntr, taum1, taup1, dtime);
 }
 
+int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (mode < -1 || mode > 1) return fail(d, MOM5GPU_EINVAL, "set_barotropic_fusion: mode -1, 0 or 1");
+  if (mode != d->bt_fused) {
+    // the cached subcycle graphs hold the other form (their key is the kernel arguments)
+    for (auto& gr : d->bt_graphs)
+      if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    d->bt_graphs.clear();
+  }
+  d->bt_fused = mode;
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj) {
   if (!d) return MOM5GPU_EINVAL;
   if ((rows != 16 && rows != 24 && rows != 32 && rows != 64) || prefetch < 0 || prefetch > 3 ||

@@ -633,6 +633,126 @@ DEVI void bt_corr_body(BtArgs a, int so, int sn, double wgt, int bx, int by) {
   }
 }
 
+// One whole B-grid subcycle -- predictor, momentum, corrector -- in one launch
+// on a tile of TX x TY data-domain points: the predictor's surface pressure on
+// the tile and a ring of one (west and south one wider, east and north the
+// +1 the pressure gradient reads) and the momentum on the tile and its west and
+// south ring are recomputed by each tile that needs them, in shared memory, so
+// the corrector of the tile needs nothing from another block in this launch.
+// Every point's arithmetic is that of bt_pred_body, bt_mom_b_body and
+// bt_corr_body, in the same order, so the results are the same bits.  The
+// divergence the predictor reuses comes from plane `so` of a.dvs and the
+// corrector writes plane `sn` (two planes: a neighbouring tile may still be
+// reading the previous one).  For domains where three launches per subcycle
+// cost more than the ring recompute.
+template <int TX, int TY>
+DEVI void bt_fused_body(BtArgs a, int so, int sn, int reuse, double wgt, int bx, int by) {
+  constexpr int PX = TX + 2, PY = TY + 2;  // pressure: points x0-1 .. x0+TX, y0-1 .. y0+TY
+  constexpr int MX = TX + 1, MY = TY + 1;  // momentum: points x0-1 .. x0+TX-1, y0-1 .. y0+TY-1
+  __shared__ double ps_s[PY * PX];
+  __shared__ double un_s[MY * MX], vn_s[MY * MX], uh_s[MY * MX], vh_s[MY * MX];
+  const Geo& g = a.g;
+  const long n2 = g.n2;
+  const int x0 = bx * TX, y0 = by * TY;
+  const double* dvs_o = a.dvs + (long)so * n2;
+  // ---- predictor and surface pressure (bt_pred_body) ----
+  for (int e = threadIdx.x; e < PX * PY; e += blockDim.x) {
+    const int i0 = x0 - 1 + e % PX, j0 = y0 - 1 + e / PX;
+    if (i0 < 0 || i0 > g.ni + 1 || j0 < 0 || j0 > g.nj + 1) continue;
+    int i = i0, j = j0;
+    if (!halo_image(g, i, j)) {
+      i = i0;
+      j = j0;
+    }
+    const double* eo = a.eta_bt + so * n2;
+    const long q = I2(g, i, j);
+    double en;
+    if (dpos(a.gamma)) {
+      double dv = reuse ? dvs_o[q] : div_ud_bh(a, a.uhb + so * n2, a.vhb + so * n2, i, j);
+      double tm = a.tmask1[q];
+      double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
+      en = eo[q] + a.dtbt_gamma_rho0r * (tmp + a.steady[q]);
+    } else {
+      en = eo[q];
+    }
+    const long q0 = I2(g, i0, j0);
+    ps_s[e] = a.rho_g[q0] * en + a.patm[q0];
+  }
+  __syncthreads();
+  // ---- momentum (bt_mom_b_body) ----
+  for (int e = threadIdx.x; e < MX * MY; e += blockDim.x) {
+    const int li = e % MX, lj = e / MX;
+    const int i = x0 - 1 + li, j = y0 - 1 + lj;
+    if (i < 0 || i > g.ni + 1 || j < 0 || j > g.nj + 1) continue;
+    const long q = I2(g, i, j);
+    double gx = 0.0, gy = 0.0;
+    if (i <= g.ni && j <= g.nj) {
+      double um = a.umask1[q];
+      if (!is_zero(um)) {
+        const int pe = lj * PX + li;  // pressure point (i, j)
+        double p00 = ps_s[pe], p10 = ps_s[pe + 1], p01 = ps_s[pe + PX], p11 = ps_s[pe + PX + 1];
+        double p_fay = half_exact(p00 + p01);
+        double p_fax = half_exact(p00 + p10);
+        double pip_fay = half_exact(p10 + p11);
+        double pjp_fax = half_exact(p01 + p11);
+        gx = mask_mul((pip_fay - p_fay) * a.dxur[q], um);
+        gy = mask_mul((pjp_fax - p_fax) * a.dyur[q], um);
+      }
+    }
+    double pf1 = -a.thicku[q] * gx;
+    double pf2 = -a.thicku[q] * gy;
+    double uo = a.ubt[so * n2 + q], vo = a.vbt[so * n2 + q];
+    double hf = half_exact(a.f[q]);
+    double t1 = uo + a.dtbt * plus_zero(hf * vo + pf1 + a.forcing_u[q]);
+    double t2 = vo + a.dtbt * plus_zero((-hf) * uo + pf2 + a.forcing_v[q]);
+    double un = a.cori2[q] * (t1 + a.cori1[q] * t2);
+    double vn = a.cori2[q] * (t2 - a.cori1[q] * t1);
+    double uh = un * a.dyu[q], vh = vn * a.dxu[q];
+    un_s[e] = un;
+    vn_s[e] = vn;
+    uh_s[e] = uh;
+    vh_s[e] = vh;
+    if (li >= 1 && lj >= 1) {  // the tile's own points: the state the next subcycle reads
+      a.ubt[sn * n2 + q] = un;
+      a.vbt[sn * n2 + q] = vn;
+      a.uhb[sn * n2 + q] = uh;
+      a.vhb[sn * n2 + q] = vh;
+    }
+  }
+  __syncthreads();
+  // ---- corrector and accumulation (bt_corr_body) ----
+  double* dvs_n = a.dvs + (long)sn * n2;
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    const int li = e % TX + 1, lj = e / TX + 1;  // in the momentum arrays
+    const int i = x0 - 1 + li, j = y0 - 1 + lj;
+    if (i > g.ni + 1 || j > g.nj + 1) continue;
+    const long q = I2(g, i, j);
+    const int m = lj * MX + li, mw = m - 1, ms = m - MX, msw = ms - 1;
+    double dv = 0.0;
+    if (i >= 1 && j >= 1) {  // div_ud_bh
+      double uh_bay = half_exact(uh_s[m] + uh_s[ms]);
+      double vh_bax = half_exact(vh_s[m] + vh_s[mw]);
+      double uhim_bay = half_exact(uh_s[mw] + uh_s[msw]);
+      double vhjm_bax = half_exact(vh_s[ms] + vh_s[msw]);
+      dv = ((uh_bay - uhim_bay) + (vh_bax - vhjm_bax)) * a.datr[q];
+    }
+    dvs_n[q] = dv;
+    double tm = a.tmask1[q];
+    double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
+    double en = a.eta_bt[so * n2 + q] + a.dtbt_rho0r * (tmp + a.steady[q]);
+    a.eta_bt[sn * n2 + q] = en;
+    a.eta_bar[q] = a.eta_bar[q] + en;
+    double un = un_s[m], vn = vn_s[m];
+    if (a.stepB) {
+      a.udrho_u[q] = a.udrho_u[q] + wgt * un;
+      a.udrho_v[q] = a.udrho_v[q] + wgt * vn;
+    } else {
+      a.udrho_u[q] = a.udrho_u[q] + un;
+      a.udrho_v[q] = a.udrho_v[q] + vn;
+    }
+  }
+}
+
 DEVI void bt_post2_body(BtArgs a, double* conv, double* eta_u, double* ps_out, int bx, int by) {
   const Geo& g = a.g;
   int i = bx * blockDim.x + threadIdx.x;

@@ -110,6 +110,7 @@ struct mom5gpu_domain {
   int tune_mixed_pf = 0;     // precision form: 1 tracer levels prefetched by cp.async (height 16), 2 TMA-staged tiles
   int* tma_err = nullptr;    // set by the TMA-staged kernel when a bounded wait gave up
   int tune_y_tj = 0;         // FP64 y-pass rows per thread
+  int bt_fused = -1;         // exact B-grid subcycle in one launch: 1 yes, 0 three launches, -1 by domain size
   // CUDA graphs of the barotropic subcycle loop, one per set of kernel arguments
   // (the bytes of the BtArgs it was captured with: time levels rotate), at most
   // kBtGraphs, the oldest replaced first
@@ -196,8 +197,9 @@ struct BtArgs {
   double* btf;        // precision form, B grid: folded step coefficients (bt_fast_body.cuh), else nullptr
   double* dvs;        // divergence of the corrector's transports, reused by the next subcycle's predictor
 };
-// planes of barotropic scratch: 17 for the exact path, 9 more for the precision form
-constexpr int kBtPlanes = 17, kBtFastPlanes = 9;
+// planes of barotropic scratch: 18 for the exact path (the reused divergence in
+// two planes for the one-launch subcycle), 9 more for the precision form
+constexpr int kBtPlanes = 18, kBtFastPlanes = 9;
 struct BtExtra {
   const double *eta_bar_tau, *eta_tau, *ud_tau, *vd_tau, *pme, *river, *source, *eta_smooth;
   double *conv, *eta_u, *ps_out, *gxo, *gyo;

@@ -1260,6 +1260,20 @@ __global__ void k_bt_pred(BtArgs a, int so, int sn, int reuse) { bt_pred_body(a,
 __global__ void k_bt_mom_b(BtArgs a, int so, int sn) { bt_mom_b_body(a, so, sn, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_mom_c(BtArgs a, int so, int sn, int itime) { bt_mom_c_body(a, so, sn, itime, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) { bt_corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y); }
+constexpr int kFusedTX = 64, kFusedTY = 8;
+__global__ void __launch_bounds__(256) k_bt_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
+  bt_fused_body<kFusedTX, kFusedTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
+}
+// The one-launch subcycle pays a recomputed ring (about 10% more FP64 work) to
+// save two launches and the round trips of the pressure and transports: it wins
+// where launches, not the FP64 pipe, set the time -- domains of up to about half
+// a million columns.
+constexpr long kFusedMaxColumns = 1L << 19;
+static bool use_fused(const mom5gpu_domain* d, const BtArgs& a) {
+  if (a.cgrid || a.btf) return false;
+  if (d->bt_fused >= 0) return d->bt_fused == 1;
+  return a.g.n2 <= kFusedMaxColumns;
+}
 __global__ void k_bt_post2(BtArgs a, double* conv, double* eta_u, double* ps_out) { bt_post2_body(a, conv, eta_u, ps_out, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_post3(BtArgs a, const double* ps, double* gxo, double* gyo) { bt_post3_body(a, ps, gxo, gyo, blockIdx.x, blockIdx.y); }
 
@@ -1397,8 +1411,9 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   cudaStream_t s = d->stream;
   ClockScope clk(d, SEC_BAROTROPIC);
   int halo = (g.cx || g.cy) ? 1 : 0;
-  count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) + (long)a.nts * (3 + (a.cgrid ? 2 * halo : 0)) + 4 +
-                       5 * halo);
+  const bool fused = use_fused(d, a);
+  count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) +
+                        (long)a.nts * (fused ? 1 : 3 + (a.cgrid ? 2 * halo : 0)) + 4 + 5 * halo);
   k_bt_init<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, src,
                                                           esm, d->opt.initsum_with_bar);
   dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
@@ -1410,11 +1425,16 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   if (a.btf) launch_btf_prep(a, s);
   // the nts subcycles (3 to 5 launches each, all arguments in a): one CUDA graph,
   // captured on first use and replayed while a is unchanged
+  const dim3 gf((g.ni + 2 + kFusedTX - 1) / kFusedTX, (g.nj + 2 + kFusedTY - 1) / kFusedTY);
   auto subcycles = [&](cudaStream_t st) {
     for (int itime = 1; itime <= a.nts; ++itime) {
       int so = (itime + 0) % 2, sn = (itime + 1) % 2;
       if (a.btf) {  // precision form: FP32 increments
         launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), itime > 1, st);
+        continue;
+      }
+      if (fused) {  // predictor, momentum and corrector in one launch
+        k_bt_fused<<<gf, 256, 0, st>>>(a, so, sn, itime > 1, (double)(a.nts - itime + 1));
         continue;
       }
       k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, itime > 1);

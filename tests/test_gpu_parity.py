@@ -471,6 +471,45 @@ def test_barotropic_matches(env, cyclic_x, stepping_B, cgrid):
     assert np.abs(out["eta_t_bar"]).max() > 0 and np.abs(out["udrho_u"]).max() > 0
 
 
+@pytest.mark.parametrize("fusion", [0, 1])
+@pytest.mark.parametrize("cyclic_x,cyclic_y,stepping_B", [(True, False, True), (False, False, False),
+                                                         (True, True, True)])
+def test_barotropic_subcycle_forms_match(env, fusion, cyclic_x, cyclic_y, stepping_B):
+    """The exact B-grid subcycle as three launches or as one launch per subcycle
+    (ring of pressure and transports recomputed per tile), on a domain of several
+    tiles with partial ones: every output equal to the restatement over three
+    baroclinic steps, also when the form changes between steps."""
+    capi, O = env
+    sp = grid.DomainSpec(ni=150, nj=29, nk=1, lon0=0.0, lon1=150.0, lat0=-55.0, lat1=55.0, cyclic_x=cyclic_x,
+                         cyclic_y=cyclic_y, hmin=None, ridge_amp=1200.0, ntracers=0, seed=71,
+                         continent=None if cyclic_y else (40, 8, 9, 6))
+    from mom5_gb300 import harness
+    dom = grid.make_domain(sp)
+    opts = capi.default_options(barotropic_time_stepping_A=int(not stepping_B),
+                                barotropic_time_stepping_B=int(stepping_B))
+    d = harness.load(dom, options=opts)
+    nts = d.barotropic_init(dtuv=300.0, dtbt=30.0)
+    g = O.domain_arrays(dom)
+    dims = O.dims(sp)
+    st = _baro_state(dom)
+    tau = 1
+    for step, mode in enumerate((fusion, fusion, 1 - fusion)):
+        d.set_barotropic_fusion(mode)
+        taup1 = 3 - tau
+        d.update_ocean_barotropic(tau, taup1)
+        out = O.update_ocean_barotropic(dims, g, st, nts, 30.0, time_stepping_B=stepping_B)
+        for k, fid in (("eta_t_bar", capi.F.ETA_T_BAR), ("udrho_u", capi.F.UDRHO_U), ("udrho_v", capi.F.UDRHO_V),
+                       ("conv_rho_ud_t", capi.F.CONV_RHO_UD_T), ("eta_u", capi.F.ETA_U)):
+            got = d.get(fid, level=taup1)
+            assert equal(got, out[k]), f"step {step} form {mode} {k}: {diff_report(got, out[k])}"
+        st = {"eta_t": st["eta_t"], "eta_t_bar": out["eta_t_bar"], "udrho_u": out["udrho_u"],
+              "udrho_v": out["udrho_v"]}
+        d.set(capi.F.ETA_T, np.ascontiguousarray(st["eta_t"]), level=taup1)
+        tau = taup1
+    with pytest.raises(capi.Mom5GpuError):
+        d.set_barotropic_fusion(2)
+
+
 def test_barotropic_graph_follows_arguments(env):
     """The subcycle loop is replayed from a CUDA graph keyed by its kernel
     arguments: repeated level pairs replay, a new dtbt (new nts and step
