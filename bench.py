@@ -92,9 +92,13 @@ def adv_bytes(ni, nj, nk, ntr):
     return 8 * ni * nj * nk * (2 * ntr + 5) + 8 * ni * nj * 7
 
 
-# DRAM bytes per tracer-cell of the advection launch set, from an ncu capture of the
-# 360x270x50 block: FP64 4.740 GB, precision form 0.975 GB for 360*270*50*10 tracer-cells.
-TRAFFIC_PER_TRACER_CELL = {"fp64": 4.740e9 / (360 * 270 * 50 * 10), "mixed": 0.975e9 / (360 * 270 * 50 * 10)}
+# DRAM bytes per tracer-cell of the advection launch set from ncu captures: FP64, the
+# 360x270x50 block (4.740 GB for 360*270*50*10 tracer-cells); precision form, the TMA-staged
+# kernel (the launch shape chosen on C2) on the 1440x360x50 band, 10.3 waves (6.099 GB for
+# 1440*360*50*10 tracer-cells).
+TRAFFIC_PER_TRACER_CELL = {"fp64": 4.740e9 / (360 * 270 * 50 * 10), "mixed": 6.099e9 / (1440 * 360 * 50 * 10)}
+TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the advection launch set on a 360x270x50 block, scaled by tracer-cells",
+                  "mixed": "ncu DRAM bytes of the TMA-staged kernel on a 1440x360x50 band, scaled by tracer-cells"}
 
 
 # FP64 thread-instructions per tracer-cell of the exact MDFL passes (z + x + y) and per
@@ -544,8 +548,7 @@ def run_ours(args, rank, world):
                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                     "algorithmic_bytes_per_launch": bytes_adv, "ms_per_launch": round(per, 3),
                     "traffic": round(TRAFFIC_PER_TRACER_CELL[args.precision] * cells * ntr) if headline else None,
-                    "traffic_source": "ncu DRAM bytes of the advection launch set on a 360x270x50 block, "
-                                      "scaled by tracer-cells"}
+                    "traffic_source": TRAFFIC_SOURCE[args.precision]}
     elif bt_roof is not None:
         roofline = dict(bt_roof, bound="hbm", kernel="barotropic subcycle loop (streaming model)",
                         peak_source=peak_kind, algorithmic_bytes_per_launch=bt_bytes(ni, nj, nts),

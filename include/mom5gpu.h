@@ -316,13 +316,12 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
  * gives the same results bit for bit.  A TMA-staged launch whose bounded wait
  * gave up is reported by the next mom5gpu_synchronize as MOM5GPU_ETIMEDOUT. */
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
-/* Form of the exact B-grid barotropic subcycle: 1 = predictor, momentum and
- * corrector in one launch per subcycle, each tile recomputing the ring of
- * pressure and transports it reads (about 10% more FP64 work, two launches and
- * the pressure round trip saved); 0 = three launches per subcycle; -1
- * (default) = one launch on domains of up to 524288 data-domain columns,
- * where launches rather than the FP64 pipe set the time.  Both give the same
- * results bit for bit. */
+/* Form of the exact B-grid barotropic subcycle: 0 (default) = predictor,
+ * momentum and corrector as three launches per subcycle; 1 = one launch per
+ * subcycle, each tile recomputing the ring of pressure and transports it reads
+ * (about 11% more FP64 work for two launches and the pressure round trip
+ * saved; slower on the measured workloads).  Both give the same results bit
+ * for bit. */
 int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode);
 int mom5gpu_get_tuning(const mom5gpu_domain* d, int* rows, int* prefetch, int* tj);
 /* eta_and_pbot_tendency (ocean_barotropic.F90:2668-2734), depth-based. */

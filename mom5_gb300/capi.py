@@ -324,7 +324,7 @@ class Domain:
         self.check(lib().mom5gpu_set_tuning(self.h, rows, int(prefetch), tj))
 
     def set_barotropic_fusion(self, mode: int):
-        """1: one launch per exact B-grid subcycle; 0: three; -1: by domain size."""
+        """1: one launch per exact B-grid subcycle; 0 (default): three."""
         self.check(lib().mom5gpu_set_barotropic_fusion(self.h, int(mode)))
 
     def set_itt0(self, itt0):

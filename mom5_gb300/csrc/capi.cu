@@ -870,7 +870,7 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
 
 int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode) {
   if (!d) return MOM5GPU_EINVAL;
-  if (mode < -1 || mode > 1) return fail(d, MOM5GPU_EINVAL, "set_barotropic_fusion: mode -1, 0 or 1");
+  if (mode < 0 || mode > 1) return fail(d, MOM5GPU_EINVAL, "set_barotropic_fusion: mode 0 or 1");
   if (mode != d->bt_fused) {
     // the cached subcycle graphs hold the other form (their key is the kernel arguments)
     for (auto& gr : d->bt_graphs)

@@ -110,7 +110,7 @@ struct mom5gpu_domain {
   int tune_mixed_pf = 0;     // precision form: 1 tracer levels prefetched by cp.async (height 16), 2 TMA-staged tiles
   int* tma_err = nullptr;    // set by the TMA-staged kernel when a bounded wait gave up
   int tune_y_tj = 0;         // FP64 y-pass rows per thread
-  int bt_fused = -1;         // exact B-grid subcycle in one launch: 1 yes, 0 three launches, -1 by domain size
+  int bt_fused = 0;          // exact B-grid subcycle: 1 one launch, 0 three launches
   // CUDA graphs of the barotropic subcycle loop, one per set of kernel arguments
   // (the bytes of the BtArgs it was captured with: time levels rotate), at most
   // kBtGraphs, the oldest replaced first

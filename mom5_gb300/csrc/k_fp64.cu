@@ -1264,15 +1264,16 @@ constexpr int kFusedTX = 64, kFusedTY = 8;
 __global__ void __launch_bounds__(256) k_bt_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
   bt_fused_body<kFusedTX, kFusedTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
 }
-// The one-launch subcycle pays a recomputed ring (about 10% more FP64 work) to
-// save two launches and the round trips of the pressure and transports: it wins
-// where launches, not the FP64 pipe, set the time -- domains of up to about half
-// a million columns.
-constexpr long kFusedMaxColumns = 1L << 19;
+// The one-launch subcycle pays a recomputed ring (about 11% more FP64 work) to
+// save two launches and the round trips of the pressure and transports.
+// Measured on GB300 it loses on both barotropic workloads (C1 360x300: 1.81 ms
+// per 80 subcycles against 1.44 ms; C2: 12.3 ms per 60 against 10.7 ms): the
+// three-launch form is already near the FP64 pipe's rate on large domains and
+// has four times the blocks on small ones, so it stays the default and the
+// one-launch form is chosen only on request.
 static bool use_fused(const mom5gpu_domain* d, const BtArgs& a) {
   if (a.cgrid || a.btf) return false;
-  if (d->bt_fused >= 0) return d->bt_fused == 1;
-  return a.g.n2 <= kFusedMaxColumns;
+  return d->bt_fused == 1;
 }
 __global__ void k_bt_post2(BtArgs a, double* conv, double* eta_u, double* ps_out) { bt_post2_body(a, conv, eta_u, ps_out, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_post3(BtArgs a, const double* ps, double* gxo, double* gyo) { bt_post3_body(a, ps, gxo, gyo, blockIdx.x, blockIdx.y); }

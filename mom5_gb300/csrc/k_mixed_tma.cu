@@ -245,10 +245,14 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
     const unsigned wt = (in && wet) ? 1u : 0u;
     const unsigned wA = __shfl_up_sync(full, wt, 1), wC = __shfl_down_sync(full, wt, 1);
     const unsigned wD = __shfl_down_sync(full, wt, 2);
+    // every tracer's level k+2 first (issued a level ago), so that no wait -- a
+    // memory fence to the compiler -- separates the tracers' work below and
+    // their instructions can interleave
+    for (int n = 0; n < ntr; ++n)
+      if (!mbar_wait(&s.bar[n], (unsigned)(k & 1))) bad = true;
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
       if (n >= ntr) break;
-      if (!mbar_wait(&s.bar[n], (unsigned)(k & 1))) bad = true;
       float tzv = 0.f, tk = 0.f, fzv = 0.f;
       if (in) {
         const float tkp2 = d2f(direct ? s.t[n][sc] : a.T[(long)n * g.n3 + (long)kp2 * g.n2 + o]);

@@ -506,8 +506,9 @@ def test_barotropic_subcycle_forms_match(env, fusion, cyclic_x, cyclic_y, steppi
               "udrho_v": out["udrho_v"]}
         d.set(capi.F.ETA_T, np.ascontiguousarray(st["eta_t"]), level=taup1)
         tau = taup1
-    with pytest.raises(capi.Mom5GpuError):
-        d.set_barotropic_fusion(2)
+    for bad in (-1, 2):
+        with pytest.raises(capi.Mom5GpuError):
+            d.set_barotropic_fusion(bad)
 
 
 def test_barotropic_graph_follows_arguments(env):
