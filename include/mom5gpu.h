@@ -316,13 +316,25 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
  * gives the same results bit for bit.  A TMA-staged launch whose bounded wait
  * gave up is reported by the next mom5gpu_synchronize as MOM5GPU_ETIMEDOUT. */
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
-/* Form of the exact B-grid barotropic subcycle: 0 (default) = predictor,
- * momentum and corrector as three launches per subcycle; 1 = one launch per
- * subcycle, each tile recomputing the ring of pressure and transports it reads
- * (about 11% more FP64 work for two launches and the pressure round trip
- * saved; slower on the measured workloads).  Both give the same results bit
- * for bit. */
+/* Form of the exact B-grid barotropic subcycles (update_ocean_barotropic,
+ * ocean_barotropic.F90:3344-3575): 0 (default) = predictor, momentum and
+ * corrector as three launches per subcycle, replayed from a CUDA graph; 1 = one
+ * launch per subcycle, each tile recomputing the ring of pressure and
+ * transports it reads (about 11% more FP64 work); 2 = all subcycles of a step
+ * in one cooperative launch, a bounded grid barrier between the phases (a wait
+ * that gives up is reported by mom5gpu_synchronize as MOM5GPU_ETIMEDOUT; inside
+ * a stream capture the three launches are used).  Forms 1 and 2 were slower
+ * than 0 on every measured domain.  Every form gives the same results bit for
+ * bit. */
 int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode);
+/* Self-test of the grid barrier of the cooperative subcycle launch: `rounds`
+ * (1..100000) barriers over a full resident grid, after each of which every
+ * block checks that every block arrived (MOM5GPU_ENUMERIC if one passed
+ * early).  With unreachable != 0 each barrier waits for one block more than the
+ * grid holds, so every wait runs out after about 8 ms of SM clocks and the
+ * call returns MOM5GPU_ETIMEDOUT from the next mom5gpu_synchronize, the
+ * context still usable.  MOM5GPU_EUNSUPPORTED without cooperative launch. */
+int mom5gpu_grid_barrier_selftest(mom5gpu_domain* d, int rounds, int unreachable);
 int mom5gpu_get_tuning(const mom5gpu_domain* d, int* rows, int* prefetch, int* tj);
 /* eta_and_pbot_tendency (ocean_barotropic.F90:2668-2734), depth-based. */
 int mom5gpu_eta_and_pbot_tendency(mom5gpu_domain* d, int tau);

@@ -126,6 +126,7 @@ def lib() -> C.CDLL:
             "mom5gpu_set_itt0": (C.c_int, [vp, C.c_long]),
             "mom5gpu_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
             "mom5gpu_set_barotropic_fusion": (C.c_int, [vp, C.c_int]),
+            "mom5gpu_grid_barrier_selftest": (C.c_int, [vp, C.c_int, C.c_int]),
             "mom5gpu_get_tuning": (C.c_int, [vp, ip, ip, ip]),
             "mom5gpu_copy_field_async": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
             "mom5gpu_set_tracer_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p]),
@@ -324,8 +325,16 @@ class Domain:
         self.check(lib().mom5gpu_set_tuning(self.h, rows, int(prefetch), tj))
 
     def set_barotropic_fusion(self, mode: int):
-        """1: one launch per exact B-grid subcycle; 0 (default): three."""
+        """Exact B-grid subcycles: 0 (default) three launches each, 1 one
+        launch each, 2 all in one cooperative launch."""
         self.check(lib().mom5gpu_set_barotropic_fusion(self.h, int(mode)))
+
+    def grid_barrier_selftest(self, rounds: int, unreachable: bool = False):
+        """Run the cooperative grid barrier `rounds` times and check its order;
+        with unreachable the waits run out and the next synchronize raises
+        ETIMEDOUT."""
+        self.check(lib().mom5gpu_grid_barrier_selftest(self.h, int(rounds), 1 if unreachable else 0))
+        self.synchronize()
 
     def set_itt0(self, itt0):
         self.check(lib().mom5gpu_set_itt0(self.h, int(itt0)))

@@ -195,6 +195,23 @@ static void resolve_clocks(mom5gpu_domain* d) {
   d->clocks.clear();
 }
 
+// The device words of the bounded waits, in one allocation: the error word
+// (bit 0: a TMA-staged copy did not arrive; bit 1: a grid barrier gave up) and
+// the arrival counter of the cooperative subcycle kernel's grid barriers.
+int ensure_wait_words(mom5gpu_domain* d) {
+  if (d->wait_err) return MOM5GPU_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p, 0, 2 * sizeof(int));
+  if (e != cudaSuccess) {
+    if (p) cudaFree(p);
+    return cuda_fail(d, e, "error word");
+  }
+  d->wait_err = (int*)p;
+  d->bt_sync = (unsigned*)p + 1;
+  return MOM5GPU_OK;
+}
+
 }  // namespace mom5
 
 // ============================================================================
@@ -292,7 +309,7 @@ void mom5gpu_destroy(mom5gpu_domain* d) {
     if (p) cudaFree(p);
   if (d->mixed_scr) cudaFree(d->mixed_scr);
   if (d->flag) cudaFree(d->flag);
-  if (d->tma_err) cudaFree(d->tma_err);
+  if (d->wait_err) cudaFree(d->wait_err);  // bt_sync shares its allocation
   if (d->hz) cudaFree(d->hz);
   if (d->hx) cudaFree(d->hx);
   if (d->kmt_d) cudaFree(d->kmt_d);
@@ -320,12 +337,14 @@ int mom5gpu_synchronize(mom5gpu_domain* d) {
   if (!d) return MOM5GPU_EINVAL;
   cudaError_t e = cudaStreamSynchronize(d->stream);
   if (e != cudaSuccess) return cuda_fail(d, e, "synchronize");
-  if (d->tma_err) {  // a bounded wait of the TMA-staged precision kernel gave up
+  if (d->wait_err) {  // a bounded wait of a kernel gave up
     int v = 0;
-    e = cudaMemcpy(&v, d->tma_err, sizeof(int), cudaMemcpyDeviceToHost);
+    e = cudaMemcpy(&v, d->wait_err, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(d, e, "synchronize");
     if (v) {
-      cudaMemset(d->tma_err, 0, sizeof(int));
+      cudaMemset(d->wait_err, 0, sizeof(int));
+      if (v & 2)
+        return fail(d, MOM5GPU_ETIMEDOUT, "barotropic subcycles: a grid barrier wait gave up; the step's results are void");
       return fail(d, MOM5GPU_ETIMEDOUT, "precision form: a tile's staged copy did not arrive; its results are void");
     }
   }
@@ -870,7 +889,7 @@ int mom5gpu_tracer_advection_step(mom5gpu_domain* d, int taum1, int tau, int tau
 
 int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode) {
   if (!d) return MOM5GPU_EINVAL;
-  if (mode < 0 || mode > 1) return fail(d, MOM5GPU_EINVAL, "set_barotropic_fusion: mode 0 or 1");
+  if (mode < 0 || mode > 2) return fail(d, MOM5GPU_EINVAL, "set_barotropic_fusion: mode 0, 1 or 2");
   if (mode != d->bt_fused) {
     // the cached subcycle graphs hold the other form (their key is the kernel arguments)
     for (auto& gr : d->bt_graphs)
@@ -879,6 +898,12 @@ int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode) {
   }
   d->bt_fused = mode;
   return MOM5GPU_OK;
+}
+
+int mom5gpu_grid_barrier_selftest(mom5gpu_domain* d, int rounds, int unreachable) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (rounds < 1 || rounds > 100000) return fail(d, MOM5GPU_EINVAL, "grid_barrier_selftest: rounds 1..100000");
+  return grid_barrier_selftest(d, rounds, unreachable);
 }
 
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj) {

@@ -108,9 +108,13 @@ struct mom5gpu_domain {
   // autotuned launch shapes (0 = built-in heuristic)
   int tune_mixed_rows = 32;  // precision-form tile height incl. halo: 16, 24, 32 or 64
   int tune_mixed_pf = 0;     // precision form: 1 tracer levels prefetched by cp.async (height 16), 2 TMA-staged tiles
-  int* tma_err = nullptr;    // set by the TMA-staged kernel when a bounded wait gave up
+  int* wait_err = nullptr;   // set when a bounded device wait gave up: bit 0 a TMA-staged copy, bit 1 a grid barrier
+  unsigned* bt_sync = nullptr;  // arrival counter of the cooperative barotropic subcycle's grid barriers
   int tune_y_tj = 0;         // FP64 y-pass rows per thread
-  int bt_fused = 0;          // exact B-grid subcycle: 1 one launch, 0 three launches
+  int bt_fused = 0;          // exact B-grid subcycles: 0 three launches each, 1 one launch each,
+                             // 2 all in one cooperative launch
+  int coop_blocks = 0;       // resident blocks per SM of the cooperative subcycle kernel (0: not queried, -1: none)
+  int coop_sms = 0;          // SMs of the device
   // CUDA graphs of the barotropic subcycle loop, one per set of kernel arguments
   // (the bytes of the BtArgs it was captured with: time levels rotate), at most
   // kBtGraphs, the oldest replaced first
@@ -268,6 +272,7 @@ int launch_barotropic_forcing(mom5gpu_domain* d);
 int launch_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vcoord, bool linear_fs, bool dzwu_k0);
 int launch_advection_velocity(mom5gpu_domain* d, int tau);
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);
+int grid_barrier_selftest(mom5gpu_domain* d, int rounds, int unreachable);
 int launch_content(mom5gpu_domain* d, int n, int level, double* out_host);
 int launch_eta_integral(mom5gpu_domain* d, const double* eta, double* out_host);
 int launch_check_finite(mom5gpu_domain* d, const double* a, size_t count, int* out_host);
@@ -312,6 +317,7 @@ int prepare_batch_mixed();
 int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, int taup1, double dtime,
                       bool fused_update);
 // TMA-staged variant of one launch (k_mixed_tma.cu); MOM5GPU_EUNSUPPORTED: use the plain kernel
+int ensure_wait_words(mom5gpu_domain* d);
 int launch_mixed_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all);
 
 }  // namespace mom5

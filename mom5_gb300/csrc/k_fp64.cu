@@ -1264,17 +1264,175 @@ constexpr int kFusedTX = 64, kFusedTY = 8;
 __global__ void __launch_bounds__(256) k_bt_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
   bt_fused_body<kFusedTX, kFusedTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
 }
-// The one-launch subcycle pays a recomputed ring (about 11% more FP64 work) to
-// save two launches and the round trips of the pressure and transports.
-// Measured on GB300 it loses on both barotropic workloads (C1 360x300: 1.81 ms
-// per 80 subcycles against 1.44 ms; C2: 12.3 ms per 60 against 10.7 ms): the
-// three-launch form is already near the FP64 pipe's rate on large domains and
-// has four times the blocks on small ones, so it stays the default and the
-// one-launch form is chosen only on request.
-static bool use_fused(const mom5gpu_domain* d, const BtArgs& a) {
-  if (a.cgrid || a.btf) return false;
-  return d->bt_fused == 1;
+// ---- every exact B-grid subcycle of a step in one cooperative launch ----
+//
+// A persistent grid of 128-thread blocks, all resident (cooperative launch),
+// walks the blocks of the predictor, momentum and corrector launches (virtual
+// block vb = bx + nbx*by of their (ni+2)/128 x (nj+2) grid) with the same
+// bodies, and a grid barrier stands where a launch boundary stood, so the
+// results are those of the three launches bit for bit.  A barrier is an
+// arrival counter: thread 0 of each block publishes the block's writes (fence),
+// adds one and waits until the counter reaches the barrier's target.  The wait
+// is bounded (kGridWaitCycles of the SM clock, about a second) and watches the
+// error word: a block that gives up sets bit 1 of it and returns, every other
+// block gives up at its barrier too, and mom5gpu_synchronize reports
+// MOM5GPU_ETIMEDOUT.
+constexpr long long kGridWaitCycles = 1LL << 31;
+
+DEVI unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
+DEVI int ld_relaxed_s32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// false when this block or another gave up (the caller returns)
+DEVI bool grid_barrier(unsigned* ctr, unsigned target, int* err, long long limit) {
+  __shared__ int pass;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    int ok = 1;
+    const long long t0 = clock64();
+    while (ld_acquire_u32(ctr) < target) {
+      if (ld_relaxed_s32(err) & 2) {
+        ok = 0;
+        break;
+      }
+      if (clock64() - t0 > limit) {
+        atomicOr(err, 2);
+        ok = 0;
+        break;
+      }
+    }
+    __threadfence();
+    pass = ok;
+  }
+  __syncthreads();
+  return pass != 0;
+}
+
+__global__ void __launch_bounds__(128) k_bt_coop(BtArgs a, unsigned* ctr, int* err) {
+  const Geo& g = a.g;
+  const int nbx = (g.ni + 2 + 127) / 128, nvb = nbx * (g.nj + 2);
+  const unsigned per = gridDim.x;
+  unsigned target = 0;
+  for (int itime = 1; itime <= a.nts; ++itime) {
+    const int so = itime % 2, sn = (itime + 1) % 2;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) bt_pred_body(a, so, sn, itime > 1, vb % nbx, vb / nbx);
+    if (!grid_barrier(ctr, target += per, err, kGridWaitCycles)) return;
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) bt_mom_b_body(a, so, sn, vb % nbx, vb / nbx);
+    if (!grid_barrier(ctr, target += per, err, kGridWaitCycles)) return;
+    const double wgt = (double)(a.nts - itime + 1);
+    for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) bt_corr_body(a, so, sn, wgt, vb % nbx, vb / nbx);
+    if (itime < a.nts && !grid_barrier(ctr, target += per, err, kGridWaitCycles)) return;
+  }
+}
+
+// Barrier self-test: `rounds` barriers over a full resident grid; after each,
+// every block checks that every block has written the round's number (or the
+// next one's).  With extra > 0 the target counts more arrivals than the grid
+// has blocks, so every wait runs out after `limit` cycles.
+__global__ void __launch_bounds__(128) k_grid_barrier_check(unsigned* ctr, int* err, int* slots, int rounds,
+                                                            unsigned extra, long long limit, int* bad) {
+  unsigned target = 0;
+  for (int r = 1; r <= rounds; ++r) {
+    if (threadIdx.x == 0) slots[blockIdx.x] = r;
+    target += gridDim.x + extra;
+    if (!grid_barrier(ctr, target, err, limit)) return;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+      const int v = ((volatile int*)slots)[b];
+      if (v < r || v > r + 1) atomicOr(bad, 1);
+    }
+  }
+}
+
+// Resident blocks per SM of a cooperative kernel (-1: no cooperative launch).
+static int coop_resident(mom5gpu_domain* d, const void* kernel) {
+  int dev = 0, coop = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!d->coop_sms) cudaDeviceGetAttribute(&d->coop_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0) != cudaSuccess) per = 0;
+  cudaGetLastError();
+  return (coop && per > 0 && d->coop_sms > 0) ? per : -1;
+}
+
+// Every SM gets the same number of blocks, no more than the walk has blocks of
+// work for and no more than can be resident.
+static int launch_bt_coop(mom5gpu_domain* d, const BtArgs& a, cudaStream_t s) {
+  int rc = ensure_wait_words(d);
+  if (rc) return rc;
+  if (!d->coop_blocks) d->coop_blocks = coop_resident(d, (const void*)k_bt_coop);
+  if (d->coop_blocks < 0) return MOM5GPU_EUNSUPPORTED;
+  const Geo& g = a.g;
+  const int nvb = ((g.ni + 2 + 127) / 128) * (g.nj + 2);
+  int bps = (nvb + d->coop_sms - 1) / d->coop_sms;
+  if (bps > d->coop_blocks) bps = d->coop_blocks;
+  cudaMemsetAsync(d->bt_sync, 0, sizeof(unsigned), s);
+  BtArgs av = a;
+  unsigned* ctr = d->bt_sync;
+  int* err = d->wait_err;
+  void* args[] = {&av, &ctr, &err};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_bt_coop, dim3(d->coop_sms * bps), dim3(128), args, 0, s);
+  return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "barotropic subcycles (cooperative launch)");
+}
+
+// Form of the exact B-grid subcycles: 0 three launches each (replayed from a
+// CUDA graph; the default), 1 one launch each (k_bt_fused, the ring
+// recomputed), 2 all of a step in one cooperative launch (k_bt_coop).  Measured
+// on GB300 both alternatives are slower on every domain tried: the one-launch
+// form adds about 11% FP64 work for its ring to a loop bound by the FP64 pipe;
+// the cooperative launch holds 7 blocks of 72 registers per SM (28 warps)
+// against the three kernels' 16 blocks of 30-32 registers (64 warps), which
+// hide the FP64 latency better, and a grid barrier across about a thousand
+// blocks costs as much as a launch gap of the graph replay.
+static int bt_form(const mom5gpu_domain* d, const BtArgs& a) {
+  if (a.cgrid || a.btf) return 0;
+  return d->bt_fused;
+}
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return cs != cudaStreamCaptureStatusNone;
+}
+
+int grid_barrier_selftest(mom5gpu_domain* d, int rounds, int unreachable) {
+  int rc = ensure_wait_words(d);
+  if (rc) return rc;
+  const int per = coop_resident(d, (const void*)k_grid_barrier_check);
+  if (per < 0) return MOM5GPU_EUNSUPPORTED;
+  const int nb = per * d->coop_sms;
+  int* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, sizeof(int) * (nb + 1));
+  if (e != cudaSuccess) return cuda_fail(d, e, "grid barrier self-test");
+  cudaStream_t s = d->stream;
+  cudaMemsetAsync(buf, 0, sizeof(int) * (nb + 1), s);
+  cudaMemsetAsync(d->bt_sync, 0, sizeof(unsigned), s);
+  unsigned* ctr = d->bt_sync;
+  int* err = d->wait_err;
+  int* slots = buf;
+  int* bad = buf + nb;
+  unsigned extra = unreachable ? 1u : 0u;
+  long long limit = unreachable ? (1LL << 24) : kGridWaitCycles;  // about 8 ms when every wait must run out
+  void* args[] = {&ctr, &err, &slots, &rounds, &extra, &limit, &bad};
+  e = cudaLaunchCooperativeKernel((const void*)k_grid_barrier_check, dim3(nb), dim3(128), args, 0, s);
+  int hbad = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(d, e, "grid barrier self-test");
+  if (hbad) return fail(d, MOM5GPU_ENUMERIC, "grid barrier self-test: a block passed a barrier early");
+  return MOM5GPU_OK;
+}
+
 __global__ void k_bt_post2(BtArgs a, double* conv, double* eta_u, double* ps_out) { bt_post2_body(a, conv, eta_u, ps_out, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_post3(BtArgs a, const double* ps, double* gxo, double* gyo) { bt_post3_body(a, ps, gxo, gyo, blockIdx.x, blockIdx.y); }
 
@@ -1412,9 +1570,11 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   cudaStream_t s = d->stream;
   ClockScope clk(d, SEC_BAROTROPIC);
   int halo = (g.cx || g.cy) ? 1 : 0;
-  const bool fused = use_fused(d, a);
+  const int form = bt_form(d, a);
+  const bool coop = form == 2 && !capturing(s);
+  const bool fused = form == 1;
   count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) +
-                        (long)a.nts * (fused ? 1 : 3 + (a.cgrid ? 2 * halo : 0)) + 4 + 5 * halo);
+                        (coop ? 1 : (long)a.nts * (fused ? 1 : 3 + (a.cgrid ? 2 * halo : 0))) + 4 + 5 * halo);
   k_bt_init<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, src,
                                                           esm, d->opt.initsum_with_bar);
   dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
@@ -1449,7 +1609,9 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
       k_bt_corr<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
     }
   };
-  if (!replay_subcycle_graph(d, a, subcycles)) subcycles(s);
+  int crc = coop ? launch_bt_coop(d, a, s) : MOM5GPU_EUNSUPPORTED;
+  if (crc != MOM5GPU_OK && crc != MOM5GPU_EUNSUPPORTED) return crc;
+  if (crc == MOM5GPU_EUNSUPPORTED && !replay_subcycle_graph(d, a, subcycles)) subcycles(s);
   double rntsp1 = 1.0 / ((double)a.nts + 1.0);
   double rnts = a.stepB ? 2.0 / ((double)a.nts * (double)(a.nts + 1)) : 1.0 / (double)a.nts;
   k_bt_post1<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(n2, rntsp1, rnts, a.eta_bar, a.udrho_u, a.udrho_v);

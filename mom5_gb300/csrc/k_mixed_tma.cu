@@ -253,11 +253,17 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
       if (n >= ntr) break;
-      float tzv = 0.f, tk = 0.f, fzv = 0.f;
+      // Every position computes and the values of those outside the domain, of
+      // dry faces and of halo cells are discarded by selects: no branch, so no
+      // divergent paths, in the tracer loop.  A position outside a wall reads its
+      // level at the offset o = 0 (in the array; its value is never kept).
+      const float tkp2 = d2f(direct ? s.t[n][sc] : a.T[(long)n * g.n3 + (long)kp2 * g.n2 + o]);
+      const float tk = w1[n];
+      float fzv, ftn = ftp[n];
+      const float tzc = z_cell(w0[n], tk, w2[n], tkp2, mb, zmf, zd0, zd1, zc, m_datr, zdtr, zwd, ftn, fzv);
+      const float tzv = in ? tzc : 0.f;
       if (in) {
-        const float tkp2 = d2f(direct ? s.t[n][sc] : a.T[(long)n * g.n3 + (long)kp2 * g.n2 + o]);
-        tk = w1[n];
-        tzv = z_cell(w0[n], tk, w2[n], tkp2, mb, zmf, zd0, zd1, zc, m_datr, zdtr, zwd, ftp[n], fzv);
+        ftp[n] = ftn;
         w0[n] = tk;
         w1[n] = w2[n];
         w2[n] = tkp2;
@@ -265,13 +271,13 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
       // x flux of face zi (between zi and zi+1) by warp shuffles
       const float tA = __shfl_up_sync(full, tzv, 1), tC = __shfl_down_sync(full, tzv, 1);
       const float tD = __shfl_down_sync(full, tzv, 2);
-      float f = 0.f;
-      if (zi >= 1 && zi <= 29 && wt && wC) f = h_flux(tA, tzv, tC, tD, wA, wD, xmf, xd0, xd1, xc);
+      const float hf = h_flux(tA, tzv, tC, tD, wA, wD, xmf, xd0, xd1, xc);
+      const float f = (zi >= 1 && zi <= 29 && wt && wC) ? hf : 0.f;
       const float fw = __shfl_up_sync(full, f, 1);
-      float t = 0.f, fi = 0.f;
-      if (xin) t = x_cell(tzv, tk, fw, f, xcoef, xdiv, fi);
-      s.tx[n][c] = t;
-      s.fzx[n][c] = fa(fzv, fi);
+      float fic;
+      const float tc = x_cell(tzv, tk, fw, f, xcoef, xdiv, fic);
+      s.tx[n][c] = xin ? tc : 0.f;
+      s.fzx[n][c] = fa(in ? fzv : 0.f, xin ? fic : 0.f);
     }
     // every tracer's slot is read: each takes level k+3
     if (__syncthreads_or(bad)) goto abort;
@@ -291,14 +297,13 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
     const bool yface = zj >= 1 && zj <= ZR - 3 && zi >= 2 && zi <= 29;
     const bool m0 = yface && s.wet[c - 32], m1 = yface && s.wet[c];
     const bool m2 = yface && s.wet[c + 32], m3 = yface && s.wet[c + 64];
+    // rows either side of face zj; a position without a y face reads its own row
+    const int cA = yface ? c - 32 : c, cC = yface ? c + 32 : c, cD = yface ? c + 64 : c;
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
       if (n >= ntr) break;
-      float fyv = 0.f;
-      if (m1 && m2)
-        fyv = h_flux(s.tx[n][c - 32], s.tx[n][c], s.tx[n][c + 32], s.tx[n][c + 64], m1 && m0, m3 && m2, ymf, yd0, yd1,
-                     yc);
-      s.fy[n][c] = fyv;
+      const float hf = h_flux(s.tx[n][cA], s.tx[n][c], s.tx[n][cC], s.tx[n][cD], m1 && m0, m3 && m2, ymf, yd0, yd1, yc);
+      s.fy[n][c] = (m1 && m2) ? hf : 0.f;
     }
     if (__syncthreads_or(bad)) goto abort;
     // ---- outputs of the interior cells ----
@@ -394,7 +399,7 @@ int run_tma_zr(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, 
   if (!ok) return fail(d, MOM5GPU_ECUDA, "TMA precision kernel: tensor-map encoding failed");
   constexpr int TJ = ZR - 4;
   dim3 grid((g.ni + TI - 1) / TI, (g.nj + TJ - 1) / TJ);
-  k_mdfl_mixed_tma<NC, ZR, MINB><<<grid, 32 * ZR, smem, d->stream>>>(a, n0, zt0, maps, d->tma_err);
+  k_mdfl_mixed_tma<NC, ZR, MINB><<<grid, 32 * ZR, smem, d->stream>>>(a, n0, zt0, maps, d->wait_err);
   count_launches(d, 1);
   return MOM5GPU_OK;
 }
@@ -431,11 +436,8 @@ int run_tma_pairs(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tal
 // the caller then launches the plain kernel.
 int launch_mixed_tma(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
   if (d->geo.ni % 2 != 0) return MOM5GPU_EUNSUPPORTED;
-  if (!d->tma_err) {
-    cudaError_t e = cudaMalloc(&d->tma_err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(d->tma_err, 0, sizeof(int));
-    if (e != cudaSuccess) return cuda_fail(d, e, "TMA precision kernel: error word");
-  }
+  int rc = ensure_wait_words(d);
+  if (rc) return rc;
   if (d->tune_mixed_pf == 3) return run_tma_pairs(d, a, n0, Tall, zt0, ntr_all);
   if (a.ntr <= 1) return run_tma<1>(d, a, n0, Tall, zt0, ntr_all);
   if (a.ntr <= 2) return run_tma<2>(d, a, n0, Tall, zt0, ntr_all);

@@ -102,7 +102,10 @@ DEVI float z_cell(float tkm1, float tk, float tkp1, float tkp2, unsigned mb, flo
   float Rjp = (mkm1 && mk) ? fs(tkm1, tk) : 0.f;
   float Rj = (mk && mkp1) ? fs(tk, tkp1) : 0.f;
   float Rjm = (mkp1 && mkp2) ? fs(tkp1, tkp2) : 0.f;
-  float fbt = (mkp1 && mk) ? face_flux(mf, Rjm, Rj, Rjp, tkp1, tk, d0, d1, c) : 0.f;
+  // the flux of every face is formed and a dry face's discarded: a select, not a
+  // branch around the division and the limiter
+  const float ff = face_flux(mf, Rjm, Rj, Rjp, tkp1, tk, d0, d1, c);
+  float fbt = (mkp1 && mk) ? ff : 0.f;
   float adiv = fm(datr, fs(fbt, ftp));
   fz = fm(dtr, adiv);
   ftp = fbt;

@@ -471,14 +471,15 @@ def test_barotropic_matches(env, cyclic_x, stepping_B, cgrid):
     assert np.abs(out["eta_t_bar"]).max() > 0 and np.abs(out["udrho_u"]).max() > 0
 
 
-@pytest.mark.parametrize("fusion", [0, 1])
+@pytest.mark.parametrize("fusion", [0, 1, 2])
 @pytest.mark.parametrize("cyclic_x,cyclic_y,stepping_B", [(True, False, True), (False, False, False),
                                                          (True, True, True)])
 def test_barotropic_subcycle_forms_match(env, fusion, cyclic_x, cyclic_y, stepping_B):
-    """The exact B-grid subcycle as three launches or as one launch per subcycle
-    (ring of pressure and transports recomputed per tile), on a domain of several
-    tiles with partial ones: every output equal to the restatement over three
-    baroclinic steps, also when the form changes between steps."""
+    """The exact B-grid subcycle as three launches, as one launch per subcycle
+    (ring of pressure and transports recomputed per tile), as one cooperative
+    launch for all subcycles (grid barriers between the phases), on a domain of
+    several tiles with partial ones: every output equal to the restatement over
+    three baroclinic steps, also when the form changes between steps."""
     capi, O = env
     sp = grid.DomainSpec(ni=150, nj=29, nk=1, lon0=0.0, lon1=150.0, lat0=-55.0, lat1=55.0, cyclic_x=cyclic_x,
                          cyclic_y=cyclic_y, hmin=None, ridge_amp=1200.0, ntracers=0, seed=71,
@@ -493,7 +494,7 @@ def test_barotropic_subcycle_forms_match(env, fusion, cyclic_x, cyclic_y, steppi
     dims = O.dims(sp)
     st = _baro_state(dom)
     tau = 1
-    for step, mode in enumerate((fusion, fusion, 1 - fusion)):
+    for step, mode in enumerate((fusion, fusion, (fusion + 2) % 3)):
         d.set_barotropic_fusion(mode)
         taup1 = 3 - tau
         d.update_ocean_barotropic(tau, taup1)
@@ -506,7 +507,7 @@ def test_barotropic_subcycle_forms_match(env, fusion, cyclic_x, cyclic_y, steppi
               "udrho_v": out["udrho_v"]}
         d.set(capi.F.ETA_T, np.ascontiguousarray(st["eta_t"]), level=taup1)
         tau = taup1
-    for bad in (-1, 2):
+    for bad in (-1, 3):
         with pytest.raises(capi.Mom5GpuError):
             d.set_barotropic_fusion(bad)
 
