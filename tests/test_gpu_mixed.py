@@ -132,7 +132,7 @@ def test_mixed_multi_tile_and_partial_tiles(gpu_lib, case):
 def test_precision_form_launch_shapes_agree(gpu_lib, case):
     """Every launch shape of the precision form (tile height 32, 64, 24, 16, 16 with the
     tracer prefetch through cp.async, and heights 16 and 24 staged by TMA with the
-    tracer levels carried in registers, height 16 also with at most 5 tracers per
+    tracer levels carried down the column, height 16 also with at most 5 tracers per
     block) gives the same tracers bit for bit; an odd ni takes the plain kernel for
     the TMA shapes."""
     capi = gpu_lib
