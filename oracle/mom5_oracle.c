@@ -12,9 +12,10 @@
  * reference there; the reference tree holds no golden vectors for these
  * routines (its only regression data are whole-model checksums that need
  * missing experiment inputs).  Parity of this file is therefore pinned by the
- * analytic and property tests in tests/test_oracle_*.py and, where a Fortran
- * compiler exists on the GPU host, by the stubbed-reference comparison recipe
- * in oracle/ref_fortran/.
+ * analytic and property tests in tests/test_oracle_*.py (among them known
+ * answers of the advection equation: exact translation of polynomial profiles
+ * in uniform flow, tests/analytic.py).  No Fortran compiler exists on the GPU
+ * host either.
  *
  * Conventions (mirroring the Fortran arrays of the reference):
  *   - compute domain i = 1..ni, j = 1..nj (isc=1, iec=ni); the data domain has

@@ -1,0 +1,108 @@
+"""Known answers from the mathematics of the advection equation, shared by the
+oracle and GPU tests.
+
+In a box with uniform metrics (dx, dy, dz) and a uniform velocity, the exact
+solution translates the tracer by (u, v, w)*dt.  Cell averages commute with
+translation, so cell averages that follow a polynomial P(i, j, k) of the cell
+indices become P(i - cx, j - cy, k + cz) (k counts downward, w > 0 is upward).
+
+- MDFL Sweby (ocean_tracer_advect.F90:3806-4066) is direction split into 1-D
+  passes of the third-order DST3 scheme (d0 = (2-cfl)(1-cfl)/6,
+  d1 = (1-cfl^2)/6): exact in space and time for polynomials of degree 3
+  while the limiter is inactive (a smooth profile at moderate Courant numbers).
+- Upwind (:2238-2294, :2792-2824) is the first-order DST scheme: exact for
+  linear profiles.
+- The centred 2nd/4th/6th-order and Quicker fluxes are spatial
+  discretisations: on a quadratic their flux divergence is the exact
+  derivative, so one forward step gives P - dt*(u, v, -w).grad P.
+
+Cells away from the boundaries (whose halo rules are not those of a
+polynomial) must match these to roundoff.  The expectations are derived from
+the equation, not from a reading of the Fortran."""
+import numpy as np
+
+RHO0 = 1035.0
+
+VELOCITIES = [(0.4, 0.0, 0.0), (0.0, -0.3, 0.0), (0.0, 0.0, 1e-3), (0.4, -0.3, 1e-3), (-0.2, 0.25, -2e-3)]
+
+
+def cubic(x, y, z):
+    return 5.0 + 0.3 * x + 0.01 * x * x + 0.002 * y * y + 1e-4 * z ** 3 + 1e-4 * x * y * z
+
+
+def linear(x, y, z):
+    return 1.0 + 0.2 * x - 0.15 * y + 0.05 * z
+
+
+def quadratic(x, y, z):
+    return 1.0 + 0.2 * x + 0.01 * x * x - 0.15 * y + 0.003 * y * y + 0.05 * z + 0.002 * z * z
+
+
+def quadratic_grad(x, y, z):
+    return 0.2 + 0.02 * x, -0.15 + 0.006 * y, 0.05 + 0.004 * z
+
+
+PROFILES = {"cubic": cubic, "linear": linear, "quadratic": quadratic}
+
+
+def indices(shape):
+    nk, nyd, nxd = shape
+    K, J, I = np.meshgrid(np.arange(nk, dtype=float), np.arange(nyd, dtype=float), np.arange(nxd, dtype=float),
+                          indexing="ij")
+    return I, J, K
+
+
+def profile(kind, shape):
+    I, J, K = indices(shape)
+    return PROFILES[kind](I, J, K)
+
+
+def expected(kind, shape, u, v, w, dt, spacing):
+    """The known answer after one forward step of dt: a translated profile for
+    the schemes exact in space and time (cubic: MDFL Sweby; linear: upwind),
+    the forward-Euler step of the exact tendency for the quadratic."""
+    dx, dy, dz = spacing
+    I, J, K = indices(shape)
+    cx, cy, cz = u * dt / dx, v * dt / dy, w * dt / dz
+    if kind != "quadratic":
+        return PROFILES[kind](I - cx, J - cy, K + cz)
+    gx, gy, gz = quadratic_grad(I, J, K)
+    return quadratic(I, J, K) - cx * gx - cy * gy + cz * gz
+
+
+def make_box(kind, u, v, w, ni=30, nj=30, nk=30, dx=8000.0, dy=6000.0, dz=10.0):
+    """A grid.Domain with uniform metrics and levels, every cell wet, uniform
+    velocity (u, v, w) and one tracer = the profile `kind` on the whole data
+    domain.  Returns the domain and (dx, dy, dz)."""
+    import torch
+    from mom5_gb300 import grid
+    sp = grid.DomainSpec(ni=ni, nj=nj, nk=nk, lon0=0.0, lon1=0.1 * ni, lat0=-0.05 * nj, lat1=0.05 * nj,
+                         continent=None, hmin=None, ntracers=1, seed=0)
+    dom = grid.make_domain(sp)
+    for k in ("dxt", "dxte", "dxtn", "dxu"):
+        dom[k].fill_(dx)
+    for k in ("dyt", "dyte", "dytn", "dyu"):
+        dom[k].fill_(dy)
+    dom["dat"].fill_(dx * dy)
+    dom["datr"].fill_(1.0 / (dx * dy))
+    dom["rho_dzt"].fill_(RHO0 * dz)
+    dom["rho_dztr"].fill_(1.0 / (RHO0 * dz))
+    dom["tmask"].fill_(1.0)
+    dom.dzt = torch.full((nk,), dz, dtype=torch.float64)
+    dom.zw = torch.cumsum(dom.dzt, 0)
+    dom["uhrho_et"].fill_(u * RHO0 * dz)
+    dom["vhrho_nt"].fill_(v * RHO0 * dz)
+    dom["wrho_bt"].fill_(w * RHO0)
+    dom["T"][0].copy_(torch.from_numpy(profile(kind, tuple(dom["T"][0].shape))))
+    return dom, (dx, dy, dz)
+
+
+def interior(a, margin=8):
+    """Cells at least `margin` cells from every boundary."""
+    nk, nyd, nxd = a.shape
+    return a[margin:nk - margin, margin:nyd - margin, margin:nxd - margin]
+
+
+def rel_err(got, want):
+    g, e = interior(np.asarray(got)), interior(np.asarray(want))
+    return np.abs(g - e).max() / np.abs(e).max()

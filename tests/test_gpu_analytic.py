@@ -1,0 +1,54 @@
+"""Known answers from the advection equation through the C ABI (tests/analytic.py):
+on a uniform box in uniform flow, one mom5gpu_tracer_advection_step of MDFL
+Sweby translates a cubic exactly, upwind a linear profile, and the centred
+2nd/4th/6th-order and Quicker schemes take the exact forward-Euler step of a
+quadratic -- to FP64 roundoff on the drop-in path, within the precision form's
+FP32 tolerance for MDFL in that form."""
+import pytest
+
+import analytic as A
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("mdfl_sweby", "cubic"), ("upwind", "linear"), ("quicker", "quadratic"), ("centred2", "quadratic"),
+         ("centred4", "quadratic"), ("centred6", "quadratic")]
+
+
+def _scheme_id(capi, name):
+    return {"mdfl_sweby": capi.ADVECT_MDFL_SWEBY, "upwind": capi.ADVECT_UPWIND, "quicker": capi.ADVECT_QUICKER,
+            "centred2": capi.ADVECT_2ND_ORDER, "centred4": capi.ADVECT_4TH_ORDER,
+            "centred6": capi.ADVECT_6TH_ORDER}[name]
+
+
+def _step(capi, dom, scheme, dt, precision=None):
+    from mom5_gb300 import harness
+    opts = capi.default_options(precision=precision) if precision is not None else None
+    d = harness.load(dom, options=opts, scheme=_scheme_id(capi, scheme))
+    d.tracer_advection_step(1, 1, 2, dt)
+    T = d.get(capi.F.TRACER, n=1, level=2).reshape(tuple(dom["T"][0].shape))
+    d.close()
+    return T
+
+
+@pytest.mark.parametrize("vel", [(0.4, -0.3, 1e-3), (-0.2, 0.25, -2e-3), (0.0, 0.0, 1e-3)])
+@pytest.mark.parametrize("scheme,kind", CASES)
+def test_drop_in_matches_the_advection_equation(gpu_lib, scheme, kind, vel):
+    capi = gpu_lib
+    u, v, w = vel
+    dom, spacing = A.make_box(kind, u, v, w)
+    dt = 2000.0
+    T = _step(capi, dom, scheme, dt)
+    E = A.expected(kind, T.shape, u, v, w, dt, spacing)
+    assert A.rel_err(T, E) < 2e-15
+    assert A.rel_err(T, dom["T"][0].numpy()) > 1e-4
+
+
+@pytest.mark.parametrize("vel", [(0.4, -0.3, 1e-3), (-0.2, 0.25, -2e-3)])
+def test_precision_form_matches_the_advection_equation(gpu_lib, vel):
+    capi = gpu_lib
+    u, v, w = vel
+    dom, spacing = A.make_box("cubic", u, v, w, ni=62, nj=40)  # several TMA tiles (ni even)
+    dt = 2000.0
+    T = _step(capi, dom, "mdfl_sweby", dt, precision=capi.PRECISION_MIXED)
+    E = A.expected("cubic", T.shape, u, v, w, dt, spacing)
+    assert A.rel_err(T, E) < 1e-6
