@@ -1,5 +1,5 @@
-"""Known answers from the mathematics of the advection equation, shared by the
-oracle and GPU tests.
+"""Known answers from the mathematics of the advection equation and of the
+barotropic momentum equation (at the end), shared by the oracle and GPU tests.
 
 In a box with uniform metrics (dx, dy, dz) and a uniform velocity, the exact
 solution translates the tracer by (u, v, w)*dt.  Cell averages commute with
@@ -106,3 +106,52 @@ def interior(a, margin=8):
 def rel_err(got, want):
     g, e = interior(np.asarray(got)), interior(np.asarray(want))
     return np.abs(g - e).max() / np.abs(e).max()
+
+
+# ---- barotropic subcycle ----
+#
+# With no Coriolis force, no forcing, a flat bottom (depth H), every cell wet and
+# a sea surface of uniform slope, the depth-integrated transport udrho
+# (kg m^-1 s^-1) accelerates uniformly, d(udrho)/dt = -H rho0 g grad(eta),
+# and its divergence vanishes, so eta does not change away from the walls.  The
+# state after subcycle n is u0 + n*a*dtbt; the step's time average over the nts
+# subcycles weights n equally (time stepping A, mean n = (nts+1)/2) or by
+# nts-n+1 (time stepping B, mean n = (nts+2)/3).
+
+GRAV = 9.8
+
+
+def make_baro_box(sx, sy, u0, v0, ni=60, nj=50, dx=8000.0, dy=6000.0, depth=4000.0):
+    """A one-level grid.Domain with uniform metrics, f = 0, no forcing, eta =
+    0.5 + sx*i + sy*j and uniform transports (u0, v0) at time level tau."""
+    import torch
+    from mom5_gb300 import grid
+    sp = grid.DomainSpec(ni=ni, nj=nj, nk=1, lon0=0.0, lon1=0.1 * ni, lat0=-0.05 * nj, lat1=0.05 * nj,
+                         continent=None, hmin=None, depth=depth, ntracers=0, seed=0)
+    dom = grid.make_domain(sp)
+    for k, v in (("dxt", dx), ("dxte", dx), ("dxtn", dx), ("dxu", dx), ("dte", dx), ("dtw", dx),
+                 ("dyt", dy), ("dyte", dy), ("dytn", dy), ("dyu", dy), ("dus", dy), ("dun", dy),
+                 ("dxur", 1 / dx), ("dyur", 1 / dy), ("dxter", 1 / dx), ("dytnr", 1 / dy),
+                 ("dat", dx * dy), ("datr", 1 / (dx * dy)), ("daur", 1 / (dx * dy)), ("f", 0.0),
+                 ("tmask1", 1.0), ("umask1", 1.0), ("tmasken_e1", 1.0), ("tmasken_n1", 1.0),
+                 ("patm", 0.0), ("pme", 0.0), ("river", 0.0), ("source", 0.0), ("eta_smooth", 0.0),
+                 ("forcing_u", 0.0), ("forcing_v", 0.0), ("thicku", depth), ("thicken_e", depth),
+                 ("thicken_n", depth), ("rho_g", RHO0 * GRAV), ("udrho_u", u0), ("udrho_v", v0)):
+        dom[k].fill_(v)
+    J, I = np.meshgrid(np.arange(nj + 2, dtype=float), np.arange(ni + 2, dtype=float), indexing="ij")
+    eta = torch.from_numpy(0.5 + sx * I + sy * J)
+    dom["eta_t"].copy_(eta)
+    dom["eta_t_bar"].copy_(eta)
+    return dom, (dx, dy, depth)
+
+
+def baro_expected(sx, sy, u0, v0, nts, dtbt, spacing, stepping_B):
+    dx, dy, depth = spacing
+    ax, ay = -depth * RHO0 * GRAV * sx / dx, -depth * RHO0 * GRAV * sy / dy
+    nbar = (nts + 2) / 3.0 if stepping_B else (nts + 1) / 2.0
+    return u0 + ax * dtbt * nbar, v0 + ay * dtbt * nbar
+
+
+def interior2(a, margin=15):
+    nyd, nxd = a.shape
+    return a[margin:nyd - margin, margin:nxd - margin]

@@ -52,3 +52,29 @@ def test_precision_form_matches_the_advection_equation(gpu_lib, vel):
     T = _step(capi, dom, "mdfl_sweby", dt, precision=capi.PRECISION_MIXED)
     E = A.expected("cubic", T.shape, u, v, w, dt, spacing)
     assert A.rel_err(T, E) < 1e-6
+
+
+@pytest.mark.parametrize("fusion", [0, 1, 2])
+@pytest.mark.parametrize("stepping_B", [False, True])
+def test_barotropic_matches_the_momentum_equation(gpu_lib, stepping_B, fusion):
+    """A sea surface of uniform slope, f = 0, no forcing, flat bottom: the
+    exact B-grid subcycles (each form) accelerate the transports uniformly at
+    -H rho0 g grad(eta) and the step returns their time average; eta keeps its
+    value away from the walls."""
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    sx, sy, u0, v0, nts, dtbt = 1e-3, -5e-4, 100.0, -50.0, 10, 20.0
+    dom, spacing = A.make_baro_box(sx, sy, u0, v0)
+    opts = capi.default_options(barotropic_time_stepping_A=int(not stepping_B),
+                                barotropic_time_stepping_B=int(stepping_B))
+    d = harness.load(dom, options=opts)
+    assert d.barotropic_init(dtuv=nts * dtbt / 2, dtbt=dtbt) == nts
+    d.set_barotropic_fusion(fusion)
+    d.update_ocean_barotropic(1, 2)
+    shape = tuple(dom["eta_t"].shape)
+    get = lambda fid: d.get(fid, level=2).reshape(shape)
+    eu, ev = A.baro_expected(sx, sy, u0, v0, nts, dtbt, spacing, stepping_B)
+    assert abs(A.interior2(get(capi.F.UDRHO_U)) - eu).max() <= 1e-10 * abs(eu)
+    assert abs(A.interior2(get(capi.F.UDRHO_V)) - ev).max() <= 1e-10 * abs(ev)
+    assert abs(A.interior2(get(capi.F.ETA_T_BAR)) - A.interior2(dom["eta_t"].numpy())).max() <= 1e-12
+    d.close()

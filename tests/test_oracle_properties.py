@@ -314,6 +314,26 @@ def test_schemes_match_the_advection_equation(O, scheme, kind, vel):
     assert A.rel_err(Tn, dom["T"][0].numpy()) > 1e-4
 
 
+@pytest.mark.parametrize("stepping_B", [False, True])
+def test_barotropic_matches_the_momentum_equation(O, stepping_B):
+    """Known answer (tests/analytic.py): with f = 0, no forcing, a flat bottom
+    and a sea surface of uniform slope, pred_corr_tropic_depth_bgrid
+    (ocean_barotropic.F90:3225-3579) accelerates the transports uniformly at
+    -H rho0 g grad(eta), eta keeps its value, and update_ocean_barotropic
+    (:2763-3033) returns the subcycles' time average."""
+    import analytic as A
+    sx, sy, u0, v0, nts, dtbt = 1e-3, -5e-4, 100.0, -50.0, 10, 20.0
+    dom, spacing = A.make_baro_box(sx, sy, u0, v0)
+    g, d = O.domain_arrays(dom), O.dims(dom.spec)
+    st = {k: g[k].copy() for k in ("eta_t", "eta_t_bar", "udrho_u", "udrho_v")}
+    out = O.update_ocean_barotropic(d, g, st, nts, dtbt, time_stepping_B=stepping_B)
+    eu, ev = A.baro_expected(sx, sy, u0, v0, nts, dtbt, spacing, stepping_B)
+    assert np.abs(A.interior2(out["udrho_u"]) - eu).max() <= 1e-10 * abs(eu)
+    assert np.abs(A.interior2(out["udrho_v"]) - ev).max() <= 1e-10 * abs(ev)
+    assert np.abs(A.interior2(out["eta_t_bar"]) - A.interior2(g["eta_t"])).max() <= 1e-12
+    assert np.abs(A.interior2(out["conv_rho_ud_t"])).max() <= 1e-10 * abs(eu) / spacing[0]
+
+
 def test_quicker_weights_uniform_grid(O):
     """On a uniform grid quicker_init (:1510-1578) gives quick = 1/2 and the
     curvature weights 1/8, -1/4 (relative form of the classic 3/8, 6/8, -1/8)."""
