@@ -88,18 +88,25 @@ DEVI bool mbar_wait(uint64_t* b, unsigned parity) {
 }
 
 // Where the window of each tracer (levels k-1, k, k+1 in FP32 and the flux
-// through the top face) lives: in registers, or (SW) in shared memory as a ring
-// of three levels (level L in slot L mod 3), which frees about 35 registers of
-// the 10-tracer 16-row kernel for its own scheduling (measured 1.8% faster).
-template <int NC, int ZR, bool SW>
+// through the top face) lives (WM): 0 all in registers; 1 the top-face flux in
+// shared memory, the levels in registers; 2 all in shared memory, the levels as
+// a ring of three (level L in slot L mod 3).  Moving state to shared memory
+// frees registers for the kernel's own scheduling: 35 in the 10-tracer 16-row
+// kernel (WM 2, measured 1.8% faster), 10 in the 24-row kernel (WM 1), whose
+// shared memory has room for no more.
+template <int NC, int ZR, int WM>
 struct WindowStore {};
 template <int NC, int ZR>
-struct WindowStore<NC, ZR, true> {
+struct WindowStore<NC, ZR, 1> {
+  float ftp[NC][ZR * 32];
+};
+template <int NC, int ZR>
+struct WindowStore<NC, ZR, 2> {
   float win[3][NC][ZR * 32];
   float ftp[NC][ZR * 32];
 };
 
-template <int NC, int ZR, bool SW>
+template <int NC, int ZR, int WM>
 struct TmaSmem {
   static constexpr int SLOT = ZR * BX;  // doubles per box (a multiple of 16: 128-byte aligned slots)
   double t[NC][SLOT];                   // level k+2 of each tracer
@@ -110,11 +117,11 @@ struct TmaSmem {
   uint8_t wet[ZR * 32];                 // tmask at level k
   alignas(8) uint64_t bar[NC + 1];      // one per tracer slot, one for the fields
   int pending[NC + 1];                  // 1 + parity of a phase in flight, 0 = none (thread 0's bookkeeping)
-  WindowStore<NC, ZR, SW> ws;
+  WindowStore<NC, ZR, WM> ws;
 };
-// the window in shared memory where it fits beside one block per SM
+// as much of the window in shared memory as fits beside one block per SM
 template <int NC, int ZR, int MINB>
-constexpr bool kSharedWindow = ZR == 16 && MINB == 1;
+constexpr int kWindowMode = MINB != 1 ? 0 : ZR == 16 ? 2 : 1;
 
 // One level is three phases with a block barrier between them: (1) the level's
 // face terms, (2) the z and x passes of every tracer, (3) the y fluxes of every
@@ -122,8 +129,8 @@ constexpr bool kSharedWindow = ZR == 16 && MINB == 1;
 template <int NC, int ZR, int MINB>
 __global__ void __launch_bounds__(32 * ZR, MINB)
     k_mdfl_mixed_tma(MixArgs a, int n0, int zt0, const __grid_constant__ TmaMaps maps, int* err) {
-  constexpr bool SW = kSharedWindow<NC, ZR, MINB>;
-  using S = TmaSmem<NC, ZR, SW>;
+  constexpr int WM = kWindowMode<NC, ZR, MINB>;
+  using S = TmaSmem<NC, ZR, WM>;
   constexpr int SLOT = S::SLOT;
   constexpr int TJ = ZR - 4;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -178,8 +185,8 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
   }
   // the window of each tracer: levels km1, k, kp1 (at k = 0: 0, 0, min(1, nk-1)),
   // and the flux through the top face
-  constexpr int NW = SW ? 1 : NC;
-  float w0[NW], w1[NW], w2[NW], ftp[NW];
+  constexpr int NW = WM == 2 ? 1 : NC, NF = WM == 0 ? NC : 1;
+  float w0[NW], w1[NW], w2[NW], ftp[NF];
   {
     const int l1 = g.nk > 1 ? 1 : 0;
 #pragma unroll
@@ -190,16 +197,16 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
         t0 = d2f(T[o]);
         t1 = d2f(T[(long)l1 * g.n2 + o]);
       }
-      if constexpr (SW) {  // the level above level 0 is level 0 itself (ring slot 2)
+      if constexpr (WM == 2) {  // the level above level 0 is level 0 itself (ring slot 2)
         s.ws.win[2][n][c] = t0;
         s.ws.win[0][n][c] = t0;
         s.ws.win[1][n][c] = t1;
-        s.ws.ftp[n][c] = 0.f;
       } else {
         w0[n] = w1[n] = t0;
         w2[n] = t1;
-        ftp[n] = 0.f;
       }
+      if constexpr (WM == 0) ftp[n] = 0.f;
+      else s.ws.ftp[n][c] = 0.f;
     }
   }
   // wet bits of levels km1, k, kp1, kp2 (mask2 at the raw position)
@@ -289,27 +296,30 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
       // level at the offset o = 0 (in the array; its value is never kept).
       const float tkp2 = d2f(direct ? s.t[n][sc] : a.T[(long)n * g.n3 + (long)kp2 * g.n2 + o]);
       float tkm1, tk, tkp1, ftn, fzv;
-      if constexpr (SW) {
+      if constexpr (WM == 2) {
         tkm1 = s.ws.win[r_km1][n][c];
         tk = s.ws.win[r_k][n][c];
         tkp1 = s.ws.win[r_kp1][n][c];
-        ftn = s.ws.ftp[n][c];
       } else {
         tkm1 = w0[n];
         tk = w1[n];
         tkp1 = w2[n];
-        ftn = ftp[n];
       }
+      if constexpr (WM == 0) ftn = ftp[n];
+      else ftn = s.ws.ftp[n][c];
       const float tzc = z_cell(tkm1, tk, tkp1, tkp2, mb, zmf, zd0, zd1, zc, m_datr, zdtr, zwd, ftn, fzv);
       const float tzv = in ? tzc : 0.f;
-      if constexpr (SW) {
-        s.ws.ftp[n][c] = in ? ftn : 0.f;
+      if constexpr (WM == 2) {
         s.ws.win[r_km1][n][c] = tkp2;  // level k+2 takes the slot of level k-1
       } else if (in) {
-        ftp[n] = ftn;
         w0[n] = tk;
         w1[n] = w2[n];
         w2[n] = tkp2;
+      }
+      if constexpr (WM == 0) {
+        if (in) ftp[n] = ftn;
+      } else {
+        s.ws.ftp[n][c] = in ? ftn : 0.f;
       }
       // x flux of face zi (between zi and zi+1) by warp shuffles
       const float tA = __shfl_up_sync(full, tzv, 1), tC = __shfl_down_sync(full, tzv, 1);
@@ -360,7 +370,7 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
           // T(taup1) = T + (rho_dzt(taum1)*rho_dztr - 1)*T + rho_dzt(tau)*rho_dztr*dT; T(k) in FP32 is
           // ring slot k mod 3, or w0 after the shift
           float tkk;
-          if constexpr (SW) tkk = s.ws.win[k % 3][n][c];
+          if constexpr (WM == 2) tkk = s.ws.win[k % 3][n][c];
           else tkk = w0[n];
           const double tn = a.T[(long)n * g.n3 + p] + f2d(update_inc(uq, tkk, ur, dT));
           double* out = a.out + (long)(n0 + n) * g.n3;
@@ -430,7 +440,7 @@ bool encode(CUtensorMap* m, const double* base, const Geo& g, long nz, int rows)
 template <int NC, int ZR, int MINB>
 int run_tma_zr(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tall, int zt0, int ntr_all) {
   const Geo& g = d->geo;
-  constexpr size_t smem = sizeof(TmaSmem<NC, ZR, kSharedWindow<NC, ZR, MINB>>);
+  constexpr size_t smem = sizeof(TmaSmem<NC, ZR, kWindowMode<NC, ZR, MINB>>);
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(k_mdfl_mixed_tma<NC, ZR, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
