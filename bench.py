@@ -373,16 +373,17 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     barotropic forcing) and reads its results back (tracers; eta_t_bar, udrho),
     stream-ordered copies (mom5gpu_copy_field_async) ordered by events.
 
-    Uploads go into device staging buffers on the upload stream as soon as the
-    previous step's staging copies are done, so they run beside the previous
-    step's read-back; a staging stream then copies them into their fields
-    (device to device, mom5gpu_copy_boxes: a kernel, so the copy engines stay
-    with the host link) once the field is free: a tracer time level after its
-    read-back two steps earlier (three time levels rotate), the velocity after
-    the previous step's advection, the forcing after its barotropic step.
-    `warm` untimed steps first (first-touch allocations, graph captures); the
-    timed steps are timed on the host wall clock and each stream's work by
-    CUDA events."""
+    Three time levels rotate, so the tracer level a step reads is the one the
+    step two before wrote: its tracers are uploaded straight into that level
+    (mom5gpu_copy_field_async, host to device) as soon as that step's read-back
+    of it is done, during the previous step's compute.  The velocity and the
+    forcing have one copy each in the library, busy until the previous step's
+    advection or barotropic step ends: they are uploaded into device staging
+    buffers early and moved into their fields by a staging stream
+    (mom5gpu_copy_boxes, a kernel, so the copy engines stay with the host link)
+    once the field is free.  `warm` untimed steps first (first-touch
+    allocations, graph captures); the timed steps are timed on the host wall
+    clock and each stream's work by CUDA events."""
     import numpy as np
     import torch
     from mom5_gb300 import capi
@@ -391,13 +392,14 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     dev = lambda n: torch.empty(n, dtype=torch.float64, device="cuda")
     n3, nw = d.count(F.TRACER), d.count(F.WRHO_BT)
     n2 = d.count(F.ETA_T_BAR)
-    ups = []    # (field, n, host buffer, device staging buffer, when the field is free: "level", "adv", "step")
+    ups = []    # staged: (field, n, host buffer, device staging buffer, when the field is free: "adv", "step")
+    direct = []  # straight into the field's time level: (field, n, host buffer)
     downs = []  # (field, n, host buffer)
     if ntr > 0:
         for n in range(1, ntr + 1):
             h = pin(n3)
             h.copy_(torch.from_numpy(d.get(F.TRACER, n=n, level=1)))
-            ups.append((F.TRACER, n, h, dev(n3), "level"))
+            direct.append((F.TRACER, n, h))
             downs.append((F.TRACER, n, pin(n3)))
         for fid, cnt in ((F.UHRHO_ET, n3), (F.VHRHO_NT, n3), (F.WRHO_BT, nw)):
             h = pin(cnt)
@@ -416,7 +418,7 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     h2d, stg, d2h = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
     total = warm + steps
     tev = lambda: torch.cuda.Event(enable_timing=True)
-    names = ("up0", "up1", "stg1", "c0", "adv", "c1", "d2h0", "d2h1")
+    names = ("up0", "ups1", "upt0", "up1", "stg1", "c0", "adv", "c1", "d2h0", "d2h1")
     ev = {k: [tev() for _ in range(total)] for k in names}
     torch.cuda.synchronize()
     t0 = None
@@ -432,23 +434,30 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
         with torch.cuda.stream(h2d):
             for _, _, h, buf, _ in ups:
                 buf.copy_(h, non_blocking=True)
+        ev["ups1"][s_].record(h2d)
+        # host -> tracer level lin, once the read-back of the step that wrote it is done
+        if s_ >= 2:
+            h2d.wait_event(ev["d2h1"][s_ - 2])
+        ev["upt0"][s_].record(h2d)
+        for fid, n, h in direct:
+            d.copy_field_async(fid, h.data_ptr(), 1, h2d.cuda_stream, n=n, level=lin)
         ev["up1"][s_].record(h2d)
         # staging -> fields, each once its field is free, by the library's box copy
         # (a kernel: the copy engines are busy with the host link)
-        stg.wait_event(ev["up1"][s_])
-        for when, after in (("level", "d2h1"), ("adv", "adv"), ("step", "c1")):
-            back = 2 if when == "level" else 1
-            if s_ >= back:
-                stg.wait_event(ev[after][s_ - back])
+        for when, after in (("adv", "adv"), ("step", "c1")):
+            if s_ >= 1:
+                stg.wait_event(ev[after][s_ - 1])
             boxes = []
             for fid, n, _, buf, w in ups:
                 if w == when:
-                    dst = d.device_ptr(fid, n=n, level=lin if fid == F.TRACER else 0)
-                    boxes.append(capi.Box(buf.data_ptr(), dst, (1, buf.numel(), buf.numel()),
+                    boxes.append(capi.Box(buf.data_ptr(), d.device_ptr(fid), (1, buf.numel(), buf.numel()),
                                           (1, buf.numel(), buf.numel()), (buf.numel(), 1, 1)))
-            capi.copy_boxes(boxes, stg.cuda_stream)
+            if boxes:
+                stg.wait_event(ev["ups1"][s_])
+                capi.copy_boxes(boxes, stg.cuda_stream)
         ev["stg1"][s_].record(stg)
         stream.wait_event(ev["stg1"][s_])
+        stream.wait_event(ev["up1"][s_])
         ev["c0"][s_].record(stream)
         if ntr > 0:
             d.tracer_advection_step(lin, lin, lout, wl.dtts)
@@ -467,12 +476,12 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     mean = lambda a, b: float(np.mean([ev[a][s].elapsed_time(ev[b][s]) for s in rng]))
     wait = float(np.mean([ev["c1"][s - 1].elapsed_time(ev["c0"][s]) for s in rng]))
     span = ev["c0"][warm].elapsed_time(ev["c1"][total - 1]) / steps
-    hb = 8 * sum(h.numel() for _, _, h, _, _ in ups)
+    hb = 8 * (sum(h.numel() for _, _, h, _, _ in ups) + sum(h.numel() for _, _, h in direct))
     db = 8 * sum(h.numel() for _, _, h in downs)
-    up, rb = mean("up0", "up1"), mean("d2h0", "d2h1")
+    up, rb = mean("up0", "ups1") + mean("upt0", "up1"), mean("d2h0", "d2h1")
     timeline = {"unit": "ms per step (means over the timed steps, CUDA events)",
                 "host_wall": round(te * 1e3, 3), "compute_span": round(span, 3), "compute": round(mean("c0", "c1"), 3),
-                "upload": round(up, 3), "readback": round(rb, 3), "staging_to_fields": round(mean("up1", "stg1"), 3),
+                "upload": round(up, 3), "readback": round(rb, 3), "staging_to_fields": round(mean("ups1", "stg1"), 3),
                 "compute_waits_for_inputs": round(wait, 3),
                 "upload_GBps": round(hb / up / 1e6, 1) if up > 0 else None,
                 "readback_GBps": round(db / rb / 1e6, 1) if rb > 0 else None}
@@ -558,15 +567,20 @@ def run_ours(args, rank, world):
 
     e2e = None
     if not args.no_e2e:
-        te, hb, db, timeline = run_e2e(d, stream, wl, ntr, max(3, min(args.steps, 30)))
+        # at least 30 steps: the first step's upload and the last one's read-back, which
+        # nothing can overlap, are spread over a run of steps as in a simulation
+        e2e_steps = min(max(args.steps, 30), 100)
+        te, hb, db, timeline = run_e2e(d, stream, wl, ntr, e2e_steps)
         e2e = {"value": round(cells / te, 1), "unit": "cell-updates/s", "h2d_bytes_per_step": hb,
-               "d2h_bytes_per_step": db, "steps": max(3, min(args.steps, 30)),
-               "api": "mom5gpu_copy_field_async (pinned host buffers, read-back stream), host->staging copies on "
-                      "an upload stream, mom5gpu_copy_boxes (staging->fields) / mom5gpu_tracer_advection_step / "
+               "d2h_bytes_per_step": db, "steps": e2e_steps,
+               "api": "mom5gpu_copy_field_async (pinned host buffers: tracers host->time level on an upload "
+                      "stream, results device->host on a read-back stream), velocity and forcing host->staging "
+                      "then mom5gpu_copy_boxes (staging->fields) / mom5gpu_tracer_advection_step / "
                       "mom5gpu_update_ocean_barotropic",
-               "timing": "host wall clock over the steps, every copy inside; uploads land in device staging "
-                         "buffers beside the previous step's read-back and compute, then are copied into their "
-                         "fields (three time levels rotate)", "timeline": timeline}
+               "timing": "host wall clock over the steps, every copy inside; a step's tracers go straight into "
+                         "the time level it reads (three rotate) once that level's read-back is done, during the "
+                         "previous step's compute; velocity and forcing land in staging buffers and are copied "
+                         "into their fields once the previous step is done with them", "timeline": timeline}
 
     l2note = ("inputs larger than L2 (tracer state alone %.1f GB)" % (2 * ntr * cells * 8 / 1e9)
               if 2 * ntr * cells * 8 > 129e6 else "inputs smaller than L2, not flushed (launch/latency-bound case)")
