@@ -97,6 +97,28 @@ def make_box(kind, u, v, w, ni=30, nj=30, nk=30, dx=8000.0, dy=6000.0, dz=10.0):
     return dom, (dx, dy, dz)
 
 
+# At Courant number 1 in every direction MDFL's limiter and DST3 terms vanish
+# (d0 = d1 = 0, slope (1-cfl)/(1e-30+cfl) = 0): every pass is first-order
+# upwind at Courant number 1 and moves any profile, a random one included,
+# exactly one cell.  dx/0.4 = dy/0.3 = dz/5e-4 = 20000 s.
+CFL1_DT = 20000.0
+CFL1_VELOCITIES = [(0.4, 0.0, 0.0), (0.0, -0.3, 0.0), (0.0, 0.0, 5e-4), (0.4, 0.3, 5e-4), (-0.4, -0.3, -5e-4)]
+
+
+def make_random_box(u, v, w, seed=5):
+    """make_box with a uniform-random tracer; returns (domain, spacing, tracer)."""
+    import torch
+    dom, spacing = make_box("linear", u, v, w)
+    T0 = np.random.default_rng(seed).uniform(0.0, 1.0, size=tuple(dom["T"][0].shape))
+    dom["T"][0].copy_(torch.from_numpy(T0))
+    return dom, spacing, T0
+
+
+def shifted_one_cell(T0, u, v, w):
+    """T0 moved one cell along each non-zero velocity component (k counts down)."""
+    return np.roll(T0, shift=(-int(np.sign(w)), int(np.sign(v)), int(np.sign(u))), axis=(0, 1, 2))
+
+
 def interior(a, margin=8):
     """Cells at least `margin` cells from every boundary."""
     nk, nyd, nxd = a.shape

@@ -43,6 +43,16 @@ def test_drop_in_matches_the_advection_equation(gpu_lib, scheme, kind, vel):
     assert A.rel_err(T, dom["T"][0].numpy()) > 1e-4
 
 
+@pytest.mark.parametrize("vel", [(0.4, 0.3, 5e-4), (-0.4, -0.3, -5e-4)])
+def test_mdfl_at_courant_one_moves_any_field_one_cell(gpu_lib, vel):
+    """Drop-in MDFL at Courant number 1: a random tracer moves exactly one cell."""
+    capi = gpu_lib
+    u, v, w = vel
+    dom, _, T0 = A.make_random_box(u, v, w)
+    T = _step(capi, dom, "mdfl_sweby", A.CFL1_DT)
+    assert abs(A.interior(T) - A.interior(A.shifted_one_cell(T0, u, v, w))).max() < 2e-15
+
+
 @pytest.mark.parametrize("vel", [(0.4, -0.3, 1e-3), (-0.2, 0.25, -2e-3)])
 def test_precision_form_matches_the_advection_equation(gpu_lib, vel):
     capi = gpu_lib

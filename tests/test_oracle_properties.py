@@ -314,6 +314,22 @@ def test_schemes_match_the_advection_equation(O, scheme, kind, vel):
     assert A.rel_err(Tn, dom["T"][0].numpy()) > 1e-4
 
 
+@pytest.mark.parametrize("vel", [(0.4, 0.0, 0.0), (0.0, -0.3, 0.0), (0.0, 0.0, 5e-4), (0.4, 0.3, 5e-4),
+                                 (-0.4, -0.3, -5e-4)])
+def test_mdfl_at_courant_one_moves_any_field_one_cell(O, vel):
+    """At Courant number 1 the Sweby limiter (:3868-3878) and the DST3 terms
+    vanish and each MDFL pass is upwind at Courant number 1: a random tracer
+    moves exactly one cell along each velocity component (tests/analytic.py)."""
+    import analytic as A
+    u, v, w = vel
+    dom, _, T0 = A.make_random_box(u, v, w)
+    g, d = O.domain_arrays(dom), O.dims(dom.spec)
+    T = g["T"][0]
+    dt = A.CFL1_DT
+    Tn = O.update_tracer(d, g, T, O.advect_mdfl_sweby(d, g, T, dt, 1.0), dt)
+    assert np.abs(A.interior(Tn) - A.interior(A.shifted_one_cell(T0, u, v, w))).max() < 2e-15
+
+
 @pytest.mark.parametrize("stepping_B", [False, True])
 def test_barotropic_matches_the_momentum_equation(O, stepping_B):
     """Known answer (tests/analytic.py): with f = 0, no forcing, a flat bottom
