@@ -385,6 +385,22 @@ int mom5gpu_ocean_barotropic_forcing(mom5gpu_domain* d);
  * (total_tracer, ocean_tracer_diag.F90:2380-2415) with a compensated,
  * fixed-order reduction (double-double), written to *out (host). */
 int mom5gpu_global_tracer_content(mom5gpu_domain* d, int n, int level, double* out);
+/* The same content as an exact fixed-point sum, for sums over decomposed
+ * domains that must not depend on the decomposition (the reproducing global
+ * sum of a 2-D block decomposition).  Each column's value (the reference's
+ * k-sum) is truncated to a multiple of 2^-100 and added as an integer, split
+ * into MOM5GPU_FIXED_CHUNKS 32-bit chunks (chunk i weighs 2^(32 i - 100)), each
+ * summed in a signed 64-bit accumulator: acc[MOM5GPU_FIXED_CHUNKS] receives
+ * the domain's accumulators (host).  Integer sums are exact and associative,
+ * so the accumulators of the blocks of a decomposed domain, added element by
+ * element in any order (an integer allreduce between ranks), equal those of
+ * the whole domain.  Up to 2^31 columns per sum; MOM5GPU_ENUMERIC if a column
+ * value is not finite or |value| >= 2^155. */
+#define MOM5GPU_FIXED_CHUNKS 8
+int mom5gpu_tracer_content_fixed(mom5gpu_domain* d, int n, int level, long long* acc);
+/* The double nearest to the value of such accumulators (ties to even).
+ * Needs no device. */
+int mom5gpu_fixed_to_double(const long long* acc, double* out);
 /* Sum of tmask1*dat*eta_t_bar(level), compensated, to *out (host). */
 int mom5gpu_global_eta_integral(mom5gpu_domain* d, int field, int level, double* out);
 /* 1 if any non-finite value is in tracer n (0 = all) at `level`, else 0, to *out. */

@@ -135,6 +135,8 @@ def lib() -> C.CDLL:
             "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
             "mom5gpu_update_ucell_thickness": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
+            "mom5gpu_tracer_content_fixed": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_longlong)]),
+            "mom5gpu_fixed_to_double": (C.c_int, [C.POINTER(C.c_longlong), dp]),
             "mom5gpu_global_eta_integral": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_check_finite": (C.c_int, [vp, C.c_int, C.c_int, ip]),
             "mom5gpu_enable_timing": (C.c_int, [vp, C.c_int]),
@@ -166,6 +168,24 @@ def lib() -> C.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+FIXED_CHUNKS = 8  # MOM5GPU_FIXED_CHUNKS
+
+
+def fixed_to_double(acc) -> float:
+    """The double nearest to a sum of fixed-point content accumulators
+    (mom5gpu_fixed_to_double; no device needed)."""
+    if len(acc) != FIXED_CHUNKS:
+        raise ValueError(f"{FIXED_CHUNKS} accumulators expected")
+    if any(not -(1 << 63) <= int(v) < (1 << 63) for v in acc):
+        raise OverflowError("an accumulator exceeds 64 bits: too many values in one sum")
+    a = (C.c_longlong * FIXED_CHUNKS)(*[int(v) for v in acc])
+    out = C.c_double()
+    st = lib().mom5gpu_fixed_to_double(a, C.byref(out))
+    if st:
+        raise Mom5GpuError(st, "fixed_to_double")
+    return out.value
 
 
 def default_options(**kw) -> Options:
@@ -395,6 +415,14 @@ class Domain:
         out = C.c_double()
         self.check(lib().mom5gpu_global_tracer_content(self.h, n, level, C.byref(out)))
         return out.value
+
+    def tracer_content_fixed(self, n, level) -> list:
+        """The exact fixed-point accumulators of tracer n's content (FIXED_CHUNKS
+        Python ints; add them element by element across blocks, then
+        fixed_to_double)."""
+        acc = (C.c_longlong * FIXED_CHUNKS)()
+        self.check(lib().mom5gpu_tracer_content_fixed(self.h, n, level, acc))
+        return [int(v) for v in acc]
 
     def global_eta_integral(self, field, level) -> float:
         out = C.c_double()

@@ -1058,6 +1058,54 @@ int mom5gpu_global_tracer_content(mom5gpu_domain* d, int n, int level, double* o
   return launch_content(d, n, level, out);
 }
 
+int mom5gpu_tracer_content_fixed(mom5gpu_domain* d, int n, int level, long long* acc) {
+  if (!d || !acc) return MOM5GPU_EINVAL;
+  if (n < 1 || n > d->dims.num_prog_tracers || level < 1 || level > 3)
+    return fail(d, MOM5GPU_EINVAL, "tracer_content_fixed: tracer %d level %d", n, level);
+  return launch_content_fixed(d, n, level, acc);
+}
+
+// Normalise the chunk accumulators into a two's complement integer of 32-bit
+// words (value = X * 2^-100), take its magnitude and round the top bits to 53.
+int mom5gpu_fixed_to_double(const long long* acc, double* out) {
+  if (!acc || !out) return MOM5GPU_EINVAL;
+  constexpr int NC = MOM5GPU_FIXED_CHUNKS, NW = NC + 3;  // words; room for the carries
+  uint32_t w[NW];
+  long long carry = 0;
+  for (int i = 0; i < NW; ++i) {
+    // acc[i] + carry fits: |acc| < 2^63 - 2^32 * 2^31 headroom is the caller's (<= 2^31 values)
+    long long v = (i < NC ? acc[i] : 0) + carry;
+    w[i] = (uint32_t)(v & 0xffffffffLL);
+    carry = (v - (long long)w[i]) / 4294967296LL;  // exact: v - low word is a multiple of 2^32
+  }
+  const bool neg = (w[NW - 1] & 0x80000000u) != 0;
+  if (neg) {  // magnitude: two's complement negation
+    uint64_t c = 1;
+    for (int i = 0; i < NW; ++i) {
+      uint64_t t = (uint64_t)(uint32_t)~w[i] + c;
+      w[i] = (uint32_t)t;
+      c = t >> 32;
+    }
+  }
+  int top = -1;  // highest set bit
+  for (int i = NW - 1; i >= 0 && top < 0; --i)
+    if (w[i]) top = 32 * i + 31 - __builtin_clz(w[i]);
+  if (top < 0) {
+    *out = 0.0;
+    return MOM5GPU_OK;
+  }
+  auto bit = [&](int b) -> unsigned { return b < 0 ? 0u : (w[b >> 5] >> (b & 31)) & 1u; };
+  // 53 significant bits from `top` down, then round to nearest, ties to even
+  uint64_t m = 0;
+  for (int b = top; b > top - 53; --b) m = (m << 1) | bit(b);
+  const int lsb = top - 52;
+  unsigned guard = bit(lsb - 1), sticky = 0;
+  for (int b = lsb - 2; b >= 0 && !sticky; --b) sticky |= bit(b);
+  if (guard && (sticky || (m & 1u))) ++m;  // a carry to 2^53 stays exact in ldexp
+  *out = ldexp((double)m, lsb - 100) * (neg ? -1.0 : 1.0);
+  return MOM5GPU_OK;
+}
+
 int mom5gpu_global_eta_integral(mom5gpu_domain* d, int field, int level, double* out) {
   if (!d || !out) return MOM5GPU_EINVAL;
   const FieldInfo* fi = field_info(field);

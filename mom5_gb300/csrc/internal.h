@@ -274,6 +274,7 @@ int launch_advection_velocity(mom5gpu_domain* d, int tau);
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);
 int grid_barrier_selftest(mom5gpu_domain* d, int rounds, int unreachable);
 int launch_content(mom5gpu_domain* d, int n, int level, double* out_host);
+int launch_content_fixed(mom5gpu_domain* d, int n, int level, long long* acc_host);
 int launch_eta_integral(mom5gpu_domain* d, const double* eta, double* out_host);
 int launch_check_finite(mom5gpu_domain* d, const double* a, size_t count, int* out_host);
 

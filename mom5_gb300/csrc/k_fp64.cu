@@ -2169,6 +2169,93 @@ int launch_content(mom5gpu_domain* d, int n, int level, double* out_host) {
   return MOM5GPU_OK;
 }
 
+// ---- exact fixed-point content (decomposition-independent) ----
+//
+// Each column's content (the same k-sum as k_content) is truncated to a
+// multiple of 2^-kFixFrac and added as an integer, split into kFixChunks
+// 32-bit chunks (chunk i weighs 2^(32 i - kFixFrac)) each summed in a signed
+// 64-bit accumulator.  Integer addition is exact and associative, so any order
+// of summation -- threads, blocks, the blocks of a decomposed domain, ranks of
+// an allreduce -- gives the same accumulators.  Up to 2^31 values per sum;
+// |value| < 2^(32 kFixChunks - kFixFrac) = 2^156, else the overflow flag is set.
+constexpr int kFixChunks = MOM5GPU_FIXED_CHUNKS, kFixFrac = 100;
+
+DEVI void fix_add(long long* acc, double x, int* overflow) {
+  const long long b = bits_of(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0x7ff) {  // Inf or NaN
+    *overflow = 1;
+    return;
+  }
+  const unsigned long long m = (unsigned long long)(b & 0x000fffffffffffffLL) | (ex ? (1ULL << 52) : 0ULL);
+  const int p = (ex ? ex : 1) - 1075 + kFixFrac;  // x = m * 2^(p - kFixFrac)
+  if (m && p + 53 > 32 * kFixChunks) {
+    *overflow = 1;
+    return;
+  }
+  const bool neg = b < 0;
+#pragma unroll
+  for (int i = 0; i < kFixChunks; ++i) {
+    const int sh = 32 * i - p;  // chunk i = bits [sh, sh+32) of m
+    unsigned long long c = 0;
+    if (sh >= 0) c = sh < 64 ? (m >> sh) & 0xffffffffULL : 0ULL;
+    else c = -sh < 32 ? (m << -sh) & 0xffffffffULL : 0ULL;
+    acc[i] += neg ? -(long long)c : (long long)c;
+  }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_content_fixed(Geo g, const double* tmask, const double* dat,
+                                                               const double* rdz, const double* T,
+                                                               unsigned long long* out, int* overflow) {
+  long long acc[kFixChunks] = {};
+  int ovf = 0;
+  long ncol = (long)g.ni * g.nj;
+  for (long c = blockIdx.x * (long)kRedThreads + threadIdx.x; c < ncol; c += (long)gridDim.x * kRedThreads) {
+    int i = (int)(c % g.ni) + 1, j = (int)(c / g.ni) + 1;
+    double col = 0.0;
+    double da = dat[I2(g, i, j)];
+    for (int k = 0; k < g.nk; ++k) {
+      long p = I3(g, i, j, k);
+      double t = tmask[p] != 0.0 ? 1.0 * tmask[p] * da : 0.0;
+      col = col + t * rdz[p] * T[p];
+    }
+    fix_add(acc, col, &ovf);
+  }
+  // integer sums: the warp, then one atomic per chunk and warp (two's complement
+  // addition modulo 2^64 is exact while the true sum fits)
+#pragma unroll
+  for (int q = 0; q < kFixChunks; ++q) {
+    long long v = acc[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&out[q], (unsigned long long)v);
+  }
+  if (ovf) atomicOr(overflow, 1);
+}
+
+int launch_content_fixed(mom5gpu_domain* d, int n, int level, long long* acc_host) {
+  int rc = ensure_red(d);
+  if (rc) return rc;
+  const Geo& g = d->geo;
+  const double* tmask = fptr(d, MOM5GPU_TMASK, 0, 0);
+  const double* dat = fptr(d, MOM5GPU_DAT, 0, 0);
+  const double* rdz = fptr(d, MOM5GPU_RHO_DZT, 0, level);
+  const double* T = fptr(d, MOM5GPU_TRACER, n, level);
+  if (!tmask || !dat || !rdz || !T) return fail(d, MOM5GPU_ESTATE, "content: a required field was never set");
+  // accumulators and the overflow flag in the reduction scratch (2*kRedBlocks + 8 doubles)
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(d->red);
+  int* ovf = reinterpret_cast<int*>(acc + kFixChunks);
+  cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * (kFixChunks + 1), d->stream);
+  k_content_fixed<<<kRedBlocks, kRedThreads, 0, d->stream>>>(g, tmask, dat, rdz, T, acc, ovf);
+  long long hbuf[kFixChunks + 1];
+  cudaMemcpyAsync(hbuf, acc, sizeof(long long) * (kFixChunks + 1), cudaMemcpyDeviceToHost, d->stream);
+  cudaError_t e = cudaStreamSynchronize(d->stream);
+  if (e != cudaSuccess) return cuda_fail(d, e, "fixed-point content");
+  if ((int)hbuf[kFixChunks])
+    return fail(d, MOM5GPU_ENUMERIC, "fixed-point content: a column value is not finite or exceeds 2^155");
+  for (int q = 0; q < kFixChunks; ++q) acc_host[q] = hbuf[q];
+  return MOM5GPU_OK;
+}
+
 int launch_eta_integral(mom5gpu_domain* d, const double* eta, double* out_host) {
   int rc = ensure_red(d);
   if (rc) return rc;

@@ -233,6 +233,11 @@ class LocalExchange:
         capi.copy_boxes(boxes, self.stream)
 
 
+def add_fixed(a, b):
+    """Element-by-element sum of two fixed-point accumulator lists (exact)."""
+    return [int(x) + int(y) for x, y in zip(a, b)]
+
+
 class RankExchange:
     """One block per process of a torch.distributed group (rank r = block r):
     each region goes through a contiguous buffer, isend / irecv with the
@@ -281,6 +286,16 @@ class RankExchange:
         for recv_reg, buf in landed:
             self.unpack(key, recv_reg, buf)
 
+    def allreduce_fixed(self, acc):
+        """Sum fixed-point accumulators over the ranks: an integer allreduce,
+        exact and independent of the reduction order, so every rank gets the
+        whole domain's accumulators."""
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([int(v) for v in acc], dtype=torch.int64)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=self.group)
+        return [int(v) for v in t.tolist()]
+
 
 # ----------------------------------------------------------------------------- stepping
 class Decomposed:
@@ -309,6 +324,18 @@ class Decomposed:
             d.mdfl_pass(3, taum1, tau, dtime)
             d.update_tracer(0, taum1, taup1, dtime)
         self.ex.exchange(HALO_FIELD, capi.F.TRACER, 0, taup1)
+
+    def global_tracer_content(self, n: int, level: int) -> float:
+        """Global content of tracer n over every block: the blocks' exact
+        fixed-point accumulators added (and summed over the ranks when the
+        exchanger has ranks), rounded once -- the same double for every
+        decomposition of the domain, the undecomposed one included."""
+        acc = [0] * capi.FIXED_CHUNKS
+        for d in self.blocks:
+            acc = add_fixed(acc, d.tracer_content_fixed(n, level))
+        if hasattr(self.ex, "allreduce_fixed"):
+            acc = self.ex.allreduce_fixed(acc)
+        return capi.fixed_to_double(acc)
 
     def update_ocean_barotropic(self, tau: int, taup1: int):
         """update_ocean_barotropic (B grid, FP64), decomposed: a halo update of

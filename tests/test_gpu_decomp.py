@@ -66,6 +66,11 @@ def test_decomposed_steps_equal_one_domain(gpu_lib, px, py, cx, cy, sweby_all):
             ref = one.get(fid).reshape(got.shape)
             inner = (Ellipsis, slice(1, -1), slice(1, -1))
             assert equal(got[inner], ref[inner]), f"step {step} field {fid}"
+        # the reproducing global sum: the same double for the blocks as for the whole domain
+        for n in range(1, sp.ntracers + 1):
+            whole = capi.fixed_to_double(one.tracer_content_fixed(n, taup1))
+            assert dec.global_tracer_content(n, taup1) == whole
+            assert abs(whole - one.global_tracer_content(n, taup1)) <= 1e-15 * abs(whole)
         tau = taup1
     for d in blocks:
         d.close()
@@ -83,4 +88,32 @@ def test_block_refuses_cyclic_and_wide_tracer_sets(gpu_lib):
     with pytest.raises(capi.Mom5GpuError) as e:
         d.set_neighbours(1, 1, 0, 0)
     assert e.value.status == capi.EUNSUPPORTED
+    d.close()
+
+
+def test_fixed_content_is_the_exact_sum_of_the_columns(gpu_lib):
+    """mom5gpu_tracer_content_fixed: the accumulators hold exactly the sum of
+    each column's content (the reference's k-sum, total_tracer,
+    ocean_tracer_diag.F90:2380-2415, formed here with numpy in the same
+    order) truncated to a multiple of 2^-100."""
+    from fractions import Fraction
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    sp = grid.DomainSpec(ni=45, nj=31, nk=12, lon0=0.0, lon1=45.0, lat0=-30.0, lat1=30.0, cyclic_x=True,
+                         continent=(11, 8, 6, 5), wavelength_cells=6.0, ntracers=2, seed=77)
+    dom = grid.make_domain(sp)
+    d = harness.load(dom)
+    tm, dat, rdz = dom["tmask"].numpy(), dom["dat"].numpy(), dom["rho_dzt"].numpy()
+    for n in (1, 2):
+        T = dom["T"][n - 1].numpy()
+        col = np.zeros((sp.nj, sp.ni))
+        da = dat[1:-1, 1:-1]
+        for k in range(sp.nk):
+            m = tm[k, 1:-1, 1:-1]
+            t = np.where(m != 0.0, (1.0 * m) * da, 0.0)
+            col = col + (t * rdz[k, 1:-1, 1:-1]) * T[k, 1:-1, 1:-1]
+        want = sum(int(Fraction(float(c)) * (1 << 100)) for c in col.ravel())
+        acc = d.tracer_content_fixed(n, 1)
+        assert sum(a << (32 * i) for i, a in enumerate(acc)) == want
+        assert capi.fixed_to_double(acc) == float(Fraction(want, 1 << 100))
     d.close()
