@@ -48,6 +48,7 @@ module mom5gpu_c
        F_DZTEN_E = 136, F_DZTEN_N = 137, F_DEPTH_ZT = 138, F_DEPTH_ZWT = 139, F_DEPTH_ZU = 140, &
        F_DEPTH_ZWU = 141, F_MASS_U = 142, F_MASS_EN_E = 143, F_MASS_EN_N = 144
   integer(c_int), parameter :: MOM5GPU_ADVECT_PSOM = 11
+  integer, parameter :: MOM5GPU_FIXED_CHUNKS = 8
 
   type, bind(C) :: mom5gpu_dims
      integer(c_int) :: ni, nj, nk, cyclic_x, cyclic_y, num_prog_tracers, horz_grid
@@ -228,6 +229,18 @@ module mom5gpu_c
        integer(c_int), value :: n, level
        real(c_double), intent(out) :: total
      end function
+     integer(c_int) function mom5gpu_tracer_content_fixed(dom, n, level, acc) &
+          bind(C, name="mom5gpu_tracer_content_fixed")
+       import :: c_int, c_ptr, c_long_long, MOM5GPU_FIXED_CHUNKS
+       type(c_ptr), value :: dom
+       integer(c_int), value :: n, level
+       integer(c_long_long), intent(out) :: acc(MOM5GPU_FIXED_CHUNKS)
+     end function
+     integer(c_int) function mom5gpu_fixed_to_double(acc, total) bind(C, name="mom5gpu_fixed_to_double")
+       import :: c_int, c_long_long, c_double, MOM5GPU_FIXED_CHUNKS
+       integer(c_long_long), intent(in) :: acc(MOM5GPU_FIXED_CHUNKS)
+       real(c_double), intent(out) :: total
+     end function
   end interface
 end module mom5gpu_c
 
@@ -239,7 +252,7 @@ module mom5gpu_mod
   ! and ocean_barotropic_mod.
   use, intrinsic :: iso_c_binding
   use mom5gpu_c
-  use mpp_mod,          only: mpp_error, FATAL
+  use mpp_mod,          only: mpp_error, FATAL, mpp_sum
   use ocean_types_mod,  only: ocean_time_type, ocean_adv_vel_type, ocean_thickness_type, ocean_density_type, &
                               ocean_prog_tracer_type, ocean_external_mode_type, ocean_velocity_type, &
                               ocean_lagrangian_type, ocean_grid_type
@@ -250,7 +263,7 @@ module mom5gpu_mod
   public :: horz_advect_tracer, vert_advect_tracer
   public :: update_ocean_barotropic, eta_and_pbot_tendency, eta_and_pbot_update
   public :: ocean_advection_velocity, ocean_barotropic_forcing, device_restart_write
-  public :: update_ucell_thickness, device_thickness_options
+  public :: update_ucell_thickness, device_thickness_options, device_total_tracer
 
   ! ocean_thickness_nml switches and the vertical coordinate (ocean_parameters.F90:107-112)
   ! used by update_ucell_thickness; set once by the host driver
@@ -275,6 +288,22 @@ contains
        call mpp_error(FATAL, 'mom5gpu ('//where//'): '//trim(msg(1:index(msg, c_null_char)-1)))
     endif
   end subroutine check
+
+  ! total_tracer (ocean_tracer_diag.F90:2380-2415) of prognostic tracer n at
+  ! time level `index`, the same on any processor count (the role of
+  ! BITWISE_EXACT_SUM): each PE's device forms its exact fixed-point column
+  ! sums, the integer accumulators are summed over the PEs (mpp_sum of
+  ! integer(8), exact) and rounded once.
+  function device_total_tracer(n, index) result(total)
+    integer, intent(in) :: n, index
+    real :: total
+    integer(c_long_long) :: acc(MOM5GPU_FIXED_CHUNKS)
+    real(c_double) :: t
+    call check(mom5gpu_tracer_content_fixed(dom, int(n, c_int), int(index, c_int), acc), 'total_tracer')
+    call mpp_sum(acc, MOM5GPU_FIXED_CHUNKS)
+    call check(mom5gpu_fixed_to_double(acc, t), 'total_tracer')
+    total = t
+  end function device_total_tracer
 
   ! Called once from ocean_model_init after the grid and the first state exist:
   ! takes ownership of the device domain created by the host driver.
