@@ -42,8 +42,20 @@ void field_region(const mom5gpu_dims& dm, int nlev, int side, int role, long* of
   n[2] = nlev;
 }
 
-__global__ void k_copy_boxes(const mom5gpu_box* __restrict__ boxes) {
-  const mom5gpu_box b = boxes[blockIdx.y];
+// The boxes of one launch travel in the launch's own parameter block, by value:
+// no table is uploaded, so the launch needs no copy engine (those stay with the
+// host link, where a small upload would queue behind gigabytes of field copies)
+// and the host never waits for an earlier launch to free a table.
+template <int N>
+struct BoxSet {
+  mom5gpu_box b[N];
+};
+constexpr int kBoxesSmall = 8, kBoxesPerLaunch = 256;  // 640 B and 20 KB of parameters
+static_assert(sizeof(BoxSet<kBoxesPerLaunch>) <= 32000, "kernel parameters are limited to 32764 bytes");
+
+template <int N>
+__global__ void k_copy_boxes(const __grid_constant__ BoxSet<N> set) {
+  const mom5gpu_box& b = set.b[blockIdx.y];
   const long nx = b.n[0], nxy = nx * b.n[1], total = nxy * b.n[2];
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
     const long z = e / nxy, r = e - z * nxy, y = r / nx, x = r - y * nx;
@@ -52,22 +64,16 @@ __global__ void k_copy_boxes(const mom5gpu_box* __restrict__ boxes) {
   }
 }
 
-// boxes of one launch: kernel parameters by value are limited, so the boxes go
-// through device tables uploaded from pinned staging; a ring of tables lets the
-// host queue many exchanges ahead of the GPU (a table is reused once the launch
-// that read it has run)
-constexpr int kBoxesPerLaunch = 256, kTables = 32;
-struct BoxTable {
-  mom5gpu_box* dev = nullptr;
-  mom5gpu_box* host = nullptr;
-  cudaEvent_t free_ev = nullptr;
-};
-struct BoxRing {
-  BoxTable t[kTables];
-  int next = 0;
-  bool ready = false;
-};
-thread_local BoxRing g_ring;
+template <int N>
+cudaError_t launch_boxes(const mom5gpu_box* boxes, int nb, long most, cudaStream_t s) {
+  BoxSet<N> set;
+  memset(&set, 0, sizeof(set));
+  memcpy(set.b, boxes, sizeof(mom5gpu_box) * nb);
+  unsigned bx = (unsigned)((most + 255) / 256);
+  if (bx > 1024) bx = 1024;
+  k_copy_boxes<N><<<dim3(bx, nb), 256, 0, s>>>(set);
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -213,19 +219,7 @@ int mom5gpu_halo_base(mom5gpu_domain* d, int kind, int field, int n, int level, 
 int mom5gpu_copy_boxes(const mom5gpu_box* boxes, int count, void* stream) {
   if (count < 0 || (count > 0 && !boxes)) return MOM5GPU_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  BoxRing& ring = g_ring;
-  if (!ring.ready) {
-    for (BoxTable& t : ring.t) {
-      cudaError_t e = cudaMalloc(&t.dev, sizeof(mom5gpu_box) * kBoxesPerLaunch);
-      if (e == cudaSuccess) e = cudaMallocHost(&t.host, sizeof(mom5gpu_box) * kBoxesPerLaunch);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.free_ev, cudaEventDisableTiming);
-      if (e != cudaSuccess) return fail(nullptr, MOM5GPU_ENOMEM, "copy_boxes: %s", cudaGetErrorString(e));
-    }
-    ring.ready = true;
-  }
   for (int b0 = 0; b0 < count; b0 += kBoxesPerLaunch) {
-    BoxTable& t = ring.t[ring.next];
-    ring.next = (ring.next + 1) % kTables;
     int nb = count - b0 < kBoxesPerLaunch ? count - b0 : kBoxesPerLaunch;
     long most = 1;
     for (int b = 0; b < nb; ++b) {
@@ -235,18 +229,8 @@ int mom5gpu_copy_boxes(const mom5gpu_box* boxes, int count, void* stream) {
       long e = (long)x.n[0] * x.n[1] * x.n[2];
       if (e > most) most = e;
     }
-    // this table's previous launch must have read it
-    cudaError_t e = cudaEventSynchronize(t.free_ev);
-    if (e != cudaSuccess) return fail(nullptr, MOM5GPU_ECUDA, "copy_boxes: %s", cudaGetErrorString(e));
-    memcpy(t.host, boxes + b0, sizeof(mom5gpu_box) * nb);
-    e = cudaMemcpyAsync(t.dev, t.host, sizeof(mom5gpu_box) * nb, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) {
-      unsigned bx = (unsigned)((most + 255) / 256);
-      if (bx > 1024) bx = 1024;
-      k_copy_boxes<<<dim3(bx, nb), 256, 0, s>>>(t.dev);
-      e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaEventRecord(t.free_ev, s);
+    cudaError_t e = nb <= kBoxesSmall ? launch_boxes<kBoxesSmall>(boxes + b0, nb, most, s)
+                                      : launch_boxes<kBoxesPerLaunch>(boxes + b0, nb, most, s);
     if (e != cudaSuccess) return fail(nullptr, MOM5GPU_ECUDA, "copy_boxes: %s", cudaGetErrorString(e));
   }
   return MOM5GPU_OK;
