@@ -325,7 +325,10 @@ int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
  * that gives up is reported by mom5gpu_synchronize as MOM5GPU_ETIMEDOUT; inside
  * a stream capture the three launches are used).  Forms 1 and 2 were slower
  * than 0 on every measured domain.  Every form gives the same results bit for
- * bit. */
+ * bit.  A domain in the precision form (MOM5GPU_PRECISION_MIXED) has forms 0
+ * and 1 of its own subcycle (mode 2 runs form 0): form 1 was faster on a
+ * 360x300 domain, where the launches set the time, and slower on 1440x1080;
+ * both give the same bits. */
 int mom5gpu_set_barotropic_fusion(mom5gpu_domain* d, int mode);
 /* Self-test of the grid barrier of the cooperative subcycle launch: `rounds`
  * (1..100000) barriers over a full resident grid, after each of which every

@@ -203,7 +203,7 @@ struct BtArgs {
 };
 // planes of barotropic scratch: 18 for the exact path (the reused divergence in
 // two planes for the one-launch subcycle), 9 more for the precision form
-constexpr int kBtPlanes = 18, kBtFastPlanes = 9;
+constexpr int kBtPlanes = 18, kBtFastPlanes = 10;
 struct BtExtra {
   const double *eta_bar_tau, *eta_tau, *ud_tau, *vd_tau, *pme, *river, *source, *eta_smooth;
   double *conv, *eta_u, *ps_out, *gxo, *gyo;
@@ -260,7 +260,7 @@ int launch_eta_tendency(mom5gpu_domain* d, int tau);
 int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
 // precision-form barotropic subcycle (k_mixed.cu, k_batch.cu)
 void launch_btf_prep(const BtArgs& a, cudaStream_t s);
-void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, bool reuse, cudaStream_t s);
+int launch_btf_subcycle(const BtArgs& a, int itime, int nts, bool fused, cudaStream_t s);
 int launch_centred(mom5gpu_domain* d, int n, int tau, int order, bool horz);
 int ensure_kmt_device(mom5gpu_domain* d);
 int launch_mdfl_sup_b(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
@@ -304,8 +304,7 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
                                   cudaStream_t s);
 // precision form: folded subcycle over the work list (k_batch.cu)
 void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s);
-void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, bool reuse,
-                               cudaStream_t s);
+int launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int itime, int nts, cudaStream_t s);
 void launch_batch_barotropic_post(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, int phase,
                                   cudaStream_t s);
 // precision form: persistent kernel over (entry, tile) items

@@ -66,6 +66,10 @@ __global__ void __launch_bounds__(128) kb_btf_corr(const BtArgs* d, BatchWork w,
   BTF_ENTRY
   btfast::corr_body(a, so, sn, wgt, bx, by);
 }
+__global__ void __launch_bounds__(128) kb_btf_corr_pred(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+  BTF_ENTRY
+  btfast::corr_pred_body(a, so, sn, wgt, bx, by);
+}
 
 template <int NC, int ZR>
 int configure() {
@@ -97,12 +101,18 @@ void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s)
   if (w.tb2 > 0) kb_btf_prep<<<w.tb2, 128, 0, s>>>(bt, w);
 }
 
-void launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int so, int sn, double wgt, bool reuse,
-                               cudaStream_t s) {
-  if (w.tb2 <= 0) return;
-  kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, reuse);
+// subcycle itime of nts, as the one-domain form 0: the predictor launched only in
+// the first subcycle, the corrector forming the next subcycle's predictor in all
+// but the last; returns the launches
+int launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int itime, int nts, cudaStream_t s) {
+  if (w.tb2 <= 0) return 0;
+  const int so = itime % 2, sn = (itime + 1) % 2;
+  const double wgt = (double)(nts - itime + 1);
+  if (itime == 1) kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, 0);
   kb_btf_mom<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
-  kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
+  if (itime < nts) kb_btf_corr_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
+  else kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
+  return itime == 1 ? 3 : 2;
 }
 
 int prepare_batch_mixed() {

@@ -158,7 +158,7 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
   for (int itime = 1; itime <= nts; ++itime) {
     int so = (itime + 0) % 2, sn = (itime + 1) % 2;
     if (fast) {  // precision form: folded FP64 subcycle
-      launch_batch_btf_subcycle(bt, w, so, sn, (double)(nts - itime + 1), itime > 1, s);
+      launch_batch_btf_subcycle(bt, w, itime, nts, s);
       continue;
     }
     kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, itime > 1);

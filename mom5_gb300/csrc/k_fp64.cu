@@ -1392,7 +1392,8 @@ static int launch_bt_coop(mom5gpu_domain* d, const BtArgs& a, cudaStream_t s) {
 // hide the FP64 latency better, and a grid barrier across about a thousand
 // blocks costs as much as a launch gap of the graph replay.
 static int bt_form(const mom5gpu_domain* d, const BtArgs& a) {
-  if (a.cgrid || a.btf) return 0;
+  if (a.cgrid) return 0;
+  if (a.btf) return d->bt_fused == 1 ? 1 : 0;  // the precision form has no cooperative form
   return d->bt_fused;
 }
 static bool capturing(cudaStream_t s) {
@@ -1573,8 +1574,10 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   const int form = bt_form(d, a);
   const bool coop = form == 2 && !capturing(s);
   const bool fused = form == 1;
-  count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) +
-                        (coop ? 1 : (long)a.nts * (fused ? 1 : 3 + (a.cgrid ? 2 * halo : 0))) + 4 + 5 * halo);
+  const long sub_launches = coop    ? 1
+                            : a.btf ? (fused ? (long)a.nts : 1 + 2L * a.nts)
+                                    : (long)a.nts * (fused ? 1 : 3 + (a.cgrid ? 2 * halo : 0));
+  count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) + sub_launches + 4 + 5 * halo);
   k_bt_init<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, src,
                                                           esm, d->opt.initsum_with_bar);
   dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
@@ -1591,7 +1594,7 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
     for (int itime = 1; itime <= a.nts; ++itime) {
       int so = (itime + 0) % 2, sn = (itime + 1) % 2;
       if (a.btf) {  // precision form: FP32 increments
-        launch_btf_subcycle(a, so, sn, (double)(a.nts - itime + 1), itime > 1, st);
+        launch_btf_subcycle(a, itime, a.nts, fused, st);
         continue;
       }
       if (fused) {  // predictor, momentum and corrector in one launch

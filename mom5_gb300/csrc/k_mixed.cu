@@ -84,17 +84,46 @@ __global__ void __launch_bounds__(128) k_btf_mom(BtArgs a, int so, int sn) {
 __global__ void __launch_bounds__(128) k_btf_corr(BtArgs a, int so, int sn, double wgt) {
   btfast::corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
 }
+__global__ void __launch_bounds__(128) k_btf_corr_pred(BtArgs a, int so, int sn, double wgt) {
+  btfast::corr_pred_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
+}
 
 void launch_btf_prep(const BtArgs& a, cudaStream_t s) {
   dim3 g2((a.g.ni + 2 + 127) / 128, a.g.nj + 2);
   k_btf_prep<<<g2, 128, 0, s>>>(a);
 }
 
-void launch_btf_subcycle(const BtArgs& a, int so, int sn, double wgt, bool reuse, cudaStream_t s) {
+// One launch per subcycle (mom5gpu_set_barotropic_fusion mode 1): 32 x 8 tiles of
+// 352 threads, one point per thread in each phase (the 34 x 10 surface-pressure
+// ring is the largest).  Measured per precision-form step: 0.62 ms against 0.81
+// ms for the three launches on 360x300 (80 subcycles), where the launches set the
+// time, but 6.7 ms against 5.0 ms on 1440x1080 (60 subcycles), which the three
+// streaming launches keep near the memory bound.  On 360x300 the 64 x 8 (256
+// threads, several points per thread), 32 x 16, 128 x 4 and 64 x 16 tiles took
+// 0.81-1.01 ms.
+constexpr int kBtfTX = 32, kBtfTY = 8, kBtfThreads = 352;
+__global__ void __launch_bounds__(kBtfThreads) k_btf_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
+  btfast::fused_body<kBtfTX, kBtfTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
+}
+
+// Subcycle itime of nts.  Form 0: the predictor (a launch of its own only in the
+// first subcycle), the momentum step, and the corrector, which in every
+// subcycle but the last also forms the next subcycle's predictor; 1 + 2*nts
+// launches per step.  Form 1: one launch per subcycle.  Returns the launches.
+int launch_btf_subcycle(const BtArgs& a, int itime, int nts, bool fused, cudaStream_t s) {
+  const int so = itime % 2, sn = (itime + 1) % 2;
+  const double wgt = (double)(nts - itime + 1);
+  if (fused) {
+    dim3 gf((a.g.ni + 2 + kBtfTX - 1) / kBtfTX, (a.g.nj + 2 + kBtfTY - 1) / kBtfTY);
+    k_btf_fused<<<gf, kBtfThreads, 0, s>>>(a, so, sn, itime > 1, wgt);
+    return 1;
+  }
   dim3 g2((a.g.ni + 2 + 127) / 128, a.g.nj + 2);
-  k_btf_pred<<<g2, 128, 0, s>>>(a, so, sn, reuse);
+  if (itime == 1) k_btf_pred<<<g2, 128, 0, s>>>(a, so, sn, 0);
   k_btf_mom<<<g2, 128, 0, s>>>(a, so, sn);
-  k_btf_corr<<<g2, 128, 0, s>>>(a, so, sn, wgt);
+  if (itime < nts) k_btf_corr_pred<<<g2, 128, 0, s>>>(a, so, sn, wgt);
+  else k_btf_corr<<<g2, 128, 0, s>>>(a, so, sn, wgt);
+  return itime == 1 ? 3 : 2;
 }
 
 int make_mix_args(mom5gpu_domain* d, int taum1, int tau, int taup1, double dtime, MixArgs* ap) {

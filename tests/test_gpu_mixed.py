@@ -208,3 +208,41 @@ def test_precision_form_barotropic_is_fp64_accurate(gpu_lib, oracle_lib, cyclic_
             d.set(fid, np.ascontiguousarray(out[k]), level=taup1)
         tau = taup1
     print(f"precision-form barotropic: worst relative error {worst:.2e}")
+
+
+@pytest.mark.parametrize("cyclic_x,cyclic_y,stepping_B", [(True, False, True), (False, False, False),
+                                                         (True, True, True), (False, True, False)])
+def test_precision_form_barotropic_one_launch_equals_three(gpu_lib, cyclic_x, cyclic_y, stepping_B):
+    """The precision-form subcycle as one launch per subcycle (each 64x8 tile
+    recomputing the surface pressure and transports of its ring) gives the same
+    bits as the three launches per subcycle, on a domain of several tiles with
+    partial ones, over three baroclinic steps, also when the form changes
+    between steps."""
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    sp = grid.DomainSpec(ni=150, nj=29, nk=1, lon0=0.0, lon1=150.0, lat0=-55.0, lat1=55.0, cyclic_x=cyclic_x,
+                         cyclic_y=cyclic_y, hmin=None, ridge_amp=1200.0, ntracers=0, seed=73,
+                         continent=None if cyclic_y else (40, 8, 9, 6))
+    dom = grid.make_domain(sp)
+    per_level = (capi.F.ETA_T_BAR, capi.F.UDRHO_U, capi.F.UDRHO_V, capi.F.CONV_RHO_UD_T, capi.F.ETA_U)
+    names = per_level + (capi.F.PS, capi.F.GRAD_PS_X, capi.F.GRAD_PS_Y)
+    outs = {}
+    for forms in ((0, 0, 0), (1, 1, 1), (1, 0, 1)):
+        opts = capi.default_options(barotropic_time_stepping_A=int(not stepping_B),
+                                    barotropic_time_stepping_B=int(stepping_B), precision=capi.PRECISION_MIXED)
+        d = harness.load(dom, options=opts)
+        d.barotropic_init(dtuv=600.0, dtbt=30.0)
+        tau, got = 1, []
+        for mode in forms:
+            d.set_barotropic_fusion(mode)
+            d.update_ocean_barotropic(tau, 3 - tau)
+            tau = 3 - tau
+            got.append([d.get(f, level=tau) if f in per_level else d.get(f) for f in names])
+        d.close()
+        outs[forms] = got
+    ref = outs[(0, 0, 0)]
+    assert np.abs(ref[-1][0]).max() > 0 and np.abs(ref[-1][1]).max() > 0
+    for forms in ((1, 1, 1), (1, 0, 1)):
+        for step in range(3):
+            for f, a, b in zip(names, outs[forms][step], ref[step]):
+                assert np.array_equal(a, b), f"forms {forms} step {step} field {f}: max diff {np.abs(a - b).max()}"
