@@ -184,7 +184,7 @@ int enqueue_step(mom5gpu_batch* b, const BatchWork& w, const std::vector<std::pa
   }
   launch_batch_barotropic_loop(b->d_bt, b->d_btx, w, b->nts, b->stepB, b->prec == MOM5GPU_PRECISION_MIXED, s);
   launch_batch_barotropic_post(b->d_bt, b->d_btx, w, b->nts, b->stepB, 1, s);
-  launches += 2 + (b->prec == MOM5GPU_PRECISION_MIXED ? 2 + 2L * b->nts : 3L * b->nts);
+  launches += 2 + (b->prec == MOM5GPU_PRECISION_MIXED ? 2 + 2L * b->nts : 1 + 2L * b->nts);
   auto fill = [&](int field) {
     for (auto& it : list) {
       mom5gpu_domain* d = b->doms[it.first];

@@ -633,6 +633,66 @@ DEVI void bt_corr_body(BtArgs a, int so, int sn, double wgt, int bx, int by) {
   }
 }
 
+// B grid: the corrector of subcycle t and the predictor of subcycle t+1 in one
+// pass.  With reuse the predictor of a point reads only the divergence and the
+// corrected eta of that point (or, for a halo point in a periodic direction, of
+// its image), so the thread of a point forms the next surface pressure from the
+// values it has just computed, and the thread of a compute point also forms it
+// at the periodic halo points whose image it is.  The predicted eta is not
+// stored (the next corrector overwrites it unread), nor is the divergence.  The
+// operations are bt_corr_body's and bt_pred_body's, so the bits are theirs.
+DEVI void bt_corr_pred_body(BtArgs a, int so, int sn, double wgt, int bx, int by) {
+  const Geo& g = a.g;
+  int i = bx * blockDim.x + threadIdx.x;
+  int j = by;
+  if (i > g.ni + 1) return;
+  const long n2 = g.n2;
+  long q = I2(g, i, j);
+  double dv = div_ud_bh(a, a.uhb + sn * n2, a.vhb + sn * n2, i, j);
+  double tm = a.tmask1[q];
+  double tmp = is_zero(tm) ? 0.0 : mask_mul(-dv, tm);
+  const double st = tmp + a.steady[q];
+  double en = a.eta_bt[so * n2 + q] + a.dtbt_rho0r * st;
+  a.eta_bt[sn * n2 + q] = en;
+  a.eta_bar[q] = a.eta_bar[q] + en;
+  double un = a.ubt[sn * n2 + q], vn = a.vbt[sn * n2 + q];
+  if (a.stepB) {
+    a.udrho_u[q] = a.udrho_u[q] + wgt * un;
+    a.udrho_v[q] = a.udrho_v[q] + wgt * vn;
+  } else {
+    a.udrho_u[q] = a.udrho_u[q] + un;
+    a.udrho_v[q] = a.udrho_v[q] + vn;
+  }
+  // the next subcycle's predictor (bt_pred_body with reuse)
+  const double ep = dpos(a.gamma) ? en + a.dtbt_gamma_rho0r * st : en;
+  int ii = i, jj = j;
+  if (!halo_image(g, ii, jj) || (ii == i && jj == j)) a.ps[q] = a.rho_g[q] * ep + a.patm[q];
+  if (i < 1 || i > g.ni || j < 1 || j > g.nj) return;
+  int hx[2], nhx = 0, hy[2], nhy = 0;  // periodic halo points whose image this is
+  if (g.cx) {
+    if (i == g.ni) hx[nhx++] = 0;
+    if (i == 1) hx[nhx++] = g.ni + 1;
+  }
+  if (g.cy) {
+    if (j == g.nj) hy[nhy++] = 0;
+    if (j == 1) hy[nhy++] = g.nj + 1;
+  }
+  for (int u = 0; u < nhx; ++u) {
+    const long r = I2(g, hx[u], j);
+    a.ps[r] = a.rho_g[r] * ep + a.patm[r];
+  }
+  for (int v = 0; v < nhy; ++v) {
+    const long r = I2(g, i, hy[v]);
+    a.ps[r] = a.rho_g[r] * ep + a.patm[r];
+  }
+  if (g.cx && g.cy)
+    for (int u = 0; u < nhx; ++u)
+      for (int v = 0; v < nhy; ++v) {
+        const long r = I2(g, hx[u], hy[v]);
+        a.ps[r] = a.rho_g[r] * ep + a.patm[r];
+      }
+}
+
 // One whole B-grid subcycle -- predictor, momentum, corrector -- in one launch
 // on a tile of TX x TY data-domain points: the predictor's surface pressure on
 // the tile and a ring of one (west and south one wider, east and north the

@@ -92,6 +92,10 @@ __global__ void __launch_bounds__(128) kb_bt_corr(const BtArgs* d, BatchWork w, 
   BT2D_ENTRY
   bt_corr_body(a, so, sn, wgt, bx, by);
 }
+__global__ void __launch_bounds__(128) kb_bt_corr_pred(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+  BT2D_ENTRY
+  bt_corr_pred_body(a, so, sn, wgt, bx, by);
+}
 __global__ void __launch_bounds__(256) kb_bt_post1(const BtArgs* d, BatchWork w, double rntsp1, double rnts) {
   int e = find_entry(w.pb1, w.count, blockIdx.x);
   const BtArgs& a = d[w.entries[e]];
@@ -161,9 +165,11 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
       launch_batch_btf_subcycle(bt, w, itime, nts, s);
       continue;
     }
-    kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, itime > 1);
+    // as the one-domain form: the predictor launched only in the first subcycle
+    if (itime == 1) kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, 0);
     kb_bt_mom_b<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
-    kb_bt_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));
+    if (itime < nts) kb_bt_corr_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));
+    else kb_bt_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));
   }
   (void)stepB;
 }

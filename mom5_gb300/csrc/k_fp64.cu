@@ -1260,6 +1260,9 @@ __global__ void k_bt_pred(BtArgs a, int so, int sn, int reuse) { bt_pred_body(a,
 __global__ void k_bt_mom_b(BtArgs a, int so, int sn) { bt_mom_b_body(a, so, sn, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_mom_c(BtArgs a, int so, int sn, int itime) { bt_mom_c_body(a, so, sn, itime, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) { bt_corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_corr_pred(BtArgs a, int so, int sn, double wgt) {
+  bt_corr_pred_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
+}
 constexpr int kFusedTX = 64, kFusedTY = 8;
 __global__ void __launch_bounds__(256) k_bt_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
   bt_fused_body<kFusedTX, kFusedTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
@@ -1574,9 +1577,10 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
   const int form = bt_form(d, a);
   const bool coop = form == 2 && !capturing(s);
   const bool fused = form == 1;
-  const long sub_launches = coop    ? 1
-                            : a.btf ? (fused ? (long)a.nts : 1 + 2L * a.nts)
-                                    : (long)a.nts * (fused ? 1 : 3 + (a.cgrid ? 2 * halo : 0));
+  const long sub_launches = coop      ? 1
+                            : fused   ? (long)a.nts
+                            : a.cgrid ? (long)a.nts * (3 + 2 * halo)
+                                      : 1 + 2L * a.nts;
   count_launches(d, 1 + (a.cgrid ? 1 : 0) + (a.btf ? 1 : 0) + sub_launches + 4 + 5 * halo);
   k_bt_init<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, src,
                                                           esm, d->opt.initsum_with_bar);
@@ -1601,14 +1605,19 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
         k_bt_fused<<<gf, 256, 0, st>>>(a, so, sn, itime > 1, (double)(a.nts - itime + 1));
         continue;
       }
-      k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, itime > 1);
       if (!a.cgrid) {
+        // B grid: the predictor as a launch of its own only in the first
+        // subcycle; every corrector but the last forms the next predictor
+        if (itime == 1) k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, 0);
         k_bt_mom_b<<<g2, 128, 0, st>>>(a, so, sn);
-      } else {
-        k_bt_mom_c<<<g2, 128, 0, st>>>(a, so, sn, itime);
-        launch_halo_fill(g, a.ubt + sn * n2, 1, 3, st);
-        launch_halo_fill(g, a.vbt + sn * n2, 1, 3, st);
+        if (itime < a.nts) k_bt_corr_pred<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
+        else k_bt_corr<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
+        continue;
       }
+      k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, itime > 1);
+      k_bt_mom_c<<<g2, 128, 0, st>>>(a, so, sn, itime);
+      launch_halo_fill(g, a.ubt + sn * n2, 1, 3, st);
+      launch_halo_fill(g, a.vbt + sn * n2, 1, 3, st);
       k_bt_corr<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
     }
   };
