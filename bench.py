@@ -102,10 +102,12 @@ TRAFFIC_SOURCE = {"fp64": "ncu DRAM bytes of the advection launch set on a 360x2
 
 
 # FP64 thread-instructions per tracer-cell of the exact MDFL passes (z + x + y) and per
-# column of one exact barotropic subcycle, counted by ncu on the 360x270x50 block; the
+# column of one exact barotropic subcycle (momentum 29.7 + corrector with the next
+# predictor 21.0 in the steady state; 50.8 averaged over a 60-subcycle step with its
+# first predictor and last corrector), counted by ncu on the 360x270x50 block; the
 # FP64 instruction rate of GB300 measured with a probe kernel.
 FP64_OPS_PER_TRACER_CELL = 62.4
-FP64_OPS_PER_COLUMN_SUBCYCLE = 52.8
+FP64_OPS_PER_COLUMN_SUBCYCLE = 50.8
 FP64_PEAK_OPS = 5.05e11
 
 

@@ -317,13 +317,14 @@ int mom5gpu_autotune(mom5gpu_domain* d, double dtime, char* report, size_t repor
  * gave up is reported by the next mom5gpu_synchronize as MOM5GPU_ETIMEDOUT. */
 int mom5gpu_set_tuning(mom5gpu_domain* d, int rows, int prefetch, int tj);
 /* Form of the exact B-grid barotropic subcycles (update_ocean_barotropic,
- * ocean_barotropic.F90:3344-3575): 0 (default) = predictor, momentum and
- * corrector as three launches per subcycle, replayed from a CUDA graph; 1 = one
+ * ocean_barotropic.F90:3344-3575): 0 (default) = momentum, and corrector with
+ * the next subcycle's predictor, as two launches per subcycle (the predictor of
+ * the first subcycle a third), replayed from a CUDA graph; 1 = one
  * launch per subcycle, each tile recomputing the ring of pressure and
  * transports it reads (about 11% more FP64 work); 2 = all subcycles of a step
  * in one cooperative launch, a bounded grid barrier between the phases (a wait
  * that gives up is reported by mom5gpu_synchronize as MOM5GPU_ETIMEDOUT; inside
- * a stream capture the three launches are used).  Forms 1 and 2 were slower
+ * a stream capture form 0 is used).  Forms 1 and 2 were slower
  * than 0 on every measured domain.  Every form gives the same results bit for
  * bit.  A domain in the precision form (MOM5GPU_PRECISION_MIXED) has forms 0
  * and 1 of its own subcycle (mode 2 runs form 0): form 1 was faster on a
