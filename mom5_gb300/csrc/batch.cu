@@ -34,7 +34,11 @@ struct mom5gpu_batch {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   int g_key[2] = {-1, -1};
   long g_launches[2] = {0, 0};  // kernels per replay of each graph
-  int* d_counter = nullptr;
+  int* d_counter = nullptr;  // [0] plain precision tiles, [1] TMA-staged tiles
+  // precision form: a table of tensor maps per (domain, parity) for the
+  // TMA-staged tiles, and which domains have one (even ni)
+  unsigned char* d_tma = nullptr;
+  std::vector<char> tma_ok;
   // tuning
   int rows = 32, tj = 0, blocks_per_sm = 2, sms = 152;
   bool any_cyclic = false;
@@ -78,6 +82,10 @@ int build_descriptors(mom5gpu_batch* b, double dtime) {
   std::vector<BtArgs> bt(2 * n);
   std::vector<BtExtra> bx(2 * n);
   std::vector<MixArgs> mx(2 * n);
+  // tensor maps of the TMA-staged precision tiles, (domain, parity) entries
+  const size_t tb = batch_tma_bytes();
+  std::vector<unsigned char> tma(b->prec == MOM5GPU_PRECISION_FP64 ? 0 : tb * 2 * n, 0);
+  b->tma_ok.assign(n, 0);
   for (int i = 0; i < n; ++i) {
     mom5gpu_domain* d = b->doms[i];
     for (int p = 0; p < 2; ++p) {
@@ -90,6 +98,11 @@ int build_descriptors(mom5gpu_batch* b, double dtime) {
         m[2 * i + p].th_fresh = 1;  // the step zeroes only the halo ring of th_tendency
       } else if ((rc = make_mix_args(d, taum1, tau, taup1, dtime, &mx[2 * i + p]))) {
         return bfail(b, rc, "domain %d: %s", i, d->err.c_str());
+      } else {
+        // both parities or neither: a domain's tiles are all staged or all plain
+        int tr = fill_batch_tma(d, mx[2 * i + p], tma.data() + tb * (2 * i + p));
+        if (tr != MOM5GPU_OK && tr != MOM5GPU_EUNSUPPORTED) return bfail(b, tr, "domain %d: %s", i, d->err.c_str());
+        b->tma_ok[i] = (p == 0 ? tr == MOM5GPU_OK : b->tma_ok[i] && tr == MOM5GPU_OK) ? 1 : 0;
       }
       if ((rc = make_bt_args(d, tau, taup1, &bt[2 * i + p], &bx[2 * i + p])))
         return bfail(b, rc, "domain %d: %s", i, d->err.c_str());
@@ -101,6 +114,7 @@ int build_descriptors(mom5gpu_batch* b, double dtime) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_upd, u.data(), sizeof(UpdArgs) * 2 * n, cudaMemcpyHostToDevice, b->stream);
   } else {
     e = cudaMemcpyAsync(b->d_mix, mx.data(), sizeof(MixArgs) * 2 * n, cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_tma, tma.data(), tma.size(), cudaMemcpyHostToDevice, b->stream);
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_bt, bt.data(), sizeof(BtArgs) * 2 * n, cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_btx, bx.data(), sizeof(BtExtra) * 2 * n, cudaMemcpyHostToDevice, b->stream);
@@ -112,7 +126,8 @@ int build_descriptors(mom5gpu_batch* b, double dtime) {
 }
 
 // Work list of (domain, parity) entries as ints: entries, then the prefix sums of
-// the passes z, x, y, update, 2-D barotropic, 1-D barotropic, precision form.
+// the passes z, x, y, update, 2-D barotropic, 1-D barotropic, precision form
+// (plain tiles), precision form (TMA-staged tiles).
 void fill_work(const mom5gpu_batch* b, const std::vector<std::pair<int, int>>& list, std::vector<int>& h, BatchWork& w) {
   int c = (int)list.size();
   int TJ = tj_of(b);
@@ -121,15 +136,16 @@ void fill_work(const mom5gpu_batch* b, const std::vector<std::pair<int, int>>& l
   std::stable_sort(order.begin(), order.end(), [&](const std::pair<int, int>& a, const std::pair<int, int>& z) {
     return b->doms[a.first]->geo.n3 > b->doms[z.first]->geo.n3;
   });
-  h.assign((size_t)c + 7 * (size_t)(c + 1), 0);
+  h.assign((size_t)c + 8 * (size_t)(c + 1), 0);
   int* ent = h.data();
-  int* pr[7];
-  for (int k = 0; k < 7; ++k) pr[k] = ent + c + k * (c + 1);
+  int* pr[8];
+  for (int k = 0; k < 8; ++k) pr[k] = ent + c + k * (c + 1);
   for (int e = 0; e < c; ++e) {
-    ent[e] = 2 * order[e].first + order[e].second;
-    BatchBlocks bb = batch_blocks(b->doms[order[e].first]->geo, TJ, b->rows);
-    int v[7] = {bb.z, bb.x, bb.y, bb.u, bb.b2, bb.b1, bb.m};
-    for (int k = 0; k < 7; ++k) pr[k][e + 1] = pr[k][e] + v[k];
+    const int dom = order[e].first;
+    ent[e] = 2 * dom + order[e].second;
+    BatchBlocks bb = batch_blocks(b->doms[dom]->geo, TJ, b->rows, dom < (int)b->tma_ok.size() && b->tma_ok[dom]);
+    int v[8] = {bb.z, bb.x, bb.y, bb.u, bb.b2, bb.b1, bb.m, bb.t};
+    for (int k = 0; k < 8; ++k) pr[k][e + 1] = pr[k][e] + v[k];
   }
   w.count = c;
   w.tz = pr[0][c];
@@ -139,6 +155,7 @@ void fill_work(const mom5gpu_batch* b, const std::vector<std::pair<int, int>>& l
   w.tb2 = pr[4][c];
   w.tb1 = pr[5][c];
   w.tm = pr[6][c];
+  w.tt = pr[7][c];
 }
 
 void bind_work(BatchWork& w, const int* d) {
@@ -152,6 +169,7 @@ void bind_work(BatchWork& w, const int* d) {
   w.pb2 = p + 4 * (c + 1);
   w.pb1 = p + 5 * (c + 1);
   w.pm = p + 6 * (c + 1);
+  w.pt = p + 7 * (c + 1);
 }
 
 // every kernel of one batched step, in stream order
@@ -177,9 +195,10 @@ int enqueue_step(mom5gpu_batch* b, const BatchWork& w, const std::vector<std::pa
         launches += b->ntr;
       }
     } else {
-      rc = launch_batch_mixed(b->d_mix, w, b->ntr, b->rows, b->blocks_per_sm * b->sms, b->d_counter, s);
+      rc = launch_batch_mixed(b->d_mix, b->d_tma, w, b->ntr, b->rows, b->blocks_per_sm * b->sms, b->sms, b->d_counter,
+                              s);
       if (rc) return bfail(b, rc, "precision-form batch launch");
-      launches += 1;
+      launches += (w.tm > 0 ? 1 : 0) + (b->rows == 24 && w.tt > 0 ? 1 : 0);
     }
   }
   launch_batch_barotropic_loop(b->d_bt, b->d_btx, w, b->nts, b->stepB, b->prec == MOM5GPU_PRECISION_MIXED, s);
@@ -339,12 +358,13 @@ int mom5gpu_batch_create(mom5gpu_domain* const* domains, int n, mom5gpu_batch** 
   size_t nd = 2 * (size_t)n;
   if (e == cudaSuccess) e = cudaMalloc(&b->d_bt, sizeof(BtArgs) * nd);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_btx, sizeof(BtExtra) * nd);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, 2 * sizeof(int));
   if (e == cudaSuccess && b->prec == MOM5GPU_PRECISION_FP64) {
     e = cudaMalloc(&b->d_mdfl, sizeof(MdflArgs) * nd);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_upd, sizeof(UpdArgs) * nd);
   } else if (e == cudaSuccess) {
     e = cudaMalloc(&b->d_mix, sizeof(MixArgs) * nd);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tma, batch_tma_bytes() * nd);
   }
   if (e != cudaSuccess) {
     mom5gpu_batch_destroy(b);
@@ -361,6 +381,7 @@ int mom5gpu_batch_create(mom5gpu_domain* const* domains, int n, mom5gpu_batch** 
     }
   } else {
     int rc = prepare_batch_mixed();
+    if (!rc) rc = prepare_batch_mixed_tma();
     if (rc) {
       mom5gpu_batch_destroy(b);
       return fail(nullptr, rc, "batch_create: kernel attributes");
@@ -378,7 +399,7 @@ void mom5gpu_batch_destroy(mom5gpu_batch* b) {
     if (b->d_work_all[p]) cudaFree(b->d_work_all[p]);
   }
   for (void* p : {(void*)b->d_mdfl, (void*)b->d_upd, (void*)b->d_bt, (void*)b->d_btx, (void*)b->d_mix, (void*)b->d_work,
-                  (void*)b->d_counter})
+                  (void*)b->d_counter, (void*)b->d_tma})
     if (p) cudaFree(p);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
@@ -464,7 +485,7 @@ int mom5gpu_batch_get_tuning(const mom5gpu_batch* b, int* rows, int* tj, int* bl
 
 int mom5gpu_batch_set_tuning(mom5gpu_batch* b, int rows, int tj, int blocks_per_sm) {
   if (!b) return MOM5GPU_EINVAL;
-  if (rows != 16 && rows != 32) return bfail(b, MOM5GPU_EINVAL, "set_tuning: rows %d (16 or 32)", rows);
+  if (rows != 16 && rows != 24 && rows != 32) return bfail(b, MOM5GPU_EINVAL, "set_tuning: rows %d (16, 24 or 32)", rows);
   if (tj != 0 && tj != 2 && tj != 4 && tj != 8 && tj != 16)
     return bfail(b, MOM5GPU_EINVAL, "set_tuning: tj %d (0, 2, 4, 8 or 16)", tj);
   if (blocks_per_sm < 1 || blocks_per_sm > 4)
@@ -480,9 +501,9 @@ int mom5gpu_batch_autotune(mom5gpu_batch* b, double dtime, char* report, size_t 
   struct Cand {
     int rows, tj, bps;
   };
-  static const Cand kMixed[] = {{32, 0, 1}, {32, 0, 2}, {16, 0, 2}, {16, 0, 3}, {16, 0, 4}};
+  static const Cand kMixed[] = {{32, 0, 1}, {32, 0, 2}, {16, 0, 2}, {16, 0, 3}, {16, 0, 4}, {24, 0, 2}};
   static const Cand kFp64[] = {{32, 2, 2}, {32, 4, 2}, {32, 8, 2}, {32, 16, 2}};
-  std::vector<Cand> cands = b->prec == MOM5GPU_PRECISION_MIXED ? std::vector<Cand>(kMixed, kMixed + 5)
+  std::vector<Cand> cands = b->prec == MOM5GPU_PRECISION_MIXED ? std::vector<Cand>(kMixed, kMixed + 6)
                                                                  : std::vector<Cand>(kFp64, kFp64 + 4);
   std::vector<int> idx(b->doms.size()), par(b->doms.size(), 0);
   for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;

@@ -286,15 +286,16 @@ int ensure_mdfl_scratch(mom5gpu_domain* d, int ntr);
 // e; p*[e] is the first block of entry e in each pass (p*[count] = total).
 struct BatchWork {
   const int* entries;
-  const int *pz, *px, *py, *pu, *pb2, *pb1, *pm;
+  const int *pz, *px, *py, *pu, *pb2, *pb1, *pm, *pt;
   int count;
-  int tz, tx, ty, tu, tb2, tb1, tm;  // total blocks of each pass
+  int tz, tx, ty, tu, tb2, tb1, tm, tt;  // total blocks of each pass
 };
-// blocks of one domain in each pass, for the work-list prefix sums
+// blocks of one domain in each pass, for the work-list prefix sums; t: the
+// TMA-staged precision tiles (mixed_rows 24 on a domain that allows them)
 struct BatchBlocks {
-  int z, x, y, u, b2, b1, m;
+  int z, x, y, u, b2, b1, m, t;
 };
-BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows);
+BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma);
 // FP64: z/x/y MDFL passes and the explicit update for every entry
 void launch_batch_fp64_advection(const MdflArgs* mdfl, const UpdArgs* upd, const BatchWork& w, int ntr, bool sweby,
                                  int TJ, cudaStream_t s);
@@ -303,15 +304,25 @@ void launch_batch_fp64_advection(const MdflArgs* mdfl, const UpdArgs* upd, const
 void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, bool fast,
                                   cudaStream_t s);
 // precision form: folded subcycle over the work list (k_batch.cu)
+// precision form, TMA-staged 24-row tiles over a batch's work list (k_mixed_tma.cu):
+// the bytes of one (domain, parity) entry of the device table, filling an entry
+// (MOM5GPU_EUNSUPPORTED when the domain cannot be described to TMA), the launch
+size_t batch_tma_bytes();
+int fill_batch_tma(mom5gpu_domain* d, const MixArgs& a, void* host_entry);
+int launch_batch_mixed_tma(const MixArgs* mix, const void* tma, const BatchWork& w, int ntr, int blocks, int* counter,
+                           cudaStream_t s);
 void launch_batch_btf_prep(const BtArgs* bt, const BatchWork& w, cudaStream_t s);
 int launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int itime, int nts, cudaStream_t s);
 void launch_batch_barotropic_post(const BtArgs* bt, const BtExtra* x, const BatchWork& w, int nts, int stepB, int phase,
                                   cudaStream_t s);
 // precision form: persistent kernel over (entry, tile) items
-int launch_batch_mixed(const MixArgs* mix, const BatchWork& w, int ntr, int rows, int blocks, int* counter,
-                       cudaStream_t s);
+// rows 16 or 32: the plain persistent tile kernel; rows 24: the TMA-staged tiles
+// (table tma, counter[1]) and the plain 32-row tiles for the other domains
+int launch_batch_mixed(const MixArgs* mix, const void* tma, const BatchWork& w, int ntr, int rows, int blocks,
+                       int sms, int* counter, cudaStream_t s);
 // sets the shared-memory attribute of every instantiation (before any graph capture)
 int prepare_batch_mixed();
+int prepare_batch_mixed_tma();
 
 // ---- precision form (k_mixed.cu) ----
 int launch_mdfl_mixed(mom5gpu_domain* d, int n_first, int ntr, int taum1, int tau, int taup1, double dtime,

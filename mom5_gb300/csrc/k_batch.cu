@@ -122,10 +122,13 @@ int prepare_batch_mixed() {
   return rc ? MOM5GPU_ECUDA : MOM5GPU_OK;
 }
 
-int launch_batch_mixed(const MixArgs* mix, const BatchWork& w, int ntr, int rows, int blocks, int* counter,
-                       cudaStream_t s) {
-  if (w.tm <= 0) return MOM5GPU_OK;
-  return rows == 16 ? run_nc<16>(mix, w, ntr, blocks, counter, s) : run_nc<32>(mix, w, ntr, blocks, counter, s);
+int launch_batch_mixed(const MixArgs* mix, const void* tma, const BatchWork& w, int ntr, int rows, int blocks,
+                       int sms, int* counter, cudaStream_t s) {
+  int rc = MOM5GPU_OK;
+  if (w.tm > 0)
+    rc = rows == 16 ? run_nc<16>(mix, w, ntr, blocks, counter, s) : run_nc<32>(mix, w, ntr, blocks, counter, s);
+  if (rc == MOM5GPU_OK && rows == 24 && w.tt > 0) rc = launch_batch_mixed_tma(mix, tma, w, ntr, sms, counter + 1, s);
+  return rc;
 }
 
 }  // namespace mom5

@@ -126,7 +126,7 @@ void adv(const MdflArgs* m, const UpdArgs* u, const BatchWork& w, int TJ, cudaSt
 
 }  // namespace
 
-BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows) {
+BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma) {
   BatchBlocks b;
   int nb = (g.ni + 127) / 128;
   b.z = nb * g.nj;
@@ -135,8 +135,11 @@ BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows) {
   b.u = nb * g.nj * g.nk;
   b.b2 = ((g.ni + 2 + 127) / 128) * (g.nj + 2);
   b.b1 = (int)((g.n2 + 255) / 256);
-  int tj = mixed_rows - 4;
-  b.m = ((g.ni + 27) / 28) * ((g.nj + tj - 1) / tj);
+  // rows 24: TMA-staged 24-row tiles where the domain allows them, else the plain 32-row tiles
+  const bool staged = mixed_rows == 24 && tma;
+  int tj = (mixed_rows == 24 ? 32 : mixed_rows) - 4;
+  b.m = staged ? 0 : ((g.ni + 27) / 28) * ((g.nj + tj - 1) / tj);
+  b.t = staged ? ((g.ni + 27) / 28) * ((g.nj + 19) / 20) : 0;
   return b;
 }
 

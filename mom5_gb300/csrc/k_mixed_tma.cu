@@ -38,6 +38,7 @@
 // block and two blocks per SM.
 #include <cuda.h>
 #include <math.h>
+#include <string.h>
 
 #include "mixed_body.cuh"
 
@@ -59,6 +60,7 @@ DEVI void mbar_init(uint64_t* b) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(b)) : "memory");
 }
 DEVI void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+DEVI void mbar_inval(uint64_t* b) { asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(su32(b)) : "memory"); }
 DEVI void mbar_expect(uint64_t* b, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
 }
@@ -137,9 +139,12 @@ constexpr int kOutRing = 4;
 // One level is three phases with a block barrier between them: (1) the level's
 // face terms, (2) the z and x passes of every tracer, (3) the y fluxes of every
 // tracer, then the outputs -- three barriers per level whatever the tracer count.
+// One tile (tile_x, tile_y) of the domain a, with the block's whole shared memory;
+// false when a bounded wait gave up (*err set; the block must stop).  The
+// barriers are initialised at the start and invalidated at the end, so a
+// persistent block can run tile after tile.
 template <int NC, int ZR, int MINB>
-__global__ void __launch_bounds__(32 * ZR, MINB)
-    k_mdfl_mixed_tma(MixArgs a, int n0, int zt0, const __grid_constant__ TmaMaps maps, int* err) {
+DEVI bool tma_tile(const MixArgs& a, int n0, int zt0, const TmaMaps& maps, int* err, int tile_x, int tile_y) {
   constexpr int WM = kWindowMode<NC, ZR, MINB>;
   using S = TmaSmem<NC, ZR, WM>;
   constexpr int SLOT = S::SLOT;
@@ -149,7 +154,7 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
   S& s = *reinterpret_cast<S*>(smem_raw);
   const Geo& g = a.g;
   const int zi = threadIdx.x & 31, zj = threadIdx.x >> 5, c = zj * 32 + zi;
-  const int i0 = 1 + blockIdx.x * TI, j0 = 1 + blockIdx.y * TJ;
+  const int i0 = 1 + tile_x * TI, j0 = 1 + tile_y * TJ;
   const int bx0 = i0 - 3, by0 = j0 - 2;  // box origin (bx0 even)
   const int sc = zj * BX + zi + 1;       // this position in a box
   const float dt = a.dtime;
@@ -416,7 +421,11 @@ __global__ void __launch_bounds__(32 * ZR, MINB)
     // the window of wet bits moves down one level
     mb = (mb >> 1) | (m_next ? 8u : 0u);
   }
-  return;
+  // every copy of this tile has been waited for (the last level issues none)
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int q = 0; q <= NC; ++q) mbar_inval(&s.bar[q]);
+  return true;
 
 abort:
   if (threadIdx.x == 0) {
@@ -426,6 +435,13 @@ abort:
       if (s.pending[q]) mbar_wait(&s.bar[q], (unsigned)(s.pending[q] - 1));
   }
   __syncthreads();
+  return false;
+}
+
+template <int NC, int ZR, int MINB>
+__global__ void __launch_bounds__(32 * ZR, MINB)
+    k_mdfl_mixed_tma(MixArgs a, int n0, int zt0, const __grid_constant__ TmaMaps maps, int* err) {
+  tma_tile<NC, ZR, MINB>(a, n0, zt0, maps, err, blockIdx.x, blockIdx.y);
 }
 
 // ---- host side ----
@@ -510,7 +526,99 @@ int run_tma_pairs(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tal
   return MOM5GPU_OK;
 }
 
+// ---- batches: TMA-staged 24-row tiles over a work list ----
+
+// one (domain, parity) entry of a batch's device table: the tensor maps of its
+// tracer level and fields, and its domain's error word
+struct BatchTma {
+  TmaMaps m;
+  int* err;
+};
+
+DEVI int find_tile_entry(const int* prefix, int count, int b) {
+  int lo = 0, hi = count;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Persistent: one block of 768 threads per SM takes tiles from an atomic counter
+// (largest domains first) and runs each as the one-domain kernel does.  A block
+// whose bounded wait gave up stops; the others go on, and the domain's
+// mom5gpu_synchronize reports MOM5GPU_ETIMEDOUT.
+template <int NC>
+__global__ void __launch_bounds__(32 * 24, 1)
+    kb_mixed_tma(const MixArgs* __restrict__ d, const BatchTma* __restrict__ tm, BatchWork w, int* counter) {
+  __shared__ int item;
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = item;
+    __syncthreads();
+    if (it >= w.tt) return;
+    const int e = find_tile_entry(w.pt, w.count, it);
+    const int ent = w.entries[e];
+    const MixArgs& a = d[ent];
+    const int local = it - w.pt[e];
+    const int ntx = (a.g.ni + TI - 1) / TI;
+    if (!tma_tile<NC, 24, 1>(a, 0, 0, tm[ent].m, tm[ent].err, local % ntx, local / ntx)) return;
+  }
+}
+
+template <int NC>
+int configure_batch_tma() {
+  return cudaFuncSetAttribute(kb_mixed_tma<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(TmaSmem<NC, 24, kWindowMode<NC, 24, 1>>)) == cudaSuccess
+             ? MOM5GPU_OK
+             : MOM5GPU_ECUDA;
+}
+
+template <int NC>
+void run_batch_tma(const MixArgs* mix, const BatchTma* tm, const BatchWork& w, int blocks, int* counter,
+                   cudaStream_t s) {
+  cudaMemsetAsync(counter, 0, sizeof(int), s);
+  kb_mixed_tma<NC><<<blocks, 32 * 24, sizeof(TmaSmem<NC, 24, kWindowMode<NC, 24, 1>>), s>>>(mix, tm, w, counter);
+}
+
 }  // namespace
+
+size_t batch_tma_bytes() { return sizeof(BatchTma); }
+
+int fill_batch_tma(mom5gpu_domain* d, const MixArgs& a, void* host_entry) {
+  const Geo& g = d->geo;
+  if (g.ni % 2 != 0 || !a.T || a.ntr < 1) return MOM5GPU_EUNSUPPORTED;
+  int rc = ensure_wait_words(d);
+  if (rc) return rc;
+  BatchTma t;
+  memset(&t, 0, sizeof(t));
+  bool ok = encode(&t.m.T, a.T, g, (long)a.ntr * g.nk, 24) && encode(&t.m.f[F_UH], a.uh, g, g.nk, 24) &&
+            encode(&t.m.f[F_VH], a.vh, g, g.nk, 24) && encode(&t.m.f[F_W], a.w, g, g.nk + 1, 24) &&
+            encode(&t.m.f[F_RDZ], a.rdz, g, g.nk, 24) && encode(&t.m.f[F_RDZR], a.rdzr, g, g.nk, 24) &&
+            encode(&t.m.f[F_RDZM1], a.rdz_m1, g, g.nk, 24);
+  if (!ok) return MOM5GPU_EUNSUPPORTED;
+  t.err = d->wait_err;
+  memcpy(host_entry, &t, sizeof(t));
+  return MOM5GPU_OK;
+}
+
+int prepare_batch_mixed_tma() {
+  int rc = configure_batch_tma<1>() | configure_batch_tma<2>() | configure_batch_tma<4>() | configure_batch_tma<10>();
+  return rc ? MOM5GPU_ECUDA : MOM5GPU_OK;
+}
+
+int launch_batch_mixed_tma(const MixArgs* mix, const void* tma, const BatchWork& w, int ntr, int blocks, int* counter,
+                           cudaStream_t s) {
+  if (w.tt <= 0) return MOM5GPU_OK;
+  const BatchTma* tm = static_cast<const BatchTma*>(tma);
+  if (ntr <= 1) run_batch_tma<1>(mix, tm, w, blocks, counter, s);
+  else if (ntr <= 2) run_batch_tma<2>(mix, tm, w, blocks, counter, s);
+  else if (ntr <= 4) run_batch_tma<4>(mix, tm, w, blocks, counter, s);
+  else run_batch_tma<10>(mix, tm, w, blocks, counter, s);
+  return MOM5GPU_OK;
+}
 
 // The TMA variant of one launch of launch_mdfl_mixed (a = the launch's
 // arguments, tracers zt0 .. zt0+a.ntr-1 of the level whose first tracer is

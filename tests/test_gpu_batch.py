@@ -41,13 +41,19 @@ def snapshot(capi, d, ntr, level):
     return out
 
 
-@pytest.mark.parametrize("precision,ntr", [(0, 3), (1, 3), (0, 10), (1, 10)])
-def test_batch_equals_single_domain_steps(gpu_lib, precision, ntr):
+@pytest.mark.parametrize("precision,ntr,rows", [(0, 3, None), (1, 3, None), (0, 10, None), (1, 10, None), (1, 3, 24),
+                                                (1, 10, 24)])
+def test_batch_equals_single_domain_steps(gpu_lib, precision, ntr, rows):
+    """rows 24: the precision form's TMA-staged tiles for the domains with an
+    even ni (40, 64, 18 of SIZES) and the plain tiles for the others, in one
+    step; every launch shape gives the same bits as the one-domain path."""
     capi = gpu_lib
     from mom5_gb300 import harness
     single, _ = make_domains(capi, harness, precision, SIZES, ntr)
     batched, _ = make_domains(capi, harness, precision, SIZES, ntr)
     b = capi.Batch(batched)
+    if rows:
+        b.tuning = (rows, 0, 2)
     # step 1: every domain, parity 0, through a work list
     for d in single:
         d.tracer_advection_step(1, 1, 2, DT)
@@ -120,7 +126,10 @@ def test_batch_tuning_get_set(gpu_lib):
     assert b.tuning == (32, 0, 2)
     b.tuning = (16, 4, 3)
     assert b.tuning == (16, 4, 3)
-    for bad in ((24, 0, 2), (32, 3, 2), (32, 0, 0), (32, 0, 5)):
+    b.tuning = (24, 0, 2)
+    assert b.tuning == (24, 0, 2)
+    b.tuning = (16, 4, 3)
+    for bad in ((20, 0, 2), (32, 3, 2), (32, 0, 0), (32, 0, 5)):
         with pytest.raises(capi.Mom5GpuError):
             b.tuning = bad
     assert b.tuning == (16, 4, 3)
