@@ -143,18 +143,21 @@ def rel_err(got, want):
 GRAV = 9.8
 
 
-def make_baro_box(sx, sy, u0, v0, ni=60, nj=50, dx=8000.0, dy=6000.0, depth=4000.0):
-    """A one-level grid.Domain with uniform metrics, f = 0, no forcing, eta =
-    0.5 + sx*i + sy*j and uniform transports (u0, v0) at time level tau."""
+def make_baro_box(sx, sy, u0, v0, ni=60, nj=50, dx=8000.0, dy=6000.0, depth=4000.0, f=0.0, periodic=False):
+    """A one-level grid.Domain with uniform metrics, a uniform Coriolis
+    parameter f (0 by default), no forcing, eta = 0.5 + sx*i + sy*j and uniform
+    transports (u0, v0) at time level tau; walled, or periodic in both
+    directions."""
     import torch
     from mom5_gb300 import grid
     sp = grid.DomainSpec(ni=ni, nj=nj, nk=1, lon0=0.0, lon1=0.1 * ni, lat0=-0.05 * nj, lat1=0.05 * nj,
-                         continent=None, hmin=None, depth=depth, ntracers=0, seed=0)
+                         continent=None, hmin=None, depth=depth, ntracers=0, seed=0, cyclic_x=periodic,
+                         cyclic_y=periodic)
     dom = grid.make_domain(sp)
     for k, v in (("dxt", dx), ("dxte", dx), ("dxtn", dx), ("dxu", dx), ("dte", dx), ("dtw", dx),
                  ("dyt", dy), ("dyte", dy), ("dytn", dy), ("dyu", dy), ("dus", dy), ("dun", dy),
                  ("dxur", 1 / dx), ("dyur", 1 / dy), ("dxter", 1 / dx), ("dytnr", 1 / dy),
-                 ("dat", dx * dy), ("datr", 1 / (dx * dy)), ("daur", 1 / (dx * dy)), ("f", 0.0),
+                 ("dat", dx * dy), ("datr", 1 / (dx * dy)), ("daur", 1 / (dx * dy)), ("f", f),
                  ("tmask1", 1.0), ("umask1", 1.0), ("tmasken_e1", 1.0), ("tmasken_n1", 1.0),
                  ("patm", 0.0), ("pme", 0.0), ("river", 0.0), ("source", 0.0), ("eta_smooth", 0.0),
                  ("forcing_u", 0.0), ("forcing_v", 0.0), ("thicku", depth), ("thicken_e", depth),
@@ -172,6 +175,40 @@ def baro_expected(sx, sy, u0, v0, nts, dtbt, spacing, stepping_B):
     ax, ay = -depth * RHO0 * GRAV * sx / dx, -depth * RHO0 * GRAV * sy / dy
     nbar = (nts + 2) / 3.0 if stepping_B else (nts + 1) / 2.0
     return u0 + ax * dtbt * nbar, v0 + ay * dtbt * nbar
+
+
+# With a flat sea surface and uniform transports on an f-plane (no forcing, no
+# pressure gradient, no divergence) the transports only rotate: the inertial
+# oscillation du/dt = f v, dv/dt = -f u.
+# - B grid: the subcycle takes it Crank-Nicolson, u(n+1) - u(n) = dt f (v(n) +
+#   v(n+1))/2 and likewise for v, which is a rotation by the angle theta with
+#   cos(theta) = (1 - a^2)/(1 + a^2), sin(theta) = 2a/(1 + a^2), a = f dt/2:
+#   the amplitude is kept exactly.
+# - C grid: the Coriolis force is extrapolated by the third-order Adams-Bashforth
+#   weights (23, -16, 5)/12 from the subcycles of the same step, u(n+1) = u(n) +
+#   dt (23 C(n) - 16 C(n-1) + 5 C(n-2))/12 with C = f v for u and -f u for v,
+#   the force of the step's initial state standing in for the subcycles before
+#   the first (whose update is then forward Euler).
+# The step returns the subcycles' average (weights 1, or nts-n+1 for time
+# stepping B).
+
+def baro_inertial_expected(f, u0, v0, nts, dtbt, stepping_B, cgrid=False):
+    u, v = float(u0), float(v0)
+    hist = [(f * v, -f * u)] * 2  # (C_u, C_v) standing in for the subcycles before the first
+    a = 0.5 * f * dtbt
+    c, s = (1 - a * a) / (1 + a * a), 2 * a / (1 + a * a)
+    su = sv = sw = 0.0
+    for n in range(1, nts + 1):
+        if cgrid:
+            hist.insert(0, (f * v, -f * u))
+            cu = sum(w * h[0] for w, h in zip((23 / 12, -16 / 12, 5 / 12), hist))
+            cv = sum(w * h[1] for w, h in zip((23 / 12, -16 / 12, 5 / 12), hist))
+            u, v = u + dtbt * cu, v + dtbt * cv
+        else:
+            u, v = c * u + s * v, -s * u + c * v
+        w = (nts - n + 1) if stepping_B else 1.0
+        su, sv, sw = su + w * u, sv + w * v, sw + w
+    return su / sw, sv / sw
 
 
 def interior2(a, margin=15):

@@ -3,7 +3,9 @@ on a uniform box in uniform flow, one mom5gpu_tracer_advection_step of MDFL
 Sweby translates a cubic exactly, upwind a linear profile, and the centred
 2nd/4th/6th-order and Quicker schemes take the exact forward-Euler step of a
 quadratic -- to FP64 roundoff on the drop-in path, within the precision form's
-FP32 tolerance for MDFL in that form."""
+FP32 tolerance for MDFL in that form; and from the barotropic momentum equation
+(a uniform surface slope; an inertial oscillation on an f-plane)."""
+import numpy as np
 import pytest
 
 import analytic as A
@@ -87,4 +89,34 @@ def test_barotropic_matches_the_momentum_equation(gpu_lib, stepping_B, fusion):
     assert abs(A.interior2(get(capi.F.UDRHO_U)) - eu).max() <= 1e-10 * abs(eu)
     assert abs(A.interior2(get(capi.F.UDRHO_V)) - ev).max() <= 1e-10 * abs(ev)
     assert abs(A.interior2(get(capi.F.ETA_T_BAR)) - A.interior2(dom["eta_t"].numpy())).max() <= 1e-12
+    d.close()
+
+
+@pytest.mark.parametrize("grid_kind,fusion,precision", [("b", 0, 0), ("b", 1, 0), ("b", 2, 0), ("c", 0, 0),
+                                                        ("b", 0, 1), ("b", 1, 1)])
+@pytest.mark.parametrize("stepping_B", [False, True])
+def test_barotropic_inertial_oscillation(gpu_lib, grid_kind, fusion, precision, stepping_B):
+    """A flat sea surface and uniform transports on an f-plane (doubly periodic):
+    the transports only rotate, Crank-Nicolson on the B grid (every subcycle
+    form), Adams-Bashforth-3 on the C grid, and the step returns their time
+    average (tests/analytic.py); 1e-12 of the amplitude for the exact path,
+    1e-6 for the precision form."""
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    f, u0, v0, nts, dtbt = 1.4e-4, 100.0, -50.0, 20, 20.0
+    dom, spacing = A.make_baro_box(0.0, 0.0, u0, v0, f=f, periodic=True)
+    opts = capi.default_options(barotropic_time_stepping_A=int(not stepping_B),
+                                barotropic_time_stepping_B=int(stepping_B),
+                                precision=capi.PRECISION_MIXED if precision else capi.PRECISION_FP64)
+    d = harness.load(dom, options=opts, horz_grid=capi.CGRID if grid_kind == "c" else capi.BGRID)
+    assert d.barotropic_init(dtuv=nts * dtbt / 2, dtbt=dtbt) == nts
+    d.set_barotropic_fusion(fusion)
+    d.update_ocean_barotropic(1, 2)
+    shape = tuple(dom["eta_t"].shape)
+    get = lambda fid: d.get(fid, level=2).reshape(shape)
+    eu, ev = A.baro_inertial_expected(f, u0, v0, nts, dtbt, stepping_B, cgrid=grid_kind == "c")
+    tol = (1e-6 if precision else 1e-12) * np.hypot(eu, ev)
+    assert abs(A.interior2(get(capi.F.UDRHO_U)) - eu).max() <= tol
+    assert abs(A.interior2(get(capi.F.UDRHO_V)) - ev).max() <= tol
+    assert abs(A.interior2(get(capi.F.ETA_T_BAR)) - 0.5).max() <= (1e-9 if precision else 1e-13)
     d.close()

@@ -350,6 +350,29 @@ def test_barotropic_matches_the_momentum_equation(O, stepping_B):
     assert np.abs(A.interior2(out["conv_rho_ud_t"])).max() <= 1e-10 * abs(eu) / spacing[0]
 
 
+@pytest.mark.parametrize("cgrid", [False, True])
+@pytest.mark.parametrize("stepping_B", [False, True])
+def test_barotropic_inertial_oscillation(O, stepping_B, cgrid):
+    """Known answer (tests/analytic.py): a flat sea surface and uniform
+    transports on an f-plane only rotate.  The B-grid subcycle
+    (pred_corr_tropic_depth_bgrid, ocean_barotropic.F90:3225-3579) is the
+    Crank-Nicolson rotation, the C-grid one (pred_corr_tropic_depth_cgrid,
+    :3601-3965) the Adams-Bashforth-3 extrapolation of the Coriolis force; the
+    step returns the subcycles' time average and eta stays flat (a doubly
+    periodic domain: no walls, so no waves)."""
+    import analytic as A
+    f, u0, v0, nts, dtbt = 1.4e-4, 100.0, -50.0, 20, 20.0
+    dom, spacing = A.make_baro_box(0.0, 0.0, u0, v0, f=f, periodic=True)
+    g, d = O.domain_arrays(dom), O.dims(dom.spec)
+    st = {k: g[k].copy() for k in ("eta_t", "eta_t_bar", "udrho_u", "udrho_v")}
+    out = O.update_ocean_barotropic(d, g, st, nts, dtbt, time_stepping_B=stepping_B, cgrid=cgrid)
+    eu, ev = A.baro_inertial_expected(f, u0, v0, nts, dtbt, stepping_B, cgrid)
+    amp = np.hypot(eu, ev)
+    assert np.abs(A.interior2(out["udrho_u"]) - eu).max() <= 1e-12 * amp
+    assert np.abs(A.interior2(out["udrho_v"]) - ev).max() <= 1e-12 * amp
+    assert np.abs(A.interior2(out["eta_t_bar"]) - 0.5).max() <= 1e-13
+
+
 def test_quicker_weights_uniform_grid(O):
     """On a uniform grid quicker_init (:1510-1578) gives quick = 1/2 and the
     curvature weights 1/8, -1/4 (relative form of the classic 3/8, 6/8, -1/8)."""
