@@ -130,6 +130,97 @@ def rel_err(got, want):
     return np.abs(g - e).max() / np.abs(e).max()
 
 
+# ---- the Sweby limiter's branches ----
+#
+# MDFL Sweby is the third-order DST scheme with Sweby's flux limiter: along the
+# flow, the face value is T_up + psi*(T_dn - T_up) with
+#   psi = max(0, min(1, d0 + d1*theta, (1 - c)/c*theta)),
+#   d0 = (2 - c)(1 - c)/6, d1 = (1 - c^2)/6,
+# theta the ratio of the difference upstream of the face to the difference
+# across it, and c the Courant number.  On a profile whose differences along
+# the flow form a geometric sequence (T = r^i, or T alternating, theta = -1)
+# theta is the same at every face, so one psi holds everywhere and one step of
+# the 1-D flux form gives the cell values directly.  The cases below put psi on
+# each branch: the DST3 line, the slope bound (1 - c)/c*theta, the bound 1, and
+# 0 (upwind) where theta < 0.
+
+LIMITER_CASES = {
+    # name: (profile ratio r or "alt", Courant number c, sign of the velocity, branch)
+    "line": (3.0, 0.4, +1, "line"),
+    "slope": (8.0, 0.6, +1, "slope"),
+    "one": (0.2, 0.1, +1, "one"),
+    "zero": ("alt", 0.4, +1, "zero"),
+    "slope_negative_u": (1.0 / 8.0, 0.6, -1, "slope"),
+    "one_negative_u": (5.0, 0.1, -1, "one"),
+}
+
+
+def limiter_psi(theta, c):
+    d0, d1 = (2 - c) * (1 - c) / 6, (1 - c * c) / 6
+    return max(0.0, min(1.0, d0 + d1 * theta, (1 - c) / c * theta)), d0 + d1 * theta, (1 - c) / c * theta
+
+
+def limiter_profile(r, shape, axis):
+    """T = r^i (or 1 + 0.1*(-1)^i) along `axis` of a (nk, nyd, nxd) array."""
+    idx = np.arange(shape[axis], dtype=float)
+    line = 1.0 + 0.1 * (-1.0) ** idx if r == "alt" else r ** idx
+    view = [1, 1, 1]
+    view[axis] = shape[axis]
+    return np.broadcast_to(line.reshape(view), shape).copy()
+
+
+def limiter_theta(r, sign):
+    if r == "alt":
+        return -1.0
+    return 1.0 / r if sign > 0 else r
+
+
+def limiter_expected(T, axis, c, sign, psi):
+    """One step of the 1-D flux form with one psi at every face, along `axis`
+    (i increasing); only cells away from the ends are meaningful."""
+    Tp = np.roll(T, -1, axis)  # T(i+1)
+    if sign > 0:
+        F = T + psi * (Tp - T)  # face i+1/2, upstream cell i
+        return T - c * (F - np.roll(F, 1, axis))
+    F = Tp - psi * (Tp - T)  # face i+1/2, upstream cell i+1
+    return T + c * (F - np.roll(F, 1, axis))
+
+
+def make_limiter_box(case, axis, ni=30, nj=30, nk=12, dx=8000.0, dy=6000.0, dz=10.0, dt=2000.0):
+    """make_box with flow along x (axis 2) or y (axis 1) at the case's Courant
+    number and the case's profile along it; returns (domain, expected, psi)."""
+    import torch
+    r, c, sign, branch = LIMITER_CASES[case]
+    spacing = dx if axis == 2 else dy
+    vel = sign * c * spacing / dt
+    u, v = (vel, 0.0) if axis == 2 else (0.0, vel)
+    dom, _ = make_box("linear", u, v, 0.0, ni=ni, nj=nj, nk=nk, dx=dx, dy=dy, dz=dz)
+    shape = tuple(dom["T"][0].shape)
+    T0 = limiter_profile(r, shape, axis)
+    dom["T"][0].copy_(torch.from_numpy(T0))
+    psi, line, slope = limiter_psi(limiter_theta(r, sign), c)
+    chosen = {"line": line, "slope": slope, "one": 1.0, "zero": 0.0}[branch]
+    assert psi == chosen, (case, psi, line, slope)  # the case sits on its branch
+    return dom, limiter_expected(T0, axis, c, sign, psi), psi
+
+
+def rel_err_side(got, want, margin=8):
+    """max|got - want| / max|want| away from the side boundaries."""
+    g, e = np.asarray(got), np.asarray(want)
+    _, nyd, nxd = g.shape
+    g, e = g[:, margin:nyd - margin, margin:nxd - margin], e[:, margin:nyd - margin, margin:nxd - margin]
+    return float(np.abs(g - e).max() / np.abs(e).max())
+
+
+def rel_err_cells(got, want, margin=8):
+    """Largest per-cell relative difference away from the side boundaries (the
+    limiter boxes have no vertical flow, so every level counts)."""
+    g, e = np.asarray(got), np.asarray(want)
+    _, nyd, nxd = g.shape
+    g, e = g[:, margin:nyd - margin, margin:nxd - margin], e[:, margin:nyd - margin, margin:nxd - margin]
+    return float((np.abs(g - e) / np.abs(e)).max())
+
+
 # ---- barotropic subcycle ----
 #
 # With no Coriolis force, no forcing, a flat bottom (depth H), every cell wet and
