@@ -186,15 +186,17 @@ def limiter_expected(T, axis, c, sign, psi):
     return T + c * (F - np.roll(F, 1, axis))
 
 
-def make_limiter_box(case, axis, ni=30, nj=30, nk=12, dx=8000.0, dy=6000.0, dz=10.0, dt=2000.0):
-    """make_box with flow along x (axis 2) or y (axis 1) at the case's Courant
-    number and the case's profile along it; returns (domain, expected, psi)."""
+def make_limiter_box(case, axis, ni=30, nj=30, nk=None, dx=8000.0, dy=6000.0, dz=10.0, dt=2000.0):
+    """make_box with flow along x (axis 2), y (axis 1) or z (axis 0: k counts
+    down, so the case's sign is that of -w) at the case's Courant number and the
+    case's profile along it; returns (domain, expected, psi)."""
     import torch
     r, c, sign, branch = LIMITER_CASES[case]
-    spacing = dx if axis == 2 else dy
+    nk = nk if nk is not None else (30 if axis == 0 else 12)
+    spacing = (dz, dy, dx)[axis]
     vel = sign * c * spacing / dt
-    u, v = (vel, 0.0) if axis == 2 else (0.0, vel)
-    dom, _ = make_box("linear", u, v, 0.0, ni=ni, nj=nj, nk=nk, dx=dx, dy=dy, dz=dz)
+    u, v, w = (vel, 0.0, 0.0) if axis == 2 else (0.0, vel, 0.0) if axis == 1 else (0.0, 0.0, -vel)
+    dom, _ = make_box("linear", u, v, w, ni=ni, nj=nj, nk=nk, dx=dx, dy=dy, dz=dz)
     shape = tuple(dom["T"][0].shape)
     T0 = limiter_profile(r, shape, axis)
     dom["T"][0].copy_(torch.from_numpy(T0))
@@ -204,20 +206,22 @@ def make_limiter_box(case, axis, ni=30, nj=30, nk=12, dx=8000.0, dy=6000.0, dz=1
     return dom, limiter_expected(T0, axis, c, sign, psi), psi
 
 
-def rel_err_side(got, want, margin=8):
-    """max|got - want| / max|want| away from the side boundaries."""
-    g, e = np.asarray(got), np.asarray(want)
-    _, nyd, nxd = g.shape
-    g, e = g[:, margin:nyd - margin, margin:nxd - margin], e[:, margin:nyd - margin, margin:nxd - margin]
+def _away(a, margin, vertical):
+    nk, nyd, nxd = a.shape
+    km = margin if vertical else 0
+    return a[km:nk - km, margin:nyd - margin, margin:nxd - margin]
+
+
+def rel_err_side(got, want, margin=8, vertical=False):
+    """max|got - want| / max|want| away from the side boundaries (and from the
+    top and bottom when the flow is vertical)."""
+    g, e = _away(np.asarray(got), margin, vertical), _away(np.asarray(want), margin, vertical)
     return float(np.abs(g - e).max() / np.abs(e).max())
 
 
-def rel_err_cells(got, want, margin=8):
-    """Largest per-cell relative difference away from the side boundaries (the
-    limiter boxes have no vertical flow, so every level counts)."""
-    g, e = np.asarray(got), np.asarray(want)
-    _, nyd, nxd = g.shape
-    g, e = g[:, margin:nyd - margin, margin:nxd - margin], e[:, margin:nyd - margin, margin:nxd - margin]
+def rel_err_cells(got, want, margin=8, vertical=False):
+    """Largest per-cell relative difference, cells as in rel_err_side."""
+    g, e = _away(np.asarray(got), margin, vertical), _away(np.asarray(want), margin, vertical)
     return float((np.abs(g - e) / np.abs(e)).max())
 
 
