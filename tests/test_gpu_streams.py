@@ -32,3 +32,33 @@ def test_first_touch_copy_on_another_stream(gpu_lib):
     got = d.get(capi.F.TRACER, n=2, level=3)
     assert np.array_equal(got, src.numpy())
     d.close()
+
+
+@pytest.mark.parametrize("count", [1, 8, 9, 300])
+def test_copy_boxes_strided(gpu_lib, count):
+    """mom5gpu_copy_boxes moves every box of a call, strided on both sides, in
+    launches of up to 256 boxes whose descriptors travel as kernel parameters
+    (8 or fewer in a small parameter block): 1, 8, 9 and 300 boxes against the
+    same copies made with numpy."""
+    capi = gpu_lib
+    import torch
+    rng = np.random.default_rng(count)
+    src = torch.from_numpy(rng.standard_normal(4096 * 8)).cuda()
+    dst = torch.zeros(4096 * 8, dtype=torch.float64, device="cuda")
+    want = np.zeros(dst.numel())
+    s_np = src.cpu().numpy()
+    boxes = []
+    for b in range(count):
+        n = [int(rng.integers(1, 6)), int(rng.integers(1, 5)), int(rng.integers(1, 4))]
+        ss = [int(rng.integers(1, 3)), 8, 40]        # source strides: elements, rows, planes
+        ds = [1, n[0], n[0] * n[1]]                  # destination: packed
+        so = int(rng.integers(0, src.numel() - 200))
+        do = (b * 64) % (dst.numel() - 64)           # distinct 64-element slots (count <= 512)
+        for z in range(n[2]):
+            for y in range(n[1]):
+                for x in range(n[0]):
+                    want[do + x * ds[0] + y * ds[1] + z * ds[2]] = s_np[so + x * ss[0] + y * ss[1] + z * ss[2]]
+        boxes.append(capi.Box(src.data_ptr() + 8 * so, dst.data_ptr() + 8 * do, tuple(ss), tuple(ds), tuple(n)))
+    capi.copy_boxes(boxes)
+    torch.cuda.synchronize()
+    assert np.array_equal(dst.cpu().numpy(), want)
