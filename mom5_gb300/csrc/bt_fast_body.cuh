@@ -12,10 +12,10 @@
 //   A  = dtbt*f/2
 //   BX = -dtbt*thicku*dxur*umask/2, BY = -dtbt*thicku*dyur*umask/2 on compute
 //        points (0 elsewhere: no pressure gradient there)
-//   FU = dtbt*forcing_u, FV = dtbt*forcing_v
 //   G1 = cori2 - 1, G2 = cori2*cori1            (the Coriolis rotation as an increment)
-//   PX = BX*Px(patm + rho_g*E), PY = BY*Py(patm + rho_g*E)
-//        (the pressure gradient of the step's initial surface E, an FP64 plane)
+//   PX = BX*Px(patm + rho_g*E) + dtbt*forcing_u, PY = BY*Py(patm + rho_g*E) + dtbt*forcing_v
+//        (the pressure gradient of the step's initial surface E, an FP64 plane, and
+//        the forcing, each rounded to FP32 and summed in FP32)
 //   RG = rho_g
 // With D the undivided DIV_UD numerator of the transports and Px, Py the
 // undivided corner differences of rho_g*(eta - E) (a float plane PS written by
@@ -23,7 +23,7 @@
 // against the gradient), a subcycle is
 //   eta(new) = eta(old) + [S + K*D]
 //   u(new)   = u + [d1 + G1*t1 + G2*t2],  v(new) = v + [d2 + G1*t2 - G2*t1]
-//   d1 = A*v + BX*Px + PX + FU,  d2 = -A*u + BY*Py + PY + FV,  t1 = u + d1,  t2 = v + d2
+//   d1 = A*v + BX*Px + PX,  d2 = -A*u + BY*Py + PY,  t1 = u + d1,  t2 = v + d2
 // (algebraically u(new) = cori2*(t1 + cori1*t2), v(new) = cori2*(t2 - cori1*t1)),
 // the brackets in FP32 and each added to the FP64 state with one FP64 add.  D
 // is formed from four FP64 differences of neighbouring transports summed in
@@ -40,7 +40,8 @@ namespace btfast {
 
 #define DEVI __device__ __forceinline__
 
-enum { KG = 0, SG, KC, SC, A, BX, BY, FU, FV, G1, G2, PX, PY, RG, PS, DV, E0, E1, DV1, NPLANES };
+enum { KG = 0, SG, KC, SC, A, BX, BY, G1, G2, PX, PY, RG, PS, DV, E0, E1, DV1, NPLANES };
+static_assert(E0 % 2 == 0, "the FP64 plane E starts on an 8-byte boundary");
 static_assert(NPLANES <= 2 * kBtFastPlanes, "float planes of the precision-form subcycle");
 
 DEVI long I2(const Geo& g, int i, int j) { return (long)j * g.nxd + i; }
@@ -115,18 +116,15 @@ DEVI void mom_point(const BtArgs& a, int so, long q, float px, float py, double&
   const long n2 = a.g.n2;
   double uo = a.ubt[so * n2 + q], vo = a.vbt[so * n2 + q];
   float uf = mixed::d2f_rn(uo), vf = mixed::d2f_rn(vo), hf = plane(a, A)[q];
-  float d1 = fmaf(hf, vf, fmaf(plane(a, BX)[q], px, plane(a, PX)[q] + plane(a, FU)[q]));
-  float d2 = fmaf(-hf, uf, fmaf(plane(a, BY)[q], py, plane(a, PY)[q] + plane(a, FV)[q]));
+  float d1 = fmaf(hf, vf, fmaf(plane(a, BX)[q], px, plane(a, PX)[q]));
+  float d2 = fmaf(-hf, uf, fmaf(plane(a, BY)[q], py, plane(a, PY)[q]));
   float t1 = uf + d1, t2 = vf + d2, g1 = plane(a, G1)[q], g2 = plane(a, G2)[q];
   un = uo + mixed::f2d(d1 + fmaf(g1, t1, g2 * t2));
   vn = vo + mixed::f2d(d2 + fmaf(g1, t2, -g2 * t1));
 }
-// corrector of point q from its divergence D and new transports, with the time sums
-DEVI double corr_point(const BtArgs& a, int so, int sn, double wgt, long q, float D, double un, double vn) {
-  const long n2 = a.g.n2;
-  double en = a.eta_bt[so * n2 + q] + mixed::f2d(fmaf(plane(a, KC)[q], D, plane(a, SC)[q]));
-  a.eta_bt[sn * n2 + q] = en;
-  a.eta_bar[q] += en;
+// time sums of the transports of point q, formed where the new transports are
+// (the momentum step; the corrector does not change them)
+DEVI void sum_point(const BtArgs& a, double wgt, long q, double un, double vn) {
   if (a.stepB) {
     a.udrho_u[q] = fma(wgt, un, a.udrho_u[q]);
     a.udrho_v[q] = fma(wgt, vn, a.udrho_v[q]);
@@ -134,6 +132,13 @@ DEVI double corr_point(const BtArgs& a, int so, int sn, double wgt, long q, floa
     a.udrho_u[q] += un;
     a.udrho_v[q] += vn;
   }
+}
+// corrector of point q from its divergence D, with the time sum of eta
+DEVI double corr_point(const BtArgs& a, int so, int sn, long q, float D) {
+  const long n2 = a.g.n2;
+  double en = a.eta_bt[so * n2 + q] + mixed::f2d(fmaf(plane(a, KC)[q], D, plane(a, SC)[q]));
+  a.eta_bt[sn * n2 + q] = en;
+  a.eta_bar[q] += en;
   return en;
 }
 
@@ -153,8 +158,6 @@ DEVI void prep_body(const BtArgs& a, int bx, int by) {
   double bxq = comp ? -th * a.dxur[q] : 0.0, byq = comp ? -th * a.dyur[q] : 0.0;
   plane(a, BX)[q] = (float)bxq;
   plane(a, BY)[q] = (float)byq;
-  plane(a, FU)[q] = (float)(a.dtbt * a.forcing_u[q]);
-  plane(a, FV)[q] = (float)(a.dtbt * a.forcing_v[q]);
   plane(a, G1)[q] = (float)(a.cori2[q] - 1.0);
   plane(a, G2)[q] = (float)(a.cori2[q] * a.cori1[q]);
   // E = eta_bt at the first subcycle's old level (eta_t_bar(tau), set by the init kernel)
@@ -167,8 +170,8 @@ DEVI void prep_body(const BtArgs& a, int bx, int by) {
     pxa = bxq * ((p10 + p11) - (p00 + p01));
     pya = byq * ((p01 + p11) - (p00 + p10));
   }
-  plane(a, PX)[q] = (float)pxa;
-  plane(a, PY)[q] = (float)pya;
+  plane(a, PX)[q] = (float)pxa + (float)(a.dtbt * a.forcing_u[q]);
+  plane(a, PY)[q] = (float)pya + (float)(a.dtbt * a.forcing_v[q]);
   plane(a, RG)[q] = (float)a.rho_g[q];
 }
 
@@ -184,7 +187,7 @@ DEVI void pred_body(const BtArgs& a, int so, int sn, int reuse, int bx, int by) 
   plane(a, PS)[q0] = ps;
 }
 
-DEVI void mom_body(const BtArgs& a, int so, int sn, int bx, int by) {
+DEVI void mom_body(const BtArgs& a, int so, int sn, double wgt, int bx, int by) {
   const Geo& g = a.g;
   int i = bx * blockDim.x + threadIdx.x, j = by;
   if (i > g.ni + 1) return;
@@ -200,16 +203,17 @@ DEVI void mom_body(const BtArgs& a, int so, int sn, int bx, int by) {
   a.vbt[sn * n2 + q] = vn;
   a.uhb[sn * n2 + q] = un * a.dyu[q];
   a.vhb[sn * n2 + q] = vn * a.dxu[q];
+  sum_point(a, wgt, q, un, vn);
 }
 
-DEVI void corr_body(const BtArgs& a, int so, int sn, double wgt, int bx, int by) {
+DEVI void corr_body(const BtArgs& a, int so, int sn, int bx, int by) {
   const Geo& g = a.g;
   int i = bx * blockDim.x + threadIdx.x, j = by;
   if (i > g.ni + 1) return;
   long q = I2(g, i, j), n2 = g.n2;
   float D = div_num(g, a.uhb + sn * n2, a.vhb + sn * n2, i, j);
   plane(a, DV)[q] = D;
-  corr_point(a, so, sn, wgt, q, D, a.ubt[sn * n2 + q], a.vbt[sn * n2 + q]);
+  corr_point(a, so, sn, q, D);
 }
 
 // Corrector of subcycle t and predictor of subcycle t+1 in one launch.  The
@@ -220,13 +224,13 @@ DEVI void corr_body(const BtArgs& a, int so, int sn, double wgt, int bx, int by)
 // it is.  The predicted eta is not stored (the next corrector overwrites it
 // unread), nor is the divergence.  Same arithmetic as corr_body then pred_body
 // with reuse, so the same bits.
-DEVI void corr_pred_body(const BtArgs& a, int so, int sn, double wgt, int bx, int by) {
+DEVI void corr_pred_body(const BtArgs& a, int so, int sn, int bx, int by) {
   const Geo& g = a.g;
   int i = bx * blockDim.x + threadIdx.x, j = by;
   if (i > g.ni + 1) return;
   long q = I2(g, i, j), n2 = g.n2;
   const float D = div_num(g, a.uhb + sn * n2, a.vhb + sn * n2, i, j);
-  double en = corr_point(a, so, sn, wgt, q, D, a.ubt[sn * n2 + q], a.vbt[sn * n2 + q]);
+  double en = corr_point(a, so, sn, q, D);
   // the next subcycle's predictor at this point (pred_point with reuse)
   if (a.gamma > 0.0) en += mixed::f2d(fmaf(plane(a, KG)[q], D, plane(a, SG)[q]));
   float* ps = plane(a, PS);
@@ -276,7 +280,7 @@ DEVI void fused_body(const BtArgs& a, int so, int sn, int reuse, double wgt, int
   constexpr int PXN = TX + 2, PYN = TY + 2;  // PS: points x0-1 .. x0+TX, y0-1 .. y0+TY
   constexpr int MX = TX + 1, MY = TY + 1;    // momentum: points x0-1 .. x0+TX-1, y0-1 .. y0+TY-1
   __shared__ float ps_s[PYN * PXN];
-  __shared__ double un_s[MY * MX], vn_s[MY * MX], uh_s[MY * MX], vh_s[MY * MX];
+  __shared__ double uh_s[MY * MX], vh_s[MY * MX];
   const Geo& g = a.g;
   const long n2 = g.n2;
   const int x0 = bx * TX, y0 = by * TY;
@@ -304,8 +308,6 @@ DEVI void fused_body(const BtArgs& a, int so, int sn, int reuse, double wgt, int
     double un, vn;
     mom_point(a, so, q, px, py, un, vn);
     const double uh = un * a.dyu[q], vh = vn * a.dxu[q];
-    un_s[e] = un;
-    vn_s[e] = vn;
     uh_s[e] = uh;
     vh_s[e] = vh;
     if (li >= 1 && lj >= 1) {  // the tile's own points: the state the next subcycle reads
@@ -313,10 +315,11 @@ DEVI void fused_body(const BtArgs& a, int so, int sn, int reuse, double wgt, int
       a.vbt[sn * n2 + q] = vn;
       a.uhb[sn * n2 + q] = uh;
       a.vhb[sn * n2 + q] = vh;
+      sum_point(a, wgt, q, un, vn);
     }
   }
   __syncthreads();
-  // ---- corrector and time sums on the tile ----
+  // ---- corrector and the time sum of eta on the tile ----
   for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
     const int li = e % TX + 1, lj = e / TX + 1;  // in the momentum arrays
     const int i = x0 - 1 + li, j = y0 - 1 + lj;
@@ -327,7 +330,7 @@ DEVI void fused_body(const BtArgs& a, int so, int sn, int reuse, double wgt, int
                         ? div_sum(uh_s[m], uh_s[mw], uh_s[ms], uh_s[msw], vh_s[m], vh_s[mw], vh_s[ms], vh_s[msw])
                         : 0.0f;
     dv_n[q] = D;
-    corr_point(a, so, sn, wgt, q, D, un_s[m], vn_s[m]);
+    corr_point(a, so, sn, q, D);
   }
 }
 

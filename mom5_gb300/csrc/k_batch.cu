@@ -58,17 +58,17 @@ __global__ void __launch_bounds__(128) kb_btf_pred(const BtArgs* d, BatchWork w,
   BTF_ENTRY
   btfast::pred_body(a, so, sn, reuse, bx, by);
 }
-__global__ void __launch_bounds__(128) kb_btf_mom(const BtArgs* d, BatchWork w, int so, int sn) {
+__global__ void __launch_bounds__(128) kb_btf_mom(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
   BTF_ENTRY
-  btfast::mom_body(a, so, sn, bx, by);
+  btfast::mom_body(a, so, sn, wgt, bx, by);
 }
-__global__ void __launch_bounds__(128) kb_btf_corr(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+__global__ void __launch_bounds__(128) kb_btf_corr(const BtArgs* d, BatchWork w, int so, int sn) {
   BTF_ENTRY
-  btfast::corr_body(a, so, sn, wgt, bx, by);
+  btfast::corr_body(a, so, sn, bx, by);
 }
-__global__ void __launch_bounds__(128) kb_btf_corr_pred(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+__global__ void __launch_bounds__(128) kb_btf_corr_pred(const BtArgs* d, BatchWork w, int so, int sn) {
   BTF_ENTRY
-  btfast::corr_pred_body(a, so, sn, wgt, bx, by);
+  btfast::corr_pred_body(a, so, sn, bx, by);
 }
 
 template <int NC, int ZR>
@@ -109,9 +109,9 @@ int launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int itime, i
   const int so = itime % 2, sn = (itime + 1) % 2;
   const double wgt = (double)(nts - itime + 1);
   if (itime == 1) kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, 0);
-  kb_btf_mom<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
-  if (itime < nts) kb_btf_corr_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
-  else kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
+  kb_btf_mom<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
+  if (itime < nts) kb_btf_corr_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
+  else kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
   return itime == 1 ? 3 : 2;
 }
 

@@ -78,14 +78,14 @@ __global__ void __launch_bounds__(128) k_btf_prep(BtArgs a) { btfast::prep_body(
 __global__ void __launch_bounds__(128) k_btf_pred(BtArgs a, int so, int sn, int reuse) {
   btfast::pred_body(a, so, sn, reuse, blockIdx.x, blockIdx.y);
 }
-__global__ void __launch_bounds__(128) k_btf_mom(BtArgs a, int so, int sn) {
-  btfast::mom_body(a, so, sn, blockIdx.x, blockIdx.y);
+__global__ void __launch_bounds__(128) k_btf_mom(BtArgs a, int so, int sn, double wgt) {
+  btfast::mom_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
 }
-__global__ void __launch_bounds__(128) k_btf_corr(BtArgs a, int so, int sn, double wgt) {
-  btfast::corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
+__global__ void __launch_bounds__(128) k_btf_corr(BtArgs a, int so, int sn) {
+  btfast::corr_body(a, so, sn, blockIdx.x, blockIdx.y);
 }
-__global__ void __launch_bounds__(128) k_btf_corr_pred(BtArgs a, int so, int sn, double wgt) {
-  btfast::corr_pred_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
+__global__ void __launch_bounds__(128) k_btf_corr_pred(BtArgs a, int so, int sn) {
+  btfast::corr_pred_body(a, so, sn, blockIdx.x, blockIdx.y);
 }
 
 void launch_btf_prep(const BtArgs& a, cudaStream_t s) {
@@ -95,12 +95,12 @@ void launch_btf_prep(const BtArgs& a, cudaStream_t s) {
 
 // One launch per subcycle (mom5gpu_set_barotropic_fusion mode 1): 32 x 8 tiles of
 // 352 threads, one point per thread in each phase (the 34 x 10 surface-pressure
-// ring is the largest).  Measured per precision-form step: 0.62 ms against 0.81
-// ms for the three launches on 360x300 (80 subcycles), where the launches set the
-// time, but 6.7 ms against 5.0 ms on 1440x1080 (60 subcycles), which the three
-// streaming launches keep near the memory bound.  On 360x300 the 64 x 8 (256
-// threads, several points per thread), 32 x 16, 128 x 4 and 64 x 16 tiles took
-// 0.81-1.01 ms.
+// ring is the largest).  Measured per precision-form step: 0.66 ms against 0.72
+// ms for form 0 on 360x300 (80 subcycles), where the launches set the time, but
+// 7.2 ms against 4.6 ms on 1440x1080 (60 subcycles), which form 0's streaming
+// launches keep near the memory bound.  On 360x300 the 64 x 8 (256 threads,
+// several points per thread), 32 x 16, 128 x 4 and 64 x 16 tiles were slower
+// than 32 x 8.
 constexpr int kBtfTX = 32, kBtfTY = 8, kBtfThreads = 352;
 __global__ void __launch_bounds__(kBtfThreads) k_btf_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
   btfast::fused_body<kBtfTX, kBtfTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
@@ -120,9 +120,9 @@ int launch_btf_subcycle(const BtArgs& a, int itime, int nts, bool fused, cudaStr
   }
   dim3 g2((a.g.ni + 2 + 127) / 128, a.g.nj + 2);
   if (itime == 1) k_btf_pred<<<g2, 128, 0, s>>>(a, so, sn, 0);
-  k_btf_mom<<<g2, 128, 0, s>>>(a, so, sn);
-  if (itime < nts) k_btf_corr_pred<<<g2, 128, 0, s>>>(a, so, sn, wgt);
-  else k_btf_corr<<<g2, 128, 0, s>>>(a, so, sn, wgt);
+  k_btf_mom<<<g2, 128, 0, s>>>(a, so, sn, wgt);
+  if (itime < nts) k_btf_corr_pred<<<g2, 128, 0, s>>>(a, so, sn);
+  else k_btf_corr<<<g2, 128, 0, s>>>(a, so, sn);
   return itime == 1 ? 3 : 2;
 }
 
