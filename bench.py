@@ -377,8 +377,8 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
 
     Three time levels rotate, so the tracer level a step reads is the one the
     step two before wrote: its tracers are uploaded straight into that level
-    (mom5gpu_copy_field_async, host to device) as soon as that step's read-back
-    of it is done, during the previous step's compute.  The velocity and the
+    (mom5gpu_copy_field_async, host to device), each as soon as that step's
+    read-back of the same tracer is done, during the previous step's compute.  The velocity and the
     forcing have one copy each in the library, busy until the previous step's
     advection or barotropic step ends: they are uploaded into device staging
     buffers early and moved into their fields by a staging stream
@@ -422,6 +422,7 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
     tev = lambda: torch.cuda.Event(enable_timing=True)
     names = ("up0", "ups1", "upt0", "up1", "stg1", "c0", "adv", "c1", "d2h0", "d2h1")
     ev = {k: [tev() for _ in range(total)] for k in names}
+    tr_done = []  # per step: tracer n -> event after its read-back
     torch.cuda.synchronize()
     t0 = None
     for s_ in range(total):
@@ -437,11 +438,12 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
             for _, _, h, buf, _ in ups:
                 buf.copy_(h, non_blocking=True)
         ev["ups1"][s_].record(h2d)
-        # host -> tracer level lin, once the read-back of the step that wrote it is done
-        if s_ >= 2:
-            h2d.wait_event(ev["d2h1"][s_ - 2])
+        # host -> tracer level lin, each tracer once its read-back by the step
+        # that wrote the level is done (the two directions of the link overlap)
         ev["upt0"][s_].record(h2d)
         for fid, n, h in direct:
+            if s_ >= 2:
+                h2d.wait_event(tr_done[s_ - 2][n])
             d.copy_field_async(fid, h.data_ptr(), 1, h2d.cuda_stream, n=n, level=lin)
         ev["up1"][s_].record(h2d)
         # staging -> fields, each once its field is free, by the library's box copy
@@ -469,8 +471,12 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
         ev["c1"][s_].record(stream)
         d2h.wait_event(ev["c1"][s_])
         ev["d2h0"][s_].record(d2h)
+        tr_done.append({})
         for fid, n, h in downs:
             d.copy_field_async(fid, h.data_ptr(), 0, d2h.cuda_stream, n=n, level=lout)
+            if fid == F.TRACER:
+                tr_done[s_][n] = torch.cuda.Event()
+                tr_done[s_][n].record(d2h)
         ev["d2h1"][s_].record(d2h)
     torch.cuda.synchronize()
     te = (time.perf_counter() - t0) / steps
@@ -485,7 +491,8 @@ def run_e2e(d, stream, wl, ntr, steps, warm=3):
                 "host_wall": round(te * 1e3, 3), "compute_span": round(span, 3), "compute": round(mean("c0", "c1"), 3),
                 "upload": round(up, 3), "readback": round(rb, 3), "staging_to_fields": round(mean("ups1", "stg1"), 3),
                 "compute_waits_for_inputs": round(wait, 3),
-                "upload_GBps": round(hb / up / 1e6, 1) if up > 0 else None,
+                "upload_GBps": round(hb / up / 1e6, 1) if up > 0 else None,  # a lower bound: the tracer
+                # uploads' span includes their waits for the read-back of each tracer
                 "readback_GBps": round(db / rb / 1e6, 1) if rb > 0 else None}
     return te, hb, db, timeline
 
