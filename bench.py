@@ -899,7 +899,9 @@ def main():
         how = (f"whole grid, OpenMP on {cores} threads" if info["reported"] == "openmp"
                else f"{cores} processes x walled block {r['block']}")
         out = {"metric": METRIC, "value": round(v, 1), "unit": "cell-updates/s", "n_gpus": world,
-               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": round(1e3 * r["seconds"] / max(1, r["steps_timed"]), 3),
+               "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
                "config": {"workload": f"{args.config.upper()}: {wl.describe(spec)}, reference algorithm on the "
                                       f"host cores (the faster of: whole grid with OpenMP; one walled block per "
