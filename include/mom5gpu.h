@@ -449,10 +449,11 @@ int mom5gpu_batch_step(mom5gpu_batch* b, const int* index, const int* parity, in
 int mom5gpu_batch_autotune(mom5gpu_batch* b, double dtime, char* report, size_t report_len);
 /* Read or set the launch shape directly (e.g. to reuse one autotune result on
  * several batches): rows = precision-form tile height (16 or 32; 24 = the
- * TMA-staged 24-row tiles, one block per SM, for every domain with an even ni,
- * and the 32-row tiles for the others), tj = FP64 y-pass rows per thread (0 =
- * automatic, else 2, 4, 8 or 16), blocks_per_sm = resident blocks per SM of the
- * persistent launch of the plain tiles (1..4).  A TMA-staged tile whose bounded
+ * TMA-staged tiles, 24 rows or 32 for at most 4 tracers, one block per SM, for
+ * every domain with an even ni, and the plain 32-row tiles for the others), tj
+ * = FP64 y-pass rows per thread (0 = automatic, else 2, 4, 8 or 16),
+ * blocks_per_sm = resident blocks per SM of the persistent launch of the plain
+ * tiles (1..4).  A TMA-staged tile whose bounded
  * wait gave up is reported by the next mom5gpu_synchronize of its domain as
  * MOM5GPU_ETIMEDOUT. */
 int mom5gpu_batch_get_tuning(const mom5gpu_batch* b, int* rows, int* tj, int* blocks_per_sm);

@@ -143,7 +143,8 @@ void fill_work(const mom5gpu_batch* b, const std::vector<std::pair<int, int>>& l
   for (int e = 0; e < c; ++e) {
     const int dom = order[e].first;
     ent[e] = 2 * dom + order[e].second;
-    BatchBlocks bb = batch_blocks(b->doms[dom]->geo, TJ, b->rows, dom < (int)b->tma_ok.size() && b->tma_ok[dom]);
+    BatchBlocks bb =
+        batch_blocks(b->doms[dom]->geo, TJ, b->rows, dom < (int)b->tma_ok.size() && b->tma_ok[dom], b->ntr);
     int v[8] = {bb.z, bb.x, bb.y, bb.u, bb.b2, bb.b1, bb.m, bb.t};
     for (int k = 0; k < 8; ++k) pr[k][e + 1] = pr[k][e] + v[k];
   }

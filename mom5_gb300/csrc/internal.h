@@ -295,7 +295,7 @@ struct BatchWork {
 struct BatchBlocks {
   int z, x, y, u, b2, b1, m, t;
 };
-BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma);
+BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma, int ntr);
 // FP64: z/x/y MDFL passes and the explicit update for every entry
 void launch_batch_fp64_advection(const MdflArgs* mdfl, const UpdArgs* upd, const BatchWork& w, int ntr, bool sweby,
                                  int TJ, cudaStream_t s);
@@ -308,6 +308,7 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
 // the bytes of one (domain, parity) entry of the device table, filling an entry
 // (MOM5GPU_EUNSUPPORTED when the domain cannot be described to TMA), the launch
 size_t batch_tma_bytes();
+int batch_tma_rows(int ntr);
 int fill_batch_tma(mom5gpu_domain* d, const MixArgs& a, void* host_entry);
 int launch_batch_mixed_tma(const MixArgs* mix, const void* tma, const BatchWork& w, int ntr, int blocks, int* counter,
                            cudaStream_t s);

@@ -126,7 +126,7 @@ void adv(const MdflArgs* m, const UpdArgs* u, const BatchWork& w, int TJ, cudaSt
 
 }  // namespace
 
-BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma) {
+BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma, int ntr) {
   BatchBlocks b;
   int nb = (g.ni + 127) / 128;
   b.z = nb * g.nj;
@@ -139,7 +139,8 @@ BatchBlocks batch_blocks(const Geo& g, int TJ, int mixed_rows, bool tma) {
   const bool staged = mixed_rows == 24 && tma;
   int tj = (mixed_rows == 24 ? 32 : mixed_rows) - 4;
   b.m = staged ? 0 : ((g.ni + 27) / 28) * ((g.nj + tj - 1) / tj);
-  b.t = staged ? ((g.ni + 27) / 28) * ((g.nj + 19) / 20) : 0;
+  const int ttj = staged ? batch_tma_rows(ntr) - 4 : 1;
+  b.t = staged ? ((g.ni + 27) / 28) * ((g.nj + ttj - 1) / ttj) : 0;
   return b;
 }
 

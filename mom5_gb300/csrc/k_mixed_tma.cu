@@ -526,7 +526,13 @@ int run_tma_pairs(mom5gpu_domain* d, const MixArgs& a, int n0, const double* Tal
   return MOM5GPU_OK;
 }
 
-// ---- batches: TMA-staged 24-row tiles over a work list ----
+// ---- batches: TMA-staged tiles over a work list ----
+
+// tile height of the batched TMA kernel for a tracer count: 32 rows (1024 threads)
+// where the shared memory holds them, at most 4 tracers (C3, 4 tracers: 19.27 ms
+// per step against 19.37 with 24 rows), else 24
+template <int NC>
+constexpr int kBatchRows = NC <= 4 ? 32 : 24;
 
 // one (domain, parity) entry of a batch's device table: the tensor maps of its
 // tracer level and fields, and its domain's error word
@@ -545,13 +551,14 @@ DEVI int find_tile_entry(const int* prefix, int count, int b) {
   return lo;
 }
 
-// Persistent: one block of 768 threads per SM takes tiles from an atomic counter
+// Persistent: one block (768 or 1024 threads) per SM takes tiles from an atomic counter
 // (largest domains first) and runs each as the one-domain kernel does.  A block
 // whose bounded wait gave up stops; the others go on, and the domain's
 // mom5gpu_synchronize reports MOM5GPU_ETIMEDOUT.
 template <int NC>
-__global__ void __launch_bounds__(32 * 24, 1)
+__global__ void __launch_bounds__(32 * kBatchRows<NC>, 1)
     kb_mixed_tma(const MixArgs* __restrict__ d, const BatchTma* __restrict__ tm, BatchWork w, int* counter) {
+  constexpr int ZR = kBatchRows<NC>;
   __shared__ int item;
   for (;;) {
     if (threadIdx.x == 0) item = atomicAdd(counter, 1);
@@ -564,14 +571,15 @@ __global__ void __launch_bounds__(32 * 24, 1)
     const MixArgs& a = d[ent];
     const int local = it - w.pt[e];
     const int ntx = (a.g.ni + TI - 1) / TI;
-    if (!tma_tile<NC, 24, 1>(a, 0, 0, tm[ent].m, tm[ent].err, local % ntx, local / ntx)) return;
+    if (!tma_tile<NC, ZR, 1>(a, 0, 0, tm[ent].m, tm[ent].err, local % ntx, local / ntx)) return;
   }
 }
 
 template <int NC>
 int configure_batch_tma() {
+  constexpr int ZR = kBatchRows<NC>;
   return cudaFuncSetAttribute(kb_mixed_tma<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sizeof(TmaSmem<NC, 24, kWindowMode<NC, 24, 1>>)) == cudaSuccess
+                              (int)sizeof(TmaSmem<NC, ZR, kWindowMode<NC, ZR, 1>>)) == cudaSuccess
              ? MOM5GPU_OK
              : MOM5GPU_ECUDA;
 }
@@ -579,13 +587,19 @@ int configure_batch_tma() {
 template <int NC>
 void run_batch_tma(const MixArgs* mix, const BatchTma* tm, const BatchWork& w, int blocks, int* counter,
                    cudaStream_t s) {
+  constexpr int ZR = kBatchRows<NC>;
   cudaMemsetAsync(counter, 0, sizeof(int), s);
-  kb_mixed_tma<NC><<<blocks, 32 * 24, sizeof(TmaSmem<NC, 24, kWindowMode<NC, 24, 1>>), s>>>(mix, tm, w, counter);
+  kb_mixed_tma<NC><<<blocks, 32 * ZR, sizeof(TmaSmem<NC, ZR, kWindowMode<NC, ZR, 1>>), s>>>(mix, tm, w, counter);
 }
 
 }  // namespace
 
 size_t batch_tma_bytes() { return sizeof(BatchTma); }
+
+// the tile height for ntr tracers (the kernel instantiation launch_batch_mixed_tma picks)
+int batch_tma_rows(int ntr) {
+  return ntr <= 1 ? kBatchRows<1> : ntr <= 2 ? kBatchRows<2> : ntr <= 4 ? kBatchRows<4> : kBatchRows<10>;
+}
 
 int fill_batch_tma(mom5gpu_domain* d, const MixArgs& a, void* host_entry) {
   const Geo& g = d->geo;
@@ -594,10 +608,11 @@ int fill_batch_tma(mom5gpu_domain* d, const MixArgs& a, void* host_entry) {
   if (rc) return rc;
   BatchTma t;
   memset(&t, 0, sizeof(t));
-  bool ok = encode(&t.m.T, a.T, g, (long)a.ntr * g.nk, 24) && encode(&t.m.f[F_UH], a.uh, g, g.nk, 24) &&
-            encode(&t.m.f[F_VH], a.vh, g, g.nk, 24) && encode(&t.m.f[F_W], a.w, g, g.nk + 1, 24) &&
-            encode(&t.m.f[F_RDZ], a.rdz, g, g.nk, 24) && encode(&t.m.f[F_RDZR], a.rdzr, g, g.nk, 24) &&
-            encode(&t.m.f[F_RDZM1], a.rdz_m1, g, g.nk, 24);
+  const int zr = batch_tma_rows(a.ntr);
+  bool ok = encode(&t.m.T, a.T, g, (long)a.ntr * g.nk, zr) && encode(&t.m.f[F_UH], a.uh, g, g.nk, zr) &&
+            encode(&t.m.f[F_VH], a.vh, g, g.nk, zr) && encode(&t.m.f[F_W], a.w, g, g.nk + 1, zr) &&
+            encode(&t.m.f[F_RDZ], a.rdz, g, g.nk, zr) && encode(&t.m.f[F_RDZR], a.rdzr, g, g.nk, zr) &&
+            encode(&t.m.f[F_RDZM1], a.rdz_m1, g, g.nk, zr);
   if (!ok) return MOM5GPU_EUNSUPPORTED;
   t.err = d->wait_err;
   memcpy(host_entry, &t, sizeof(t));
