@@ -192,8 +192,8 @@ int enqueue_step(mom5gpu_batch* b, const BatchWork& w, const std::vector<std::pa
         mom5gpu_domain* d = b->doms[it.first];
         if (!(d->geo.cx || d->geo.cy)) continue;
         double* tp1 = fptr(d, MOM5GPU_TRACER, 1, 2 - it.second);
-        for (int n = 0; n < b->ntr; ++n) launch_halo_fill(d->geo, tp1 + (long)n * d->geo.n3, d->geo.nk, 3, s);
-        launches += b->ntr;
+        launch_halo_fill(d->geo, tp1, b->ntr * d->geo.nk, 3, s);  // every tracer's levels, one after another
+        launches += 1;
       }
     } else {
       rc = launch_batch_mixed(b->d_mix, b->d_tma, w, b->ntr, b->rows, b->blocks_per_sm * b->sms, b->sms, b->d_counter,

@@ -1138,10 +1138,13 @@ int launch_update_tracer(mom5gpu_domain* d, int n_first, int ntr, int taum1, int
   u.Tp1 += (long)(n_first - 1) * g.n3;
   u.th += (long)(n_first - 1) * g.n3;
   ClockScope clk(d, SEC_UPDATE);
-  count_launches(d, 1 + ((g.cx || g.cy) ? ntr : 0));
+  const bool contiguous = u.tstride == g.n3;  // the tracers' levels follow one another: one halo fill
+  count_launches(d, 1 + ((g.cx || g.cy) ? (contiguous ? 1 : ntr) : 0));
   dim3 grid((g.ni + 127) / 128, g.nj, g.nk);
   k_update_tracer<<<grid, 128, 0, d->stream>>>(u);
-  for (int n = 0; n < ntr; ++n) launch_halo_fill(g, u.Tp1 + n * u.tstride, g.nk, 3, d->stream);
+  if (contiguous) launch_halo_fill(g, u.Tp1, ntr * g.nk, 3, d->stream);
+  else
+    for (int n = 0; n < ntr; ++n) launch_halo_fill(g, u.Tp1 + n * u.tstride, g.nk, 3, d->stream);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "update_tracer");
 }
