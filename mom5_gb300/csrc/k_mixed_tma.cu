@@ -10,9 +10,9 @@
 //     k-1, k, k+1 carried down the column (in a shared-memory ring or in
 //     registers), so each level of each tracer is brought on chip once instead
 //     of four times;
-//   * three block barriers per level (face terms; z and x passes of every
-//     tracer; y fluxes of every tracer), the per-tracer intermediates in shared
-//     memory, instead of two barriers per tracer;
+//   * two block barriers per level (after the z and x passes of every tracer
+//     and after the y fluxes of every tracer), the per-tracer intermediates in
+//     shared memory, instead of two barriers per tracer;
 //   * the level that enters the window (k+2) arrives by TMA
 //     (cp.async.bulk.tensor, completion on an mbarrier) into one shared-memory
 //     slot per tracer, requested as soon as the slot is free -- one level and
@@ -136,9 +136,12 @@ constexpr int kWindowMode = MINB != 1 ? 0 : ZR == 16 ? 2 : 1;
 // together before their stores, were slower).
 constexpr int kOutRing = 4;
 
-// One level is three phases with a block barrier between them: (1) the level's
-// face terms, (2) the z and x passes of every tracer, (3) the y fluxes of every
-// tracer, then the outputs -- three barriers per level whatever the tracer count.
+// One level is three phases: (1) the level's face terms, (2) the z and x passes
+// of every tracer, (3) the y fluxes of every tracer, then the outputs, with a
+// block barrier after phases 2 and 3 -- two barriers per level whatever the
+// tracer count.  Phase 1 reads only the field boxes and its own registers, so it
+// runs into phase 2 without one; the next level's field boxes are fetched after
+// the phase 2 barrier, which every thread reaches only once its phase 1 is done.
 // One tile (tile_x, tile_y) of the domain a, with the block's whole shared memory;
 // false when a bounded wait gave up (*err set; the block must stop).  The
 // barriers are initialised at the start and invalidated at the end, so a
@@ -280,18 +283,8 @@ DEVI bool tma_tile(const MixArgs& a, int n0, int zt0, const TmaMaps& maps, int* 
         }
       }
     }
+    // read by the neighbouring rows in phase 3, after the next barrier
     s.wet[c] = in && wet;
-    // every thread is done with the level's field boxes: fetch the next level's
-    if (__syncthreads_or(bad)) goto abort;
-    if (threadIdx.x == 0) {
-      if (k + 1 < g.nk) {
-        mbar_expect(&s.bar[NC], 6u * SLOT * 8u);
-        for (int f = 0; f < 6; ++f) tma3(s.f[f], &maps.f[f], bx0, by0, f == F_W ? k + 2 : k + 1, &s.bar[NC]);
-        s.pending[NC] = 1 + ((k + 1) & 1);
-      } else {
-        s.pending[NC] = 0;
-      }
-    }
 
     const int r_km1 = (k + 2) % 3, r_k = k % 3, r_kp1 = (k + 1) % 3;  // ring slots of levels k-1, k, k+1
     // ---- phase 2: z and x passes of every tracer ----
@@ -349,9 +342,17 @@ DEVI bool tma_tile(const MixArgs& a, int n0, int zt0, const TmaMaps& maps, int* 
       s.tx[n][c] = xin ? tc : 0.f;
       s.fzx[n][c] = fa(in ? fzv : 0.f, xin ? fic : 0.f);
     }
-    // every tracer's slot is read: each takes level k+3
+    // every thread is done with the level's field boxes and every tracer's slot:
+    // the fields of the next level and level k+3 of each tracer are fetched
     if (__syncthreads_or(bad)) goto abort;
     if (threadIdx.x == 0) {
+      if (k + 1 < g.nk) {
+        mbar_expect(&s.bar[NC], 6u * SLOT * 8u);
+        for (int f = 0; f < 6; ++f) tma3(s.f[f], &maps.f[f], bx0, by0, f == F_W ? k + 2 : k + 1, &s.bar[NC]);
+        s.pending[NC] = 1 + ((k + 1) & 1);
+      } else {
+        s.pending[NC] = 0;
+      }
       for (int n = 0; n < ntr; ++n) {
         if (k + 1 < g.nk) {
           mbar_expect(&s.bar[n], SLOT * 8u);
