@@ -258,6 +258,32 @@ int launch_tmask_limit(mom5gpu_domain* d, int n, int tau);
 int launch_tmask_limit_ts_same(mom5gpu_domain* d, int nt, int ns);
 int launch_eta_tendency(mom5gpu_domain* d, int tau);
 int launch_eta_update(mom5gpu_domain* d, int taum1, int taup1, double dtime);
+// Programmatic dependent launch of the barotropic subcycle kernels.  A kernel
+// launched by launch_pdl may be scheduled while the kernel before it in the
+// stream runs its last blocks; its blocks first wait in pdl_wait()
+// (griddepcontrol.wait) until that kernel has completed and its writes are
+// visible, then allow the next kernel to be scheduled (pdl_trigger), so every
+// kernel still reads only completed results.  Launched the ordinary way, the
+// two instructions do nothing.
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+#endif
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s, A... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // precision-form barotropic subcycle (k_mixed.cu, k_batch.cu)
 void launch_btf_prep(const BtArgs& a, cudaStream_t s);
 int launch_btf_subcycle(const BtArgs& a, int itime, int nts, bool fused, cudaStream_t s);

@@ -55,18 +55,26 @@ __global__ void __launch_bounds__(128) kb_btf_prep(const BtArgs* d, BatchWork w)
   btfast::prep_body(a, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_btf_pred(const BtArgs* d, BatchWork w, int so, int sn, int reuse) {
+  pdl_wait();
+  pdl_trigger();
   BTF_ENTRY
   btfast::pred_body(a, so, sn, reuse, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_btf_mom(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   BTF_ENTRY
   btfast::mom_body(a, so, sn, wgt, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_btf_corr(const BtArgs* d, BatchWork w, int so, int sn) {
+  pdl_wait();
+  pdl_trigger();
   BTF_ENTRY
   btfast::corr_body(a, so, sn, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_btf_corr_pred(const BtArgs* d, BatchWork w, int so, int sn) {
+  pdl_wait();
+  pdl_trigger();
   BTF_ENTRY
   btfast::corr_pred_body(a, so, sn, bx, by);
 }
@@ -108,10 +116,11 @@ int launch_batch_btf_subcycle(const BtArgs* bt, const BatchWork& w, int itime, i
   if (w.tb2 <= 0) return 0;
   const int so = itime % 2, sn = (itime + 1) % 2;
   const double wgt = (double)(nts - itime + 1);
-  if (itime == 1) kb_btf_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, 0);
-  kb_btf_mom<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, wgt);
-  if (itime < nts) kb_btf_corr_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
-  else kb_btf_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
+  const dim3 g2(w.tb2), b(128);
+  if (itime == 1) launch_pdl(kb_btf_pred, g2, b, s, bt, w, so, sn, 0);
+  launch_pdl(kb_btf_mom, g2, b, s, bt, w, so, sn, wgt);
+  if (itime < nts) launch_pdl(kb_btf_corr_pred, g2, b, s, bt, w, so, sn);
+  else launch_pdl(kb_btf_corr, g2, b, s, bt, w, so, sn);
   return itime == 1 ? 3 : 2;
 }
 

@@ -81,18 +81,26 @@ __global__ void __launch_bounds__(256) kb_bt_init(const BtArgs* d, const BtExtra
   int bx = local % nb, by = local / nb;
 
 __global__ void __launch_bounds__(128) kb_bt_pred(const BtArgs* d, BatchWork w, int so, int sn, int reuse) {
+  pdl_wait();
+  pdl_trigger();
   BT2D_ENTRY
   bt_pred_body(a, so, sn, reuse, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_bt_mom_b(const BtArgs* d, BatchWork w, int so, int sn) {
+  pdl_wait();
+  pdl_trigger();
   BT2D_ENTRY
   bt_mom_b_body(a, so, sn, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_bt_corr(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   BT2D_ENTRY
   bt_corr_body(a, so, sn, wgt, bx, by);
 }
 __global__ void __launch_bounds__(128) kb_bt_corr_pred(const BtArgs* d, BatchWork w, int so, int sn, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   BT2D_ENTRY
   bt_corr_pred_body(a, so, sn, wgt, bx, by);
 }
@@ -170,10 +178,13 @@ void launch_batch_barotropic_loop(const BtArgs* bt, const BtExtra* x, const Batc
       continue;
     }
     // as the one-domain form: the predictor launched only in the first subcycle
-    if (itime == 1) kb_bt_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, 0);
-    kb_bt_mom_b<<<w.tb2, 128, 0, s>>>(bt, w, so, sn);
-    if (itime < nts) kb_bt_corr_pred<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));
-    else kb_bt_corr<<<w.tb2, 128, 0, s>>>(bt, w, so, sn, (double)(nts - itime + 1));
+    // programmatic dependents (launch_pdl), as the one-domain subcycle kernels
+    const dim3 g2(w.tb2), b(128);
+    const double wgt = (double)(nts - itime + 1);
+    if (itime == 1) launch_pdl(kb_bt_pred, g2, b, s, bt, w, so, sn, 0);
+    launch_pdl(kb_bt_mom_b, g2, b, s, bt, w, so, sn);
+    if (itime < nts) launch_pdl(kb_bt_corr_pred, g2, b, s, bt, w, so, sn, wgt);
+    else launch_pdl(kb_bt_corr, g2, b, s, bt, w, so, sn, wgt);
   }
   (void)stepB;
 }

@@ -1259,11 +1259,26 @@ __global__ void k_bt_init(BtArgs a, const double* eta_bar_tau, const double* eta
                           const double* vd_tau, const double* pme, const double* river, const double* source,
                           const double* eta_smooth, int initsum_with_bar) { bt_init_body(a, eta_bar_tau, eta_tau, ud_tau, vd_tau, pme, river, source, eta_smooth, initsum_with_bar, blockIdx.x, blockIdx.y); }
 __global__ void k_bt_cgrid_init(BtArgs a) { bt_cgrid_init_body(a, blockIdx.x, blockIdx.y); }
-__global__ void k_bt_pred(BtArgs a, int so, int sn, int reuse) { bt_pred_body(a, so, sn, reuse, blockIdx.x, blockIdx.y); }
-__global__ void k_bt_mom_b(BtArgs a, int so, int sn) { bt_mom_b_body(a, so, sn, blockIdx.x, blockIdx.y); }
+// The B-grid subcycle kernels are launched as programmatic dependents (launch_pdl).
+__global__ void k_bt_pred(BtArgs a, int so, int sn, int reuse) {
+  pdl_wait();
+  pdl_trigger();
+  bt_pred_body(a, so, sn, reuse, blockIdx.x, blockIdx.y);
+}
+__global__ void k_bt_mom_b(BtArgs a, int so, int sn) {
+  pdl_wait();
+  pdl_trigger();
+  bt_mom_b_body(a, so, sn, blockIdx.x, blockIdx.y);
+}
 __global__ void k_bt_mom_c(BtArgs a, int so, int sn, int itime) { bt_mom_c_body(a, so, sn, itime, blockIdx.x, blockIdx.y); }
-__global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) { bt_corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y); }
+__global__ void k_bt_corr(BtArgs a, int so, int sn, double wgt) {
+  pdl_wait();
+  pdl_trigger();
+  bt_corr_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
+}
 __global__ void k_bt_corr_pred(BtArgs a, int so, int sn, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   bt_corr_pred_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
 }
 // 32 x 8 tiles of 352 threads: one point per thread in each phase (the 34 x 10
@@ -1271,6 +1286,8 @@ __global__ void k_bt_corr_pred(BtArgs a, int so, int sn, double wgt) {
 // per thread, took 1.80 ms per step on 360x300 against 1.41 ms
 constexpr int kFusedTX = 32, kFusedTY = 8, kFusedThreads = 352;
 __global__ void __launch_bounds__(kFusedThreads) k_bt_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   bt_fused_body<kFusedTX, kFusedTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
 }
 // ---- every exact B-grid subcycle of a step in one cooperative launch ----
@@ -1608,16 +1625,17 @@ int launch_barotropic(mom5gpu_domain* d, int tau, int taup1) {
         continue;
       }
       if (fused) {  // predictor, momentum and corrector in one launch
-        k_bt_fused<<<gf, kFusedThreads, 0, st>>>(a, so, sn, itime > 1, (double)(a.nts - itime + 1));
+        launch_pdl(k_bt_fused, gf, dim3(kFusedThreads), st, a, so, sn, (int)(itime > 1), (double)(a.nts - itime + 1));
         continue;
       }
       if (!a.cgrid) {
         // B grid: the predictor as a launch of its own only in the first
         // subcycle; every corrector but the last forms the next predictor
-        if (itime == 1) k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, 0);
-        k_bt_mom_b<<<g2, 128, 0, st>>>(a, so, sn);
-        if (itime < a.nts) k_bt_corr_pred<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
-        else k_bt_corr<<<g2, 128, 0, st>>>(a, so, sn, (double)(a.nts - itime + 1));
+        const double wgt = (double)(a.nts - itime + 1);
+        if (itime == 1) launch_pdl(k_bt_pred, g2, dim3(128), st, a, so, sn, 0);
+        launch_pdl(k_bt_mom_b, g2, dim3(128), st, a, so, sn);
+        if (itime < a.nts) launch_pdl(k_bt_corr_pred, g2, dim3(128), st, a, so, sn, wgt);
+        else launch_pdl(k_bt_corr, g2, dim3(128), st, a, so, sn, wgt);
         continue;
       }
       k_bt_pred<<<g2, 128, 0, st>>>(a, so, sn, itime > 1);

@@ -75,16 +75,25 @@ int run_mixed(mom5gpu_domain* d, MixArgs a, int n0) {
 }  // namespace
 
 __global__ void __launch_bounds__(128) k_btf_prep(BtArgs a) { btfast::prep_body(a, blockIdx.x, blockIdx.y); }
+// The subcycle kernels are launched as programmatic dependents (launch_pdl).
 __global__ void __launch_bounds__(128) k_btf_pred(BtArgs a, int so, int sn, int reuse) {
+  pdl_wait();
+  pdl_trigger();
   btfast::pred_body(a, so, sn, reuse, blockIdx.x, blockIdx.y);
 }
 __global__ void __launch_bounds__(128) k_btf_mom(BtArgs a, int so, int sn, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   btfast::mom_body(a, so, sn, wgt, blockIdx.x, blockIdx.y);
 }
 __global__ void __launch_bounds__(128) k_btf_corr(BtArgs a, int so, int sn) {
+  pdl_wait();
+  pdl_trigger();
   btfast::corr_body(a, so, sn, blockIdx.x, blockIdx.y);
 }
 __global__ void __launch_bounds__(128) k_btf_corr_pred(BtArgs a, int so, int sn) {
+  pdl_wait();
+  pdl_trigger();
   btfast::corr_pred_body(a, so, sn, blockIdx.x, blockIdx.y);
 }
 
@@ -103,6 +112,8 @@ void launch_btf_prep(const BtArgs& a, cudaStream_t s) {
 // than 32 x 8.
 constexpr int kBtfTX = 32, kBtfTY = 8, kBtfThreads = 352;
 __global__ void __launch_bounds__(kBtfThreads) k_btf_fused(BtArgs a, int so, int sn, int reuse, double wgt) {
+  pdl_wait();
+  pdl_trigger();
   btfast::fused_body<kBtfTX, kBtfTY>(a, so, sn, reuse, wgt, blockIdx.x, blockIdx.y);
 }
 
@@ -115,14 +126,14 @@ int launch_btf_subcycle(const BtArgs& a, int itime, int nts, bool fused, cudaStr
   const double wgt = (double)(nts - itime + 1);
   if (fused) {
     dim3 gf((a.g.ni + 2 + kBtfTX - 1) / kBtfTX, (a.g.nj + 2 + kBtfTY - 1) / kBtfTY);
-    k_btf_fused<<<gf, kBtfThreads, 0, s>>>(a, so, sn, itime > 1, wgt);
+    launch_pdl(k_btf_fused, gf, dim3(kBtfThreads), s, a, so, sn, (int)(itime > 1), wgt);
     return 1;
   }
   dim3 g2((a.g.ni + 2 + 127) / 128, a.g.nj + 2);
-  if (itime == 1) k_btf_pred<<<g2, 128, 0, s>>>(a, so, sn, 0);
-  k_btf_mom<<<g2, 128, 0, s>>>(a, so, sn, wgt);
-  if (itime < nts) k_btf_corr_pred<<<g2, 128, 0, s>>>(a, so, sn);
-  else k_btf_corr<<<g2, 128, 0, s>>>(a, so, sn);
+  if (itime == 1) launch_pdl(k_btf_pred, g2, dim3(128), s, a, so, sn, 0);
+  launch_pdl(k_btf_mom, g2, dim3(128), s, a, so, sn, wgt);
+  if (itime < nts) launch_pdl(k_btf_corr_pred, g2, dim3(128), s, a, so, sn);
+  else launch_pdl(k_btf_corr, g2, dim3(128), s, a, so, sn);
   return itime == 1 ? 3 : 2;
 }
 
