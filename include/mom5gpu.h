@@ -156,6 +156,25 @@ enum mom5gpu_field {
   MOM5GPU_MASS_U,        /* 2D (t), Thickness%mass_u */
   MOM5GPU_MASS_EN_E,     /* 2D, Thickness%mass_en(:,:,1) */
   MOM5GPU_MASS_EN_N,     /* 2D, Thickness%mass_en(:,:,2) */
+  /* barotropic friction of ocean_barotropic_forcing (udrho_lap / udrho_bih) */
+  MOM5GPU_DYUE = 150,    /* 2D, Grd%dyue */
+  MOM5GPU_DXUER,         /* 2D, Grd%dxuer */
+  MOM5GPU_DXUN,          /* 2D, Grd%dxun */
+  MOM5GPU_DYUNR,         /* 2D, Grd%dyunr */
+  MOM5GPU_LAP_VISC_CEU,  /* 2D, lap_visc_ceu of ocean_lap_friction (zero unless set) */
+  MOM5GPU_LAP_VISC_CNU,  /* 2D, lap_visc_cnu */
+  MOM5GPU_BIH_VISC_CEU,  /* 2D, bih_visc_ceu of ocean_bih_friction (zero unless set) */
+  MOM5GPU_BIH_VISC_CNU,  /* 2D, bih_visc_cnu */
+  MOM5GPU_LAP_CEU_BACK,  /* 2D, background viscosities of ocean_barotropic_init */
+  MOM5GPU_LAP_CNU_BACK,  /*     (ocean_barotropic.F90:1306-1341), formed from DXU, */
+  MOM5GPU_BIH_CEU_BACK,  /*     DYU, UMASK1 and the udrho_*_vel_micom options by */
+  MOM5GPU_BIH_CNU_BACK,  /*     mom5gpu_ocean_barotropic_forcing_tau */
+  MOM5GPU_LAP_FRICTION_BT_U, /* 2D, Velocity%lap_friction_bt(:,:,1) */
+  MOM5GPU_LAP_FRICTION_BT_V, /* 2D, Velocity%lap_friction_bt(:,:,2) */
+  MOM5GPU_BIH_FRICTION_BT_U, /* 2D, Velocity%bih_friction_bt(:,:,1) */
+  MOM5GPU_BIH_FRICTION_BT_V, /* 2D, Velocity%bih_friction_bt(:,:,2) */
+  MOM5GPU_BIH_DEL2_VEL_U,    /* 2D, del2_vel(:,:,1) of ocean_bih_friction */
+  MOM5GPU_BIH_DEL2_VEL_V,    /* 2D, del2_vel(:,:,2) */
   MOM5GPU_FIELD_END
 };
 
@@ -188,6 +207,13 @@ typedef struct mom5gpu_options {
   int zero_nonlinear_forcing_bt;  /* default 0 */
   /* ocean_tracer_advect_nml psom_limit_prather, ocean_tracer_advect.F90:489 */
   int psom_limit_prather;         /* default 0: Merryfield-Holloway limiter */
+  /* ocean_barotropic_nml, ocean_barotropic.F90:599-604: Laplacian / biharmonic
+   * friction on udrho(tau) added to forcing_bt once per baroclinic step
+   * (mom5gpu_ocean_barotropic_forcing_tau) */
+  int udrho_lap;                  /* default 0 */
+  int udrho_bih;                  /* default 0 */
+  double udrho_lap_vel_micom;     /* default 0.05 m/s */
+  double udrho_bih_vel_micom;     /* default 0.01 m/s */
 } mom5gpu_options;
 
 typedef struct mom5gpu_domain mom5gpu_domain;
@@ -383,6 +409,19 @@ int mom5gpu_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vert_coordi
  * tmasken(k=1)*(smf - bmf) on the compute domain, zero halo then the single-PE
  * halo update; honours zero_forcing_bt and zero_nonlinear_forcing_bt. */
 int mom5gpu_ocean_barotropic_forcing(mom5gpu_domain* d);
+/* ocean_barotropic_forcing with Time%tau = tau: as mom5gpu_ocean_barotropic_forcing,
+ * plus the barotropic friction on UDRHO_U/V(tau) (:3105-3120).  With udrho_lap:
+ * lap_friction_barotropic (ocean_lap_friction.F90:423-446), BDX_EU(c_e*FDX_U(u))
+ * + BDY_NU(c_n*FDY_U(u)) times umask with c = *_BACK + *_VISC
+ * (ocean_operators.F90:917-930, :973-986, :1202-1215, :1258-1271); with udrho_bih:
+ * bih_friction_barotropic (ocean_bih_friction.F90:416-454), the operator applied
+ * twice and negated.  Each result has a zero halo and then the single-PE halo
+ * update; it is written to LAP/BIH_FRICTION_BT_U/V (zero when its switch is off)
+ * and forcing_bt = forcing_bt + friction_lap + friction_bih on the data domain,
+ * before zero_forcing_bt.  The *_BACK viscosities are formed first, as
+ * ocean_barotropic_init forms them.  mom5gpu_ocean_barotropic_forcing returns
+ * MOM5GPU_EINVAL when either switch is set. */
+int mom5gpu_ocean_barotropic_forcing_tau(mom5gpu_domain* d, int tau);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Global content of tracer n at a time level, sum of tmask*dat*rho_dzt(level)*T

@@ -67,7 +67,9 @@ class Options(C.Structure):
                 ("barotropic_time_stepping_A", C.c_int), ("barotropic_time_stepping_B", C.c_int),
                 ("initsum_with_bar", C.c_int), ("pred_corr_gamma", C.c_double), ("rho0", C.c_double),
                 ("grav", C.c_double), ("precision", C.c_int), ("zero_forcing_bt", C.c_int),
-                ("zero_nonlinear_forcing_bt", C.c_int), ("psom_limit_prather", C.c_int)]
+                ("zero_nonlinear_forcing_bt", C.c_int), ("psom_limit_prather", C.c_int),
+                ("udrho_lap", C.c_int), ("udrho_bih", C.c_int), ("udrho_lap_vel_micom", C.c_double),
+                ("udrho_bih_vel_micom", C.c_double)]
 
 
 class Box(C.Structure):
@@ -133,6 +135,7 @@ def lib() -> C.CDLL:
             "mom5gpu_write_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
             "mom5gpu_read_restart": (C.c_int, [vp, C.c_char_p, C.c_int]),
             "mom5gpu_ocean_barotropic_forcing": (C.c_int, [vp]),
+            "mom5gpu_ocean_barotropic_forcing_tau": (C.c_int, [vp, C.c_int]),
             "mom5gpu_update_ucell_thickness": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
             "mom5gpu_global_tracer_content": (C.c_int, [vp, C.c_int, C.c_int, dp]),
             "mom5gpu_tracer_content_fixed": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_longlong)]),
@@ -400,8 +403,13 @@ class Domain:
     def tracer_boundary_terms(self, n=0):
         self.check(lib().mom5gpu_tracer_boundary_terms(self.h, n))
 
-    def ocean_barotropic_forcing(self):
-        self.check(lib().mom5gpu_ocean_barotropic_forcing(self.h))
+    def ocean_barotropic_forcing(self, tau=None):
+        """ocean_barotropic_forcing; with tau (Time%tau), the barotropic friction on
+        udrho(tau) too (options udrho_lap / udrho_bih)."""
+        if tau is None:
+            self.check(lib().mom5gpu_ocean_barotropic_forcing(self.h))
+        else:
+            self.check(lib().mom5gpu_ocean_barotropic_forcing_tau(self.h, tau))
 
     def update_ucell_thickness(self, taup1, vert_coordinate=GEOPOTENTIAL, linear_free_surface=False,
                                update_dzwu_k0=True):

@@ -8,7 +8,9 @@ per-tracer setters of the C ABI.
                                   "psom_limit_prather": false},
       "ocean_barotropic_nml": {"barotropic_time_stepping_A": false, "barotropic_time_stepping_B": true,
                                "pred_corr_gamma": 0.2, "initsum_with_bar": true,
-                               "zero_forcing_bt": false, "zero_nonlinear_forcing_bt": false},
+                               "zero_forcing_bt": false, "zero_nonlinear_forcing_bt": false,
+                               "udrho_lap": false, "udrho_bih": false, "udrho_lap_vel_micom": 0.05,
+                               "udrho_bih_vel_micom": 0.01},
       "ocean_parameters": {"rho0": 1035.0, "grav": 9.8},
       "library": {"precision": "fp64"},
       "tracers": [{"name": "temp", "horiz_advect_scheme": "mdfl_sweby", "vert_advect_scheme": "mdfl_sweby",
@@ -39,7 +41,8 @@ _NML_KEYS = {
     "ocean_tracer_advect_nml": {"advect_sweby_all", "limit_with_upwind", "zero_tracer_advect_horz",
                                 "zero_tracer_advect_vert", "psom_limit_prather"},
     "ocean_barotropic_nml": {"barotropic_time_stepping_A", "barotropic_time_stepping_B", "pred_corr_gamma",
-                             "initsum_with_bar", "zero_forcing_bt", "zero_nonlinear_forcing_bt"},
+                             "initsum_with_bar", "zero_forcing_bt", "zero_nonlinear_forcing_bt", "udrho_lap",
+                             "udrho_bih", "udrho_lap_vel_micom", "udrho_bih_vel_micom"},
     "ocean_parameters": {"rho0", "grav"},
     "library": {"precision"},
 }

@@ -70,6 +70,15 @@ const FieldInfo kFields[] = {
     {MOM5GPU_DEPTH_ZU, S3D, false, false},    {MOM5GPU_DEPTH_ZWU, S3D, false, false},
     {MOM5GPU_MASS_U, S2D, false, true},       {MOM5GPU_MASS_EN_E, S2D, false, false},
     {MOM5GPU_MASS_EN_N, S2D, false, false},
+    {MOM5GPU_DYUE, S2D, false, false},        {MOM5GPU_DXUER, S2D, false, false},
+    {MOM5GPU_DXUN, S2D, false, false},        {MOM5GPU_DYUNR, S2D, false, false},
+    {MOM5GPU_LAP_VISC_CEU, S2D, false, false}, {MOM5GPU_LAP_VISC_CNU, S2D, false, false},
+    {MOM5GPU_BIH_VISC_CEU, S2D, false, false}, {MOM5GPU_BIH_VISC_CNU, S2D, false, false},
+    {MOM5GPU_LAP_CEU_BACK, S2D, false, false}, {MOM5GPU_LAP_CNU_BACK, S2D, false, false},
+    {MOM5GPU_BIH_CEU_BACK, S2D, false, false}, {MOM5GPU_BIH_CNU_BACK, S2D, false, false},
+    {MOM5GPU_LAP_FRICTION_BT_U, S2D, false, false}, {MOM5GPU_LAP_FRICTION_BT_V, S2D, false, false},
+    {MOM5GPU_BIH_FRICTION_BT_U, S2D, false, false}, {MOM5GPU_BIH_FRICTION_BT_V, S2D, false, false},
+    {MOM5GPU_BIH_DEL2_VEL_U, S2D, false, false}, {MOM5GPU_BIH_DEL2_VEL_V, S2D, false, false},
 };
 
 // field storage: one block per (field, level) holding every tracer of that level
@@ -236,6 +245,10 @@ void mom5gpu_default_options(mom5gpu_options* o) {
   o->zero_forcing_bt = 0;
   o->zero_nonlinear_forcing_bt = 0;
   o->psom_limit_prather = 0;
+  o->udrho_lap = 0;
+  o->udrho_bih = 0;
+  o->udrho_lap_vel_micom = 0.05;
+  o->udrho_bih_vel_micom = 0.01;
 }
 
 const char* mom5gpu_strerror(int s) {
@@ -1041,7 +1054,17 @@ int mom5gpu_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vert_coordi
 
 int mom5gpu_ocean_barotropic_forcing(mom5gpu_domain* d) {
   if (!d) return MOM5GPU_EINVAL;
-  return launch_barotropic_forcing(d);
+  if (d->opt.udrho_lap || d->opt.udrho_bih)
+    return fail(d, MOM5GPU_EINVAL,
+                "ocean_barotropic_forcing: udrho_lap/udrho_bih act on udrho(tau): use "
+                "mom5gpu_ocean_barotropic_forcing_tau");
+  return launch_barotropic_forcing(d, 0);
+}
+
+int mom5gpu_ocean_barotropic_forcing_tau(mom5gpu_domain* d, int tau) {
+  if (!d) return MOM5GPU_EINVAL;
+  if (tau < 1 || tau > 3) return fail(d, MOM5GPU_EINVAL, "ocean_barotropic_forcing: tau %d (1..3)", tau);
+  return launch_barotropic_forcing(d, tau);
 }
 
 int mom5gpu_update_ocean_barotropic(mom5gpu_domain* d, int tau, int taup1) {

@@ -294,7 +294,7 @@ int launch_mdppm(mom5gpu_domain* d, int n, int taum1, int tau, double dtime);
 int launch_psom(mom5gpu_domain* d, int n, int taum1, double dtime);
 int launch_quickmom3_horz(mom5gpu_domain* d, int n, int taum1, int tau);
 int launch_tracer_boundary(mom5gpu_domain* d, int n);
-int launch_barotropic_forcing(mom5gpu_domain* d);
+int launch_barotropic_forcing(mom5gpu_domain* d, int tau);  // tau 0: no friction
 int launch_update_ucell_thickness(mom5gpu_domain* d, int taup1, int vcoord, bool linear_fs, bool dzwu_k0);
 int launch_advection_velocity(mom5gpu_domain* d, int tau);
 int launch_barotropic(mom5gpu_domain* d, int tau, int taup1);

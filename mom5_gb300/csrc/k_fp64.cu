@@ -1849,7 +1849,7 @@ int launch_tracer_boundary(mom5gpu_domain* d, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141), no barotropic friction
+// ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141)
 // ---------------------------------------------------------------------------
 __global__ void k_baro_forcing(Geo g, const double* tmen, const double* accel, const double* smf, const double* bmf,
                                int nonlinear, double* f) {
@@ -1872,12 +1872,191 @@ __global__ void k_plus_zero_2d(long n2, double* f) {
   if (q < n2) f[q] = plus_zero(plus_zero(f[q]));
 }
 
-int launch_barotropic_forcing(mom5gpu_domain* d) {
+// forcing_bt + friction_lap + friction_bih on the data domain (:3114-3120); a
+// null friction is the reference's 0.0
+__global__ void k_plus_friction_2d(long n2, double* f, const double* lap, const double* bih) {
+  long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (q >= n2) return;
+  double v = f[q] + (lap ? lap[q] : 0.0);
+  f[q] = v + (bih ? bih[q] : 0.0);
+}
+
+// Background viscosities of the barotropic friction (ocean_barotropic.F90:1306-1335):
+// smooth_lap_udrho = umask*vel_lap*(2*dxu*dyu/(dxu+dyu)) and smooth_bih_udrho =
+// umask*vel_bih*(...)**3 (x**3 as (x*x)*x), averaged onto the east and north
+// faces on the compute domain; zero on the halo, which the caller then updates.
+struct FricBack {
+  const double *dxu, *dyu, *umask;
+  double vel_lap, vel_bih;
+  double *lap_e, *lap_n, *bih_e, *bih_n;
+};
+DEVI void smooth_udrho(const FricBack& a, long q, double& sl, double& sb) {
+  double x = 2.0 * a.dxu[q] * a.dyu[q] / (a.dxu[q] + a.dyu[q]);
+  double um = a.umask[q];
+  sl = um * a.vel_lap * x;
+  sb = um * a.vel_bih * (x * x * x);
+}
+__global__ void k_bt_fric_back(Geo g, FricBack a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double le = 0.0, ln = 0.0, be = 0.0, bn = 0.0;
+  if (i >= 1 && i <= g.ni && j >= 1 && j <= g.nj) {
+    double sl, sb, sle, sbe, sln, sbn;
+    smooth_udrho(a, q, sl, sb);
+    smooth_udrho(a, I2(g, i + 1, j), sle, sbe);
+    smooth_udrho(a, I2(g, i, j + 1), sln, sbn);
+    le = 0.5 * (sl + sle);
+    ln = 0.5 * (sl + sln);
+    be = 0.5 * (sb + sbe);
+    bn = 0.5 * (sb + sbn);
+  }
+  a.lap_e[q] = le;
+  a.lap_n[q] = ln;
+  a.bih_e[q] = be;
+  a.bih_n[q] = bn;
+}
+// bih_ceu_back = sqrt(bih_ceu_back) over the data domain after its halo update (:1340-1341)
+__global__ void k_sqrt_2d(long n2, double* a, double* b) {
+  long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (q >= n2) return;
+  a[q] = sqrt(a[q]);
+  b[q] = sqrt(b[q]);
+}
+
+// One application of the barotropic friction operator on the compute domain
+// (lap_friction_barotropic, ocean_lap_friction.F90:433-440; each iteration of
+// bih_friction_barotropic, ocean_bih_friction.F90:428-448):
+//   tmp = BDX_EU((ce_back + ce_visc)*FDX_U(a)) + BDY_NU((cn_back + cn_visc)*FDY_U(a))
+// with FDX_U(a)(i) = (a(i+1)-a(i))*dxuer(i), BDX_EU(X)(i) = (dyue(i)*X(i) -
+// dyue(i-1)*X(i-1))*daur(i), FDY_U, BDY_NU likewise with dyunr and dxun
+// (ocean_operators.F90:917-930, :973-986, :1202-1215, :1258-1271); out = tmp*umask,
+// or (-tmp)*umask for the second biharmonic iteration.  Zero on the halo, which
+// the caller then updates (the reference's arrays start at 0.0 and only their
+// compute domain is written).
+struct FricOp {
+  const double *dyue, *dxuer, *dxun, *dyunr, *daur, *umask;
+  const double *ce_back, *ce_visc, *cn_back, *cn_visc;
+};
+__global__ void k_bt_fric_op(Geo g, FricOp m, const double* a, int negate, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i > g.ni + 1) return;
+  long q = I2(g, i, j);
+  double v = 0.0;
+  if (i >= 1 && i <= g.ni && j >= 1 && j <= g.nj) {
+    const long qw = I2(g, i - 1, j), qe = I2(g, i + 1, j), qs = I2(g, i, j - 1), qn = I2(g, i, j + 1);
+    double fx = (a[qe] - a[q]) * m.dxuer[q];
+    double fxw = (a[q] - a[qw]) * m.dxuer[qw];
+    double xe = (m.ce_back[q] + m.ce_visc[q]) * fx;
+    double xw = (m.ce_back[qw] + m.ce_visc[qw]) * fxw;
+    double bdx = (m.dyue[q] * xe - m.dyue[qw] * xw) * m.daur[q];
+    double fy = (a[qn] - a[q]) * m.dyunr[q];
+    double fys = (a[q] - a[qs]) * m.dyunr[qs];
+    double yn = (m.cn_back[q] + m.cn_visc[q]) * fy;
+    double ys = (m.cn_back[qs] + m.cn_visc[qs]) * fys;
+    double bdy = (m.dxun[q] * yn - m.dxun[qs] * ys) * m.daur[q];
+    double tmp = bdx + bdy;
+    v = (negate ? -tmp : tmp) * m.umask[q];
+  }
+  out[q] = v;
+}
+
+// The barotropic friction of one velocity component a = udrho(:,:,n,tau) into
+// lap (udrho_lap) and bih (udrho_bih; del2 is ocean_bih_friction's del2_vel),
+// each with its halo update; a friction that is off is zeroed.
+static void launch_bt_friction(const mom5gpu_domain* d, const FricOp& lap_op, const FricOp& bih_op, const double* a,
+                               double* lap, double* bih, double* del2, cudaStream_t s) {
+  const Geo& g = d->geo;
+  dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
+  if (d->opt.udrho_lap) {
+    k_bt_fric_op<<<g2, 128, 0, s>>>(g, lap_op, a, 0, lap);
+    launch_halo_fill(g, lap, 1, 3, s);
+  } else {
+    cudaMemsetAsync(lap, 0, sizeof(double) * g.n2, s);
+  }
+  if (d->opt.udrho_bih) {
+    k_bt_fric_op<<<g2, 128, 0, s>>>(g, bih_op, a, 0, del2);
+    launch_halo_fill(g, del2, 1, 3, s);
+    k_bt_fric_op<<<g2, 128, 0, s>>>(g, bih_op, del2, 1, bih);
+    launch_halo_fill(g, bih, 1, 3, s);
+  } else {
+    cudaMemsetAsync(bih, 0, sizeof(double) * g.n2, s);
+  }
+}
+
+int launch_barotropic_forcing(mom5gpu_domain* d, int tau) {
   const Geo& g = d->geo;
   double* fu = fptr(d, MOM5GPU_FORCING_BT_U, 0, 0);
   double* fv = fptr(d, MOM5GPU_FORCING_BT_V, 0, 0);
   if (!fu || !fv) return fail(d, MOM5GPU_ESTATE, "ocean_barotropic_forcing: a field could not be allocated");
   cudaStream_t s = d->stream;
+  const bool friction = tau > 0;
+  const bool halo = g.cx || g.cy;
+  dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
+  unsigned nb = (unsigned)((g.n2 + 255) / 256);
+  double *lap_u = nullptr, *lap_v = nullptr, *bih_u = nullptr, *bih_v = nullptr;
+  if (friction) {
+    // the background viscosities (ocean_barotropic_init), then the friction of
+    // udrho(tau) (:3105-3113); the inputs of a switch that is on must be set
+    FricBack fb;
+    fb.dxu = fptr_if_set(d, MOM5GPU_DXU, 0, 0);
+    fb.dyu = fptr_if_set(d, MOM5GPU_DYU, 0, 0);
+    fb.umask = fptr_if_set(d, MOM5GPU_UMASK1, 0, 0);
+    fb.vel_lap = d->opt.udrho_lap_vel_micom;
+    fb.vel_bih = d->opt.udrho_bih_vel_micom;
+    fb.lap_e = fptr(d, MOM5GPU_LAP_CEU_BACK, 0, 0);
+    fb.lap_n = fptr(d, MOM5GPU_LAP_CNU_BACK, 0, 0);
+    fb.bih_e = fptr(d, MOM5GPU_BIH_CEU_BACK, 0, 0);
+    fb.bih_n = fptr(d, MOM5GPU_BIH_CNU_BACK, 0, 0);
+    FricOp lo;
+    lo.dyue = fptr_if_set(d, MOM5GPU_DYUE, 0, 0);
+    lo.dxuer = fptr_if_set(d, MOM5GPU_DXUER, 0, 0);
+    lo.dxun = fptr_if_set(d, MOM5GPU_DXUN, 0, 0);
+    lo.dyunr = fptr_if_set(d, MOM5GPU_DYUNR, 0, 0);
+    lo.daur = fptr_if_set(d, MOM5GPU_DAUR, 0, 0);
+    lo.umask = fb.umask;
+    FricOp bo = lo;
+    lo.ce_back = fb.lap_e;
+    lo.cn_back = fb.lap_n;
+    lo.ce_visc = fptr(d, MOM5GPU_LAP_VISC_CEU, 0, 0);
+    lo.cn_visc = fptr(d, MOM5GPU_LAP_VISC_CNU, 0, 0);
+    bo.ce_back = fb.bih_e;
+    bo.cn_back = fb.bih_n;
+    bo.ce_visc = fptr(d, MOM5GPU_BIH_VISC_CEU, 0, 0);
+    bo.cn_visc = fptr(d, MOM5GPU_BIH_VISC_CNU, 0, 0);
+    const double* uu = fptr_if_set(d, MOM5GPU_UDRHO_U, 0, tau);
+    const double* uv = fptr_if_set(d, MOM5GPU_UDRHO_V, 0, tau);
+    lap_u = fptr(d, MOM5GPU_LAP_FRICTION_BT_U, 0, 0);
+    lap_v = fptr(d, MOM5GPU_LAP_FRICTION_BT_V, 0, 0);
+    bih_u = fptr(d, MOM5GPU_BIH_FRICTION_BT_U, 0, 0);
+    bih_v = fptr(d, MOM5GPU_BIH_FRICTION_BT_V, 0, 0);
+    double* del2_u = fptr(d, MOM5GPU_BIH_DEL2_VEL_U, 0, 0);
+    double* del2_v = fptr(d, MOM5GPU_BIH_DEL2_VEL_V, 0, 0);
+    const bool on = d->opt.udrho_lap || d->opt.udrho_bih;
+    if (!fb.lap_e || !fb.lap_n || !fb.bih_e || !fb.bih_n || !lo.ce_visc || !lo.cn_visc || !bo.ce_visc ||
+        !bo.cn_visc || !lap_u || !lap_v || !bih_u || !bih_v || !del2_u || !del2_v)
+      return fail(d, MOM5GPU_ESTATE, "ocean_barotropic_forcing: a field could not be allocated");
+    if (on && (!fb.dxu || !fb.dyu || !fb.umask || !lo.dyue || !lo.dxuer || !lo.dxun || !lo.dyunr || !lo.daur ||
+               !uu || !uv))
+      return fail(d, MOM5GPU_ESTATE,
+                  "ocean_barotropic_forcing: barotropic friction needs DXU, DYU, UMASK1, DYUE, DXUER, DXUN, DYUNR, "
+                  "DAUR and UDRHO_U/V(tau)");
+    if (on) {
+      k_bt_fric_back<<<g2, 128, 0, s>>>(g, fb);
+      launch_halo_fill(g, fb.lap_e, 1, 3, s);
+      launch_halo_fill(g, fb.lap_n, 1, 3, s);
+      launch_halo_fill(g, fb.bih_e, 1, 3, s);
+      launch_halo_fill(g, fb.bih_n, 1, 3, s);
+      k_sqrt_2d<<<nb, 256, 0, s>>>(g.n2, fb.bih_e, fb.bih_n);
+      launch_bt_friction(d, lo, bo, uu, lap_u, bih_u, del2_u, s);
+      launch_bt_friction(d, lo, bo, uv, lap_v, bih_v, del2_v, s);
+    } else {
+      for (double* z : {lap_u, lap_v, bih_u, bih_v}) cudaMemsetAsync(z, 0, sizeof(double) * g.n2, s);
+      lap_u = lap_v = bih_u = bih_v = nullptr;
+    }
+    const int per = (d->opt.udrho_lap ? 1 + (halo ? 1 : 0) : 0) + (d->opt.udrho_bih ? 2 + (halo ? 2 : 0) : 0);
+    count_launches(d, on ? 2 + (halo ? 4 : 0) + 2 * per : 0);
+  }
   if (d->opt.zero_forcing_bt) {  // (:3126-3134)
     count_launches(d, 0);
     cudaMemsetAsync(fu, 0, sizeof(double) * g.n2, s);
@@ -1894,15 +2073,18 @@ int launch_barotropic_forcing(mom5gpu_domain* d) {
     if (!te || !tn || !au || !av || !su || !sv || !bu || !bv)
       return fail(d, MOM5GPU_ESTATE, "ocean_barotropic_forcing: a field could not be allocated");
     int nl = d->opt.zero_nonlinear_forcing_bt ? 0 : 1;
-    dim3 g2((g.ni + 2 + 127) / 128, g.nj + 2);
     count_launches(d, 4 + ((g.cx || g.cy) ? 2 : 0));
     k_baro_forcing<<<g2, 128, 0, s>>>(g, te, au, su, bu, nl, fu);
     k_baro_forcing<<<g2, 128, 0, s>>>(g, tn, av, sv, bv, nl, fv);
     launch_halo_fill(g, fu, 1, 3, s);
     launch_halo_fill(g, fv, 1, 3, s);
-    unsigned nb = (unsigned)((g.n2 + 255) / 256);
-    k_plus_zero_2d<<<nb, 256, 0, s>>>(g.n2, fu);
-    k_plus_zero_2d<<<nb, 256, 0, s>>>(g.n2, fv);
+    if (lap_u || bih_u) {
+      k_plus_friction_2d<<<nb, 256, 0, s>>>(g.n2, fu, lap_u, bih_u);
+      k_plus_friction_2d<<<nb, 256, 0, s>>>(g.n2, fv, lap_v, bih_v);
+    } else {
+      k_plus_zero_2d<<<nb, 256, 0, s>>>(g.n2, fu);
+      k_plus_zero_2d<<<nb, 256, 0, s>>>(g.n2, fv);
+    }
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MOM5GPU_OK : cuda_fail(d, e, "ocean_barotropic_forcing");

@@ -46,7 +46,11 @@ module mom5gpu_c
        F_PSOM_SZ = 125, F_PSOM_SZZ = 126, F_PSOM_SXY = 127, F_PSOM_SXZ = 128, F_PSOM_SYZ = 129, &
        F_UMASK = 130, F_DZT = 131, F_DZWT = 132, F_DZU = 133, F_DZWU = 134, F_RHO_DZUR = 135, &
        F_DZTEN_E = 136, F_DZTEN_N = 137, F_DEPTH_ZT = 138, F_DEPTH_ZWT = 139, F_DEPTH_ZU = 140, &
-       F_DEPTH_ZWU = 141, F_MASS_U = 142, F_MASS_EN_E = 143, F_MASS_EN_N = 144
+       F_DEPTH_ZWU = 141, F_MASS_U = 142, F_MASS_EN_E = 143, F_MASS_EN_N = 144, &
+       F_DYUE = 150, F_DXUER = 151, F_DXUN = 152, F_DYUNR = 153, F_LAP_VISC_CEU = 154, F_LAP_VISC_CNU = 155, &
+       F_BIH_VISC_CEU = 156, F_BIH_VISC_CNU = 157, F_LAP_CEU_BACK = 158, F_LAP_CNU_BACK = 159, &
+       F_BIH_CEU_BACK = 160, F_BIH_CNU_BACK = 161, F_LAP_FRICTION_BT_U = 162, F_LAP_FRICTION_BT_V = 163, &
+       F_BIH_FRICTION_BT_U = 164, F_BIH_FRICTION_BT_V = 165, F_BIH_DEL2_VEL_U = 166, F_BIH_DEL2_VEL_V = 167
   integer(c_int), parameter :: MOM5GPU_ADVECT_PSOM = 11
   integer, parameter :: MOM5GPU_FIXED_CHUNKS = 8
 
@@ -61,6 +65,8 @@ module mom5gpu_c
      integer(c_int) :: precision
      integer(c_int) :: zero_forcing_bt, zero_nonlinear_forcing_bt
      integer(c_int) :: psom_limit_prather
+     integer(c_int) :: udrho_lap, udrho_bih
+     real(c_double) :: udrho_lap_vel_micom, udrho_bih_vel_micom
   end type mom5gpu_options
 
   interface
@@ -215,6 +221,12 @@ module mom5gpu_c
      integer(c_int) function mom5gpu_ocean_barotropic_forcing(dom) bind(C, name="mom5gpu_ocean_barotropic_forcing")
        import :: c_int, c_ptr
        type(c_ptr), value :: dom
+     end function
+     integer(c_int) function mom5gpu_ocean_barotropic_forcing_tau(dom, tau) &
+          bind(C, name="mom5gpu_ocean_barotropic_forcing_tau")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: dom
+       integer(c_int), value :: tau
      end function
      integer(c_int) function mom5gpu_update_ucell_thickness(dom, taup1, vert_coordinate, linear_free_surface, &
           update_dzwu_k0) bind(C, name="mom5gpu_update_ucell_thickness")
@@ -484,9 +496,16 @@ contains
     call check(mom5gpu_set_field(dom, F_SMF_V, 0, 0, Velocity%smf(:,:,2), 0), 'smf')
     call check(mom5gpu_set_field(dom, F_BMF_U, 0, 0, Velocity%bmf(:,:,1), 0), 'bmf')
     call check(mom5gpu_set_field(dom, F_BMF_V, 0, 0, Velocity%bmf(:,:,2), 0), 'bmf')
-    call check(mom5gpu_ocean_barotropic_forcing(dom), 'ocean_barotropic_forcing')
+    ! with udrho_lap / udrho_bih the friction acts on udrho(tau), which is on the
+    ! device; lap_visc_* / bih_visc_* are set by the host after its friction modules
+    ! form them (F_LAP_VISC_CEU ... F_BIH_VISC_CNU)
+    call check(mom5gpu_ocean_barotropic_forcing_tau(dom, Time%tau), 'ocean_barotropic_forcing')
     call check(mom5gpu_get_field(dom, F_FORCING_BT_U, 0, 0, Ext_mode%forcing_bt(:,:,1), 0), 'forcing_bt')
     call check(mom5gpu_get_field(dom, F_FORCING_BT_V, 0, 0, Ext_mode%forcing_bt(:,:,2), 0), 'forcing_bt')
+    call check(mom5gpu_get_field(dom, F_LAP_FRICTION_BT_U, 0, 0, Velocity%lap_friction_bt(:,:,1), 0), 'lap_friction_bt')
+    call check(mom5gpu_get_field(dom, F_LAP_FRICTION_BT_V, 0, 0, Velocity%lap_friction_bt(:,:,2), 0), 'lap_friction_bt')
+    call check(mom5gpu_get_field(dom, F_BIH_FRICTION_BT_U, 0, 0, Velocity%bih_friction_bt(:,:,1), 0), 'bih_friction_bt')
+    call check(mom5gpu_get_field(dom, F_BIH_FRICTION_BT_V, 0, 0, Velocity%bih_friction_bt(:,:,2), 0), 'bih_friction_bt')
   end subroutine ocean_barotropic_forcing
 
   subroutine device_thickness_options(vert_coordinate, linear_free_surface, update_dzwu_k0)

@@ -2275,10 +2275,14 @@ void orc_tracer_boundary_terms(const orc_dims* d, const double* tmask, const int
     }
 }
 
-/* ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141) with udrho_lap =
- * udrho_bih = .false. (their default): one component; tmasken and accel are 3-D. */
-void orc_ocean_barotropic_forcing(const orc_dims* d, int zero_nonlinear, int zero_forcing, const double* tmasken,
-                                  const double* accel, const double* smf, const double* bmf, double* forcing) {
+/* ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141), one component;
+ * tmasken and accel are 3-D.  friction_lap and friction_bih (data domain) are the
+ * component's barotropic frictions, or NULL for the reference's 0.0 (udrho_lap =
+ * udrho_bih = .false., their default). */
+void orc_ocean_barotropic_forcing_friction(const orc_dims* d, int zero_nonlinear, int zero_forcing,
+                                           const double* tmasken, const double* accel, const double* smf,
+                                           const double* bmf, const double* friction_lap,
+                                           const double* friction_bih, double* forcing) {
   size_t n2 = (size_t)NXD(d) * NYD(d);
   double* wrk = (double*)calloc(n2, sizeof(double));
   for (size_t q = 0; q < n2; ++q) forcing[q] = 0.0;
@@ -2295,10 +2299,141 @@ void orc_ocean_barotropic_forcing(const orc_dims* d, int zero_nonlinear, int zer
       forcing[q] = wrk[q] + tmasken[q] * (smf[q] - bmf[q]);
     }
   orc_halo_update_2d(d, forcing, 3);
-  for (size_t q = 0; q < n2; ++q) forcing[q] = forcing[q] + 0.0 + 0.0; /* + friction_lap + friction_bih */
+  for (size_t q = 0; q < n2; ++q)
+    forcing[q] = forcing[q] + (friction_lap ? friction_lap[q] : 0.0) + (friction_bih ? friction_bih[q] : 0.0);
   if (zero_forcing)
     for (size_t q = 0; q < n2; ++q) forcing[q] = 0.0;
   free(wrk);
+}
+
+void orc_ocean_barotropic_forcing(const orc_dims* d, int zero_nonlinear, int zero_forcing, const double* tmasken,
+                                  const double* accel, const double* smf, const double* bmf, double* forcing) {
+  orc_ocean_barotropic_forcing_friction(d, zero_nonlinear, zero_forcing, tmasken, accel, smf, bmf, NULL, NULL,
+                                        forcing);
+}
+
+/* Background viscosities of the barotropic friction, as ocean_barotropic_init
+ * forms them (ocean_barotropic.F90:1306-1341): all four start at 0.0;
+ * smooth_lap_udrho = umask*udrho_lap_vel_micom*(2.0*dxu*dyu/(dxu+dyu)) and
+ * smooth_bih_udrho = umask*udrho_bih_vel_micom*(...)**3 over the data domain
+ * (x**3 evaluated as x*x*x, left to right); the east and north face averages
+ * 0.5*(s(i,j)+s(i+1,j)), 0.5*(s(i,j)+s(i,j+1)) on the compute domain; the
+ * halo update of each; then the square root of the two biharmonic ones over
+ * the data domain. */
+void orc_bt_friction_back(const orc_dims* d, const double* dxu, const double* dyu, const double* umask1,
+                          double vel_lap, double vel_bih, double* lap_ceu, double* lap_cnu, double* bih_ceu,
+                          double* bih_cnu) {
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* sl = (double*)malloc(n2 * sizeof(double));
+  double* sb = (double*)malloc(n2 * sizeof(double));
+  for (size_t q = 0; q < n2; ++q) {
+    double x = 2.0 * dxu[q] * dyu[q] / (dxu[q] + dyu[q]);
+    sl[q] = umask1[q] * vel_lap * x;
+    sb[q] = umask1[q] * vel_bih * (x * x * x);
+    lap_ceu[q] = lap_cnu[q] = bih_ceu[q] = bih_cnu[q] = 0.0;
+  }
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) {
+      size_t q = I2(d, i, j), qe = I2(d, i + 1, j), qn = I2(d, i, j + 1);
+      lap_ceu[q] = 0.5 * (sl[q] + sl[qe]);
+      lap_cnu[q] = 0.5 * (sl[q] + sl[qn]);
+      bih_ceu[q] = 0.5 * (sb[q] + sb[qe]);
+      bih_cnu[q] = 0.5 * (sb[q] + sb[qn]);
+    }
+  orc_halo_update_2d(d, lap_ceu, 3);
+  orc_halo_update_2d(d, lap_cnu, 3);
+  orc_halo_update_2d(d, bih_ceu, 3);
+  orc_halo_update_2d(d, bih_cnu, 3);
+  for (size_t q = 0; q < n2; ++q) {
+    bih_ceu[q] = sqrt(bih_ceu[q]);
+    bih_cnu[q] = sqrt(bih_cnu[q]);
+  }
+  free(sl);
+  free(sb);
+}
+
+/* The ocean_operators B-grid operators on the data domain, in the reference's
+ * ranges (halo 1): FDX_U(a)(i,j) = (a(i+1,j)-a(i,j))*dxuer(i,j), 0.0 at ied
+ * (ocean_operators.F90:973-986); FDY_U with dyunr, 0.0 at jed (:1258-1271);
+ * BDX_EU(a)(i,j) = (dyue(i,j)*a(i,j) - dyue(i-1,j)*a(i-1,j))*daur(i,j), 0.0 at
+ * isd (:917-930); BDY_NU with dxun, 0.0 at jsd (:1202-1215). */
+static void op_fdx_u(const orc_dims* d, const double* dxuer, const double* a, double* out) {
+  for (int j = 0; j <= d->nj + 1; ++j) {
+    for (int i = 0; i <= d->ni; ++i) out[I2(d, i, j)] = (a[I2(d, i + 1, j)] - a[I2(d, i, j)]) * dxuer[I2(d, i, j)];
+    out[I2(d, d->ni + 1, j)] = 0.0;
+  }
+}
+static void op_fdy_u(const orc_dims* d, const double* dyunr, const double* a, double* out) {
+  for (int j = 0; j <= d->nj; ++j)
+    for (int i = 0; i <= d->ni + 1; ++i) out[I2(d, i, j)] = (a[I2(d, i, j + 1)] - a[I2(d, i, j)]) * dyunr[I2(d, i, j)];
+  for (int i = 0; i <= d->ni + 1; ++i) out[I2(d, i, d->nj + 1)] = 0.0;
+}
+static void op_bdx_eu(const orc_dims* d, const double* dyue, const double* daur, const double* a, double* out) {
+  for (int j = 0; j <= d->nj + 1; ++j) {
+    for (int i = 1; i <= d->ni + 1; ++i)
+      out[I2(d, i, j)] = (dyue[I2(d, i, j)] * a[I2(d, i, j)] - dyue[I2(d, i - 1, j)] * a[I2(d, i - 1, j)]) *
+                         daur[I2(d, i, j)];
+    out[I2(d, 0, j)] = 0.0;
+  }
+}
+static void op_bdy_nu(const orc_dims* d, const double* dxun, const double* daur, const double* a, double* out) {
+  for (int j = 1; j <= d->nj + 1; ++j)
+    for (int i = 0; i <= d->ni + 1; ++i)
+      out[I2(d, i, j)] = (dxun[I2(d, i, j)] * a[I2(d, i, j)] - dxun[I2(d, i, j - 1)] * a[I2(d, i, j - 1)]) *
+                         daur[I2(d, i, j)];
+  for (int i = 0; i <= d->ni + 1; ++i) out[I2(d, i, 0)] = 0.0;
+}
+
+/* tmp = BDX_EU((ce_back+ce_visc)*FDX_U(a)) + BDY_NU((cn_back+cn_visc)*FDY_U(a)) as
+ * whole-array expressions; out = tmp*umask (negate: -tmp*umask) on the compute
+ * domain of an array that was 0.0, then its halo update
+ * (ocean_lap_friction.F90:433-443; ocean_bih_friction.F90:428-451). */
+static void bt_friction_op(const orc_dims* d, const double* const* m, const double* ce_back, const double* ce_visc,
+                           const double* cn_back, const double* cn_visc, const double* a, int negate, double* out) {
+  const double *dyue = m[0], *dxuer = m[1], *dxun = m[2], *dyunr = m[3], *daur = m[4], *umask1 = m[5];
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  double* fx = (double*)malloc(n2 * sizeof(double));
+  double* fy = (double*)malloc(n2 * sizeof(double));
+  double* bx = (double*)malloc(n2 * sizeof(double));
+  double* by = (double*)malloc(n2 * sizeof(double));
+  op_fdx_u(d, dxuer, a, fx);
+  op_fdy_u(d, dyunr, a, fy);
+  for (size_t q = 0; q < n2; ++q) {
+    fx[q] = (ce_back[q] + ce_visc[q]) * fx[q];
+    fy[q] = (cn_back[q] + cn_visc[q]) * fy[q];
+  }
+  op_bdx_eu(d, dyue, daur, fx, bx);
+  op_bdy_nu(d, dxun, daur, fy, by);
+  for (size_t q = 0; q < n2; ++q) out[q] = 0.0;
+  for (int j = 1; j <= d->nj; ++j)
+    for (int i = 1; i <= d->ni; ++i) {
+      size_t q = I2(d, i, j);
+      double tmp = bx[q] + by[q];
+      out[q] = (negate ? -tmp : tmp) * umask1[q];
+    }
+  orc_halo_update_2d(d, out, 3);
+  free(fx);
+  free(fy);
+  free(bx);
+  free(by);
+}
+
+/* The barotropic friction of one component a = udrho(:,:,n,tau) (ocean_barotropic.F90:
+ * 3105-3113): friction_lap = lap_friction_barotropic (ocean_lap_friction.F90:423-446)
+ * when lap, friction_bih = bih_friction_barotropic (ocean_bih_friction.F90:416-454:
+ * del2_vel, then the negated second iteration) when bih; 0.0 otherwise.
+ * m = {dyue, dxuer, dxun, dyunr, daur, umask1}; c = {lap_ceu_back, lap_cnu_back,
+ * lap_visc_ceu, lap_visc_cnu, bih_ceu_back, bih_cnu_back, bih_visc_ceu,
+ * bih_visc_cnu}; del2 receives del2_vel when bih. */
+void orc_bt_friction(const orc_dims* d, int lap, int bih, const double* const* m, const double* const* c,
+                     const double* a, double* friction_lap, double* friction_bih, double* del2) {
+  size_t n2 = (size_t)NXD(d) * NYD(d);
+  for (size_t q = 0; q < n2; ++q) friction_lap[q] = friction_bih[q] = 0.0;
+  if (lap) bt_friction_op(d, m, c[0], c[2], c[1], c[3], a, 0, friction_lap);
+  if (bih) {
+    bt_friction_op(d, m, c[4], c[6], c[5], c[7], a, 0, del2);
+    bt_friction_op(d, m, c[4], c[6], c[5], c[7], del2, 1, friction_bih);
+  }
 }
 
 /* total_tracer (ocean_tracer_diag.F90:2395-2412) with conversion = 1: the

@@ -283,12 +283,42 @@ def tracer_boundary_terms(d, g, kmt, pme, tpme, eta_smooth, pbot_smooth, th):
     return out
 
 
-def ocean_barotropic_forcing(d, tmasken, accel, smf, bmf, zero_nonlinear=False, zero_forcing=False):
+def ocean_barotropic_forcing(d, tmasken, accel, smf, bmf, zero_nonlinear=False, zero_forcing=False,
+                             friction_lap=None, friction_bih=None):
+    """One component of forcing_bt (ocean_barotropic.F90:3058-3141); friction_lap /
+    friction_bih: that component's barotropic frictions (None: 0.0)."""
     out = np.zeros((d.nj + 2, d.ni + 2))
     keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (tmasken, accel, smf, bmf)]
-    lib().orc_ocean_barotropic_forcing(C.byref(d), int(zero_nonlinear), int(zero_forcing), *[p(a) for a in keep],
-                                       p(out))
+    fr = [None if f is None else np.ascontiguousarray(f, dtype=np.float64) for f in (friction_lap, friction_bih)]
+    lib().orc_ocean_barotropic_forcing_friction(C.byref(d), int(zero_nonlinear), int(zero_forcing),
+                                                *[p(a) for a in keep], *[None if f is None else p(f) for f in fr],
+                                                p(out))
     return out
+
+
+def bt_friction_back(d, dxu, dyu, umask1, vel_lap=0.05, vel_bih=0.01):
+    """(lap_ceu_back, lap_cnu_back, bih_ceu_back, bih_cnu_back) as ocean_barotropic_init
+    forms them (ocean_barotropic.F90:1306-1341)."""
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (dxu, dyu, umask1)]
+    out = [np.zeros((d.nj + 2, d.ni + 2)) for _ in range(4)]
+    lib().orc_bt_friction_back(C.byref(d), *[p(a) for a in keep], C.c_double(vel_lap), C.c_double(vel_bih),
+                               *[p(o) for o in out])
+    return tuple(out)
+
+
+def bt_friction(d, lap, bih, metrics, coefs, a):
+    """(friction_lap, friction_bih, del2_vel) of one udrho component
+    (ocean_barotropic.F90:3105-3113).  metrics: dyue, dxuer, dxun, dyunr, daur, umask1;
+    coefs: lap_ceu_back, lap_cnu_back, lap_visc_ceu, lap_visc_cnu, bih_ceu_back,
+    bih_cnu_back, bih_visc_ceu, bih_visc_cnu."""
+    m = [np.ascontiguousarray(x, dtype=np.float64) for x in metrics]
+    c = [np.ascontiguousarray(x, dtype=np.float64) for x in coefs]
+    assert len(m) == 6 and len(c) == 8
+    mp, cp = (DP * 6)(*[p(x) for x in m]), (DP * 8)(*[p(x) for x in c])
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    out = [np.zeros((d.nj + 2, d.ni + 2)) for _ in range(3)]
+    lib().orc_bt_friction(C.byref(d), int(lap), int(bih), mp, cp, p(a), *[p(o) for o in out])
+    return tuple(out)
 
 
 def total_tracer(d, g, T):

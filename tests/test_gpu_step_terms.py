@@ -4,7 +4,8 @@ the C restatement, value for value:
   through mom5gpu_tracer_boundary_terms;
 - ocean_barotropic_forcing (ocean_barotropic.F90:3058-3141) through
   mom5gpu_ocean_barotropic_forcing, with its zero_nonlinear_forcing_bt and
-  zero_forcing_bt options, on cyclic and walled domains."""
+  zero_forcing_bt options, on cyclic and walled domains, and with the
+  barotropic friction on udrho(tau) through mom5gpu_ocean_barotropic_forcing_tau."""
 import numpy as np
 import pytest
 
@@ -83,6 +84,96 @@ def test_barotropic_forcing_matches(gpu_lib, oracle_lib, cyclic_x, opt):
     for fid, ref in ((F.FORCING_BT_U, ru), (F.FORCING_BT_V, rv)):
         got = d.get(fid)
         assert np.array_equal(got.view(np.uint64), ref.ravel().view(np.uint64)), f"{fid}: bits differ"
+    d.close()
+
+
+@pytest.mark.parametrize("which", ["lap", "bih", "both", "none", "both_zero_forcing"])
+@pytest.mark.parametrize("cyc", [(False, False), (True, False), (True, True)])
+def test_barotropic_friction_matches(gpu_lib, oracle_lib, which, cyc):
+    """The barotropic friction of ocean_barotropic_forcing (ocean_barotropic.F90:
+    3105-3120) through mom5gpu_ocean_barotropic_forcing_tau: the background
+    viscosities (:1306-1341), lap_friction_barotropic (ocean_lap_friction.F90:
+    423-446) and bih_friction_barotropic (ocean_bih_friction.F90:416-454) of
+    udrho(tau), and forcing_bt with the frictions added (also under
+    zero_forcing_bt), every field equal to the restatement bit for bit on the
+    data domain; walled, x-periodic and doubly periodic domains, the lateral
+    friction modules' viscosities random."""
+    capi, O = gpu_lib, oracle_lib
+    from mom5_gb300 import harness
+    F = capi.F
+    cx, cy = cyc
+    sp = grid.DomainSpec(ni=35, nj=27, nk=8, lon0=0.0, lon1=35.0, lat0=-30.0, lat1=30.0, cyclic_x=cx,
+                         cyclic_y=cy, continent=(9, 8, 6, 5), wavelength_cells=6.0, ntracers=1, seed=57)
+    dom = grid.make_domain(sp)
+    lap, bih = which.startswith(("lap", "both")), which.startswith(("bih", "both"))
+    zf = which.endswith("zero_forcing")
+    vl, vb = 0.07, 0.013
+    opts = capi.default_options(udrho_lap=int(lap), udrho_bih=int(bih), udrho_lap_vel_micom=vl,
+                                udrho_bih_vel_micom=vb, zero_forcing_bt=int(zf))
+    d = harness.load(dom, options=opts)
+    rng = np.random.default_rng(21)
+    tm = dom["tmask"].numpy()
+    shp3, shp2 = tm.shape, tm.shape[1:]
+    jit = lambda a: a * (1.0 + 0.01 * rng.standard_normal(shp2))
+    dxu, dyu, um = (dom[k].numpy().copy() for k in ("dxu", "dyu", "umask1"))
+    met = [jit(dyu), 1.0 / jit(dxu), jit(dxu), 1.0 / jit(dyu), dom["daur"].numpy().copy(), um]
+    for fid, a in zip((F.DYUE, F.DXUER, F.DXUN, F.DYUNR), met[:4]):
+        d.set(fid, a)
+    visc = [2e3 * rng.random(shp2) for _ in range(4)]
+    for fid, a in zip((F.LAP_VISC_CEU, F.LAP_VISC_CNU, F.BIH_VISC_CEU, F.BIH_VISC_CNU), visc):
+        d.set(fid, a)
+    tau = 2
+    ud = [1e3 * rng.standard_normal(shp2) for _ in range(2)]
+    d.set(F.UDRHO_U, ud[0], level=tau)
+    d.set(F.UDRHO_V, ud[1], level=tau)
+    ten, tnn = tm * (rng.random(shp3) > 0.1), tm * (rng.random(shp3) > 0.1)
+    d.set(F.TMASKEN_E, ten)
+    d.set(F.TMASKEN_N, tnn)
+    x = {k: rng.standard_normal(shp3) for k in ("au", "av")}
+    x.update({k: rng.standard_normal(shp2) * 0.1 for k in ("su", "sv", "bu", "bv")})
+    for fid, k in ((F.ACCEL_U, "au"), (F.ACCEL_V, "av"), (F.SMF_U, "su"), (F.SMF_V, "sv"), (F.BMF_U, "bu"),
+                   (F.BMF_V, "bv")):
+        d.set(fid, x[k])
+    d.ocean_barotropic_forcing(tau)
+
+    def same(fid, ref):
+        got = d.get(fid)
+        assert np.array_equal(got.view(np.uint64), np.ascontiguousarray(ref).ravel().view(np.uint64)), \
+            f"field {fid}: bits differ"
+
+    dims = O.dims(sp)
+    back = O.bt_friction_back(dims, dxu, dyu, um, vl, vb)
+    if lap or bih:
+        for fid, ref in zip((F.LAP_CEU_BACK, F.LAP_CNU_BACK, F.BIH_CEU_BACK, F.BIH_CNU_BACK), back):
+            same(fid, ref)
+    coefs = [back[0], back[1], visc[0], visc[1], back[2], back[3], visc[2], visc[3]]
+    for comp, (te, ak, sk, bk) in enumerate(((ten, "au", "su", "bu"), (tnn, "av", "sv", "bv"))):
+        fl, fb, del2 = O.bt_friction(dims, lap, bih, met, coefs, ud[comp])
+        same((F.LAP_FRICTION_BT_U, F.LAP_FRICTION_BT_V)[comp], fl)
+        same((F.BIH_FRICTION_BT_U, F.BIH_FRICTION_BT_V)[comp], fb)
+        if bih:
+            same((F.BIH_DEL2_VEL_U, F.BIH_DEL2_VEL_V)[comp], del2)
+            assert np.abs(fb).max() > 0
+        if lap:
+            assert np.abs(fl).max() > 0
+        ref = O.ocean_barotropic_forcing(dims, te, x[ak], x[sk], x[bk], zero_forcing=zf,
+                                         friction_lap=fl if (lap or bih) else None,
+                                         friction_bih=fb if (lap or bih) else None)
+        same((F.FORCING_BT_U, F.FORCING_BT_V)[comp], ref)
+    d.close()
+
+
+def test_barotropic_friction_needs_tau(gpu_lib):
+    """With udrho_lap set, the entry point without tau refuses (the friction acts
+    on udrho(tau)), and tau must be a time level."""
+    capi = gpu_lib
+    from mom5_gb300 import harness
+    dom = grid.make_domain(_spec(False, ntr=1))
+    d = harness.load(dom, options=capi.default_options(udrho_lap=1))
+    with pytest.raises(capi.Mom5GpuError):
+        d.ocean_barotropic_forcing()
+    with pytest.raises(capi.Mom5GpuError):
+        d.ocean_barotropic_forcing(4)
     d.close()
 
 

@@ -557,3 +557,57 @@ def test_ucell_thickness_rules(O, vcoord):
     assert np.array_equal(out["thicku"], want)
     assert np.allclose(out["mass_u"], (st["umask"] * out["rho_dzu"]).sum(0), rtol=1e-14, atol=0)
     assert np.allclose(out["thicken_n"], out["dzten_n"].sum(0), rtol=1e-14, atol=0)
+
+
+def _uniform_friction_metrics(ni, nj, dx, dy):
+    one = np.ones((nj + 2, ni + 2))
+    # dyue, dxuer, dxun, dyunr, daur, umask1 of a uniform B grid, every U cell wet
+    return [dy * one, one / dx, dx * one, one / dy, one / (dx * dy), one.copy()]
+
+
+@pytest.mark.parametrize("axis", ["x", "y"])
+def test_barotropic_friction_of_a_parabola(O, axis):
+    """Barotropic friction on a uniform grid (dx = 2, dy = 4) with constant
+    viscosities (back + visc = 0.75 east, 0.625 north; every value and operation
+    exact): the Laplacian (ocean_lap_friction.F90:423-446) of u = x^2 is 2*c_e at
+    every compute point and of u = y^2 is 2*c_n; the biharmonic
+    (ocean_bih_friction.F90:416-454) of the same u has del2_vel = 2*c and a second
+    iteration that vanishes where all the neighbours are compute points (walled
+    box: zero halo)."""
+    from oracle.oracle import Dims
+    ni, nj, dx, dy = 10, 8, 2.0, 4.0
+    d = Dims(ni, nj, 1, 0, 0)
+    m = _uniform_friction_metrics(ni, nj, dx, dy)
+    shp = (nj + 2, ni + 2)
+    ce, cn = 0.75, 0.625
+    coefs = [np.full(shp, 0.5), np.full(shp, 0.5), np.full(shp, ce - 0.5), np.full(shp, cn - 0.5),
+             np.full(shp, 0.25), np.full(shp, 0.125), np.full(shp, ce - 0.25), np.full(shp, cn - 0.125)]
+    j, i = np.meshgrid(np.arange(nj + 2), np.arange(ni + 2), indexing="ij")
+    u = (i * dx) ** 2 if axis == "x" else (j * dy) ** 2
+    c = ce if axis == "x" else cn
+    lap, bih, del2 = O.bt_friction(d, True, True, m, coefs, u.astype(float))
+    assert np.all(lap[1:-1, 1:-1] == 2 * c)
+    assert np.all(del2[1:-1, 1:-1] == 2 * c)
+    assert np.all(bih[2:-2, 2:-2] == 0.0)
+    assert np.all(lap[0, :] == 0) and np.all(bih[:, 0] == 0)  # walls: the halo stays 0.0
+    # a linear u: no Laplacian friction
+    lin = (3.0 * i * dx + 5.0 * j * dy).astype(float)
+    lap2, _, _ = O.bt_friction(d, True, False, m, coefs, lin)
+    assert np.all(lap2[1:-1, 1:-1] == 0.0)
+
+
+def test_barotropic_friction_background_viscosity(O):
+    """lap/bih_c*u_back of ocean_barotropic_init (ocean_barotropic.F90:1306-1341) on
+    square U cells of side 4: the MICOM viscosity vel*4 (Laplacian) and
+    sqrt(vel*4^3) (biharmonic) on the compute domain, zero in a walled halo, the
+    periodic copy in a cyclic one."""
+    from oracle.oracle import Dims
+    ni, nj = 6, 5
+    for cyclic in (0, 1):
+        d = Dims(ni, nj, 1, cyclic, 0)
+        one = np.ones((nj + 2, ni + 2))
+        le, ln, be, bn = O.bt_friction_back(d, 4.0 * one, 4.0 * one, one, 0.05, 0.01)
+        for a, want in ((le, 0.05 * 4.0), (ln, 0.05 * 4.0), (be, math.sqrt(0.01 * 64.0)), (bn, math.sqrt(0.01 * 64.0))):
+            assert np.allclose(a[1:-1, 1:-1], want, rtol=1e-15, atol=0)
+            assert np.all(a[0, :] == 0) and np.all(a[-1, :] == 0)
+            assert np.all(a[1:-1, 0] == (a[1:-1, ni] if cyclic else 0.0))
