@@ -112,9 +112,39 @@ DEVI double face_flux(double mf, double Rjm, double Rj, double Rjp, double Tp, d
 // tracer loops stay rolled (one copy of the loop body in the instruction cache).
 constexpr int kMdflThreads = 128;
 
-// z pass: one thread per column, march down k.
-template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith>
-DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
+// Face terms of the bottom face of level k of one column: w(k+1), the mass flux
+// and the limiter coefficients of the Courant number (ocean_tracer_advect.F90:
+// 3860-3866), evaluated the same way wherever a level's face is formed.
+struct ZFace {
+  double wk, massflux, d0, d1, c, rdz;
+};
+DEVI ZFace z_face(const MdflArgs& a, const Geo& g, int i, int j, int k, double dat) {
+  ZFace f;
+  f.wk = a.w[I3(g, i, j, k + 1)];
+  f.rdz = a.rdz[I3(g, i, j, k)];
+  f.massflux = dat * f.wk;
+  double cfl = fabs(div_seeded(f.wk * a.dtime, f.rdz));
+  f.d0 = (2.0 - cfl) * (1.0 - cfl) * kOneSixth;
+  f.d1 = (1.0 - cfl * cfl) * kOneSixth;
+  f.c = div_seeded(1.0 - cfl, add_1em30(cfl));
+  return f;
+}
+// R(m) = (m(m) && m(m1)) ? T(m) - T(m1) : 0 with m1 = min(m+1, nk-1): the masked
+// vertical difference that the column march forms once per level
+template <class Ar>
+DEVI double z_rdiff(const MdflArgs& a, const Geo& g, const double* T, int i, int j, int m) {
+  const int m1 = m + 1 < g.nk ? m + 1 : g.nk - 1;
+  return (a.mask2[IM(g, i, j, m)] && a.mask2[IM(g, i, j, m1)]) ? Ar::sub(T[I3(g, i, j, m)], T[I3(g, i, j, m1)])
+                                                                 : 0.0;
+}
+
+// z pass: one thread per column, march down levels k0..k1-1 (SEG; else the whole
+// column).  A segment that starts below the surface first forms what the march
+// from the surface would carry into level k0 -- the flux through its top face
+// (the bottom face of level k0-1) and R(k0-1), R(k0) -- with the same
+// operations, so every segment length gives the same bits.
+template <bool ALL, bool SWEBY, int MAXN, class Ar = MdflFaceArith, class Au = MdflUpdArith, bool SEG = false>
+DEVI void mdfl_z_body(MdflArgs a, int bx, int by, int k0 = 0, int k1 = -1) {
   // ftp: flux through the top face; Rp, Rc: the masked differences R(k-1), R(k),
   // R(k) = (m(k) && m(k1)) ? T(k) - T(k1) : 0 with k1 = min(k+1, nk-1).  The
   // reference's Rjp at level k is R(k-1) (+0 at k = 0) and its Rjm is R(k+1), so
@@ -125,25 +155,47 @@ DEVI void mdfl_z_body(MdflArgs a, int bx, int by) {
   int i = bx * blockDim.x + t + 1;
   int j = by + 1;
   if (i > g.ni) return;
-  {
-    const int k1 = g.nk > 1 ? 1 : 0;
-    const bool m0 = a.mask2[IM(g, i, j, 0)], m1 = a.mask2[IM(g, i, j, k1)];
+  if (!SEG) k0 = 0, k1 = g.nk;  // whole columns: the segment code is not compiled in
+  if (k1 < 0 || k1 > g.nk) k1 = g.nk;
+  double wk_top = 0.0;  // w at the top face of level k0 (0 at the surface)
+  if (!SEG || k0 == 0) {
+    const int k1s = g.nk > 1 ? 1 : 0;
+    const bool m0 = a.mask2[IM(g, i, j, 0)], m1 = a.mask2[IM(g, i, j, k1s)];
 #pragma unroll 1
     for (int n = 0; n < a.ntr; ++n) {
       const double* T = a.T + n * a.tstride;
       ftp[n][t] = 0.0;
       Rp[n][t] = 0.0;
-      Rc[n][t] = (m0 && m1) ? Ar::sub(T[I3(g, i, j, 0)], T[I3(g, i, j, k1)]) : 0.0;
+      Rc[n][t] = (m0 && m1) ? Ar::sub(T[I3(g, i, j, 0)], T[I3(g, i, j, k1s)]) : 0.0;
     }
+  } else {
+    // the bottom face of level kq = k0-1, as the march forms it there
+    const int kq = k0 - 1;
+    const ZFace f = z_face(a, g, i, j, kq, a.dat[I2(g, i, j)]);
+    const bool fm = a.mask2[IM(g, i, j, k0)] && a.mask2[IM(g, i, j, kq)];
+#pragma unroll 1
+    for (int n = 0; n < a.ntr; ++n) {
+      const double* T = a.T + n * a.tstride;
+      const double Rjp = kq > 0 ? z_rdiff<Ar>(a, g, T, i, j, kq - 1) : 0.0;
+      const double Rj = z_rdiff<Ar>(a, g, T, i, j, kq);
+      const double Rjm = z_rdiff<Ar>(a, g, T, i, j, k0);
+      ftp[n][t] = fm ? face_flux<SWEBY, Ar>(f.massflux, Rjm, Rj, Rjp, T[I3(g, i, j, k0)], T[I3(g, i, j, kq)], f.d0,
+                                             f.d1, f.c)
+                     : 0.0;
+      Rp[n][t] = Rj;
+      Rc[n][t] = Rjm;
+    }
+    wk_top = f.wk;
   }
-  double wkm1 = 0.0;
+  double wkm1 = wk_top;
   const double dat = a.dat[I2(g, i, j)];
   const double datr = a.datr[I2(g, i, j)];
-  for (int k = 0; k < g.nk; ++k) {
+  for (int k = k0; k < k1; ++k) {
     int kp1 = k + 1 < g.nk ? k + 1 : g.nk - 1;
     int kp2 = k + 2 < g.nk ? k + 2 : g.nk - 1;
     bool mk = a.mask2[IM(g, i, j, k)];
     bool mkp1 = a.mask2[IM(g, i, j, kp1)], mkp2 = a.mask2[IM(g, i, j, kp2)];
+    // the face terms as z_face forms them
     double wk = a.w[I3(g, i, j, k + 1)];
     double rdz = a.rdz[I3(g, i, j, k)];
     double massflux = dat * wk;

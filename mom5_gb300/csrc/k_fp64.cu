@@ -90,6 +90,37 @@ template <bool ALL, bool SWEBY, int MAXN>
 __global__ void __launch_bounds__(128) k_mdfl_z(MdflArgs a) {
   mdfl_z_body<ALL, SWEBY, MAXN>(a, blockIdx.x, blockIdx.y);
 }
+// blockIdx.z: the segment of L levels
+template <bool ALL, bool SWEBY, int MAXN>
+__global__ void __launch_bounds__(128) k_mdfl_z_seg(MdflArgs a, int L) {
+  const int k0 = blockIdx.z * L;
+  mdfl_z_body<ALL, SWEBY, MAXN, MdflFaceArith, MdflUpdArith, true>(a, blockIdx.x, blockIdx.y, k0, k0 + L);
+}
+
+// Levels per z-pass segment.  A domain with few columns gives the column march
+// few blocks (120 x 80 columns: 80 blocks on 152 SMs), each a long latency-bound
+// chain; cutting the columns into segments of L levels multiplies the blocks by
+// nk / L for one extra face per segment.  Aim at about four blocks per SM.
+static int z_segment_levels(const Geo& g) {
+  const long blocks = (long)((g.ni + 127) / 128) * g.nj;
+  const long want = 4L * 152;
+  if (blocks >= want || g.nk < 4) return g.nk;
+  int nseg = (int)((want + blocks - 1) / blocks);
+  if (nseg > g.nk / 2) nseg = g.nk / 2;  // segments of at least two levels
+  int L = (g.nk + nseg - 1) / nseg;
+  return L < 2 ? 2 : L;
+}
+template <bool ALL, bool SWEBY, int MAXN>
+static void launch_mdfl_z(const MdflArgs& a, cudaStream_t s) {
+  const Geo& g = a.g;
+  const int L = z_segment_levels(g);
+  if (L >= g.nk) {
+    k_mdfl_z<ALL, SWEBY, MAXN><<<dim3((g.ni + 127) / 128, g.nj), 128, 0, s>>>(a);
+  } else {
+    dim3 grid((g.ni + 127) / 128, g.nj, (g.nk + L - 1) / L);
+    k_mdfl_z_seg<ALL, SWEBY, MAXN><<<grid, 128, 0, s>>>(a, L);
+  }
+}
 
 template <bool ALL, bool SWEBY, int MAXN>
 __global__ void __launch_bounds__(kTX) k_mdfl_x(MdflArgs a) {
@@ -104,8 +135,7 @@ __global__ void __launch_bounds__(128, 6) k_mdfl_y(MdflArgs a, int TJ) {
 template <bool ALL, bool SWEBY, int MAXN>
 static void run_mdfl(const MdflArgs& a, cudaStream_t s) {
   const Geo& g = a.g;
-  dim3 bz((g.ni + 127) / 128, g.nj);
-  k_mdfl_z<ALL, SWEBY, MAXN><<<bz, 128, 0, s>>>(a);
+  launch_mdfl_z<ALL, SWEBY, MAXN>(a, s);
   dim3 bx((g.ni + kTX - 1) / kTX, g.nj, g.nk);
   k_mdfl_x<ALL, SWEBY, MAXN><<<bx, kTX, 0, s>>>(a);
   // rows per thread: keep >= ~8 warps per SM of work where the domain allows
@@ -130,8 +160,7 @@ template <bool ALL, bool SWEBY, int MAXN>
 static void run_mdfl_one(const MdflArgs& a, int pass, cudaStream_t s) {
   const Geo& g = a.g;
   if (pass == 1) {
-    dim3 bz((g.ni + 127) / 128, g.nj);
-    k_mdfl_z<ALL, SWEBY, MAXN><<<bz, 128, 0, s>>>(a);
+    launch_mdfl_z<ALL, SWEBY, MAXN>(a, s);
   } else if (pass == 2) {
     dim3 bx((g.ni + kTX - 1) / kTX, g.nj, g.nk);
     k_mdfl_x<ALL, SWEBY, MAXN><<<bx, kTX, 0, s>>>(a);
