@@ -21,7 +21,19 @@ def test_defaults_are_the_reference_namelist_defaults(cfgmod):
     assert (o.advect_sweby_all, o.limit_with_upwind, o.zero_tracer_advect_horz, o.zero_tracer_advect_vert) == (0, 0, 0, 0)
     assert o.pred_corr_gamma == 0.2 and o.rho0 == 1035.0 and o.grav == 9.8 and o.initsum_with_bar == 1
     assert o.psom_limit_prather == 0 and o.precision == capi.PRECISION_FP64
+    assert (o.udrho_lap, o.udrho_bih, o.udrho_lap_vel_micom, o.udrho_bih_vel_micom) == (0, 0, 0.05, 0.01)
     assert c.tracers == []
+
+
+def test_barotropic_friction_namelist(cfgmod):
+    """ocean_barotropic_nml udrho_lap / udrho_bih and their MICOM velocities
+    (ocean_barotropic.F90:599-604) reach mom5gpu_options."""
+    c = cfgmod.parse({"ocean_barotropic_nml": {"udrho_lap": True, "udrho_bih": False, "udrho_lap_vel_micom": 0.1,
+                                               "udrho_bih_vel_micom": 0.02}})
+    o = c.options
+    assert (o.udrho_lap, o.udrho_bih, o.udrho_lap_vel_micom, o.udrho_bih_vel_micom) == (1, 0, 0.1, 0.02)
+    with pytest.raises(ValueError):
+        cfgmod.parse({"ocean_barotropic_nml": {"udrho_lap_micom": 0.1}})
 
 
 def test_namelists_and_field_table(cfgmod, tmp_path):
